@@ -1,0 +1,366 @@
+"""Benchmark: FFA acceleration search, 2^23 samples, on one GB300 (or N replicas).
+
+Workload (one step): the full time-domain FFA search of one float32 series of
+2^23 samples at 64 us (noise N(0,1) plus a 5 ms pulsar with 20 m/s^2
+line-of-sight acceleration at S/N 15): frequency 50-500 Hz, acceleration
++-50 m/s^2, 64 bins, boxcar widths 1,2,4,8,16. Brute fold, 9 DP levels, the
+last two banded and fused with boxcar scoring; 193 x 7,730,942 final
+parameter sets = 1.49e9 period-trials, every one scored at every width.
+
+``value``   period-trials/s with the series already in HBM (CUDA events).
+``e2e``     the same through ``ffa_search`` from pinned host buffers: the H2D
+            copy of the series and the D2H read of the best candidate are
+            inside the timed region (wall clock, synchronised).
+``--impl reference`` times the CPU oracle (the C restatement of pyloki's numba
+loops, all host threads) on a bounded frequency band of the same search.
+
+Under torchrun every rank searches its own series (independent replicas,
+weak scaling); the step time is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "period-trials/s"
+WORKLOAD = "ffa_accel_search_2^23"
+
+
+def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0):
+    from pyloki_gb300 import ParamLimits, PulsarSearchConfig
+
+    return PulsarSearchConfig(
+        nsamps=2**23, tsamp=64e-6, nbins=64, eta=1.0,
+        param_limits=ParamLimits.from_taylor((freq_lo, freq_hi), accel=(-50.0, 50.0)).limits,
+        ducy_max=0.25, wtsp=2.0, use_fourier=False, bseg_brute=16384)
+
+
+def make_series(seed: int):
+    from pyloki_gb300.simulation import make_series as ms
+
+    return ms(2**23, 64e-6, freq=200.0, snr=15.0, ducy=0.05, accel=20.0, seed=seed)
+
+
+def cpu_band_cfg(band_hz: float):
+    """The same search restricted to [500 - band_hz, 500] Hz: identical bseg,
+    frequency step and acceleration grid (the grids depend on f_max only)."""
+    return make_cfg(500.0 - band_hz, 500.0)
+
+
+def final_trials(cfg) -> int:
+    return int(np.prod(cfg.get_param_grid_count(cfg.niters_ffa)))
+
+
+def run_cpu_oracle(cfg, ts, nthreads: int = 0) -> tuple[float, int]:
+    """One CPU search of the band sample with the oracle; returns (seconds, trials)."""
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    fold = O.ffa_execute(ts.ts_e, ts.ts_v, cfg, nthreads=nthreads)
+    snr = O.boxcar_snr(O.fold_norm(fold[0]), cfg.score_widths, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    assert snr.shape[-1] == len(cfg.score_widths)
+    return dt, final_trials(cfg)
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+
+        def reader():
+            for line in self.proc.stdout:
+                self.rows.append([c.strip() for c in line.split(",")])
+
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread is not None:
+                self.thread.join(timeout=5)
+
+    def summary(self) -> dict:
+        rows = [r for r in self.rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(cfg, phase: str) -> float:
+    """Algorithmic HBM bytes of one search phase (reads once + writes once)."""
+    prof = 2 * cfg.nbins * 4
+    n = cfg.niters_ffa
+
+    def lvl(level):
+        nseg = cfg.nsamps // (cfg.bseg_brute * 2**level)
+        return nseg * int(np.prod(cfg.get_param_grid_count(level))) * prof
+
+    if phase == "brutefold":
+        return 2 * 4 * cfg.nsamps + lvl(0)
+    if phase == "levels":  # levels 1..n-2 materialised (banded last two)
+        return float(sum(lvl(level) + lvl(level - 1) for level in range(1, n - 1)))
+    if phase == "final":  # read level n-2 once, write S/N of every final trial
+        return float(lvl(n - 2) + final_trials(cfg) * len(cfg.score_widths) * 4)
+    raise ValueError(phase)
+
+
+def bench_gpu(args) -> dict | None:
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.search import ffa_search
+    from pyloki_gb300.timeseries import TimeSeries
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = make_cfg()
+    ts_host = make_series(seed=1000 + rank)
+    ts_e_pin = torch.from_numpy(ts_host.ts_e).pin_memory()
+    ts_v_pin = torch.from_numpy(ts_host.ts_v).pin_memory()
+    ts_dev = TimeSeries(ts_e_pin.to(dev), ts_v_pin.to(dev), cfg.tsamp)
+    trials = final_trials(cfg)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist is not None:
+            dist.barrier()
+
+    def one_step(events=None):
+        dyp = DynamicProgramming(ts_dev, cfg, device=dev)
+        snr = dyp.search(band_bytes=args.band_bytes, phase_events=events)
+        return dyp, snr
+
+    for _ in range(args.warmup):
+        one_step()
+    barrier()
+    launches = 0
+    phases = {"brutefold": 0.0, "levels": 0.0, "final": 0.0}
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clocks:
+        start.record()
+        step_events = []
+        for _ in range(args.steps):
+            ev: list = []
+            dyp, snr = one_step(ev)
+            launches += dyp.launches
+            step_events.append(ev)
+            del snr
+        end.record()
+        barrier()
+    total_ms = start.elapsed_time(end)
+    for ev in step_events:
+        marks = dict(ev)
+        phases["brutefold"] += marks["start"].elapsed_time(marks["brutefold"])
+        phases["levels"] += marks["brutefold"].elapsed_time(marks["levels"])
+        phases["final"] += marks["levels"].elapsed_time(marks["final"])
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+
+    # ---- end to end through the public API, host buffers ------------------
+    ts_pinned = TimeSeries(ts_e_pin, ts_v_pin, cfg.tsamp)
+    for _ in range(max(1, args.warmup // 2)):
+        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
+        pg.find_best_params()
+    barrier()
+    t0 = time.perf_counter()
+    best = None
+    for _ in range(args.steps):
+        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
+        best = pg.find_best_params()
+        del pg
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return None
+
+    dom = max(phases, key=phases.get)
+    dom_ms = phases[dom] / args.steps
+    ab = algorithmic_bytes(cfg, dom)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = ab / (dom_ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC,
+        "value": world * trials / (ms_per_step * 1e-3),
+        "unit": "trials/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded N(0,1) noise + 5 ms pulsar, accel 20 m/s^2, S/N 15)",
+        "config": {"workload": WORKLOAD, "nsamps": cfg.nsamps, "tsamp": cfg.tsamp,
+                   "nbins": cfg.nbins, "freq_hz": [50.0, 500.0], "accel_ms2": [-50.0, 50.0],
+                   "widths": cfg.score_widths.tolist(), "levels": cfg.niters_ffa,
+                   "final_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
+                   "trials_per_step": trials, "band_bytes": args.band_bytes,
+                   "l2": "inputs larger than L2 (>51 GB read per step)",
+                   "parallelism": f"replicas x{world}"},
+        "phases_ms": {k: v / args.steps for k, v in phases.items()},
+        "roofline": {"kernel": {"brutefold": "brutefold_kernel (+phase_map)",
+                                "levels": "ffa_level_kernel (levels 1..7)",
+                                "final": "ffa_level_kernel bands + ffa_level_score_kernel"}[dom],
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": ab, "traffic": None},
+        "e2e": {"value": world * trials / (e2e_ms * 1e-3), "unit": "trials/s",
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 4 * cfg.nsamps,
+                "d2h_bytes_per_step": 8 + 4},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "best_candidate": {k: float(v) for k, v in best.items()},
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        cfg_b = cpu_band_cfg(args.cpu_band_hz)
+        from oracle import oracle as O
+
+        ts_b = make_series(seed=1000)
+        dt, nt = run_cpu_oracle(cfg_b, ts_b)
+        out["cpu_baseline"] = {"value": nt / dt, "unit": "trials/s",
+                               "cores": O.max_threads(), "kind": "port",
+                               "sample": f"same search restricted to "
+                                         f"{500 - args.cpu_band_hz:g}-500 Hz ({nt} trials, "
+                                         f"{dt:.1f} s)"}
+    if dist is not None:
+        dist.destroy_process_group()
+    return out
+
+
+def bench_reference(args) -> dict | None:
+    """CPU oracle (all host threads) on a bounded band of the same search."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return None
+    from oracle import oracle as O
+
+    cfg_b = cpu_band_cfg(args.cpu_band_hz)
+    ts_b = make_series(seed=1000)
+    for _ in range(args.warmup):
+        run_cpu_oracle(cfg_b, ts_b)
+    times = []
+    nt = final_trials(cfg_b)
+    for _ in range(args.steps):
+        dt, nt = run_cpu_oracle(cfg_b, ts_b)
+        times.append(dt)
+    value = nt / (sum(times) / len(times))
+    return {
+        "metric": METRIC, "value": value, "unit": "trials/s", "impl": "reference",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "sample_band_hz": [500 - args.cpu_band_hz, 500.0],
+                   "trials_per_step": nt},
+        "cpu_baseline": {"value": value, "unit": "trials/s", "cores": O.max_threads(),
+                         "kind": "port",
+                         "sample": f"{500 - args.cpu_band_hz:g}-500 Hz band of the search "
+                                   f"({nt} trials per step)"},
+        "e2e": {"value": value, "unit": "trials/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--band-bytes", type=int, default=96 << 20)
+    ap.add_argument("--cpu-band-hz", type=float, default=4.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    out = bench_reference(args) if args.impl == "reference" else bench_gpu(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

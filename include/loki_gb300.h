@@ -1,0 +1,168 @@
+/*
+ * loki_gb300 — C ABI of the GB300 (sm_103a) FFA / scoring / pruning kernels.
+ *
+ * Every entry point takes device pointers that the caller allocated, plain
+ * sizes, and a CUDA stream (as void*; NULL = legacy default stream). Nothing
+ * here allocates device memory. Calls are asynchronous on the given stream
+ * and return a status code (LOKI_OK or a negative LOKI_ERR_*); a readable
+ * message for the last failure on the calling thread is available from
+ * loki_last_error(). Kernels never trap: range violations found on the device
+ * are written to the caller's int32 error word (0 = no error), which the
+ * caller reads after synchronising.
+ *
+ * Array layouts follow pyloki exactly (C-contiguous):
+ *   fold     float32 (nsegments, *param_counts, 2, nbins)   [2 = (ts_e, ts_v) sums]
+ *   fold_c   complex64 (nsegments, *param_counts, 2, nbins/2+1) [Fourier domain]
+ *   snr      float32 (nprofiles, nwidths)
+ */
+#ifndef LOKI_GB300_H
+#define LOKI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LOKI_OK 0
+#define LOKI_ERR_INVALID -1     /* bad argument (size, null pointer, layout) */
+#define LOKI_ERR_CUDA -2        /* a CUDA launch or runtime call failed */
+#define LOKI_ERR_UNSUPPORTED -3 /* valid but not handled (e.g. nbins too large) */
+#define LOKI_ERR_CAPACITY -4    /* output capacity too small (e.g. branch_max) */
+
+/* Device-side error word values. */
+#define LOKI_DEVERR_NONE 0
+#define LOKI_DEVERR_WINDOW 1   /* resolved index outside the input window */
+#define LOKI_DEVERR_BRANCH 2   /* branch count above branch_max */
+
+#define LOKI_MAX_PARAMS 5
+#define LOKI_MAX_WIDTHS 64
+
+/* One FFA dynamic-programming level: the current grid (optionally a window of
+ * its last, frequency, dimension) resolved against the previous level's grid
+ * (optionally a window of its last dimension). */
+typedef struct {
+  int32_t nparams;          /* 1..5, order [..., jerk, accel, freq] */
+  int32_t nbins;            /* profile bins */
+  int32_t level;            /* current FFA level, >= 1 */
+  int32_t reserved;
+  double tseg_brute;        /* seconds, bseg_brute * tsamp */
+  int64_t counts_cur[LOKI_MAX_PARAMS];   /* full grid counts, current level */
+  int64_t counts_prev[LOKI_MAX_PARAMS];  /* full grid counts, previous level */
+  double limits[LOKI_MAX_PARAMS][2];     /* param_limits (min, max) */
+  const double* param_arr[LOKI_MAX_PARAMS]; /* device: current-level grid per dim */
+  int64_t out_start;        /* first current-level frequency index computed */
+  int64_t out_width;        /* number of current-level frequency indices */
+  int64_t in_start;         /* first previous-level frequency index held in fold_in */
+  int64_t in_width;         /* previous-level frequency indices held in fold_in */
+  int64_t nseg_in;          /* segments in fold_in; output has nseg_in / 2 */
+} LokiFFALevel;
+
+/* Packed plan entry, identical to pyloki's ffacoord_dtype (ffa.py:36-43). */
+typedef struct {
+  uint32_t i_tail;
+  float shift_tail;
+  uint32_t i_head;
+  float shift_head;
+} LokiFFACoord;
+
+/* Boxcar scoring constants. hb[w] = height + b and b[w] as float64, computed
+ * by the host with the reference's expressions (detection/scoring.py:99-140). */
+typedef struct {
+  int32_t nwidths;
+  int32_t wmax;             /* max(widths) */
+  int32_t mode;             /* 0: one S/N per width; 1: max over widths */
+  int32_t reserved;
+  double inv_stdnoise;
+  int32_t widths[LOKI_MAX_WIDTHS];
+  double hb[LOKI_MAX_WIDTHS];
+  double b[LOKI_MAX_WIDTHS];
+} LokiScoreSpec;
+
+/* ---- library ---------------------------------------------------------- */
+int loki_version(void);
+const char* loki_last_error(void);
+
+/* ---- FFA (time domain, float32) --------------------------------------- */
+
+/* Brute fold of a series into (nsegments, nfreqs, 2, nbins) at the start of
+ * the FFA. Replaces core/fold.py:108-171 brutefold_start (called through
+ * ffa_taylor_init, core/fold.py:527-569). Per (segment, freq, bin) the sum is
+ * taken in sample order, so the result is bit-identical to the reference.
+ * phase_scratch holds the (freq, sample) phase-bin map; it may be smaller
+ * than nfreqs * segment_len bytes (nbins <= 256) or 2x that (nbins > 256),
+ * in which case the frequencies are processed in chunks. */
+int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
+                   const double* freqs, int64_t nfreqs, int64_t segment_len,
+                   int32_t nbins, double tsamp, double t_ref,
+                   void* phase_scratch, int64_t scratch_bytes,
+                   float* fold_out, void* stream);
+
+/* Plan table of one FFA level (one entry per current-level parameter set in
+ * the output window). Replaces the per-parameter resolve inside unify_fold
+ * (dynamic/dyn_pffa.py:462-475 -> core/fold.py:617-671) and
+ * FFAPlan.resolve_coordinates[_freq] (ffa.py:105-193). */
+int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords, int32_t* dev_err,
+                  void* stream);
+
+/* One FFA DP level: fold_out[ipair, p] = roll(fold_in[2 ipair, tail(p)], s_t)
+ * + roll(fold_in[2 ipair + 1, head(p)], s_h). Replaces unify_fold
+ * (dynamic/dyn_pffa.py:435-489) with shift_add (core/common.py:304-324). */
+int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, float* fold_out,
+                   int32_t* dev_err, void* stream);
+
+/* Final FFA level fused with normalisation and boxcar scoring of segment 0:
+ * the unify_fold of the last level, get_fold_norm (ffa.py:382-411) and
+ * boxcar_snr_nd (detection/scoring.py:156-165) in one pass; the final fold is
+ * never written. snr is the full-grid array (P_full, nwidths), or (P_full,)
+ * in mode 1; a frequency window writes only its own rows. */
+int loki_ffa_level_score(const LokiFFALevel* lvl, const float* fold_in,
+                         const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
+                         void* stream);
+
+/* Band windows for the banded final levels: for bands of band_width
+ * current-level frequency indices, the [lo, hi] range of previous-level
+ * frequency indices that their tail and head resolve to (over every other
+ * parameter). win_lo / win_hi hold ceil(counts_cur[-1] / band_width) int64.
+ * Host-side planning helper with no reference counterpart; it lets the last
+ * two levels of a large FFA run in memory-bounded frequency bands. */
+int loki_ffa_band_windows(const LokiFFALevel* lvl, int64_t band_width,
+                          int64_t* win_lo, int64_t* win_hi, void* stream);
+
+/* Banded last two levels: for each band k of band_width final frequencies,
+ * compute the penultimate level restricted to the host window
+ * [win_lo[k], win_hi[k]] into scratch (loki_ffa_level), then the final level
+ * of the band fused with scoring (loki_ffa_level_score). pen / fin describe
+ * the full penultimate and final levels (their windows are overwritten per
+ * band); fold_pp is the materialised level before the penultimate. Together
+ * these replace the last two unify_fold calls (dynamic/dyn_pffa.py:435-489)
+ * plus get_fold_norm and boxcar_snr_nd without materialising either level.
+ * win_lo / win_hi are HOST arrays (from loki_ffa_band_windows). */
+int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
+                          int64_t band_width, const int64_t* win_lo, const int64_t* win_hi,
+                          const float* fold_pp, float* scratch, int64_t scratch_floats,
+                          const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
+                          void* stream);
+
+/* ---- scoring ---------------------------------------------------------- */
+
+/* Boxcar S/N of normalised profiles (nprof, nbins) -> (nprof, nwidths) or
+ * (nprof,) in mode 1. Replaces boxcar_snr_2d / boxcar_snr_1d
+ * (detection/scoring.py:99-153). */
+int loki_boxcar_snr(const float* profiles, int64_t nprof, int32_t nbins,
+                    const LokiScoreSpec* spec, float* snr, void* stream);
+
+/* Score of (n, 2, nbins) folds: boxcar S/N of e / sqrt(v), max over widths
+ * (detection/scoring.py:249-282 snr_score_batch_func). spec->mode is ignored. */
+int loki_snr_score_batch(const float* folds, int64_t n, int32_t nbins,
+                         const LokiScoreSpec* spec, float* scores, void* stream);
+
+/* Normalised profiles out[p, j] = folds[p, 0, j] / sqrt(folds[p, 1, j]) for
+ * (n, 2, nbins) folds. Replaces get_fold_norm (ffa.py:382-411, real case). */
+int loki_fold_norm(const float* folds, int64_t n, int32_t nbins, float* out,
+                   void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LOKI_GB300_H */

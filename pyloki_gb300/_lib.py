@@ -1,0 +1,182 @@
+"""ctypes binding of ``libloki_gb300.so`` (declared in ``include/loki_gb300.h``).
+
+The library is the product path: if it cannot be loaded the import of the
+GPU entry points fails with a RuntimeError; there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+import numpy as np
+
+LOKI_OK = 0
+LOKI_ERR_INVALID = -1
+LOKI_ERR_CUDA = -2
+LOKI_ERR_UNSUPPORTED = -3
+LOKI_ERR_CAPACITY = -4
+
+LOKI_DEVERR_WINDOW = 1
+LOKI_DEVERR_BRANCH = 2
+
+MAX_PARAMS = 5
+MAX_WIDTHS = 64
+
+_LIB_PATH = Path(__file__).resolve().parent / "libloki_gb300.so"
+
+
+class LokiFFALevel(C.Structure):
+    _fields_ = [
+        ("nparams", C.c_int32),
+        ("nbins", C.c_int32),
+        ("level", C.c_int32),
+        ("reserved", C.c_int32),
+        ("tseg_brute", C.c_double),
+        ("counts_cur", C.c_int64 * MAX_PARAMS),
+        ("counts_prev", C.c_int64 * MAX_PARAMS),
+        ("limits", (C.c_double * 2) * MAX_PARAMS),
+        ("param_arr", C.c_void_p * MAX_PARAMS),
+        ("out_start", C.c_int64),
+        ("out_width", C.c_int64),
+        ("in_start", C.c_int64),
+        ("in_width", C.c_int64),
+        ("nseg_in", C.c_int64),
+    ]
+
+
+class LokiFFACoord(C.Structure):
+    _fields_ = [
+        ("i_tail", C.c_uint32),
+        ("shift_tail", C.c_float),
+        ("i_head", C.c_uint32),
+        ("shift_head", C.c_float),
+    ]
+
+
+class LokiScoreSpec(C.Structure):
+    _fields_ = [
+        ("nwidths", C.c_int32),
+        ("wmax", C.c_int32),
+        ("mode", C.c_int32),
+        ("reserved", C.c_int32),
+        ("inv_stdnoise", C.c_double),
+        ("widths", C.c_int32 * MAX_WIDTHS),
+        ("hb", C.c_double * MAX_WIDTHS),
+        ("b", C.c_double * MAX_WIDTHS),
+    ]
+
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_I32 = C.c_int32
+_D = C.c_double
+
+#: name -> (restype, argtypes); the exported C ABI.
+SIGNATURES: dict[str, tuple] = {
+    "loki_version": (C.c_int, []),
+    "loki_last_error": (C.c_char_p, []),
+    "loki_brutefold": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _I64, _P, _P]),
+    "loki_ffa_plan": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P]),
+    "loki_ffa_level": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
+    "loki_ffa_level_score": (C.c_int, [C.POINTER(LokiFFALevel), _P, C.POINTER(LokiScoreSpec),
+                                       _P, _P, _P]),
+    "loki_ffa_band_windows": (C.c_int, [C.POINTER(LokiFFALevel), _I64, _P, _P, _P]),
+    "loki_ffa_final_banded": (C.c_int, [C.POINTER(LokiFFALevel), C.POINTER(LokiFFALevel), _I64,
+                                        _P, _P, _P, _P, _I64, C.POINTER(LokiScoreSpec), _P, _P,
+                                        _P]),
+    "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
+    "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
+    "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
+}
+
+_lock = threading.Lock()
+_lib: C.CDLL | None = None
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load(path: str | Path | None = None) -> C.CDLL:
+    """Load the library (once) and bind the C ABI prototypes."""
+    global _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = Path(path) if path is not None else _LIB_PATH
+        if not p.exists():
+            msg = (f"{p} is missing: build it with `python -m pyloki_gb300.build` "
+                   "(the GPU path has no CPU fallback)")
+            raise RuntimeError(msg)
+        lib = C.CDLL(str(p))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if path is None:
+            _lib = lib
+        return lib
+
+
+class LokiError(RuntimeError):
+    """A CUDA-side failure reported by libloki_gb300."""
+
+
+def check(rc: int) -> None:
+    """Map a status code to the reference's exception types."""
+    if rc == LOKI_OK:
+        return
+    msg = load().loki_last_error().decode(errors="replace")
+    if rc in (LOKI_ERR_INVALID, LOKI_ERR_CAPACITY):
+        raise ValueError(msg)
+    if rc == LOKI_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise LokiError(msg)
+
+
+def check_dev_err(err_word) -> None:
+    """Raise if a kernel reported a device-side range error (syncs the stream)."""
+    v = int(err_word.item())
+    if v & LOKI_DEVERR_WINDOW:
+        msg = "resolved grid index fell outside the input frequency window"
+        raise LokiError(msg)
+    if v & LOKI_DEVERR_BRANCH:
+        msg = "Invalid input: increase branch_max."
+        raise ValueError(msg)
+    if v:
+        msg = f"device error word {v}"
+        raise LokiError(msg)
+
+
+def ptr(t) -> int:
+    """Device pointer of a torch tensor (or 0 for None)."""
+    return 0 if t is None else int(t.data_ptr())
+
+
+def stream_ptr(stream) -> int:
+    return int(stream.cuda_stream) if stream is not None else 0
+
+
+def score_spec(widths, nbins: int, stdnoise: float = 1.0, mode: int = 0) -> LokiScoreSpec:
+    """Boxcar constants with the reference's float64 expressions
+    (``detection/scoring.py:127-138``): h = sqrt((n-w)/(n*w)), b = w*h/(n-w)."""
+    widths = np.asarray(widths, dtype=np.int64)
+    if widths.ndim != 1 or not 1 <= len(widths) <= MAX_WIDTHS:
+        msg = f"need 1..{MAX_WIDTHS} boxcar widths, got {widths.shape}"
+        raise ValueError(msg)
+    sp = LokiScoreSpec()
+    sp.nwidths = len(widths)
+    sp.wmax = int(widths.max())
+    sp.mode = mode
+    sp.inv_stdnoise = 1.0 / stdnoise
+    size = np.int64(nbins)
+    for i, width in enumerate(widths):
+        size_w = size - width
+        height = np.sqrt(size_w / (size * width))
+        b = width * height / size_w
+        sp.widths[i] = int(width)
+        sp.hb[i] = float(height + b)
+        sp.b[i] = float(b)
+    return sp

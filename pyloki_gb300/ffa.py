@@ -1,0 +1,473 @@
+"""FFA dynamic programming on the GPU (drop-in for pyloki's ``ffa.py``).
+
+``DynamicProgramming`` keeps the reference's interface (``ffa.py:196-435``):
+``initialize`` brute-folds the series (``loki_brutefold``), ``execute`` runs
+the DP levels (``loki_ffa_level``), and the grid properties are the
+reference's. Folds live in HBM as float32 torch tensors with pyloki's layout
+``(nsegments, *param_counts, 2, nbins)``.
+
+``search`` is the memory-bounded path used by ``ffa_search``: the last level
+is fused with normalisation and boxcar scoring (``loki_ffa_level_score``) and
+never written; when the penultimate level is large, the last two levels run
+in frequency bands whose penultimate fold fits in a small scratch buffer.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from pyloki_gb300 import _lib
+from pyloki_gb300.config import PulsarSearchConfig
+from pyloki_gb300.timeseries import TimeSeries
+
+ffacoord_dtype = np.dtype(
+    [("i_tail", np.uint32), ("shift_tail", np.float32),
+     ("i_head", np.uint32), ("shift_head", np.float32)],
+)
+ffacoordfreq_dtype = np.dtype([("idx", np.uint32), ("shift", np.float32)])
+
+_GIB = 1 << 30
+
+
+def _cart_len(counts) -> int:
+    return int(np.prod(np.asarray(counts, dtype=np.int64)))
+
+
+class _Grid:
+    """Per-level grid: counts and the parameter arrays, resident on the device."""
+
+    def __init__(self, cfg: PulsarSearchConfig, level: int, device) -> None:
+        self.level = level
+        self.dparams = cfg.get_dparams(level)
+        self.param_arr = cfg.get_param_arr(self.dparams)
+        self.counts = np.array([len(p) for p in self.param_arr], dtype=np.int64)
+        self.dev = [torch.from_numpy(np.ascontiguousarray(p, dtype=np.float64)).to(device)
+                    for p in self.param_arr]
+
+    @property
+    def size(self) -> int:
+        return _cart_len(self.counts)
+
+
+_GRID_CACHE: dict[tuple, _Grid] = {}
+
+
+def _cfg_key(cfg: PulsarSearchConfig) -> tuple:
+    return (cfg.nsamps, cfg.tsamp, cfg.nbins, cfg.eta, cfg.param_limits.tobytes(),
+            cfg.bseg_brute, cfg.bseg_ffa)
+
+
+def grid(cfg: PulsarSearchConfig, level: int, device) -> _Grid:
+    """Device grid of one level, shared by every search with the same grids."""
+    key = (_cfg_key(cfg), level, str(torch.device(device)))
+    g = _GRID_CACHE.get(key)
+    if g is None:
+        if len(_GRID_CACHE) > 64:
+            _GRID_CACHE.clear()
+        g = _GRID_CACHE[key] = _Grid(cfg, level, device)
+    return g
+
+
+def level_desc(cfg: PulsarSearchConfig, cur: _Grid, prev: _Grid, nseg_in: int,
+               out_win: tuple[int, int] | None = None,
+               in_win: tuple[int, int] | None = None) -> _lib.LokiFFALevel:
+    """Build the C descriptor of one DP level (optionally frequency-windowed)."""
+    n = cfg.nparams
+    d = _lib.LokiFFALevel()
+    d.nparams = n
+    d.nbins = cfg.nbins
+    d.level = cur.level
+    d.tseg_brute = cfg.tseg_brute
+    for i in range(n):
+        d.counts_cur[i] = int(cur.counts[i])
+        d.counts_prev[i] = int(prev.counts[i])
+        d.limits[i][0] = float(cfg.param_limits[i, 0])
+        d.limits[i][1] = float(cfg.param_limits[i, 1])
+        d.param_arr[i] = cur.dev[i].data_ptr()
+    o0, ow = out_win if out_win is not None else (0, int(cur.counts[-1]))
+    i0, iw = in_win if in_win is not None else (0, int(prev.counts[-1]))
+    d.out_start, d.out_width = o0, ow
+    d.in_start, d.in_width = i0, iw
+    d.nseg_in = nseg_in
+    return d
+
+
+class DynamicProgramming:
+    """FFA dynamic programming (``ffa.py:196-435``) on one GB300.
+
+    Parameters
+    ----------
+    ts_data : TimeSeries
+        Input series (``ts_e``, ``ts_v`` float32).
+    cfg : PulsarSearchConfig
+        Search configuration (``use_fourier=False``: time-domain folds).
+    device : torch.device or str, optional
+        CUDA device, default the current one.
+    """
+
+    def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None) -> None:
+        if cfg.use_fourier:
+            msg = ("the Fourier-domain FFA (use_fourier=True) is not built yet; "
+                   "use use_fourier=False")
+            raise NotImplementedError(msg)
+        self._ts_data = ts_data
+        self._cfg = cfg
+        self._device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        self._lib = _lib.load()
+        self._err = torch.zeros(1, dtype=torch.int32, device=self._device)
+        self._data_type = np.float32
+        self._fold: torch.Tensor | None = None
+        self._ffa_level = -1
+        self.phase_scratch_bytes = _GIB
+        #: kernels launched by this object (brute fold, levels, bands, scoring)
+        self.launches = 0
+
+    # ---- reference properties ------------------------------------------------
+    @property
+    def ts_data(self) -> TimeSeries:
+        return self._ts_data
+
+    @property
+    def cfg(self) -> PulsarSearchConfig:
+        return self._cfg
+
+    @property
+    def data_type(self):
+        return self._data_type
+
+    @property
+    def device(self) -> torch.device:
+        return self._device
+
+    @property
+    def fold(self) -> torch.Tensor:
+        """Fold of the current level on the device, ``(nseg, *counts, 2, nbins)``."""
+        if self._fold is None:
+            msg = ("the fold of this level is not materialised (search() fuses the "
+                   "last level with scoring); call execute() to materialise it")
+            raise RuntimeError(msg)
+        return self._fold
+
+    @property
+    def nsegments(self) -> int:
+        return self.cfg.nsamps // (self.cfg.bseg_brute * 2**self.ffa_level)
+
+    @property
+    def nbins(self) -> int:
+        return self.cfg.nbins
+
+    @property
+    def ffa_level(self) -> int:
+        return self._ffa_level
+
+    def _grid(self, level: int) -> _Grid:
+        return grid(self.cfg, level, self._device)
+
+    @property
+    def dparams(self) -> np.ndarray:
+        return self._grid(self.ffa_level).dparams
+
+    @property
+    def dparams_actual(self) -> np.ndarray:
+        return self.cfg.get_dparams_actual(self.ffa_level)
+
+    @property
+    def param_arr(self) -> list[np.ndarray]:
+        return self._grid(self.ffa_level).param_arr
+
+    @property
+    def param_grid_count(self) -> np.ndarray:
+        return self.cfg.get_param_grid_count(self.ffa_level)
+
+    @property
+    def param_arr_dict(self) -> dict[str, np.ndarray]:
+        names = self.cfg.param_names
+        return {f"{names[i]}": p for i, p in enumerate(self.param_arr)}
+
+    @property
+    def nparam_vol(self) -> int:
+        return int(np.prod([len(p) for p in self.param_arr])) if self.param_arr else 0
+
+    @property
+    def leaves_lb(self) -> float:
+        return np.round(np.log2(self.nparam_vol), 2)
+
+    @property
+    def tseg(self) -> float:
+        return self.cfg.tseg_brute * 2**self.ffa_level
+
+    def _stream(self) -> int:
+        return _lib.stream_ptr(torch.cuda.current_stream(self._device))
+
+    # ---- level 0: brute fold -------------------------------------------------
+    def initialize(self) -> None:
+        """Brute-fold the series at the level-0 grid (``ffa.py:305-329``)."""
+        cfg = self.cfg
+        g0 = self._grid(0)
+        if cfg.nparams > 1:
+            for ip in range(cfg.nparams - 1):
+                if len(g0.param_arr[ip]) > 1:
+                    msg = (f"param_arr has {len(g0.param_arr[ip])} values, "
+                           "should have only one")
+                    raise ValueError(msg)
+        dev = self._device
+        ts_e = torch.as_tensor(self.ts_data.ts_e).to(dev, non_blocking=True)
+        ts_v = torch.as_tensor(self.ts_data.ts_v).to(dev, non_blocking=True)
+        self._fold, nl = _brutefold(ts_e, ts_v, g0.dev[-1], cfg.bseg_brute, cfg.nbins,
+                                    cfg.tsamp, 0.0 if cfg.nparams == 1 else
+                                    cfg.bseg_brute * cfg.tsamp / 2,
+                                    scratch_bytes=self.phase_scratch_bytes)
+        self.launches += nl
+        nseg, nfreq = self._fold.shape[:2]
+        self._fold = self._fold.reshape(nseg, *([1] * (cfg.nparams - 1)), nfreq, 2,
+                                        cfg.nbins)
+        self._err.zero_()
+        self._ffa_level = 0
+
+    # ---- DP levels -----------------------------------------------------------
+    def execute(self, *, show_progress: bool = False) -> None:
+        """Run every DP level, materialising each fold (``ffa.py:331-347``)."""
+        for _ in range(self.cfg.niters_ffa - self.ffa_level):
+            self._execute_iter()
+        _lib.check_dev_err(self._err)
+
+    def _execute_iter(self) -> None:
+        cur = self._grid(self.ffa_level + 1)
+        prev = self._grid(self.ffa_level)
+        nseg_in = self.nsegments
+        fold_in = self.fold
+        out = torch.empty((nseg_in // 2, cur.size, 2, self.nbins), dtype=torch.float32,
+                          device=self._device)
+        desc = level_desc(self.cfg, cur, prev, nseg_in)
+        _lib.check(self._lib.loki_ffa_level(desc, _lib.ptr(fold_in), _lib.ptr(out),
+                                            _lib.ptr(self._err), self._stream()))
+        self.launches += 1
+        self._fold = out.reshape(nseg_in // 2, *cur.counts.tolist(), 2, self.nbins)
+        self._ffa_level += 1
+
+    def get_fold_norm(self, iseg: int = 0, param_idx: tuple | None = None) -> torch.Tensor:
+        """``fold[iseg][..., 0, :] / sqrt(fold[iseg][..., 1, :])`` (``ffa.py:382-411``)."""
+        fold = self.fold[iseg]
+        if param_idx is not None:
+            idx = tuple(int(i) for i in param_idx)[-(fold.ndim - 2):]
+            fold = fold[idx]
+        lead = fold.shape[:-2]
+        flat = fold.reshape(-1, 2, self.nbins).contiguous()
+        out = torch.empty((flat.shape[0], self.nbins), dtype=torch.float32,
+                          device=self._device)
+        _lib.check(self._lib.loki_fold_norm(_lib.ptr(flat), flat.shape[0], self.nbins,
+                                            _lib.ptr(out), self._stream()))
+        self.launches += 1
+        return out.reshape(*lead, self.nbins)
+
+    def get_complexity(self) -> list[int]:
+        return [_cart_len(self.cfg.get_param_grid_count(lvl))
+                for lvl in range(self.cfg.niters_ffa + 1)]
+
+    # ---- fused, memory-bounded search ---------------------------------------
+    def level_bytes(self, level: int) -> int:
+        nseg = self.cfg.nsamps // (self.cfg.bseg_brute * 2**level)
+        return nseg * _cart_len(self.cfg.get_param_grid_count(level)) * 2 * self.nbins * 4
+
+    def search(self, widths=None, stdnoise: float = 1.0, *, mode: int = 0,
+               banded: bool | None = None, band_bytes: int = 96 << 20,
+               phase_events: list | None = None) -> torch.Tensor:
+        """S/N of every final-level parameter set (segment 0), never writing the
+        final fold. Returns ``(*counts_final, nwidths)`` (or ``counts_final``
+        for ``mode=1``, the max over widths). ``phase_events``, if given,
+        receives ``(name, cuda.Event)`` marks recorded on the launch stream
+        after the brute fold, the materialised levels and the final levels."""
+        cfg = self.cfg
+        n = cfg.niters_ffa
+        widths = cfg.score_widths if widths is None else np.asarray(widths, np.int64)
+        spec = _lib.score_spec(widths, cfg.nbins, stdnoise, mode=mode)
+        nout = len(widths) if mode == 0 else 1
+
+        def mark(name: str) -> None:
+            if phase_events is not None:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(torch.cuda.current_stream(self._device))
+                phase_events.append((name, ev))
+
+        mark("start")
+        if self.ffa_level < 0:
+            self.initialize()
+        if self.ffa_level != 0:
+            msg = "search() starts from the level-0 fold; call initialize() first"
+            raise RuntimeError(msg)
+        mark("brutefold")
+        fin = self._grid(n)
+        snr = torch.empty((fin.size, nout), dtype=torch.float32, device=self._device)
+        if banded is None:
+            banded = n >= 2 and self.level_bytes(n - 1) > 8 * band_bytes
+        if banded and n < 2:
+            banded = False
+        last_mat = n - 2 if banded else n - 1
+        while self.ffa_level < last_mat:
+            self._execute_iter()
+        mark("levels")
+        if not banded:
+            prev = self._grid(n - 1)
+            desc = level_desc(cfg, fin, prev, self.nsegments)
+            _lib.check(self._lib.loki_ffa_level_score(
+                desc, _lib.ptr(self.fold), spec, _lib.ptr(snr), _lib.ptr(self._err),
+                self._stream()))
+            self.launches += 1
+        else:
+            self._search_banded(fin, spec, snr, band_bytes)
+        mark("final")
+        self._fold = None
+        self._ffa_level = n
+        _lib.check_dev_err(self._err)
+        shape = (*fin.counts.tolist(), nout) if mode == 0 else tuple(fin.counts.tolist())
+        return snr.reshape(shape)
+
+    def band_plan(self, band_bytes: int) -> tuple[int, np.ndarray, np.ndarray]:
+        """Frequency bands for the last two levels: (final band width, lo, hi)
+        where [lo[k], hi[k]] is the penultimate frequency window of band k."""
+        cfg = self.cfg
+        n = cfg.niters_ffa
+        fin, pen = self._grid(n), self._grid(n - 1)
+        nseg_pen = cfg.nsamps // (cfg.bseg_brute * 2 ** (n - 1))
+        other_pen = _cart_len(pen.counts[:-1])
+        row = nseg_pen * other_pen * 2 * cfg.nbins * 4
+        w_pen = max(64, band_bytes // row)
+        width = max(32, int(2 * w_pen * 0.75))
+        width = min(width, int(fin.counts[-1]))
+        desc = level_desc(cfg, fin, pen, nseg_pen)
+        key = (_cfg_key(cfg), band_bytes, str(self._device))
+        if key in _BAND_CACHE:
+            return _BAND_CACHE[key]
+        for _ in range(8):
+            nb = math.ceil(int(fin.counts[-1]) / width)
+            lo = torch.empty(nb, dtype=torch.int64, device=self._device)
+            hi = torch.empty(nb, dtype=torch.int64, device=self._device)
+            _lib.check(self._lib.loki_ffa_band_windows(desc, width, _lib.ptr(lo), _lib.ptr(hi),
+                                                       self._stream()))
+            self.launches += 1
+            lo_h, hi_h = lo.cpu().numpy(), hi.cpu().numpy()
+            _BAND_CACHE[key] = (width, lo_h, hi_h)
+            if (hi_h - lo_h + 1).max() <= 2 * w_pen or width <= 32:
+                return width, lo_h, hi_h
+            width = max(32, width // 2)
+        return width, lo_h, hi_h
+
+    def _search_banded(self, fin: _Grid, spec, snr: torch.Tensor, band_bytes: int) -> None:
+        cfg = self.cfg
+        n = cfg.niters_ffa
+        pen, pp = self._grid(n - 1), self._grid(n - 2)
+        nseg_pp = self.nsegments
+        nseg_pen = nseg_pp // 2
+        width, lo, hi = self.band_plan(band_bytes)
+        wmax = int((hi - lo + 1).max())
+        other_pen = _cart_len(pen.counts[:-1])
+        scratch = torch.empty(nseg_pen * other_pen * wmax * 2 * cfg.nbins,
+                              dtype=torch.float32, device=self._device)
+        d_pen = level_desc(cfg, pen, pp, nseg_pp)
+        d_fin = level_desc(cfg, fin, pen, nseg_pen)
+        lo = np.ascontiguousarray(lo, np.int64)
+        hi = np.ascontiguousarray(hi, np.int64)
+        _lib.check(self._lib.loki_ffa_final_banded(
+            d_pen, d_fin, width, lo.ctypes.data, hi.ctypes.data, _lib.ptr(self.fold),
+            _lib.ptr(scratch), scratch.numel(), spec, _lib.ptr(snr), _lib.ptr(self._err),
+            self._stream()))
+        self.launches += 2 * len(lo)
+
+
+_BAND_CACHE: dict[tuple, tuple] = {}
+
+
+def _brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref=0.0, *,
+               scratch_bytes=_GIB) -> tuple[torch.Tensor, int]:
+    """Brute fold plus the number of kernels it launched."""
+    elem = 1 if nbins <= 256 else 2
+    nfreq = freqs.numel()
+    need = nfreq * segment_len * elem
+    nbytes = min(need, max(scratch_bytes, segment_len * elem))
+    chunk = nbytes // (segment_len * elem)
+    return brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref,
+                     scratch_bytes=scratch_bytes), 2 * math.ceil(nfreq / chunk)
+
+
+def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segment_len: int,
+              nbins: int, tsamp: float, t_ref: float = 0.0, *,
+              scratch_bytes: int = _GIB) -> torch.Tensor:
+    """Fold ``(nsegments, nfreqs, 2, nbins)`` (``core/fold.py:108-171``)."""
+    lib = _lib.load()
+    nsamps = ts_e.numel()
+    nseg = math.ceil(nsamps / segment_len)
+    nfreq = freqs.numel()
+    elem = 1 if nbins <= 256 else 2
+    need = nfreq * segment_len * elem
+    scratch = torch.empty(min(need, max(scratch_bytes, segment_len * elem)),
+                          dtype=torch.uint8, device=ts_e.device)
+    fold = torch.empty((nseg, nfreq, 2, nbins), dtype=torch.float32, device=ts_e.device)
+    stream = _lib.stream_ptr(torch.cuda.current_stream(ts_e.device))
+    _lib.check(lib.loki_brutefold(_lib.ptr(ts_e), _lib.ptr(ts_v), nsamps, _lib.ptr(freqs),
+                                  nfreq, segment_len, nbins, tsamp, t_ref,
+                                  _lib.ptr(scratch), scratch.numel(), _lib.ptr(fold),
+                                  stream))
+    return fold
+
+
+class FFAPlan:
+    """Per-level coordinate plan (``ffa.py:53-193``), resolved on the GPU."""
+
+    def __init__(self, cfg: PulsarSearchConfig, *, device=None) -> None:
+        self._cfg = cfg
+        self._device = torch.device(device or "cuda")
+        self.n_params = cfg.nparams
+        self.n_levels = cfg.niters_ffa + 1
+        self.params = [cfg.get_param_arr(cfg.get_dparams(lvl)) for lvl in range(self.n_levels)]
+        self.param_counts = np.array(
+            [cfg.get_param_grid_count(lvl) for lvl in range(self.n_levels)], dtype=np.int32)
+        self.ncoords = np.array([_cart_len(c) for c in self.param_counts], dtype=np.int64)
+
+    @property
+    def cfg(self) -> PulsarSearchConfig:
+        return self._cfg
+
+    def resolve_level(self, level: int) -> np.ndarray:
+        """Plan of one level (>= 1) as an ``ffacoord_dtype`` array."""
+        lib = _lib.load()
+        cur = _Grid(self.cfg, level, self._device)
+        prev = _Grid(self.cfg, level - 1, self._device)
+        nseg_in = self.cfg.nsamps // (self.cfg.bseg_brute * 2 ** (level - 1))
+        desc = level_desc(self.cfg, cur, prev, nseg_in)
+        coords = torch.empty((cur.size, 4), dtype=torch.int32, device=self._device)
+        err = torch.zeros(1, dtype=torch.int32, device=self._device)
+        stream = _lib.stream_ptr(torch.cuda.current_stream(self._device))
+        _lib.check(lib.loki_ffa_plan(desc, _lib.ptr(coords), _lib.ptr(err), stream))
+        _lib.check_dev_err(err)
+        return coords.cpu().numpy().view(ffacoord_dtype).reshape(-1)
+
+    def resolve_coordinates(self) -> list[np.ndarray]:
+        """Plans of levels 1..n (level 0 is the brute fold and has no plan)."""
+        return [np.zeros(0, ffacoord_dtype)] + [
+            self.resolve_level(lvl) for lvl in range(1, self.n_levels)]
+
+    def resolve_coordinates_freq(self) -> list[np.ndarray]:
+        if self.n_params != 1:
+            msg = "resolve_coordinates_freq is only supported for single parameter"
+            raise ValueError(msg)
+        out = [np.zeros(0, ffacoordfreq_dtype)]
+        for lvl in range(1, self.n_levels):
+            c = self.resolve_level(lvl)
+            f = np.empty(len(c), ffacoordfreq_dtype)
+            f["idx"] = c["i_head"]
+            f["shift"] = c["shift_head"]
+            out.append(f)
+        return out
+
+
+def compute_ffa(tseries: TimeSeries, search_cfg: PulsarSearchConfig, *, quiet: bool = False,
+                show_progress: bool = False) -> torch.Tensor:
+    """Final FFA fold (``ffa.py:438-467``), materialised on the device."""
+    dyp = DynamicProgramming(tseries, search_cfg)
+    dyp.initialize()
+    dyp.execute(show_progress=show_progress)
+    return dyp.fold

@@ -1,0 +1,222 @@
+"""GPU FFA parity: the CUDA path against the reference fixtures and the oracle.
+
+Every comparison is bit-exact (assert_array_equal): the kernels reproduce the
+reference's float32/float64 operation order, so there is no tolerance.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import cfg_from_golden, load_golden
+
+pytestmark = pytest.mark.gpu
+FFA_CASES = ["ffa_freq", "ffa_accel", "ffa_jerk"]
+
+
+def _series(n, tsamp, freq, amp, seed, accel=0.0):
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) * tsamp
+    t_mid = t[n // 2]
+    phase = (t * freq + 0.5 * accel / 299792458.0 * freq * (t - t_mid) ** 2) % 1.0
+    pulse = np.exp(20.0 * (np.cos(2 * np.pi * (phase - 0.3)) - 1.0))
+    ts_e = (rng.standard_normal(n) + amp * pulse).astype(np.float32)
+    ts_v = np.ones(n, np.float32)
+    return ts_e, ts_v
+
+
+@pytest.mark.parametrize("name", FFA_CASES)
+def test_brutefold_and_levels_match_reference(cuda_device, name):
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden(name)
+    cfg = cfg_from_golden(d)
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    dyp.initialize()
+    np.testing.assert_array_equal(dyp.fold.cpu().numpy(), d["fold_0"])
+    for lvl in range(1, cfg.niters_ffa + 1):
+        dyp._execute_iter()
+        assert dyp.ffa_level == lvl
+        np.testing.assert_array_equal(dyp.fold.cpu().numpy(), d[f"fold_{lvl}"],
+                                      err_msg=f"level {lvl}")
+    np.testing.assert_array_equal(dyp.get_fold_norm().cpu().numpy(), d["fold_norm"])
+
+
+@pytest.mark.parametrize("name", FFA_CASES)
+def test_plan_matches_reference(cuda_device, name):
+    from pyloki_gb300.ffa import FFAPlan
+
+    d = load_golden(name)
+    cfg = cfg_from_golden(d)
+    plan = FFAPlan(cfg, device=cuda_device)
+    for lvl in range(1, cfg.niters_ffa + 1):
+        c = plan.resolve_level(lvl)
+        np.testing.assert_array_equal(c["i_tail"], d[f"plan_i_tail_{lvl}"])
+        np.testing.assert_array_equal(c["i_head"], d[f"plan_i_head_{lvl}"])
+        np.testing.assert_array_equal(c["shift_tail"],
+                                      d[f"plan_shift_tail_{lvl}"].astype(np.float32))
+        np.testing.assert_array_equal(c["shift_head"],
+                                      d[f"plan_shift_head_{lvl}"].astype(np.float32))
+    if cfg.nparams == 1:
+        for lvl, c in enumerate(plan.resolve_coordinates_freq()):
+            if lvl:
+                np.testing.assert_array_equal(c["idx"], d[f"plan_idx_{lvl}"])
+                np.testing.assert_array_equal(c["shift"], d[f"plan_shift_{lvl}"])
+
+
+@pytest.mark.parametrize("name", FFA_CASES)
+@pytest.mark.parametrize("path", ["materialize", "fused", "banded"])
+def test_ffa_search_snrs(cuda_device, name, path):
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.search import ffa_search
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden(name)
+    cfg = cfg_from_golden(d)
+    ts = TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp)
+    if path == "materialize":
+        _, pgram = ffa_search(ts, cfg, materialize=True, device=cuda_device)
+        snrs = pgram.snrs.cpu().numpy()
+    else:
+        dyp = DynamicProgramming(ts, cfg, device=cuda_device)
+        dyp.initialize()
+        # a tiny band budget forces many narrow bands with halos
+        snrs = dyp.search(banded=(path == "banded"), band_bytes=4096).cpu().numpy()
+    np.testing.assert_array_equal(snrs, d["snrs"])
+
+
+def test_search_max_mode(cuda_device):
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden("ffa_accel")
+    cfg = cfg_from_golden(d)
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    best = dyp.search(mode=1, banded=True, band_bytes=8192).cpu().numpy()
+    np.testing.assert_array_equal(best, d["snrs"].max(axis=-1))
+
+
+def test_periodogram_best(cuda_device):
+    from pyloki_gb300.search import ffa_search
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden("ffa_freq")
+    cfg = cfg_from_golden(d)
+    _, pgram = ffa_search(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    idx = pgram.find_best_indices()
+    assert idx == tuple(np.unravel_index(np.argmax(d["snrs"]), d["snrs"].shape))
+    best = pgram.find_best_params()
+    assert abs(best["freq"] - 12.3) < 0.05
+    assert "Best S/N" in pgram.get_summary()
+
+
+def test_freq_search_full_size_vs_oracle(cuda_device):
+    """2^20 samples, 1-10 Hz, 64 bins, widths 1..32: every level materialised
+    on both sides and compared bit for bit."""
+    from pyloki_gb300.config import PulsarSearchConfig
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    n = 2**20
+    cfg = PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0, param_limits=[(1.0, 10.0)],
+                             ducy_max=0.5, wtsp=2.0, use_fourier=False)
+    ts_e, ts_v = _series(n, cfg.tsamp, 2.0, 0.3, 5)
+    dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
+    dyp.initialize()
+    dyp.execute()
+    ref = O.ffa_execute(ts_e, ts_v, cfg)
+    np.testing.assert_array_equal(dyp.fold.cpu().numpy(), ref)
+    from pyloki_gb300.scoring import boxcar_snr_nd
+
+    snrs = boxcar_snr_nd(dyp.get_fold_norm(), cfg.score_widths).cpu().numpy()
+    np.testing.assert_array_equal(snrs, O.boxcar_snr(O.fold_norm(ref[0]), cfg.score_widths))
+
+
+def test_accel_search_spot_trials_vs_oracle(cuda_device):
+    """Banded fused accel search at 2^18 samples; random trials and the best
+    trial re-derived by the oracle's single-trial recursion."""
+    from pyloki_gb300.config import ParamLimits, PulsarSearchConfig
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    n = 2**18
+    cfg = PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
+                             param_limits=ParamLimits.from_taylor((100.0, 140.0),
+                                                                  accel=(-2000.0, 2000.0)).limits,
+                             ducy_max=0.25, wtsp=2.0, use_fourier=False)
+    ts_e, ts_v = _series(n, cfg.tsamp, 123.4, 0.4, 6, accel=700.0)
+    dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
+    snrs = dyp.search(banded=True, band_bytes=1 << 20).cpu().numpy()
+    flat = snrs.reshape(-1, snrs.shape[-1])
+    rng = np.random.default_rng(0)
+    pick = np.unique(np.concatenate([rng.integers(0, len(flat), 200),
+                                     [int(np.argmax(flat.max(axis=1)))]]))
+    prof = O.ffa_trials(ts_e, ts_v, cfg, pick)
+    ref = O.boxcar_snr(O.fold_norm(prof), cfg.score_widths)
+    np.testing.assert_array_equal(flat[pick], ref)
+    # unbanded fused path gives the same array
+    dyp2 = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
+    np.testing.assert_array_equal(dyp2.search(banded=False).cpu().numpy(), snrs)
+
+
+def test_brutefold_chunked_scratch_and_wide_bins(cuda_device):
+    """Phase scratch smaller than the map (frequency chunks) and nbins > 256
+    (16-bit phase map) against the oracle."""
+    import torch
+
+    from pyloki_gb300.ffa import brutefold
+
+    rng = np.random.default_rng(3)
+    n, seg = 3 * 4096 + 1000, 4096  # ragged last segment
+    ts_e = rng.standard_normal(n).astype(np.float32)
+    ts_v = (1 + rng.random(n)).astype(np.float32)
+    for nbins, freqs in [(64, np.linspace(5.0, 9.0, 37)), (300, np.linspace(2.0, 3.0, 11))]:
+        ref = O.brutefold(ts_e, ts_v, freqs, seg, nbins, 64e-6, 0.01)
+        te = torch.from_numpy(ts_e).to(cuda_device)
+        tv = torch.from_numpy(ts_v).to(cuda_device)
+        tf = torch.from_numpy(freqs).to(cuda_device)
+        out = brutefold(te, tv, tf, seg, nbins, 64e-6, 0.01, scratch_bytes=3 * seg * 2)
+        np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_window_violation_is_reported_not_faulted(cuda_device):
+    """A level whose input window misses the resolved indices sets the device
+    error word (the access is skipped) and the host raises."""
+    import torch
+
+    from pyloki_gb300 import _lib
+    from pyloki_gb300.ffa import DynamicProgramming, _Grid, level_desc
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden("ffa_accel")
+    cfg = cfg_from_golden(d)
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    dyp.initialize()
+    cur, prev = _Grid(cfg, 1, cuda_device), _Grid(cfg, 0, cuda_device)
+    w = 3
+    desc = level_desc(cfg, cur, prev, dyp.nsegments, in_win=(0, w))
+    fold_in = dyp.fold.reshape(dyp.nsegments, -1, 2, cfg.nbins)[:, :w].contiguous()
+    out = torch.zeros((dyp.nsegments // 2, cur.size, 2, cfg.nbins), device=cuda_device)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda_device)
+    lib = _lib.load()
+    _lib.check(lib.loki_ffa_level(desc, _lib.ptr(fold_in), _lib.ptr(out), _lib.ptr(err),
+                                  _lib.stream_ptr(torch.cuda.current_stream())))
+    with pytest.raises(_lib.LokiError):
+        _lib.check_dev_err(err)
+
+
+def test_scaling_linearity_property(cuda_device):
+    """Size-independent property: scaling ts_e by 2 and ts_v by 4 scales every
+    fold exactly and leaves every S/N bit-identical."""
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden("ffa_jerk")
+    cfg = cfg_from_golden(d)
+    a = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    b = DynamicProgramming(TimeSeries(2 * d["ts_e"], 4 * d["ts_v"], cfg.tsamp), cfg,
+                           device=cuda_device)
+    np.testing.assert_array_equal(a.search().cpu().numpy(), b.search().cpu().numpy())
