@@ -237,13 +237,13 @@ def bench_gpu(args) -> dict | None:
     ts_pinned = TimeSeries(ts_e_pin, ts_v_pin, cfg.tsamp)
     for _ in range(max(1, args.warmup // 2)):
         _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
-        pg.find_best_params()
+        pg.find_best_params(ignore_nan=True)
     barrier()
     t0 = time.perf_counter()
     best = None
     for _ in range(args.steps):
         _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
-        best = pg.find_best_params()
+        best = pg.find_best_params(ignore_nan=True)
         del pg
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -345,6 +345,30 @@ def bench_reference(args) -> dict | None:
     }
 
 
+def profile_once(args) -> None:
+    """One search of the benchmark workload (optionally on a shorter series)
+    with no timing; the command that the ncu summaries are captured from."""
+    import torch
+
+    from pyloki_gb300 import ParamLimits, PulsarSearchConfig
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.simulation import make_series as ms
+
+    n = 2**args.nsamps_log2
+    cfg = PulsarSearchConfig(
+        nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
+        param_limits=ParamLimits.from_taylor((50.0, 500.0), accel=(-50.0, 50.0)).limits,
+        ducy_max=0.25, wtsp=2.0, use_fourier=False,
+        bseg_brute=16384 if n == 2**23 else 0)
+    ts = ms(n, 64e-6, freq=200.0, snr=15.0, ducy=0.05, accel=20.0, seed=1000)
+    dyp = DynamicProgramming(ts, cfg, device=torch.device("cuda", 0))
+    snr = dyp.search(band_bytes=args.band_bytes)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_once": True, "nsamps": n, "levels": cfg.niters_ffa,
+                      "final_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
+                      "launches": dyp.launches, "snr_shape": list(snr.shape)}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -354,7 +378,14 @@ def main() -> None:
     ap.add_argument("--band-bytes", type=int, default=96 << 20)
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="run exactly one search (for ncu captures) and exit")
+    ap.add_argument("--nsamps-log2", type=int, default=23,
+                    help="series length for --profile-once (smaller ncu cases)")
     args = ap.parse_args()
+    if args.profile_once:
+        profile_once(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     out = bench_reference(args) if args.impl == "reference" else bench_gpu(args)

@@ -56,6 +56,10 @@ typedef struct {
   int64_t in_start;         /* first previous-level frequency index held in fold_in */
   int64_t in_width;         /* previous-level frequency indices held in fold_in */
   int64_t nseg_in;          /* segments in fold_in; output has nseg_in / 2 */
+  /* Optional (may be NULL): device float2 array, counts_cur[nparams-1]
+   * entries, of the last-dimension grid split as (float(f), float(f - float(f))).
+   * Lets the kernels skip one FP64 operation per parameter set. */
+  const float* last_split;
 } LokiFFALevel;
 
 /* Packed plan entry, identical to pyloki's ffacoord_dtype (ffa.py:36-43). */
@@ -143,6 +147,12 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
                           const float* fold_pp, float* scratch, int64_t scratch_floats,
                           const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
                           void* stream);
+
+/* Floats of scratch loki_ffa_final_banded needs for penultimate windows of at
+ * most max_window frequencies: the band fold plus two small per-level resolve
+ * tables. Returns -1 for invalid descriptors. */
+int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
+                                      int64_t max_window);
 
 /* ---- scoring ---------------------------------------------------------- */
 

@@ -43,6 +43,7 @@ class LokiFFALevel(C.Structure):
         ("in_start", C.c_int64),
         ("in_width", C.c_int64),
         ("nseg_in", C.c_int64),
+        ("last_split", C.c_void_p),
     ]
 
 
@@ -86,6 +87,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_ffa_final_banded": (C.c_int, [C.POINTER(LokiFFALevel), C.POINTER(LokiFFALevel), _I64,
                                         _P, _P, _P, _P, _I64, C.POINTER(LokiScoreSpec), _P, _P,
                                         _P]),
+    "loki_ffa_final_banded_scratch": (C.c_int64, [C.POINTER(LokiFFALevel),
+                                                  C.POINTER(LokiFFALevel), _I64]),
     "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),

@@ -2,8 +2,8 @@
 
 ``python -m pyloki_gb300.build`` compiles every ``csrc/*.cu`` translation unit
 in parallel with nvcc (one ``-gencode`` for sm_103a) and links the shared
-library next to this file. ``--fmad=false`` keeps numpy's rounding (no
-contracted multiply-adds), which the bit-exact kernels rely on.
+library next to this file. ``--fmad=false`` (device) and ``-ffp-contract=off`` (host) keep numpy's
+rounding (no contracted multiply-adds), which the bit-exact kernels rely on.
 """
 
 from __future__ import annotations
@@ -24,6 +24,7 @@ NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "--fmad=false", "--expt-relaxed-constexpr",
     "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+    "-Xcompiler", "-ffp-contract=off",
 ]
 
 

@@ -1,0 +1,197 @@
+// Brute fold at the start of the FFA (core/fold.py:108-171 brutefold_start).
+//
+// The reference computes a phase-bin map per (frequency, sample in segment)
+// and then, per segment and frequency, adds every sample into its bin in time
+// order. Here the map is built once per frequency chunk (phase_map_kernel, FP64
+// with the reference's rounding) and shared by all segments; the fold kernel
+// gives each thread one (segment, frequency) and walks the samples in time
+// order exactly like the reference loop, so every bin sum is bit-identical.
+//
+// Per thread the running sums of the current bin stay in registers; all 2 x
+// nbins sums live in shared memory laid out [bin][thread] (conflict-free).
+// The map row is read 16 bytes at a time and the series 4 samples at a time
+// (the 8 threads' series loads of one block are broadcasts of the same
+// addresses). Blocks are ordered segment-fastest so that the map rows of the
+// frequencies in flight stay in L2 while every segment consumes them.
+#include <algorithm>
+
+#include "loki_common.cuh"
+
+namespace loki {
+
+template <typename T>
+__global__ void phase_map_kernel(const double* __restrict__ freqs, int64_t nfreq,
+                                 int64_t seg_len, int nbins, double tsamp, double t_ref,
+                                 T* __restrict__ map) {
+  const int64_t total = nfreq * seg_len;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = k / seg_len;
+    const int64_t i = k - f * seg_len;
+    const double pt = __dsub_rn(__dmul_rn((double)i, tsamp), t_ref);
+    int b = round_shift(phase_idx(pt, freqs[f], nbins, 0.0), nbins);
+    // Only a non-finite frequency can leave [0, nbins); keep every
+    // accumulator index in bounds (the host rejects such grids up front).
+    if (b < 0 || b >= nbins) b = 0;
+    map[k] = (T)b;
+  }
+}
+
+template <typename T>
+struct MapVec;
+template <>
+struct MapVec<uint8_t> {
+  static constexpr int N = 16;
+  __device__ static int get(const uint4& v, int k) {
+    const unsigned w = k < 4 ? v.x : k < 8 ? v.y : k < 12 ? v.z : v.w;
+    return (w >> (8 * (k & 3))) & 0xFF;
+  }
+};
+template <>
+struct MapVec<uint16_t> {
+  static constexpr int N = 8;
+  __device__ static int get(const uint4& v, int k) {
+    const unsigned w = k < 2 ? v.x : k < 4 ? v.y : k < 6 ? v.z : v.w;
+    return (w >> (16 * (k & 1))) & 0xFFFF;
+  }
+};
+
+__device__ __forceinline__ float f4get(const float4& v, int k) {
+  return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+brutefold_seq_kernel(const float* __restrict__ ts_e, const float* __restrict__ ts_v,
+                     int64_t nsamps, const T* __restrict__ map, int64_t nfreq_chunk,
+                     int64_t f_offset, int64_t nfreq_total, int64_t seg_len, int64_t nseg,
+                     int nbins, float* __restrict__ fold) {
+  extern __shared__ float acc[];  // [2 * nbins][blockDim.x]
+  const int BS = blockDim.x;
+  const int t = threadIdx.x;
+  const int64_t seg = blockIdx.x % nseg;
+  const int64_t fi = (blockIdx.x / nseg) * BS + t;
+  if (fi >= nfreq_chunk) return;  // no block-level synchronisation follows
+  for (int b = 0; b < 2 * nbins; ++b) acc[b * BS + t] = 0.0f;
+  const int64_t start = seg * seg_len;
+  const int64_t len = std::min<int64_t>(seg_len, nsamps - start);
+  const T* m = map + fi * seg_len;
+  const float* e = ts_e + start;
+  const float* v = ts_v + start;
+  int cur = 0;
+  float ae = 0.0f, av = 0.0f;
+  constexpr int VN = MapVec<T>::N;
+  int64_t i = 0;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(m) | reinterpret_cast<uintptr_t>(e) |
+                         reinterpret_cast<uintptr_t>(v)) & 15) == 0;
+  if (aligned) {
+    for (; i + VN <= len; i += VN) {
+      const uint4 mv = *reinterpret_cast<const uint4*>(m + i);
+      float4 ev[VN / 4], vv[VN / 4];
+#pragma unroll
+      for (int q = 0; q < VN / 4; ++q) {
+        ev[q] = __ldg(reinterpret_cast<const float4*>(e + i) + q);
+        vv[q] = __ldg(reinterpret_cast<const float4*>(v + i) + q);
+      }
+#pragma unroll
+      for (int k = 0; k < VN; ++k) {
+        const int b = MapVec<T>::get(mv, k);
+        if (b != cur) {
+          acc[cur * BS + t] = ae;
+          acc[(nbins + cur) * BS + t] = av;
+          ae = acc[b * BS + t];
+          av = acc[(nbins + b) * BS + t];
+          cur = b;
+        }
+        ae = __fadd_rn(ae, f4get(ev[k >> 2], k & 3));
+        av = __fadd_rn(av, f4get(vv[k >> 2], k & 3));
+      }
+    }
+  }
+  for (; i < len; ++i) {
+    const int b = (int)m[i];
+    if (b != cur) {
+      acc[cur * BS + t] = ae;
+      acc[(nbins + cur) * BS + t] = av;
+      ae = acc[b * BS + t];
+      av = acc[(nbins + b) * BS + t];
+      cur = b;
+    }
+    ae = __fadd_rn(ae, e[i]);
+    av = __fadd_rn(av, v[i]);
+  }
+  acc[cur * BS + t] = ae;
+  acc[(nbins + cur) * BS + t] = av;
+  float* out = fold + ((size_t)seg * nfreq_total + f_offset + fi) * 2 * nbins;
+  if ((nbins & 1) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0 && (nbins % 2) == 0 &&
+      ((2 * nbins) & 3) == 0) {
+    for (int b = 0; b < 2 * nbins; b += 4)
+      *reinterpret_cast<float4*>(out + b) =
+          make_float4(acc[b * BS + t], acc[(b + 1) * BS + t], acc[(b + 2) * BS + t],
+                      acc[(b + 3) * BS + t]);
+  } else {
+    for (int b = 0; b < 2 * nbins; ++b) out[b] = acc[b * BS + t];
+  }
+}
+
+static int brutefold_block(int nbins) {
+  // 2 * nbins floats of shared memory per thread; keep <= 200 KB per block.
+  int bs = 128;
+  while (bs > 32 && (size_t)bs * 2 * nbins * sizeof(float) > 200 * 1024) bs >>= 1;
+  return bs;
+}
+
+}  // namespace loki
+
+using namespace loki;
+
+extern "C" int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
+                              const double* freqs, int64_t nfreqs, int64_t segment_len,
+                              int32_t nbins, double tsamp, double t_ref, void* phase_scratch,
+                              int64_t scratch_bytes, float* fold_out, void* stream) {
+  if (!ts_e || !ts_v || !freqs || !phase_scratch || !fold_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if (nsamps <= 0 || nfreqs <= 0 || segment_len <= 0)
+    return set_error(LOKI_ERR_INVALID, "nsamps, nfreqs and segment_len must be > 0");
+  if (nbins < 1 || nbins > 768)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins %d outside [1, 768]", nbins);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nseg = (nsamps + segment_len - 1) / segment_len;
+  const int elem = nbins <= 256 ? 1 : 2;
+  int64_t chunk = scratch_bytes / (segment_len * elem);
+  if (chunk < 1)
+    return set_error(LOKI_ERR_CAPACITY, "phase scratch of %lld bytes holds no frequency",
+                     (long long)scratch_bytes);
+  chunk = std::min(chunk, nfreqs);
+  const int bs = brutefold_block(nbins);
+  const size_t smem = (size_t)bs * 2 * nbins * sizeof(float);
+  if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large");
+  if (cudaFuncSetAttribute(brutefold_seq_kernel<uint8_t>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(brutefold_seq_kernel<uint16_t>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  for (int64_t f0 = 0; f0 < nfreqs; f0 += chunk) {
+    const int64_t nf = std::min(chunk, nfreqs - f0);
+    const int64_t total = nf * segment_len;
+    const int mblocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 64);
+    const int64_t blocks = nseg * ((nf + bs - 1) / bs);
+    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    if (elem == 1) {
+      uint8_t* map = (uint8_t*)phase_scratch;
+      phase_map_kernel<uint8_t><<<mblocks, 256, 0, s>>>(freqs + f0, nf, segment_len, nbins,
+                                                       tsamp, t_ref, map);
+      brutefold_seq_kernel<uint8_t><<<(unsigned)blocks, bs, smem, s>>>(
+          ts_e, ts_v, nsamps, map, nf, f0, nfreqs, segment_len, nseg, nbins, fold_out);
+    } else {
+      uint16_t* map = (uint16_t*)phase_scratch;
+      phase_map_kernel<uint16_t><<<mblocks, 256, 0, s>>>(freqs + f0, nf, segment_len, nbins,
+                                                        tsamp, t_ref, map);
+      brutefold_seq_kernel<uint16_t><<<(unsigned)blocks, bs, smem, s>>>(
+          ts_e, ts_v, nsamps, map, nf, f0, nfreqs, segment_len, nseg, nbins, fold_out);
+    }
+    int rc = check_launch("brutefold");
+    if (rc) return rc;
+  }
+  return LOKI_OK;
+}

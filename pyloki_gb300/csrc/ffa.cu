@@ -1,99 +1,23 @@
-// FFA kernels: brute fold, per-level plan, DP level, fused final level+score.
+// FFA dynamic-programming kernels: per-level plan, DP level, the final level
+// fused with normalisation and boxcar scoring, and the banded driver.
 //
 // Data layout in HBM (identical to pyloki): fold (nseg, P, 2, nbins) float32,
 // C-contiguous, P = flattened parameter grid with the frequency axis fastest.
 #include <algorithm>
 
 #include "loki_common.cuh"
+#include "resolve.cuh"
 #include "score.cuh"
 
 namespace loki {
 
 // ---------------------------------------------------------------------------
-// Brute fold (core/fold.py:108-171 brutefold_start)
+// Plan table (exact FP64 path; the f32 shift is part of the output)
 // ---------------------------------------------------------------------------
 
-// Phase-bin map of one segment: map[f][i] = get_phase_idx_int(i*tsamp - t_ref,
-// freq[f], nbins, 0). Depends only on (freq, sample-in-segment), so one map
-// serves every segment (and every series with the same grid).
-template <typename T>
-__global__ void phase_map_kernel(const double* __restrict__ freqs, int64_t nfreq,
-                                 int64_t seg_len, int nbins, double tsamp,
-                                 double t_ref, T* __restrict__ map) {
-  const int64_t total = nfreq * seg_len;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = k / seg_len;
-    const int64_t i = k - f * seg_len;
-    const double pt = __dsub_rn(__dmul_rn((double)i, tsamp), t_ref);
-    map[k] = (T)round_shift(phase_idx(pt, freqs[f], nbins, 0.0), nbins);
-  }
-}
-
-// One warp per (segment, frequency). Samples are consumed in chunks of 32 in
-// time order; inside a chunk the lanes that hit the same bin are ranked by
-// lane index (match_any + popc) and added rank by rank, so every bin receives
-// its samples in exactly the sequential order of the reference loop.
-// Accumulators live in shared memory (2 * nbins floats per warp).
-template <typename T, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32)
-brutefold_kernel(const float* __restrict__ ts_e, const float* __restrict__ ts_v,
-                 int64_t nsamps, const T* __restrict__ map, int64_t nfreq_chunk,
-                 int64_t f_offset, int64_t nfreq_total, int64_t seg_len,
-                 int64_t nseg, int nbins, float* __restrict__ fold) {
-  extern __shared__ float acc_all[];
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const int64_t seg = blockIdx.x % nseg;
-  const int64_t fi = (blockIdx.x / nseg) * WARPS + warp;
-  float* acc_e = acc_all + (size_t)warp * 2 * nbins;
-  float* acc_v = acc_e + nbins;
-  for (int j = lane; j < 2 * nbins; j += 32) acc_e[j] = 0.0f;
-  __syncwarp();
-  if (fi >= nfreq_chunk) return;
-  const int64_t start = seg * seg_len;
-  const int64_t len = std::min<int64_t>(seg_len, nsamps - start);
-  const T* mrow = map + fi * seg_len;
-  const float* se = ts_e + start;
-  const float* sv = ts_v + start;
-  const unsigned lt = lanemask_lt();
-  for (int64_t base = 0; base < len; base += 32) {
-    const int64_t i = base + lane;
-    const bool valid = i < len;
-    const unsigned bin = valid ? (unsigned)mrow[i] : 0xFFFFFFFFu;
-    const float e = valid ? se[i] : 0.0f;
-    const float v = valid ? sv[i] : 0.0f;
-    const unsigned peers = __match_any_sync(0xFFFFFFFFu, bin);
-    const int rank = __popc(peers & lt);
-    const int maxrank = (int)__reduce_max_sync(0xFFFFFFFFu, valid ? (unsigned)rank : 0u);
-    for (int r = 0; r <= maxrank; ++r) {
-      if (valid && rank == r) {
-        acc_e[bin] = __fadd_rn(acc_e[bin], e);
-        acc_v[bin] = __fadd_rn(acc_v[bin], v);
-      }
-      __syncwarp();
-    }
-  }
-  float* out = fold + ((size_t)seg * nfreq_total + f_offset + fi) * 2 * nbins;
-  for (int j = lane; j < 2 * nbins; j += 32) out[j] = acc_e[j];
-}
-
-// ---------------------------------------------------------------------------
-// Plan / level helpers
-// ---------------------------------------------------------------------------
-
-struct Resolved {
-  int64_t in_tail;  // flattened index into fold_in's parameter axis (window applied)
-  int64_t in_head;
-  double ph_tail;
-  double ph_head;
-  bool ok;
-};
-
-// Decompose output parameter q of the (windowed) current grid into values.
 __device__ __forceinline__ void out_param(const LokiFFALevel& L, int64_t q, double* pset) {
   const int n = L.nparams;
-  int64_t last = L.out_start + q % L.out_width;
+  const int64_t last = L.out_start + q % L.out_width;
   int64_t rest = q / L.out_width;
   pset[n - 1] = L.param_arr[n - 1][last];
   for (int d = n - 2; d >= 0; --d) {
@@ -103,29 +27,13 @@ __device__ __forceinline__ void out_param(const LokiFFALevel& L, int64_t q, doub
   }
 }
 
-__device__ __forceinline__ int64_t flat_in(const LokiFFALevel& L, const int64_t* idx,
-                                           bool* ok) {
+__device__ __forceinline__ int64_t flat_in(const LokiFFALevel& L, const int64_t* idx, bool* ok) {
   const int n = L.nparams;
   int64_t flat = 0;
   for (int d = 0; d < n - 1; ++d) flat = flat * L.counts_prev[d] + idx[d];
   const int64_t il = idx[n - 1] - L.in_start;
   if (il < 0 || il >= L.in_width) *ok = false;
   return flat * L.in_width + il;
-}
-
-__device__ __forceinline__ Resolved resolve_q(const LokiFFALevel& L, int64_t q) {
-  double pset[LOKI_MAX_PARAMS];
-  int64_t idx[LOKI_MAX_PARAMS];
-  out_param(L, q, pset);
-  Resolved r;
-  r.ok = true;
-  r.ph_tail = ffa_resolve(pset, L.nparams, L.level, 0, L.tseg_brute, L.nbins,
-                          L.counts_prev, L.limits, idx);
-  r.in_tail = flat_in(L, idx, &r.ok);
-  r.ph_head = ffa_resolve(pset, L.nparams, L.level, 1, L.tseg_brute, L.nbins,
-                          L.counts_prev, L.limits, idx);
-  r.in_head = flat_in(L, idx, &r.ok);
-  return r;
 }
 
 __host__ __device__ __forceinline__ int64_t n_out_params(const LokiFFALevel& L) {
@@ -145,43 +53,174 @@ __global__ void ffa_plan_kernel(LokiFFALevel L, LokiFFACoord* __restrict__ coord
   const int64_t Q = n_out_params(L);
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < Q;
        q += (int64_t)gridDim.x * blockDim.x) {
-    Resolved r = resolve_q(L, q);
-    if (!r.ok) atomicOr(err, LOKI_DEVERR_WINDOW);
+    double pset[LOKI_MAX_PARAMS];
+    int64_t idx[LOKI_MAX_PARAMS];
+    out_param(L, q, pset);
+    bool ok = true;
+    const double pt = ffa_resolve(pset, L.nparams, L.level, 0, L.tseg_brute, L.nbins,
+                                  L.counts_prev, L.limits, idx);
+    const int64_t it = flat_in(L, idx, &ok);
+    const double ph = ffa_resolve(pset, L.nparams, L.level, 1, L.tseg_brute, L.nbins,
+                                  L.counts_prev, L.limits, idx);
+    const int64_t ih = flat_in(L, idx, &ok);
+    if (!ok) atomicOr(err, LOKI_DEVERR_WINDOW);
     LokiFFACoord c;
-    c.i_tail = (uint32_t)r.in_tail;
-    c.shift_tail = __double2float_rn(r.ph_tail);
-    c.i_head = (uint32_t)r.in_head;
-    c.shift_head = __double2float_rn(r.ph_head);
+    c.i_tail = (uint32_t)it;
+    c.shift_tail = __double2float_rn(pt);
+    c.i_head = (uint32_t)ih;
+    c.shift_head = __double2float_rn(ph);
     coords[q] = c;
   }
 }
 
-// Each warp owns 32 consecutive output parameters: lane k resolves parameter
-// k (FP64, once per level), then the warp streams the roll-add of every
-// segment pair for the 32 parameters, pair-major so that neighbouring
-// parameters (neighbouring frequencies) are read and written together.
-__global__ void __launch_bounds__(256)
-ffa_level_kernel(LokiFFALevel L, const float* __restrict__ in, float* __restrict__ out,
-                 int32_t* __restrict__ err) {
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t Q = n_out_params(L);
-  const int64_t P_in = n_in_params(L);
-  const int64_t q0 = gw * 32;
-  if (q0 >= Q) return;
-  const int nb = L.nbins;
-  int64_t my_t = 0, my_h = 0;
-  int my_st = 0, my_sh = 0;
-  bool my_ok = false;
-  if (q0 + lane < Q) {
-    Resolved r = resolve_q(L, q0 + lane);
-    my_ok = r.ok;
-    my_t = r.in_tail;
-    my_h = r.in_head;
-    my_st = round_shift(r.ph_tail, nb);
-    my_sh = round_shift(r.ph_head, nb);
-    if (!r.ok) atomicOr(err, LOKI_DEVERR_WINDOW);
+// ---------------------------------------------------------------------------
+// Trial resolution shared by the level kernels
+// ---------------------------------------------------------------------------
+
+// Each lane resolves one output parameter (q0 + lane) using the block's
+// table of per-other quantities (or computes them itself when the block
+// spans too many others).
+struct LaneTrial {
+  int64_t t, h;
+  int st, sh;
+  bool ok;
+};
+
+__device__ __forceinline__ LaneTrial lane_trial(const LokiFFALevel& L, const LevelK& K,
+                                                const OtherTable& T, bool tab,
+                                                const OtherRes* __restrict__ gtab,
+                                                int64_t n_other, int64_t q, int64_t Q,
+                                                int32_t* err) {
+  LaneTrial r{0, 0, 0, 0, false};
+  if (q >= Q) return r;
+  const int64_t other = q / L.out_width;
+  TrialRes tr;
+  if (gtab) {
+    tr = resolve_trial(L, K, gtab[other], gtab[n_other + other], q);
+  } else if (tab) {
+    const int oi = (int)(other - T.first);
+    tr = resolve_trial(L, K, T.e[0][oi], T.e[1][oi], q);
+  } else {
+    const OtherRes ot = make_other(L, K, other, 0);
+    const OtherRes oh = make_other(L, K, other, 1);
+    tr = resolve_trial(L, K, ot, oh, q);
   }
+  r.t = tr.in_tail;
+  r.h = tr.in_head;
+  r.st = tr.s_tail;
+  r.sh = tr.s_head;
+  r.ok = tr.ok;
+  if (!tr.ok) atomicOr(err, LOKI_DEVERR_WINDOW);
+  return r;
+}
+
+// Roll of one (2, 64) profile row held as one float4 per lane (lane l holds
+// component l >> 4, bins 4 (l & 15) .. + 3): out[j] = in[(j - s) mod 64] per
+// component, assembled from two neighbouring lanes by shuffles.
+__device__ __forceinline__ float4 roll64(const float4 x, int s, int lane) {
+  const int q = s >> 2, r = s & 3;
+  const int base = lane & 16, l16 = lane & 15;
+  const int srcA = base | ((l16 - q) & 15);
+  const float a0 = __shfl_sync(0xFFFFFFFFu, x.x, srcA);
+  const float a1 = __shfl_sync(0xFFFFFFFFu, x.y, srcA);
+  const float a2 = __shfl_sync(0xFFFFFFFFu, x.z, srcA);
+  const float a3 = __shfl_sync(0xFFFFFFFFu, x.w, srcA);
+  if (r == 0) return make_float4(a0, a1, a2, a3);
+  const int srcB = base | ((l16 - q - 1) & 15);
+  const float b1 = __shfl_sync(0xFFFFFFFFu, x.y, srcB);
+  const float b2 = __shfl_sync(0xFFFFFFFFu, x.z, srcB);
+  const float b3 = __shfl_sync(0xFFFFFFFFu, x.w, srcB);
+  if (r == 1) return make_float4(b3, a0, a1, a2);
+  if (r == 2) return make_float4(b2, b3, a0, a1);
+  return make_float4(b1, b2, b3, a0);
+}
+
+__device__ __forceinline__ float4 add4(const float4 a, const float4 b) {
+  return make_float4(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z),
+                     __fadd_rn(a.w, b.w));
+}
+
+// ---------------------------------------------------------------------------
+// DP level (unify_fold, dynamic/dyn_pffa.py:435-489 + shift_add
+// core/common.py:304-324). Each warp owns 32 consecutive output parameters;
+// lane k resolves parameter k once, then the warp streams the roll-add of
+// every segment pair, pair-major, so neighbouring parameters (neighbouring
+// frequencies) are read and written together.
+// ---------------------------------------------------------------------------
+
+constexpr int kLevelWarps = 8;
+constexpr int kBatch = 4;
+
+// nbins == 64: one float4 per lane per row, four rows in flight per lane.
+__global__ void __launch_bounds__(kLevelWarps * 32, 4)
+ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                   float* __restrict__ out, int32_t* __restrict__ err,
+                   const OtherRes* __restrict__ gtab, int64_t n_other) {
+  __shared__ OtherTable T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t Q = n_out_params(L), P_in = n_in_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * kLevelWarps * 32;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + kLevelWarps * 32, Q) - 1);
+    __syncthreads();
+  }
+  const int64_t q0 = qb + warp * 32;
+  if (q0 >= Q) return;
+  const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
+  const int kmax = (int)std::min<int64_t>(32, Q - q0);
+  const int64_t nseg_out = L.nseg_in / 2;
+  for (int64_t ip = 0; ip < nseg_out; ++ip) {
+    const float4* in_t = reinterpret_cast<const float4*>(in) + (size_t)(2 * ip) * P_in * 32;
+    const float4* in_h = reinterpret_cast<const float4*>(in) + (size_t)(2 * ip + 1) * P_in * 32;
+    float4* o = reinterpret_cast<float4*>(out) + ((size_t)ip * Q + q0) * 32;
+    for (int k0 = 0; k0 < kmax; k0 += kBatch) {
+      float4 tv[kBatch], hv[kBatch];
+      int st[kBatch], sh[kBatch];
+      bool ok[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int k = k0 + u;
+        const int src = k < kmax ? k : 0;
+        const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, src);
+        const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, src);
+        st[u] = __shfl_sync(0xFFFFFFFFu, me.st, src);
+        sh[u] = __shfl_sync(0xFFFFFFFFu, me.sh, src);
+        ok[u] = __shfl_sync(0xFFFFFFFFu, me.ok, src) && k < kmax;
+        if (ok[u]) {
+          tv[u] = __ldg(in_t + (size_t)it * 32 + lane);
+          hv[u] = __ldg(in_h + (size_t)ih * 32 + lane);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        if (!ok[u]) continue;  // uniform across the warp
+        const float4 a = roll64(tv[u], st[u], lane);
+        const float4 b = roll64(hv[u], sh[u], lane);
+        o[(size_t)(k0 + u) * 32 + lane] = add4(a, b);
+      }
+    }
+  }
+}
+
+// Any nbins: scalar, lane j handles bins j, j + 32, ...
+__global__ void __launch_bounds__(kLevelWarps * 32, 4)
+ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                 float* __restrict__ out, int32_t* __restrict__ err,
+                 const OtherRes* __restrict__ gtab, int64_t n_other) {
+  __shared__ OtherTable T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t Q = n_out_params(L), P_in = n_in_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * kLevelWarps * 32;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + kLevelWarps * 32, Q) - 1);
+    __syncthreads();
+  }
+  const int64_t q0 = qb + warp * 32;
+  if (q0 >= Q) return;
+  const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
+  const int nb = L.nbins;
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
   const int64_t nseg_out = L.nseg_in / 2;
   const size_t row = (size_t)2 * nb;
@@ -190,11 +229,11 @@ ffa_level_kernel(LokiFFALevel L, const float* __restrict__ in, float* __restrict
     const float* in_h = in + (size_t)(2 * ip + 1) * P_in * row;
     float* o_base = out + ((size_t)ip * Q + q0) * row;
     for (int k = 0; k < kmax; ++k) {
-      const int64_t it = __shfl_sync(0xFFFFFFFFu, my_t, k);
-      const int64_t ih = __shfl_sync(0xFFFFFFFFu, my_h, k);
-      const int st = __shfl_sync(0xFFFFFFFFu, my_st, k);
-      const int sh = __shfl_sync(0xFFFFFFFFu, my_sh, k);
-      const bool ok = __shfl_sync(0xFFFFFFFFu, my_ok, k);
+      const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, k);
+      const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, k);
+      const int st = __shfl_sync(0xFFFFFFFFu, me.st, k);
+      const int sh = __shfl_sync(0xFFFFFFFFu, me.sh, k);
+      const bool ok = __shfl_sync(0xFFFFFFFFu, me.ok, k);
       if (!ok) continue;
       const float* t = in_t + (size_t)it * row;
       const float* h = in_h + (size_t)ih * row;
@@ -211,45 +250,133 @@ ffa_level_kernel(LokiFFALevel L, const float* __restrict__ in, float* __restrict
   }
 }
 
-// Final level fused with get_fold_norm and boxcar scoring, segment 0 only.
-// Lane k resolves parameter k; the warp builds the 32 normalised profiles in
-// its shared tile, then lane k scores row k.
-__global__ void __launch_bounds__(128)
-ffa_level_score_kernel(LokiFFALevel L, const float* __restrict__ in, LokiScoreSpec sp,
-                       float* __restrict__ snr, int32_t* __restrict__ err) {
+// ---------------------------------------------------------------------------
+// Final level fused with get_fold_norm (ffa.py:382-411) and boxcar scoring
+// (detection/scoring.py:99-165), segment 0 only: the warp builds 32
+// normalised profiles in its shared tile, then lane k scores row k.
+// ---------------------------------------------------------------------------
+
+constexpr int kScoreWarps = 4;
+
+__device__ __forceinline__ void score_out(const LokiFFALevel& L, const LokiScoreSpec& sp,
+                                          const ScoreK& SK, float* tile, int stride, int lane,
+                                          int64_t q0, int kmax, float* snr) {
+  __syncwarp();
+  if (lane < kmax) {
+    const int64_t q = q0 + lane;
+    const int64_t full = (q / L.out_width) * L.counts_cur[L.nparams - 1] + L.out_start +
+                         q % L.out_width;
+    const int nout = sp.mode == 0 ? sp.nwidths : 1;
+    float* row = tile + lane * stride;
+    if (SK.pow2_64) score_row64_pow2(row, sp, SK, snr + (size_t)full * nout);
+    else score_row(row, L.nbins, sp, snr + (size_t)full * nout);
+  }
+}
+
+__global__ void __launch_bounds__(kScoreWarps * 32)
+ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                         LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
+                         int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
+                         int64_t n_other) {
+  __shared__ OtherTable T;
   extern __shared__ float tiles[];
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int stride = score_stride(64, sp.wmax);
+  float* tile = tiles + (size_t)warp * 32 * stride;
+  const int64_t Q = n_out_params(L), P_in = n_in_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
+    __syncthreads();
+  }
+  const int64_t q0 = qb + warp * 32;
+  if (q0 >= Q) return;
+  const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
+  const int kmax = (int)std::min<int64_t>(32, Q - q0);
+  const float* in_t = in;                     // segment 0 of fold_in
+  const float* in_h = in + (size_t)P_in * 128;  // segment 1 of fold_in
+  // Lane j gathers bins j and j + 32 of both components at the rolled
+  // positions, so it owns e and v of its two output bins.
+  for (int k0 = 0; k0 < kmax; k0 += kBatch) {
+    float te[kBatch][2], tv[kBatch][2], he[kBatch][2], hv[kBatch][2];
+    bool ok[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int k = k0 + u;
+      const int src = k < kmax ? k : 0;
+      const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, src);
+      const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, src);
+      const int st = __shfl_sync(0xFFFFFFFFu, me.st, src);
+      const int sh = __shfl_sync(0xFFFFFFFFu, me.sh, src);
+      ok[u] = __shfl_sync(0xFFFFFFFFu, me.ok, src) && k < kmax;
+      if (ok[u]) {
+        const float* t = in_t + (size_t)it * 128;
+        const float* h = in_h + (size_t)ih * 128;
+        const int jt0 = (lane - st) & 63, jt1 = (lane + 32 - st) & 63;
+        const int jh0 = (lane - sh) & 63, jh1 = (lane + 32 - sh) & 63;
+        te[u][0] = __ldg(t + jt0);
+        te[u][1] = __ldg(t + jt1);
+        tv[u][0] = __ldg(t + 64 + jt0);
+        tv[u][1] = __ldg(t + 64 + jt1);
+        he[u][0] = __ldg(h + jh0);
+        he[u][1] = __ldg(h + jh1);
+        hv[u][0] = __ldg(h + 64 + jh0);
+        hv[u][1] = __ldg(h + 64 + jh1);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int k = k0 + u;
+      if (k >= kmax) break;
+      float* trow = tile + k * stride;
+      if (!ok[u]) {
+        trow[lane] = 0.0f;
+        trow[lane + 32] = 0.0f;
+        continue;
+      }
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float e = __fadd_rn(te[u][c], he[u][c]);
+        const float v = __fadd_rn(tv[u][c], hv[u][c]);
+        trow[lane + 32 * c] = __fdiv_rn(e, __fsqrt_rn(v));
+      }
+    }
+  }
+  score_out(L, sp, SK, tile, stride, lane, q0, kmax, snr);
+}
+
+__global__ void __launch_bounds__(kScoreWarps * 32)
+ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                       LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
+                       int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
+                       int64_t n_other) {
+  __shared__ OtherTable T;
+  extern __shared__ float tiles[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nb = L.nbins;
   const int stride = score_stride(nb, sp.wmax);
   float* tile = tiles + (size_t)warp * 32 * stride;
-  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t Q = n_out_params(L);
-  const int64_t P_in = n_in_params(L);
-  const int64_t q0 = gw * 32;
-  if (q0 >= Q) return;
-  int64_t my_t = 0, my_h = 0;
-  int my_st = 0, my_sh = 0;
-  bool my_ok = false;
-  if (q0 + lane < Q) {
-    Resolved r = resolve_q(L, q0 + lane);
-    my_ok = r.ok;
-    my_t = r.in_tail;
-    my_h = r.in_head;
-    my_st = round_shift(r.ph_tail, nb);
-    my_sh = round_shift(r.ph_head, nb);
-    if (!r.ok) atomicOr(err, LOKI_DEVERR_WINDOW);
+  const int64_t Q = n_out_params(L), P_in = n_in_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
+    __syncthreads();
   }
+  const int64_t q0 = qb + warp * 32;
+  if (q0 >= Q) return;
+  const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
   const size_t row = (size_t)2 * nb;
-  const float* in_t = in;                      // segment 0 of fold_in
-  const float* in_h = in + (size_t)P_in * row;  // segment 1 of fold_in
+  const float* in_t = in;
+  const float* in_h = in + (size_t)P_in * row;
   for (int k = 0; k < kmax; ++k) {
-    const int64_t it = __shfl_sync(0xFFFFFFFFu, my_t, k);
-    const int64_t ih = __shfl_sync(0xFFFFFFFFu, my_h, k);
-    const int st = __shfl_sync(0xFFFFFFFFu, my_st, k);
-    const int sh = __shfl_sync(0xFFFFFFFFu, my_sh, k);
-    const bool ok = __shfl_sync(0xFFFFFFFFu, my_ok, k);
+    const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, k);
+    const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, k);
+    const int st = __shfl_sync(0xFFFFFFFFu, me.st, k);
+    const int sh = __shfl_sync(0xFFFFFFFFu, me.sh, k);
+    const bool ok = __shfl_sync(0xFFFFFFFFu, me.ok, k);
     float* trow = tile + k * stride;
     if (!ok) {
       for (int j = lane; j < nb; j += 32) trow[j] = 0.0f;
@@ -267,16 +394,7 @@ ffa_level_score_kernel(LokiFFALevel L, const float* __restrict__ in, LokiScoreSp
       trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
     }
   }
-  __syncwarp();
-  if (lane < kmax) {
-    // Output row = full-grid flattened index of this parameter set, so that a
-    // frequency window writes its rows in place in the (P_full, nout) array.
-    const int64_t q = q0 + lane;
-    const int64_t full = (q / L.out_width) * L.counts_cur[L.nparams - 1] + L.out_start +
-                         q % L.out_width;
-    const int nout = sp.mode == 0 ? sp.nwidths : 1;
-    score_row(tile + lane * stride, nb, sp, snr + (size_t)full * nout);
-  }
+  score_out(L, sp, SK, tile, stride, lane, q0, kmax, snr);
 }
 
 // Previous-level frequency window needed by each band of current-level
@@ -310,8 +428,8 @@ __global__ void ffa_band_window_kernel(LokiFFALevel L, int64_t band_width, int64
     for (int side = 0; side < 2; ++side) {
       pset[n - 1] = L.param_arr[n - 1][side ? g1 : g0];
       for (int latter = 0; latter < 2; ++latter) {
-        ffa_resolve(pset, n, L.level, latter, L.tseg_brute, L.nbins, L.counts_prev,
-                    L.limits, idx);
+        ffa_resolve(pset, n, L.level, latter, L.tseg_brute, L.nbins, L.counts_prev, L.limits,
+                    idx);
         mn = min(mn, idx[n - 1]);
         mx = max(mx, idx[n - 1]);
       }
@@ -350,7 +468,7 @@ static int check_level(const LokiFFALevel* L) {
   return LOKI_OK;
 }
 
-static int fill_spec_check(const LokiScoreSpec* sp, int nbins) {
+static int check_spec(const LokiScoreSpec* sp, int nbins) {
   if (!sp) return set_error(LOKI_ERR_INVALID, "null score spec");
   if (sp->nwidths < 1 || sp->nwidths > LOKI_MAX_WIDTHS)
     return set_error(LOKI_ERR_INVALID, "nwidths %d out of range", sp->nwidths);
@@ -370,127 +488,75 @@ int score_smem_bytes(int nbins, int wmax, int warps) {
 }
 
 int score_warps_per_block(int nbins, int wmax) {
-  int w = 4;
+  int w = kScoreWarps;
   while (w > 1 && score_smem_bytes(nbins, wmax, w) > 200 * 1024) w >>= 1;
   return w;
+}
+
+// Aligned float4 rows are required by the nbins == 64 kernels.
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+static int launch_level(const LokiFFALevel& L, const LevelK& K, const float* in, float* out,
+                        int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
+                        int64_t n_other = 0) {
+  const int64_t Q = n_out_params(L);
+  const int64_t blocks = (Q + kLevelWarps * 32 - 1) / (kLevelWarps * 32);
+  if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+  if (L.nbins == 64 && aligned16(in) && aligned16(out))
+    ffa_level64_kernel<<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
+                                                                     n_other);
+  else
+    ffa_level_kernel<<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
+                                                                   n_other);
+  return LOKI_OK;
+}
+
+static int launch_level_score(const LokiFFALevel& L, const LevelK& K, const float* in,
+                              const LokiScoreSpec& sp, const ScoreK& SK, float* snr,
+                              int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
+                              int64_t n_other = 0) {
+  const bool fast = L.nbins == 64;
+  const int warps = fast ? kScoreWarps : score_warps_per_block(L.nbins, sp.wmax);
+  const int smem = score_smem_bytes(L.nbins, sp.wmax, warps);
+  auto kern = fast ? ffa_level_score64_kernel : ffa_level_score_kernel;
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+          cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  const int64_t Q = n_out_params(L);
+  const int64_t blocks = (Q + warps * 32 - 1) / (warps * 32);
+  if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+  kern<<<(unsigned)blocks, warps * 32, smem, s>>>(L, K, in, sp, SK, snr, err, gtab, n_other);
+  return LOKI_OK;
+}
+
+// Per-level table of the exact per-(latter, other) resolve quantities,
+// entry [latter * n_other + other].
+__global__ void other_table_kernel(LokiFFALevel L, LevelK K, OtherRes* __restrict__ tab,
+                                   int64_t n_other) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 2 * n_other;
+       t += (int64_t)gridDim.x * blockDim.x)
+    tab[t] = make_other(L, K, t % n_other, (int)(t / n_other));
+}
+
+static int64_t n_other_of(const LokiFFALevel& L) {
+  int64_t n = 1;
+  for (int d = 0; d < L.nparams - 1; ++d) n *= L.counts_cur[d];
+  return n;
+}
+
+// Floats of OtherRes table for one level (rounded up to 64-byte units).
+static int64_t table_floats(const LokiFFALevel& L) {
+  const int64_t bytes = 2 * n_other_of(L) * (int64_t)sizeof(OtherRes);
+  return ((bytes + 63) / 64) * 16;
 }
 
 }  // namespace loki
 
 using namespace loki;
 
-extern "C" int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
-                              const double* freqs, int64_t nfreqs, int64_t segment_len,
-                              int32_t nbins, double tsamp, double t_ref,
-                              void* phase_scratch, int64_t scratch_bytes,
-                              float* fold_out, void* stream) {
-  if (!ts_e || !ts_v || !freqs || !phase_scratch || !fold_out)
-    return set_error(LOKI_ERR_INVALID, "null pointer argument");
-  if (nsamps <= 0 || nfreqs <= 0 || segment_len <= 0)
-    return set_error(LOKI_ERR_INVALID, "nsamps, nfreqs and segment_len must be > 0");
-  if (nbins < 1 || nbins > 4096)
-    return set_error(LOKI_ERR_UNSUPPORTED, "nbins %d outside [1, 4096]", nbins);
-  cudaStream_t s = (cudaStream_t)stream;
-  const int64_t nseg = (nsamps + segment_len - 1) / segment_len;
-  const int elem = nbins <= 256 ? 1 : 2;
-  int64_t chunk = scratch_bytes / (segment_len * elem);
-  if (chunk < 1)
-    return set_error(LOKI_ERR_CAPACITY, "phase scratch of %lld bytes holds no frequency",
-                     (long long)scratch_bytes);
-  chunk = std::min(chunk, nfreqs);
-  constexpr int WARPS = 8;
-  const size_t smem = (size_t)WARPS * 2 * nbins * sizeof(float);
-  if (smem > 48 * 1024) {
-    cudaError_t e1 = cudaFuncSetAttribute(brutefold_kernel<uint8_t, WARPS>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaError_t e2 = cudaFuncSetAttribute(brutefold_kernel<uint16_t, WARPS>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e1 != cudaSuccess || e2 != cudaSuccess)
-      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
-  }
-  for (int64_t f0 = 0; f0 < nfreqs; f0 += chunk) {
-    const int64_t nf = std::min(chunk, nfreqs - f0);
-    const int64_t total = nf * segment_len;
-    const int mblocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 64);
-    const int64_t fblocks = (nf + WARPS - 1) / WARPS;
-    const int64_t blocks = nseg * fblocks;
-    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
-    if (elem == 1) {
-      uint8_t* map = (uint8_t*)phase_scratch;
-      phase_map_kernel<uint8_t><<<mblocks, 256, 0, s>>>(freqs + f0, nf, segment_len, nbins,
-                                                       tsamp, t_ref, map);
-      brutefold_kernel<uint8_t, WARPS><<<(unsigned)blocks, WARPS * 32, smem, s>>>(
-          ts_e, ts_v, nsamps, map, nf, f0, nfreqs, segment_len, nseg, nbins, fold_out);
-    } else {
-      uint16_t* map = (uint16_t*)phase_scratch;
-      phase_map_kernel<uint16_t><<<mblocks, 256, 0, s>>>(freqs + f0, nf, segment_len, nbins,
-                                                        tsamp, t_ref, map);
-      brutefold_kernel<uint16_t, WARPS><<<(unsigned)blocks, WARPS * 32, smem, s>>>(
-          ts_e, ts_v, nsamps, map, nf, f0, nfreqs, segment_len, nseg, nbins, fold_out);
-    }
-    int rc = check_launch("brutefold");
-    if (rc) return rc;
-  }
-  return LOKI_OK;
-}
-
-extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
-                                     int64_t band_width, const int64_t* win_lo,
-                                     const int64_t* win_hi, const float* fold_pp,
-                                     float* scratch, int64_t scratch_floats,
-                                     const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
-                                     void* stream) {
-  int rc = check_level(pen);
-  if (rc) return rc;
-  rc = check_level(fin);
-  if (rc) return rc;
-  rc = fill_spec_check(spec, fin->nbins);
-  if (rc) return rc;
-  if (!win_lo || !win_hi || !fold_pp || !scratch || !snr || !dev_err)
-    return set_error(LOKI_ERR_INVALID, "null pointer argument");
-  if (band_width < 1) return set_error(LOKI_ERR_INVALID, "band_width < 1");
-  if (fin->level != pen->level + 1 || pen->nseg_in != 2 * fin->nseg_in ||
-      fin->nparams != pen->nparams)
-    return set_error(LOKI_ERR_INVALID, "pen/fin descriptors are not consecutive levels");
-  cudaStream_t s = (cudaStream_t)stream;
-  const int warps = score_warps_per_block(fin->nbins, spec->wmax);
-  const int smem = score_smem_bytes(fin->nbins, spec->wmax, warps);
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(ffa_level_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
-    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
-  const int n = fin->nparams;
-  const int64_t nf = fin->counts_cur[n - 1];
-  const int64_t nbands = (nf + band_width - 1) / band_width;
-  int64_t other_pen = 1;
-  for (int d = 0; d < n - 1; ++d) other_pen *= pen->counts_cur[d];
-  const int64_t prof_floats = 2 * (int64_t)fin->nbins;
-  LokiFFALevel P = *pen, F = *fin;
-  for (int64_t k = 0; k < nbands; ++k) {
-    const int64_t h0 = win_lo[k], wh = win_hi[k] - win_lo[k] + 1;
-    if (wh < 1 || h0 < 0 || h0 + wh > pen->counts_cur[n - 1])
-      return set_error(LOKI_ERR_INVALID, "band %lld has an invalid window", (long long)k);
-    if (fin->nseg_in * other_pen * wh * prof_floats > scratch_floats)
-      return set_error(LOKI_ERR_CAPACITY, "band %lld needs more scratch", (long long)k);
-    P.out_start = h0;
-    P.out_width = wh;
-    const int64_t Qp = n_out_params(P);
-    const int64_t bp = ((Qp + 31) / 32 + 7) / 8;
-    ffa_level_kernel<<<(unsigned)bp, 256, 0, s>>>(P, fold_pp, scratch, dev_err);
-    F.out_start = k * band_width;
-    F.out_width = std::min(band_width, nf - F.out_start);
-    F.in_start = h0;
-    F.in_width = wh;
-    const int64_t Qf = n_out_params(F);
-    const int64_t bf = ((Qf + 31) / 32 + warps - 1) / warps;
-    ffa_level_score_kernel<<<(unsigned)bf, warps * 32, smem, s>>>(F, scratch, *spec, snr,
-                                                                  dev_err);
-  }
-  return check_launch("ffa_final_banded");
-}
-
-extern "C" int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords,
-                             int32_t* dev_err, void* stream) {
+extern "C" int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords, int32_t* dev_err,
+                             void* stream) {
   int rc = check_level(lvl);
   if (rc) return rc;
   if (!coords || !dev_err) return set_error(LOKI_ERR_INVALID, "null output pointer");
@@ -500,42 +566,30 @@ extern "C" int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords,
   return check_launch("ffa_plan");
 }
 
-extern "C" int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in,
-                              float* fold_out, int32_t* dev_err, void* stream) {
+extern "C" int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, float* fold_out,
+                              int32_t* dev_err, void* stream) {
   int rc = check_level(lvl);
   if (rc) return rc;
   if (!fold_in || !fold_out || !dev_err)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
-  const int64_t Q = n_out_params(*lvl);
-  const int64_t warps = (Q + 31) / 32;
-  const int64_t blocks = (warps + 7) / 8;
-  if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
-  ffa_level_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(*lvl, fold_in, fold_out,
-                                                                       dev_err);
+  const LevelK K = make_level_k(*lvl);
+  rc = launch_level(*lvl, K, fold_in, fold_out, dev_err, (cudaStream_t)stream);
+  if (rc) return rc;
   return check_launch("ffa_level");
 }
 
 extern "C" int loki_ffa_level_score(const LokiFFALevel* lvl, const float* fold_in,
-                                    const LokiScoreSpec* spec, float* snr,
-                                    int32_t* dev_err, void* stream) {
+                                    const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
+                                    void* stream) {
   int rc = check_level(lvl);
   if (rc) return rc;
-  rc = fill_spec_check(spec, lvl->nbins);
+  rc = check_spec(spec, lvl->nbins);
   if (rc) return rc;
   if (!fold_in || !snr || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
-  const int warps = score_warps_per_block(lvl->nbins, spec->wmax);
-  const int smem = score_smem_bytes(lvl->nbins, spec->wmax, warps);
-  if (smem > 48 * 1024) {
-    if (cudaFuncSetAttribute(ffa_level_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
-      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
-  }
-  const int64_t Q = n_out_params(*lvl);
-  const int64_t nw = (Q + 31) / 32;
-  const int64_t blocks = (nw + warps - 1) / warps;
-  if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
-  ffa_level_score_kernel<<<(unsigned)blocks, warps * 32, smem, (cudaStream_t)stream>>>(
-      *lvl, fold_in, *spec, snr, dev_err);
+  const LevelK K = make_level_k(*lvl);
+  const ScoreK SK = make_score_k(*spec, lvl->nbins);
+  rc = launch_level_score(*lvl, K, fold_in, *spec, SK, snr, dev_err, (cudaStream_t)stream);
+  if (rc) return rc;
   return check_launch("ffa_level_score");
 }
 
@@ -560,4 +614,72 @@ extern "C" int loki_ffa_band_windows(const LokiFFALevel* lvl, int64_t band_width
                                                 (unsigned long long*)win_lo,
                                                 (unsigned long long*)win_hi);
   return check_launch("ffa_band_windows");
+}
+
+extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
+                                     int64_t band_width, const int64_t* win_lo,
+                                     const int64_t* win_hi, const float* fold_pp, float* scratch,
+                                     int64_t scratch_floats, const LokiScoreSpec* spec,
+                                     float* snr, int32_t* dev_err, void* stream) {
+  int rc = check_level(pen);
+  if (rc) return rc;
+  rc = check_level(fin);
+  if (rc) return rc;
+  rc = check_spec(spec, fin->nbins);
+  if (rc) return rc;
+  if (!win_lo || !win_hi || !fold_pp || !scratch || !snr || !dev_err)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if (band_width < 1) return set_error(LOKI_ERR_INVALID, "band_width < 1");
+  if (fin->level != pen->level + 1 || pen->nseg_in != 2 * fin->nseg_in ||
+      fin->nparams != pen->nparams)
+    return set_error(LOKI_ERR_INVALID, "pen/fin descriptors are not consecutive levels");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = fin->nparams;
+  const int64_t nf = fin->counts_cur[n - 1];
+  const int64_t nbands = (nf + band_width - 1) / band_width;
+  int64_t other_pen = 1;
+  for (int d = 0; d < n - 1; ++d) other_pen *= pen->counts_cur[d];
+  const int64_t prof_floats = 2 * (int64_t)fin->nbins;
+  const LevelK KP = make_level_k(*pen);
+  const LevelK KF = make_level_k(*fin);
+  const ScoreK SK = make_score_k(*spec, fin->nbins);
+  // The per-other tables of both levels are the same for every band: build
+  // them once at the end of the scratch buffer.
+  const int64_t tab_floats = table_floats(*pen) + table_floats(*fin);
+  if (tab_floats >= scratch_floats)
+    return set_error(LOKI_ERR_CAPACITY, "scratch too small for the resolve tables");
+  const int64_t band_floats = ((scratch_floats - tab_floats) / 16) * 16;
+  OtherRes* tab_p = reinterpret_cast<OtherRes*>(scratch + band_floats);
+  OtherRes* tab_f = reinterpret_cast<OtherRes*>(scratch + band_floats + table_floats(*pen));
+  const int64_t no_p = n_other_of(*pen), no_f = n_other_of(*fin);
+  other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_p + 127) / 128, 1024), 128, 0, s>>>(
+      *pen, KP, tab_p, no_p);
+  other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_f + 127) / 128, 1024), 128, 0, s>>>(
+      *fin, KF, tab_f, no_f);
+  LokiFFALevel P = *pen, F = *fin;
+  for (int64_t k = 0; k < nbands; ++k) {
+    const int64_t h0 = win_lo[k], wh = win_hi[k] - win_lo[k] + 1;
+    if (wh < 1 || h0 < 0 || h0 + wh > pen->counts_cur[n - 1])
+      return set_error(LOKI_ERR_INVALID, "band %lld has an invalid window", (long long)k);
+    if (fin->nseg_in * other_pen * wh * prof_floats > band_floats)
+      return set_error(LOKI_ERR_CAPACITY, "band %lld needs more scratch", (long long)k);
+    P.out_start = h0;
+    P.out_width = wh;
+    rc = launch_level(P, KP, fold_pp, scratch, dev_err, s, tab_p, no_p);
+    if (rc) return rc;
+    F.out_start = k * band_width;
+    F.out_width = std::min(band_width, nf - F.out_start);
+    F.in_start = h0;
+    F.in_width = wh;
+    rc = launch_level_score(F, KF, scratch, *spec, SK, snr, dev_err, s, tab_f, no_f);
+    if (rc) return rc;
+  }
+  return check_launch("ffa_final_banded");
+}
+
+extern "C" int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
+                                                 int64_t max_window) {
+  if (check_level(pen) || check_level(fin) || max_window < 1) return -1;
+  const int64_t band = fin->nseg_in * n_other_of(*pen) * max_window * 2 * (int64_t)fin->nbins;
+  return ((band + 15) / 16) * 16 + table_floats(*pen) + table_floats(*fin);
 }

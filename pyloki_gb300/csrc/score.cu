@@ -14,7 +14,7 @@ int score_warps_per_block(int nbins, int wmax);
 // runs the sequential prefix sum and the width scan of row k.
 template <bool FROM_EV>
 __global__ void __launch_bounds__(128)
-score_kernel(const float* __restrict__ in, int64_t nprof, int nb, LokiScoreSpec sp,
+score_kernel(const float* __restrict__ in, int64_t nprof, int nb, LokiScoreSpec sp, ScoreK SK,
              float* __restrict__ out) {
   extern __shared__ float tiles[];
   const int lane = threadIdx.x & 31;
@@ -37,7 +37,9 @@ score_kernel(const float* __restrict__ in, int64_t nprof, int nb, LokiScoreSpec 
   __syncwarp();
   if (lane < kmax) {
     const int nout = sp.mode == 0 ? sp.nwidths : 1;
-    score_row(tile + lane * stride, nb, sp, out + (size_t)(p0 + lane) * nout);
+    float* row = tile + lane * stride;
+    if (SK.pow2_64) score_row64_pow2(row, sp, SK, out + (size_t)(p0 + lane) * nout);
+    else score_row(row, nb, sp, out + (size_t)(p0 + lane) * nout);
   }
 }
 
@@ -69,7 +71,8 @@ static int launch_score(const float* in, int64_t nprof, int nbins, LokiScoreSpec
   const int64_t nw = (nprof + 31) / 32;
   const int64_t blocks = (nw + warps - 1) / warps;
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
-  score_kernel<FROM_EV><<<(unsigned)blocks, warps * 32, smem, s>>>(in, nprof, nbins, sp, out);
+  const ScoreK SK = make_score_k(sp, nbins);
+  score_kernel<FROM_EV><<<(unsigned)blocks, warps * 32, smem, s>>>(in, nprof, nbins, sp, SK, out);
   return check_launch(what);
 }
 

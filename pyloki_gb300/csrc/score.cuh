@@ -57,11 +57,132 @@ __device__ __forceinline__ double snr_width(const float* row, int nbins, int w,
   return __dsub_rn(__dmul_rn(hb, (double)dmax), __dmul_rn(b, (double)total));
 }
 
+// ---- fast path: nbins == 64, widths 1, 2, 4, ..., 2^(nw-1) -----------------
+//
+// The reference's S/N of one width is RN32(RN64(RN64(hb*d) - RN64(b*T))) with
+// d = max prefix difference and T = total (both float32). It is estimated in
+// two-float FP32 (hb, b split into hi/lo floats, exact products by FMA, exact
+// two-sum); when the estimate is farther than 2^-40 * max(|hb d|, |b T|) from
+// an f32 rounding midpoint the rounding of the FP64 chain is certain,
+// otherwise the FP64 chain is evaluated.
+struct ScoreK {
+  float hb_hi[LOKI_MAX_WIDTHS], hb_lo[LOKI_MAX_WIDTHS];
+  float b_hi[LOKI_MAX_WIDTHS], b_lo[LOKI_MAX_WIDTHS];
+  int pow2_64;  // nbins == 64 and widths == 1, 2, 4, ... (<= 32)
+  int inv_one;  // inv_stdnoise == 1
+};
+
+inline ScoreK make_score_k(const LokiScoreSpec& sp, int nbins) {
+  ScoreK k;
+  bool pow2 = nbins == 64 && sp.nwidths <= 6;
+  for (int i = 0; i < sp.nwidths; ++i) {
+    k.hb_hi[i] = (float)sp.hb[i];
+    k.hb_lo[i] = (float)(sp.hb[i] - (double)k.hb_hi[i]);
+    k.b_hi[i] = (float)sp.b[i];
+    k.b_lo[i] = (float)(sp.b[i] - (double)k.b_hi[i]);
+    if (sp.widths[i] != (1 << i)) pow2 = false;
+  }
+  k.pow2_64 = pow2 ? 1 : 0;
+  k.inv_one = sp.inv_stdnoise == 1.0 ? 1 : 0;
+  return k;
+}
+
+__device__ __forceinline__ float snr_fast(float d, float T, float hbh, float hbl, float bh,
+                                          float bl, double hb, double b) {
+  const float p1 = hbh * d;
+  float e1 = fmaf(hbh, d, -p1);
+  e1 = fmaf(hbl, d, e1);
+  const float p2 = bh * T;
+  float e2 = fmaf(bh, T, -p2);
+  e2 = fmaf(bl, T, e2);
+  const float s = p1 - p2;
+  const float bb = s - p1;
+  const float es = (p1 - (s - bb)) + (-p2 - bb);
+  const float lo = (e1 - e2) + es;
+  const float r = s + lo;
+  const float res = (s - r) + lo;
+  const unsigned bits = __float_as_uint(fabsf(r));
+  const unsigned expo = bits >> 23;
+  if (expo > 30 && expo < 255 && (bits & 0x7FFFFFu) != 0u) {
+    const float half_ulp = __uint_as_float((expo - 24u) << 23);
+    const float margin = fmaxf(fabsf(p1), fabsf(p2)) * 9.094947e-13f;  // 2^-40
+    if (fabsf(res) < half_ulp - margin) return r;
+  }
+  return __double2float_rn(__dsub_rn(__dmul_rn(hb, (double)d), __dmul_rn(b, (double)T)));
+}
+
+// Two IEEE round-to-nearest subtractions in one instruction (sm_100+ f32x2).
+__device__ __forceinline__ void sub2(float a0, float a1, float b0, float b1, float& d0,
+                                     float& d1) {
+  unsigned long long a, b, d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(a) : "f"(a0), "f"(a1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(b) : "f"(b0), "f"(b1));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d0), "=f"(d1) : "l"(d));
+}
+
+// max of three; a NaN input is ignored like Python's max(acc, nan) == acc.
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float m;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(a), "f"(b), "f"(c));
+  return m;
+}
+
+template <int W>
+__device__ __forceinline__ float dmax64(const float (&P)[96]) {
+  float m = -FLT_MAX;
+#pragma unroll
+  for (int i = 0; i < 64; i += 2) {
+    float d0, d1;
+    sub2(P[i + W], P[i + W + 1], P[i], P[i + 1], d0, d1);
+    m = max3(m, d0, d1);
+  }
+  return m;
+}
+
+// Sequential prefix in registers, then the width scans with compile-time
+// indices (no shared-memory traffic after the row is read once).
+__device__ __forceinline__ void score_row64_pow2(const float* row, const LokiScoreSpec& sp,
+                                                 const ScoreK& K, float* out) {
+  float P[96];
+  P[0] = row[0];
+#pragma unroll
+  for (int i = 1; i < 64; ++i) P[i] = __fadd_rn(P[i - 1], row[i]);
+  const float total = P[63];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) P[64 + j] = __fadd_rn(P[j], total);
+  float best = -FLT_MAX;
+  for (int iw = 0; iw < sp.nwidths; ++iw) {
+    float dm;
+    switch (iw) {
+      case 0: dm = dmax64<1>(P); break;
+      case 1: dm = dmax64<2>(P); break;
+      case 2: dm = dmax64<4>(P); break;
+      case 3: dm = dmax64<8>(P); break;
+      case 4: dm = dmax64<16>(P); break;
+      default: dm = dmax64<32>(P); break;
+    }
+    float s;
+    if (K.inv_one) {
+      s = snr_fast(dm, total, K.hb_hi[iw], K.hb_lo[iw], K.b_hi[iw], K.b_lo[iw], sp.hb[iw],
+                   sp.b[iw]);
+    } else {
+      const double x = __dsub_rn(__dmul_rn(sp.hb[iw], (double)dm),
+                                 __dmul_rn(sp.b[iw], (double)total));
+      s = __double2float_rn(__dmul_rn(x, sp.inv_stdnoise));
+    }
+    if (sp.mode == 0) out[iw] = s;
+    else if (s > best) best = s;
+  }
+  if (sp.mode != 0) out[0] = best;
+}
+
 // Score the row owned by this lane. mode 0 writes nwidths values at out,
 // mode 1 writes the max over widths at out[0].
 __device__ __forceinline__ void score_row(float* row, int nbins, const LokiScoreSpec& sp,
                                           float* out) {
   const float total = prefix_row(row, nbins, sp.wmax);
+  // (generic path: any nbins and width list, prefix in shared memory)
   if (sp.mode == 0) {
     for (int iw = 0; iw < sp.nwidths; ++iw) {
       double s = snr_width(row, nbins, sp.widths[iw], sp.hb[iw], sp.b[iw], total);

@@ -46,6 +46,11 @@ class _Grid:
         self.counts = np.array([len(p) for p in self.param_arr], dtype=np.int64)
         self.dev = [torch.from_numpy(np.ascontiguousarray(p, dtype=np.float64)).to(device)
                     for p in self.param_arr]
+        # last-dimension grid as float2 (hi, lo): f == hi + lo to ~2^-48
+        last = np.ascontiguousarray(self.param_arr[-1], dtype=np.float64)
+        hi = last.astype(np.float32)
+        lo = (last - hi.astype(np.float64)).astype(np.float32)
+        self.split = torch.from_numpy(np.stack([hi, lo], axis=1).copy()).to(device)
 
     @property
     def size(self) -> int:
@@ -92,6 +97,7 @@ def level_desc(cfg: PulsarSearchConfig, cur: _Grid, prev: _Grid, nseg_in: int,
     d.out_start, d.out_width = o0, ow
     d.in_start, d.in_width = i0, iw
     d.nseg_in = nseg_in
+    d.last_split = cur.split.data_ptr()
     return d
 
 
@@ -214,6 +220,10 @@ class DynamicProgramming:
                     msg = (f"param_arr has {len(g0.param_arr[ip])} values, "
                            "should have only one")
                     raise ValueError(msg)
+        freqs = g0.param_arr[-1]
+        if not np.all(np.isfinite(freqs)) or np.any(freqs <= 0):
+            msg = "Frequency must be positive."
+            raise ValueError(msg)
         dev = self._device
         ts_e = torch.as_tensor(self.ts_data.ts_e).to(dev, non_blocking=True)
         ts_v = torch.as_tensor(self.ts_data.ts_v).to(dev, non_blocking=True)
@@ -364,11 +374,13 @@ class DynamicProgramming:
         nseg_pen = nseg_pp // 2
         width, lo, hi = self.band_plan(band_bytes)
         wmax = int((hi - lo + 1).max())
-        other_pen = _cart_len(pen.counts[:-1])
-        scratch = torch.empty(nseg_pen * other_pen * wmax * 2 * cfg.nbins,
-                              dtype=torch.float32, device=self._device)
         d_pen = level_desc(cfg, pen, pp, nseg_pp)
         d_fin = level_desc(cfg, fin, pen, nseg_pen)
+        nfl = int(self._lib.loki_ffa_final_banded_scratch(d_pen, d_fin, wmax))
+        if nfl <= 0:
+            msg = "invalid banded level descriptors"
+            raise ValueError(msg)
+        scratch = torch.empty(nfl, dtype=torch.float32, device=self._device)
         lo = np.ascontiguousarray(lo, np.int64)
         hi = np.ascontiguousarray(hi, np.int64)
         _lib.check(self._lib.loki_ffa_final_banded(

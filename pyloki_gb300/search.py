@@ -39,15 +39,20 @@ class Periodogram:
     def ndim(self) -> int:
         return len(self.param_names)
 
-    def find_best_indices(self) -> tuple[int, ...]:
+    def find_best_indices(self, *, ignore_nan: bool = False) -> tuple[int, ...]:
+        """Index of the maximum S/N. Like the reference (``np.argmax``) a NaN
+        S/N (a profile with an empty bin: e / sqrt(0)) wins unless
+        ``ignore_nan`` is set."""
         if isinstance(self.snrs, torch.Tensor):
-            flat = int(torch.argmax(self.snrs).item())
+            s = torch.nan_to_num(self.snrs, nan=-torch.inf) if ignore_nan else self.snrs
+            flat = int(torch.argmax(s).item())
         else:
-            flat = int(np.argmax(self.snrs))
+            s = np.where(np.isnan(self.snrs), -np.inf, self.snrs) if ignore_nan else self.snrs
+            flat = int(np.argmax(s))
         return tuple(int(i) for i in np.unravel_index(flat, tuple(self.snrs.shape)))
 
-    def find_best_params(self) -> dict[str, float]:
-        idx = self.find_best_indices()
+    def find_best_params(self, *, ignore_nan: bool = False) -> dict[str, float]:
+        idx = self.find_best_indices(ignore_nan=ignore_nan)
         best = {name: self.params[name][i] for name, i in zip(self.param_names, idx, strict=False)}
         return {"snr": float(self.snrs[idx]), **best}
 

@@ -15,7 +15,7 @@ def declared_symbols() -> list[str]:
     names = []
     for hdr in (ROOT / "include").glob("*.h"):
         text = re.sub(r"/\*.*?\*/", "", hdr.read_text(), flags=re.S)
-        names += re.findall(r"^\s*(?:int|const char\*|void)\s+(loki_\w+)\s*\(", text, flags=re.M)
+        names += re.findall(r"^\s*(?:int64_t|int|const char\*|void)\s+(loki_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 

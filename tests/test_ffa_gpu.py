@@ -157,6 +157,9 @@ def test_accel_search_spot_trials_vs_oracle(cuda_device):
     prof = O.ffa_trials(ts_e, ts_v, cfg, pick)
     ref = O.boxcar_snr(O.fold_norm(prof), cfg.score_widths)
     np.testing.assert_array_equal(flat[pick], ref)
+    # every trial against the oracle's fully materialised search
+    full = O.boxcar_snr(O.fold_norm(O.ffa_execute(ts_e, ts_v, cfg)[0]), cfg.score_widths)
+    np.testing.assert_array_equal(snrs, full)
     # unbanded fused path gives the same array
     dyp2 = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
     np.testing.assert_array_equal(dyp2.search(banded=False).cpu().numpy(), snrs)

@@ -51,6 +51,24 @@ def test_ragged_counts_and_wide_widths(cuda_device, nprof, nbins, widths):
     np.testing.assert_array_equal(snr_score_batch(comb, w), O.snr_score_batch(comb, w))
 
 
+def test_empty_bins_nan_semantics(cuda_device):
+    """Folds with zero-variance (empty) bins give e / sqrt(0) = NaN or inf
+    entries; the NaN propagation and max-skipping must match the reference."""
+    from pyloki_gb300.scoring import boxcar_snr_nd, snr_score_batch
+
+    rng = np.random.default_rng(7)
+    n, nb = 200, 64
+    comb = np.stack([rng.standard_normal((n, nb)), 1 + rng.random((n, nb))], axis=1)
+    comb = comb.astype(np.float32)
+    comb[::3, 1, ::2] = 0.0          # every other bin empty: 0 / 0 = NaN
+    comb[::3, 0, ::2] = 0.0
+    comb[1::7, 1, 5] = 0.0           # a single zero variance with e != 0: +-inf
+    w = np.array([1, 2, 4, 8, 16, 32], np.int64)
+    np.testing.assert_array_equal(snr_score_batch(comb, w), O.snr_score_batch(comb, w))
+    norm = O.fold_norm(comb)
+    np.testing.assert_array_equal(boxcar_snr_nd(norm, w), O.boxcar_snr(norm, w))
+
+
 def test_empty_input(cuda_device):
     from pyloki_gb300.scoring import boxcar_snr_nd, snr_score_batch
 
