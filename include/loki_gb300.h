@@ -154,6 +154,101 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
 int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                       int64_t max_window);
 
+/* ---- enumerate-prune (Taylor basis, float32 folds) -------------------- */
+
+/* Constants of one pruning level, computed by the host with the reference's
+ * numpy expressions (prune.py:165-332 with core/taylor.py:68-339):
+ * leaves are (P + 2, 2) float64 rows [d_P .. d_1, d_0, (f0, flag)] x (value,
+ * error); backtracks are (P + 2) int32 [parent, ffa param idx.., phase]. */
+typedef struct {
+  int32_t poly_order;     /* P (number of Taylor parameters d_P..d_1), <= 5 */
+  int32_t nbins;
+  int32_t nparams_ffa;    /* parameters of the FFA grid (backtrack columns) */
+  int32_t moving;         /* 1: moving grid, 0: fixed grid */
+  int32_t tiling;         /* 0 aggressive, 1 quadrature, 2 conservative */
+  int32_t branch_max;
+  double eta_m;           /* eta - FLOAT_EPSILON */
+  double dfc[LOKI_MAX_PARAMS];      /* poly_taylor_step_f(...) * C, order d_P..d_1 */
+  double fac[LOKI_MAX_PARAMS];      /* bin-shift factors (psr_utils.py:227-248) */
+  double tm_a[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1]; /* Taylor shift to t0_add */
+  double tm_i[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1]; /* ... to t0_init (moving) */
+  double tm_n[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1]; /* transform to t0_next */
+  double tm_e[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1]; /* |tm_n| or tm_n**2 */
+  double dt_phase;        /* t0_add - t0_init */
+  int64_t n_accel, n_freq;          /* FFA grid counts of the accel / freq axes */
+  double accel_min, accel_inv;      /* accel_inv = n_accel / range, 0 if flat */
+  double freq_min, freq_inv;
+} LokiPruneLevel;
+
+/* Per-parent branching result. */
+typedef struct {
+  double first[LOKI_MAX_PARAMS];  /* first child centre (or the parent value) */
+  double dact[LOKI_MAX_PARAMS];   /* actual child step (or the parent step) */
+  int32_t count[LOKI_MAX_PARAMS];
+  int32_t reserved[3];
+} LokiBranchInfo;
+
+/* Branch every parent (core/taylor.py:68-169 poly_taylor_branch_batch):
+ * info[i] and the exclusive child offsets (n_parents + 1 int64; the last is
+ * the number of leaves). scan_scratch needs loki_scan_scratch_bytes(n + 1). */
+int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves, int64_t n_parents,
+                      LokiBranchInfo* info, int64_t* offsets, void* scan_scratch,
+                      int64_t scan_scratch_bytes, int32_t* dev_err, void* stream);
+
+/* Resolve, gather, shift-add and score every child leaf (core/taylor.py:
+ * 172-277, core/common.py:375-400, detection/scoring.py:249-282). Writes the
+ * child score, its (accel, freq) FFA indices and its phase; score_minmax
+ * (2 floats, min then max) is atomically folded over all children. */
+int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves, const float* folds,
+                     int64_t n_parents, const LokiBranchInfo* info, const int64_t* offsets,
+                     int64_t n_children, const float* fold_segment,
+                     const LokiScoreSpec* spec, float* child_scores, int32_t* child_idx,
+                     double* child_phase, float* score_minmax, int32_t* dev_err,
+                     void* stream);
+
+/* Ids of the children whose score >= threshold, in order (no overflow). */
+int loki_prune_select(const float* child_scores, int64_t n_children, double threshold,
+                      int64_t* surv_ids, int64_t* n_surv, void* scan_scratch,
+                      int64_t scan_scratch_bytes, void* stream);
+
+/* Exact batch-sequential selection with the overflow rule of
+ * WorldTree.add_batch / prune_on_overload (utils/world_tree.py:482-551), for
+ * when more than capacity children pass. One block walks the parent batches
+ * in order; ids (capacity + 16 * batch children) int64 and keys (same count)
+ * float32 are scratch. Writes the survivor ids, their count and the final
+ * threshold (float64). */
+int loki_prune_select_overflow(const float* child_scores, const int64_t* offsets,
+                               int64_t n_parents, int64_t batch_size, double threshold,
+                               int64_t capacity, int64_t* surv_ids, int64_t* n_surv,
+                               double* thr_out, int64_t* scratch_ids, float* scratch_keys,
+                               int64_t scratch_len, void* stream);
+
+/* Write the new tree from the survivors (transform core/taylor.py:323-339,
+ * backtrack prune.py:307-312): leaves, folds, scores, scores_ep, backtracks. */
+int loki_prune_emit(const LokiPruneLevel* lvl, const double* leaves, const float* folds,
+                    const LokiBranchInfo* info, const int64_t* offsets, int64_t n_parents,
+                    const float* fold_segment, const int64_t* surv_ids, int64_t n_surv,
+                    const float* child_scores, const int32_t* child_idx,
+                    const double* child_phase, double* leaves_out, float* folds_out,
+                    float* scores_out, float* scores_ep_out, int32_t* bt_out,
+                    void* stream);
+
+/* Re-fold every survivor over all segments so far and re-score it
+ * (dynamic/dyn_poly_taylor.py:587-628 ascend_func). Device arrays, one entry
+ * per segment in accumulation order: tm_seg the Taylor shift matrices
+ * ((P+1)^2 doubles each, to t0_seg - t0_cur), dt_seg the phase time offsets,
+ * seg_idx the segment index into ffa_fold (nseg_ffa, *counts, 2, nbins) whose
+ * segments are seg_stride floats apart. Overwrites folds and scores and copies
+ * the old scores to scores_ep. */
+int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves, float* folds,
+                      float* scores, float* scores_ep, int64_t n, int32_t nseg,
+                      const double* tm_seg, const double* dt_seg, const int32_t* seg_idx,
+                      const float* ffa_fold, int64_t seg_stride, const LokiScoreSpec* spec,
+                      int32_t* dev_err, void* stream);
+
+/* Scratch bytes for the internal scans over n elements. */
+int64_t loki_scan_scratch_bytes(int64_t n);
+
 /* ---- scoring ---------------------------------------------------------- */
 
 /* Boxcar S/N of normalised profiles (nprof, nbins) -> (nprof, nwidths) or

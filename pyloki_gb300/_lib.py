@@ -69,10 +69,50 @@ class LokiScoreSpec(C.Structure):
     ]
 
 
+_M6 = (C.c_double * (MAX_PARAMS + 1)) * (MAX_PARAMS + 1)
+
+
+class LokiPruneLevel(C.Structure):
+    _fields_ = [
+        ("poly_order", C.c_int32),
+        ("nbins", C.c_int32),
+        ("nparams_ffa", C.c_int32),
+        ("moving", C.c_int32),
+        ("tiling", C.c_int32),
+        ("branch_max", C.c_int32),
+        ("eta_m", C.c_double),
+        ("dfc", C.c_double * MAX_PARAMS),
+        ("fac", C.c_double * MAX_PARAMS),
+        ("tm_a", _M6),
+        ("tm_i", _M6),
+        ("tm_n", _M6),
+        ("tm_e", _M6),
+        ("dt_phase", C.c_double),
+        ("n_accel", C.c_int64),
+        ("n_freq", C.c_int64),
+        ("accel_min", C.c_double),
+        ("accel_inv", C.c_double),
+        ("freq_min", C.c_double),
+        ("freq_inv", C.c_double),
+    ]
+
+
+class LokiBranchInfo(C.Structure):
+    _fields_ = [
+        ("first", C.c_double * MAX_PARAMS),
+        ("dact", C.c_double * MAX_PARAMS),
+        ("count", C.c_int32 * MAX_PARAMS),
+        ("reserved", C.c_int32 * 3),
+    ]
+
+
+BRANCH_INFO_BYTES = C.sizeof(LokiBranchInfo)
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
 _D = C.c_double
+_PL = C.POINTER(LokiPruneLevel)
 
 #: name -> (restype, argtypes); the exported C ABI.
 SIGNATURES: dict[str, tuple] = {
@@ -92,6 +132,17 @@ SIGNATURES: dict[str, tuple] = {
     "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
+    "loki_scan_scratch_bytes": (C.c_int64, [_I64]),
+    "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
+    "loki_prune_score": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _I64, _P,
+                                   C.POINTER(LokiScoreSpec), _P, _P, _P, _P, _P, _P]),
+    "loki_prune_select": (C.c_int, [_P, _I64, _D, _P, _P, _P, _I64, _P]),
+    "loki_prune_select_overflow": (C.c_int, [_P, _P, _I64, _I64, _D, _I64, _P, _P, _P, _P,
+                                             _P, _I64, _P]),
+    "loki_prune_emit": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P,
+                                  _P, _P, _P, _P, _P]),
+    "loki_prune_ascend": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64,
+                                    C.POINTER(LokiScoreSpec), _P, _P]),
 }
 
 _lock = threading.Lock()

@@ -93,17 +93,18 @@ __device__ __forceinline__ LaneTrial lane_trial(const LokiFFALevel& L, const Lev
                                                 int32_t* err) {
   LaneTrial r{0, 0, 0, 0, false};
   if (q >= Q) return r;
-  const int64_t other = q / L.out_width;
+  int64_t other, off;
+  q_split(L, K, q, other, off);
   TrialRes tr;
   if (gtab) {
-    tr = resolve_trial(L, K, gtab[other], gtab[n_other + other], q);
+    tr = resolve_trial(L, K, gtab[other], gtab[n_other + other], off);
   } else if (tab) {
     const int oi = (int)(other - T.first);
-    tr = resolve_trial(L, K, T.e[0][oi], T.e[1][oi], q);
+    tr = resolve_trial(L, K, T.e[0][oi], T.e[1][oi], off);
   } else {
     const OtherRes ot = make_other(L, K, other, 0);
     const OtherRes oh = make_other(L, K, other, 1);
-    tr = resolve_trial(L, K, ot, oh, q);
+    tr = resolve_trial(L, K, ot, oh, off);
   }
   r.t = tr.in_tail;
   r.h = tr.in_head;
@@ -152,20 +153,15 @@ constexpr int kLevelWarps = 8;
 constexpr int kBatch = 4;
 
 // nbins == 64: one float4 per lane per row, four rows in flight per lane.
-__global__ void __launch_bounds__(kLevelWarps * 32, 4)
-ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
-                   float* __restrict__ out, int32_t* __restrict__ err,
-                   const OtherRes* __restrict__ gtab, int64_t n_other) {
-  __shared__ OtherTable T;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// One warp's work: output parameters [q0, q0 + 32).
+__device__ __forceinline__ void level64_warp(const LokiFFALevel& L, const LevelK& K,
+                                             const float* __restrict__ in,
+                                             float* __restrict__ out, int32_t* err,
+                                             const OtherTable& T, bool tab,
+                                             const OtherRes* __restrict__ gtab,
+                                             int64_t n_other, int64_t q0) {
+  const int lane = threadIdx.x & 31;
   const int64_t Q = n_out_params(L), P_in = n_in_params(L);
-  const int64_t qb = (int64_t)blockIdx.x * kLevelWarps * 32;
-  bool tab = false;
-  if (!gtab) {  // uniform: the whole block takes the same branch
-    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + kLevelWarps * 32, Q) - 1);
-    __syncthreads();
-  }
-  const int64_t q0 = qb + warp * 32;
   if (q0 >= Q) return;
   const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
@@ -201,6 +197,22 @@ ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
       }
     }
   }
+}
+
+__global__ void __launch_bounds__(kLevelWarps * 32, 4)
+ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                   float* __restrict__ out, int32_t* __restrict__ err,
+                   const OtherRes* __restrict__ gtab, int64_t n_other) {
+  __shared__ OtherTable T;
+  const int warp = threadIdx.x >> 5;
+  const int64_t Q = n_out_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * kLevelWarps * 32;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + kLevelWarps * 32, Q) - 1);
+    __syncthreads();
+  }
+  level64_warp(L, K, in, out, err, T, tab, gtab, n_other, qb + warp * 32);
 }
 
 // Any nbins: scalar, lane j handles bins j, j + 32, ...
@@ -258,14 +270,15 @@ ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
 
 constexpr int kScoreWarps = 4;
 
-__device__ __forceinline__ void score_out(const LokiFFALevel& L, const LokiScoreSpec& sp,
-                                          const ScoreK& SK, float* tile, int stride, int lane,
-                                          int64_t q0, int kmax, float* snr) {
+__device__ __forceinline__ void score_out(const LokiFFALevel& L, const LevelK& K,
+                                          const LokiScoreSpec& sp, const ScoreK& SK,
+                                          float* tile, int stride, int lane, int64_t q0,
+                                          int kmax, float* snr) {
   __syncwarp();
   if (lane < kmax) {
-    const int64_t q = q0 + lane;
-    const int64_t full = (q / L.out_width) * L.counts_cur[L.nparams - 1] + L.out_start +
-                         q % L.out_width;
+    int64_t other, off;
+    q_split(L, K, q0 + lane, other, off);
+    const int64_t full = other * L.counts_cur[L.nparams - 1] + L.out_start + off;
     const int nout = sp.mode == 0 ? sp.nwidths : 1;
     float* row = tile + lane * stride;
     if (SK.pow2_64) score_row64_pow2(row, sp, SK, snr + (size_t)full * nout);
@@ -273,24 +286,17 @@ __device__ __forceinline__ void score_out(const LokiFFALevel& L, const LokiScore
   }
 }
 
-__global__ void __launch_bounds__(kScoreWarps * 32)
-ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
-                         LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
-                         int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
-                         int64_t n_other) {
-  __shared__ OtherTable T;
-  extern __shared__ float tiles[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// One warp's work of the fused final level: parameters [q0, q0 + 32).
+__device__ __forceinline__ void score64_warp(const LokiFFALevel& L, const LevelK& K,
+                                             const float* __restrict__ in,
+                                             const LokiScoreSpec& sp, const ScoreK& SK,
+                                             float* __restrict__ snr, int32_t* err,
+                                             const OtherTable& T, bool tab,
+                                             const OtherRes* __restrict__ gtab,
+                                             int64_t n_other, int64_t q0, float* tile) {
+  const int lane = threadIdx.x & 31;
   const int stride = score_stride(64, sp.wmax);
-  float* tile = tiles + (size_t)warp * 32 * stride;
   const int64_t Q = n_out_params(L), P_in = n_in_params(L);
-  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
-  bool tab = false;
-  if (!gtab) {  // uniform: the whole block takes the same branch
-    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
-    __syncthreads();
-  }
-  const int64_t q0 = qb + warp * 32;
   if (q0 >= Q) return;
   const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
@@ -343,7 +349,51 @@ ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
       }
     }
   }
-  score_out(L, sp, SK, tile, stride, lane, q0, kmax, snr);
+  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr);
+}
+
+__global__ void __launch_bounds__(kScoreWarps * 32)
+ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+                         LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
+                         int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
+                         int64_t n_other) {
+  __shared__ OtherTable T;
+  extern __shared__ float tiles[];
+  const int warp = threadIdx.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(64, sp.wmax);
+  const int64_t Q = n_out_params(L);
+  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
+  bool tab = false;
+  if (!gtab) {  // uniform: the whole block takes the same branch
+    tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
+    __syncthreads();
+  }
+  score64_warp(L, K, in, sp, SK, snr, err, T, tab, gtab, n_other, qb + warp * 32, tile);
+}
+
+// Banded pipeline step (nbins == 64): blocks [0, nblk_f) score final band k
+// from scratch buffer k % 2 while the remaining blocks build the penultimate
+// band k + 1 into the other buffer, so the small penultimate-level work fills
+// the SMs the scoring leaves idle. Launch order alone orders the buffers:
+// step k + 1 starts after step k has finished both halves.
+__global__ void __launch_bounds__(kScoreWarps * 32)
+band_union64_kernel(LokiFFALevel F, LevelK KF, const float* __restrict__ in_f,
+                    LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
+                    const OtherRes* __restrict__ tab_f, int64_t no_f, int64_t nblk_f,
+                    LokiFFALevel P, LevelK KP, const float* __restrict__ in_p,
+                    float* __restrict__ out_p, const OtherRes* __restrict__ tab_p,
+                    int64_t no_p, int32_t* __restrict__ err) {
+  extern __shared__ float tiles[];
+  __shared__ OtherTable T;  // unused: both levels come with global tables
+  const int warp = threadIdx.x >> 5;
+  if (blockIdx.x < nblk_f) {
+    float* tile = tiles + (size_t)warp * 32 * score_stride(64, sp.wmax);
+    score64_warp(F, KF, in_f, sp, SK, snr, err, T, false, tab_f, no_f,
+                 (int64_t)blockIdx.x * blockDim.x + warp * 32, tile);
+  } else {
+    level64_warp(P, KP, in_p, out_p, err, T, false, tab_p, no_p,
+                 (int64_t)(blockIdx.x - nblk_f) * blockDim.x + warp * 32);
+  }
 }
 
 __global__ void __launch_bounds__(kScoreWarps * 32)
@@ -394,7 +444,7 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
       trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
     }
   }
-  score_out(L, sp, SK, tile, stride, lane, q0, kmax, snr);
+  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr);
 }
 
 // Previous-level frequency window needed by each band of current-level
@@ -640,8 +690,8 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
   int64_t other_pen = 1;
   for (int d = 0; d < n - 1; ++d) other_pen *= pen->counts_cur[d];
   const int64_t prof_floats = 2 * (int64_t)fin->nbins;
-  const LevelK KP = make_level_k(*pen);
-  const LevelK KF = make_level_k(*fin);
+  LevelK KP = make_level_k(*pen);
+  LevelK KF = make_level_k(*fin);
   const ScoreK SK = make_score_k(*spec, fin->nbins);
   // The per-other tables of both levels are the same for every band: build
   // them once at the end of the scratch buffer.
@@ -663,14 +713,58 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
       return set_error(LOKI_ERR_INVALID, "band %lld has an invalid window", (long long)k);
     if (fin->nseg_in * other_pen * wh * prof_floats > band_floats)
       return set_error(LOKI_ERR_CAPACITY, "band %lld needs more scratch", (long long)k);
+  }
+  const int64_t half = ((band_floats / 2) / 16) * 16;
+  int64_t wmax_win = 0;
+  for (int64_t k = 0; k < nbands; ++k) wmax_win = std::max(wmax_win, win_hi[k] - win_lo[k] + 1);
+  const bool pipelined = fin->nbins == 64 && aligned16(fold_pp) && aligned16(scratch) &&
+                         fin->nseg_in * other_pen * wmax_win * prof_floats <= half;
+  if (pipelined) {
+    // Software pipeline over bands with two scratch buffers.
+    float* buf[2] = {scratch, scratch + half};
+    const int smem = score_smem_bytes(64, spec->wmax, kScoreWarps);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(band_union64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+    P.out_start = win_lo[0];
+    P.out_width = win_hi[0] - win_lo[0] + 1;
+    set_out_width(KP, P);
+    rc = launch_level(P, KP, fold_pp, buf[0], dev_err, s, tab_p, no_p);
+    if (rc) return rc;
+    for (int64_t k = 0; k < nbands; ++k) {
+      F.out_start = k * band_width;
+      F.out_width = std::min(band_width, nf - F.out_start);
+      F.in_start = win_lo[k];
+      F.in_width = win_hi[k] - win_lo[k] + 1;
+      set_out_width(KF, F);
+      const int64_t nblk_f = (n_out_params(F) + kScoreWarps * 32 - 1) / (kScoreWarps * 32);
+      int64_t nblk_p = 0;
+      if (k + 1 < nbands) {
+        P.out_start = win_lo[k + 1];
+        P.out_width = win_hi[k + 1] - win_lo[k + 1] + 1;
+        set_out_width(KP, P);
+        nblk_p = (n_out_params(P) + kScoreWarps * 32 - 1) / (kScoreWarps * 32);
+      }
+      if (nblk_f + nblk_p > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+      band_union64_kernel<<<(unsigned)(nblk_f + nblk_p), kScoreWarps * 32, smem, s>>>(
+          F, KF, buf[k & 1], *spec, SK, snr, tab_f, no_f, nblk_f, P, KP, fold_pp,
+          buf[(k + 1) & 1], tab_p, no_p, dev_err);
+    }
+    return check_launch("ffa_final_banded");
+  }
+  for (int64_t k = 0; k < nbands; ++k) {
+    const int64_t h0 = win_lo[k], wh = win_hi[k] - win_lo[k] + 1;
     P.out_start = h0;
     P.out_width = wh;
+    set_out_width(KP, P);
     rc = launch_level(P, KP, fold_pp, scratch, dev_err, s, tab_p, no_p);
     if (rc) return rc;
     F.out_start = k * band_width;
     F.out_width = std::min(band_width, nf - F.out_start);
     F.in_start = h0;
     F.in_width = wh;
+    set_out_width(KF, F);
     rc = launch_level_score(F, KF, scratch, *spec, SK, snr, dev_err, s, tab_f, no_f);
     if (rc) return rc;
   }
@@ -680,6 +774,7 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
 extern "C" int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                                  int64_t max_window) {
   if (check_level(pen) || check_level(fin) || max_window < 1) return -1;
+  // two band buffers (the banded pipeline double-buffers) plus the tables
   const int64_t band = fin->nseg_in * n_other_of(*pen) * max_window * 2 * (int64_t)fin->nbins;
-  return ((band + 15) / 16) * 16 + table_floats(*pen) + table_floats(*fin);
+  return 2 * (((band + 15) / 16) * 16) + table_floats(*pen) + table_floats(*fin);
 }

@@ -22,6 +22,29 @@ namespace loki {
 int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
 
+// Division by a runtime-constant 32-bit divisor d >= 1 with a precomputed
+// multiplier (Granlund & Montgomery 1994): q = (t + ((n - t) >> 1)) >> (l - 1),
+// t = umulhi(m, n), l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1.
+// Exact for every 32-bit n.
+struct FastDiv32 {
+  uint32_t d, m, s;  // s = l - 1 (unused when d == 1)
+
+  __host__ __device__ static FastDiv32 make(uint32_t dv) {
+    FastDiv32 f;
+    f.d = dv;
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < dv) ++l;
+    f.m = (uint32_t)((((1ull << l) - dv) << 32) / dv + 1);
+    f.s = l ? l - 1 : 0;
+    return f;
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    if (d == 1) return n;
+    const uint32_t t = __umulhi(m, n);
+    return (t + ((n - t) >> 1)) >> s;
+  }
+};
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

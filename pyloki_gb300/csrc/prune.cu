@@ -1,0 +1,889 @@
+// Enumerate-prune kernels for the Taylor basis with float32 folds
+// (prune.py:165-332 pruning_iteration_batched with the PrunePolyTaylorDPFuncts
+// plugin, dynamic/dyn_poly_taylor.py:396-690).
+//
+// One level = branch (per parent) -> exclusive scan of child counts -> score
+// (per child: branch value, FP64 resolve, gather + roll + add, boxcar S/N) ->
+// selection (in child order, with the exact overflow rule when needed) ->
+// emit (transform the survivors, write the new tree). Child order is parent
+// order then the C-order odometer over the branched parameters, which is the
+// order the reference appends survivors in.
+//
+// FP64 arithmetic follows the reference's numpy operations with round-to-
+// nearest intrinsics (no contraction); the batched Taylor shifts reproduce
+// the BLAS matrix product, which accumulates each output with forward fused
+// multiply-adds (acc = fma(x_j, T_ij, acc), j = 0..P).
+#include <algorithm>
+
+#include "loki_common.cuh"
+#include "score.cuh"
+
+namespace loki {
+
+int score_smem_bytes(int nbins, int wmax, int warps);
+
+// ---------------------------------------------------------------------------
+// exclusive scan of int64 (counts) or of score >= threshold flags
+// ---------------------------------------------------------------------------
+
+constexpr int kScanBlock = 1024;
+
+template <bool FLAGS>
+__device__ __forceinline__ int64_t scan_in(const void* in, int64_t i, int64_t n, double thr) {
+  if (i >= n) return 0;
+  if (FLAGS) return ((double)reinterpret_cast<const float*>(in)[i] >= thr) ? 1 : 0;
+  return reinterpret_cast<const int64_t*>(in)[i];
+}
+
+template <bool FLAGS>
+__global__ void __launch_bounds__(kScanBlock)
+scan_block_kernel(const void* in, int64_t n, double thr, int64_t* out, int64_t* sums) {
+  __shared__ int64_t warp_tot[32];
+  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t x = scan_in<FLAGS>(in, i, n, thr);
+  int64_t v = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) warp_tot[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_tot[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  const int64_t incl = v + (warp ? warp_tot[warp - 1] : 0);
+  if (i < n) out[i] = incl - x;  // exclusive within the block
+  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = incl;
+}
+
+// Single block: exclusive scan of the block sums (any count), carry-chained.
+__global__ void __launch_bounds__(kScanBlock)
+scan_sums_kernel(int64_t* sums, int64_t nblocks, int64_t* total) {
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nblocks; base += kScanBlock) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t x = i < nblocks ? sums[i] : 0;
+    int64_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_tot[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const int64_t incl = v + (warp ? warp_tot[warp - 1] : 0);
+    const int64_t c = carry;
+    if (i < nblocks) sums[i] = c + incl - x;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void scan_add_kernel(int64_t* out, int64_t n, const int64_t* sums) {
+  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+}
+
+// out[0..n) exclusive scan, out[n] = total.
+template <bool FLAGS>
+static int exclusive_scan(const void* in, int64_t n, double thr, int64_t* out, void* scratch,
+                          int64_t scratch_bytes, cudaStream_t s) {
+  const int64_t nblocks = std::max<int64_t>(1, (n + kScanBlock - 1) / kScanBlock);
+  if (scratch_bytes < nblocks * (int64_t)sizeof(int64_t))
+    return set_error(LOKI_ERR_CAPACITY, "scan scratch too small");
+  int64_t* sums = reinterpret_cast<int64_t*>(scratch);
+  if (n == 0) {
+    if (cudaMemsetAsync(out, 0, sizeof(int64_t), s) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
+    return LOKI_OK;
+  }
+  scan_block_kernel<FLAGS><<<(unsigned)nblocks, kScanBlock, 0, s>>>(in, n, thr, out, sums);
+  scan_sums_kernel<<<1, kScanBlock, 0, s>>>(sums, nblocks, out + n);
+  scan_add_kernel<<<(unsigned)nblocks, kScanBlock, 0, s>>>(out, n, sums);
+  return check_launch("exclusive_scan");
+}
+
+// ---------------------------------------------------------------------------
+// shared FP64 pieces
+// ---------------------------------------------------------------------------
+
+// y_i = sum_j x_j T_ij accumulated with forward fused multiply-adds.
+__device__ __forceinline__ double tdot(const double* x, const double (*T)[LOKI_MAX_PARAMS + 1],
+                                       int i, int m) {
+  double acc = 0.0;
+  for (int j = 0; j < m; ++j) acc = __fma_rn(x[j], T[i][j], acc);
+  return acc;
+}
+
+// get_nearest_indices_2d_batch for one axis (utils/psr_utils.py:517-554).
+__device__ __forceinline__ int64_t axis_index(double v, double vmin, double inv, int64_t n) {
+  if (!(inv > 0.0)) return 0;
+  const double raw = __dmul_rn(__dsub_rn(v, vmin), inv);
+  int64_t idx = (int64_t)__dadd_rn(raw, LOKI_FLOAT_EPSILON);
+  if (idx < 0) idx = 0;
+  else if (idx >= n) idx = n - 1;
+  return idx;
+}
+
+// Child leaf parameters [d_P .. d_1] from the parent's branching info.
+__device__ __forceinline__ void child_params(const LokiBranchInfo& B, int P, int64_t local,
+                                             double* pv) {
+  for (int j = P - 1; j >= 0; --j) {
+    const int64_t c = B.count[j];
+    const int64_t k = local % c;
+    local /= c;
+    pv[j] = (c == 1 && k == 0) ? B.first[j]
+                               : __dadd_rn(B.first[j], __dmul_rn((double)k, B.dact[j]));
+  }
+}
+
+struct ChildRes {
+  int32_t ia, iff;  // (accel, freq) FFA grid indices
+  double phase;
+};
+
+// poly_taylor_resolve_batch (moving) / poly_taylor_fixed_resolve_batch
+// (core/taylor.py:172-277) for one child with params pv[0..P] (d_P..d_1, d_0).
+__device__ __forceinline__ ChildRes resolve_child(const LokiPruneLevel& D, const double* pv,
+                                                  double f0) {
+  const int P = D.poly_order, m = P + 1;
+  double accel, vel, dd;
+  if (D.moving) {
+    accel = tdot(pv, D.tm_a, P - 2, m);
+    vel = __dsub_rn(tdot(pv, D.tm_a, P - 1, m), tdot(pv, D.tm_i, P - 1, m));
+    dd = __dsub_rn(tdot(pv, D.tm_a, P, m), tdot(pv, D.tm_i, P, m));
+  } else {
+    accel = tdot(pv, D.tm_a, P - 2, m);
+    vel = tdot(pv, D.tm_a, P - 1, m);
+    dd = tdot(pv, D.tm_a, P, m);
+  }
+  const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(vel, LOKI_C_VAL)));
+  const double delay = __ddiv_rn(dd, LOKI_C_VAL);
+  ChildRes r;
+  r.phase = phase_idx(D.dt_phase, f0, D.nbins, delay);
+  r.ia = (int32_t)axis_index(accel, D.accel_min, D.accel_inv, D.n_accel);
+  r.iff = (int32_t)axis_index(freq, D.freq_min, D.freq_inv, D.n_freq);
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// branch
+// ---------------------------------------------------------------------------
+
+__global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                                    int64_t n, LokiBranchInfo* __restrict__ info,
+                                    int64_t* __restrict__ counts, int32_t* __restrict__ err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int P = D.poly_order;
+  const double* lf = leaves + i * (P + 2) * 2;
+  const double f0 = lf[(P + 1) * 2];
+  const double fscale = __ddiv_rn(f0, LOKI_C_VAL);
+  LokiBranchInfo B;
+  int64_t total = 1;
+  for (int j = 0; j < P; ++j) {
+    const double pcur = lf[2 * j], dcur = lf[2 * j + 1];
+    const double dnew = __ddiv_rn(D.dfc[j], f0);
+    const double fb = __dmul_rn(D.fac[j], fscale);
+    const double shift = __dmul_rn(fabs(__dsub_rn(dcur, dnew)), fb);
+    int64_t num = 1;
+    double dact = dcur, first = pcur;
+    if (!(dcur > 0.0) || !(dnew > 0.0)) {
+      atomicOr(err, LOKI_DEVERR_BRANCH);
+    } else {
+      const double ratio = __ddiv_rn(dcur, dnew);
+      num = (int64_t)ceil(__dsub_rn(ratio, LOKI_FLOAT_EPSILON));
+      if (num < 1) num = 1;
+      if (num > D.branch_max) {
+        atomicOr(err, LOKI_DEVERR_BRANCH);
+        num = D.branch_max;
+      }
+      dact = __ddiv_rn(dcur, (double)num);
+      const double pmin = __dsub_rn(pcur, __ddiv_rn(dcur, 2.0));
+      first = __dadd_rn(pmin, __ddiv_rn(dact, 2.0));
+    }
+    if (shift < D.eta_m) {
+      num = 1;
+      dact = dcur;
+      first = pcur;
+    }
+    B.first[j] = first;
+    B.dact[j] = dact;
+    B.count[j] = (int32_t)num;
+    total *= num;
+  }
+  info[i] = B;
+  counts[i] = total;
+}
+
+// ---------------------------------------------------------------------------
+// score: warp per 32 children
+// ---------------------------------------------------------------------------
+
+constexpr int kPruneWarps = 4;
+
+__device__ __forceinline__ int64_t find_parent(const int64_t* offsets, int64_t n, int64_t c) {
+  int64_t lo = 0, hi = n;  // offsets[lo] <= c < offsets[hi]
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (offsets[mid] <= c) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ unsigned float_key(float x) {
+  const unsigned u = __float_as_uint(x);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float key_float(unsigned k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                   const float* __restrict__ folds, int64_t n_parents,
+                   const LokiBranchInfo* __restrict__ info, const int64_t* __restrict__ offsets,
+                   int64_t n_children, const float* __restrict__ seg, LokiScoreSpec sp,
+                   ScoreK SK, float* __restrict__ scores, int32_t* __restrict__ cidx,
+                   double* __restrict__ cphase, unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float tiles[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, P = D.poly_order;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tile = tiles + (size_t)warp * 32 * stride;
+  const int64_t c0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+  if (c0 >= n_children) return;
+  const int kmax = (int)std::min<int64_t>(32, n_children - c0);
+  // lane k resolves child c0 + k
+  int64_t my_par = 0, my_row = 0;
+  int my_shift = 0;
+  if (lane < kmax) {
+    const int64_t c = c0 + lane;
+    const int64_t par = find_parent(offsets, n_parents, c);
+    const LokiBranchInfo B = info[par];
+    const double* lf = leaves + par * (P + 2) * 2;
+    double pv[LOKI_MAX_PARAMS + 1];
+    child_params(B, P, c - offsets[par], pv);
+    pv[P] = lf[P * 2];  // d_0
+    const ChildRes r = resolve_child(D, pv, lf[(P + 1) * 2]);
+    cidx[2 * c] = r.ia;
+    cidx[2 * c + 1] = r.iff;
+    cphase[c] = r.phase;
+    my_par = par;
+    my_row = (int64_t)r.ia * D.n_freq + r.iff;
+    my_shift = round_shift(r.phase, nb);
+  }
+  for (int k = 0; k < kmax; ++k) {
+    const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
+    const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+    const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+    const float* pf = folds + par * 2 * nb;
+    const float* sf = seg + row * 2 * nb;
+    float* trow = tile + k * stride;
+    for (int j = lane; j < nb; j += 32) {
+      int js = j - sh;
+      js += (js < 0) ? nb : 0;
+      const float e = __fadd_rn(pf[j], sf[js]);
+      const float v = __fadd_rn(pf[nb + j], sf[nb + js]);
+      trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
+    }
+  }
+  __syncwarp();
+  if (lane < kmax) {
+    float* row = tile + lane * stride;
+    float s;
+    if (SK.pow2_64) score_row64_pow2(row, sp, SK, &s);
+    else score_row(row, nb, sp, &s);
+    scores[c0 + lane] = s;
+    if (s == s) {  // NaN scores do not enter min/max (like np.min on finite data)
+      atomicMin(minmax_keys, float_key(s));
+      atomicMax(minmax_keys + 1, float_key(s));
+    }
+  }
+}
+
+__global__ void minmax_init_kernel(unsigned* keys) {
+  keys[0] = 0xFFFFFFFFu;
+  keys[1] = 0u;
+}
+
+__global__ void minmax_finish_kernel(const unsigned* keys, float* out) {
+  if (keys[0] == 0xFFFFFFFFu) {  // no finite score
+    out[0] = 0.0f;
+    out[1] = 0.0f;
+  } else {
+    out[0] = key_float(keys[0]);
+    out[1] = key_float(keys[1]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// selection without overflow
+// ---------------------------------------------------------------------------
+
+__global__ void select_scatter_kernel(const float* __restrict__ scores, int64_t n, double thr,
+                                      const int64_t* __restrict__ pos, int64_t* __restrict__ ids) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n && (double)scores[i] >= thr) ids[pos[i]] = i;
+}
+
+// ---------------------------------------------------------------------------
+// selection with the overflow rule (single block, sequential over batches)
+// ---------------------------------------------------------------------------
+
+constexpr int kSelThreads = 1024;
+
+// Block-wide exclusive scan of one flag per thread; returns the offset of this
+// thread and writes the block total.
+__device__ __forceinline__ int block_scan_flag(int f, int* total, int* wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned b = __ballot_sync(0xFFFFFFFFu, f);
+  const int before = __popc(b & lanemask_lt());
+  if (lane == 0) wsum[warp] = __popc(b);
+  __syncthreads();
+  if (warp == 0) {
+    int w = wsum[lane];
+    int v = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+      if (lane >= o) v += y;
+    }
+    wsum[lane] = v - w;  // exclusive
+    if (lane == 31) wsum[32] = v;
+  }
+  __syncthreads();
+  const int off = wsum[warp] + before;
+  *total = wsum[32];
+  __syncthreads();
+  return off;
+}
+
+// Value of ascending rank r among keys[0..n) (radix select, 4 x 8 bits).
+__device__ unsigned block_select(const unsigned* keys, int64_t n, int64_t r, unsigned* hist) {
+  unsigned prefix = 0, mask = 0;
+  for (int shift = 24; shift >= 0; shift -= 8) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const unsigned k = keys[i];
+      if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 0xFF], 1u);
+    }
+    __syncthreads();
+    __shared__ unsigned sel_digit;
+    __shared__ long long sel_r;
+    if (threadIdx.x == 0) {
+      long long acc = 0;
+      int d = 0;
+      for (; d < 256; ++d) {
+        if (acc + hist[d] > r) break;
+        acc += hist[d];
+      }
+      sel_digit = (unsigned)(d < 256 ? d : 255);
+      sel_r = r - acc;
+    }
+    __syncthreads();
+    prefix |= sel_digit << shift;
+    mask |= 0xFFu << shift;
+    r = sel_r;
+    __syncthreads();
+  }
+  return prefix;
+}
+
+__global__ void __launch_bounds__(kSelThreads)
+select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restrict__ offsets,
+                       int64_t n_parents, int64_t batch, double thr, int64_t cap,
+                       int64_t* __restrict__ ids, int64_t* __restrict__ n_out,
+                       double* __restrict__ thr_out, int64_t* __restrict__ tmp_ids,
+                       unsigned* __restrict__ keys) {
+  __shared__ int wsum[33];
+  __shared__ unsigned hist[256];
+  __shared__ long long vs_sh;
+  __shared__ double cur_sh;
+  if (threadIdx.x == 0) {
+    vs_sh = 0;
+    cur_sh = thr;
+  }
+  __syncthreads();
+  for (int64_t p0 = 0; p0 < n_parents; p0 += batch) {
+    const int64_t p1 = std::min(p0 + batch, n_parents);
+    const int64_t c_lo = offsets[p0], c_hi = offsets[p1];
+    if (c_hi == c_lo) continue;
+    const double eff_in = fmax(thr, cur_sh);
+    // pass 1: count passing children of the batch
+    int64_t m = 0;
+    for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+      const int64_t c = base + threadIdx.x;
+      const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
+      int tot;
+      block_scan_flag(f, &tot, wsum);
+      m += tot;
+    }
+    int64_t vs = vs_sh;
+    if (m <= cap - vs) {  // fast path: append in order
+      int64_t w = vs;
+      for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+        const int64_t c = base + threadIdx.x;
+        const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
+        int tot;
+        const int off = block_scan_flag(f, &tot, wsum);
+        if (f) ids[w + off] = c;
+        w += tot;
+      }
+      if (threadIdx.x == 0) vs_sh = vs + m;
+      __syncthreads();
+      continue;
+    }
+    // prune_on_overload: keys of the current tree and of the passing batch
+    int64_t w = vs;
+    for (int64_t i = threadIdx.x; i < vs; i += kSelThreads) keys[i] = float_key(scores[ids[i]]);
+    for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+      const int64_t c = base + threadIdx.x;
+      const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
+      int tot;
+      const int off = block_scan_flag(f, &tot, wsum);
+      if (f) {
+        keys[w + off] = float_key(scores[c]);
+        tmp_ids[w - vs + off] = c;
+      }
+      w += tot;
+    }
+    __syncthreads();
+    const int64_t total = vs + m;
+    const unsigned kth = block_select(keys, total, total - cap, hist);
+    const unsigned mid = block_select(keys, total, total - total / 2 - 1, hist);
+    double eff = cur_sh;
+    const double tk = nextafter((double)key_float(kth), INFINITY);
+    const double tm = nextafter((double)key_float(mid), INFINITY);
+    eff = fmax(eff, fmax(tk, tm));
+    // keep tree entries >= eff (stable)
+    int64_t kept = 0;
+    for (int64_t base = 0; base < vs; base += kSelThreads) {
+      const int64_t i = base + threadIdx.x;
+      int64_t id = 0;
+      int f = 0;
+      if (i < vs) {
+        id = ids[i];
+        f = (double)scores[id] >= eff ? 1 : 0;
+      }
+      int tot;
+      const int off = block_scan_flag(f, &tot, wsum);
+      if (f) keys[kept + off] = (unsigned)(id & 0xFFFFFFFFu), tmp_ids[m + kept + off] = id;
+      kept += tot;
+    }
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < kept; i += kSelThreads) ids[i] = tmp_ids[m + i];
+    __syncthreads();
+    // pending batch entries >= eff, in order, up to the free space
+    const int64_t space = cap - kept;
+    int64_t added = 0;
+    for (int64_t base = 0; base < m; base += kSelThreads) {
+      const int64_t i = base + threadIdx.x;
+      int64_t id = 0;
+      int f = 0;
+      if (i < m) {
+        id = tmp_ids[i];
+        f = (double)scores[id] >= eff ? 1 : 0;
+      }
+      int tot;
+      const int off = block_scan_flag(f, &tot, wsum);
+      if (f && added + off < space) ids[kept + added + off] = id;
+      added += tot;
+    }
+    if (threadIdx.x == 0) {
+      vs_sh = kept + std::min(added, space);
+      cur_sh = eff;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *n_out = vs_sh;
+    *thr_out = cur_sh;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// emit: thread per survivor for the leaf, warp per 32 survivors for folds
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                  const float* __restrict__ folds, const LokiBranchInfo* __restrict__ info,
+                  const int64_t* __restrict__ offsets, int64_t n_parents,
+                  const float* __restrict__ seg, const int64_t* __restrict__ surv,
+                  int64_t n_surv, const float* __restrict__ cscores,
+                  const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
+                  double* __restrict__ lout, float* __restrict__ fout,
+                  float* __restrict__ sout, float* __restrict__ seout,
+                  int32_t* __restrict__ bout) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, P = D.poly_order, m = P + 1;
+  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+  if (s0 >= n_surv) return;
+  const int kmax = (int)std::min<int64_t>(32, n_surv - s0);
+  int64_t my_par = 0, my_row = 0;
+  int my_shift = 0;
+  if (lane < kmax) {
+    const int64_t s = s0 + lane;
+    const int64_t c = surv[s];
+    const int64_t par = find_parent(offsets, n_parents, c);
+    const LokiBranchInfo B = info[par];
+    const double* lf = leaves + par * (P + 2) * 2;
+    double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
+    child_params(B, P, c - offsets[par], pv);
+    pv[P] = lf[P * 2];
+    for (int j = 0; j < P; ++j) ev[j] = B.dact[j];
+    ev[P] = 0.0;
+    double* lo = lout + s * (P + 2) * 2;
+    if (D.moving) {
+      for (int i = 0; i < m; ++i) lo[2 * i] = tdot(pv, D.tm_n, i, m);
+      if (D.tiling == 0) {
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dmul_rn(ev[i], fabs(D.tm_n[i][i]));
+      } else if (D.tiling == 2) {
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = tdot(ev, D.tm_e, i, m);
+      } else {
+        double e2[LOKI_MAX_PARAMS + 1];
+        for (int j = 0; j < m; ++j) e2[j] = __dmul_rn(ev[j], ev[j]);
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dsqrt_rn(tdot(e2, D.tm_e, i, m));
+      }
+    } else {
+      for (int i = 0; i < m; ++i) {
+        lo[2 * i] = pv[i];
+        lo[2 * i + 1] = ev[i];
+      }
+    }
+    lo[2 * m] = lf[2 * m];          // f0
+    lo[2 * m + 1] = lf[2 * m + 1];  // basis flag
+    const float sc = cscores[c];
+    sout[s] = sc;
+    seout[s] = sc;
+    int32_t* bt = bout + s * (P + 2);
+    const int ia = cidx[2 * c], iff = cidx[2 * c + 1];
+    bt[0] = (int32_t)par;
+    for (int j = 1; j < P + 1; ++j) bt[j] = 0;
+    bt[D.nparams_ffa - 1] = ia;  // column 1 + (nparams_ffa - 2)
+    bt[D.nparams_ffa] = iff;     // column 1 + (nparams_ffa - 1)
+    bt[P + 1] = (int32_t)cphase[c];
+    my_par = par;
+    my_row = (int64_t)ia * D.n_freq + iff;
+    my_shift = round_shift(cphase[c], nb);
+  }
+  for (int k = 0; k < kmax; ++k) {
+    const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
+    const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+    const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+    const float* pf = folds + par * 2 * nb;
+    const float* sf = seg + row * 2 * nb;
+    float* o = fout + (s0 + k) * 2 * nb;
+    for (int j = lane; j < nb; j += 32) {
+      int js = j - sh;
+      js += (js < 0) ? nb : 0;
+      o[j] = __fadd_rn(pf[j], sf[js]);
+      o[nb + j] = __fadd_rn(pf[nb + j], sf[nb + js]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// ascend: warp per 32 survivors, segments accumulated in order
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                    float* __restrict__ folds, float* __restrict__ scores,
+                    float* __restrict__ scores_ep, int64_t n, int nseg,
+                    const double* __restrict__ tm_seg, const double* __restrict__ dt_seg,
+                    const int32_t* __restrict__ seg_idx, const float* __restrict__ ffa,
+                    int64_t seg_stride, LokiScoreSpec sp, ScoreK SK) {
+  extern __shared__ float tiles[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, P = D.poly_order, m = P + 1;
+  // per warp: the 32 accumulators (2 * nb each) followed by the score tile
+  const int stride = score_stride(nb, sp.wmax);
+  float* acc = tiles + (size_t)warp * 32 * (2 * nb + stride);
+  float* tile = acc + 32 * 2 * nb;
+  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+  if (s0 >= n) return;
+  const int kmax = (int)std::min<int64_t>(32, n - s0);
+  for (int k = 0; k < kmax; ++k)
+    for (int j = lane; j < 2 * nb; j += 32) acc[k * 2 * nb + j] = 0.0f;
+  double pv[LOKI_MAX_PARAMS + 1];
+  double f0 = 1.0;
+  if (lane < kmax) {
+    const double* lf = leaves + (s0 + lane) * (P + 2) * 2;
+    for (int i = 0; i < m; ++i) pv[i] = lf[2 * i];
+    f0 = lf[2 * m];
+  }
+  __syncwarp();
+  for (int sg = 0; sg < nseg; ++sg) {
+    const double(*T)[LOKI_MAX_PARAMS + 1] =
+        reinterpret_cast<const double(*)[LOKI_MAX_PARAMS + 1]>(tm_seg + sg * 36);
+    int64_t my_row = 0;
+    int my_shift = 0;
+    if (lane < kmax) {
+      const double accel = tdot(pv, T, P - 2, m);
+      const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(tdot(pv, T, P - 1, m),
+                                                               LOKI_C_VAL)));
+      const double delay = __ddiv_rn(tdot(pv, T, P, m), LOKI_C_VAL);
+      const double ph = phase_idx(dt_seg[sg], f0, nb, delay);
+      const int64_t ia = axis_index(accel, D.accel_min, D.accel_inv, D.n_accel);
+      const int64_t iff = axis_index(freq, D.freq_min, D.freq_inv, D.n_freq);
+      my_row = ia * D.n_freq + iff;
+      my_shift = round_shift(ph, nb);
+    }
+    const float* fseg = ffa + (int64_t)seg_idx[sg] * seg_stride;
+    for (int k = 0; k < kmax; ++k) {
+      const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+      const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+      const float* sf = fseg + row * 2 * nb;
+      float* a = acc + k * 2 * nb;
+      for (int j = lane; j < nb; j += 32) {
+        int js = j - sh;
+        js += (js < 0) ? nb : 0;
+        a[j] = __fadd_rn(a[j], sf[js]);
+        a[nb + j] = __fadd_rn(a[nb + j], sf[nb + js]);
+      }
+    }
+  }
+  __syncwarp();
+  for (int k = 0; k < kmax; ++k) {
+    const float* a = acc + k * 2 * nb;
+    float* o = folds + (s0 + k) * 2 * nb;
+    float* trow = tile + k * stride;
+    for (int j = lane; j < nb; j += 32) {
+      o[j] = a[j];
+      o[nb + j] = a[nb + j];
+      trow[j] = __fdiv_rn(a[j], __fsqrt_rn(a[nb + j]));
+    }
+  }
+  __syncwarp();
+  if (lane < kmax) {
+    scores_ep[s0 + lane] = scores[s0 + lane];
+    float s;
+    float* row = tile + lane * stride;
+    if (SK.pow2_64) score_row64_pow2(row, sp, SK, &s);
+    else score_row(row, nb, sp, &s);
+    scores[s0 + lane] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+static int check_prune(const LokiPruneLevel* D) {
+  if (!D) return set_error(LOKI_ERR_INVALID, "null prune level descriptor");
+  if (D->poly_order < 2 || D->poly_order > LOKI_MAX_PARAMS)
+    return set_error(LOKI_ERR_INVALID, "poly_order %d outside [2, %d]", D->poly_order,
+                     LOKI_MAX_PARAMS);
+  if (D->nbins < 2) return set_error(LOKI_ERR_INVALID, "nbins < 2");
+  if (D->nparams_ffa < 2 || D->nparams_ffa > D->poly_order)
+    return set_error(LOKI_ERR_INVALID, "nparams_ffa %d outside [2, poly_order]",
+                     D->nparams_ffa);
+  if (D->n_accel < 1 || D->n_freq < 1) return set_error(LOKI_ERR_INVALID, "empty FFA grid");
+  if (D->tiling < 0 || D->tiling > 2) return set_error(LOKI_ERR_INVALID, "bad tiling");
+  return LOKI_OK;
+}
+
+static int prune_spec_check(const LokiScoreSpec* sp, int nbins) {
+  if (!sp || sp->nwidths < 1 || sp->nwidths > LOKI_MAX_WIDTHS)
+    return set_error(LOKI_ERR_INVALID, "bad score spec");
+  if (nbins + sp->wmax > 1024)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax above 1024 for pruning");
+  return LOKI_OK;
+}
+
+}  // namespace loki
+
+using namespace loki;
+
+extern "C" int64_t loki_scan_scratch_bytes(int64_t n) {
+  return std::max<int64_t>(1, (n + kScanBlock - 1) / kScanBlock) * (int64_t)sizeof(int64_t);
+}
+
+extern "C" int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves,
+                                 int64_t n_parents, LokiBranchInfo* info, int64_t* offsets,
+                                 void* scan_scratch, int64_t scan_scratch_bytes,
+                                 int32_t* dev_err, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  if (n_parents < 0) return set_error(LOKI_ERR_INVALID, "n_parents < 0");
+  if (!offsets || !dev_err || (n_parents && (!leaves || !info)))
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n_parents > 0) {
+    // child counts go to offsets[0..n), scanned in place
+    prune_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
+        *lvl, leaves, n_parents, info, offsets, dev_err);
+    rc = check_launch("prune_branch");
+    if (rc) return rc;
+  }
+  return exclusive_scan<false>(offsets, n_parents, 0.0, offsets, scan_scratch,
+                               scan_scratch_bytes, s);
+}
+
+extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
+                                const float* folds, int64_t n_parents,
+                                const LokiBranchInfo* info, const int64_t* offsets,
+                                int64_t n_children, const float* fold_segment,
+                                const LokiScoreSpec* spec, float* child_scores,
+                                int32_t* child_idx, double* child_phase, float* score_minmax,
+                                int32_t* dev_err, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (!score_minmax || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned* keys = reinterpret_cast<unsigned*>(score_minmax);  // reused as ordered keys
+  minmax_init_kernel<<<1, 1, 0, s>>>(keys);
+  if (n_children > 0) {
+    if (!leaves || !folds || !info || !offsets || !fold_segment || !child_scores ||
+        !child_idx || !child_phase)
+      return set_error(LOKI_ERR_INVALID, "null pointer argument");
+    LokiScoreSpec sp = *spec;
+    sp.mode = 1;
+    const ScoreK SK = make_score_k(sp, lvl->nbins);
+    const int smem = score_smem_bytes(lvl->nbins, sp.wmax, kPruneWarps);
+    if (smem > 200 * 1024)
+      return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(prune_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+    const int64_t blocks = (n_children + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    prune_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
+        *lvl, leaves, folds, n_parents, info, offsets, n_children, fold_segment, sp, SK,
+        child_scores, child_idx, child_phase, keys);
+  }
+  minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
+  return check_launch("prune_score");
+}
+
+extern "C" int loki_prune_select(const float* child_scores, int64_t n_children,
+                                 double threshold, int64_t* surv_ids, int64_t* n_surv,
+                                 void* scan_scratch, int64_t scan_scratch_bytes, void* stream) {
+  if (n_children < 0 || !n_surv) return set_error(LOKI_ERR_INVALID, "bad select arguments");
+  if (n_children > 0 && (!child_scores || !surv_ids))
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  // positions are scanned into surv_ids' tail-free temp: reuse surv_ids is not
+  // possible (scatter reads positions), so positions live in the scratch
+  // after the block sums.
+  const int64_t sums_bytes = loki_scan_scratch_bytes(n_children);
+  const int64_t need = sums_bytes + (n_children + 1) * (int64_t)sizeof(int64_t);
+  if (scan_scratch_bytes < need)
+    return set_error(LOKI_ERR_CAPACITY, "select scratch needs %lld bytes", (long long)need);
+  int64_t* pos = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(scan_scratch) + sums_bytes);
+  int rc = exclusive_scan<true>(child_scores, n_children, threshold, pos, scan_scratch,
+                                sums_bytes, s);
+  if (rc) return rc;
+  if (n_children > 0)
+    select_scatter_kernel<<<(unsigned)((n_children + 255) / 256), 256, 0, s>>>(
+        child_scores, n_children, threshold, pos, surv_ids);
+  if (cudaMemcpyAsync(n_surv, pos + n_children, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) !=
+      cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaMemcpyAsync failed");
+  return check_launch("prune_select");
+}
+
+extern "C" int loki_prune_select_overflow(const float* child_scores, const int64_t* offsets,
+                                          int64_t n_parents, int64_t batch_size,
+                                          double threshold, int64_t capacity,
+                                          int64_t* surv_ids, int64_t* n_surv, double* thr_out,
+                                          int64_t* scratch_ids, float* scratch_keys,
+                                          int64_t scratch_len, void* stream) {
+  if (batch_size < 1 || capacity < 1 || n_parents < 0)
+    return set_error(LOKI_ERR_INVALID, "bad overflow selection arguments");
+  if (!child_scores || !offsets || !surv_ids || !n_surv || !thr_out || !scratch_ids ||
+      !scratch_keys)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  select_overflow_kernel<<<1, kSelThreads, 0, (cudaStream_t)stream>>>(
+      child_scores, offsets, n_parents, batch_size, threshold, capacity, surv_ids, n_surv,
+      thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys));
+  (void)scratch_len;
+  return check_launch("prune_select_overflow");
+}
+
+extern "C" int loki_prune_emit(const LokiPruneLevel* lvl, const double* leaves,
+                               const float* folds, const LokiBranchInfo* info,
+                               const int64_t* offsets, int64_t n_parents,
+                               const float* fold_segment, const int64_t* surv_ids,
+                               int64_t n_surv, const float* child_scores,
+                               const int32_t* child_idx, const double* child_phase,
+                               double* leaves_out, float* folds_out, float* scores_out,
+                               float* scores_ep_out, int32_t* bt_out, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  if (n_surv <= 0) return LOKI_OK;
+  if (!leaves || !folds || !info || !offsets || !fold_segment || !surv_ids || !child_scores ||
+      !child_idx || !child_phase || !leaves_out || !folds_out || !scores_out ||
+      !scores_ep_out || !bt_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  const int64_t blocks = (n_surv + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  prune_emit_kernel<<<(unsigned)blocks, kPruneWarps * 32, 0, (cudaStream_t)stream>>>(
+      *lvl, leaves, folds, info, offsets, n_parents, fold_segment, surv_ids, n_surv,
+      child_scores, child_idx, child_phase, leaves_out, folds_out, scores_out, scores_ep_out,
+      bt_out);
+  return check_launch("prune_emit");
+}
+
+extern "C" int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves, float* folds,
+                                 float* scores, float* scores_ep, int64_t n, int32_t nseg,
+                                 const double* tm_seg, const double* dt_seg,
+                                 const int32_t* seg_idx, const float* ffa_fold,
+                                 int64_t seg_stride, const LokiScoreSpec* spec,
+                                 int32_t* dev_err, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (n <= 0) return LOKI_OK;
+  if (nseg < 1 || !leaves || !folds || !scores || !scores_ep || !tm_seg || !dt_seg ||
+      !seg_idx || !ffa_fold || !dev_err)
+    return set_error(LOKI_ERR_INVALID, "bad ascend arguments");
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, lvl->nbins);
+  const int nb = lvl->nbins;
+  const int smem = kPruneWarps * 32 * (2 * nb + score_stride(nb, sp.wmax)) * (int)sizeof(float);
+  if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for ascend");
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(prune_ascend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  const int64_t blocks = (n + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  prune_ascend_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, (cudaStream_t)stream>>>(
+      *lvl, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa_fold,
+      seg_stride, sp, SK);
+  return check_launch("prune_ascend");
+}

@@ -28,7 +28,29 @@ struct LevelK {
   double tmat[2][LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1];  // RN(dt^(i-j) / (i-j)!)
   double scale_last;  // counts_prev[n-1] / (vmax - vmin), for the estimate only
   float B_hi, B_lo;   // fmin * scale_last - 1e-6 as a two-float
+  FastDiv32 wdiv;     // division by out_width (valid when use_fd)
+  int use_fd;         // all output indices fit in 32 bits
 };
+
+// Output parameter q of the windowed grid -> (other index, offset in window).
+__host__ __device__ inline void set_out_width(LevelK& K, const LokiFFALevel& L) {
+  int64_t q = L.out_width;
+  for (int d = 0; d < L.nparams - 1; ++d) q *= L.counts_cur[d];
+  K.use_fd = (q < (1ll << 32) && L.out_width < (1ll << 32)) ? 1 : 0;
+  K.wdiv = FastDiv32::make(K.use_fd ? (uint32_t)L.out_width : 1u);
+}
+
+__device__ __forceinline__ void q_split(const LokiFFALevel& L, const LevelK& K, int64_t q,
+                                        int64_t& other, int64_t& off) {
+  if (K.use_fd) {
+    const uint32_t o = K.wdiv.div((uint32_t)q);
+    other = o;
+    off = (int64_t)((uint32_t)q - o * (uint32_t)L.out_width);
+  } else {
+    other = q / L.out_width;
+    off = q - other * L.out_width;
+  }
+}
 
 struct OtherRes {
   double om;       // f multiplier: RN(1 - RN(v'/c)); exactly 1 for one parameter
@@ -73,6 +95,7 @@ inline LevelK make_level_k(const LokiFFALevel& L) {
   const double B = vmin * K.scale_last - LOKI_FLOAT_EPSILON;
   K.B_hi = (float)B;
   K.B_lo = (float)(B - (double)K.B_hi);
+  set_out_width(K, L);
   return K;
 }
 
@@ -119,6 +142,21 @@ __device__ inline OtherRes make_other(const LokiFFALevel& L, const LevelK& K, in
   return o;
 }
 
+// Exact FP64 chains, out of line so they only run when the estimate is
+// inconclusive (the compiler must not evaluate them speculatively).
+static __device__ __noinline__ int64_t trial_index_exact(double f, double om, int64_t n_grid,
+                                                  double vmin, double vmax) {
+  return nearest_index(__dmul_rn(f, om), n_grid, vmin, vmax);
+}
+
+static __device__ __noinline__ int trial_shift_exact(double g, double f, int nbins) {
+  const double x = __dmul_rn(g, f);
+  const double ph = __dsub_rn(x, floor(x));
+  double ip = __dmul_rn(ph, (double)nbins);
+  if (ip >= (double)nbins) ip = 0.0;
+  return round_shift(ip, nbins);
+}
+
 // Previous-level index of the frequency coordinate. Returns it exactly.
 __device__ __forceinline__ int64_t trial_index(const OtherRes& o, double f, float f_hi,
                                                float f_lo, const LokiFFALevel& L,
@@ -145,8 +183,7 @@ __device__ __forceinline__ int64_t trial_index(const OtherRes& o, double f, floa
     else if (idx >= n_grid) idx = n_grid - 1;
     return idx;
   }
-  const double fn = __dmul_rn(f, o.om);
-  return nearest_index(fn, n_grid, L.limits[n - 1][0], L.limits[n - 1][1]);
+  return trial_index_exact(f, o.om, n_grid, L.limits[n - 1][0], L.limits[n - 1][1]);
 }
 
 // Rounded relative shift in bins. Returns it exactly.
@@ -165,11 +202,7 @@ __device__ __forceinline__ int trial_shift(const OtherRes& o, double f, float f_
     int s = (int)k;
     return s >= nbins ? s - nbins : s;
   }
-  const double x = __dmul_rn(o.g, f);
-  double ph = __dsub_rn(x, floor(x));
-  double ip = __dmul_rn(ph, (double)nbins);
-  if (ip >= (double)nbins) ip = 0.0;
-  return round_shift(ip, nbins);
+  return trial_shift_exact(o.g, f, nbins);
 }
 
 // The others spanned by a block's consecutive output parameters, tabulated in
@@ -207,9 +240,9 @@ struct TrialRes {
 
 __device__ __forceinline__ TrialRes resolve_trial(const LokiFFALevel& L, const LevelK& K,
                                                   const OtherRes& ot, const OtherRes& oh,
-                                                  int64_t q) {
+                                                  int64_t off) {
   const int n = L.nparams;
-  const int64_t last = L.out_start + q % L.out_width;
+  const int64_t last = L.out_start + off;
   const double f = L.param_arr[n - 1][last];
   float f_hi, f_lo;
   if (L.last_split) {

@@ -87,6 +87,12 @@ inline ScoreK make_score_k(const LokiScoreSpec& sp, int nbins) {
   return k;
 }
 
+// Exact FP64 chain; out of line so the compiler cannot evaluate it
+// speculatively on the (common) fast path.
+static __device__ __noinline__ float snr_exact(float d, float T, double hb, double b) {
+  return __double2float_rn(__dsub_rn(__dmul_rn(hb, (double)d), __dmul_rn(b, (double)T)));
+}
+
 __device__ __forceinline__ float snr_fast(float d, float T, float hbh, float hbl, float bh,
                                           float bl, double hb, double b) {
   const float p1 = hbh * d;
@@ -108,7 +114,7 @@ __device__ __forceinline__ float snr_fast(float d, float T, float hbh, float hbl
     const float margin = fmaxf(fabsf(p1), fabsf(p2)) * 9.094947e-13f;  // 2^-40
     if (fabsf(res) < half_ulp - margin) return r;
   }
-  return __double2float_rn(__dsub_rn(__dmul_rn(hb, (double)d), __dmul_rn(b, (double)T)));
+  return snr_exact(d, T, hb, b);
 }
 
 // Two IEEE round-to-nearest subtractions in one instruction (sm_100+ f32x2).
@@ -128,14 +134,40 @@ __device__ __forceinline__ float max3(float a, float b, float c) {
   return m;
 }
 
-template <int W>
-__device__ __forceinline__ float dmax64(const float (&P)[96]) {
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+  unsigned long long x;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "f"(a), "f"(b));
+  return x;
+}
+
+__device__ __forceinline__ void unpack2(unsigned long long x, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x));
+}
+
+// The prefix is held as 48 register pairs P2[k] = (P[2k], P[2k+1]); for even
+// widths both operands of the packed subtraction are register pairs already.
+template <int H>  // width W = 2H
+__device__ __forceinline__ float dmax64_even(const unsigned long long (&P2)[48]) {
   float m = -FLT_MAX;
 #pragma unroll
-  for (int i = 0; i < 64; i += 2) {
+  for (int k = 0; k < 32; ++k) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(P2[k + H]), "l"(P2[k]));
     float d0, d1;
-    sub2(P[i + W], P[i + W + 1], P[i], P[i + 1], d0, d1);
+    unpack2(d, d0, d1);
     m = max3(m, d0, d1);
+  }
+  return m;
+}
+
+__device__ __forceinline__ float dmax64_w1(const unsigned long long (&P2)[48]) {
+  float m = -FLT_MAX;
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    float a0, a1, b0, b1;
+    unpack2(P2[k], a0, a1);
+    unpack2(P2[k + 1], b0, b1);
+    m = max3(m, __fsub_rn(a1, a0), __fsub_rn(b0, a1));
   }
   return m;
 }
@@ -144,23 +176,29 @@ __device__ __forceinline__ float dmax64(const float (&P)[96]) {
 // indices (no shared-memory traffic after the row is read once).
 __device__ __forceinline__ void score_row64_pow2(const float* row, const LokiScoreSpec& sp,
                                                  const ScoreK& K, float* out) {
-  float P[96];
-  P[0] = row[0];
+  unsigned long long P2[48];
+  float s = row[0];
 #pragma unroll
-  for (int i = 1; i < 64; ++i) P[i] = __fadd_rn(P[i - 1], row[i]);
-  const float total = P[63];
+  for (int k = 0; k < 32; ++k) {
+    const float s0 = k == 0 ? s : __fadd_rn(s, row[2 * k]);
+    s = __fadd_rn(s0, row[2 * k + 1]);
+    P2[k] = pack2(s0, s);
+  }
+  const float total = s;
+  const unsigned long long tt = pack2(total, total);
 #pragma unroll
-  for (int j = 0; j < 32; ++j) P[64 + j] = __fadd_rn(P[j], total);
+  for (int k = 0; k < 16; ++k)  // circular extension: P[64 + j] = P[j] + total
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(P2[32 + k]) : "l"(P2[k]), "l"(tt));
   float best = -FLT_MAX;
   for (int iw = 0; iw < sp.nwidths; ++iw) {
     float dm;
     switch (iw) {
-      case 0: dm = dmax64<1>(P); break;
-      case 1: dm = dmax64<2>(P); break;
-      case 2: dm = dmax64<4>(P); break;
-      case 3: dm = dmax64<8>(P); break;
-      case 4: dm = dmax64<16>(P); break;
-      default: dm = dmax64<32>(P); break;
+      case 0: dm = dmax64_w1(P2); break;
+      case 1: dm = dmax64_even<1>(P2); break;
+      case 2: dm = dmax64_even<2>(P2); break;
+      case 3: dm = dmax64_even<4>(P2); break;
+      case 4: dm = dmax64_even<8>(P2); break;
+      default: dm = dmax64_even<16>(P2); break;
     }
     float s;
     if (K.inv_one) {

@@ -1,0 +1,632 @@
+"""Enumerate-prune search on the GPU (drop-in for pyloki's ``prune.py``).
+
+``Pruning`` keeps the reference's interface (``prune.py:347-782``): one
+``execute_iter`` per added segment runs the level on the device as
+
+    loki_prune_branch   -> child counts and offsets (one host sync: leaf count)
+    loki_prune_score    -> resolve + gather + shift-add + score of every leaf
+    loki_prune_select   -> survivors in leaf order (one host sync: survivor count)
+    loki_prune_select_overflow  (only when more than ``max_sugg`` survive)
+    loki_prune_emit     -> transformed survivors = the new tree
+
+and ``prune_dyp_tree`` runs one pass per reference segment. The per-level
+constants (Taylor shift matrices, grid-step factors) are computed here with
+the reference's numpy expressions (``core/taylor.py``, ``utils/psr_utils.py``,
+``utils/transforms.py``) so the kernels reproduce its arithmetic.
+
+Supported plugin: Taylor basis, time-domain folds (``PrunePolyTaylorDPFuncts``
+with ``use_fourier=False``), moving or fixed grid, all three tiling strategies.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from pyloki_gb300 import _lib
+from pyloki_gb300.config import C_VAL, FLOAT_EPSILON, fact, poly_taylor_step_f
+from pyloki_gb300.scheme import MiddleOutScheme, determine_ref_segs_pareto
+
+_TILING = {"aggressive": 0, "quadrature": 1, "conservative": 2}
+
+
+def taylor_matrix(delta_t: float, n: int) -> np.ndarray:
+    """Lower-triangular Taylor shift matrix (``utils/transforms.py:41-45``)."""
+    powers = np.tril(np.arange(n)[:, np.newaxis] - np.arange(n))
+    return delta_t**powers / fact(powers) * np.tril(np.ones_like(powers))
+
+
+def shift_factors(poly_order: int, tobs: float, nbins: int) -> np.ndarray:
+    """Bin-shift factors of poly_taylor_shift_d_vec (``utils/psr_utils.py:227-248``)."""
+    k = np.arange(poly_order - 1, -1, -1)
+    factors = (tobs - 0) ** (k + 1) * nbins / fact(k + 1)
+    return factors / 2**k
+
+
+def _set6(dst, m: np.ndarray) -> None:
+    n = m.shape[0]
+    for i in range(6):
+        for j in range(6):
+            dst[i][j] = float(m[i, j]) if i < n and j < n else 0.0
+
+
+@dataclasses.dataclass
+class PruneStats:
+    """Statistics of one pruning level (``io/cands.py:17-103``)."""
+
+    level: int
+    seg_idx: int
+    threshold: float
+    score_min: float = 0.0
+    score_max: float = 0.0
+    n_branches: int = 1
+    n_leaves: int = 1
+    n_leaves_phy: int = 1
+    n_leaves_surv: int = 1
+
+    @property
+    def lb_leaves(self) -> float:
+        return float(np.round(np.log2(self.n_leaves), 2)) if self.n_leaves else 0.0
+
+    @property
+    def branch_frac(self) -> float:
+        return 0.0 if self.n_branches == 0 else round(self.n_leaves_phy / self.n_branches, 2)
+
+    @property
+    def surv_frac(self) -> float:
+        return 0.0 if self.n_leaves_phy == 0 else round(self.n_leaves_surv / self.n_leaves_phy, 2)
+
+    def get_summary(self) -> str:
+        return (f"Prune level: {self.level:3d}, seg_idx: {self.seg_idx:3d}, "
+                f"leaves: {self.lb_leaves:5.2f}, branch_frac: {self.branch_frac:5.2f}, "
+                f"score thresh: {self.threshold:5.2f}, max: {self.score_max:5.2f}, "
+                f"min: {self.score_min:5.2f}, P(surv): {self.surv_frac:4.2f}\n")
+
+
+class WorldTree:
+    """Survivor buffer on the device (``utils/world_tree.py:24-178``)."""
+
+    def __init__(self, leaves: torch.Tensor, folds: torch.Tensor, scores: torch.Tensor,
+                 backtracks: torch.Tensor, scores_ep: torch.Tensor | None = None) -> None:
+        self.leaves = leaves
+        self.folds = folds
+        self.scores = scores
+        self.scores_ep = scores.clone() if scores_ep is None else scores_ep
+        self.backtracks = backtracks
+
+    @property
+    def valid_size(self) -> int:
+        return int(self.scores.shape[0])
+
+    @property
+    def size(self) -> int:
+        return self.valid_size
+
+    @property
+    def nparams(self) -> int:
+        return int(self.leaves.shape[1]) - 2
+
+    @property
+    def size_lb(self) -> float:
+        return float(np.log2(self.valid_size)) if self.valid_size else 0.0
+
+    @property
+    def score_max(self) -> float:
+        return float(self.scores.max().item()) if self.valid_size else 0.0
+
+    @property
+    def score_min(self) -> float:
+        return float(self.scores.min().item()) if self.valid_size else 0.0
+
+    def get_best_k(self, k: int) -> tuple[np.ndarray, np.ndarray]:
+        """Top-k leaves by score, descending (``world_tree.py:441-459``)."""
+        leaves_out = np.zeros((k, *self.leaves.shape[1:]), dtype=np.float64)
+        scores_out = np.zeros(k, dtype=np.float32)
+        k_take = min(k, self.valid_size)
+        if k_take == 0:
+            return leaves_out, scores_out
+        s = self.scores
+        idx = torch.argmax(s).reshape(1) if k_take == 1 else torch.topk(s, k_take).indices
+        leaves_out[:k_take] = self.leaves[idx].cpu().numpy()
+        scores_out[:k_take] = s[idx].cpu().numpy()
+        return leaves_out, scores_out
+
+
+@dataclasses.dataclass
+class PruneIntegrationStep:
+    """One hop in a survivor's pruning integration path (``prune.py:334-344``)."""
+
+    level: int
+    survivor_idx: int
+    seg_idx: int
+    parent_idx: int
+    param_idx: np.ndarray
+    phase_shift: int
+
+
+class _Buffers:
+    """Grow-only device buffers reused across levels."""
+
+    def __init__(self, device) -> None:
+        self.device = device
+        self.bufs: dict[str, torch.Tensor] = {}
+
+    def get(self, name: str, numel: int, dtype) -> torch.Tensor:
+        t = self.bufs.get(name)
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = torch.empty(max(numel, 1) + (numel >> 3), dtype=dtype, device=self.device)
+            self.bufs[name] = t
+        return t[:numel]
+
+
+class Pruning:
+    """Enumerate-prune run over one FFA fold (``prune.py:347-782``).
+
+    Parameters
+    ----------
+    dyp : DynamicProgramming
+        FFA with its final level materialised (``execute()``).
+    threshold_scheme : array
+        One score threshold per pruning level.
+    max_sugg : int
+        Capacity of the survivor buffer; beyond it the reference's overflow
+        rule (top-k / median threshold raise) applies exactly.
+    batch_size : int
+        Parent batch size of the reference's sequential loop; it only matters
+        for the overflow rule, which is batch-sequential.
+    """
+
+    def __init__(self, dyp, threshold_scheme, max_sugg: int = 2**17, batch_size: int = 1024,
+                 poly_basis: str = "taylor", intermediate_k: int = 1, *,
+                 use_moving_grid: bool = True, logger=None) -> None:
+        cfg = dyp.cfg
+        if dyp.fold.ndim > 8:
+            msg = "Pruning currently supports initial data till 5 param dimensions."
+            raise ValueError(msg)
+        key = (cfg.prune_poly_order == 5, poly_basis, cfg.use_fourier)
+        if key not in {(True, "taylor", True), (True, "taylor", False),
+                       (False, "taylor", True), (False, "taylor", False),
+                       (False, "chebyshev", True), (False, "chebyshev", False)}:
+            msg = f"Invalid pruning configuration: {key}"
+            raise ValueError(msg)
+        if key != (False, "taylor", False):
+            msg = f"pruning plugin {key} (circular / chebyshev / complex) is not built yet"
+            raise NotImplementedError(msg)
+        self._dyp = dyp
+        self._threshold_scheme = np.asarray(threshold_scheme, dtype=np.float64)
+        self._max_sugg = int(max_sugg)
+        self._batch_size = int(batch_size)
+        self._intermediate_k = intermediate_k
+        self._use_moving_grid = use_moving_grid
+        self._logger = logger
+        self._lib = _lib.load()
+        self._device = dyp.device
+        self._buf = _Buffers(self._device)
+        self._err = torch.zeros(1, dtype=torch.int32, device=self._device)
+        self.poly_order = cfg.prune_poly_order
+        self.nparams_ffa = cfg.nparams
+        if self.nparams_ffa != self.poly_order or self.nparams_ffa < 2:
+            # poly_taylor_seed copies the FFA grid rows into the Taylor rows
+            # (core/taylor.py:56-63), which needs one FFA parameter per order.
+            msg = (f"the Taylor pruning plugin needs prune_poly_order == FFA parameters "
+                   f"(got {self.poly_order} and {self.nparams_ffa})")
+            raise ValueError(msg)
+        self.spec = _lib.score_spec(cfg.score_widths, cfg.nbins, 1.0, mode=1)
+        self.param_grid_count_init = np.asarray(dyp.param_grid_count, np.int64)
+        #: kernels launched by this object
+        self.launches = 0
+
+    # ---- reference properties -----------------------------------------------
+    @property
+    def dyp(self):
+        return self._dyp
+
+    @property
+    def threshold_scheme(self) -> np.ndarray:
+        return self._threshold_scheme
+
+    @property
+    def max_sugg(self) -> int:
+        return self._max_sugg
+
+    @property
+    def batch_size(self) -> int:
+        return self._batch_size
+
+    @property
+    def intermediate_k(self) -> int:
+        return self._intermediate_k
+
+    @property
+    def use_moving_grid(self) -> bool:
+        return self._use_moving_grid
+
+    @property
+    def prune_level(self) -> int:
+        return self._prune_level
+
+    @property
+    def prune_complete(self) -> bool:
+        return self._prune_complete
+
+    @property
+    def scheme(self) -> MiddleOutScheme:
+        return self._scheme
+
+    @property
+    def world_tree(self) -> WorldTree:
+        return self._world_tree
+
+    @property
+    def pstats(self) -> list[PruneStats]:
+        return self._pstats
+
+    @property
+    def backtrack_hist(self) -> list[torch.Tensor]:
+        return self._backtrack_hist
+
+    @property
+    def best_intermediate_arr(self) -> np.ndarray:
+        return self._best_intermediate_arr
+
+    def _stream(self) -> int:
+        return _lib.stream_ptr(torch.cuda.current_stream(self._device))
+
+    def _fold_segment(self, seg: int) -> torch.Tensor:
+        f = self.dyp.fold[seg]
+        return f.contiguous() if not f.is_contiguous() else f
+
+    # ---- seed (core/taylor.py:14-65, dyn_poly_taylor.py:405-423) -------------
+    def _seed(self, fold_segment: torch.Tensor) -> WorldTree:
+        cfg = self.dyp.cfg
+        P = self.poly_order
+        param_arr = self.dyp.param_arr
+        dparams = np.asarray(self.dyp.dparams_actual, np.float64)
+        mesh = np.meshgrid(*param_arr, indexing="ij")
+        cart = np.stack([m.ravel() for m in mesh], axis=1)
+        n = cart.shape[0]
+        f0 = cart[:, -1]
+        df = np.broadcast_to(dparams[-1], (n,))
+        leaves = np.zeros((n, P + 2, 2), dtype=np.float64)
+        leaves[:, : P - 1, 0] = cart[:, :-1]
+        leaves[:, : P - 1, 1] = dparams[:-1]
+        leaves[:, -3, 0] = 0
+        leaves[:, -3, 1] = df * (C_VAL / f0)
+        leaves[:, -2, 0] = 0
+        leaves[:, -1, 0] = f0
+        leaves[:, -1, 1] = 0
+        folds = fold_segment.reshape(n, 2, cfg.nbins).contiguous()
+        from pyloki_gb300.scoring import snr_score_batch
+
+        scores = snr_score_batch(folds, cfg.score_widths)
+        bt = torch.zeros((n, P + 2), dtype=torch.int32, device=self._device)
+        return WorldTree(torch.from_numpy(leaves).to(self._device), folds, scores, bt)
+
+    def initialize(self, ref_seg: int, log_file: Path | None = None) -> None:
+        self._scheme = MiddleOutScheme(self.dyp.nsegments, ref_seg, self.dyp.tseg, 1)
+        self._prune_complete = False
+        self._prune_level = 0
+        self._world_tree = self._seed(self._fold_segment(self.scheme.ref_idx))
+        self._backtrack_hist: list[torch.Tensor] = []
+        self._best_intermediate_arr = np.zeros(
+            (self.dyp.nsegments - 1, self.intermediate_k),
+            dtype=np.dtype([("param_sets", np.float64, (self.poly_order + 2, 2)),
+                            ("scores", np.float32)]))
+        wt = self._world_tree
+        st = PruneStats(level=0, seg_idx=self.scheme.get_segment_idx(0), threshold=0,
+                        score_min=wt.score_min, score_max=wt.score_max,
+                        n_branches=wt.size, n_leaves=wt.size, n_leaves_phy=wt.size,
+                        n_leaves_surv=wt.size)
+        self._pstats = [st]
+        self._timers: list[np.ndarray] = []
+        if log_file is not None:
+            with Path(log_file).open("a") as f:
+                f.write(st.get_summary())
+
+    # ---- per-level constants ---------------------------------------------------
+    def level_desc(self, level: int) -> _lib.LokiPruneLevel:
+        cfg = self.dyp.cfg
+        sc = self.scheme
+        moving = self.use_moving_grid
+        P = self.poly_order
+        coord_init = sc.get_coord(0)
+        coord_cur = sc.get_current_coord(level, moving)
+        coord_next = sc.get_coord(level)
+        coord_add = sc.get_segment_coord(level)
+        d = _lib.LokiPruneLevel()
+        d.poly_order = P
+        d.nbins = cfg.nbins
+        d.nparams_ffa = self.nparams_ffa
+        d.moving = 1 if moving else 0
+        d.tiling = _TILING[cfg.tiling_strategy]
+        d.branch_max = cfg.branch_max
+        d.eta_m = cfg.eta - FLOAT_EPSILON
+        tobs = coord_cur[1]
+        dfc = (poly_taylor_step_f(P, tobs, cfg.nbins, cfg.eta, 0)[np.newaxis, :] * C_VAL)[0]
+        fac = shift_factors(P, tobs, cfg.nbins)
+        for j in range(P):
+            d.dfc[j] = float(dfc[j])
+            d.fac[j] = float(fac[j])
+        if moving:
+            _set6(d.tm_a, taylor_matrix(coord_add[0] - coord_cur[0], P + 1))
+            _set6(d.tm_i, taylor_matrix(coord_init[0] - coord_cur[0], P + 1))
+            tn = taylor_matrix(coord_next[0] - coord_cur[0], P + 1)
+            _set6(d.tm_n, tn)
+            _set6(d.tm_e, tn**2 if cfg.tiling_strategy == "quadrature" else np.abs(tn))
+        else:
+            _set6(d.tm_a, taylor_matrix(coord_add[0] - coord_init[0], P + 1))
+        d.dt_phase = coord_add[0] - coord_init[0]
+        counts = self.param_grid_count_init
+        lim = cfg.param_limits
+        d.n_accel, d.n_freq = int(counts[-2]), int(counts[-1])
+        a_min, a_max = lim[-2]
+        f_min, f_max = lim[-1]
+        d.accel_min = float(a_min)
+        d.accel_inv = float(counts[-2] / (a_max - a_min)) if a_max > a_min else 0.0
+        d.freq_min = float(f_min)
+        d.freq_inv = float(counts[-1] / (f_max - f_min)) if f_max > f_min else 0.0
+        return d
+
+    # ---- one level (prune.py:615-669) ------------------------------------------
+    def execute_iter(self, log_file: Path | None = None) -> None:
+        if self.prune_complete:
+            return
+        self._prune_level += 1
+        level = self._prune_level
+        lib = self._lib
+        stream = self._stream()
+        seg_idx = self.scheme.get_segment_idx(level)
+        fold_segment = self._fold_segment(seg_idx)
+        threshold = float(self.threshold_scheme[level - 1])
+        d = self.level_desc(level)
+        tree = self._world_tree
+        n_par = tree.valid_size
+        P = self.poly_order
+        offsets = self._buf.get("offsets", n_par + 1, torch.int64)
+        info = self._buf.get("info", n_par * _lib.BRANCH_INFO_BYTES, torch.uint8)
+        sb = int(lib.loki_scan_scratch_bytes(n_par + 1))
+        scan = self._buf.get("scan", sb, torch.uint8)
+        _lib.check(lib.loki_prune_branch(d, _lib.ptr(tree.leaves), n_par, _lib.ptr(info),
+                                         _lib.ptr(offsets), _lib.ptr(scan), sb,
+                                         _lib.ptr(self._err), stream))
+        n_child = int(offsets[n_par].item())
+        _lib.check_dev_err(self._err)
+        scores = self._buf.get("cscores", n_child, torch.float32)
+        cidx = self._buf.get("cidx", 2 * n_child, torch.int32)
+        cphase = self._buf.get("cphase", n_child, torch.float64)
+        minmax = self._buf.get("minmax", 2, torch.float32)
+        _lib.check(lib.loki_prune_score(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par,
+                                        _lib.ptr(info), _lib.ptr(offsets), n_child,
+                                        _lib.ptr(fold_segment), self.spec, _lib.ptr(scores),
+                                        _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(minmax),
+                                        _lib.ptr(self._err), stream))
+        ssb = int(lib.loki_scan_scratch_bytes(n_child)) + 8 * (n_child + 1)
+        sscan = self._buf.get("sscan", ssb, torch.uint8)
+        surv = self._buf.get("surv", max(n_child, 1), torch.int64)
+        n_surv_d = self._buf.get("nsurv", 1, torch.int64)
+        _lib.check(lib.loki_prune_select(_lib.ptr(scores), n_child, threshold, _lib.ptr(surv),
+                                         _lib.ptr(n_surv_d), _lib.ptr(sscan), ssb, stream))
+        n_surv = int(n_surv_d.item())
+        self.launches += 9
+        if n_surv > self.max_sugg:
+            n_surv = self._select_overflow(scores, offsets, n_par, n_child, threshold, surv,
+                                           n_surv_d)
+        nb = self.dyp.cfg.nbins
+        dev = self._device
+        new = WorldTree(torch.empty((n_surv, P + 2, 2), dtype=torch.float64, device=dev),
+                        torch.empty((n_surv, 2, nb), dtype=torch.float32, device=dev),
+                        torch.empty(n_surv, dtype=torch.float32, device=dev),
+                        torch.empty((n_surv, P + 2), dtype=torch.int32, device=dev),
+                        torch.empty(n_surv, dtype=torch.float32, device=dev))
+        _lib.check(lib.loki_prune_emit(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds),
+                                       _lib.ptr(info), _lib.ptr(offsets), n_par,
+                                       _lib.ptr(fold_segment), _lib.ptr(surv), n_surv,
+                                       _lib.ptr(scores), _lib.ptr(cidx), _lib.ptr(cphase),
+                                       _lib.ptr(new.leaves), _lib.ptr(new.folds),
+                                       _lib.ptr(new.scores), _lib.ptr(new.scores_ep),
+                                       _lib.ptr(new.backtracks), stream))
+        self.launches += 1
+        mm = minmax.cpu().numpy() if n_child else np.zeros(2, np.float32)
+        st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
+                        score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
+                        n_leaves=n_child, n_leaves_phy=n_child, n_leaves_surv=n_surv)
+        self._pstats.append(st)
+        if log_file is not None:
+            with Path(log_file).open("a") as f:
+                f.write(st.get_summary())
+        if n_surv == 0:
+            self._prune_complete = True
+            self._world_tree = new
+            return
+        slot = self._best_intermediate_arr[level - 1]
+        slot["param_sets"], slot["scores"] = new.get_best_k(self.intermediate_k)
+        self._backtrack_hist.append(new.backtracks)
+        self._world_tree = new
+
+    def _select_overflow(self, scores, offsets, n_par, n_child, threshold, surv, n_surv_d) -> int:
+        """Exact batch-sequential selection when more than ``max_sugg`` pass."""
+        off = offsets.cpu().numpy()
+        b = self.batch_size
+        starts = np.arange(0, n_par, b)
+        ends = np.minimum(starts + b, n_par)
+        max_batch = int((off[ends] - off[starts]).max()) if n_par else 0
+        n = self.max_sugg + max_batch + 1
+        ids = self._buf.get("ovf_ids", n, torch.int64)
+        keys = self._buf.get("ovf_keys", n, torch.float32)
+        thr_d = self._buf.get("ovf_thr", 1, torch.float64)
+        _lib.check(self._lib.loki_prune_select_overflow(
+            _lib.ptr(scores), _lib.ptr(offsets), n_par, b, threshold, self.max_sugg,
+            _lib.ptr(surv), _lib.ptr(n_surv_d), _lib.ptr(thr_d), _lib.ptr(ids), _lib.ptr(keys),
+            n, self._stream()))
+        self.launches += 1
+        return int(n_surv_d.item())
+
+    # ---- ascend (prune.py:671-693, dyn_poly_taylor.py:587-628) -----------------
+    def _do_ascend(self) -> None:
+        if self.prune_complete or self.world_tree.valid_size == 0:
+            return
+        sc = self.scheme
+        P = self.poly_order
+        coord_end = sc.get_previous_coord(self.prune_level + 1, self.use_moving_grid)
+        seg_idx, seg_coords = sc.get_segment_coords_so_far(self.prune_level)
+        nseg = len(seg_idx)
+        tm = np.zeros((nseg, 6, 6), np.float64)
+        dts = np.zeros(nseg, np.float64)
+        for s in range(nseg):
+            dt = seg_coords[s, 0] - coord_end[0]
+            tm[s, : P + 1, : P + 1] = taylor_matrix(dt, P + 1)
+            dts[s] = dt
+        dev = self._device
+        tm_d = torch.from_numpy(tm).to(dev)
+        dt_d = torch.from_numpy(dts).to(dev)
+        si_d = torch.from_numpy(seg_idx.astype(np.int32)).to(dev)
+        fold = self.dyp.fold
+        stride = int(np.prod(fold.shape[1:]))
+        d = self.level_desc(self.prune_level)
+        wt = self.world_tree
+        _lib.check(self._lib.loki_prune_ascend(
+            d, _lib.ptr(wt.leaves), _lib.ptr(wt.folds), _lib.ptr(wt.scores),
+            _lib.ptr(wt.scores_ep), wt.valid_size, nseg, _lib.ptr(tm_d), _lib.ptr(dt_d),
+            _lib.ptr(si_d), _lib.ptr(fold), stride, self.spec, _lib.ptr(self._err),
+            self._stream()))
+        self.launches += 1
+
+    # ---- report (core/taylor.py:342-360) ---------------------------------------
+    def report(self) -> np.ndarray:
+        leaves = self.world_tree.leaves.cpu().numpy()
+        return poly_taylor_report_batch(leaves)
+
+    def execute(self, ref_seg: int, ascend_levels: list[int] | None = None,
+                outdir: str | Path = "./", log_file: Path | None = None,
+                result_file: Path | None = None, task_id: int = 0) -> dict:
+        """Full run for one reference segment; returns the run's results."""
+        asc = frozenset(ascend_levels) if ascend_levels is not None else None
+        self.initialize(ref_seg, log_file)
+        for _ in range(self.dyp.nsegments - 1):
+            self.execute_iter(log_file)
+            if asc is not None and self.prune_level in asc:
+                self._do_ascend()
+        if asc is None or self.prune_level not in asc:
+            self._do_ascend()
+        return {
+            "run_name": f"{ref_seg:03d}_{task_id:02d}",
+            "scheme": self.scheme.data.copy(),
+            "param_sets": self.report(),
+            "scores": self.world_tree.scores.cpu().numpy(),
+            "scores_ep": self.world_tree.scores_ep.cpu().numpy(),
+            "level_stats": self.pstats,
+        }
+
+    def trace_integration_path(self, survivor_idx: int,
+                               level: int | None = None) -> list[PruneIntegrationStep]:
+        """Walk parent links back to the seed (``prune.py:695-755``)."""
+        n_levels = len(self._backtrack_hist)
+        if n_levels == 0:
+            msg = "No backtrack history; run pruning before tracing a path."
+            raise ValueError(msg)
+        if level is None:
+            level = n_levels
+        if not 1 <= level <= n_levels:
+            msg = f"level must be in [1, {n_levels}], got {level}"
+            raise ValueError(msg)
+        steps = []
+        lvl, idx = level, survivor_idx
+        while lvl >= 1:
+            bts = self._backtrack_hist[lvl - 1]
+            if idx < 0 or idx >= len(bts):
+                msg = f"survivor_idx {idx} out of range [0, {len(bts)}) at level {lvl}"
+                raise ValueError(msg)
+            bt = bts[idx].cpu().numpy()
+            nparams = len(bt) - 2
+            steps.append(PruneIntegrationStep(level=lvl, survivor_idx=idx,
+                                              seg_idx=self.scheme.get_segment_idx(lvl),
+                                              parent_idx=int(bt[0]),
+                                              param_idx=bt[1: nparams + 1].copy(),
+                                              phase_shift=int(bt[-1])))
+            if lvl == 1:
+                break
+            idx = int(bt[0])
+            lvl -= 1
+        return steps[::-1]
+
+
+def poly_taylor_report_batch(leaves: np.ndarray) -> np.ndarray:
+    """Gauge transform of the final leaves (``core/taylor.py:342-360``)."""
+    out = leaves.copy()
+    vals = leaves[:, :-3, 0]
+    sigs = leaves[:, :-3, 1]
+    v_final = leaves[:, -3, 0]
+    dv_final = leaves[:, -3, 1]
+    f0 = leaves[:, -1, 0]
+    s = 1 - v_final / C_VAL
+    out[:, :-3, 0] = vals / s[:, None]
+    out[:, :-3, 1] = np.sqrt((sigs / s[:, None]) ** 2
+                             + ((vals / (C_VAL * s[:, None] ** 2)) ** 2) * (dv_final[:, None] ** 2))
+    out[:, -3, 0] = f0 * s
+    out[:, -3, 1] = f0 * dv_final / C_VAL
+    return out
+
+
+def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
+                   ref_segs: list[int] | None = None, ascend_levels: list[int] | None = None,
+                   max_sugg: int = 2**18, batch_size: int = 1024, outdir: str | Path = "./",
+                   file_prefix: str = "test", poly_basis: str = "taylor", *,
+                   use_moving_grid: bool = True, n_workers: int = 4) -> str:
+    """Prune from several reference segments (``prune.py:824-932``).
+
+    Runs are executed one after another on the device (``n_workers`` is
+    validated like the reference but a single GPU needs no process pool).
+    Results are written as one ``.npz`` with the reference's per-run groups
+    (``runs/<ref:03d>_<task:02d>/{scheme, param_sets, scores, scores_ep}``).
+    """
+    if not isinstance(n_workers, int | np.integer):
+        msg = f"n_workers must be an integer, got {type(n_workers)}"
+        raise TypeError(msg)
+    if n_workers < 1:
+        msg = f"n_workers must be greater than 0, got {n_workers}"
+        raise ValueError(msg)
+    if n_runs is not None:
+        if not 1 <= n_runs <= dyp.nsegments:
+            msg = f"n_runs must be between 1 and {dyp.nsegments}, got {n_runs}"
+            raise ValueError(msg)
+        ref_segs = determine_ref_segs_pareto(dyp.nsegments, n_runs)
+    elif ref_segs is None:
+        msg = "Either n_runs or ref_segs must be provided"
+        raise ValueError(msg)
+    outdir = Path(outdir)
+    outdir.mkdir(parents=True, exist_ok=True)
+    filebase = f"{file_prefix}_pruning_nstages_{dyp.nsegments}"
+    log_file = outdir / f"{filebase}_log.txt"
+    result_file = outdir / f"{filebase}_results.npz"
+    if log_file.exists() or result_file.exists():
+        msg = f"{log_file} or {result_file} already exists"
+        raise FileExistsError(msg)
+    log_file.write_text("Pruning log\n")
+    out = {"param_names": np.asarray(dyp.cfg.param_names), "nsegments": dyp.nsegments,
+           "max_sugg": max_sugg, "threshold_scheme": np.asarray(threshold_scheme)}
+    prn = Pruning(dyp, threshold_scheme, max_sugg=max_sugg, batch_size=batch_size,
+                  poly_basis=poly_basis, use_moving_grid=use_moving_grid)
+    for ref_seg in ref_segs:
+        with log_file.open("a") as f:
+            f.write(f"Pruning log for ref segment: {ref_seg}\n")
+        res = prn.execute(ref_seg, ascend_levels=ascend_levels, log_file=log_file)
+        g = f"runs/{res['run_name']}"
+        out[f"{g}/scheme"] = res["scheme"]
+        out[f"{g}/param_sets"] = res["param_sets"]
+        out[f"{g}/scores"] = res["scores"]
+        out[f"{g}/scores_ep"] = res["scores_ep"]
+        out[f"{g}/level_stats"] = np.array(
+            [(s.level, s.seg_idx, s.threshold, s.score_min, s.score_max, s.n_branches,
+              s.n_leaves, s.n_leaves_phy, s.n_leaves_surv) for s in res["level_stats"]],
+            dtype=np.float64)
+    np.savez_compressed(result_file, **out)
+    return result_file.as_posix()
+
+
+def leaves_per_second(stats: list[PruneStats], seconds: float) -> float:
+    """Prune leaves/s: leaves emitted by branch (``n_leaves``) over the run time."""
+    return float(sum(s.n_leaves for s in stats[1:])) / seconds if seconds > 0 else math.inf

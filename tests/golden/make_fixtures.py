@@ -133,6 +133,87 @@ def scoring_case(name: str, nbins: int, nprof: int, ducy_max: float, wtsp: float
     print(name, widths)
 
 
+def prune_series(n: int, tsamp: float, f0: float, accel: float, seed: int):
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) * tsamp
+    tc = t[n // 2]
+    ph = (t - accel * (t - tc) ** 2 / 2 / 299792458.0) * f0
+    pulse = np.exp(10 * (np.cos(2 * np.pi * (ph - 0.4)) - 1))
+    ts_e = (rng.standard_normal(n) + 0.25 * pulse).astype(np.float32)
+    return ts_e, np.ones(n, np.float32)
+
+
+def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
+               max_sugg: int = 2**16, batch_size: int = 64, ref_seg: int = 8,
+               fold_levels: tuple = (5, 11), thr_offset: float = 0.0,
+               leaf_cap: int = 6000) -> None:
+    """Taylor (poly_order 3, real folds) enumerate-prune run of 15 levels."""
+    import tempfile
+
+    from pyloki.config import ParamLimits, PulsarSearchConfig
+    from pyloki.ffa import DynamicProgramming
+    from pyloki.io.timeseries import TimeSeries
+    from pyloki.prune import Pruning
+
+    n, tsamp = 2**17, 2.5e-4
+    ts_e, ts_v = prune_series(n, tsamp, 100.3, 300.0, 5)
+    lim = ParamLimits.from_taylor((100.0, 101.0), accel=(-20000.0, 20000.0),
+                                  jerk=(-3000.0, 3000.0)).limits
+    cfg = PulsarSearchConfig(nsamps=n, tsamp=tsamp, nbins=32, eta=1.0, param_limits=lim,
+                             ducy_max=0.3, wtsp=2.0, use_fourier=False, bseg_ffa=n // 16,
+                             prune_poly_order=3, branch_max=16, tiling_strategy=tiling)
+    dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, tsamp), cfg)
+    dyp.initialize()
+    dyp.execute(show_progress=False)
+    thr = np.linspace(3.0, 7.5, dyp.nsegments - 1) + thr_offset
+    prn = Pruning(dyp, thr, max_sugg=max_sugg, batch_size=batch_size,
+                  use_moving_grid=moving)
+    log = Path(tempfile.mkdtemp()) / "log.txt"
+    log.touch()
+    prn.initialize(ref_seg, log)
+    out = {"ts_e": ts_e, "ts_v": ts_v, **_cfg_dict(cfg), "thresholds": thr,
+           "max_sugg": np.int64(max_sugg), "batch_size": np.int64(batch_size),
+           "ref_seg": np.int64(ref_seg), "moving": np.int64(moving),
+           "poly_order": np.int64(3), "branch_max": np.int64(16),
+           "fold_ffa": np.asarray(dyp.fold), "scheme": prn.scheme.data.copy()}
+    wt = prn.world_tree
+    out["seed_leaves"] = wt.leaves[: wt.valid_size].copy()
+    out["seed_scores"] = wt.scores[: wt.valid_size].copy()
+    nparams = cfg.nparams
+    for lvl in range(1, dyp.nsegments):
+        prn.execute_iter(log)
+        wt = prn.world_tree
+        v = wt.valid_size
+        st = prn.pstats.stats_list[-1]
+        out[f"stats_{lvl}"] = np.array([st.n_branches, st.n_leaves, st.n_leaves_phy,
+                                        st.n_leaves_surv], np.int64)
+        out[f"smm_{lvl}"] = np.array([st.score_min, st.score_max], np.float64)
+        out[f"scores_{lvl}"] = wt.scores[:v].copy()
+        if v <= leaf_cap:
+            out[f"leaves_{lvl}"] = wt.leaves[:v].copy()
+            bt = wt.backtracks[:v]
+            out[f"bt_{lvl}"] = np.concatenate([bt[:, : nparams + 1], bt[:, -1:]],
+                                              axis=1).copy()
+        if lvl in fold_levels:
+            out[f"folds_{lvl}"] = wt.folds[:v].copy()
+        if prn.prune_complete:
+            break
+    out["levels_done"] = np.int64(prn.prune_level)
+    prn._do_ascend()
+    wt = prn.world_tree
+    v = wt.valid_size
+    out["asc_scores"] = wt.scores[:v].copy()
+    out["asc_scores_ep"] = wt.scores_ep[:v].copy()
+    if v <= leaf_cap:
+        out["asc_folds"] = wt.folds[:v].copy()
+        out["final_leaves"] = wt.leaves[:v].copy()
+    coord_end = prn.scheme.get_previous_coord(prn.prune_level + 1, prn.use_moving_grid)
+    coord_report = prn.scheme.get_report_coord(prn.use_moving_grid)
+    out["report"] = prn.prune_funcs.report(wt.leaves[:v].copy(), coord_report, coord_end)
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "levels", prn.prune_level, "survivors", v)
+
+
 def main() -> None:
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_src = args[0] if args else "/root/reference/src"
@@ -140,17 +221,42 @@ def main() -> None:
     import refshim
 
     refshim.install(ref_src)
+    # numba types `float32_array >= float64` as a float64 comparison. Under
+    # plain numpy 2 the overflow threshold that world_tree derives with
+    # math.nextafter is a Python float, i.e. a weak scalar, so numpy would
+    # compare in float32 instead. Returning np.float64 restores the numba
+    # typing for the prune_on_overload comparisons.
+    import math as _math
+    import types as _types
+
+    from pyloki.utils import world_tree as _wt
+
+    _wt.math = _types.SimpleNamespace(
+        nextafter=lambda a, b: np.float64(_math.nextafter(a, b)))
     import logging
 
     logging.disable(logging.CRITICAL)
-    if "--skip-scoring" not in sys.argv:
+    if "--skip-scoring" not in sys.argv and "--prune-only" not in sys.argv:
         scoring_case("score_nb64", 64, 512, 0.5, 2.0, 11)
         scoring_case("score_nb50", 50, 256, 0.2, 1.5, 12)
         scoring_case("score_nb100", 100, 128, 0.3, 1.3, 13)
+    if "--prune-only" in sys.argv:
+        prune_cases()
+        return
     ffa_case("ffa_freq", 2**15, [(10.0, 14.0)], 64, 12.3, 21)
     ffa_case("ffa_accel", 2**15, [(-3.0e5, 3.0e5), (200.0, 202.0)], 64, 201.1, 22)
     ffa_case("ffa_jerk", 2**15, [(-1.0e7, 1.0e7), (-3.0e5, 3.0e5), (200.0, 201.0)],
              50, 200.4, 23, ducy_max=0.2, wtsp=1.5)
+    prune_cases()
+
+
+def prune_cases() -> None:
+    prune_case("prune_taylor")
+    prune_case("prune_taylor_cons", tiling="conservative", fold_levels=(), thr_offset=1.5)
+    prune_case("prune_taylor_quad", tiling="quadrature", fold_levels=(), thr_offset=1.5)
+    prune_case("prune_taylor_fixed", moving=False, fold_levels=())
+    prune_case("prune_taylor_overflow", max_sugg=1024, batch_size=64, ref_seg=3,
+               fold_levels=(12,))
 
 
 if __name__ == "__main__":

@@ -78,3 +78,32 @@ def test_score_spec_constants():
     h = np.sqrt((64 - 8) / (64 * 8))
     b = 8 * h / (64 - 8)
     assert sp.hb[3] == h + b and sp.b[3] == b
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the C structs have the header's sizes and offsets."""
+    import subprocess
+
+    from pyloki_gb300 import _lib
+
+    structs = [_lib.LokiFFALevel, _lib.LokiFFACoord, _lib.LokiScoreSpec,
+               _lib.LokiPruneLevel, _lib.LokiBranchInfo]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "loki_gb300.h"',
+             "int main(void) {"]
+    for st in structs:
+        name = st.__name__
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for fname, _ in st._fields_:
+            lines.append(f'printf("{name}.{fname} %zu\\n", offsetof({name}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True,
+                                                       text=True, check=True).stdout.splitlines())
+    for st in structs:
+        name = st.__name__
+        assert int(got[name]) == ctypes.sizeof(st), name
+        for fname, _ in st._fields_:
+            assert int(got[f"{name}.{fname}"]) == getattr(st, fname).offset, (name, fname)

@@ -1,0 +1,119 @@
+"""GPU enumerate-prune (Taylor basis) against runs of the pyloki reference.
+
+Every level is compared with the reference's tree after the same level: the
+statistics, the survivor scores, the backtracks and (where stored) the folds
+exactly; the FP64 leaf parameters to 1e-13 relative (they are exact on the
+machine that generated the fixtures; another machine's libm pow may move the
+host-computed Taylor constants by an ulp).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
+         "prune_taylor_overflow"]
+TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature"}
+
+
+def _cfg(d, name):
+    from pyloki_gb300.config import PulsarSearchConfig
+
+    return PulsarSearchConfig(
+        nsamps=int(d["nsamps"]), tsamp=float(d["tsamp"]), nbins=int(d["nbins"]),
+        eta=float(d["eta"]), param_limits=d["param_limits"], ducy_max=float(d["ducy_max"]),
+        wtsp=float(d["wtsp"]), use_fourier=False, bseg_ffa=int(d["bseg_ffa"]),
+        prune_poly_order=int(d["poly_order"]), branch_max=int(d["branch_max"]),
+        tiling_strategy=TILING.get(name, "aggressive"))
+
+
+def _run(name, cuda_device):
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import Pruning
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden(name)
+    cfg = _cfg(d, name)
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg,
+                             device=cuda_device)
+    dyp.initialize()
+    dyp.execute()
+    np.testing.assert_array_equal(dyp.fold.cpu().numpy(), d["fold_ffa"])
+    prn = Pruning(dyp, d["thresholds"], max_sugg=int(d["max_sugg"]),
+                  batch_size=int(d["batch_size"]), use_moving_grid=bool(d["moving"]))
+    return d, prn
+
+
+def _leaves_close(got, ref, what):
+    np.testing.assert_allclose(got, ref, rtol=1e-13, atol=0, err_msg=what)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_prune_levels_match_reference(cuda_device, name):
+    d, prn = _run(name, cuda_device)
+    prn.initialize(int(d["ref_seg"]))
+    np.testing.assert_array_equal(prn.scheme.data, d["scheme"])
+    wt = prn.world_tree
+    _leaves_close(wt.leaves.cpu().numpy(), d["seed_leaves"], "seed leaves")
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["seed_scores"])
+    nparams = prn.nparams_ffa
+    for lvl in range(1, int(d["levels_done"]) + 1):
+        prn.execute_iter()
+        st = prn.pstats[-1]
+        np.testing.assert_array_equal(
+            [st.n_branches, st.n_leaves, st.n_leaves_phy, st.n_leaves_surv],
+            d[f"stats_{lvl}"], err_msg=f"stats level {lvl}")
+        np.testing.assert_array_equal([st.score_min, st.score_max],
+                                      d[f"smm_{lvl}"].astype(np.float32).astype(np.float64),
+                                      err_msg=f"score min/max level {lvl}")
+        wt = prn.world_tree
+        np.testing.assert_array_equal(wt.scores.cpu().numpy(), d[f"scores_{lvl}"],
+                                      err_msg=f"scores level {lvl}")
+        if f"leaves_{lvl}" in d:
+            _leaves_close(wt.leaves.cpu().numpy(), d[f"leaves_{lvl}"], f"leaves level {lvl}")
+            bt = wt.backtracks.cpu().numpy()
+            got = np.concatenate([bt[:, : nparams + 1], bt[:, -1:]], axis=1)
+            np.testing.assert_array_equal(got, d[f"bt_{lvl}"], err_msg=f"bt level {lvl}")
+        if f"folds_{lvl}" in d:
+            np.testing.assert_array_equal(wt.folds.cpu().numpy(), d[f"folds_{lvl}"])
+    prn._do_ascend()
+    wt = prn.world_tree
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["asc_scores"])
+    np.testing.assert_array_equal(wt.scores_ep.cpu().numpy(), d["asc_scores_ep"])
+    if "asc_folds" in d:
+        np.testing.assert_array_equal(wt.folds.cpu().numpy(), d["asc_folds"])
+        _leaves_close(wt.leaves.cpu().numpy(), d["final_leaves"], "final leaves")
+        _leaves_close(prn.report(), d["report"], "report")
+
+
+def test_trace_integration_path(cuda_device):
+    d, prn = _run("prune_taylor", cuda_device)
+    prn.initialize(int(d["ref_seg"]))
+    for _ in range(int(d["levels_done"])):
+        prn.execute_iter()
+    steps = prn.trace_integration_path(0)
+    assert [s.level for s in steps] == list(range(1, len(steps) + 1))
+    assert steps[-1].survivor_idx == 0
+    for a, b in zip(steps[:-1], steps[1:], strict=False):
+        assert b.parent_idx == a.survivor_idx
+    with pytest.raises(ValueError):
+        prn.trace_integration_path(10**9)
+
+
+def test_prune_dyp_tree_writes_results(cuda_device, tmp_path):
+    from pyloki_gb300.prune import prune_dyp_tree
+
+    d, prn = _run("prune_taylor", cuda_device)
+    path = prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=2, max_sugg=int(d["max_sugg"]),
+                          batch_size=int(d["batch_size"]), outdir=tmp_path, n_workers=1)
+    res = np.load(path)
+    runs = sorted({k.split("/")[1] for k in res.files if k.startswith("runs/")})
+    assert len(runs) == 2
+    with pytest.raises(FileExistsError):
+        prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=2, outdir=tmp_path, n_workers=1)
+    with pytest.raises(ValueError):
+        prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=0, outdir=tmp_path / "x")
