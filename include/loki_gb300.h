@@ -102,6 +102,23 @@ int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
                    void* phase_scratch, int64_t scratch_bytes,
                    float* fold_out, void* stream);
 
+/* loki_brutefold without a caller-supplied phase scratch and without any
+ * device allocation: no counterpart in the reference. For callers that may
+ * not allocate device memory: cudaMalloc and cudaFree synchronise the whole
+ * device, stalling a host pipeline that keeps other streams busy, and a host
+ * that holds a fixed device-memory budget has nothing left to hand out.
+ * The map lives in a fixed 16 MiB device array of the library (its size is
+ * returned by loki_brutefold_noalloc_scratch_bytes), so segment_len is
+ * limited to 16 Mi samples for nbins <= 256 and 8 Mi for nbins > 256;
+ * beyond that it returns LOKI_ERR_CAPACITY. The array is shared by all calls
+ * on one device: calls that overlap on the GPU (different streams, no
+ * ordering between them) race on it; calls on one stream are ordered. */
+int loki_brutefold_noalloc(const float* ts_e, const float* ts_v, int64_t nsamps,
+                           const double* freqs, int64_t nfreqs, int64_t segment_len,
+                           int32_t nbins, double tsamp, double t_ref,
+                           float* fold_out, void* stream);
+int64_t loki_brutefold_noalloc_scratch_bytes(void);
+
 /* Plan table of one FFA level (one entry per current-level parameter set in
  * the output window). Replaces the per-parameter resolve inside unify_fold
  * (dynamic/dyn_pffa.py:462-475 -> core/fold.py:617-671) and

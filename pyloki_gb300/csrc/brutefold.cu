@@ -14,6 +14,7 @@
 // addresses). Blocks are ordered segment-fastest so that the map rows of the
 // frequencies in flight stay in L2 while every segment consumes them.
 #include <algorithm>
+#include <mutex>
 
 #include "loki_common.cuh"
 
@@ -194,4 +195,66 @@ extern "C" int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsam
     if (rc) return rc;
   }
   return LOKI_OK;
+}
+
+// Fixed phase-map scratch of loki_brutefold_noalloc. 16 MiB holds the map of
+// one frequency for segments of up to 16 Mi samples (nbins <= 256, one byte a
+// sample) or 8 Mi samples (nbins > 256, two bytes); larger frequency grids are
+// processed in chunks of as many frequencies as the array holds.
+static constexpr int64_t kNoAllocScratchBytes = int64_t(16) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_phase_scratch[kNoAllocScratchBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices];
+
+// Device address of the array on the current device, looked up once per device.
+int noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices)
+    return set_error(LOKI_ERR_UNSUPPORTED, "device ordinal %d above %d", dev, kMaxDevices - 1);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_phase_scratch);
+    if (e != cudaSuccess || !p)
+      return set_error(LOKI_ERR_CUDA, "cudaGetSymbolAddress of the phase scratch failed: %s",
+                       cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return LOKI_OK;
+}
+}  // namespace
+
+extern "C" int64_t loki_brutefold_noalloc_scratch_bytes(void) { return kNoAllocScratchBytes; }
+
+extern "C" int loki_brutefold_noalloc(const float* ts_e, const float* ts_v, int64_t nsamps,
+                                      const double* freqs, int64_t nfreqs, int64_t segment_len,
+                                      int32_t nbins, double tsamp, double t_ref, float* fold_out,
+                                      void* stream) {
+  if (!ts_e || !ts_v || !freqs || !fold_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if (nsamps <= 0 || nfreqs <= 0 || segment_len <= 0)
+    return set_error(LOKI_ERR_INVALID, "nsamps, nfreqs and segment_len must be > 0");
+  if (nbins < 1 || nbins > 768)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins %d outside [1, 768]", nbins);
+  const int64_t elem = nbins <= 256 ? 1 : 2;
+  if (segment_len > kNoAllocScratchBytes / elem)
+    return set_error(LOKI_ERR_CAPACITY,
+                     "segment_len %lld above the no-alloc limit of %lld samples for nbins %d "
+                     "(fixed %lld-byte phase scratch)",
+                     (long long)segment_len, (long long)(kNoAllocScratchBytes / elem), nbins,
+                     (long long)kNoAllocScratchBytes);
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  // Every map entry a fold reads is written by the phase-map launch of the same
+  // chunk, and every fold_out element by one fold thread: nothing is cleared.
+  return loki_brutefold(ts_e, ts_v, nsamps, freqs, nfreqs, segment_len, nbins, tsamp, t_ref,
+                        scratch, kNoAllocScratchBytes, fold_out, stream);
 }
