@@ -38,6 +38,10 @@ if str(ROOT) not in sys.path:
 
 METRIC = "period-trials/s"
 WORKLOAD = "ffa_accel_search_2^23"
+# DRAM bytes (read + write) per final trial of band_union64_kernel: ncu
+# capture of three launches of the same search at 2^21 samples (122.75 MB per
+# launch, 474k trials per launch); profiles/band_union64_kernel_ffa_accel_2^21.md.
+UNION_DRAM_BYTES_PER_TRIAL = 259.0
 
 
 def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0):
@@ -206,8 +210,8 @@ def bench_gpu(args) -> dict | None:
     for _ in range(args.warmup):
         one_step()
     barrier()
-    launches = 0
     phases = {"brutefold": 0.0, "levels": 0.0, "final": 0.0}
+    phase_launches = dict.fromkeys(phases, 0)
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clocks:
@@ -216,7 +220,10 @@ def bench_gpu(args) -> dict | None:
         for _ in range(args.steps):
             ev: list = []
             dyp, snr = one_step(ev)
-            launches += dyp.launches
+            m = dyp.phase_marks
+            phase_launches["brutefold"] += m["brutefold"] - m["start"]
+            phase_launches["levels"] += m["levels"] - m["brutefold"]
+            phase_launches["final"] += m["final"] - m["levels"]
             step_events.append(ev)
             del snr
         end.record()
@@ -262,6 +269,10 @@ def bench_gpu(args) -> dict | None:
     ab = algorithmic_bytes(cfg, dom)
     peak, peak_kind = measured_peak_hbm()
     achieved = ab / (dom_ms * 1e-3) / 1e9
+    dom_launches = max(1, phase_launches[dom] // args.steps)
+    traffic = None
+    if dom == "final":  # DRAM bytes per final trial from the ncu capture, x trials per launch
+        traffic = UNION_DRAM_BYTES_PER_TRIAL * trials / dom_launches
     out = {
         "metric": METRIC,
         "value": world * trials / (ms_per_step * 1e-3),
@@ -283,16 +294,23 @@ def bench_gpu(args) -> dict | None:
                    "l2": "inputs larger than L2 (>51 GB read per step)",
                    "parallelism": f"replicas x{world}"},
         "phases_ms": {k: v / args.steps for k, v in phases.items()},
-        "roofline": {"kernel": {"brutefold": "brutefold_kernel (+phase_map)",
-                                "levels": "ffa_level_kernel (levels 1..7)",
-                                "final": "ffa_level_kernel bands + ffa_level_score_kernel"}[dom],
+        "roofline": {"kernel": {"brutefold": "brutefold_seq_kernel (+phase_map_kernel)",
+                                "levels": "ffa_level64_kernel (materialised levels)",
+                                "final": "band_union64_kernel (penultimate band + fused "
+                                         "final-level scoring)"}[dom],
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes": ab, "traffic": None},
+                     "launches_per_step": dom_launches,
+                     "algorithmic_bytes_per_launch": ab / dom_launches,
+                     "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read+write of band_union64_kernel at "
+                                       "2^21 samples, scaled per final trial"
+                                       if traffic is not None else None},
         "e2e": {"value": world * trials / (e2e_ms * 1e-3), "unit": "trials/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 4 * cfg.nsamps,
                 "d2h_bytes_per_step": 8 + 4},
-        "gpu_launches": launches,
+        "gpu_launches": sum(phase_launches.values()),
+        "gpu_launches_per_step": {k: v // args.steps for k, v in phase_launches.items()},
         "clocks": clocks.summary(),
         "best_candidate": {k: float(v) for k, v in best.items()},
     }

@@ -86,6 +86,9 @@ typedef struct {
 /* ---- library ---------------------------------------------------------- */
 int loki_version(void);
 const char* loki_last_error(void);
+/* Kernels this library has enqueued from the calling host thread so far
+ * (monotone). No reference counterpart: it lets a caller count launches. */
+int64_t loki_launch_count(void);
 
 /* ---- FFA (time domain, float32) --------------------------------------- */
 

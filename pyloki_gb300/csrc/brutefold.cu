@@ -178,6 +178,8 @@ extern "C" int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsam
     const int mblocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 64);
     const int64_t blocks = nseg * ((nf + bs - 1) / bs);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    note_launch();
+    note_launch();
     if (elem == 1) {
       uint8_t* map = (uint8_t*)phase_scratch;
       phase_map_kernel<uint8_t><<<mblocks, 256, 0, s>>>(freqs + f0, nf, segment_len, nbins,

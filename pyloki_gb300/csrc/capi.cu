@@ -7,6 +7,9 @@
 namespace loki {
 
 static thread_local char g_last_error[512] = "";
+static thread_local long long g_launches = 0;
+
+void note_launch() { ++g_launches; }
 
 int set_error(int code, const char* fmt, ...) {
   va_list ap;
@@ -28,3 +31,5 @@ int check_launch(const char* what) {
 extern "C" int loki_version(void) { return 1; }
 
 extern "C" const char* loki_last_error(void) { return loki::g_last_error; }
+
+extern "C" int64_t loki_launch_count(void) { return loki::g_launches; }

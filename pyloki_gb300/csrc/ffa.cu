@@ -552,6 +552,7 @@ static int launch_level(const LokiFFALevel& L, const LevelK& K, const float* in,
   const int64_t Q = n_out_params(L);
   const int64_t blocks = (Q + kLevelWarps * 32 - 1) / (kLevelWarps * 32);
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+  note_launch();
   if (L.nbins == 64 && aligned16(in) && aligned16(out))
     ffa_level64_kernel<<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
                                                                      n_other);
@@ -576,6 +577,7 @@ static int launch_level_score(const LokiFFALevel& L, const LevelK& K, const floa
   const int64_t Q = n_out_params(L);
   const int64_t blocks = (Q + warps * 32 - 1) / (warps * 32);
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+  note_launch();
   kern<<<(unsigned)blocks, warps * 32, smem, s>>>(L, K, in, sp, SK, snr, err, gtab, n_other);
   return LOKI_OK;
 }
@@ -612,6 +614,7 @@ extern "C" int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords, int3
   if (!coords || !dev_err) return set_error(LOKI_ERR_INVALID, "null output pointer");
   const int64_t Q = n_out_params(*lvl);
   const int blocks = (int)std::min<int64_t>((Q + 255) / 256, 152 * 32);
+  note_launch();
   ffa_plan_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(*lvl, coords, dev_err);
   return check_launch("ffa_plan");
 }
@@ -660,6 +663,7 @@ extern "C" int loki_ffa_band_windows(const LokiFFALevel* lvl, int64_t band_width
     return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
   const int64_t total = nbands * n_other;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  note_launch();
   ffa_band_window_kernel<<<blocks, 256, 0, s>>>(*lvl, band_width, nbands,
                                                 (unsigned long long*)win_lo,
                                                 (unsigned long long*)win_hi);
@@ -702,6 +706,8 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
   OtherRes* tab_p = reinterpret_cast<OtherRes*>(scratch + band_floats);
   OtherRes* tab_f = reinterpret_cast<OtherRes*>(scratch + band_floats + table_floats(*pen));
   const int64_t no_p = n_other_of(*pen), no_f = n_other_of(*fin);
+  note_launch();
+  note_launch();
   other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_p + 127) / 128, 1024), 128, 0, s>>>(
       *pen, KP, tab_p, no_p);
   other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_f + 127) / 128, 1024), 128, 0, s>>>(
@@ -747,6 +753,7 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
         nblk_p = (n_out_params(P) + kScoreWarps * 32 - 1) / (kScoreWarps * 32);
       }
       if (nblk_f + nblk_p > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+      note_launch();
       band_union64_kernel<<<(unsigned)(nblk_f + nblk_p), kScoreWarps * 32, smem, s>>>(
           F, KF, buf[k & 1], *spec, SK, snr, tab_f, no_f, nblk_f, P, KP, fold_pp,
           buf[(k + 1) & 1], tab_p, no_p, dev_err);

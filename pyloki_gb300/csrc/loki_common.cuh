@@ -21,6 +21,8 @@ namespace loki {
 // Host-side error recording (defined in capi.cu).
 int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
+// Counts one kernel launch of this host thread (read by loki_launch_count).
+void note_launch();
 
 // Division by a runtime-constant 32-bit divisor d >= 1 with a precomputed
 // multiplier (Granlund & Montgomery 1994): q = (t + ((n - t) >> 1)) >> (l - 1),

@@ -122,6 +122,7 @@ static int exclusive_scan(const void* in, int64_t n, double thr, int64_t* out, v
       return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
     return LOKI_OK;
   }
+  for (int i = 0; i < 3; ++i) note_launch();
   scan_block_kernel<FLAGS><<<(unsigned)nblocks, kScanBlock, 0, s>>>(in, n, thr, out, sums);
   scan_sums_kernel<<<1, kScanBlock, 0, s>>>(sums, nblocks, out + n);
   scan_add_kernel<<<(unsigned)nblocks, kScanBlock, 0, s>>>(out, n, sums);
@@ -741,6 +742,7 @@ extern "C" int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves
   cudaStream_t s = (cudaStream_t)stream;
   if (n_parents > 0) {
     // child counts go to offsets[0..n), scanned in place
+    note_launch();
     prune_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
         *lvl, leaves, n_parents, info, offsets, dev_err);
     rc = check_launch("prune_branch");
@@ -764,6 +766,7 @@ extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
   if (!score_minmax || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
   cudaStream_t s = (cudaStream_t)stream;
   unsigned* keys = reinterpret_cast<unsigned*>(score_minmax);  // reused as ordered keys
+  note_launch();
   minmax_init_kernel<<<1, 1, 0, s>>>(keys);
   if (n_children > 0) {
     if (!leaves || !folds || !info || !offsets || !fold_segment || !child_scores ||
@@ -781,10 +784,12 @@ extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     const int64_t blocks = (n_children + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    note_launch();
     prune_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
         *lvl, leaves, folds, n_parents, info, offsets, n_children, fold_segment, sp, SK,
         child_scores, child_idx, child_phase, keys);
   }
+  note_launch();
   minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
   return check_launch("prune_score");
 }
@@ -807,6 +812,7 @@ extern "C" int loki_prune_select(const float* child_scores, int64_t n_children,
   int rc = exclusive_scan<true>(child_scores, n_children, threshold, pos, scan_scratch,
                                 sums_bytes, s);
   if (rc) return rc;
+  if (n_children > 0) note_launch();
   if (n_children > 0)
     select_scatter_kernel<<<(unsigned)((n_children + 255) / 256), 256, 0, s>>>(
         child_scores, n_children, threshold, pos, surv_ids);
@@ -827,6 +833,7 @@ extern "C" int loki_prune_select_overflow(const float* child_scores, const int64
   if (!child_scores || !offsets || !surv_ids || !n_surv || !thr_out || !scratch_ids ||
       !scratch_keys)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
   select_overflow_kernel<<<1, kSelThreads, 0, (cudaStream_t)stream>>>(
       child_scores, offsets, n_parents, batch_size, threshold, capacity, surv_ids, n_surv,
       thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys));
@@ -850,6 +857,7 @@ extern "C" int loki_prune_emit(const LokiPruneLevel* lvl, const double* leaves,
       !scores_ep_out || !bt_out)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const int64_t blocks = (n_surv + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  note_launch();
   prune_emit_kernel<<<(unsigned)blocks, kPruneWarps * 32, 0, (cudaStream_t)stream>>>(
       *lvl, leaves, folds, info, offsets, n_parents, fold_segment, surv_ids, n_surv,
       child_scores, child_idx, child_phase, leaves_out, folds_out, scores_out, scores_ep_out,
@@ -882,6 +890,7 @@ extern "C" int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves
                            smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t blocks = (n + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  note_launch();
   prune_ascend_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, (cudaStream_t)stream>>>(
       *lvl, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa_fold,
       seg_stride, sp, SK);

@@ -72,6 +72,7 @@ static int launch_score(const float* in, int64_t nprof, int nbins, LokiScoreSpec
   const int64_t blocks = (nw + warps - 1) / warps;
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
   const ScoreK SK = make_score_k(sp, nbins);
+  note_launch();
   score_kernel<FROM_EV><<<(unsigned)blocks, warps * 32, smem, s>>>(in, nprof, nbins, sp, SK, out);
   return check_launch(what);
 }
@@ -126,6 +127,7 @@ extern "C" int loki_fold_norm(const float* folds, int64_t n, int32_t nbins, floa
   if (!folds || !out) return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const int64_t total = n * nbins;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 152 * 32);
+  note_launch();
   fold_norm_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(folds, n, nbins, out);
   return check_launch("fold_norm");
 }

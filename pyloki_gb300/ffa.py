@@ -131,6 +131,8 @@ class DynamicProgramming:
         self.phase_scratch_bytes = _GIB
         #: kernels launched by this object (brute fold, levels, bands, scoring)
         self.launches = 0
+        #: library launch counter at the phase marks of the last search()
+        self.phase_marks: dict[str, int] = {}
 
     # ---- reference properties ------------------------------------------------
     @property
@@ -298,6 +300,7 @@ class DynamicProgramming:
         nout = len(widths) if mode == 0 else 1
 
         def mark(name: str) -> None:
+            self.phase_marks[name] = self._lib.loki_launch_count()
             if phase_events is not None:
                 ev = torch.cuda.Event(enable_timing=True)
                 ev.record(torch.cuda.current_stream(self._device))
@@ -383,11 +386,12 @@ class DynamicProgramming:
         scratch = torch.empty(nfl, dtype=torch.float32, device=self._device)
         lo = np.ascontiguousarray(lo, np.int64)
         hi = np.ascontiguousarray(hi, np.int64)
+        before = self._lib.loki_launch_count()
         _lib.check(self._lib.loki_ffa_final_banded(
             d_pen, d_fin, width, lo.ctypes.data, hi.ctypes.data, _lib.ptr(self.fold),
             _lib.ptr(scratch), scratch.numel(), spec, _lib.ptr(snr), _lib.ptr(self._err),
             self._stream()))
-        self.launches += 2 * len(lo)
+        self.launches += self._lib.loki_launch_count() - before
 
 
 _BAND_CACHE: dict[tuple, tuple] = {}
