@@ -16,6 +16,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "loki_oracle.c"
+SOURCES = (SRC, HERE / "prune_oracle.c")
 LIB = HERE / "libloki_oracle.so"
 CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
           "-std=c11"]
@@ -28,9 +29,10 @@ _D = C.c_double
 
 
 def build(force: bool = False) -> Path:
-    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+    newest = max(s.stat().st_mtime for s in SOURCES)
+    if force or not LIB.exists() or LIB.stat().st_mtime < newest:
         tmp = str(LIB) + f".{os.getpid()}.tmp"
-        subprocess.run(["gcc", *CFLAGS, str(SRC), "-o", tmp, "-lm"], check=True)
+        subprocess.run(["gcc", *CFLAGS, *map(str, SOURCES), "-o", tmp, "-lm"], check=True)
         os.replace(tmp, LIB)
     return LIB
 

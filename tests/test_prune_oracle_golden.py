@@ -1,0 +1,66 @@
+"""The CPU pruning oracle against runs of the pyloki reference (no GPU).
+
+Same fixtures and the same per-level checks as the GPU pruning tests: the
+oracle is pinned to the reference before it is used to check anything else.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.conftest import load_golden
+
+CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
+         "prune_taylor_overflow"]
+TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature"}
+
+
+def _run(name):
+    from oracle.prune_oracle import PruneRun
+    from pyloki_gb300.config import PulsarSearchConfig
+
+    d = load_golden(name)
+    cfg = PulsarSearchConfig(
+        nsamps=int(d["nsamps"]), tsamp=float(d["tsamp"]), nbins=int(d["nbins"]),
+        eta=float(d["eta"]), param_limits=d["param_limits"], ducy_max=float(d["ducy_max"]),
+        wtsp=float(d["wtsp"]), use_fourier=False, bseg_ffa=int(d["bseg_ffa"]),
+        prune_poly_order=int(d["poly_order"]), branch_max=int(d["branch_max"]),
+        tiling_strategy=TILING.get(name, "aggressive"))
+    n = cfg.niters_ffa
+    param_arr = cfg.get_param_arr(cfg.get_dparams(n))
+    run = PruneRun(cfg, d["fold_ffa"], param_arr, cfg.get_dparams_actual(n), d["thresholds"],
+                   max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]),
+                   moving=bool(d["moving"]), nthreads=2)
+    return d, run
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_prune_oracle_matches_reference(name):
+    d, run = _run(name)
+    run.seed(int(d["ref_seg"]))
+    np.testing.assert_array_equal(run.scheme.data, d["scheme"])
+    np.testing.assert_allclose(run.leaves, d["seed_leaves"], rtol=1e-13, atol=0)
+    np.testing.assert_array_equal(run.scores, d["seed_scores"])
+    nparams = run.cfg.nparams
+    for lvl in range(1, int(d["levels_done"]) + 1):
+        assert run.step() or lvl == int(d["levels_done"])
+        n_br, n_l, n_phy, n_s = run.stats[-1]
+        np.testing.assert_array_equal([n_br, n_l, n_phy, n_s], d[f"stats_{lvl}"],
+                                      err_msg=f"stats level {lvl}")
+        np.testing.assert_array_equal(
+            run.smm[-1], d[f"smm_{lvl}"].astype(np.float32).astype(np.float64),
+            err_msg=f"score min/max level {lvl}")
+        np.testing.assert_array_equal(run.scores, d[f"scores_{lvl}"], err_msg=f"level {lvl}")
+        if f"leaves_{lvl}" in d:
+            np.testing.assert_allclose(run.leaves, d[f"leaves_{lvl}"], rtol=1e-13, atol=0)
+            bt = run.backtracks
+            got = np.concatenate([bt[:, : nparams + 1], bt[:, -1:]], axis=1)
+            np.testing.assert_array_equal(got, d[f"bt_{lvl}"], err_msg=f"bt level {lvl}")
+        if f"folds_{lvl}" in d:
+            np.testing.assert_array_equal(run.folds, d[f"folds_{lvl}"])
+    run.ascend()
+    np.testing.assert_array_equal(run.scores, d["asc_scores"])
+    np.testing.assert_array_equal(run.scores_ep, d["asc_scores_ep"])
+    if "asc_folds" in d:
+        np.testing.assert_array_equal(run.folds, d["asc_folds"])
