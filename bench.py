@@ -65,6 +65,164 @@ def cpu_band_cfg(band_hz: float):
     return make_cfg(500.0 - band_hz, 500.0)
 
 
+PRUNE_WORKLOAD = "taylor4_prune_circular_orbit_2^22"
+PRUNE_MAX_SUGG = 2**18
+PRUNE_BATCH = 1024
+PRUNE_THRESHOLD_FINAL = 4.0
+# HBM bytes per leaf of prune_score_kernel: the parent fold (2 x 64 f32) read
+# once, the score (f32), grid indices (2 x i32) and phase (f64) written. The
+# added segment's fold (146 rows, 75 KB) stays in L2.
+PRUNE_SCORE_BYTES_PER_LEAF = 2 * 64 * 4 + 4 + 8 + 8
+
+
+def make_prune_cfg():
+    """Circular-orbit search with a Taylor tree to the 4th derivative: 2^22
+    samples at 64 us, 128 segments, 64 bins, FFA grid (1, 1, 1, 146)."""
+    from pyloki_gb300 import ParamLimits, PulsarSearchConfig
+
+    n = 2**22
+    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=4)
+    return PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
+                              param_limits=lim.limits, use_fourier=False, bseg_ffa=n // 128,
+                              prune_poly_order=4)
+
+
+def make_prune_series(seed: int):
+    """3 ms pulsar (S/N 10) in a circular orbit: P_orb 2-10 h, projected
+    semi-major axis 0.1-2 lt-s, orbital phase uniform; all drawn from ``seed``."""
+    from pyloki_gb300.simulation import make_series as ms
+
+    rng = np.random.default_rng(seed)
+    orbit = (rng.uniform(2.0, 10.0) * 3600.0, rng.uniform(0.1, 2.0), rng.uniform(0, 2 * np.pi))
+    return ms(2**22, 64e-6, freq=333.33, snr=10.0, orbit=orbit, seed=seed), orbit
+
+
+def prune_thresholds(nseg: int, final: float = PRUNE_THRESHOLD_FINAL) -> np.ndarray:
+    """Per-level thresholds rising as sqrt(segments folded), reaching ``final``."""
+    return final * np.sqrt(np.arange(1, nseg) / (nseg - 1))
+
+
+def prune_cpu(nthreads: int = 0) -> dict:
+    """The same pruning run on the CPU oracle (all host threads)."""
+    from oracle import oracle as O
+    from oracle.prune_oracle import PruneRun
+
+    cfg = make_prune_cfg()
+    ts, _ = make_prune_series(seed=2000)
+    fold = O.ffa_execute(ts.ts_e, ts.ts_v, cfg, nthreads)
+    n = cfg.niters_ffa
+    nseg = fold.shape[0]
+    run = PruneRun(cfg, fold, cfg.get_param_arr(cfg.get_dparams(n)), cfg.get_dparams_actual(n),
+                   prune_thresholds(nseg), max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH,
+                   nthreads=nthreads)
+    dt = run.run(nseg // 2)
+    return {"value": run.n_leaves_total / dt, "unit": "leaves/s", "cores": O.max_threads(),
+            "kind": "port", "leaves": run.n_leaves_total, "seconds": dt,
+            "sample": f"one full run ({nseg - 1} levels, ref segment {nseg // 2})"}
+
+
+def bench_prune_gpu(args, dev) -> dict:
+    """Prune leaves/s of one enumerate-prune run per step (device-resident
+    FFA fold), plus the same run end to end from a pinned host series."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import Pruning
+    from pyloki_gb300.timeseries import TimeSeries
+
+    from pyloki_gb300 import _lib
+
+    lib = _lib.load()
+    cfg = make_prune_cfg()
+    ts_host, orbit = make_prune_series(seed=2000)
+    e_pin = torch.from_numpy(ts_host.ts_e).pin_memory()
+    v_pin = torch.from_numpy(ts_host.ts_v).pin_memory()
+    dyp = DynamicProgramming(TimeSeries(e_pin.to(dev), v_pin.to(dev), cfg.tsamp), cfg,
+                             device=dev)
+    dyp.initialize()
+    dyp.execute()
+    nseg = dyp.nsegments
+    thr = prune_thresholds(nseg)
+    ref = nseg // 2
+    prn = Pruning(dyp, thr, max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
+
+    def one_run(events=None) -> int:
+        prn.score_events = events
+        prn.initialize(ref)
+        for _ in range(nseg - 1):
+            prn.execute_iter()
+            if prn.prune_complete:
+                break
+        prn._do_ascend()
+        return sum(st.n_leaves for st in prn.pstats[1:])
+
+    for _ in range(args.warmup):
+        one_run()
+    torch.cuda.synchronize(dev)
+    leaves = 0
+    score_events: list = []
+    c0 = lib.loki_launch_count()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(args.steps):
+        leaves += one_run(score_events)
+    end.record()
+    torch.cuda.synchronize(dev)
+    launches = lib.loki_launch_count() - c0
+    ms = start.elapsed_time(end)
+    score_ms = sum(e0.elapsed_time(e1) for _, e0, e1 in score_events)
+    score_leaves = sum(n for n, _, _ in score_events)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = score_leaves * PRUNE_SCORE_BYTES_PER_LEAF / (score_ms * 1e-3) / 1e9
+    survivors = int(prn.world_tree.valid_size)
+    best = float(prn.world_tree.scores.max().item()) if survivors else float("nan")
+
+    # end to end: pinned host series -> FFA -> pruning run -> results on the host
+    from pyloki_gb300.timeseries import TimeSeries as TS
+
+    host_ts = TS(e_pin, v_pin, cfg.tsamp)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    d2h = 0
+    e2e_leaves = 0
+    for _ in range(args.steps):
+        dp = DynamicProgramming(host_ts, cfg, device=dev)
+        dp.initialize()
+        dp.execute()
+        pr = Pruning(dp, thr, max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
+        res = pr.execute(ref)
+        e2e_leaves += sum(st.n_leaves for st in res["level_stats"][1:])
+        d2h = res["param_sets"].nbytes + res["scores"].nbytes + res["scores_ep"].nbytes
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    return {
+        "metric": "prune leaves/s", "value": leaves / (ms * 1e-3), "unit": "leaves/s",
+        "ms_per_step": ms / args.steps, "leaves_per_step": leaves // args.steps,
+        "dtype": "f32 folds, f64 parameters",
+        "data": "synthetic (seeded N(0,1) noise + 3 ms pulsar in a circular orbit, S/N 10)",
+        "config": {"workload": PRUNE_WORKLOAD, "nsamps": cfg.nsamps, "tsamp": cfg.tsamp,
+                   "nbins": cfg.nbins, "poly_order": 4, "segments": nseg,
+                   "ffa_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
+                   "widths": cfg.score_widths.tolist(), "max_sugg": PRUNE_MAX_SUGG,
+                   "batch_size": PRUNE_BATCH, "ref_segment": ref,
+                   "thresholds": f"{PRUNE_THRESHOLD_FINAL} * sqrt(level / {nseg - 1})",
+                   "orbit": {"p_orb_h": orbit[0] / 3600, "x_lts": orbit[1], "psi": orbit[2]},
+                   "l2": "segment folds (75 KB) are L2-resident; tree folds stream"},
+        "roofline": {"kernel": "prune_score_kernel (resolve + gather + shift-add + score)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "bytes_per_leaf": PRUNE_SCORE_BYTES_PER_LEAF,
+                     "kernel_ms_per_step": score_ms / args.steps,
+                     "launches_per_step": len(score_events) // args.steps, "traffic": None},
+        "e2e": {"value": e2e_leaves / e2e_s, "unit": "leaves/s",
+                "ms_per_step": e2e_s * 1e3 / args.steps, "h2d_bytes_per_step": 8 * cfg.nsamps,
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "survivors": survivors, "best_score": best,
+    }
+
+
 def final_trials(cfg) -> int:
     return int(np.prod(cfg.get_param_grid_count(cfg.niters_ffa)))
 
@@ -325,6 +483,10 @@ def bench_gpu(args) -> dict | None:
                                "sample": f"same search restricted to "
                                          f"{500 - args.cpu_band_hz:g}-500 Hz ({nt} trials, "
                                          f"{dt:.1f} s)"}
+    if not args.no_prune:
+        out["prune"] = bench_prune_gpu(args, dev)
+        if world == 1 and not args.no_cpu_baseline:
+            out["prune"]["cpu_baseline"] = prune_cpu()
     if dist is not None:
         dist.destroy_process_group()
     return out
@@ -361,6 +523,13 @@ def bench_reference(args) -> dict | None:
         "e2e": {"value": value, "unit": "trials/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if not args.no_prune:
+        p = prune_cpu()
+        out["prune"] = {"metric": "prune leaves/s", "value": p["value"], "unit": "leaves/s",
+                        "config": {"workload": PRUNE_WORKLOAD}, "cpu_baseline": p,
+                        "e2e": {"value": p["value"], "unit": "leaves/s",
+                                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out
 
 
 def profile_once(args) -> None:
@@ -396,6 +565,8 @@ def main() -> None:
     ap.add_argument("--band-bytes", type=int, default=96 << 20)
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-prune", action="store_true",
+                    help="skip the enumerate-prune (leaves/s) measurement")
     ap.add_argument("--profile-once", action="store_true",
                     help="run exactly one search (for ncu captures) and exit")
     ap.add_argument("--nsamps-log2", type=int, default=23,

@@ -219,6 +219,9 @@ class Pruning:
         self.param_grid_count_init = np.asarray(dyp.param_grid_count, np.int64)
         #: kernels launched by this object
         self.launches = 0
+        #: if a list, every level appends (start, end) CUDA events recorded on
+        #: the launch stream around its loki_prune_score call
+        self.score_events: list | None = None
 
     # ---- reference properties -----------------------------------------------
     @property
@@ -399,11 +402,18 @@ class Pruning:
         cidx = self._buf.get("cidx", 2 * n_child, torch.int32)
         cphase = self._buf.get("cphase", n_child, torch.float64)
         minmax = self._buf.get("minmax", 2, torch.float32)
+        if self.score_events is not None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(torch.cuda.current_stream(self._device))
         _lib.check(lib.loki_prune_score(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par,
                                         _lib.ptr(info), _lib.ptr(offsets), n_child,
                                         _lib.ptr(fold_segment), self.spec, _lib.ptr(scores),
                                         _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(minmax),
                                         _lib.ptr(self._err), stream))
+        if self.score_events is not None:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(torch.cuda.current_stream(self._device))
+            self.score_events.append((n_child, e0, e1))
         ssb = int(lib.loki_scan_scratch_bytes(n_child)) + 8 * (n_child + 1)
         sscan = self._buf.get("sscan", ssb, torch.uint8)
         surv = self._buf.get("surv", max(n_child, 1), torch.int64)
