@@ -174,7 +174,7 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
 int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                       int64_t max_window);
 
-/* ---- enumerate-prune (Taylor basis, float32 folds) -------------------- */
+/* ---- enumerate-prune (Taylor / Chebyshev basis, float32 folds) -------- */
 
 /* Constants of one pruning level, computed by the host with the reference's
  * numpy expressions (prune.py:165-332 with core/taylor.py:68-339):
@@ -198,6 +198,24 @@ typedef struct {
   int64_t n_accel, n_freq;          /* FFA grid counts of the accel / freq axes */
   double accel_min, accel_inv;      /* accel_inv = n_accel / range, 0 if flat */
   double freq_min, freq_inv;
+  /* Chebyshev basis (core/chebyshev.py; basis = 1). Leaves then hold
+   * coefficients [alpha_P .. alpha_0]; every matrix M below is applied as
+   * y_i = sum_j x_j M[i][j] with forward fused multiply-adds, i.e. the host
+   * passes the transpose of the reference's right-hand matrix:
+   *   tm_b  = C(prev -> cur)^T        parent shift before branching
+   *   tm_be = |C|^T or (C**2)^T       its error matrix (tiling 2 / 1)
+   *   tm_a, tm_i = C(cur -> t_add / t_init, same scale)^T   (resolve)
+   *   tm_n, tm_e = C(cur -> next)^T and its error matrix   (transform)
+   *   tm_r  = R^T (Chebyshev -> power series connection matrix)
+   * and the Taylor value of order k is (d_k * cfact[k]) / ctsk[k]. For the
+   * Taylor basis (basis = 0) these fields are ignored. */
+  int32_t basis;
+  int32_t reserved2;
+  double tm_b[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1];
+  double tm_be[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1];
+  double tm_r[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1];
+  double cfact[LOKI_MAX_PARAMS + 1];  /* k! */
+  double ctsk[LOKI_MAX_PARAMS + 1];   /* scale**k */
 } LokiPruneLevel;
 
 /* Per-parent branching result. */
@@ -205,7 +223,8 @@ typedef struct {
   double first[LOKI_MAX_PARAMS];  /* first child centre (or the parent value) */
   double dact[LOKI_MAX_PARAMS];   /* actual child step (or the parent step) */
   int32_t count[LOKI_MAX_PARAMS];
-  int32_t reserved[3];
+  int32_t reserved;
+  double d0;                      /* the children's lowest-order value */
 } LokiBranchInfo;
 
 /* Branch every parent (core/taylor.py:68-169 poly_taylor_branch_batch):

@@ -94,6 +94,13 @@ class LokiPruneLevel(C.Structure):
         ("accel_inv", C.c_double),
         ("freq_min", C.c_double),
         ("freq_inv", C.c_double),
+        ("basis", C.c_int32),
+        ("reserved2", C.c_int32),
+        ("tm_b", _M6),
+        ("tm_be", _M6),
+        ("tm_r", _M6),
+        ("cfact", C.c_double * (MAX_PARAMS + 1)),
+        ("ctsk", C.c_double * (MAX_PARAMS + 1)),
     ]
 
 
@@ -102,7 +109,8 @@ class LokiBranchInfo(C.Structure):
         ("first", C.c_double * MAX_PARAMS),
         ("dact", C.c_double * MAX_PARAMS),
         ("count", C.c_int32 * MAX_PARAMS),
-        ("reserved", C.c_int32 * 3),
+        ("reserved", C.c_int32),
+        ("d0", C.c_double),
     ]
 
 

@@ -168,13 +168,53 @@ struct ChildRes {
   double phase;
 };
 
+// cheby_to_taylor (utils/transforms.py:556-583) of coefficients a[0..P]
+// (alpha_P..alpha_0), lowest three Taylor orders only: d_k =
+// ((rev(a) @ R)[k] * k!) / scale**k for k = 2 (accel), 1 (velocity), 0 (delay).
+__device__ __forceinline__ void cheby_low3(const LokiPruneLevel& D, const double* a, int m,
+                                           double* d2, double* d1, double* d0) {
+  double ar[LOKI_MAX_PARAMS + 1];
+  for (int i = 0; i < m; ++i) ar[i] = a[m - 1 - i];
+  double d[3];
+  for (int k = 0; k < 3; ++k)
+    d[k] = __ddiv_rn(__dmul_rn(tdot(ar, D.tm_r, k, m), D.cfact[k]), D.ctsk[k]);
+  *d0 = d[0];
+  *d1 = d[1];
+  *d2 = d[2];
+}
+
+// Chebyshev resolve (core/chebyshev.py:180-277): shift the coefficients to
+// t_add (and t_init on the moving grid) at the current scale, then read the
+// Taylor accel / velocity / delay there.
+__device__ __forceinline__ void cheby_kinematics(const LokiPruneLevel& D, const double* pv,
+                                                 double* accel, double* vel, double* dd) {
+  const int m = D.poly_order + 1;
+  double a[LOKI_MAX_PARAMS + 1];
+  for (int i = 0; i < m; ++i) a[i] = tdot(pv, D.tm_a, i, m);
+  double a2, a1, a0;
+  cheby_low3(D, a, m, &a2, &a1, &a0);
+  *accel = a2;
+  if (D.moving) {
+    for (int i = 0; i < m; ++i) a[i] = tdot(pv, D.tm_i, i, m);
+    double i2, i1, i0;
+    cheby_low3(D, a, m, &i2, &i1, &i0);
+    *vel = __dsub_rn(a1, i1);
+    *dd = __dsub_rn(a0, i0);
+  } else {
+    *vel = a1;
+    *dd = a0;
+  }
+}
+
 // poly_taylor_resolve_batch (moving) / poly_taylor_fixed_resolve_batch
 // (core/taylor.py:172-277) for one child with params pv[0..P] (d_P..d_1, d_0).
 __device__ __forceinline__ ChildRes resolve_child(const LokiPruneLevel& D, const double* pv,
                                                   double f0) {
   const int P = D.poly_order, m = P + 1;
   double accel, vel, dd;
-  if (D.moving) {
+  if (D.basis == 1) {
+    cheby_kinematics(D, pv, &accel, &vel, &dd);
+  } else if (D.moving) {
     accel = tdot(pv, D.tm_a, P - 2, m);
     vel = __dsub_rn(tdot(pv, D.tm_a, P - 1, m), tdot(pv, D.tm_i, P - 1, m));
     dd = __dsub_rn(tdot(pv, D.tm_a, P, m), tdot(pv, D.tm_i, P, m));
@@ -201,14 +241,41 @@ __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__
                                     int64_t* __restrict__ counts, int32_t* __restrict__ err) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int P = D.poly_order;
+  const int P = D.poly_order, m = P + 1;
   const double* lf = leaves + i * (P + 2) * 2;
   const double f0 = lf[(P + 1) * 2];
   const double fscale = __ddiv_rn(f0, LOKI_C_VAL);
+  // Parent values and errors in the current domain: as stored (Taylor), or
+  // shifted from the previous to the current Chebyshev domain with
+  // shift_cheby_full (utils/transforms.py:650-701).
+  double pval[LOKI_MAX_PARAMS + 1], perr[LOKI_MAX_PARAMS + 1];
+  if (D.basis == 1) {
+    double raw[LOKI_MAX_PARAMS + 1], rawe[LOKI_MAX_PARAMS + 1];
+    for (int k = 0; k < m; ++k) {
+      raw[k] = lf[2 * k];
+      rawe[k] = lf[2 * k + 1];
+    }
+    for (int k = 0; k < m; ++k) pval[k] = tdot(raw, D.tm_b, k, m);
+    if (D.tiling == 0) {
+      for (int k = 0; k < m; ++k) perr[k] = __dmul_rn(rawe[k], fabs(D.tm_b[k][k]));
+    } else if (D.tiling == 2) {
+      for (int k = 0; k < m; ++k) perr[k] = tdot(rawe, D.tm_be, k, m);
+    } else {
+      double e2[LOKI_MAX_PARAMS + 1];
+      for (int k = 0; k < m; ++k) e2[k] = __dmul_rn(rawe[k], rawe[k]);
+      for (int k = 0; k < m; ++k) perr[k] = __dsqrt_rn(tdot(e2, D.tm_be, k, m));
+    }
+  } else {
+    for (int k = 0; k < m; ++k) {
+      pval[k] = lf[2 * k];
+      perr[k] = lf[2 * k + 1];
+    }
+  }
   LokiBranchInfo B;
+  B.d0 = pval[P];
   int64_t total = 1;
   for (int j = 0; j < P; ++j) {
-    const double pcur = lf[2 * j], dcur = lf[2 * j + 1];
+    const double pcur = pval[j], dcur = perr[j];
     const double dnew = __ddiv_rn(D.dfc[j], f0);
     const double fb = __dmul_rn(D.fac[j], fscale);
     const double shift = __dmul_rn(fabs(__dsub_rn(dcur, dnew)), fb);
@@ -292,7 +359,7 @@ prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     const double* lf = leaves + par * (P + 2) * 2;
     double pv[LOKI_MAX_PARAMS + 1];
     child_params(B, P, c - offsets[par], pv);
-    pv[P] = lf[P * 2];  // d_0
+    pv[P] = B.d0;  // d_0 (alpha_0 in the current domain for Chebyshev)
     const ChildRes r = resolve_child(D, pv, lf[(P + 1) * 2]);
     cidx[2 * c] = r.ia;
     cidx[2 * c + 1] = r.iff;
@@ -560,7 +627,7 @@ prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     const double* lf = leaves + par * (P + 2) * 2;
     double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
     child_params(B, P, c - offsets[par], pv);
-    pv[P] = lf[P * 2];
+    pv[P] = B.d0;
     for (int j = 0; j < P; ++j) ev[j] = B.dact[j];
     ev[P] = 0.0;
     double* lo = lout + s * (P + 2) * 2;
@@ -650,10 +717,18 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     int64_t my_row = 0;
     int my_shift = 0;
     if (lane < kmax) {
-      const double accel = tdot(pv, T, P - 2, m);
-      const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(tdot(pv, T, P - 1, m),
-                                                               LOKI_C_VAL)));
-      const double delay = __ddiv_rn(tdot(pv, T, P, m), LOKI_C_VAL);
+      double accel, vel, dd;
+      if (D.basis == 1) {  // core/chebyshev.py:280-320: shift to t0_seg, then Taylor
+        double a[LOKI_MAX_PARAMS + 1];
+        for (int i = 0; i < m; ++i) a[i] = tdot(pv, T, i, m);
+        cheby_low3(D, a, m, &accel, &vel, &dd);
+      } else {
+        accel = tdot(pv, T, P - 2, m);
+        vel = tdot(pv, T, P - 1, m);
+        dd = tdot(pv, T, P, m);
+      }
+      const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(vel, LOKI_C_VAL)));
+      const double delay = __ddiv_rn(dd, LOKI_C_VAL);
       const double ph = phase_idx(dt_seg[sg], f0, nb, delay);
       const int64_t ia = axis_index(accel, D.accel_min, D.accel_inv, D.n_accel);
       const int64_t iff = axis_index(freq, D.freq_min, D.freq_inv, D.n_freq);

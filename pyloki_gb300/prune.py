@@ -27,7 +27,7 @@ from pathlib import Path
 import numpy as np
 import torch
 
-from pyloki_gb300 import _lib
+from pyloki_gb300 import _lib, chebyshev
 from pyloki_gb300.config import C_VAL, FLOAT_EPSILON, fact, poly_taylor_step_f
 from pyloki_gb300.scheme import MiddleOutScheme, determine_ref_segs_pareto
 
@@ -193,9 +193,10 @@ class Pruning:
                        (False, "chebyshev", True), (False, "chebyshev", False)}:
             msg = f"Invalid pruning configuration: {key}"
             raise ValueError(msg)
-        if key != (False, "taylor", False):
-            msg = f"pruning plugin {key} (circular / chebyshev / complex) is not built yet"
+        if key not in {(False, "taylor", False), (False, "chebyshev", False)}:
+            msg = f"pruning plugin {key} (circular / complex) is not built yet"
             raise NotImplementedError(msg)
+        self.poly_basis = poly_basis
         self._dyp = dyp
         self._threshold_scheme = np.asarray(threshold_scheme, dtype=np.float64)
         self._max_sugg = int(max_sugg)
@@ -302,6 +303,8 @@ class Pruning:
         leaves[:, -2, 0] = 0
         leaves[:, -1, 0] = f0
         leaves[:, -1, 1] = 0
+        if self.poly_basis == "chebyshev":  # core/chebyshev.py:14-70
+            leaves = chebyshev.seed_leaves(param_arr, dparams, P, self.scheme.get_coord(0)[1])
         folds = fold_segment.reshape(n, 2, cfg.nbins).contiguous()
         from pyloki_gb300.scoring import snr_score_batch
 
@@ -363,6 +366,8 @@ class Pruning:
         else:
             _set6(d.tm_a, taylor_matrix(coord_add[0] - coord_init[0], P + 1))
         d.dt_phase = coord_add[0] - coord_init[0]
+        if self.poly_basis == "chebyshev":
+            self._cheby_level(d, level, coord_init, coord_cur, coord_next, coord_add)
         counts = self.param_grid_count_init
         lim = cfg.param_limits
         d.n_accel, d.n_freq = int(counts[-2]), int(counts[-1])
@@ -373,6 +378,50 @@ class Pruning:
         d.freq_min = float(f_min)
         d.freq_inv = float(counts[-1] / (f_max - f_min)) if f_max > f_min else 0.0
         return d
+
+    def _cheby_scale(self, d: _lib.LokiPruneLevel, scale: float) -> None:
+        """cheby_to_taylor constants for the domain scale (transforms.py:556-583)."""
+        P = self.poly_order
+        _set6(d.tm_r, chebyshev.conn_matrix_r(P).T)
+        k = np.arange(P + 1, dtype=np.int64)
+        cf, tk = fact(k), scale**k
+        for i in range(P + 1):
+            d.cfact[i] = float(cf[i])
+            d.ctsk[i] = float(tk[i])
+
+    def _cheby_level(self, d: _lib.LokiPruneLevel, level: int, coord_init, coord_cur,
+                     coord_next, coord_add) -> None:
+        """Chebyshev constants of one level (core/chebyshev.py:72-320,
+        utils/psr_utils.py:258-278, utils/transforms.py:650-738)."""
+        cfg = self.dyp.cfg
+        P = self.poly_order
+        moving = self.use_moving_grid
+        tiling = cfg.tiling_strategy
+        d.basis = 1
+        dphi = cfg.eta / cfg.nbins
+        for j in range(P):
+            d.dfc[j] = float((np.zeros(P, np.float64) + dphi)[j] * C_VAL)
+            d.fac[j] = float(cfg.nbins)
+
+        def err_matrix(c: np.ndarray) -> np.ndarray:
+            return (c**2 if tiling == "quadrature" else np.abs(c)).T
+
+        coord_prev = self.scheme.get_previous_coord(level, moving)
+        cb = chebyshev.transform_matrix(P, coord_prev[0], coord_prev[1], coord_cur[0],
+                                        coord_cur[1])
+        _set6(d.tm_b, cb.T)
+        _set6(d.tm_be, err_matrix(cb))
+        t0_cur, s_cur = coord_cur
+        if moving:
+            _set6(d.tm_a, chebyshev.transform_matrix(P, t0_cur, s_cur, coord_add[0], s_cur).T)
+            _set6(d.tm_i, chebyshev.transform_matrix(P, t0_cur, s_cur, coord_init[0], s_cur).T)
+            cn = chebyshev.transform_matrix(P, t0_cur, s_cur, coord_next[0], coord_next[1])
+            _set6(d.tm_n, cn.T)
+            _set6(d.tm_e, err_matrix(cn))
+        else:  # coord_cur is the fixed-grid coordinate (t0_init, scale)
+            _set6(d.tm_a, chebyshev.transform_matrix(P, coord_init[0], s_cur, coord_add[0],
+                                                     s_cur).T)
+        self._cheby_scale(d, s_cur)
 
     # ---- one level (prune.py:615-669) ------------------------------------------
     def execute_iter(self, log_file: Path | None = None) -> None:
@@ -486,9 +535,14 @@ class Pruning:
         nseg = len(seg_idx)
         tm = np.zeros((nseg, 6, 6), np.float64)
         dts = np.zeros(nseg, np.float64)
+        cheby = self.poly_basis == "chebyshev"
         for s in range(nseg):
             dt = seg_coords[s, 0] - coord_end[0]
-            tm[s, : P + 1, : P + 1] = taylor_matrix(dt, P + 1)
+            if cheby:  # core/chebyshev.py:280-320 (shift at the end-domain scale)
+                tm[s, : P + 1, : P + 1] = chebyshev.transform_matrix(
+                    P, coord_end[0], coord_end[1], seg_coords[s, 0], coord_end[1]).T
+            else:
+                tm[s, : P + 1, : P + 1] = taylor_matrix(dt, P + 1)
             dts[s] = dt
         dev = self._device
         tm_d = torch.from_numpy(tm).to(dev)
@@ -497,6 +551,8 @@ class Pruning:
         fold = self.dyp.fold
         stride = int(np.prod(fold.shape[1:]))
         d = self.level_desc(self.prune_level)
+        if cheby:
+            self._cheby_scale(d, coord_end[1])
         wt = self.world_tree
         _lib.check(self._lib.loki_prune_ascend(
             d, _lib.ptr(wt.leaves), _lib.ptr(wt.folds), _lib.ptr(wt.scores),
@@ -505,9 +561,14 @@ class Pruning:
             self._stream()))
         self.launches += 1
 
-    # ---- report (core/taylor.py:342-360) ---------------------------------------
+    # ---- report (core/taylor.py:342-360, dyn_poly_cheby.py:824-840) ------------
     def report(self) -> np.ndarray:
         leaves = self.world_tree.leaves.cpu().numpy()
+        if self.poly_basis == "chebyshev":
+            # The reference's fixed-grid branch computes a shift to the report
+            # domain and discards it, so both grids report the leaves as held.
+            return chebyshev.report_batch(leaves, self.scheme.get_report_coord(
+                self.use_moving_grid))
         return poly_taylor_report_batch(leaves)
 
     def execute(self, ref_seg: int, ascend_levels: list[int] | None = None,

@@ -146,7 +146,7 @@ def prune_series(n: int, tsamp: float, f0: float, accel: float, seed: int):
 def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
                max_sugg: int = 2**16, batch_size: int = 64, ref_seg: int = 8,
                fold_levels: tuple = (5, 11), thr_offset: float = 0.0,
-               leaf_cap: int = 6000) -> None:
+               leaf_cap: int = 6000, basis: str = "taylor") -> None:
     """Taylor (poly_order 3, real folds) enumerate-prune run of 15 levels."""
     import tempfile
 
@@ -166,7 +166,7 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
     dyp.initialize()
     dyp.execute(show_progress=False)
     thr = np.linspace(3.0, 7.5, dyp.nsegments - 1) + thr_offset
-    prn = Pruning(dyp, thr, max_sugg=max_sugg, batch_size=batch_size,
+    prn = Pruning(dyp, thr, max_sugg=max_sugg, batch_size=batch_size, poly_basis=basis,
                   use_moving_grid=moving)
     log = Path(tempfile.mkdtemp()) / "log.txt"
     log.touch()
@@ -174,7 +174,7 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
     out = {"ts_e": ts_e, "ts_v": ts_v, **_cfg_dict(cfg), "thresholds": thr,
            "max_sugg": np.int64(max_sugg), "batch_size": np.int64(batch_size),
            "ref_seg": np.int64(ref_seg), "moving": np.int64(moving),
-           "poly_order": np.int64(3), "branch_max": np.int64(16),
+           "poly_order": np.int64(3), "branch_max": np.int64(16), "basis": np.str_(basis),
            "fold_ffa": np.asarray(dyp.fold), "scheme": prn.scheme.data.copy()}
     wt = prn.world_tree
     out["seed_leaves"] = wt.leaves[: wt.valid_size].copy()
@@ -240,14 +240,28 @@ def main() -> None:
         scoring_case("score_nb64", 64, 512, 0.5, 2.0, 11)
         scoring_case("score_nb50", 50, 256, 0.2, 1.5, 12)
         scoring_case("score_nb100", 100, 128, 0.3, 1.3, 13)
+    if "--cheby-only" in sys.argv:
+        cheby_cases()
+        return
     if "--prune-only" in sys.argv:
         prune_cases()
+        cheby_cases()
         return
     ffa_case("ffa_freq", 2**15, [(10.0, 14.0)], 64, 12.3, 21)
     ffa_case("ffa_accel", 2**15, [(-3.0e5, 3.0e5), (200.0, 202.0)], 64, 201.1, 22)
     ffa_case("ffa_jerk", 2**15, [(-1.0e7, 1.0e7), (-3.0e5, 3.0e5), (200.0, 201.0)],
              50, 200.4, 23, ducy_max=0.2, wtsp=1.5)
     prune_cases()
+    cheby_cases()
+
+
+def cheby_cases() -> None:
+    prune_case("prune_cheby", basis="chebyshev")
+    prune_case("prune_cheby_cons", basis="chebyshev", tiling="conservative", fold_levels=(),
+               thr_offset=1.5)
+    prune_case("prune_cheby_quad", basis="chebyshev", tiling="quadrature", fold_levels=(),
+               thr_offset=1.5)
+    prune_case("prune_cheby_fixed", basis="chebyshev", moving=False, fold_levels=())
 
 
 def prune_cases() -> None:

@@ -16,8 +16,14 @@ from tests.conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
-         "prune_taylor_overflow"]
-TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature"}
+         "prune_taylor_overflow", "prune_cheby", "prune_cheby_fixed", "prune_cheby_cons",
+         "prune_cheby_quad"]
+TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature",
+          "prune_cheby_cons": "conservative", "prune_cheby_quad": "quadrature"}
+
+
+def _basis(d) -> str:
+    return str(d["basis"]) if "basis" in d else "taylor"
 
 
 def _cfg(d, name):
@@ -44,7 +50,8 @@ def _run(name, cuda_device):
     dyp.execute()
     np.testing.assert_array_equal(dyp.fold.cpu().numpy(), d["fold_ffa"])
     prn = Pruning(dyp, d["thresholds"], max_sugg=int(d["max_sugg"]),
-                  batch_size=int(d["batch_size"]), use_moving_grid=bool(d["moving"]))
+                  batch_size=int(d["batch_size"]), poly_basis=_basis(d),
+                  use_moving_grid=bool(d["moving"]))
     return d, prn
 
 
