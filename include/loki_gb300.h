@@ -174,6 +174,34 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
 int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                       int64_t max_window);
 
+/* ---- FFA (Fourier domain, complex64 = 2 x float32 per coefficient) ----
+ * Folds are (nseg, nparams..., 2, nbins / 2 + 1) complex64, nbins even.
+ * The float32 / complex64 arithmetic follows the reference's expressions;
+ * its BLAS, numpy cos/sin and pocketfft are not reproduced bit for bit. */
+
+/* Complex brute fold (core/fold.py:395-481 brutefold_start_complex_opt, via
+ * ffa_taylor_init_complex 572-614): the DFT of every segment at the
+ * harmonics h * f, h = 0 .. nbins / 2, with the t_ref phase correction.
+ * nsamps must be a multiple of segment_len. */
+int loki_brutefold_complex(const float* ts_e, const float* ts_v, int64_t nsamps,
+                           const double* freqs, int64_t nfreqs, int64_t segment_len,
+                           int32_t nbins, double tsamp, double t_ref, void* fold_out,
+                           void* stream);
+
+/* One complex DP level (dynamic/dyn_pffa.py:435-489 with shift_add_complex,
+ * core/common.py:344-372): out[ipair, p] = tail * e^{-2 pi i k s_t / nbins}
+ * + head * e^{-2 pi i k s_h / nbins} by phasor recurrence over k, the rows
+ * and float32 shifts taken from the level's plan (loki_ffa_plan). Whole
+ * levels only (no frequency window). */
+int loki_ffa_level_complex(const LokiFFALevel* lvl, const LokiFFACoord* plan,
+                           const void* fold_in, void* fold_out, void* stream);
+
+/* Normalised profiles of complex folds (ffa.py:401-411): irfft of both
+ * components to nbins samples, then e / sqrt(v); folds (n, 2, nbins / 2 + 1)
+ * complex64 -> out (n, nbins) float32. */
+int loki_fold_norm_complex(const void* folds, int64_t n, int32_t nbins, float* out,
+                           void* stream);
+
 /* ---- enumerate-prune (Taylor / Chebyshev basis, float32 folds) -------- */
 
 /* Constants of one pruning level, computed by the host with the reference's
@@ -216,6 +244,14 @@ typedef struct {
   double tm_r[LOKI_MAX_PARAMS + 1][LOKI_MAX_PARAMS + 1];
   double cfact[LOKI_MAX_PARAMS + 1];  /* k! */
   double ctsk[LOKI_MAX_PARAMS + 1];   /* scale**k */
+  /* Circular-orbit Taylor tree (core/circular.py; basis = 2, poly_order 5):
+   * significance levels of the circular classification and of the physical
+   * validation, (2 pi / p_orb_min)**2, the mass constant, and the time
+   * offsets of the closed-form circular propagation. On the moving grid
+   * circ_dt_add / circ_dt_init / circ_dt_next are t0_add / t0_init /
+   * t0_next minus t0_cur; on the fixed grid circ_dt_add is t0_add - t0_init. */
+  double circ_sig_prop, circ_sig_valid, circ_omega_max_sq, circ_x_mass;
+  double circ_dt_add, circ_dt_init, circ_dt_next;
 } LokiPruneLevel;
 
 /* Per-parent branching result. */
@@ -284,6 +320,50 @@ int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves, float* fo
                       const double* tm_seg, const double* dt_seg, const int32_t* seg_idx,
                       const float* ffa_fold, int64_t seg_stride, const LokiScoreSpec* spec,
                       int32_t* dev_err, void* stream);
+
+/* ---- circular-orbit tree (basis = 2, poly_order 5) ---------------------
+ * One level of prune.py:165-332 with the PruneCircTaylorDPFuncts plugin
+ * (dynamic/dyn_circular_taylor.py:444-740, core/circular.py:13-705):
+ *   loki_prune_circ_branch  circ_taylor_branch_batch: per-parent branching
+ *       info, and exclusive scans (n + 1 int64 each) of the children that keep
+ *       the parent crackle (keep_off) and of those from crackle expansion
+ *       (exp_off); children total = keep_off[n] + exp_off[n].
+ *   loki_prune_circ_map     every child at its batch-ordered position in
+ *       child_map (16 bytes each) and its circ_taylor_validate_batch result
+ *       as 1.0 / 0.0 in valid_flags; compact with loki_prune_select
+ *       (threshold 0.5) to the valid children (n_leaves_phy of them).
+ *   loki_prune_circ_score   resolve (circular or Taylor propagation by
+ *       get_circ_mask class), gather, shift-add and score of every valid
+ *       child; child_class (int8) and batch_taylor (int32 per parent batch)
+ *       feed the basis flag; batch_offsets (n + 1 int64) are the valid-child
+ *       offsets at parent-batch boundaries, for loki_prune_select_overflow.
+ *   loki_prune_circ_emit    circ_taylor_transform_batch, basis flags,
+ *       backtracks and folds of the survivors (ids into the valid list).
+ * The ascend is loki_prune_ascend with basis 2. */
+int loki_prune_circ_branch(const LokiPruneLevel* lvl, const double* leaves,
+                           int64_t n_parents, LokiBranchInfo* info, int64_t* keep_off,
+                           int64_t* exp_off, void* scan_scratch, int64_t scan_scratch_bytes,
+                           int32_t* dev_err, void* stream);
+int loki_prune_circ_map(const LokiPruneLevel* lvl, const double* leaves, int64_t n_parents,
+                        int64_t batch_size, const LokiBranchInfo* info,
+                        const int64_t* keep_off, const int64_t* exp_off, void* child_map,
+                        float* valid_flags, void* stream);
+int loki_prune_circ_score(const LokiPruneLevel* lvl, const double* leaves, const float* folds,
+                          int64_t n_parents, int64_t batch_size, const LokiBranchInfo* info,
+                          const void* child_map, const int64_t* keep_off,
+                          const int64_t* exp_off, const int64_t* valid_ids, int64_t n_valid,
+                          const float* fold_segment, const LokiScoreSpec* spec,
+                          float* child_scores, int32_t* child_idx, double* child_phase,
+                          int8_t* child_class, int32_t* batch_taylor, int64_t* batch_offsets,
+                          float* score_minmax, int32_t* dev_err, void* stream);
+int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* leaves, const float* folds,
+                         int64_t batch_size, const LokiBranchInfo* info, const void* child_map,
+                         const int64_t* valid_ids, const float* fold_segment,
+                         const int64_t* surv_ids, int64_t n_surv, const float* child_scores,
+                         const int32_t* child_idx, const double* child_phase,
+                         const int8_t* child_class, const int32_t* batch_taylor,
+                         double* leaves_out, float* folds_out, float* scores_out,
+                         float* scores_ep_out, int32_t* bt_out, void* stream);
 
 /* Scratch bytes for the internal scans over n elements. */
 int64_t loki_scan_scratch_bytes(int64_t n);

@@ -101,6 +101,13 @@ class LokiPruneLevel(C.Structure):
         ("tm_r", _M6),
         ("cfact", C.c_double * (MAX_PARAMS + 1)),
         ("ctsk", C.c_double * (MAX_PARAMS + 1)),
+        ("circ_sig_prop", C.c_double),
+        ("circ_sig_valid", C.c_double),
+        ("circ_omega_max_sq", C.c_double),
+        ("circ_x_mass", C.c_double),
+        ("circ_dt_add", C.c_double),
+        ("circ_dt_init", C.c_double),
+        ("circ_dt_next", C.c_double),
     ]
 
 
@@ -143,6 +150,9 @@ SIGNATURES: dict[str, tuple] = {
     "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
+    "loki_brutefold_complex": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
+    "loki_ffa_level_complex": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
+    "loki_fold_norm_complex": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_scan_scratch_bytes": (C.c_int64, [_I64]),
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_score": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _I64, _P,
@@ -154,7 +164,17 @@ SIGNATURES: dict[str, tuple] = {
                                   _P, _P, _P, _P, _P]),
     "loki_prune_ascend": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64,
                                     C.POINTER(LokiScoreSpec), _P, _P]),
+    "loki_prune_circ_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
+    "loki_prune_circ_map": (C.c_int, [_PL, _P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "loki_prune_circ_score": (C.c_int, [_PL, _P, _P, _I64, _I64, _P, _P, _P, _P, _P, _I64, _P,
+                                        C.POINTER(LokiScoreSpec), _P, _P, _P, _P, _P, _P, _P,
+                                        _P, _P]),
+    "loki_prune_circ_emit": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P,
+                                       _P, _P, _P, _P, _P, _P, _P, _P]),
 }
+
+#: bytes of one circular-tree child record (parent, cartesian index, crackle index, pad)
+CIRC_CHILD_BYTES = 16
 
 _lock = threading.Lock()
 _lib: C.CDLL | None = None

@@ -681,6 +681,47 @@ prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
 }
 
 // ---------------------------------------------------------------------------
+// circular-orbit propagation, shared by the circular tree and its ascend
+// ---------------------------------------------------------------------------
+
+// get_circ_mask (core/circular.py:13-79): 1 snap-circular, 2 crackle-circular
+// (the snap/accel hole), 0 Taylor.
+__device__ __forceinline__ int circ_class(const double* v, const double* e, double sig) {
+  const double crackle = v[0], snap = v[1], jerk = v[2], accel = v[3];
+  const bool sig_snap = fabs(snap) > __dmul_rn(sig, e[1]);
+  const bool sig_accel = fabs(accel) > __dmul_rn(sig, e[3]);
+  const bool sig_jerk = fabs(jerk) > __dmul_rn(sig, e[2]);
+  const bool snap_circ = sig_snap && sig_accel && __dmul_rn(-snap, accel) > 0.0;
+  if (snap_circ) return 1;
+  if (sig_jerk && __dmul_rn(-crackle, jerk) > 0.0) return 2;
+  return 0;
+}
+
+// shift_taylor_circular_params (utils/transforms.py:246-299): closed-form
+// circular-orbit propagation of [d5 .. d0] by dt (values only). cos and sin
+// are CUDA's double-precision functions.
+__device__ __forceinline__ void circ_shift(const double* p, double dt, bool hole, double* out) {
+  const double d5 = p[0], d4 = p[1], d3 = p[2], d2 = p[3], d1 = p[4], d0 = p[5];
+  const double wsq = hole ? __ddiv_rn(-d5, d3) : __ddiv_rn(-d4, d2);
+  const double w = __dsqrt_rn(wsq);
+  const double wdt = __dmul_rn(w, dt);
+  const double c = cos(wdt), s = sin(wdt);
+  const double d2j = __dadd_rn(__dmul_rn(d2, c), __dmul_rn(__ddiv_rn(d3, w), s));
+  const double d3j = __dsub_rn(__dmul_rn(d3, c), __dmul_rn(__dmul_rn(d2, w), s));
+  const double d1ci = __ddiv_rn(-d3, wsq);
+  const double d1cj = __ddiv_rn(-d3j, wsq);
+  const double e1 = __dsub_rn(d1, d1ci);
+  const double d0cj = __ddiv_rn(-d2j, wsq);
+  const double d0ci = __ddiv_rn(-d2, wsq);
+  out[0] = __dmul_rn(-wsq, d3j);
+  out[1] = __dmul_rn(-wsq, d2j);
+  out[2] = d3j;
+  out[3] = d2j;
+  out[4] = __dadd_rn(d1cj, e1);
+  out[5] = __dadd_rn(__dadd_rn(d0cj, __dsub_rn(d0, d0ci)), __dmul_rn(e1, dt));
+}
+
+// ---------------------------------------------------------------------------
 // ascend: warp per 32 survivors, segments accumulated in order
 // ---------------------------------------------------------------------------
 
@@ -705,10 +746,16 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     for (int j = lane; j < 2 * nb; j += 32) acc[k * 2 * nb + j] = 0.0f;
   double pv[LOKI_MAX_PARAMS + 1];
   double f0 = 1.0;
+  int cls = 0;  // circular tree: class of the survivor (core/circular.py:597-666)
   if (lane < kmax) {
     const double* lf = leaves + (s0 + lane) * (P + 2) * 2;
-    for (int i = 0; i < m; ++i) pv[i] = lf[2 * i];
+    double ev[LOKI_MAX_PARAMS + 1];
+    for (int i = 0; i < m; ++i) {
+      pv[i] = lf[2 * i];
+      ev[i] = lf[2 * i + 1];
+    }
     f0 = lf[2 * m];
+    if (D.basis == 2) cls = circ_class(pv, ev, D.circ_sig_prop);
   }
   __syncwarp();
   for (int sg = 0; sg < nseg; ++sg) {
@@ -722,6 +769,12 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
         double a[LOKI_MAX_PARAMS + 1];
         for (int i = 0; i < m; ++i) a[i] = tdot(pv, T, i, m);
         cheby_low3(D, a, m, &accel, &vel, &dd);
+      } else if (cls != 0) {  // circular survivors: closed-form propagation
+        double a[6];
+        circ_shift(pv, dt_seg[sg], cls == 2, a);
+        accel = a[3];
+        vel = a[4];
+        dd = a[5];
       } else {
         accel = tdot(pv, T, P - 2, m);
         vel = tdot(pv, T, P - 1, m);
@@ -768,6 +821,388 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     if (SK.pow2_64) score_row64_pow2(row, sp, SK, &s);
     else score_row(row, nb, sp, &s);
     scores[s0 + lane] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// circular-orbit Taylor tree (core/circular.py, dynamic/dyn_circular_taylor.py)
+//
+// Leaves are [d5 (crackle), d4 (snap), d3, d2, d1, d0, (f0, flag)]. Children
+// of one parent batch are ordered as the reference builds them: first every
+// child that keeps the parent's crackle (cartesian order over the batch),
+// then the children whose crackle is expanded, each expansion in crackle
+// order. Physical validation drops children before scoring, so the scored
+// list is the compacted list of valid children.
+// ---------------------------------------------------------------------------
+
+// One child of the circular tree: parent, index in the parent's cartesian
+// product over d4..d1, and the crackle sub-index (-1: parent crackle kept).
+struct CircChild {
+  int32_t parent, cart, crackle, pad;
+};
+
+// circ_validate_batch (core/circular.py:82-124) for one child.
+__device__ __forceinline__ bool circ_valid(const LokiPruneLevel& D, const double* v,
+                                           const double* e) {
+  const double snap = v[1], accel = v[3], sig = D.circ_sig_valid;
+  const bool sig_snap = fabs(snap) > __dmul_rn(sig, e[1]);
+  const bool sig_accel = fabs(accel) > __dmul_rn(sig, e[3]);
+  if (!(sig_snap && sig_accel)) return true;
+  if (!(__dmul_rn(-snap, accel) > 0.0)) return false;
+  const double wsq = __ddiv_rn(-snap, accel);
+  const double limit = __dmul_rn(D.circ_x_mass, pow(wsq, 2.0 / 3.0));
+  return wsq <= D.circ_omega_max_sq && fabs(accel) <= limit;
+}
+
+// Parameters and errors of one circular child (core/circular.py:204-394).
+__device__ __forceinline__ void circ_child(const LokiBranchInfo& B, const double* lf,
+                                           const CircChild& ch, double* pv, double* ev) {
+  const int P = 5;
+  child_params(B, P, ch.cart, pv);
+  pv[P] = B.d0;
+  for (int j = 0; j < P; ++j) ev[j] = B.dact[j];
+  ev[P] = 0.0;
+  if (ch.crackle >= 0) {  // branch_param_padded on the parent crackle cell
+    const double dact = B.dact[0];
+    const double first = __dadd_rn(__dsub_rn(lf[0], __ddiv_rn(lf[1], 2.0)),
+                                   __ddiv_rn(dact, 2.0));
+    pv[0] = __dadd_rn(first, __dmul_rn((double)ch.crackle, dact));
+  }
+}
+
+// Branch every parent (circ_taylor_branch_batch): per-parameter branching of
+// d4..d1 as in the Taylor tree, crackle deferred; counts the children that
+// keep the parent crackle and those produced by crackle expansion.
+__global__ void circ_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                                   int64_t n, LokiBranchInfo* __restrict__ info,
+                                   int64_t* __restrict__ n_keep, int64_t* __restrict__ n_exp,
+                                   int32_t* __restrict__ err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int P = 5;
+  const double* lf = leaves + i * (P + 2) * 2;
+  const double f0 = lf[(P + 1) * 2];
+  const double fscale = __ddiv_rn(f0, LOKI_C_VAL);
+  LokiBranchInfo B;
+  B.d0 = lf[2 * P];
+  bool needs0 = false;
+  int64_t num_c = 1;
+  int64_t total = 1;
+  for (int j = 0; j < P; ++j) {
+    const double pcur = lf[2 * j], dcur = lf[2 * j + 1];
+    const double dnew = __ddiv_rn(D.dfc[j], f0);
+    const double fb = __dmul_rn(D.fac[j], fscale);
+    const double shift = __dmul_rn(fabs(__dsub_rn(dcur, dnew)), fb);
+    const bool needs = shift >= D.eta_m;
+    int64_t num = 1;
+    double dact = dcur, first = pcur;
+    if (!(dcur > 0.0) || !(dnew > 0.0)) {
+      atomicOr(err, LOKI_DEVERR_BRANCH);
+    } else {
+      const double ratio = __ddiv_rn(dcur, dnew);
+      num = (int64_t)ceil(__dsub_rn(ratio, LOKI_FLOAT_EPSILON));
+      if (num < 1) num = 1;
+      if (num > D.branch_max) {
+        atomicOr(err, LOKI_DEVERR_BRANCH);
+        num = D.branch_max;
+      }
+      dact = __ddiv_rn(dcur, (double)num);
+      first = __dadd_rn(__dsub_rn(pcur, __ddiv_rn(dcur, 2.0)), __ddiv_rn(dact, 2.0));
+    }
+    if (j == 0) {  // crackle keeps the parent value; its step is the would-be child step
+      needs0 = needs;
+      num_c = num;
+      first = pcur;
+      num = 1;
+    }
+    if (!needs) {
+      num = 1;
+      dact = dcur;
+      first = pcur;
+    }
+    B.first[j] = first;
+    B.dact[j] = dact;
+    B.count[j] = (int32_t)num;
+    total *= num;
+  }
+  B.reserved = needs0 ? (int32_t)num_c : 0;
+  // first cartesian product: which children fall in the hole and expand crackle
+  const double sig = D.circ_sig_prop;
+  int64_t keep = 0, exp = 0;
+  double pv[LOKI_MAX_PARAMS + 1];
+  for (int64_t k = 0; k < total; ++k) {
+    child_params(B, P, k, pv);
+    const double snap = pv[1], jerk = pv[2], accel = pv[3];
+    const bool snap_circ = fabs(snap) > __dmul_rn(sig, B.dact[1]) &&
+                           fabs(accel) > __dmul_rn(sig, B.dact[3]) &&
+                           __dmul_rn(-snap, accel) > 0.0;
+    const bool expand = !snap_circ && fabs(jerk) > __dmul_rn(sig, B.dact[2]) && needs0;
+    if (expand) exp += num_c;
+    else ++keep;
+  }
+  info[i] = B;
+  n_keep[i] = keep;
+  n_exp[i] = exp;
+}
+
+// Children of every parent at their batch-ordered positions, plus a validity
+// flag (1.0 / 0.0) per child for the compaction.
+__global__ void circ_map_kernel(LokiPruneLevel D, const double* __restrict__ leaves, int64_t n,
+                                int64_t batch, const LokiBranchInfo* __restrict__ info,
+                                const int64_t* __restrict__ keep_off,
+                                const int64_t* __restrict__ exp_off,
+                                CircChild* __restrict__ map, float* __restrict__ validf) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int P = 5;
+  const int64_t b0 = (i / batch) * batch, b1 = std::min(b0 + batch, n);
+  int64_t pk = keep_off[i] + exp_off[b0];
+  int64_t pe = keep_off[b1] + exp_off[i];
+  const LokiBranchInfo B = info[i];
+  const double* lf = leaves + i * (P + 2) * 2;
+  const int64_t num_c = B.reserved;
+  int64_t total = 1;
+  for (int j = 0; j < P; ++j) total *= B.count[j];
+  const double sig = D.circ_sig_prop;
+  double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
+  for (int64_t k = 0; k < total; ++k) {
+    CircChild ch = {(int32_t)i, (int32_t)k, -1, 0};
+    circ_child(B, lf, ch, pv, ev);
+    const double snap = pv[1], jerk = pv[2], accel = pv[3];
+    const bool snap_circ = fabs(snap) > __dmul_rn(sig, ev[1]) &&
+                           fabs(accel) > __dmul_rn(sig, ev[3]) &&
+                           __dmul_rn(-snap, accel) > 0.0;
+    const bool expand = !snap_circ && fabs(jerk) > __dmul_rn(sig, ev[2]) && num_c > 0;
+    const float ok = circ_valid(D, pv, ev) ? 1.0f : 0.0f;  // crackle does not enter
+    if (!expand) {
+      map[pk] = ch;
+      validf[pk] = ok;
+      ++pk;
+    } else {
+      for (int64_t c = 0; c < num_c; ++c) {
+        ch.crackle = (int32_t)c;
+        map[pe] = ch;
+        validf[pe] = ok;
+        ++pe;
+      }
+    }
+  }
+}
+
+// Position of the first valid child at or after child index c.
+__device__ __forceinline__ int64_t lower_bound64(const int64_t* a, int64_t n, int64_t c) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < c) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Valid-child offsets at parent-batch boundaries (for the overflow rule).
+__global__ void circ_boff_kernel(const int64_t* __restrict__ keep_off,
+                                 const int64_t* __restrict__ exp_off, int64_t n,
+                                 const int64_t* __restrict__ valid_ids, int64_t n_valid,
+                                 int64_t* __restrict__ boff) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p > n) return;
+  boff[p] = lower_bound64(valid_ids, n_valid, keep_off[p] + exp_off[p]);
+}
+
+// Resolve (circ_taylor_resolve_batch / circ_taylor_fixed_resolve_batch) of
+// one valid child; returns its class.
+__device__ __forceinline__ int circ_resolve(const LokiPruneLevel& D, const double* pv,
+                                            const double* ev, double f0, ChildRes* r) {
+  const int m = 6;
+  const int cls = circ_class(pv, ev, D.circ_sig_prop);
+  double accel, vel, dd;
+  if (cls != 0) {
+    double a[6], b[6];
+    circ_shift(pv, D.circ_dt_add, cls == 2, a);
+    accel = a[3];
+    if (D.moving) {
+      circ_shift(pv, D.circ_dt_init, cls == 2, b);
+      vel = __dsub_rn(a[4], b[4]);
+      dd = __dsub_rn(a[5], b[5]);
+    } else {
+      vel = a[4];
+      dd = a[5];
+    }
+  } else if (D.moving) {
+    accel = tdot(pv, D.tm_a, 3, m);
+    vel = __dsub_rn(tdot(pv, D.tm_a, 4, m), tdot(pv, D.tm_i, 4, m));
+    dd = __dsub_rn(tdot(pv, D.tm_a, 5, m), tdot(pv, D.tm_i, 5, m));
+  } else {
+    accel = tdot(pv, D.tm_a, 3, m);
+    vel = tdot(pv, D.tm_a, 4, m);
+    dd = tdot(pv, D.tm_a, 5, m);
+  }
+  const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(vel, LOKI_C_VAL)));
+  const double delay = __ddiv_rn(dd, LOKI_C_VAL);
+  r->phase = phase_idx(D.dt_phase, f0, D.nbins, delay);
+  r->ia = (int32_t)axis_index(accel, D.accel_min, D.accel_inv, D.n_accel);
+  r->iff = (int32_t)axis_index(freq, D.freq_min, D.freq_inv, D.n_freq);
+  return cls;
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                  const float* __restrict__ folds, int64_t batch,
+                  const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+                  const int64_t* __restrict__ valid_ids, int64_t n_valid,
+                  const float* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                  float* __restrict__ scores, int32_t* __restrict__ cidx,
+                  double* __restrict__ cphase, int8_t* __restrict__ ccls,
+                  int32_t* __restrict__ batch_taylor, unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float tiles[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, P = 5;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tile = tiles + (size_t)warp * 32 * stride;
+  const int64_t v0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+  if (v0 >= n_valid) return;
+  const int kmax = (int)std::min<int64_t>(32, n_valid - v0);
+  int64_t my_par = 0, my_row = 0;
+  int my_shift = 0;
+  if (lane < kmax) {
+    const int64_t v = v0 + lane;
+    const CircChild ch = map[valid_ids[v]];
+    const LokiBranchInfo B = info[ch.parent];
+    const double* lf = leaves + (int64_t)ch.parent * (P + 2) * 2;
+    double pv[6], ev[6];
+    circ_child(B, lf, ch, pv, ev);
+    ChildRes r;
+    const int cls = circ_resolve(D, pv, ev, lf[(P + 1) * 2], &r);
+    if (cls == 0) atomicOr(batch_taylor + ch.parent / batch, 1);
+    cidx[2 * v] = r.ia;
+    cidx[2 * v + 1] = r.iff;
+    cphase[v] = r.phase;
+    ccls[v] = (int8_t)cls;
+    my_par = ch.parent;
+    my_row = (int64_t)r.ia * D.n_freq + r.iff;
+    my_shift = round_shift(r.phase, nb);
+  }
+  for (int k = 0; k < kmax; ++k) {
+    const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
+    const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+    const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+    const float* pf = folds + par * 2 * nb;
+    const float* sf = seg + row * 2 * nb;
+    float* trow = tile + k * stride;
+    for (int j = lane; j < nb; j += 32) {
+      int js = j - sh;
+      js += (js < 0) ? nb : 0;
+      const float e = __fadd_rn(pf[j], sf[js]);
+      const float vv = __fadd_rn(pf[nb + j], sf[nb + js]);
+      trow[j] = __fdiv_rn(e, __fsqrt_rn(vv));
+    }
+  }
+  __syncwarp();
+  if (lane < kmax) {
+    float* row = tile + lane * stride;
+    float s;
+    if (SK.pow2_64) score_row64_pow2(row, sp, SK, &s);
+    else score_row(row, nb, sp, &s);
+    scores[v0 + lane] = s;
+    if (s == s) {
+      atomicMin(minmax_keys, float_key(s));
+      atomicMax(minmax_keys + 1, float_key(s));
+    }
+  }
+}
+
+// New tree from the survivors: circ_taylor_transform_batch
+// (core/circular.py:669-705, moving grid), the basis flag written by the
+// moving-grid resolve (core/circular.py:478-509: 1 snap, 2 crackle, and 0 for
+// the crackle children of a batch that also holds Taylor children), backtracks
+// and folds.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                 const float* __restrict__ folds, int64_t batch,
+                 const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+                 const int64_t* __restrict__ valid_ids, const float* __restrict__ seg,
+                 const int64_t* __restrict__ surv, int64_t n_surv,
+                 const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
+                 const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
+                 const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
+                 float* __restrict__ fout, float* __restrict__ sout,
+                 float* __restrict__ seout, int32_t* __restrict__ bout) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, P = 5, m = 6;
+  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+  if (s0 >= n_surv) return;
+  const int kmax = (int)std::min<int64_t>(32, n_surv - s0);
+  int64_t my_par = 0, my_row = 0;
+  int my_shift = 0;
+  if (lane < kmax) {
+    const int64_t s = s0 + lane;
+    const int64_t v = surv[s];
+    const CircChild ch = map[valid_ids[v]];
+    const LokiBranchInfo B = info[ch.parent];
+    const double* lf = leaves + (int64_t)ch.parent * (P + 2) * 2;
+    double pv[6], ev[6];
+    circ_child(B, lf, ch, pv, ev);
+    const int cls = ccls[v];
+    double* lo = lout + s * (P + 2) * 2;
+    double flag = lf[2 * m + 1];
+    if (D.moving) {
+      if (cls == 1) flag = 1.0;
+      else if (cls == 2) flag = batch_taylor[ch.parent / batch] ? 0.0 : 2.0;
+      if (cls != 0) {
+        double o[6];
+        circ_shift(pv, D.circ_dt_next, cls == 2, o);
+        for (int i = 0; i < m; ++i) {
+          lo[2 * i] = o[i];
+          lo[2 * i + 1] = ev[i];
+        }
+      } else {
+        for (int i = 0; i < m; ++i) lo[2 * i] = tdot(pv, D.tm_n, i, m);
+        if (D.tiling == 0) {
+          for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dmul_rn(ev[i], fabs(D.tm_n[i][i]));
+        } else if (D.tiling == 2) {
+          for (int i = 0; i < m; ++i) lo[2 * i + 1] = tdot(ev, D.tm_e, i, m);
+        } else {
+          double e2[6];
+          for (int j = 0; j < m; ++j) e2[j] = __dmul_rn(ev[j], ev[j]);
+          for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dsqrt_rn(tdot(e2, D.tm_e, i, m));
+        }
+      }
+    } else {
+      for (int i = 0; i < m; ++i) {
+        lo[2 * i] = pv[i];
+        lo[2 * i + 1] = ev[i];
+      }
+    }
+    lo[2 * m] = lf[2 * m];
+    lo[2 * m + 1] = flag;
+    const float sc = cscores[v];
+    sout[s] = sc;
+    seout[s] = sc;
+    int32_t* bt = bout + s * (P + 2);
+    const int ia = cidx[2 * v], iff = cidx[2 * v + 1];
+    bt[0] = ch.parent;
+    for (int j = 1; j < P + 1; ++j) bt[j] = 0;
+    bt[D.nparams_ffa - 1] = ia;
+    bt[D.nparams_ffa] = iff;
+    bt[P + 1] = (int32_t)cphase[v];
+    my_par = ch.parent;
+    my_row = (int64_t)ia * D.n_freq + iff;
+    my_shift = round_shift(cphase[v], nb);
+  }
+  for (int k = 0; k < kmax; ++k) {
+    const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
+    const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+    const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+    const float* pf = folds + par * 2 * nb;
+    const float* sf = seg + row * 2 * nb;
+    float* o = fout + (s0 + k) * 2 * nb;
+    for (int j = lane; j < nb; j += 32) {
+      int js = j - sh;
+      js += (js < 0) ? nb : 0;
+      o[j] = __fadd_rn(pf[j], sf[js]);
+      o[nb + j] = __fadd_rn(pf[nb + j], sf[nb + js]);
+    }
   }
 }
 
@@ -970,4 +1405,139 @@ extern "C" int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves
       *lvl, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa_fold,
       seg_stride, sp, SK);
   return check_launch("prune_ascend");
+}
+
+// ---- circular-orbit tree --------------------------------------------------
+
+static int check_circ(const LokiPruneLevel* lvl) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  if (lvl->basis != 2 || lvl->poly_order != 5)
+    return set_error(LOKI_ERR_INVALID, "the circular tree needs basis 2 and poly_order 5");
+  return LOKI_OK;
+}
+
+extern "C" int loki_prune_circ_branch(const LokiPruneLevel* lvl, const double* leaves,
+                                      int64_t n_parents, LokiBranchInfo* info,
+                                      int64_t* keep_off, int64_t* exp_off, void* scan_scratch,
+                                      int64_t scan_scratch_bytes, int32_t* dev_err,
+                                      void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  if (n_parents < 0) return set_error(LOKI_ERR_INVALID, "n_parents < 0");
+  if (!keep_off || !exp_off || !dev_err || (n_parents && (!leaves || !info)))
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n_parents > 0) {
+    note_launch();
+    circ_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
+        *lvl, leaves, n_parents, info, keep_off, exp_off, dev_err);
+    rc = check_launch("prune_circ_branch");
+    if (rc) return rc;
+  }
+  rc = exclusive_scan<false>(keep_off, n_parents, 0.0, keep_off, scan_scratch,
+                             scan_scratch_bytes, s);
+  if (rc) return rc;
+  return exclusive_scan<false>(exp_off, n_parents, 0.0, exp_off, scan_scratch,
+                               scan_scratch_bytes, s);
+}
+
+extern "C" int loki_prune_circ_map(const LokiPruneLevel* lvl, const double* leaves,
+                                   int64_t n_parents, int64_t batch_size,
+                                   const LokiBranchInfo* info, const int64_t* keep_off,
+                                   const int64_t* exp_off, void* child_map, float* valid_flags,
+                                   void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  if (batch_size < 1 || n_parents < 0) return set_error(LOKI_ERR_INVALID, "bad batch size");
+  if (n_parents == 0) return LOKI_OK;
+  if (!leaves || !info || !keep_off || !exp_off || !child_map || !valid_flags)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  circ_map_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      *lvl, leaves, n_parents, batch_size, info, keep_off, exp_off,
+      reinterpret_cast<CircChild*>(child_map), valid_flags);
+  return check_launch("prune_circ_map");
+}
+
+extern "C" int loki_prune_circ_score(const LokiPruneLevel* lvl, const double* leaves,
+                                     const float* folds, int64_t n_parents, int64_t batch_size,
+                                     const LokiBranchInfo* info, const void* child_map,
+                                     const int64_t* keep_off, const int64_t* exp_off,
+                                     const int64_t* valid_ids, int64_t n_valid,
+                                     const float* fold_segment, const LokiScoreSpec* spec,
+                                     float* child_scores, int32_t* child_idx,
+                                     double* child_phase, int8_t* child_class,
+                                     int32_t* batch_taylor, int64_t* batch_offsets,
+                                     float* score_minmax, int32_t* dev_err, void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (batch_size < 1 || n_parents < 0 || n_valid < 0)
+    return set_error(LOKI_ERR_INVALID, "bad circular score arguments");
+  if (!score_minmax || !dev_err || !batch_taylor || !batch_offsets || !keep_off || !exp_off)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nbatch = (n_parents + batch_size - 1) / batch_size;
+  if (nbatch > 0 && cudaMemsetAsync(batch_taylor, 0, nbatch * sizeof(int32_t), s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
+  unsigned* keys = reinterpret_cast<unsigned*>(score_minmax);
+  note_launch();
+  minmax_init_kernel<<<1, 1, 0, s>>>(keys);
+  if (n_valid > 0) {
+    if (!leaves || !folds || !info || !child_map || !valid_ids || !fold_segment ||
+        !child_scores || !child_idx || !child_phase || !child_class)
+      return set_error(LOKI_ERR_INVALID, "null pointer argument");
+    LokiScoreSpec sp = *spec;
+    sp.mode = 1;
+    const ScoreK SK = make_score_k(sp, lvl->nbins);
+    const int smem = score_smem_bytes(lvl->nbins, sp.wmax, kPruneWarps);
+    if (smem > 200 * 1024)
+      return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(circ_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+    const int64_t blocks = (n_valid + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    note_launch();
+    circ_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
+        *lvl, leaves, folds, batch_size, info, reinterpret_cast<const CircChild*>(child_map),
+        valid_ids, n_valid, fold_segment, sp, SK, child_scores, child_idx, child_phase,
+        child_class, batch_taylor, keys);
+  }
+  note_launch();
+  minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
+  note_launch();
+  circ_boff_kernel<<<(unsigned)((n_parents + 1 + 255) / 256), 256, 0, s>>>(
+      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets);
+  return check_launch("prune_circ_score");
+}
+
+extern "C" int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* leaves,
+                                    const float* folds, int64_t batch_size,
+                                    const LokiBranchInfo* info, const void* child_map,
+                                    const int64_t* valid_ids, const float* fold_segment,
+                                    const int64_t* surv_ids, int64_t n_surv,
+                                    const float* child_scores, const int32_t* child_idx,
+                                    const double* child_phase, const int8_t* child_class,
+                                    const int32_t* batch_taylor, double* leaves_out,
+                                    float* folds_out, float* scores_out, float* scores_ep_out,
+                                    int32_t* bt_out, void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  if (n_surv <= 0) return LOKI_OK;
+  if (batch_size < 1) return set_error(LOKI_ERR_INVALID, "bad batch size");
+  if (!leaves || !folds || !info || !child_map || !valid_ids || !fold_segment || !surv_ids ||
+      !child_scores || !child_idx || !child_phase || !child_class || !batch_taylor ||
+      !leaves_out || !folds_out || !scores_out || !scores_ep_out || !bt_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  const int64_t blocks = (n_surv + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  note_launch();
+  circ_emit_kernel<<<(unsigned)blocks, kPruneWarps * 32, 0, (cudaStream_t)stream>>>(
+      *lvl, leaves, folds, batch_size, info, reinterpret_cast<const CircChild*>(child_map),
+      valid_ids, fold_segment, surv_ids, n_surv, child_scores, child_idx, child_phase,
+      child_class, batch_taylor, leaves_out, folds_out, scores_out, scores_ep_out, bt_out);
+  return check_launch("prune_circ_emit");
 }

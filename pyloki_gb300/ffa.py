@@ -115,17 +115,16 @@ class DynamicProgramming:
     """
 
     def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None) -> None:
-        if cfg.use_fourier:
-            msg = ("the Fourier-domain FFA (use_fourier=True) is not built yet; "
-                   "use use_fourier=False")
-            raise NotImplementedError(msg)
+        if cfg.use_fourier and cfg.nbins % 2:
+            msg = "the Fourier-domain FFA needs an even nbins (irfft length)"
+            raise ValueError(msg)
         self._ts_data = ts_data
         self._cfg = cfg
         self._device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         self._lib = _lib.load()
         self._err = torch.zeros(1, dtype=torch.int32, device=self._device)
-        self._data_type = np.float32
+        self._data_type = np.complex64 if cfg.use_fourier else np.float32
         self._fold: torch.Tensor | None = None
         self._ffa_level = -1
         self.phase_scratch_bytes = _GIB
@@ -229,6 +228,20 @@ class DynamicProgramming:
         dev = self._device
         ts_e = torch.as_tensor(self.ts_data.ts_e).to(dev, non_blocking=True)
         ts_v = torch.as_tensor(self.ts_data.ts_v).to(dev, non_blocking=True)
+        t_ref = 0.0 if cfg.nparams == 1 else cfg.bseg_brute * cfg.tsamp / 2
+        if cfg.use_fourier:  # core/fold.py:395-481,572-614
+            nseg = ts_e.numel() // cfg.bseg_brute
+            nfreq = g0.dev[-1].numel()
+            nbf = cfg.nbins // 2 + 1
+            fold = torch.empty((nseg, nfreq, 2, nbf), dtype=torch.complex64, device=dev)
+            _lib.check(self._lib.loki_brutefold_complex(
+                _lib.ptr(ts_e), _lib.ptr(ts_v), ts_e.numel(), _lib.ptr(g0.dev[-1]), nfreq,
+                cfg.bseg_brute, cfg.nbins, cfg.tsamp, t_ref, _lib.ptr(fold), self._stream()))
+            self.launches += 1
+            self._fold = fold.reshape(nseg, *([1] * (cfg.nparams - 1)), nfreq, 2, nbf)
+            self._err.zero_()
+            self._ffa_level = 0
+            return
         self._fold, nl = _brutefold(ts_e, ts_v, g0.dev[-1], cfg.bseg_brute, cfg.nbins,
                                     cfg.tsamp, 0.0 if cfg.nparams == 1 else
                                     cfg.bseg_brute * cfg.tsamp / 2,
@@ -252,6 +265,20 @@ class DynamicProgramming:
         prev = self._grid(self.ffa_level)
         nseg_in = self.nsegments
         fold_in = self.fold
+        if self.cfg.use_fourier:  # shift_add_complex (core/common.py:344-372)
+            nbf = self.nbins // 2 + 1
+            desc = level_desc(self.cfg, cur, prev, nseg_in)
+            plan = torch.empty((cur.size, 4), dtype=torch.int32, device=self._device)
+            _lib.check(self._lib.loki_ffa_plan(desc, _lib.ptr(plan), _lib.ptr(self._err),
+                                               self._stream()))
+            out = torch.empty((nseg_in // 2, cur.size, 2, nbf), dtype=torch.complex64,
+                              device=self._device)
+            _lib.check(self._lib.loki_ffa_level_complex(desc, _lib.ptr(plan), _lib.ptr(fold_in),
+                                                        _lib.ptr(out), self._stream()))
+            self.launches += 2
+            self._fold = out.reshape(nseg_in // 2, *cur.counts.tolist(), 2, nbf)
+            self._ffa_level += 1
+            return
         out = torch.empty((nseg_in // 2, cur.size, 2, self.nbins), dtype=torch.float32,
                           device=self._device)
         desc = level_desc(self.cfg, cur, prev, nseg_in)
@@ -268,11 +295,16 @@ class DynamicProgramming:
             idx = tuple(int(i) for i in param_idx)[-(fold.ndim - 2):]
             fold = fold[idx]
         lead = fold.shape[:-2]
-        flat = fold.reshape(-1, 2, self.nbins).contiguous()
+        flat = fold.reshape(-1, 2, fold.shape[-1]).contiguous()
         out = torch.empty((flat.shape[0], self.nbins), dtype=torch.float32,
                           device=self._device)
-        _lib.check(self._lib.loki_fold_norm(_lib.ptr(flat), flat.shape[0], self.nbins,
-                                            _lib.ptr(out), self._stream()))
+        if self.cfg.use_fourier:  # irfft, then e / sqrt(v)
+            _lib.check(self._lib.loki_fold_norm_complex(_lib.ptr(flat), flat.shape[0],
+                                                        self.nbins, _lib.ptr(out),
+                                                        self._stream()))
+        else:
+            _lib.check(self._lib.loki_fold_norm(_lib.ptr(flat), flat.shape[0], self.nbins,
+                                                _lib.ptr(out), self._stream()))
         self.launches += 1
         return out.reshape(*lead, self.nbins)
 
@@ -314,6 +346,16 @@ class DynamicProgramming:
             raise RuntimeError(msg)
         mark("brutefold")
         fin = self._grid(n)
+        if cfg.use_fourier:  # every level materialised, then irfft norm + boxcar
+            self.execute()
+            mark("levels")
+            from pyloki_gb300.scoring import boxcar_snr_nd
+
+            snr = boxcar_snr_nd(self.get_fold_norm(), widths, stdnoise)
+            if mode != 0:
+                snr = snr.amax(dim=-1)
+            mark("final")
+            return snr
         snr = torch.empty((fin.size, nout), dtype=torch.float32, device=self._device)
         if banded is None:
             banded = n >= 2 and self.level_bytes(n - 1) > 8 * band_bytes
@@ -400,19 +442,19 @@ _BAND_CACHE: dict[tuple, tuple] = {}
 def _brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref=0.0, *,
                scratch_bytes=_GIB) -> tuple[torch.Tensor, int]:
     """Brute fold plus the number of kernels it launched."""
-    elem = 1 if nbins <= 256 else 2
-    nfreq = freqs.numel()
-    need = nfreq * segment_len * elem
-    nbytes = min(need, max(scratch_bytes, segment_len * elem))
-    chunk = nbytes // (segment_len * elem)
-    return brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref,
-                     scratch_bytes=scratch_bytes), 2 * math.ceil(nfreq / chunk)
+    lib = _lib.load()
+    before = lib.loki_launch_count()
+    fold = brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref,
+                     scratch_bytes=scratch_bytes)
+    return fold, lib.loki_launch_count() - before
 
 
 def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segment_len: int,
               nbins: int, tsamp: float, t_ref: float = 0.0, *,
               scratch_bytes: int = _GIB) -> torch.Tensor:
-    """Fold ``(nsegments, nfreqs, 2, nbins)`` (``core/fold.py:108-171``)."""
+    """Fold ``(nsegments, nfreqs, 2, nbins)`` (``core/fold.py:108-171``).
+    ``scratch_bytes`` bounds the phase map; frequencies beyond it are folded
+    in chunks."""
     lib = _lib.load()
     nsamps = ts_e.numel()
     nseg = math.ceil(nsamps / segment_len)

@@ -193,10 +193,13 @@ class Pruning:
                        (False, "chebyshev", True), (False, "chebyshev", False)}:
             msg = f"Invalid pruning configuration: {key}"
             raise ValueError(msg)
-        if key not in {(False, "taylor", False), (False, "chebyshev", False)}:
-            msg = f"pruning plugin {key} (circular / complex) is not built yet"
+        if key not in {(False, "taylor", False), (False, "chebyshev", False),
+                       (True, "taylor", False)}:
+            msg = f"pruning plugin {key} (complex folds) is not built yet"
             raise NotImplementedError(msg)
         self.poly_basis = poly_basis
+        #: the circular-orbit Taylor tree (PruneCircTaylorDPFuncts, poly_order 5)
+        self.circular = key[0]
         self._dyp = dyp
         self._threshold_scheme = np.asarray(threshold_scheme, dtype=np.float64)
         self._max_sugg = int(max_sugg)
@@ -368,6 +371,18 @@ class Pruning:
         d.dt_phase = coord_add[0] - coord_init[0]
         if self.poly_basis == "chebyshev":
             self._cheby_level(d, level, coord_init, coord_cur, coord_next, coord_add)
+        if self.circular:  # dynamic/dyn_circular_taylor.py:341-385, config.py:475-481
+            d.basis = 2
+            d.circ_sig_prop = float(cfg.propagator_significance)
+            d.circ_sig_valid = float(cfg.validation_significance)
+            d.circ_omega_max_sq = float((2 * np.pi / cfg.p_orb_min) ** 2)
+            d.circ_x_mass = float(cfg.x_mass_const)
+            if moving:
+                d.circ_dt_add = coord_add[0] - coord_cur[0]
+                d.circ_dt_init = coord_init[0] - coord_cur[0]
+                d.circ_dt_next = coord_next[0] - coord_cur[0]
+            else:
+                d.circ_dt_add = coord_add[0] - coord_init[0]
         counts = self.param_grid_count_init
         lim = cfg.param_limits
         d.n_accel, d.n_freq = int(counts[-2]), int(counts[-1])
@@ -426,6 +441,9 @@ class Pruning:
     # ---- one level (prune.py:615-669) ------------------------------------------
     def execute_iter(self, log_file: Path | None = None) -> None:
         if self.prune_complete:
+            return
+        if self.circular:
+            self._execute_iter_circ(log_file)
             return
         self._prune_level += 1
         level = self._prune_level
@@ -506,10 +524,106 @@ class Pruning:
         self._backtrack_hist.append(new.backtracks)
         self._world_tree = new
 
-    def _select_overflow(self, scores, offsets, n_par, n_child, threshold, surv, n_surv_d) -> int:
+    def _execute_iter_circ(self, log_file: Path | None = None) -> None:
+        """One level of the circular-orbit tree (prune.py:165-332 with
+        dynamic/dyn_circular_taylor.py): branch with deferred crackle, map the
+        batch-ordered children, validate, resolve + score, select, emit."""
+        self._prune_level += 1
+        level = self._prune_level
+        lib = self._lib
+        stream = self._stream()
+        seg_idx = self.scheme.get_segment_idx(level)
+        fold_segment = self._fold_segment(seg_idx)
+        threshold = float(self.threshold_scheme[level - 1])
+        d = self.level_desc(level)
+        tree = self._world_tree
+        n_par = tree.valid_size
+        P = self.poly_order
+        bs = max(1, min(self.batch_size, n_par))
+        info = self._buf.get("info", n_par * _lib.BRANCH_INFO_BYTES, torch.uint8)
+        keep = self._buf.get("keep", n_par + 1, torch.int64)
+        expd = self._buf.get("expd", n_par + 1, torch.int64)
+        sb = int(lib.loki_scan_scratch_bytes(n_par + 1))
+        scan = self._buf.get("scan", sb, torch.uint8)
+        _lib.check(lib.loki_prune_circ_branch(d, _lib.ptr(tree.leaves), n_par, _lib.ptr(info),
+                                              _lib.ptr(keep), _lib.ptr(expd), _lib.ptr(scan),
+                                              sb, _lib.ptr(self._err), stream))
+        n_child = int(keep[n_par].item()) + int(expd[n_par].item())
+        _lib.check_dev_err(self._err)
+        cmap = self._buf.get("cmap", n_child * _lib.CIRC_CHILD_BYTES, torch.uint8)
+        validf = self._buf.get("validf", n_child, torch.float32)
+        _lib.check(lib.loki_prune_circ_map(d, _lib.ptr(tree.leaves), n_par, bs, _lib.ptr(info),
+                                           _lib.ptr(keep), _lib.ptr(expd), _lib.ptr(cmap),
+                                           _lib.ptr(validf), stream))
+        vsb = int(lib.loki_scan_scratch_bytes(n_child)) + 8 * (n_child + 1)
+        vscan = self._buf.get("vscan", vsb, torch.uint8)
+        valid = self._buf.get("valid", max(n_child, 1), torch.int64)
+        n_valid_d = self._buf.get("nvalid", 1, torch.int64)
+        _lib.check(lib.loki_prune_select(_lib.ptr(validf), n_child, 0.5, _lib.ptr(valid),
+                                         _lib.ptr(n_valid_d), _lib.ptr(vscan), vsb, stream))
+        n_valid = int(n_valid_d.item())
+        scores = self._buf.get("cscores", n_valid, torch.float32)
+        cidx = self._buf.get("cidx", 2 * n_valid, torch.int32)
+        cphase = self._buf.get("cphase", n_valid, torch.float64)
+        ccls = self._buf.get("ccls", n_valid, torch.int8)
+        nbatch = (n_par + bs - 1) // bs
+        btay = self._buf.get("btay", max(nbatch, 1), torch.int32)
+        boff = self._buf.get("boff", n_par + 1, torch.int64)
+        minmax = self._buf.get("minmax", 2, torch.float32)
+        _lib.check(lib.loki_prune_circ_score(
+            d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par, bs, _lib.ptr(info),
+            _lib.ptr(cmap), _lib.ptr(keep), _lib.ptr(expd), _lib.ptr(valid), n_valid,
+            _lib.ptr(fold_segment), self.spec, _lib.ptr(scores), _lib.ptr(cidx),
+            _lib.ptr(cphase), _lib.ptr(ccls), _lib.ptr(btay), _lib.ptr(boff), _lib.ptr(minmax),
+            _lib.ptr(self._err), stream))
+        ssb = int(lib.loki_scan_scratch_bytes(n_valid)) + 8 * (n_valid + 1)
+        sscan = self._buf.get("sscan", ssb, torch.uint8)
+        surv = self._buf.get("surv", max(n_valid, 1), torch.int64)
+        n_surv_d = self._buf.get("nsurv", 1, torch.int64)
+        _lib.check(lib.loki_prune_select(_lib.ptr(scores), n_valid, threshold, _lib.ptr(surv),
+                                         _lib.ptr(n_surv_d), _lib.ptr(sscan), ssb, stream))
+        n_surv = int(n_surv_d.item())
+        if n_surv > self.max_sugg:
+            n_surv = self._select_overflow(scores, boff, n_par, n_valid, threshold, surv,
+                                           n_surv_d, batch_size=bs)
+        nb = self.dyp.cfg.nbins
+        dev = self._device
+        new = WorldTree(torch.empty((n_surv, P + 2, 2), dtype=torch.float64, device=dev),
+                        torch.empty((n_surv, 2, nb), dtype=torch.float32, device=dev),
+                        torch.empty(n_surv, dtype=torch.float32, device=dev),
+                        torch.empty((n_surv, P + 2), dtype=torch.int32, device=dev),
+                        torch.empty(n_surv, dtype=torch.float32, device=dev))
+        _lib.check(lib.loki_prune_circ_emit(
+            d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), bs, _lib.ptr(info), _lib.ptr(cmap),
+            _lib.ptr(valid), _lib.ptr(fold_segment), _lib.ptr(surv), n_surv, _lib.ptr(scores),
+            _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(ccls), _lib.ptr(btay),
+            _lib.ptr(new.leaves), _lib.ptr(new.folds), _lib.ptr(new.scores),
+            _lib.ptr(new.scores_ep), _lib.ptr(new.backtracks), stream))
+        mm = minmax.cpu().numpy() if n_valid else np.zeros(2, np.float32)
+        st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
+                        score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
+                        n_leaves=n_child, n_leaves_phy=n_valid, n_leaves_surv=n_surv)
+        self._finish_level(st, new, log_file)
+
+    def _finish_level(self, st: PruneStats, new: WorldTree, log_file: Path | None) -> None:
+        self._pstats.append(st)
+        if log_file is not None:
+            with Path(log_file).open("a") as f:
+                f.write(st.get_summary())
+        if st.n_leaves_surv == 0:
+            self._prune_complete = True
+            self._world_tree = new
+            return
+        slot = self._best_intermediate_arr[st.level - 1]
+        slot["param_sets"], slot["scores"] = new.get_best_k(self.intermediate_k)
+        self._backtrack_hist.append(new.backtracks)
+        self._world_tree = new
+
+    def _select_overflow(self, scores, offsets, n_par, n_child, threshold, surv, n_surv_d,
+                         batch_size: int | None = None) -> int:
         """Exact batch-sequential selection when more than ``max_sugg`` pass."""
         off = offsets.cpu().numpy()
-        b = self.batch_size
+        b = self.batch_size if batch_size is None else batch_size
         starts = np.arange(0, n_par, b)
         ends = np.minimum(starts + b, n_par)
         max_batch = int((off[ends] - off[starts]).max()) if n_par else 0

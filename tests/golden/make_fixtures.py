@@ -110,6 +110,37 @@ def ffa_case(name: str, n: int, limits, nbins: int, freq_inj: float, seed: int,
           "bseg", cfg.bseg_brute)
 
 
+def fourier_case(name: str, n: int, limits, nbins: int, freq_inj: float, seed: int,
+                 ducy_max: float = 0.5, wtsp: float = 2.0) -> None:
+    """Fourier-domain FFA (use_fourier=True): complex folds per level, the
+    irfft-normalised final profiles and their S/N."""
+    from pyloki.config import PulsarSearchConfig
+    from pyloki.detection import scoring
+    from pyloki.ffa import DynamicProgramming
+    from pyloki.io.timeseries import TimeSeries
+
+    tsamp = 64e-6
+    ts_e, ts_v = _series(n, tsamp, freq_inj, 0.6, seed)
+    cfg = PulsarSearchConfig(
+        nsamps=n, tsamp=tsamp, nbins=nbins, eta=1.0,
+        param_limits=np.asarray(limits, dtype=np.float64),
+        ducy_max=ducy_max, wtsp=wtsp, use_fourier=True,
+    )
+    dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, tsamp), cfg)
+    dyp.initialize()
+    out = {"ts_e": ts_e, "ts_v": ts_v, **_cfg_dict(cfg), "fold_0": dyp.fold.copy()}
+    for lvl in range(1, cfg.niters_ffa + 1):
+        dyp._execute_iter()
+        out[f"fold_{lvl}"] = dyp.fold.copy()
+    out["niters"] = np.int64(cfg.niters_ffa)
+    out["widths"] = cfg.score_widths
+    norm = dyp.get_fold_norm()
+    out["fold_norm"] = norm
+    out["snrs"] = scoring.boxcar_snr_nd(norm, cfg.score_widths, 1.0)
+    np.savez_compressed(HERE / f"{name}.npz", **out)
+    print(name, "levels", cfg.niters_ffa, "final", dyp.fold.shape)
+
+
 def scoring_case(name: str, nbins: int, nprof: int, ducy_max: float, wtsp: float,
                  seed: int) -> None:
     from pyloki.detection import scoring
@@ -143,11 +174,22 @@ def prune_series(n: int, tsamp: float, f0: float, accel: float, seed: int):
     return ts_e, np.ones(n, np.float32)
 
 
+def circ_series(n: int, tsamp: float, f0: float, p_orb: float, x_orb: float, seed: int):
+    """Noise plus a pulse delayed by a circular orbit x sin(2 pi t / P + 0.7)."""
+    rng = np.random.default_rng(seed)
+    t = np.arange(n) * tsamp
+    ph = (t - x_orb * np.sin(2 * np.pi * t / p_orb + 0.7)) * f0
+    pulse = np.exp(10 * (np.cos(2 * np.pi * (ph - 0.4)) - 1))
+    ts_e = (rng.standard_normal(n) + 0.25 * pulse).astype(np.float32)
+    return ts_e, np.ones(n, np.float32)
+
+
 def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
                max_sugg: int = 2**16, batch_size: int = 64, ref_seg: int = 8,
                fold_levels: tuple = (5, 11), thr_offset: float = 0.0,
-               leaf_cap: int = 6000, basis: str = "taylor") -> None:
-    """Taylor (poly_order 3, real folds) enumerate-prune run of 15 levels."""
+               leaf_cap: int = 6000, basis: str = "taylor", circular: bool = False) -> None:
+    """Enumerate-prune run of 15 levels (real folds): Taylor/Chebyshev of
+    order 3, or (``circular``) the circular-orbit Taylor tree of order 5."""
     import tempfile
 
     from pyloki.config import ParamLimits, PulsarSearchConfig
@@ -155,13 +197,19 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
     from pyloki.io.timeseries import TimeSeries
     from pyloki.prune import Pruning
 
-    n, tsamp = 2**17, 2.5e-4
-    ts_e, ts_v = prune_series(n, tsamp, 100.3, 300.0, 5)
-    lim = ParamLimits.from_taylor((100.0, 101.0), accel=(-20000.0, 20000.0),
-                                  jerk=(-3000.0, 3000.0)).limits
-    cfg = PulsarSearchConfig(nsamps=n, tsamp=tsamp, nbins=32, eta=1.0, param_limits=lim,
+    if circular:
+        n, tsamp, nbins, order, p_orb_min = 2**15, 4e-3, 16, 5, 100.0
+        ts_e, ts_v = circ_series(n, tsamp, 10.3, 150.0, 0.3, 31)
+        lim = ParamLimits.from_circular((9.8, 10.8), p_orb_min=p_orb_min, poly_order=5).limits
+    else:
+        n, tsamp, nbins, order, p_orb_min = 2**17, 2.5e-4, 32, 3, 0.0
+        ts_e, ts_v = prune_series(n, tsamp, 100.3, 300.0, 5)
+        lim = ParamLimits.from_taylor((100.0, 101.0), accel=(-20000.0, 20000.0),
+                                      jerk=(-3000.0, 3000.0)).limits
+    cfg = PulsarSearchConfig(nsamps=n, tsamp=tsamp, nbins=nbins, eta=1.0, param_limits=lim,
                              ducy_max=0.3, wtsp=2.0, use_fourier=False, bseg_ffa=n // 16,
-                             prune_poly_order=3, branch_max=16, tiling_strategy=tiling)
+                             prune_poly_order=order, branch_max=16, tiling_strategy=tiling,
+                             p_orb_min=p_orb_min)
     dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, tsamp), cfg)
     dyp.initialize()
     dyp.execute(show_progress=False)
@@ -174,7 +222,8 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
     out = {"ts_e": ts_e, "ts_v": ts_v, **_cfg_dict(cfg), "thresholds": thr,
            "max_sugg": np.int64(max_sugg), "batch_size": np.int64(batch_size),
            "ref_seg": np.int64(ref_seg), "moving": np.int64(moving),
-           "poly_order": np.int64(3), "branch_max": np.int64(16), "basis": np.str_(basis),
+           "poly_order": np.int64(order), "branch_max": np.int64(16), "basis": np.str_(basis),
+           "p_orb_min": np.float64(p_orb_min),
            "fold_ffa": np.asarray(dyp.fold), "scheme": prn.scheme.data.copy()}
     wt = prn.world_tree
     out["seed_leaves"] = wt.leaves[: wt.valid_size].copy()
@@ -233,6 +282,37 @@ def main() -> None:
 
     _wt.math = _types.SimpleNamespace(
         nextafter=lambda a, b: np.float64(_math.nextafter(a, b)))
+    # numpy sends a one-row batch through BLAS gemv, whose summation order is
+    # machine-specific, and every larger batch through dgemm (forward fused
+    # multiply-adds). Evaluating one-row batches as two identical rows pins
+    # the dgemm order for every batch size.
+    from pyloki.utils import transforms as _tr
+
+    def _two_rows(fn):
+        def wrapped(x, *args, **kwargs):
+            x = np.asarray(x)
+            if x.ndim >= 2 and x.shape[0] == 1:
+                return fn(np.concatenate([x, x], axis=0), *args, **kwargs)[:1]
+            return fn(x, *args, **kwargs)
+        return wrapped
+
+    for _name in ("shift_taylor_params", "shift_taylor_full", "shift_cheby_full",
+                  "cheby_to_taylor_param_shift", "cheby_to_taylor", "cheby_to_taylor_full",
+                  "taylor_to_cheby_full"):
+        setattr(_tr, _name, _two_rows(getattr(_tr, _name)))
+    # The circular branch builds its children with np.empty and never sets
+    # their d0 error (core/circular.py:329,354); whatever the allocator left
+    # there flows into the quadrature error matmul (inf * 0 = NaN). Zeroed
+    # memory, which is what the GPU path writes, makes the runs reproducible.
+    from pyloki.core import circular as _circ
+
+    class _ZeroedEmpty:
+        empty = staticmethod(np.zeros)
+
+        def __getattr__(self, name):
+            return getattr(np, name)
+
+    _circ.np = _ZeroedEmpty()
     import logging
 
     logging.disable(logging.CRITICAL)
@@ -242,6 +322,12 @@ def main() -> None:
         scoring_case("score_nb100", 100, 128, 0.3, 1.3, 13)
     if "--cheby-only" in sys.argv:
         cheby_cases()
+        return
+    if "--circ-only" in sys.argv:
+        circ_cases()
+        return
+    if "--fourier-only" in sys.argv:
+        fourier_cases()
         return
     if "--prune-only" in sys.argv:
         prune_cases()
@@ -253,6 +339,18 @@ def main() -> None:
              50, 200.4, 23, ducy_max=0.2, wtsp=1.5)
     prune_cases()
     cheby_cases()
+
+
+def fourier_cases() -> None:
+    fourier_case("ffa_freq_fourier", 2**16, [(10.0, 14.0)], 64, 12.3, 24)
+    fourier_case("ffa_accel_fourier", 2**16, [(-1.0e6, 1.0e6), (200.0, 203.0)], 32, 201.6, 25)
+
+
+def circ_cases() -> None:
+    prune_case("prune_circ", circular=True, fold_levels=(8,))
+    prune_case("prune_circ_b4", circular=True, batch_size=4, fold_levels=())
+    prune_case("prune_circ_quad", circular=True, tiling="quadrature", fold_levels=())
+    prune_case("prune_circ_fixed", circular=True, moving=False, fold_levels=())
 
 
 def cheby_cases() -> None:

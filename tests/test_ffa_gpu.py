@@ -185,6 +185,28 @@ def test_brutefold_chunked_scratch_and_wide_bins(cuda_device):
         np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
+def test_brutefold_many_segments_ragged(cuda_device):
+    """>= 32 segments (the warp-per-frequency kernel: lanes are segments),
+    a ragged last segment, partially filled last warp of segments, chunked
+    frequencies, against the oracle."""
+    import torch
+
+    from pyloki_gb300.ffa import brutefold
+
+    rng = np.random.default_rng(9)
+    seg = 1024
+    for n, nbins in [(70 * seg + 333, 64), (32 * seg, 37), (33 * seg - 16, 256)]:
+        ts_e = rng.standard_normal(n).astype(np.float32)
+        ts_v = (1 + rng.random(n)).astype(np.float32)
+        freqs = np.linspace(40.0, 47.0, 29)
+        ref = O.brutefold(ts_e, ts_v, freqs, seg, nbins, 64e-6, 0.013)
+        te = torch.from_numpy(ts_e).to(cuda_device)
+        tv = torch.from_numpy(ts_v).to(cuda_device)
+        tf = torch.from_numpy(freqs).to(cuda_device)
+        out = brutefold(te, tv, tf, seg, nbins, 64e-6, 0.013, scratch_bytes=7 * seg)
+        np.testing.assert_array_equal(out.cpu().numpy(), ref, err_msg=f"n={n} nbins={nbins}")
+
+
 def test_window_violation_is_reported_not_faulted(cuda_device):
     """A level whose input window misses the resolved indices sets the device
     error word (the access is skipped) and the host raises."""
