@@ -85,14 +85,32 @@ brutefold_seq_kernel(const float* __restrict__ ts_e, const float* __restrict__ t
   int64_t i = 0;
   const bool aligned = ((reinterpret_cast<uintptr_t>(m) | reinterpret_cast<uintptr_t>(e) |
                          reinterpret_cast<uintptr_t>(v)) & 15) == 0;
-  if (aligned) {
+  if (aligned && len >= VN) {
+    // software pipeline: the map word and series of the next VN samples are
+    // loaded while the current VN samples are added
+    uint4 mv = *reinterpret_cast<const uint4*>(m);
+    float4 ev[VN / 4], vv[VN / 4];
+#pragma unroll
+    for (int q = 0; q < VN / 4; ++q) {
+      ev[q] = __ldg(reinterpret_cast<const float4*>(e) + q);
+      vv[q] = __ldg(reinterpret_cast<const float4*>(v) + q);
+    }
     for (; i + VN <= len; i += VN) {
-      const uint4 mv = *reinterpret_cast<const uint4*>(m + i);
-      float4 ev[VN / 4], vv[VN / 4];
+      const bool more = i + 2 * VN <= len;
+      uint4 mv_n = mv;
+      float4 ev_n[VN / 4], vv_n[VN / 4];
 #pragma unroll
       for (int q = 0; q < VN / 4; ++q) {
-        ev[q] = __ldg(reinterpret_cast<const float4*>(e + i) + q);
-        vv[q] = __ldg(reinterpret_cast<const float4*>(v + i) + q);
+        ev_n[q] = ev[q];
+        vv_n[q] = vv[q];
+      }
+      if (more) {
+        mv_n = *reinterpret_cast<const uint4*>(m + i + VN);
+#pragma unroll
+        for (int q = 0; q < VN / 4; ++q) {
+          ev_n[q] = __ldg(reinterpret_cast<const float4*>(e + i + VN) + q);
+          vv_n[q] = __ldg(reinterpret_cast<const float4*>(v + i + VN) + q);
+        }
       }
 #pragma unroll
       for (int k = 0; k < VN; ++k) {
@@ -106,6 +124,12 @@ brutefold_seq_kernel(const float* __restrict__ ts_e, const float* __restrict__ t
         }
         ae = __fadd_rn(ae, f4get(ev[k >> 2], k & 3));
         av = __fadd_rn(av, f4get(vv[k >> 2], k & 3));
+      }
+      mv = mv_n;
+#pragma unroll
+      for (int q = 0; q < VN / 4; ++q) {
+        ev[q] = ev_n[q];
+        vv[q] = vv_n[q];
       }
     }
   }

@@ -14,8 +14,11 @@ constants (Taylor shift matrices, grid-step factors) are computed here with
 the reference's numpy expressions (``core/taylor.py``, ``utils/psr_utils.py``,
 ``utils/transforms.py``) so the kernels reproduce its arithmetic.
 
-Supported plugin: Taylor basis, time-domain folds (``PrunePolyTaylorDPFuncts``
-with ``use_fourier=False``), moving or fixed grid, all three tiling strategies.
+Supported plugins, time-domain folds (``use_fourier=False``), moving or fixed
+grid, all three tiling strategies: Taylor basis (``PrunePolyTaylorDPFuncts``),
+Chebyshev basis (``PrunePolyChebyshevDPFuncts``) and the circular-orbit Taylor
+tree of order 5 (``PruneCircTaylorDPFuncts``, its own branch / map / validate
+/ score / emit entry points).
 """
 
 from __future__ import annotations
@@ -488,6 +491,9 @@ class Pruning:
         _lib.check(lib.loki_prune_select(_lib.ptr(scores), n_child, threshold, _lib.ptr(surv),
                                          _lib.ptr(n_surv_d), _lib.ptr(sscan), ssb, stream))
         n_surv = int(n_surv_d.item())
+        # score min/max is final once the selection is: read it now so that
+        # the emit below runs while the host prepares the next level
+        mm = minmax.cpu().numpy() if n_child else np.zeros(2, np.float32)
         self.launches += 9
         if n_surv > self.max_sugg:
             n_surv = self._select_overflow(scores, offsets, n_par, n_child, threshold, surv,
@@ -507,7 +513,6 @@ class Pruning:
                                        _lib.ptr(new.scores), _lib.ptr(new.scores_ep),
                                        _lib.ptr(new.backtracks), stream))
         self.launches += 1
-        mm = minmax.cpu().numpy() if n_child else np.zeros(2, np.float32)
         st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
                         score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
                         n_leaves=n_child, n_leaves_phy=n_child, n_leaves_surv=n_surv)
@@ -583,6 +588,7 @@ class Pruning:
         _lib.check(lib.loki_prune_select(_lib.ptr(scores), n_valid, threshold, _lib.ptr(surv),
                                          _lib.ptr(n_surv_d), _lib.ptr(sscan), ssb, stream))
         n_surv = int(n_surv_d.item())
+        mm = minmax.cpu().numpy() if n_valid else np.zeros(2, np.float32)
         if n_surv > self.max_sugg:
             n_surv = self._select_overflow(scores, boff, n_par, n_valid, threshold, surv,
                                            n_surv_d, batch_size=bs)
@@ -599,7 +605,6 @@ class Pruning:
             _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(ccls), _lib.ptr(btay),
             _lib.ptr(new.leaves), _lib.ptr(new.folds), _lib.ptr(new.scores),
             _lib.ptr(new.scores_ep), _lib.ptr(new.backtracks), stream))
-        mm = minmax.cpu().numpy() if n_valid else np.zeros(2, np.float32)
         st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
                         score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
                         n_leaves=n_child, n_leaves_phy=n_valid, n_leaves_surv=n_surv)
