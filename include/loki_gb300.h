@@ -321,6 +321,33 @@ int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves, float* fo
                       const float* ffa_fold, int64_t seg_stride, const LokiScoreSpec* spec,
                       int32_t* dev_err, void* stream);
 
+/* ---- complex (Fourier) folds ---------------------------------------------
+ * The same steps for trees over Fourier-domain FFA folds
+ * (PrunePolyTaylorComplexDPFuncts / PrunePolyChebyshevComplexDPFuncts):
+ * folds and FFA segment rows are (2, nbins / 2 + 1) complex64, the segment
+ * row is rotated by the phasor recurrence of shift_add_complex_batch
+ * (core/common.py:403-429) and scored through its irfft
+ * (detection/scoring.py:285-292); the ascend sums rotated rows
+ * (core/common.py:460-490). Taylor and Chebyshev bases; nbins even. */
+int loki_prune_score_complex(const LokiPruneLevel* lvl, const double* leaves, const void* folds,
+                             int64_t n_parents, const LokiBranchInfo* info,
+                             const int64_t* offsets, int64_t n_children,
+                             const void* fold_segment, const LokiScoreSpec* spec,
+                             float* child_scores, int32_t* child_idx, double* child_phase,
+                             float* score_minmax, int32_t* dev_err, void* stream);
+int loki_prune_emit_complex(const LokiPruneLevel* lvl, const double* leaves, const void* folds,
+                            const LokiBranchInfo* info, const int64_t* offsets,
+                            int64_t n_parents, const void* fold_segment,
+                            const int64_t* surv_ids, int64_t n_surv, const float* child_scores,
+                            const int32_t* child_idx, const double* child_phase,
+                            double* leaves_out, void* folds_out, float* scores_out,
+                            float* scores_ep_out, int32_t* bt_out, void* stream);
+int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double* leaves, void* folds,
+                              float* scores, float* scores_ep, int64_t n, int32_t nseg,
+                              const double* tm_seg, const double* dt_seg,
+                              const int32_t* seg_idx, const void* ffa_fold, int64_t seg_stride,
+                              const LokiScoreSpec* spec, int32_t* dev_err, void* stream);
+
 /* ---- circular-orbit tree (basis = 2, poly_order 5) ---------------------
  * One level of prune.py:165-332 with the PruneCircTaylorDPFuncts plugin
  * (dynamic/dyn_circular_taylor.py:444-740, core/circular.py:13-705):

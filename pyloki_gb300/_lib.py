@@ -164,6 +164,12 @@ SIGNATURES: dict[str, tuple] = {
                                   _P, _P, _P, _P, _P]),
     "loki_prune_ascend": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P, _I64,
                                     C.POINTER(LokiScoreSpec), _P, _P]),
+    "loki_prune_score_complex": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _I64, _P,
+                                           C.POINTER(LokiScoreSpec), _P, _P, _P, _P, _P, _P]),
+    "loki_prune_emit_complex": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P,
+                                          _P, _P, _P, _P, _P, _P]),
+    "loki_prune_ascend_complex": (C.c_int, [_PL, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P,
+                                            _I64, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_prune_circ_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_circ_map": (C.c_int, [_PL, _P, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "loki_prune_circ_score": (C.c_int, [_PL, _P, _P, _I64, _I64, _P, _P, _P, _P, _P, _I64, _P,

@@ -1207,6 +1207,256 @@ circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
 }
 
 // ---------------------------------------------------------------------------
+// complex (Fourier) folds: PrunePolyTaylorComplexDPFuncts and the Chebyshev
+// counterpart. Tree folds and FFA segment rows are (2, nbf) complex64, nbf =
+// nbins / 2 + 1 (float2 re, im). One lane owns one child: it rotates the
+// segment row with the phasor recurrence of shift_add_complex_batch
+// (core/common.py:403-429), adds the parent fold, and scores the irfft of the
+// sum (detection/scoring.py:285-292).
+// ---------------------------------------------------------------------------
+
+// Phasor step exp(-2 pi i shift / nbins) with the reference's float32 angle
+// float32(-2 * float32(pi)) * float32(shift) / nbins.
+__device__ __forceinline__ float2 prune_phasor(double phase, int nbins) {
+  const float m2pi = -2.0f * (float)3.14159265358979323846;
+  const float ang = __fdiv_rn(__fmul_rn(m2pi, (float)phase), (float)nbins);
+  float sn, cs;
+  sincosf(ang, &sn, &cs);
+  return make_float2(cs, sn);
+}
+
+__device__ __forceinline__ float2 cmul_rn(float2 a, float2 b) {
+  return make_float2(__fsub_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                     __fadd_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+
+// comb = seg * phasor^k + par, both components (par may be null: seg only).
+__device__ __forceinline__ void rotate_add(const float2* __restrict__ seg,
+                                           const float2* __restrict__ par, float2 delta, int nbf,
+                                           float2* __restrict__ comb) {
+  for (int c = 0; c < 2; ++c) {
+    float2 ph = make_float2(1.0f, 0.0f);
+    for (int k = 0; k < nbf; ++k) {
+      const float2 r = cmul_rn(seg[c * nbf + k], ph);
+      const float2 p = par ? par[c * nbf + k] : make_float2(0.0f, 0.0f);
+      comb[c * nbf + k] = make_float2(__fadd_rn(r.x, p.x), __fadd_rn(r.y, p.y));
+      ph = cmul_rn(ph, delta);
+    }
+  }
+}
+
+// irfft (n = nbins, even) of both components, then e / sqrt(v) into row.
+// tw holds cos, then sin, of 2 pi t / nbins (float32 of the exact value).
+__device__ __forceinline__ void irfft_norm(const float2* __restrict__ comb, int nbins, int nbf,
+                                           const float* __restrict__ tw, float* row) {
+  const float inv = 1.0f / (float)nbins;
+  for (int j = 0; j < nbins; ++j) {
+    float x[2];
+    for (int c = 0; c < 2; ++c) {
+      const float2* X = comb + c * nbf;
+      float acc = X[0].x;
+      const float nyq = X[nbf - 1].x;
+      acc = (j & 1) ? __fsub_rn(acc, nyq) : __fadd_rn(acc, nyq);
+      int idx = 0;
+      for (int m = 1; m < nbf - 1; ++m) {
+        idx += j;
+        if (idx >= nbins) idx -= nbins;
+        const float t = __fsub_rn(__fmul_rn(X[m].x, tw[idx]), __fmul_rn(X[m].y, tw[nbins + idx]));
+        acc = __fadd_rn(acc, __fmul_rn(2.0f, t));
+      }
+      x[c] = __fmul_rn(acc, inv);
+    }
+    row[j] = __fdiv_rn(x[0], __fsqrt_rn(x[1]));
+  }
+}
+
+__device__ __forceinline__ void load_twiddles(float* tw, int nbins) {
+  for (int t = threadIdx.x; t < nbins; t += blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)t / (double)nbins, &s, &c);
+    tw[t] = (float)c;
+    tw[nbins + t] = (float)s;
+  }
+}
+
+// Per-warp shared memory of the complex kernels: 32 lanes x (2, nbf) float2
+// sums, then the 32-row score tile.
+__host__ __device__ inline size_t cplx_warp_floats(int nbins, int stride) {
+  return (size_t)32 * 2 * (nbins / 2 + 1) * 2 + (size_t)32 * stride;
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                           const float2* __restrict__ folds, int64_t n_parents,
+                           const LokiBranchInfo* __restrict__ info,
+                           const int64_t* __restrict__ offsets, int64_t n_children,
+                           const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                           float* __restrict__ scores, int32_t* __restrict__ cidx,
+                           double* __restrict__ cphase, unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t c = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (c >= n_children) return;
+  const int64_t par = find_parent(offsets, n_parents, c);
+  const LokiBranchInfo B = info[par];
+  const double* lf = leaves + par * (P + 2) * 2;
+  double pv[LOKI_MAX_PARAMS + 1];
+  child_params(B, P, c - offsets[par], pv);
+  pv[P] = B.d0;
+  const ChildRes r = resolve_child(D, pv, lf[(P + 1) * 2]);
+  cidx[2 * c] = r.ia;
+  cidx[2 * c + 1] = r.iff;
+  cphase[c] = r.phase;
+  const int64_t row = (int64_t)r.ia * D.n_freq + r.iff;
+  rotate_add(seg + row * 2 * nbf, folds + par * 2 * nbf, prune_phasor(r.phase, nb), nbf, comb);
+  float* trow = tile + lane * stride;
+  irfft_norm(comb, nb, nbf, tw, trow);
+  float s;
+  score_row(trow, nb, sp, &s);
+  scores[c] = s;
+  if (s == s) {
+    atomicMin(minmax_keys, float_key(s));
+    atomicMax(minmax_keys + 1, float_key(s));
+  }
+}
+
+// Survivors of the complex tree: transform / backtrack exactly as
+// prune_emit_kernel, the fold written as the complex sum.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                          const float2* __restrict__ folds,
+                          const LokiBranchInfo* __restrict__ info,
+                          const int64_t* __restrict__ offsets, int64_t n_parents,
+                          const float2* __restrict__ seg, const int64_t* __restrict__ surv,
+                          int64_t n_surv, const float* __restrict__ cscores,
+                          const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
+                          double* __restrict__ lout, float2* __restrict__ fout,
+                          float* __restrict__ sout, float* __restrict__ seout,
+                          int32_t* __restrict__ bout) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n_surv) return;
+  const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order, m = P + 1;
+  const int64_t c = surv[s];
+  const int64_t par = find_parent(offsets, n_parents, c);
+  const LokiBranchInfo B = info[par];
+  const double* lf = leaves + par * (P + 2) * 2;
+  double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
+  child_params(B, P, c - offsets[par], pv);
+  pv[P] = B.d0;
+  for (int j = 0; j < P; ++j) ev[j] = B.dact[j];
+  ev[P] = 0.0;
+  double* lo = lout + s * (P + 2) * 2;
+  if (D.moving) {
+    for (int i = 0; i < m; ++i) lo[2 * i] = tdot(pv, D.tm_n, i, m);
+    if (D.tiling == 0) {
+      for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dmul_rn(ev[i], fabs(D.tm_n[i][i]));
+    } else if (D.tiling == 2) {
+      for (int i = 0; i < m; ++i) lo[2 * i + 1] = tdot(ev, D.tm_e, i, m);
+    } else {
+      double e2[LOKI_MAX_PARAMS + 1];
+      for (int j = 0; j < m; ++j) e2[j] = __dmul_rn(ev[j], ev[j]);
+      for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dsqrt_rn(tdot(e2, D.tm_e, i, m));
+    }
+  } else {
+    for (int i = 0; i < m; ++i) {
+      lo[2 * i] = pv[i];
+      lo[2 * i + 1] = ev[i];
+    }
+  }
+  lo[2 * m] = lf[2 * m];
+  lo[2 * m + 1] = lf[2 * m + 1];
+  sout[s] = cscores[c];
+  seout[s] = cscores[c];
+  int32_t* bt = bout + s * (P + 2);
+  const int ia = cidx[2 * c], iff = cidx[2 * c + 1];
+  bt[0] = (int32_t)par;
+  for (int j = 1; j < P + 1; ++j) bt[j] = 0;
+  bt[D.nparams_ffa - 1] = ia;
+  bt[D.nparams_ffa] = iff;
+  bt[P + 1] = (int32_t)cphase[c];
+  const int64_t row = (int64_t)ia * D.n_freq + iff;
+  rotate_add(seg + row * 2 * nbf, folds + par * 2 * nbf, prune_phasor(cphase[c], nb), nbf,
+             fout + s * 2 * nbf);
+}
+
+// Ascend of the complex tree (dyn_poly_taylor.py:632-679 with
+// core/common.py:460-490): per survivor the rotated segment rows are summed
+// over the segments in order, then the sum is scored through its irfft.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                            float2* __restrict__ folds, float* __restrict__ scores,
+                            float* __restrict__ scores_ep, int64_t n, int nseg,
+                            const double* __restrict__ tm_seg,
+                            const double* __restrict__ dt_seg,
+                            const int32_t* __restrict__ seg_idx,
+                            const float2* __restrict__ ffa, int64_t seg_stride,
+                            LokiScoreSpec sp, ScoreK SK) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order, m = P + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t r = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (r >= n) return;
+  const double* lf = leaves + r * (P + 2) * 2;
+  double pv[LOKI_MAX_PARAMS + 1];
+  for (int i = 0; i < m; ++i) pv[i] = lf[2 * i];
+  const double f0 = lf[2 * m];
+  for (int k = 0; k < 2 * nbf; ++k) comb[k] = make_float2(0.0f, 0.0f);
+  for (int sg = 0; sg < nseg; ++sg) {
+    const double(*T)[LOKI_MAX_PARAMS + 1] =
+        reinterpret_cast<const double(*)[LOKI_MAX_PARAMS + 1]>(tm_seg + sg * 36);
+    double accel, vel, dd;
+    if (D.basis == 1) {
+      double a[LOKI_MAX_PARAMS + 1];
+      for (int i = 0; i < m; ++i) a[i] = tdot(pv, T, i, m);
+      cheby_low3(D, a, m, &accel, &vel, &dd);
+    } else {
+      accel = tdot(pv, T, P - 2, m);
+      vel = tdot(pv, T, P - 1, m);
+      dd = tdot(pv, T, P, m);
+    }
+    const double freq = __dmul_rn(f0, __dsub_rn(1.0, __ddiv_rn(vel, LOKI_C_VAL)));
+    const double delay = __ddiv_rn(dd, LOKI_C_VAL);
+    const double ph = phase_idx(dt_seg[sg], f0, nb, delay);
+    const int64_t ia = axis_index(accel, D.accel_min, D.accel_inv, D.n_accel);
+    const int64_t iff = axis_index(freq, D.freq_min, D.freq_inv, D.n_freq);
+    const float2* row = ffa + (int64_t)seg_idx[sg] * seg_stride + (ia * D.n_freq + iff) * 2 * nbf;
+    const float2 delta = prune_phasor(ph, nb);
+    for (int c = 0; c < 2; ++c) {  // res += row * phasor^k
+      float2 p = make_float2(1.0f, 0.0f);
+      for (int k = 0; k < nbf; ++k) {
+        const float2 t = cmul_rn(row[c * nbf + k], p);
+        float2& a = comb[c * nbf + k];
+        a = make_float2(__fadd_rn(a.x, t.x), __fadd_rn(a.y, t.y));
+        p = cmul_rn(p, delta);
+      }
+    }
+  }
+  float2* o = folds + r * 2 * nbf;
+  for (int k = 0; k < 2 * nbf; ++k) o[k] = comb[k];
+  float* trow = tile + lane * stride;
+  irfft_norm(comb, nb, nbf, tw, trow);
+  scores_ep[r] = scores[r];
+  float s;
+  score_row(trow, nb, sp, &s);
+  scores[r] = s;
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 
@@ -1540,4 +1790,119 @@ extern "C" int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* lea
       valid_ids, fold_segment, surv_ids, n_surv, child_scores, child_idx, child_phase,
       child_class, batch_taylor, leaves_out, folds_out, scores_out, scores_ep_out, bt_out);
   return check_launch("prune_circ_emit");
+}
+
+// ---- complex (Fourier) folds -----------------------------------------------
+
+static int cplx_smem(const LokiPruneLevel* lvl, const LokiScoreSpec& sp, int* smem) {
+  if (lvl->nbins % 2) return set_error(LOKI_ERR_INVALID, "complex folds need an even nbins");
+  const size_t bytes = ((size_t)2 * lvl->nbins +
+                        kPruneWarps * cplx_warp_floats(lvl->nbins,
+                                                       score_stride(lvl->nbins, sp.wmax))) *
+                       sizeof(float);
+  if (bytes > 200 * 1024)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for complex pruning");
+  *smem = (int)bytes;
+  return LOKI_OK;
+}
+
+extern "C" int loki_prune_score_complex(const LokiPruneLevel* lvl, const double* leaves,
+                                        const void* folds, int64_t n_parents,
+                                        const LokiBranchInfo* info, const int64_t* offsets,
+                                        int64_t n_children, const void* fold_segment,
+                                        const LokiScoreSpec* spec, float* child_scores,
+                                        int32_t* child_idx, double* child_phase,
+                                        float* score_minmax, int32_t* dev_err, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (!score_minmax || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned* keys = reinterpret_cast<unsigned*>(score_minmax);
+  note_launch();
+  minmax_init_kernel<<<1, 1, 0, s>>>(keys);
+  if (n_children > 0) {
+    if (!leaves || !folds || !info || !offsets || !fold_segment || !child_scores ||
+        !child_idx || !child_phase)
+      return set_error(LOKI_ERR_INVALID, "null pointer argument");
+    LokiScoreSpec sp = *spec;
+    sp.mode = 1;
+    const ScoreK SK = make_score_k(sp, lvl->nbins);
+    int smem = 0;
+    rc = cplx_smem(lvl, sp, &smem);
+    if (rc) return rc;
+    if (cudaFuncSetAttribute(prune_score_complex_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+    const int64_t blocks = (n_children + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    note_launch();
+    prune_score_complex_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
+        *lvl, leaves, reinterpret_cast<const float2*>(folds), n_parents, info, offsets,
+        n_children, reinterpret_cast<const float2*>(fold_segment), sp, SK, child_scores,
+        child_idx, child_phase, keys);
+  }
+  note_launch();
+  minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
+  return check_launch("prune_score_complex");
+}
+
+extern "C" int loki_prune_emit_complex(const LokiPruneLevel* lvl, const double* leaves,
+                                       const void* folds, const LokiBranchInfo* info,
+                                       const int64_t* offsets, int64_t n_parents,
+                                       const void* fold_segment, const int64_t* surv_ids,
+                                       int64_t n_surv, const float* child_scores,
+                                       const int32_t* child_idx, const double* child_phase,
+                                       double* leaves_out, void* folds_out, float* scores_out,
+                                       float* scores_ep_out, int32_t* bt_out, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  if (n_surv <= 0) return LOKI_OK;
+  if (!leaves || !folds || !info || !offsets || !fold_segment || !surv_ids || !child_scores ||
+      !child_idx || !child_phase || !leaves_out || !folds_out || !scores_out ||
+      !scores_ep_out || !bt_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  prune_emit_complex_kernel<<<(unsigned)((n_surv + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      *lvl, leaves, reinterpret_cast<const float2*>(folds), info, offsets, n_parents,
+      reinterpret_cast<const float2*>(fold_segment), surv_ids, n_surv, child_scores, child_idx,
+      child_phase, leaves_out, reinterpret_cast<float2*>(folds_out), scores_out, scores_ep_out,
+      bt_out);
+  return check_launch("prune_emit_complex");
+}
+
+extern "C" int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double* leaves,
+                                         void* folds, float* scores, float* scores_ep,
+                                         int64_t n, int32_t nseg, const double* tm_seg,
+                                         const double* dt_seg, const int32_t* seg_idx,
+                                         const void* ffa_fold, int64_t seg_stride,
+                                         const LokiScoreSpec* spec, int32_t* dev_err,
+                                         void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (n <= 0) return LOKI_OK;
+  if (nseg < 1 || !leaves || !folds || !scores || !scores_ep || !tm_seg || !dt_seg ||
+      !seg_idx || !ffa_fold || !dev_err)
+    return set_error(LOKI_ERR_INVALID, "bad ascend arguments");
+  if (lvl->basis == 2)
+    return set_error(LOKI_ERR_UNSUPPORTED, "complex folds of the circular tree");
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, lvl->nbins);
+  int smem = 0;
+  rc = cplx_smem(lvl, sp, &smem);
+  if (rc) return rc;
+  if (cudaFuncSetAttribute(prune_ascend_complex_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  const int64_t blocks = (n + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  note_launch();
+  prune_ascend_complex_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem,
+                                (cudaStream_t)stream>>>(
+      *lvl, leaves, reinterpret_cast<float2*>(folds), scores, scores_ep, n, nseg, tm_seg, dt_seg,
+      seg_idx, reinterpret_cast<const float2*>(ffa_fold), seg_stride, sp, SK);
+  return check_launch("prune_ascend_complex");
 }

@@ -51,10 +51,11 @@ def shift_factors(poly_order: int, tobs: float, nbins: int) -> np.ndarray:
 
 
 def _set6(dst, m: np.ndarray) -> None:
+    """Write ``m`` (n x n, n <= 6) into a 6 x 6 ctypes matrix, zero-padded."""
+    out = np.ctypeslib.as_array(dst)
+    out[...] = 0.0
     n = m.shape[0]
-    for i in range(6):
-        for j in range(6):
-            dst[i][j] = float(m[i, j]) if i < n and j < n else 0.0
+    out[:n, :n] = m
 
 
 @dataclasses.dataclass
@@ -196,11 +197,12 @@ class Pruning:
                        (False, "chebyshev", True), (False, "chebyshev", False)}:
             msg = f"Invalid pruning configuration: {key}"
             raise ValueError(msg)
-        if key not in {(False, "taylor", False), (False, "chebyshev", False),
-                       (True, "taylor", False)}:
-            msg = f"pruning plugin {key} (complex folds) is not built yet"
+        if key == (True, "taylor", True):
+            msg = "the circular-orbit tree over complex (Fourier) folds is not built yet"
             raise NotImplementedError(msg)
         self.poly_basis = poly_basis
+        #: folds are complex (Fourier domain): (n, 2, nbins / 2 + 1) complex64
+        self.fourier = bool(cfg.use_fourier)
         #: the circular-orbit Taylor tree (PruneCircTaylorDPFuncts, poly_order 5)
         self.circular = key[0]
         self._dyp = dyp
@@ -311,10 +313,19 @@ class Pruning:
         leaves[:, -1, 1] = 0
         if self.poly_basis == "chebyshev":  # core/chebyshev.py:14-70
             leaves = chebyshev.seed_leaves(param_arr, dparams, P, self.scheme.get_coord(0)[1])
-        folds = fold_segment.reshape(n, 2, cfg.nbins).contiguous()
         from pyloki_gb300.scoring import snr_score_batch
 
-        scores = snr_score_batch(folds, cfg.score_widths)
+        if self.fourier:  # scored through the irfft (detection/scoring.py:285-292)
+            folds = fold_segment.reshape(n, 2, cfg.nbins // 2 + 1).contiguous()
+            norm = torch.empty((n, cfg.nbins), dtype=torch.float32, device=self._device)
+            _lib.check(self._lib.loki_fold_norm_complex(_lib.ptr(folds), n, cfg.nbins,
+                                                        _lib.ptr(norm), self._stream()))
+            scores = torch.empty(n, dtype=torch.float32, device=self._device)
+            _lib.check(self._lib.loki_boxcar_snr(_lib.ptr(norm), n, cfg.nbins, self.spec,
+                                                 _lib.ptr(scores), self._stream()))
+        else:
+            folds = fold_segment.reshape(n, 2, cfg.nbins).contiguous()
+            scores = snr_score_batch(folds, cfg.score_widths)
         bt = torch.zeros((n, P + 2), dtype=torch.int32, device=self._device)
         return WorldTree(torch.from_numpy(leaves).to(self._device), folds, scores, bt)
 
@@ -341,6 +352,15 @@ class Pruning:
 
     # ---- per-level constants ---------------------------------------------------
     def level_desc(self, level: int) -> _lib.LokiPruneLevel:
+        """Constants of one level; they depend only on the reference segment
+        and the level, so repeated runs from the same segment reuse them."""
+        key = (self.scheme.ref_idx, level)
+        cache = self.__dict__.setdefault("_desc_cache", {})
+        if key not in cache:
+            cache[key] = self._level_desc(level)
+        return cache[key]
+
+    def _level_desc(self, level: int) -> _lib.LokiPruneLevel:
         cfg = self.dyp.cfg
         sc = self.scheme
         moving = self.use_moving_grid
@@ -475,7 +495,8 @@ class Pruning:
         if self.score_events is not None:
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(torch.cuda.current_stream(self._device))
-        _lib.check(lib.loki_prune_score(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par,
+        score_fn = lib.loki_prune_score_complex if self.fourier else lib.loki_prune_score
+        _lib.check(score_fn(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par,
                                         _lib.ptr(info), _lib.ptr(offsets), n_child,
                                         _lib.ptr(fold_segment), self.spec, _lib.ptr(scores),
                                         _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(minmax),
@@ -500,12 +521,14 @@ class Pruning:
                                            n_surv_d)
         nb = self.dyp.cfg.nbins
         dev = self._device
+        fold_shape = (n_surv, 2, nb // 2 + 1) if self.fourier else (n_surv, 2, nb)
         new = WorldTree(torch.empty((n_surv, P + 2, 2), dtype=torch.float64, device=dev),
-                        torch.empty((n_surv, 2, nb), dtype=torch.float32, device=dev),
+                        torch.empty(fold_shape, dtype=tree.folds.dtype, device=dev),
                         torch.empty(n_surv, dtype=torch.float32, device=dev),
                         torch.empty((n_surv, P + 2), dtype=torch.int32, device=dev),
                         torch.empty(n_surv, dtype=torch.float32, device=dev))
-        _lib.check(lib.loki_prune_emit(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds),
+        emit_fn = lib.loki_prune_emit_complex if self.fourier else lib.loki_prune_emit
+        _lib.check(emit_fn(d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds),
                                        _lib.ptr(info), _lib.ptr(offsets), n_par,
                                        _lib.ptr(fold_segment), _lib.ptr(surv), n_surv,
                                        _lib.ptr(scores), _lib.ptr(cidx), _lib.ptr(cphase),
@@ -669,11 +692,13 @@ class Pruning:
         si_d = torch.from_numpy(seg_idx.astype(np.int32)).to(dev)
         fold = self.dyp.fold
         stride = int(np.prod(fold.shape[1:]))
-        d = self.level_desc(self.prune_level)
+        d = self._level_desc(self.prune_level)  # a fresh copy: modified below
         if cheby:
             self._cheby_scale(d, coord_end[1])
         wt = self.world_tree
-        _lib.check(self._lib.loki_prune_ascend(
+        ascend_fn = (self._lib.loki_prune_ascend_complex if self.fourier
+                     else self._lib.loki_prune_ascend)
+        _lib.check(ascend_fn(
             d, _lib.ptr(wt.leaves), _lib.ptr(wt.folds), _lib.ptr(wt.scores),
             _lib.ptr(wt.scores_ep), wt.valid_size, nseg, _lib.ptr(tm_d), _lib.ptr(dt_d),
             _lib.ptr(si_d), _lib.ptr(fold), stride, self.spec, _lib.ptr(self._err),

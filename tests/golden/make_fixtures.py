@@ -187,7 +187,8 @@ def circ_series(n: int, tsamp: float, f0: float, p_orb: float, x_orb: float, see
 def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
                max_sugg: int = 2**16, batch_size: int = 64, ref_seg: int = 8,
                fold_levels: tuple = (5, 11), thr_offset: float = 0.0,
-               leaf_cap: int = 6000, basis: str = "taylor", circular: bool = False) -> None:
+               leaf_cap: int = 6000, basis: str = "taylor", circular: bool = False,
+               fourier: bool = False) -> None:
     """Enumerate-prune run of 15 levels (real folds): Taylor/Chebyshev of
     order 3, or (``circular``) the circular-orbit Taylor tree of order 5."""
     import tempfile
@@ -207,7 +208,7 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
         lim = ParamLimits.from_taylor((100.0, 101.0), accel=(-20000.0, 20000.0),
                                       jerk=(-3000.0, 3000.0)).limits
     cfg = PulsarSearchConfig(nsamps=n, tsamp=tsamp, nbins=nbins, eta=1.0, param_limits=lim,
-                             ducy_max=0.3, wtsp=2.0, use_fourier=False, bseg_ffa=n // 16,
+                             ducy_max=0.3, wtsp=2.0, use_fourier=fourier, bseg_ffa=n // 16,
                              prune_poly_order=order, branch_max=16, tiling_strategy=tiling,
                              p_orb_min=p_orb_min)
     dyp = DynamicProgramming(TimeSeries(ts_e, ts_v, tsamp), cfg)
@@ -223,7 +224,7 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
            "max_sugg": np.int64(max_sugg), "batch_size": np.int64(batch_size),
            "ref_seg": np.int64(ref_seg), "moving": np.int64(moving),
            "poly_order": np.int64(order), "branch_max": np.int64(16), "basis": np.str_(basis),
-           "p_orb_min": np.float64(p_orb_min),
+           "p_orb_min": np.float64(p_orb_min), "fourier": np.int64(fourier),
            "fold_ffa": np.asarray(dyp.fold), "scheme": prn.scheme.data.copy()}
     wt = prn.world_tree
     out["seed_leaves"] = wt.leaves[: wt.valid_size].copy()
@@ -329,6 +330,9 @@ def main() -> None:
     if "--fourier-only" in sys.argv:
         fourier_cases()
         return
+    if "--fourier-prune-only" in sys.argv:
+        fourier_prune_cases()
+        return
     if "--prune-only" in sys.argv:
         prune_cases()
         cheby_cases()
@@ -344,6 +348,11 @@ def main() -> None:
 def fourier_cases() -> None:
     fourier_case("ffa_freq_fourier", 2**16, [(10.0, 14.0)], 64, 12.3, 24)
     fourier_case("ffa_accel_fourier", 2**16, [(-1.0e6, 1.0e6), (200.0, 203.0)], 32, 201.6, 25)
+
+
+def fourier_prune_cases() -> None:
+    prune_case("prune_taylor_fourier", fourier=True, fold_levels=(5, 11))
+    prune_case("prune_cheby_fourier", fourier=True, basis="chebyshev", fold_levels=())
 
 
 def circ_cases() -> None:
