@@ -334,6 +334,7 @@ def bench_gpu(args) -> dict | None:
     import torch
 
     from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.replicas import max_over_ranks
     from pyloki_gb300.search import ffa_search
     from pyloki_gb300.timeseries import TimeSeries
 
@@ -392,10 +393,7 @@ def bench_gpu(args) -> dict | None:
         phases["brutefold"] += marks["start"].elapsed_time(marks["brutefold"])
         phases["levels"] += marks["brutefold"].elapsed_time(marks["levels"])
         phases["final"] += marks["levels"].elapsed_time(marks["final"])
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, dist, dev)  # the slowest replica
     ms_per_step = total_ms / args.steps
 
     # ---- end to end through the public API, host buffers ------------------
@@ -411,11 +409,7 @@ def bench_gpu(args) -> dict | None:
         best = pg.find_best_params(ignore_nan=True)
         del pg
     barrier()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist, dev)
 
     if rank != 0:
         if dist is not None:
