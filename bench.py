@@ -42,6 +42,8 @@ WORKLOAD = "ffa_accel_search_2^23"
 # capture of three launches of the same search at 2^21 samples (122.75 MB per
 # launch, 474k trials per launch); profiles/band_union64_kernel_ffa_accel_2^21.md.
 UNION_DRAM_BYTES_PER_TRIAL = 259.0
+BF16_TOP = 64        # candidates re-scored in FP64 and checked against the FP64 oracle
+BF16_SAMPLE = 192    # random trials added to the FP64 error sample
 
 
 def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0):
@@ -361,8 +363,8 @@ def bench_gpu(args) -> dict | None:
         if dist is not None:
             dist.barrier()
 
-    def one_step(events=None):
-        dyp = DynamicProgramming(ts_dev, cfg, device=dev)
+    def one_step(events=None, storage="f32"):
+        dyp = DynamicProgramming(ts_dev, cfg, device=dev, storage=storage)
         snr = dyp.search(band_bytes=args.band_bytes, phase_events=events)
         return dyp, snr
 
@@ -477,6 +479,9 @@ def bench_gpu(args) -> dict | None:
                                "sample": f"same search restricted to "
                                          f"{500 - args.cpu_band_hz:g}-500 Hz ({nt} trials, "
                                          f"{dt:.1f} s)"}
+    if not args.no_bf16:
+        out["ffa_bf16"] = bench_bf16(args, dev, cfg, ts_dev, ts_host, one_step, trials,
+                                     ms_per_step)
     if not args.no_prune:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
@@ -484,6 +489,85 @@ def bench_gpu(args) -> dict | None:
     if dist is not None:
         dist.destroy_process_group()
     return out
+
+
+def bench_bf16(args, dev, cfg, ts_dev, ts_host, one_step, trials, f32_ms) -> dict:
+    """The same search with bfloat16 fold storage (FP32 arithmetic): device
+    throughput, then the S/N error against the FP64 oracle on the top
+    candidates plus a random sample of trials, and the FP64 GPU re-scoring of
+    the same trials against the same oracle."""
+    import torch
+
+    from oracle import oracle as O
+
+    for _ in range(args.warmup):
+        one_step(storage="bf16")
+    torch.cuda.synchronize(dev)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    phases = {"brutefold": 0.0, "levels": 0.0, "final": 0.0}
+    step_events = []
+    start.record()
+    for _ in range(args.steps):
+        ev: list = []
+        dyp, snr = one_step(ev, storage="bf16")
+        step_events.append(ev)
+        del snr
+    end.record()
+    torch.cuda.synchronize(dev)
+    ms = start.elapsed_time(end) / args.steps
+    for ev in step_events:
+        marks = dict(ev)
+        phases["brutefold"] += marks["start"].elapsed_time(marks["brutefold"]) / args.steps
+        phases["levels"] += marks["brutefold"].elapsed_time(marks["levels"]) / args.steps
+        phases["final"] += marks["levels"].elapsed_time(marks["final"]) / args.steps
+    # precision: top candidates + random trials against the FP64 oracle
+    dyp, snr = one_step(storage="bf16")
+    flat = snr.reshape(-1, snr.shape[-1])
+    # trials with an empty bin (v = 0) have S/N NaN, as in the reference
+    best = torch.nan_to_num(flat.amax(dim=1), nan=float("-inf"))
+    top = torch.topk(best, BF16_TOP).indices.cpu().numpy()
+    rng = np.random.default_rng(7)
+    pick = np.unique(np.r_[top, rng.integers(0, flat.shape[0], BF16_SAMPLE)])
+    t0 = time.perf_counter()
+    ref = O.boxcar_snr_f64(O.ffa_trials(ts_host.ts_e, ts_host.ts_v, cfg, pick, f64=True),
+                           cfg.score_widths)
+    t_oracle = time.perf_counter() - t0
+    got = flat[torch.from_numpy(pick).to(dev)].double().cpu().numpy()
+    cand = torch.from_numpy(top).to(dev)
+    torch.cuda.synchronize(dev)
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    r0.record()
+    resc_top = dyp.rescore(cand)
+    r1.record()
+    torch.cuda.synchronize(dev)
+    resc = dyp.rescore(torch.from_numpy(pick).to(dev)).cpu().numpy()
+    fin = np.isfinite(ref) & np.isfinite(got)
+    nan_mismatch = int((np.isnan(ref) != np.isnan(got)).sum())
+    err = np.where(fin, np.abs(got - ref), 0.0)
+    rel = err / np.maximum(np.abs(np.where(fin, ref, 1.0)), 1.0)
+    rfin = np.isfinite(ref) & np.isfinite(resc)
+    rerr = np.where(rfin, np.abs(resc - ref), 0.0) / np.maximum(
+        np.abs(np.where(rfin, ref, 1.0)), 1.0)
+    in_top = np.isin(pick, top)
+    del resc_top
+    return {
+        "value": trials / (ms * 1e-3), "unit": "trials/s", "ms_per_step": ms,
+        "speedup_vs_f32_storage": f32_ms / ms, "dtype": "bf16 storage, f32 arithmetic",
+        "phases_ms": phases,
+        "snr_error_vs_fp64": {
+            "trials": int(len(pick)), "top_candidates": BF16_TOP,
+            "max_abs": float(err.max()), "max_rel": float(rel.max()),
+            "median_abs": float(np.median(err[fin])),
+            "nan_mismatch": nan_mismatch,
+            "top_max_abs": float(err[in_top].max()),
+            "rescored_max_rel": float(rerr.max()),
+            "rescore_ms_top": r0.elapsed_time(r1),
+            "oracle_s": t_oracle,
+            "note": "rel = |err| / max(|S/N_fp64|, 1); rescored = FP64 GPU re-scoring "
+                    "from the FP32 level-0 fold"},
+    }
 
 
 def bench_reference(args) -> dict | None:
@@ -559,6 +643,8 @@ def main() -> None:
     ap.add_argument("--band-bytes", type=int, default=96 << 20)
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-bf16", action="store_true",
+                    help="skip the bfloat16-storage search and its FP64 error check")
     ap.add_argument("--no-prune", action="store_true",
                     help="skip the enumerate-prune (leaves/s) measurement")
     ap.add_argument("--profile-once", action="store_true",

@@ -37,6 +37,7 @@ extern "C" {
 
 #define LOKI_MAX_PARAMS 5
 #define LOKI_MAX_WIDTHS 64
+#define LOKI_MAX_RESCORE_LEVELS 24
 
 /* One FFA dynamic-programming level: the current grid (optionally a window of
  * its last, frequency, dimension) resolved against the previous level's grid
@@ -45,7 +46,8 @@ typedef struct {
   int32_t nparams;          /* 1..5, order [..., jerk, accel, freq] */
   int32_t nbins;            /* profile bins */
   int32_t level;            /* current FFA level, >= 1 */
-  int32_t reserved;
+  int32_t storage;          /* fold element type: 0 float32, 1 bfloat16 (adds and
+                               scores in float32; each stored value rounded once) */
   double tseg_brute;        /* seconds, bseg_brute * tsamp */
   int64_t counts_cur[LOKI_MAX_PARAMS];   /* full grid counts, current level */
   int64_t counts_prev[LOKI_MAX_PARAMS];  /* full grid counts, previous level */
@@ -76,7 +78,9 @@ typedef struct {
   int32_t nwidths;
   int32_t wmax;             /* max(widths) */
   int32_t mode;             /* 0: one S/N per width; 1: max over widths */
-  int32_t reserved;
+  int32_t nseg;             /* fused final level only: output segments scored,
+                               0 or 1 = segment 0; S/N rows are segment-major
+                               (nseg, full grid, nout). Ignored elsewhere. */
   double inv_stdnoise;
   int32_t widths[LOKI_MAX_WIDTHS];
   double hb[LOKI_MAX_WIDTHS];
@@ -132,7 +136,7 @@ int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords, int32_t* dev_er
 /* One FFA DP level: fold_out[ipair, p] = roll(fold_in[2 ipair, tail(p)], s_t)
  * + roll(fold_in[2 ipair + 1, head(p)], s_h). Replaces unify_fold
  * (dynamic/dyn_pffa.py:435-489) with shift_add (core/common.py:304-324). */
-int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, float* fold_out,
+int loki_ffa_level(const LokiFFALevel* lvl, const void* fold_in, void* fold_out,
                    int32_t* dev_err, void* stream);
 
 /* Final FFA level fused with normalisation and boxcar scoring of segment 0:
@@ -140,7 +144,7 @@ int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, float* fold_ou
  * boxcar_snr_nd (detection/scoring.py:156-165) in one pass; the final fold is
  * never written. snr is the full-grid array (P_full, nwidths), or (P_full,)
  * in mode 1; a frequency window writes only its own rows. */
-int loki_ffa_level_score(const LokiFFALevel* lvl, const float* fold_in,
+int loki_ffa_level_score(const LokiFFALevel* lvl, const void* fold_in,
                          const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
                          void* stream);
 
@@ -164,7 +168,7 @@ int loki_ffa_band_windows(const LokiFFALevel* lvl, int64_t band_width,
  * win_lo / win_hi are HOST arrays (from loki_ffa_band_windows). */
 int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
                           int64_t band_width, const int64_t* win_lo, const int64_t* win_hi,
-                          const float* fold_pp, float* scratch, int64_t scratch_floats,
+                          const void* fold_pp, float* scratch, int64_t scratch_floats,
                           const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
                           void* stream);
 
@@ -173,6 +177,31 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
  * tables. Returns -1 for invalid descriptors. */
 int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                       int64_t max_window);
+
+/* Round n float32 values to bfloat16 (nearest even): the brute fold, summed
+ * in float32, enters a bfloat16-stored FFA (LokiFFALevel.storage = 1).
+ * No reference counterpart: the reference stores float32 only. */
+int loki_f32_to_bf16(const float* in, int64_t n, void* out, void* stream);
+
+/* FP64 re-scoring of FFA candidates. levels[l - 1] describes FFA level l
+ * (full grids, l = 1 .. nlevels, the last being the candidates' level); the
+ * series (ts_e, ts_v, device float32, nsamps samples) and the level-0
+ * frequency grid freqs0 (device, nfreq0 values) are those of the search;
+ * cand holds ncand flat parameter indices of the last level (device). Each
+ * candidate's fold of segment seg is rebuilt from the samples: the resolve
+ * tree (dynamic/dyn_pffa.py:462-489) gives every level-0 segment's frequency
+ * and accumulated shift, its samples are binned as in the brute fold
+ * (core/fold.py:108-171) and everything is summed in float64. snr receives
+ * (ncand, nwidths) boxcar S/N (detection/scoring.py:99-140) in float64 and
+ * prof, if not NULL, the float64 profiles (ncand, 2, nbins). A candidate
+ * index outside the last level's grid yields NaN rows.
+ * No reference counterpart: it backs bfloat16 fold storage, whose retained
+ * candidates are re-scored here. */
+int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, const float* ts_e,
+                     const float* ts_v, int64_t nsamps, double tsamp, int64_t bseg_brute,
+                     const double* freqs0, int64_t nfreq0, const int64_t* cand, int64_t ncand,
+                     int64_t seg, const LokiScoreSpec* spec, double* snr, double* prof,
+                     void* stream);
 
 /* ---- FFA (Fourier domain, complex64 = 2 x float32 per coefficient) ----
  * Folds are (nseg, nparams..., 2, nbins / 2 + 1) complex64, nbins even.

@@ -401,3 +401,63 @@ void oracle_ffa_trials(const float* ts_e, const float* ts_v, int64_t nsamps, dou
     profile_rec(&S, level, seg, idx, out + (size_t)k * 2 * nbins);
   }
 }
+
+/* The same single-trial recursion with every profile held and summed in
+ * float64 (level-0 brute folds of the float32 samples, then the shift-adds):
+ * the FP64 reference for reduced-precision fold storage. */
+static void profile_rec_f64(const OracleSeries* S, int level, int64_t seg, const int64_t* idx,
+                            double* out) {
+  const int n = S->n, nb = S->nbins;
+  if (level == 0) {
+    const double f = S->params[n - 1][idx[n - 1]];
+    const double t_ref = (n == 1) ? 0.0 : (double)S->bseg_brute * S->tsamp / 2;
+    memset(out, 0, 2 * nb * sizeof(double));
+    const int64_t start = seg * S->bseg_brute;
+    for (int64_t i = 0; i < S->bseg_brute && start + i < S->nsamps; ++i) {
+      const double pt = (double)i * S->tsamp - t_ref;
+      const int b = round_shift(phase_idx(pt, f, nb, 0.0), nb);
+      out[b] += (double)S->ts_e[start + i];
+      out[nb + b] += (double)S->ts_v[start + i];
+    }
+    return;
+  }
+  double pset[MAXP];
+  int64_t it[MAXP], ih[MAXP];
+  for (int d = 0; d < n; ++d) pset[d] = S->params[level * n + d][idx[d]];
+  const int64_t* cprev = S->counts + (size_t)(level - 1) * n;
+  const double pht = oracle_ffa_resolve(pset, n, cprev, S->limits, level, 0, S->tseg_brute, nb, it);
+  const double phh = oracle_ffa_resolve(pset, n, cprev, S->limits, level, 1, S->tseg_brute, nb, ih);
+  double* t = (double*)malloc(4 * nb * sizeof(double));
+  double* h = t + 2 * nb;
+  profile_rec_f64(S, level - 1, 2 * seg, it, t);
+  profile_rec_f64(S, level - 1, 2 * seg + 1, ih, h);
+  const int st = round_shift(pht, nb), sh = round_shift(phh, nb);
+  for (int j = 0; j < nb; ++j) {
+    const int i1 = ((j - st) % nb + nb) % nb;
+    const int i2 = ((j - sh) % nb + nb) % nb;
+    out[j] = t[i1] + h[i2];
+    out[nb + j] = t[nb + i1] + h[nb + i2];
+  }
+  free(t);
+}
+
+void oracle_ffa_trials_f64(const float* ts_e, const float* ts_v, int64_t nsamps, double tsamp,
+                           int64_t bseg_brute, int n, int nbins, const double* limits,
+                           const int64_t* counts, const double* const* params, int level,
+                           int64_t seg, const int64_t* flat_idx, int64_t ntrials, double* out,
+                           int nthreads) {
+  set_threads(nthreads);
+  OracleSeries S = {ts_e, ts_v, nsamps, tsamp, bseg_brute, n, nbins,
+                    (double)bseg_brute * tsamp, limits, counts, params};
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < ntrials; ++k) {
+    int64_t idx[MAXP];
+    int64_t rest = flat_idx[k];
+    for (int d = n - 1; d >= 0; --d) {
+      const int64_t c = counts[(size_t)level * n + d];
+      idx[d] = rest % c;
+      rest /= c;
+    }
+    profile_rec_f64(&S, level, seg, idx, out + (size_t)k * 2 * nbins);
+  }
+}

@@ -157,13 +157,15 @@ def fold_norm(folds):
     return out.reshape(*folds.shape[:-2], nb)
 
 
-def ffa_trials(ts_e, ts_v, cfg, flat_idx, level=None, seg=0, nthreads=0):
+def ffa_trials(ts_e, ts_v, cfg, flat_idx, level=None, seg=0, nthreads=0, f64=False):
     """Fold ``(ntrials, 2, nbins)`` of chosen parameter sets at ``level``
-    (default: the final level), segment ``seg``, by single-trial recursion."""
+    (default: the final level), segment ``seg``, by single-trial recursion.
+    ``f64`` holds and sums every profile in float64 (the FP64 reference)."""
     lib = load()
     if not hasattr(lib, "_trials_bound"):
-        lib.oracle_ffa_trials.argtypes = [_P, _P, _I64, _D, _I64, _I32, _I32, _P, _P, _P, _I32,
-                                          _I64, _P, _I64, _P, _I32]
+        for fn in (lib.oracle_ffa_trials, lib.oracle_ffa_trials_f64):
+            fn.argtypes = [_P, _P, _I64, _D, _I64, _I32, _I32, _P, _P, _P, _I32,
+                           _I64, _P, _I64, _P, _I32]
         lib._trials_bound = True
     level = cfg.niters_ffa if level is None else level
     n = cfg.nparams
@@ -175,8 +177,31 @@ def ffa_trials(ts_e, ts_v, cfg, flat_idx, level=None, seg=0, nthreads=0):
     counts = np.ascontiguousarray([[len(p) for p in g] for g in grids], np.int64)
     limits = np.ascontiguousarray(cfg.param_limits, np.float64)
     flat_idx = np.ascontiguousarray(flat_idx, np.int64)
-    out = np.empty((len(flat_idx), 2, cfg.nbins), np.float32)
-    lib.oracle_ffa_trials(_p(ts_e), _p(ts_v), len(ts_e), cfg.tsamp, cfg.bseg_brute, n,
-                          cfg.nbins, _p(limits), _p(counts), C.cast(ptrs, C.c_void_p), level,
-                          seg, _p(flat_idx), len(flat_idx), _p(out), nthreads)
+    out = np.empty((len(flat_idx), 2, cfg.nbins), np.float64 if f64 else np.float32)
+    fn = lib.oracle_ffa_trials_f64 if f64 else lib.oracle_ffa_trials
+    fn(_p(ts_e), _p(ts_v), len(ts_e), cfg.tsamp, cfg.bseg_brute, n, cfg.nbins, _p(limits),
+       _p(counts), C.cast(ptrs, C.c_void_p), level, seg, _p(flat_idx), len(flat_idx), _p(out),
+       nthreads)
+    return out
+
+
+def boxcar_snr_f64(folds, widths, stdnoise=1.0):
+    """Boxcar S/N ``(n, nwidths)`` of ``(n, 2, nbins)`` folds with every step in
+    float64 (detection/scoring.py:42-71 circular prefix, 99-140 S/N)."""
+    folds = np.asarray(folds, np.float64)
+    nb = folds.shape[-1]
+    widths = np.asarray(widths, np.int64)
+    norm = folds[:, 0, :] / np.sqrt(folds[:, 1, :])
+    pre = np.cumsum(norm, axis=1)
+    total = pre[:, -1:]
+    wmax = int(widths.max())
+    ext = np.arange(nb + wmax)
+    pre_ext = pre[:, ext % nb] + (ext // nb)[None, :] * total
+    out = np.empty((len(folds), len(widths)))
+    for k, w in enumerate(widths):
+        size_w = nb - w
+        height = np.sqrt(size_w / (nb * w))
+        b = w * height / size_w
+        dmax = (pre_ext[:, w:w + nb] - pre_ext[:, :nb]).max(axis=1)
+        out[:, k] = ((height + b) * dmax - b * total[:, 0]) / stdnoise
     return out

@@ -23,6 +23,7 @@ LOKI_DEVERR_BRANCH = 2
 
 MAX_PARAMS = 5
 MAX_WIDTHS = 64
+MAX_RESCORE_LEVELS = 24
 
 _LIB_PATH = Path(__file__).resolve().parent / "libloki_gb300.so"
 
@@ -32,7 +33,7 @@ class LokiFFALevel(C.Structure):
         ("nparams", C.c_int32),
         ("nbins", C.c_int32),
         ("level", C.c_int32),
-        ("reserved", C.c_int32),
+        ("storage", C.c_int32),
         ("tseg_brute", C.c_double),
         ("counts_cur", C.c_int64 * MAX_PARAMS),
         ("counts_prev", C.c_int64 * MAX_PARAMS),
@@ -61,7 +62,7 @@ class LokiScoreSpec(C.Structure):
         ("nwidths", C.c_int32),
         ("wmax", C.c_int32),
         ("mode", C.c_int32),
-        ("reserved", C.c_int32),
+        ("nseg", C.c_int32),
         ("inv_stdnoise", C.c_double),
         ("widths", C.c_int32 * MAX_WIDTHS),
         ("hb", C.c_double * MAX_WIDTHS),
@@ -150,6 +151,10 @@ SIGNATURES: dict[str, tuple] = {
     "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
+    "loki_f32_to_bf16": (C.c_int, [_P, _I64, _P, _P]),
+    "loki_ffa_rescore": (C.c_int, [C.POINTER(LokiFFALevel), _I32, _P, _P, _I64, _D, _I64, _P,
+                                   _I64, _P, _I64, _I64, C.POINTER(LokiScoreSpec), _P, _P,
+                                   _P]),
     "loki_brutefold_complex": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
     "loki_ffa_level_complex": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
     "loki_fold_norm_complex": (C.c_int, [_P, _I64, _I32, _P, _P]),

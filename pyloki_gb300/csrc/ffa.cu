@@ -3,6 +3,11 @@
 //
 // Data layout in HBM (identical to pyloki): fold (nseg, P, 2, nbins) float32,
 // C-contiguous, P = flattened parameter grid with the frequency axis fastest.
+// With LokiFFALevel.storage = 1 the folds are stored as bfloat16 instead:
+// every add and every score is still evaluated in float32, each stored
+// profile value is rounded once to bfloat16 (round to nearest even).
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 #include "loki_common.cuh"
@@ -10,6 +15,47 @@
 #include "score.cuh"
 
 namespace loki {
+
+// Element access of a fold stored as S (float or bfloat16), in float32.
+template <typename S>
+struct Store;
+
+template <>
+struct Store<float> {
+  // four consecutive values, g = index of the 16-byte group
+  static __device__ __forceinline__ float4 load4(const float* p, size_t g) {
+    return __ldg(reinterpret_cast<const float4*>(p) + g);
+  }
+  static __device__ __forceinline__ void store4(float* p, size_t g, float4 v) {
+    reinterpret_cast<float4*>(p)[g] = v;
+  }
+  static __device__ __forceinline__ float load(const float* p) { return __ldg(p); }
+  static __device__ __forceinline__ void store(float* p, float v) { *p = v; }
+};
+
+template <>
+struct Store<__nv_bfloat16> {
+  static __device__ __forceinline__ float4 load4(const __nv_bfloat16* p, size_t g) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(p) + g);
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+  static __device__ __forceinline__ void store4(__nv_bfloat16* p, size_t g, float4 v) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
+    uint2 u;
+    u.x = *reinterpret_cast<const unsigned*>(&a);
+    u.y = *reinterpret_cast<const unsigned*>(&b);
+    reinterpret_cast<uint2*>(p)[g] = u;
+  }
+  static __device__ __forceinline__ float load(const __nv_bfloat16* p) {
+    return __bfloat162float(p[0]);
+  }
+  static __device__ __forceinline__ void store(__nv_bfloat16* p, float v) {
+    *p = __float2bfloat16_rn(v);
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Plan table (exact FP64 path; the f32 shift is part of the output)
@@ -154,10 +200,10 @@ constexpr int kBatch = 4;
 
 // nbins == 64: one float4 per lane per row, four rows in flight per lane.
 // One warp's work: output parameters [q0, q0 + 32).
+template <typename S>
 __device__ __forceinline__ void level64_warp(const LokiFFALevel& L, const LevelK& K,
-                                             const float* __restrict__ in,
-                                             float* __restrict__ out, int32_t* err,
-                                             const OtherTable& T, bool tab,
+                                             const S* __restrict__ in, S* __restrict__ out,
+                                             int32_t* err, const OtherTable& T, bool tab,
                                              const OtherRes* __restrict__ gtab,
                                              int64_t n_other, int64_t q0) {
   const int lane = threadIdx.x & 31;
@@ -167,9 +213,10 @@ __device__ __forceinline__ void level64_warp(const LokiFFALevel& L, const LevelK
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
   const int64_t nseg_out = L.nseg_in / 2;
   for (int64_t ip = 0; ip < nseg_out; ++ip) {
-    const float4* in_t = reinterpret_cast<const float4*>(in) + (size_t)(2 * ip) * P_in * 32;
-    const float4* in_h = reinterpret_cast<const float4*>(in) + (size_t)(2 * ip + 1) * P_in * 32;
-    float4* o = reinterpret_cast<float4*>(out) + ((size_t)ip * Q + q0) * 32;
+    // rows of 32 four-value groups
+    const size_t g_t = (size_t)(2 * ip) * P_in * 32;
+    const size_t g_h = (size_t)(2 * ip + 1) * P_in * 32;
+    const size_t g_o = ((size_t)ip * Q + q0) * 32;
     for (int k0 = 0; k0 < kmax; k0 += kBatch) {
       float4 tv[kBatch], hv[kBatch];
       int st[kBatch], sh[kBatch];
@@ -184,8 +231,8 @@ __device__ __forceinline__ void level64_warp(const LokiFFALevel& L, const LevelK
         sh[u] = __shfl_sync(0xFFFFFFFFu, me.sh, src);
         ok[u] = __shfl_sync(0xFFFFFFFFu, me.ok, src) && k < kmax;
         if (ok[u]) {
-          tv[u] = __ldg(in_t + (size_t)it * 32 + lane);
-          hv[u] = __ldg(in_h + (size_t)ih * 32 + lane);
+          tv[u] = Store<S>::load4(in, g_t + (size_t)it * 32 + lane);
+          hv[u] = Store<S>::load4(in, g_h + (size_t)ih * 32 + lane);
         }
       }
 #pragma unroll
@@ -193,16 +240,17 @@ __device__ __forceinline__ void level64_warp(const LokiFFALevel& L, const LevelK
         if (!ok[u]) continue;  // uniform across the warp
         const float4 a = roll64(tv[u], st[u], lane);
         const float4 b = roll64(hv[u], sh[u], lane);
-        o[(size_t)(k0 + u) * 32 + lane] = add4(a, b);
+        Store<S>::store4(out, g_o + (size_t)(k0 + u) * 32 + lane, add4(a, b));
       }
     }
   }
 }
 
+template <typename S>
 __global__ void __launch_bounds__(kLevelWarps * 32, 4)
-ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
-                   float* __restrict__ out, int32_t* __restrict__ err,
-                   const OtherRes* __restrict__ gtab, int64_t n_other) {
+ffa_level64_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in, S* __restrict__ out,
+                   int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
+                   int64_t n_other) {
   __shared__ OtherTable T;
   const int warp = threadIdx.x >> 5;
   const int64_t Q = n_out_params(L);
@@ -216,10 +264,11 @@ ffa_level64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
 }
 
 // Any nbins: scalar, lane j handles bins j, j + 32, ...
+template <typename S>
 __global__ void __launch_bounds__(kLevelWarps * 32, 4)
-ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
-                 float* __restrict__ out, int32_t* __restrict__ err,
-                 const OtherRes* __restrict__ gtab, int64_t n_other) {
+ffa_level_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in, S* __restrict__ out,
+                 int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
+                 int64_t n_other) {
   __shared__ OtherTable T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t Q = n_out_params(L), P_in = n_in_params(L);
@@ -237,9 +286,9 @@ ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
   const int64_t nseg_out = L.nseg_in / 2;
   const size_t row = (size_t)2 * nb;
   for (int64_t ip = 0; ip < nseg_out; ++ip) {
-    const float* in_t = in + (size_t)(2 * ip) * P_in * row;
-    const float* in_h = in + (size_t)(2 * ip + 1) * P_in * row;
-    float* o_base = out + ((size_t)ip * Q + q0) * row;
+    const S* in_t = in + (size_t)(2 * ip) * P_in * row;
+    const S* in_h = in + (size_t)(2 * ip + 1) * P_in * row;
+    S* o_base = out + ((size_t)ip * Q + q0) * row;
     for (int k = 0; k < kmax; ++k) {
       const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, k);
       const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, k);
@@ -247,16 +296,17 @@ ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
       const int sh = __shfl_sync(0xFFFFFFFFu, me.sh, k);
       const bool ok = __shfl_sync(0xFFFFFFFFu, me.ok, k);
       if (!ok) continue;
-      const float* t = in_t + (size_t)it * row;
-      const float* h = in_h + (size_t)ih * row;
-      float* o = o_base + (size_t)k * row;
+      const S* t = in_t + (size_t)it * row;
+      const S* h = in_h + (size_t)ih * row;
+      S* o = o_base + (size_t)k * row;
       for (int j = lane; j < nb; j += 32) {
         int jt = j - st;
         jt += (jt < 0) ? nb : 0;
         int jh = j - sh;
         jh += (jh < 0) ? nb : 0;
-        o[j] = __fadd_rn(t[jt], h[jh]);
-        o[nb + j] = __fadd_rn(t[nb + jt], h[nb + jh]);
+        Store<S>::store(o + j, __fadd_rn(Store<S>::load(t + jt), Store<S>::load(h + jh)));
+        Store<S>::store(o + nb + j,
+                        __fadd_rn(Store<S>::load(t + nb + jt), Store<S>::load(h + nb + jh)));
       }
     }
   }
@@ -270,15 +320,28 @@ ffa_level_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
 
 constexpr int kScoreWarps = 4;
 
+// Segments scored by one fused final-level launch: spec.nseg output segments
+// (0 means 1: segment 0 only), S/N rows segment-major.
+__host__ __device__ __forceinline__ int64_t n_score_segs(const LokiScoreSpec& sp) {
+  return sp.nseg > 1 ? sp.nseg : 1;
+}
+
+__host__ __device__ __forceinline__ int64_t n_full_params(const LokiFFALevel& L) {
+  int64_t q = 1;
+  for (int d = 0; d < L.nparams; ++d) q *= L.counts_cur[d];
+  return q;
+}
+
 __device__ __forceinline__ void score_out(const LokiFFALevel& L, const LevelK& K,
                                           const LokiScoreSpec& sp, const ScoreK& SK,
                                           float* tile, int stride, int lane, int64_t q0,
-                                          int kmax, float* snr) {
+                                          int kmax, float* snr, int64_t seg) {
   __syncwarp();
   if (lane < kmax) {
     int64_t other, off;
     q_split(L, K, q0 + lane, other, off);
-    const int64_t full = other * L.counts_cur[L.nparams - 1] + L.out_start + off;
+    const int64_t full = seg * n_full_params(L) + other * L.counts_cur[L.nparams - 1] +
+                         L.out_start + off;
     const int nout = sp.mode == 0 ? sp.nwidths : 1;
     float* row = tile + lane * stride;
     if (SK.pow2_64) score_row64_pow2(row, sp, SK, snr + (size_t)full * nout);
@@ -287,21 +350,23 @@ __device__ __forceinline__ void score_out(const LokiFFALevel& L, const LevelK& K
 }
 
 // One warp's work of the fused final level: parameters [q0, q0 + 32).
+template <typename S>
 __device__ __forceinline__ void score64_warp(const LokiFFALevel& L, const LevelK& K,
-                                             const float* __restrict__ in,
+                                             const S* __restrict__ in,
                                              const LokiScoreSpec& sp, const ScoreK& SK,
                                              float* __restrict__ snr, int32_t* err,
                                              const OtherTable& T, bool tab,
                                              const OtherRes* __restrict__ gtab,
-                                             int64_t n_other, int64_t q0, float* tile) {
+                                             int64_t n_other, int64_t q0, float* tile,
+                                             int64_t seg) {
   const int lane = threadIdx.x & 31;
   const int stride = score_stride(64, sp.wmax);
   const int64_t Q = n_out_params(L), P_in = n_in_params(L);
   if (q0 >= Q) return;
   const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
-  const float* in_t = in;                     // segment 0 of fold_in
-  const float* in_h = in + (size_t)P_in * 128;  // segment 1 of fold_in
+  const S* in_t = in + (size_t)(2 * seg) * P_in * 128;  // segment 2 seg of fold_in
+  const S* in_h = in_t + (size_t)P_in * 128;            // segment 2 seg + 1
   // Lane j gathers bins j and j + 32 of both components at the rolled
   // positions, so it owns e and v of its two output bins.
   for (int k0 = 0; k0 < kmax; k0 += kBatch) {
@@ -317,18 +382,18 @@ __device__ __forceinline__ void score64_warp(const LokiFFALevel& L, const LevelK
       const int sh = __shfl_sync(0xFFFFFFFFu, me.sh, src);
       ok[u] = __shfl_sync(0xFFFFFFFFu, me.ok, src) && k < kmax;
       if (ok[u]) {
-        const float* t = in_t + (size_t)it * 128;
-        const float* h = in_h + (size_t)ih * 128;
+        const S* t = in_t + (size_t)it * 128;
+        const S* h = in_h + (size_t)ih * 128;
         const int jt0 = (lane - st) & 63, jt1 = (lane + 32 - st) & 63;
         const int jh0 = (lane - sh) & 63, jh1 = (lane + 32 - sh) & 63;
-        te[u][0] = __ldg(t + jt0);
-        te[u][1] = __ldg(t + jt1);
-        tv[u][0] = __ldg(t + 64 + jt0);
-        tv[u][1] = __ldg(t + 64 + jt1);
-        he[u][0] = __ldg(h + jh0);
-        he[u][1] = __ldg(h + jh1);
-        hv[u][0] = __ldg(h + 64 + jh0);
-        hv[u][1] = __ldg(h + 64 + jh1);
+        te[u][0] = Store<S>::load(t + jt0);
+        te[u][1] = Store<S>::load(t + jt1);
+        tv[u][0] = Store<S>::load(t + 64 + jt0);
+        tv[u][1] = Store<S>::load(t + 64 + jt1);
+        he[u][0] = Store<S>::load(h + jh0);
+        he[u][1] = Store<S>::load(h + jh1);
+        hv[u][0] = Store<S>::load(h + 64 + jh0);
+        hv[u][1] = Store<S>::load(h + 64 + jh1);
       }
     }
 #pragma unroll
@@ -349,11 +414,12 @@ __device__ __forceinline__ void score64_warp(const LokiFFALevel& L, const LevelK
       }
     }
   }
-  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr);
+  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr, seg);
 }
 
+template <typename S>
 __global__ void __launch_bounds__(kScoreWarps * 32)
-ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in,
                          LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
                          int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
                          int64_t n_other) {
@@ -362,13 +428,15 @@ ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
   const int warp = threadIdx.x >> 5;
   float* tile = tiles + (size_t)warp * 32 * score_stride(64, sp.wmax);
   const int64_t Q = n_out_params(L);
-  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t nblk = (Q + blockDim.x - 1) / blockDim.x;  // blocks per segment
+  const int64_t seg = blockIdx.x / nblk;
+  const int64_t qb = (blockIdx.x - seg * nblk) * blockDim.x;
   bool tab = false;
   if (!gtab) {  // uniform: the whole block takes the same branch
     tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
     __syncthreads();
   }
-  score64_warp(L, K, in, sp, SK, snr, err, T, tab, gtab, n_other, qb + warp * 32, tile);
+  score64_warp(L, K, in, sp, SK, snr, err, T, tab, gtab, n_other, qb + warp * 32, tile, seg);
 }
 
 // Banded pipeline step (nbins == 64): blocks [0, nblk_f) score final band k
@@ -378,28 +446,32 @@ ffa_level_score64_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
 // step k + 1 starts after step k has finished both halves.
 // Five resident blocks per SM (<= 102 registers): measured 12 % faster than
 // the register-limited four, though ptxas then spills 64 bytes per thread.
+template <typename S>
 __global__ void __launch_bounds__(kScoreWarps * 32, 5)
-band_union64_kernel(LokiFFALevel F, LevelK KF, const float* __restrict__ in_f,
+band_union64_kernel(LokiFFALevel F, LevelK KF, const S* __restrict__ in_f,
                     LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
                     const OtherRes* __restrict__ tab_f, int64_t no_f, int64_t nblk_f,
-                    LokiFFALevel P, LevelK KP, const float* __restrict__ in_p,
-                    float* __restrict__ out_p, const OtherRes* __restrict__ tab_p,
+                    LokiFFALevel P, LevelK KP, const S* __restrict__ in_p,
+                    S* __restrict__ out_p, const OtherRes* __restrict__ tab_p,
                     int64_t no_p, int32_t* __restrict__ err) {
   extern __shared__ float tiles[];
   __shared__ OtherTable T;  // unused: both levels come with global tables
   const int warp = threadIdx.x >> 5;
-  if (blockIdx.x < nblk_f) {
+  const int64_t nsc = nblk_f * n_score_segs(sp);  // scoring blocks, segment-major
+  if (blockIdx.x < nsc) {
     float* tile = tiles + (size_t)warp * 32 * score_stride(64, sp.wmax);
+    const int64_t seg = blockIdx.x / nblk_f;
     score64_warp(F, KF, in_f, sp, SK, snr, err, T, false, tab_f, no_f,
-                 (int64_t)blockIdx.x * blockDim.x + warp * 32, tile);
+                 (blockIdx.x - seg * nblk_f) * blockDim.x + warp * 32, tile, seg);
   } else {
     level64_warp(P, KP, in_p, out_p, err, T, false, tab_p, no_p,
-                 (int64_t)(blockIdx.x - nblk_f) * blockDim.x + warp * 32);
+                 (int64_t)(blockIdx.x - nsc) * blockDim.x + warp * 32);
   }
 }
 
+template <typename S>
 __global__ void __launch_bounds__(kScoreWarps * 32)
-ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
+ffa_level_score_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in,
                        LokiScoreSpec sp, ScoreK SK, float* __restrict__ snr,
                        int32_t* __restrict__ err, const OtherRes* __restrict__ gtab,
                        int64_t n_other) {
@@ -410,7 +482,9 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
   const int stride = score_stride(nb, sp.wmax);
   float* tile = tiles + (size_t)warp * 32 * stride;
   const int64_t Q = n_out_params(L), P_in = n_in_params(L);
-  const int64_t qb = (int64_t)blockIdx.x * blockDim.x;
+  const int64_t nblk = (Q + blockDim.x - 1) / blockDim.x;  // blocks per segment
+  const int64_t seg = blockIdx.x / nblk;
+  const int64_t qb = (blockIdx.x - seg * nblk) * blockDim.x;
   bool tab = false;
   if (!gtab) {  // uniform: the whole block takes the same branch
     tab = build_table(T, L, K, qb, std::min<int64_t>(qb + blockDim.x, Q) - 1);
@@ -421,8 +495,8 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
   const LaneTrial me = lane_trial(L, K, T, tab, gtab, n_other, q0 + lane, Q, err);
   const int kmax = (int)std::min<int64_t>(32, Q - q0);
   const size_t row = (size_t)2 * nb;
-  const float* in_t = in;
-  const float* in_h = in + (size_t)P_in * row;
+  const S* in_t = in + (size_t)(2 * seg) * P_in * row;
+  const S* in_h = in_t + (size_t)P_in * row;
   for (int k = 0; k < kmax; ++k) {
     const int64_t it = __shfl_sync(0xFFFFFFFFu, me.t, k);
     const int64_t ih = __shfl_sync(0xFFFFFFFFu, me.h, k);
@@ -434,19 +508,19 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const float* __restrict__ in,
       for (int j = lane; j < nb; j += 32) trow[j] = 0.0f;
       continue;
     }
-    const float* t = in_t + (size_t)it * row;
-    const float* h = in_h + (size_t)ih * row;
+    const S* t = in_t + (size_t)it * row;
+    const S* h = in_h + (size_t)ih * row;
     for (int j = lane; j < nb; j += 32) {
       int jt = j - st;
       jt += (jt < 0) ? nb : 0;
       int jh = j - sh;
       jh += (jh < 0) ? nb : 0;
-      const float e = __fadd_rn(t[jt], h[jh]);
-      const float v = __fadd_rn(t[nb + jt], h[nb + jh]);
+      const float e = __fadd_rn(Store<S>::load(t + jt), Store<S>::load(h + jh));
+      const float v = __fadd_rn(Store<S>::load(t + nb + jt), Store<S>::load(h + nb + jh));
       trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
     }
   }
-  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr);
+  score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr, seg);
 }
 
 // Previous-level frequency window needed by each band of current-level
@@ -532,6 +606,15 @@ static int check_spec(const LokiScoreSpec* sp, int nbins) {
   if (wmax != sp->wmax) return set_error(LOKI_ERR_INVALID, "wmax != max(widths)");
   if (nbins + wmax > 2048)
     return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax = %d above 2048", nbins + wmax);
+  if (sp->nseg < 0) return set_error(LOKI_ERR_INVALID, "spec nseg < 0");
+  return LOKI_OK;
+}
+
+// The fused final level scores segments [0, nseg) of its output.
+static int check_score_segs(const LokiFFALevel* L, const LokiScoreSpec* sp) {
+  if (n_score_segs(*sp) > L->nseg_in / 2)
+    return set_error(LOKI_ERR_INVALID, "spec nseg %d above the %lld output segments",
+                     sp->nseg, (long long)(L->nseg_in / 2));
   return LOKI_OK;
 }
 
@@ -548,40 +631,63 @@ int score_warps_per_block(int nbins, int wmax) {
 // Aligned float4 rows are required by the nbins == 64 kernels.
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-static int launch_level(const LokiFFALevel& L, const LevelK& K, const float* in, float* out,
-                        int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
-                        int64_t n_other = 0) {
+template <typename S>
+static int launch_level_t(const LokiFFALevel& L, const LevelK& K, const S* in, S* out,
+                          int32_t* err, cudaStream_t s, const OtherRes* gtab, int64_t n_other) {
   const int64_t Q = n_out_params(L);
   const int64_t blocks = (Q + kLevelWarps * 32 - 1) / (kLevelWarps * 32);
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
   note_launch();
   if (L.nbins == 64 && aligned16(in) && aligned16(out))
-    ffa_level64_kernel<<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
-                                                                     n_other);
+    ffa_level64_kernel<S><<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err,
+                                                                        gtab, n_other);
   else
-    ffa_level_kernel<<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
-                                                                   n_other);
+    ffa_level_kernel<S><<<(unsigned)blocks, kLevelWarps * 32, 0, s>>>(L, K, in, out, err, gtab,
+                                                                      n_other);
   return LOKI_OK;
 }
 
-static int launch_level_score(const LokiFFALevel& L, const LevelK& K, const float* in,
-                              const LokiScoreSpec& sp, const ScoreK& SK, float* snr,
-                              int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
-                              int64_t n_other = 0) {
+// Folds are float32 (storage 0) or bfloat16 (storage 1).
+static int launch_level(const LokiFFALevel& L, const LevelK& K, const void* in, void* out,
+                        int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
+                        int64_t n_other = 0) {
+  if (L.storage == 1)
+    return launch_level_t(L, K, static_cast<const __nv_bfloat16*>(in),
+                          static_cast<__nv_bfloat16*>(out), err, s, gtab, n_other);
+  return launch_level_t(L, K, static_cast<const float*>(in), static_cast<float*>(out), err, s,
+                        gtab, n_other);
+}
+
+template <typename S>
+static int launch_level_score_t(const LokiFFALevel& L, const LevelK& K, const S* in,
+                                const LokiScoreSpec& sp, const ScoreK& SK, float* snr,
+                                int32_t* err, cudaStream_t s, const OtherRes* gtab,
+                                int64_t n_other) {
   const bool fast = L.nbins == 64;
   const int warps = fast ? kScoreWarps : score_warps_per_block(L.nbins, sp.wmax);
   const int smem = score_smem_bytes(L.nbins, sp.wmax, warps);
-  auto kern = fast ? ffa_level_score64_kernel : ffa_level_score_kernel;
+  auto kern = fast ? ffa_level_score64_kernel<S> : ffa_level_score_kernel<S>;
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
           cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t Q = n_out_params(L);
-  const int64_t blocks = (Q + warps * 32 - 1) / (warps * 32);
+  const int64_t blocks = (Q + warps * 32 - 1) / (warps * 32) * n_score_segs(sp);
   if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
   note_launch();
   kern<<<(unsigned)blocks, warps * 32, smem, s>>>(L, K, in, sp, SK, snr, err, gtab, n_other);
   return LOKI_OK;
+}
+
+static int launch_level_score(const LokiFFALevel& L, const LevelK& K, const void* in,
+                              const LokiScoreSpec& sp, const ScoreK& SK, float* snr,
+                              int32_t* err, cudaStream_t s, const OtherRes* gtab = nullptr,
+                              int64_t n_other = 0) {
+  if (L.storage == 1)
+    return launch_level_score_t(L, K, static_cast<const __nv_bfloat16*>(in), sp, SK, snr, err,
+                                s, gtab, n_other);
+  return launch_level_score_t(L, K, static_cast<const float*>(in), sp, SK, snr, err, s, gtab,
+                              n_other);
 }
 
 // Per-level table of the exact per-(latter, other) resolve quantities,
@@ -621,7 +727,7 @@ extern "C" int loki_ffa_plan(const LokiFFALevel* lvl, LokiFFACoord* coords, int3
   return check_launch("ffa_plan");
 }
 
-extern "C" int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, float* fold_out,
+extern "C" int loki_ffa_level(const LokiFFALevel* lvl, const void* fold_in, void* fold_out,
                               int32_t* dev_err, void* stream) {
   int rc = check_level(lvl);
   if (rc) return rc;
@@ -633,12 +739,14 @@ extern "C" int loki_ffa_level(const LokiFFALevel* lvl, const float* fold_in, flo
   return check_launch("ffa_level");
 }
 
-extern "C" int loki_ffa_level_score(const LokiFFALevel* lvl, const float* fold_in,
+extern "C" int loki_ffa_level_score(const LokiFFALevel* lvl, const void* fold_in,
                                     const LokiScoreSpec* spec, float* snr, int32_t* dev_err,
                                     void* stream) {
   int rc = check_level(lvl);
   if (rc) return rc;
   rc = check_spec(spec, lvl->nbins);
+  if (rc) return rc;
+  rc = check_score_segs(lvl, spec);
   if (rc) return rc;
   if (!fold_in || !snr || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const LevelK K = make_level_k(*lvl);
@@ -674,7 +782,7 @@ extern "C" int loki_ffa_band_windows(const LokiFFALevel* lvl, int64_t band_width
 
 extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                      int64_t band_width, const int64_t* win_lo,
-                                     const int64_t* win_hi, const float* fold_pp, float* scratch,
+                                     const int64_t* win_hi, const void* fold_pp, float* scratch,
                                      int64_t scratch_floats, const LokiScoreSpec* spec,
                                      float* snr, int32_t* dev_err, void* stream) {
   int rc = check_level(pen);
@@ -683,11 +791,13 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
   if (rc) return rc;
   rc = check_spec(spec, fin->nbins);
   if (rc) return rc;
+  rc = check_score_segs(fin, spec);
+  if (rc) return rc;
   if (!win_lo || !win_hi || !fold_pp || !scratch || !snr || !dev_err)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   if (band_width < 1) return set_error(LOKI_ERR_INVALID, "band_width < 1");
   if (fin->level != pen->level + 1 || pen->nseg_in != 2 * fin->nseg_in ||
-      fin->nparams != pen->nparams)
+      fin->nparams != pen->nparams || fin->storage != pen->storage)
     return set_error(LOKI_ERR_INVALID, "pen/fin descriptors are not consecutive levels");
   cudaStream_t s = (cudaStream_t)stream;
   const int n = fin->nparams;
@@ -731,9 +841,13 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
     // Software pipeline over bands with two scratch buffers.
     float* buf[2] = {scratch, scratch + half};
     const int smem = score_smem_bytes(64, spec->wmax, kScoreWarps);
+    const bool bf16 = fin->storage == 1;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(band_union64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
+        (bf16 ? cudaFuncSetAttribute(band_union64_kernel<__nv_bfloat16>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+              : cudaFuncSetAttribute(band_union64_kernel<float>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+            cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     P.out_start = win_lo[0];
     P.out_width = win_hi[0] - win_lo[0] + 1;
@@ -754,11 +868,19 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
         set_out_width(KP, P);
         nblk_p = (n_out_params(P) + kScoreWarps * 32 - 1) / (kScoreWarps * 32);
       }
-      if (nblk_f + nblk_p > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+      if (nblk_f * n_score_segs(*spec) + nblk_p > 0x7FFFFFFF)
+        return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
       note_launch();
-      band_union64_kernel<<<(unsigned)(nblk_f + nblk_p), kScoreWarps * 32, smem, s>>>(
-          F, KF, buf[k & 1], *spec, SK, snr, tab_f, no_f, nblk_f, P, KP, fold_pp,
-          buf[(k + 1) & 1], tab_p, no_p, dev_err);
+      const unsigned grid = (unsigned)(nblk_f * n_score_segs(*spec) + nblk_p);
+      if (bf16)
+        band_union64_kernel<__nv_bfloat16><<<grid, kScoreWarps * 32, smem, s>>>(
+            F, KF, reinterpret_cast<const __nv_bfloat16*>(buf[k & 1]), *spec, SK, snr, tab_f,
+            no_f, nblk_f, P, KP, static_cast<const __nv_bfloat16*>(fold_pp),
+            reinterpret_cast<__nv_bfloat16*>(buf[(k + 1) & 1]), tab_p, no_p, dev_err);
+      else
+        band_union64_kernel<float><<<grid, kScoreWarps * 32, smem, s>>>(
+            F, KF, buf[k & 1], *spec, SK, snr, tab_f, no_f, nblk_f, P, KP,
+            static_cast<const float*>(fold_pp), buf[(k + 1) & 1], tab_p, no_p, dev_err);
     }
     return check_launch("ffa_final_banded");
   }
@@ -786,4 +908,23 @@ extern "C" int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const 
   // two band buffers (the banded pipeline double-buffers) plus the tables
   const int64_t band = fin->nseg_in * n_other_of(*pen) * max_window * 2 * (int64_t)fin->nbins;
   return 2 * (((band + 15) / 16) * 16) + table_floats(*pen) + table_floats(*fin);
+}
+
+namespace loki {
+__global__ void f32_to_bf16_kernel(const float* __restrict__ in, int64_t n,
+                                   __nv_bfloat16* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __float2bfloat16_rn(in[i]);
+}
+}  // namespace loki
+
+extern "C" int loki_f32_to_bf16(const float* in, int64_t n, void* out, void* stream) {
+  if (n < 0) return set_error(LOKI_ERR_INVALID, "n < 0");
+  if (n == 0) return LOKI_OK;
+  if (!in || !out) return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  f32_to_bf16_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 152 * 64), 256, 0,
+                       (cudaStream_t)stream>>>(in, n, static_cast<__nv_bfloat16*>(out));
+  return check_launch("f32_to_bf16");
 }

@@ -3,8 +3,10 @@
 ``DynamicProgramming`` keeps the reference's interface (``ffa.py:196-435``):
 ``initialize`` brute-folds the series (``loki_brutefold``), ``execute`` runs
 the DP levels (``loki_ffa_level``), and the grid properties are the
-reference's. Folds live in HBM as float32 torch tensors with pyloki's layout
-``(nsegments, *param_counts, 2, nbins)``.
+reference's. Folds live in HBM as torch tensors with pyloki's layout
+``(nsegments, *param_counts, 2, nbins)``; with ``storage="bf16"`` the DP
+levels store bfloat16 (FP32 arithmetic) and ``rescore`` recomputes the S/N of
+retained candidates from the samples with FP64 sums.
 
 ``search`` is the memory-bounded path used by ``ffa_search``: the last level
 is fused with normalisation and boxcar scoring (``loki_ffa_level_score``) and
@@ -78,8 +80,10 @@ def grid(cfg: PulsarSearchConfig, level: int, device) -> _Grid:
 
 def level_desc(cfg: PulsarSearchConfig, cur: _Grid, prev: _Grid, nseg_in: int,
                out_win: tuple[int, int] | None = None,
-               in_win: tuple[int, int] | None = None) -> _lib.LokiFFALevel:
-    """Build the C descriptor of one DP level (optionally frequency-windowed)."""
+               in_win: tuple[int, int] | None = None, *,
+               storage: int = 0) -> _lib.LokiFFALevel:
+    """Build the C descriptor of one DP level (optionally frequency-windowed).
+    ``storage`` 0 keeps the folds in float32, 1 in bfloat16 (FP32 arithmetic)."""
     n = cfg.nparams
     d = _lib.LokiFFALevel()
     d.nparams = n
@@ -98,7 +102,11 @@ def level_desc(cfg: PulsarSearchConfig, cur: _Grid, prev: _Grid, nseg_in: int,
     d.in_start, d.in_width = i0, iw
     d.nseg_in = nseg_in
     d.last_split = cur.split.data_ptr()
+    d.storage = storage
     return d
+
+
+STORAGES = {"f32": (0, torch.float32), "bf16": (1, torch.bfloat16)}
 
 
 class DynamicProgramming:
@@ -112,12 +120,46 @@ class DynamicProgramming:
         Search configuration (``use_fourier=False``: time-domain folds).
     device : torch.device or str, optional
         CUDA device, default the current one.
+    storage : {"f32", "bf16"}
+        Element type of the stored folds. ``"bf16"`` halves the HBM traffic of
+        every DP level; the shift-add and the scoring still compute in FP32
+        (each stored sum is rounded once to bfloat16); ``rescore`` gives the
+        FP64 S/N of retained candidates.
+    nbatch : int
+        Number of equal-length series concatenated in ``ts_data``
+        (``nbatch * cfg.nsamps`` samples). Their segments are stacked along
+        the segment axis, so every level (and the fused final scoring) runs
+        over all series in one launch; ``search`` then returns one S/N block
+        per series. Each series must end in one final segment
+        (``nsamps == bseg_brute * 2**niters_ffa``), so no segment pair spans
+        two series.
     """
 
-    def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None) -> None:
+    def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None,
+                 storage: str = "f32", nbatch: int = 1) -> None:
         if cfg.use_fourier and cfg.nbins % 2:
             msg = "the Fourier-domain FFA needs an even nbins (irfft length)"
             raise ValueError(msg)
+        if storage not in STORAGES:
+            msg = f"storage must be one of {sorted(STORAGES)}, got {storage!r}"
+            raise ValueError(msg)
+        if storage != "f32" and cfg.use_fourier:
+            msg = "reduced-precision storage is for time-domain folds only"
+            raise ValueError(msg)
+        self._storage, self._fold_dtype = STORAGES[storage]
+        self.storage = storage
+        if nbatch < 1:
+            msg = "nbatch must be >= 1"
+            raise ValueError(msg)
+        if nbatch > 1 and cfg.nsamps != cfg.bseg_brute * 2**cfg.niters_ffa:
+            msg = ("batched series need one final segment each: nsamps == bseg_brute * "
+                   f"2**niters_ffa ({cfg.nsamps} vs {cfg.bseg_brute} * 2**{cfg.niters_ffa})")
+            raise ValueError(msg)
+        if nbatch > 1 and cfg.use_fourier:
+            msg = "batched series are for time-domain folds"
+            raise ValueError(msg)
+        self.nbatch = nbatch
+        self._ts_dev: tuple[torch.Tensor, torch.Tensor] | None = None
         self._ts_data = ts_data
         self._cfg = cfg
         self._device = torch.device(device) if device is not None else torch.device(
@@ -161,7 +203,7 @@ class DynamicProgramming:
 
     @property
     def nsegments(self) -> int:
-        return self.cfg.nsamps // (self.cfg.bseg_brute * 2**self.ffa_level)
+        return self.nbatch * (self.cfg.nsamps // (self.cfg.bseg_brute * 2**self.ffa_level))
 
     @property
     def nbins(self) -> int:
@@ -228,6 +270,11 @@ class DynamicProgramming:
         dev = self._device
         ts_e = torch.as_tensor(self.ts_data.ts_e).to(dev, non_blocking=True)
         ts_v = torch.as_tensor(self.ts_data.ts_v).to(dev, non_blocking=True)
+        if ts_e.numel() != self.nbatch * cfg.nsamps or ts_v.numel() != ts_e.numel():
+            msg = (f"expected {self.nbatch} x {cfg.nsamps} samples in ts_e and ts_v, got "
+                   f"{ts_e.numel()} and {ts_v.numel()}")
+            raise ValueError(msg)
+        self._ts_dev = (ts_e, ts_v)
         t_ref = 0.0 if cfg.nparams == 1 else cfg.bseg_brute * cfg.tsamp / 2
         if cfg.use_fourier:  # core/fold.py:395-481,572-614
             nseg = ts_e.numel() // cfg.bseg_brute
@@ -248,6 +295,12 @@ class DynamicProgramming:
                                     scratch_bytes=self.phase_scratch_bytes)
         self.launches += nl
         nseg, nfreq = self._fold.shape[:2]
+        if self._storage:
+            low = torch.empty(self._fold.shape, dtype=self._fold_dtype, device=dev)
+            _lib.check(self._lib.loki_f32_to_bf16(_lib.ptr(self._fold), self._fold.numel(),
+                                                  _lib.ptr(low), self._stream()))
+            self.launches += 1
+            self._fold = low
         self._fold = self._fold.reshape(nseg, *([1] * (cfg.nparams - 1)), nfreq, 2,
                                         cfg.nbins)
         self._err.zero_()
@@ -279,9 +332,9 @@ class DynamicProgramming:
             self._fold = out.reshape(nseg_in // 2, *cur.counts.tolist(), 2, nbf)
             self._ffa_level += 1
             return
-        out = torch.empty((nseg_in // 2, cur.size, 2, self.nbins), dtype=torch.float32,
+        out = torch.empty((nseg_in // 2, cur.size, 2, self.nbins), dtype=self._fold_dtype,
                           device=self._device)
-        desc = level_desc(self.cfg, cur, prev, nseg_in)
+        desc = level_desc(self.cfg, cur, prev, nseg_in, storage=self._storage)
         _lib.check(self._lib.loki_ffa_level(desc, _lib.ptr(fold_in), _lib.ptr(out),
                                             _lib.ptr(self._err), self._stream()))
         self.launches += 1
@@ -296,6 +349,8 @@ class DynamicProgramming:
             fold = fold[idx]
         lead = fold.shape[:-2]
         flat = fold.reshape(-1, 2, fold.shape[-1]).contiguous()
+        if flat.dtype == torch.bfloat16:
+            flat = flat.float()
         out = torch.empty((flat.shape[0], self.nbins), dtype=torch.float32,
                           device=self._device)
         if self.cfg.use_fourier:  # irfft, then e / sqrt(v)
@@ -312,23 +367,66 @@ class DynamicProgramming:
         return [_cart_len(self.cfg.get_param_grid_count(lvl))
                 for lvl in range(self.cfg.niters_ffa + 1)]
 
+    def rescore(self, cand, widths=None, stdnoise: float = 1.0, *, seg: int = 0,
+                level: int | None = None,
+                return_profiles: bool = False) -> torch.Tensor | tuple[torch.Tensor, torch.Tensor]:
+        """FP64 S/N ``(ncand, nwidths)`` of candidates given as flat parameter
+        indices of ``level`` (default the final level), their folds rebuilt
+        from the samples with FP64 sums (``loki_ffa_rescore``). With
+        ``return_profiles`` also the FP64 folds ``(ncand, 2, nbins)``."""
+        if self._ts_dev is None:
+            msg = "rescore needs the series on the device: call initialize() or search() first"
+            raise RuntimeError(msg)
+        cfg = self.cfg
+        level = cfg.niters_ffa if level is None else int(level)
+        if not 1 <= level <= min(cfg.niters_ffa, _lib.MAX_RESCORE_LEVELS):
+            msg = f"level {level} outside 1..{min(cfg.niters_ffa, _lib.MAX_RESCORE_LEVELS)}"
+            raise ValueError(msg)
+        widths = cfg.score_widths if widths is None else np.asarray(widths, np.int64)
+        spec = _lib.score_spec(widths, cfg.nbins, stdnoise, mode=0)
+        cand = torch.as_tensor(cand, dtype=torch.int64).reshape(-1).to(self._device)
+        descs = (_lib.LokiFFALevel * level)()
+        for lvl in range(1, level + 1):
+            nseg_in = cfg.nsamps // (cfg.bseg_brute * 2 ** (lvl - 1))
+            descs[lvl - 1] = level_desc(cfg, self._grid(lvl), self._grid(lvl - 1), nseg_in)
+        snr = torch.empty((cand.numel(), len(widths)), dtype=torch.float64, device=self._device)
+        prof = (torch.empty((cand.numel(), 2, cfg.nbins), dtype=torch.float64,
+                            device=self._device) if return_profiles else None)
+        ts_e, ts_v = self._ts_dev
+        f0 = self._grid(0).dev[-1]
+        _lib.check(self._lib.loki_ffa_rescore(
+            descs, level, _lib.ptr(ts_e), _lib.ptr(ts_v), ts_e.numel(), cfg.tsamp,
+            cfg.bseg_brute, _lib.ptr(f0), f0.numel(), _lib.ptr(cand), cand.numel(), seg, spec,
+            _lib.ptr(snr), _lib.ptr(prof), self._stream()))
+        self.launches += 1
+        return (snr, prof) if return_profiles else snr
+
     # ---- fused, memory-bounded search ---------------------------------------
     def level_bytes(self, level: int) -> int:
-        nseg = self.cfg.nsamps // (self.cfg.bseg_brute * 2**level)
-        return nseg * _cart_len(self.cfg.get_param_grid_count(level)) * 2 * self.nbins * 4
+        nseg = self.nbatch * (self.cfg.nsamps // (self.cfg.bseg_brute * 2**level))
+        return (nseg * _cart_len(self.cfg.get_param_grid_count(level)) * 2 * self.nbins
+                * self._elem_bytes)
+
+    @property
+    def _elem_bytes(self) -> int:
+        return 2 if self._storage else 4
 
     def search(self, widths=None, stdnoise: float = 1.0, *, mode: int = 0,
                banded: bool | None = None, band_bytes: int = 96 << 20,
-               phase_events: list | None = None) -> torch.Tensor:
-        """S/N of every final-level parameter set (segment 0), never writing the
-        final fold. Returns ``(*counts_final, nwidths)`` (or ``counts_final``
-        for ``mode=1``, the max over widths). ``phase_events``, if given,
-        receives ``(name, cuda.Event)`` marks recorded on the launch stream
-        after the brute fold, the materialised levels and the final levels."""
+               phase_events: list | None = None, check: bool = True) -> torch.Tensor:
+        """S/N of every final-level parameter set (segment 0 of each series),
+        never writing the final fold. Returns ``(*counts_final, nwidths)`` (or
+        ``counts_final`` for ``mode=1``, the max over widths), with a leading
+        series axis when ``nbatch > 1``. ``phase_events``, if given, receives
+        ``(name, cuda.Event)`` marks recorded on the launch stream after the
+        brute fold, the materialised levels and the final levels. ``check=False``
+        leaves the device error word unread (no host synchronisation, as CUDA
+        graph capture requires); read it later with ``check_errors``."""
         cfg = self.cfg
         n = cfg.niters_ffa
         widths = cfg.score_widths if widths is None else np.asarray(widths, np.int64)
         spec = _lib.score_spec(widths, cfg.nbins, stdnoise, mode=mode)
+        spec.nseg = self.nbatch
         nout = len(widths) if mode == 0 else 1
 
         def mark(name: str) -> None:
@@ -356,7 +454,8 @@ class DynamicProgramming:
                 snr = snr.amax(dim=-1)
             mark("final")
             return snr
-        snr = torch.empty((fin.size, nout), dtype=torch.float32, device=self._device)
+        snr = torch.empty((self.nbatch, fin.size, nout), dtype=torch.float32,
+                          device=self._device)
         if banded is None:
             banded = n >= 2 and self.level_bytes(n - 1) > 8 * band_bytes
         if banded and n < 2:
@@ -367,7 +466,7 @@ class DynamicProgramming:
         mark("levels")
         if not banded:
             prev = self._grid(n - 1)
-            desc = level_desc(cfg, fin, prev, self.nsegments)
+            desc = level_desc(cfg, fin, prev, self.nsegments, storage=self._storage)
             _lib.check(self._lib.loki_ffa_level_score(
                 desc, _lib.ptr(self.fold), spec, _lib.ptr(snr), _lib.ptr(self._err),
                 self._stream()))
@@ -377,9 +476,23 @@ class DynamicProgramming:
         mark("final")
         self._fold = None
         self._ffa_level = n
-        _lib.check_dev_err(self._err)
+        if check:
+            _lib.check_dev_err(self._err)
         shape = (*fin.counts.tolist(), nout) if mode == 0 else tuple(fin.counts.tolist())
+        if self.nbatch > 1:
+            shape = (self.nbatch, *shape)
         return snr.reshape(shape)
+
+    def check_errors(self) -> None:
+        """Raise if a kernel of this object flagged a device error (reads the
+        error word: one host synchronisation)."""
+        _lib.check_dev_err(self._err)
+
+    def reset(self) -> None:
+        """Return to the state before ``initialize`` (grids and device series
+        stay), so that ``search`` can run again on the same buffers."""
+        self._fold = None
+        self._ffa_level = -1
 
     def band_plan(self, band_bytes: int) -> tuple[int, np.ndarray, np.ndarray]:
         """Frequency bands for the last two levels: (final band width, lo, hi)
@@ -387,14 +500,14 @@ class DynamicProgramming:
         cfg = self.cfg
         n = cfg.niters_ffa
         fin, pen = self._grid(n), self._grid(n - 1)
-        nseg_pen = cfg.nsamps // (cfg.bseg_brute * 2 ** (n - 1))
+        nseg_pen = self.nbatch * (cfg.nsamps // (cfg.bseg_brute * 2 ** (n - 1)))
         other_pen = _cart_len(pen.counts[:-1])
-        row = nseg_pen * other_pen * 2 * cfg.nbins * 4
+        row = nseg_pen * other_pen * 2 * cfg.nbins * self._elem_bytes
         w_pen = max(64, band_bytes // row)
         width = max(32, int(2 * w_pen * 0.75))
         width = min(width, int(fin.counts[-1]))
         desc = level_desc(cfg, fin, pen, nseg_pen)
-        key = (_cfg_key(cfg), band_bytes, str(self._device))
+        key = (_cfg_key(cfg), band_bytes, self._storage, self.nbatch, str(self._device))
         if key in _BAND_CACHE:
             return _BAND_CACHE[key]
         for _ in range(8):
@@ -419,8 +532,8 @@ class DynamicProgramming:
         nseg_pen = nseg_pp // 2
         width, lo, hi = self.band_plan(band_bytes)
         wmax = int((hi - lo + 1).max())
-        d_pen = level_desc(cfg, pen, pp, nseg_pp)
-        d_fin = level_desc(cfg, fin, pen, nseg_pen)
+        d_pen = level_desc(cfg, pen, pp, nseg_pp, storage=self._storage)
+        d_fin = level_desc(cfg, fin, pen, nseg_pen, storage=self._storage)
         nfl = int(self._lib.loki_ffa_final_banded_scratch(d_pen, d_fin, wmax))
         if nfl <= 0:
             msg = "invalid banded level descriptors"
