@@ -44,6 +44,9 @@ WORKLOAD = "ffa_accel_search_2^23"
 UNION_DRAM_BYTES_PER_TRIAL = 259.0
 BF16_TOP = 64        # candidates re-scored in FP64 and checked against the FP64 oracle
 BF16_SAMPLE = 192    # random trials added to the FP64 error sample
+BATCH_WORKLOAD = "ffa_jerk_batch_2^20-2^23"
+BATCH_SERIES = 32    # bounded sample of the 256-series batch (first series of the draw)
+BATCH_K = 16         # candidates kept per series
 
 
 def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0):
@@ -482,6 +485,8 @@ def bench_gpu(args) -> dict | None:
     if not args.no_bf16:
         out["ffa_bf16"] = bench_bf16(args, dev, cfg, ts_dev, ts_host, one_step, trials,
                                      ms_per_step)
+    if not args.no_batch:
+        out["batch"] = bench_batch(args, dev)
     if not args.no_prune:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
@@ -489,6 +494,105 @@ def bench_gpu(args) -> dict | None:
     if dist is not None:
         dist.destroy_process_group()
     return out
+
+
+def batch_cfg(n: int):
+    """Jerk search of one batch series of n = 2^k samples: f 50-500 Hz,
+    accel +-30 m/s^2, jerk +-0.05 m/s^3, 64 bins, widths 1-16."""
+    from pyloki_gb300 import ParamLimits, PulsarSearchConfig
+
+    return PulsarSearchConfig(
+        nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
+        param_limits=ParamLimits.from_taylor((50.0, 500.0), accel=(-30.0, 30.0),
+                                             jerk=(-0.05, 0.05)).limits,
+        ducy_max=0.25, wtsp=2.0, use_fourier=False, bseg_brute=16384)
+
+
+def make_batch_series(n_series: int, seed: int = 3000):
+    """Seeded batch: lengths uniform in [2^20, 2^23]; one series in ten carries
+    a pulsar (P 2-20 ms, accel +-30, jerk +-0.05, S/N 8-20)."""
+    from pyloki_gb300.batch import cfg3_lengths
+    from pyloki_gb300.simulation import make_series as ms
+
+    lengths = cfg3_lengths(256, seed)[:n_series]
+    rng = np.random.default_rng(seed + 1)
+    out, injected = [], []
+    for i, n in enumerate(lengths):
+        if rng.random() < 0.1:
+            p = rng.uniform(2e-3, 20e-3)
+            out.append(ms(int(n), 64e-6, freq=1.0 / p, snr=rng.uniform(8.0, 20.0), ducy=0.05,
+                          accel=rng.uniform(-30.0, 30.0), jerk=rng.uniform(-0.05, 0.05),
+                          seed=seed + 10 + i))
+            injected.append(i)
+        else:
+            out.append(ms(int(n), 64e-6, seed=seed + 10 + i))
+    return out, injected
+
+
+def bench_batch(args, dev) -> dict:
+    """Batched pattern on a bounded sample of the 256-series batch: the plain
+    path (one FP32 search per series, eager launches) against the batched
+    path (segment-stacked chunks, CUDA-graph replay, tuned chunk and band
+    sizes) with FP32 storage, and with bfloat16 storage plus FP64 re-scoring
+    of the kept candidates; recall is the batched-bf16 recovery of the plain
+    path's best S/N per series (FP64 S/N within 1e-3)."""
+    import torch
+
+    from pyloki_gb300.batch import BatchedSearch, Tuner, sequential_search
+
+    from pyloki_gb300.timeseries import TimeSeries
+
+    host, injected = make_batch_series(args.batch_series)
+    # pinned host buffers: the copies are part of every pass
+    series = [TimeSeries(torch.from_numpy(ts.ts_e).pin_memory(),
+                         torch.from_numpy(ts.ts_v).pin_memory(), ts.tsamp) for ts in host]
+
+    def timed(fn) -> tuple[float, object]:
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) * 1e3, out
+
+    ms_plain, plain = timed(lambda: sequential_search(series, batch_cfg, device=dev, k=BATCH_K))
+    ms_plain, plain = timed(lambda: sequential_search(series, batch_cfg, device=dev, k=BATCH_K))
+    tuner = Tuner()
+    res = {}
+    for name, storage, rescore in (("batched_f32", "f32", False),
+                                   ("batched_bf16_rescored", "bf16", True)):
+        bs = BatchedSearch(series, batch_cfg, device=dev, k=BATCH_K, storage=storage,
+                           rescore=rescore, tuner=tuner)
+        t0 = time.perf_counter()
+        bs.prepare()
+        prep_s = time.perf_counter() - t0
+        bs.run()  # warm replay
+        ms_b, cands = timed(bs.run)
+        res[name] = {"ms": ms_b, "trials_per_s": bs.trials() / (ms_b * 1e-3),
+                     "speedup_vs_plain": ms_plain / ms_b, "prepare_s": prep_s,
+                     "graph_launches": bs.graph_launches, "kernel_launches": bs.launches,
+                     "plan": {str(n): {"chunk": p.chunk, "band_bytes": p.band_bytes}
+                              for n, p in bs.plan.items()},
+                     "_cands": cands}
+    trials = bs.trials()
+    bf = res["batched_bf16_rescored"].pop("_cands")
+    f32 = res["batched_f32"].pop("_cands")
+    same_f32 = all(np.array_equal(a.snr_search, b.snr_search) for a, b in zip(f32, plain))
+    rec = [bool(b.snr[0] >= p.snr[0] - 1e-3) for b, p in zip(bf, plain)]
+    rec_inj = [rec[i] for i in injected]
+    lengths = {}
+    for ts in series:
+        n = 1 << (len(ts.ts_e).bit_length() - 1)
+        lengths[str(n)] = lengths.get(str(n), 0) + 1
+    return {"metric": "period-trials/s (batch)", "workload": BATCH_WORKLOAD,
+            "series": len(series), "series_per_length": lengths, "trials_per_pass": trials,
+            "k": BATCH_K, "plain_ms": ms_plain,
+            "plain_trials_per_s": trials / (ms_plain * 1e-3), **res,
+            "batched_f32_equals_plain_topk": same_f32,
+            "recall_vs_plain": float(np.mean(rec)),
+            "recall_vs_plain_injected": float(np.mean(rec_inj)) if rec_inj else None,
+            "injected_series": len(injected),
+            "note": "pinned host series, H2D copies inside every pass; lengths truncated "
+                    "to powers of two; bf16 candidates re-scored in FP64 from the samples"}
 
 
 def bench_bf16(args, dev, cfg, ts_dev, ts_host, one_step, trials, f32_ms) -> dict:
@@ -645,6 +749,10 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bf16", action="store_true",
                     help="skip the bfloat16-storage search and its FP64 error check")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the batched multi-series measurement")
+    ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
+                    help="series of the seeded 256-series batch to search")
     ap.add_argument("--no-prune", action="store_true",
                     help="skip the enumerate-prune (leaves/s) measurement")
     ap.add_argument("--profile-once", action="store_true",

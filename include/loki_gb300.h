@@ -187,21 +187,24 @@ int loki_f32_to_bf16(const float* in, int64_t n, void* out, void* stream);
  * (full grids, l = 1 .. nlevels, the last being the candidates' level); the
  * series (ts_e, ts_v, device float32, nsamps samples) and the level-0
  * frequency grid freqs0 (device, nfreq0 values) are those of the search;
- * cand holds ncand flat parameter indices of the last level (device). Each
- * candidate's fold of segment seg is rebuilt from the samples: the resolve
+ * cand holds ncand flat parameter indices of the last level (device) and
+ * segs, if not NULL, each candidate's segment of that level (device; NULL:
+ * every candidate in segment seg). Each candidate's fold is rebuilt from the
+ * samples: the resolve
  * tree (dynamic/dyn_pffa.py:462-489) gives every level-0 segment's frequency
  * and accumulated shift, its samples are binned as in the brute fold
  * (core/fold.py:108-171) and everything is summed in float64. snr receives
  * (ncand, nwidths) boxcar S/N (detection/scoring.py:99-140) in float64 and
  * prof, if not NULL, the float64 profiles (ncand, 2, nbins). A candidate
- * index outside the last level's grid yields NaN rows.
+ * index outside the last level's grid, or a segment without all its level-0
+ * segments, yields NaN rows.
  * No reference counterpart: it backs bfloat16 fold storage, whose retained
  * candidates are re-scored here. */
 int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, const float* ts_e,
                      const float* ts_v, int64_t nsamps, double tsamp, int64_t bseg_brute,
-                     const double* freqs0, int64_t nfreq0, const int64_t* cand, int64_t ncand,
-                     int64_t seg, const LokiScoreSpec* spec, double* snr, double* prof,
-                     void* stream);
+                     const double* freqs0, int64_t nfreq0, const int64_t* cand,
+                     const int64_t* segs, int64_t ncand, int64_t seg,
+                     const LokiScoreSpec* spec, double* snr, double* prof, void* stream);
 
 /* ---- FFA (Fourier domain, complex64 = 2 x float32 per coefficient) ----
  * Folds are (nseg, nparams..., 2, nbins / 2 + 1) complex64, nbins even.

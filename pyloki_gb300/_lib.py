@@ -153,7 +153,7 @@ SIGNATURES: dict[str, tuple] = {
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_f32_to_bf16": (C.c_int, [_P, _I64, _P, _P]),
     "loki_ffa_rescore": (C.c_int, [C.POINTER(LokiFFALevel), _I32, _P, _P, _I64, _D, _I64, _P,
-                                   _I64, _P, _I64, _I64, C.POINTER(LokiScoreSpec), _P, _P,
+                                   _I64, _P, _P, _I64, _I64, C.POINTER(LokiScoreSpec), _P, _P,
                                    _P]),
     "loki_brutefold_complex": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
     "loki_ffa_level_complex": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),

@@ -333,8 +333,12 @@ class BatchedSearch:
                 if g.graph is not None:
                     self.graph_launches += 1
                 # FP64 re-scoring reads the chunk's series: before the next load
-                snr64 = ([g.dyp.rescore(idx[j], seg=j).amax(dim=1) for j in range(len(part))]
-                         if self.rescore else None)
+                snr64 = None
+                if self.rescore:  # every kept candidate of the chunk in one launch
+                    segs = torch.arange(len(part), device=self.device).repeat_interleave(
+                        idx.shape[1])
+                    snr64 = g.dyp.rescore(idx.reshape(-1), seg=segs).amax(dim=1).reshape(
+                        idx.shape)
                 pending.append((n, part, vals.clone(), idx.clone(), snr64, g))
         for n, part, vals, idx, snr64, g in pending:
             cfg = self._cfgs[n]

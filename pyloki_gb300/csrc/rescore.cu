@@ -40,7 +40,8 @@ struct SeriesArgs {
 
 __global__ void __launch_bounds__(kRescoreThreads)
 rescore_kernel(const LevelChain C, int nlev, const SeriesArgs A,
-               const int64_t* __restrict__ cand, int64_t ncand, int64_t Qtop, int64_t seg,
+               const int64_t* __restrict__ cand, const int64_t* __restrict__ segs,
+               int64_t ncand, int64_t Qtop, int64_t seg_default, int64_t nseg_top,
                LokiScoreSpec sp, double* __restrict__ snr, double* __restrict__ prof) {
   extern __shared__ double sm[];
   const int n = C.L[0].nparams;
@@ -55,7 +56,8 @@ rescore_kernel(const LevelChain C, int nlev, const SeriesArgs A,
   const LokiFFALevel& top = C.L[nlev - 1];
   for (int64_t c = blockIdx.x; c < ncand; c += gridDim.x) {
     const int64_t q = cand[c];
-    if (q < 0 || q >= Qtop) {  // not a parameter set of the last level: NaN, no access
+    const int64_t seg = segs ? segs[c] : seg_default;
+    if (q < 0 || q >= Qtop || seg < 0 || seg >= nseg_top) {  // not a trial: NaN, no access
       for (int iw = threadIdx.x; iw < sp.nwidths; iw += blockDim.x)
         snr[(size_t)c * sp.nwidths + iw] = NAN;
       if (prof)
@@ -143,9 +145,9 @@ using namespace loki;
 extern "C" int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, const float* ts_e,
                                 const float* ts_v, int64_t nsamps, double tsamp,
                                 int64_t bseg_brute, const double* freqs0, int64_t nfreq0,
-                                const int64_t* cand, int64_t ncand, int64_t seg,
-                                const LokiScoreSpec* spec, double* snr, double* prof,
-                                void* stream) {
+                                const int64_t* cand, const int64_t* segs, int64_t ncand,
+                                int64_t seg, const LokiScoreSpec* spec, double* snr,
+                                double* prof, void* stream) {
   if (!levels || !ts_e || !ts_v || !freqs0 || !cand || !spec || !snr)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   if (nlevels < 1 || nlevels > LOKI_MAX_RESCORE_LEVELS)
@@ -178,8 +180,10 @@ extern "C" int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, con
   for (int i = 0; i < spec->nwidths; ++i)
     if (spec->widths[i] < 1 || spec->widths[i] > spec->wmax)
       return set_error(LOKI_ERR_INVALID, "score width outside 1..wmax");
+  // segments of the last level whose level-0 segments all exist
   const int64_t nseg0 = (nsamps + bseg_brute - 1) / bseg_brute;
-  if ((seg + 1) << nlevels > nseg0)
+  const int64_t nseg_top = nseg0 >> nlevels;
+  if (!segs && seg >= nseg_top)
     return set_error(LOKI_ERR_INVALID, "segment %lld needs level-0 segments beyond %lld",
                      (long long)seg, (long long)nseg0);
   if (ncand == 0) return LOKI_OK;
@@ -203,6 +207,6 @@ extern "C" int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, con
   const unsigned grid = (unsigned)std::min<int64_t>(ncand, 152 * 8);
   note_launch();
   rescore_kernel<<<grid, kRescoreThreads, smem, (cudaStream_t)stream>>>(
-      C, nlevels, A, cand, ncand, Qtop, seg, *spec, snr, prof);
+      C, nlevels, A, cand, segs, ncand, Qtop, seg, nseg_top, *spec, snr, prof);
   return check_launch("ffa_rescore");
 }

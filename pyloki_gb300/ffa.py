@@ -367,12 +367,14 @@ class DynamicProgramming:
         return [_cart_len(self.cfg.get_param_grid_count(lvl))
                 for lvl in range(self.cfg.niters_ffa + 1)]
 
-    def rescore(self, cand, widths=None, stdnoise: float = 1.0, *, seg: int = 0,
+    def rescore(self, cand, widths=None, stdnoise: float = 1.0, *, seg=0,
                 level: int | None = None,
                 return_profiles: bool = False) -> torch.Tensor | tuple[torch.Tensor, torch.Tensor]:
         """FP64 S/N ``(ncand, nwidths)`` of candidates given as flat parameter
         indices of ``level`` (default the final level), their folds rebuilt
-        from the samples with FP64 sums (``loki_ffa_rescore``). With
+        from the samples with FP64 sums (``loki_ffa_rescore``). ``seg`` is one
+        segment of that level for every candidate, or one per candidate (with
+        ``nbatch`` series and the final level, segment i is series i). With
         ``return_profiles`` also the FP64 folds ``(ncand, 2, nbins)``."""
         if self._ts_dev is None:
             msg = "rescore needs the series on the device: call initialize() or search() first"
@@ -385,6 +387,13 @@ class DynamicProgramming:
         widths = cfg.score_widths if widths is None else np.asarray(widths, np.int64)
         spec = _lib.score_spec(widths, cfg.nbins, stdnoise, mode=0)
         cand = torch.as_tensor(cand, dtype=torch.int64).reshape(-1).to(self._device)
+        segs = None
+        if not np.isscalar(seg):
+            segs = torch.as_tensor(seg, dtype=torch.int64).reshape(-1).to(self._device)
+            if segs.numel() != cand.numel():
+                msg = "seg must be one segment or one per candidate"
+                raise ValueError(msg)
+            seg = 0
         descs = (_lib.LokiFFALevel * level)()
         for lvl in range(1, level + 1):
             nseg_in = cfg.nsamps // (cfg.bseg_brute * 2 ** (lvl - 1))
@@ -396,8 +405,8 @@ class DynamicProgramming:
         f0 = self._grid(0).dev[-1]
         _lib.check(self._lib.loki_ffa_rescore(
             descs, level, _lib.ptr(ts_e), _lib.ptr(ts_v), ts_e.numel(), cfg.tsamp,
-            cfg.bseg_brute, _lib.ptr(f0), f0.numel(), _lib.ptr(cand), cand.numel(), seg, spec,
-            _lib.ptr(snr), _lib.ptr(prof), self._stream()))
+            cfg.bseg_brute, _lib.ptr(f0), f0.numel(), _lib.ptr(cand), _lib.ptr(segs),
+            cand.numel(), int(seg), spec, _lib.ptr(snr), _lib.ptr(prof), self._stream()))
         self.launches += 1
         return (snr, prof) if return_profiles else snr
 

@@ -113,6 +113,13 @@ def test_rescore_matches_fp64_oracle(cuda_device, name, storage):
     ref1 = O.boxcar_snr_f64(O.ffa_trials(d["ts_e"], d["ts_v"], cfg, c1, level=lvl, seg=1,
                                          f64=True), cfg.score_widths)
     np.testing.assert_allclose(got1, ref1, rtol=RESCORE_REL_TOL, atol=1e-9)
+    # one segment per candidate
+    segs = np.arange(len(c1)) % 2
+    got2 = dyp.rescore(c1, level=lvl, seg=segs).cpu().numpy()
+    np.testing.assert_allclose(got2[segs == 1], ref1[segs == 1], rtol=RESCORE_REL_TOL, atol=1e-9)
+    ref0 = O.boxcar_snr_f64(O.ffa_trials(d["ts_e"], d["ts_v"], cfg, c1[segs == 0], level=lvl,
+                                         seg=0, f64=True), cfg.score_widths)
+    np.testing.assert_allclose(got2[segs == 0], ref0, rtol=RESCORE_REL_TOL, atol=1e-9)
 
 
 def test_rescore_rejects_out_of_range_candidates(cuda_device):
@@ -127,6 +134,9 @@ def test_rescore_rejects_out_of_range_candidates(cuda_device):
     nq = int(np.prod(cfg.get_param_grid_count(cfg.niters_ffa)))
     snr = dyp.rescore([-1, nq, 0]).cpu().numpy()
     assert np.isnan(snr[:2]).all() and np.isfinite(snr[2]).all()
+    # a segment without all its level-0 segments is a NaN row, not an access
+    snr = dyp.rescore([0, 0, 0], seg=[0, 1, -1]).cpu().numpy()
+    assert np.isfinite(snr[0]).all() and np.isnan(snr[1:]).all()
     with pytest.raises(RuntimeError):  # no series on the device yet
         DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg,
                            device=cuda_device).rescore([0])
