@@ -34,6 +34,7 @@ extern "C" {
 #define LOKI_DEVERR_NONE 0
 #define LOKI_DEVERR_WINDOW 1   /* resolved index outside the input window */
 #define LOKI_DEVERR_BRANCH 2   /* branch count above branch_max */
+#define LOKI_DEVERR_TIMEOUT 4  /* a bounded wait on the tensor cores gave up */
 
 #define LOKI_MAX_PARAMS 5
 #define LOKI_MAX_WIDTHS 64
@@ -444,6 +445,54 @@ int loki_snr_score_batch(const float* folds, int64_t n, int32_t nbins,
  * (n, 2, nbins) folds. Replaces get_fold_norm (ffa.py:382-411, real case). */
 int loki_fold_norm(const float* folds, int64_t n, int32_t nbins, float* out,
                    void* stream);
+
+/* ---- learned branch proposal (tensor cores) ----------------------------
+ * A 16 -> 128 -> 128 -> 1 MLP (ReLU) scoring per-branch statistics of the
+ * pruning tree. No reference counterpart: the reference has no learned
+ * part; these entry points back the optional branch-survival model. */
+#define LOKI_MLP_FEATURES 16
+#define LOKI_MLP_HIDDEN 128
+
+/* Device pointers. Weights bfloat16 in (out, in) layout: w1 (128, 16),
+ * w2 (128, 128), w3 (128,); biases float32: b1 (128,), b2 (128,), b3 (1,). */
+typedef struct {
+  const void* w1;
+  const float* b1;
+  const void* w2;
+  const float* b2;
+  const void* w3;
+  const float* b3;
+} LokiMLP;
+
+/* Device float32 gradient sums with the shapes of LokiMLP, plus the loss sum.
+ * loki_mlp_backward adds to them (the caller zeroes them per step). */
+typedef struct {
+  float* w1;
+  float* b1;
+  float* w2;
+  float* b2;
+  float* w3;
+  float* b3;
+  float* loss;
+} LokiMLPGrad;
+
+/* Shared memory one MLP block uses (bytes). */
+int64_t loki_mlp_smem_bytes(void);
+
+/* logits[i] for features x (n, 16) float32 (rounded to bfloat16 on load). */
+int loki_mlp_forward(const LokiMLP* w, const float* x, int64_t n, float* logits,
+                     int32_t* dev_err, void* stream);
+
+/* Forward plus backward of the weighted binary cross-entropy with logits,
+ * scale * sum_i wt[i] * (softplus(z_i) - y_i z_i) (wt NULL: all ones): adds the
+ * loss and the parameter gradients to grad; logits, if not NULL, receives z. */
+int loki_mlp_backward(const LokiMLP* w, const float* x, const float* y, const float* wt,
+                      int64_t n, float scale, const LokiMLPGrad* grad, float* logits,
+                      int32_t* dev_err, void* stream);
+
+/* One Adam step over n float32 parameters (bias-corrected, step >= 1). */
+int loki_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
+                  float beta1, float beta2, float eps, int64_t step, void* stream);
 
 #ifdef __cplusplus
 }

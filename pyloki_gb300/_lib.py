@@ -20,6 +20,7 @@ LOKI_ERR_CAPACITY = -4
 
 LOKI_DEVERR_WINDOW = 1
 LOKI_DEVERR_BRANCH = 2
+LOKI_DEVERR_TIMEOUT = 4
 
 MAX_PARAMS = 5
 MAX_WIDTHS = 64
@@ -131,6 +132,17 @@ _D = C.c_double
 _PL = C.POINTER(LokiPruneLevel)
 
 #: name -> (restype, argtypes); the exported C ABI.
+class LokiMLP(C.Structure):
+    _fields_ = [("w1", C.c_void_p), ("b1", C.c_void_p), ("w2", C.c_void_p),
+                ("b2", C.c_void_p), ("w3", C.c_void_p), ("b3", C.c_void_p)]
+
+
+class LokiMLPGrad(C.Structure):
+    _fields_ = [("w1", C.c_void_p), ("b1", C.c_void_p), ("w2", C.c_void_p),
+                ("b2", C.c_void_p), ("w3", C.c_void_p), ("b3", C.c_void_p),
+                ("loss", C.c_void_p)]
+
+
 SIGNATURES: dict[str, tuple] = {
     "loki_version": (C.c_int, []),
     "loki_last_error": (C.c_char_p, []),
@@ -152,6 +164,12 @@ SIGNATURES: dict[str, tuple] = {
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_f32_to_bf16": (C.c_int, [_P, _I64, _P, _P]),
+    "loki_mlp_smem_bytes": (C.c_int64, []),
+    "loki_mlp_forward": (C.c_int, [C.POINTER(LokiMLP), _P, _I64, _P, _P, _P]),
+    "loki_mlp_backward": (C.c_int, [C.POINTER(LokiMLP), _P, _P, _P, _I64, C.c_float,
+                                    C.POINTER(LokiMLPGrad), _P, _P, _P]),
+    "loki_mlp_adam": (C.c_int, [_P, _P, _P, _P, _I64, C.c_float, C.c_float, C.c_float,
+                                C.c_float, _I64, _P]),
     "loki_ffa_rescore": (C.c_int, [C.POINTER(LokiFFALevel), _I32, _P, _P, _I64, _D, _I64, _P,
                                    _I64, _P, _P, _I64, _I64, C.POINTER(LokiScoreSpec), _P, _P,
                                    _P]),
@@ -241,6 +259,9 @@ def check_dev_err(err_word) -> None:
     if v & LOKI_DEVERR_BRANCH:
         msg = "Invalid input: increase branch_max."
         raise ValueError(msg)
+    if v & LOKI_DEVERR_TIMEOUT:
+        msg = "a bounded wait for the tensor cores timed out"
+        raise LokiError(msg)
     if v:
         msg = f"device error word {v}"
         raise LokiError(msg)
