@@ -155,3 +155,236 @@ class BranchMLP:
 
     def state(self) -> np.ndarray:
         return self.params.cpu().numpy()
+
+
+# ---- branch statistics ------------------------------------------------------
+def parent_features(prn, tree, level: int) -> torch.Tensor:
+    """(n, 16) float32 statistics of the parents entering ``level``: their
+    score against the threshold they passed and the one their children face,
+    the level, and the shape of their normalised fold (peak, mean, spread)."""
+    thr = prn.threshold_scheme
+    nlev = len(thr)
+    n = tree.valid_size
+    dev = tree.scores.device
+    s = tree.scores.float()
+    t_prev = float(thr[level - 2]) if level >= 2 else 0.0
+    t_next = float(thr[level - 1])
+    f = tree.folds
+    if f.is_complex():
+        mag = f.abs().float()
+        norm = mag[:, 0, :] / torch.sqrt(mag[:, 1, :].clamp_min(1e-30))
+    else:
+        norm = f[:, 0, :].float() / torch.sqrt(f[:, 1, :].float().clamp_min(1e-30))
+    mx = norm.amax(dim=1)
+    mean = norm.mean(dim=1)
+    std = norm.std(dim=1).clamp_min(1e-6)
+    rank = torch.empty(n, dtype=torch.float32, device=dev)
+    rank[torch.argsort(s)] = torch.arange(n, dtype=torch.float32, device=dev) / max(n - 1, 1)
+    out = torch.zeros((n, F), dtype=torch.float32, device=dev)
+    out[:, 0] = s
+    out[:, 1] = s - t_prev
+    out[:, 2] = t_next - s
+    out[:, 3] = level / nlev
+    out[:, 4] = s / float(np.sqrt(level + 1))
+    out[:, 5] = mx
+    out[:, 6] = mean
+    out[:, 7] = std
+    out[:, 8] = (mx - mean) / std
+    out[:, 9] = rank
+    out[:, 10] = float(np.log2(max(n, 1))) / 20.0
+    out[:, 11] = t_next
+    out[:, 12] = (norm > (mean + 2 * std)[:, None]).float().mean(dim=1)
+    return out
+
+
+class Recorder:
+    """Parent hook that samples (features, tree index) of every level of a
+    plain run; ``labels`` then marks the sampled parents that still have a
+    descendant ``lookahead`` levels later (or in the last tree)."""
+
+    def __init__(self, per_level: int = 4096, seed: int = 0) -> None:
+        self.per_level = per_level
+        self.rng = torch.Generator(device="cpu").manual_seed(seed)
+        self.samples: list[tuple[int, torch.Tensor, torch.Tensor]] = []
+        self.sizes: list[int] = []
+
+    def __call__(self, prn, tree, level: int):
+        n = tree.valid_size
+        self.sizes.append(n)
+        if n == 0:
+            return None
+        feats = parent_features(prn, tree, level)
+        if n > self.per_level:
+            idx = torch.randperm(n, generator=self.rng)[: self.per_level].to(tree.scores.device)
+            feats = feats[idx]
+        else:
+            idx = torch.arange(n, device=tree.scores.device)
+        self.samples.append((level, idx, feats))
+        return None
+
+    def labels(self, prn, lookahead: int) -> tuple[torch.Tensor, torch.Tensor]:
+        """Features and 0/1 labels of every sampled parent of the finished run."""
+        hist = [bt[:, 0].long().cpu().numpy() for bt in prn.backtrack_hist]
+        # sizes[t] = parents entering level t + 1 = size of tree T_t
+        sizes = list(self.sizes) + [len(hist[-1]) if hist else 0]
+        last = len(hist)  # deepest tree index T_last with survivors
+        reach = [None] * (last + 1)
+        reach[last] = np.full(sizes[last], last, np.int64)
+        for t in range(last - 1, -1, -1):
+            r = np.full(sizes[t], t, np.int64)
+            np.maximum.at(r, hist[t], reach[t + 1])
+            reach[t] = r
+        xs, ys = [], []
+        for level, idx, feats in self.samples:
+            t = level - 1
+            if t > last:
+                continue
+            horizon = min(t + lookahead, last)
+            y = reach[t][idx.cpu().numpy()] >= horizon
+            xs.append(feats)
+            ys.append(torch.from_numpy(y.astype(np.float32)).to(feats.device))
+        if not xs:
+            return torch.zeros((0, F)), torch.zeros(0)
+        return torch.cat(xs), torch.cat(ys)
+
+
+class BranchProposal:
+    """Parent hook: when a level has more than ``budget`` parents, expand the
+    ``budget`` ones the network ranks most likely to survive (kept in tree
+    order); below the budget the level is the plain algorithm."""
+
+    def __init__(self, net: BranchMLP, budget: int) -> None:
+        self.net = net
+        self.budget = int(budget)
+        self.levels_cut = 0
+
+    def __call__(self, prn, tree, level: int):
+        n = tree.valid_size
+        if n <= self.budget:
+            return None
+        z = self.net.logits(parent_features(prn, tree, level))
+        keep = torch.topk(z, self.budget).indices
+        self.levels_cut += 1
+        return torch.sort(keep).values
+
+
+def _prune_run(dyp_of, ts, cfg, thresholds, ref, hook, device, max_sugg, batch_size):
+    """One pruning run over the FFA fold of ``ts``; returns (pruning, leaves, ms)."""
+    from pyloki_gb300.prune import Pruning
+
+    dyp = dyp_of(ts)
+    prn = Pruning(dyp, thresholds, max_sugg=max_sugg, batch_size=batch_size)
+    prn.parent_hook = hook
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    t0.record()
+    prn.initialize(ref)
+    for _ in range(dyp.nsegments - 1):
+        prn.execute_iter()
+        if prn.prune_complete:
+            break
+    prn._do_ascend()
+    t1.record()
+    torch.cuda.synchronize(device)
+    leaves = sum(st.n_leaves for st in prn.pstats[1:])
+    return prn, leaves, t0.elapsed_time(t1)
+
+
+def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
+          budget: int, lookahead: int = 16, per_level: int = 2048, epochs: int = 6,
+          det_snr: float = 8.0, max_sugg: int = 2**18, batch_size: int = 1024,
+          device=None, seed: int = 0) -> dict:
+    """Train the branch-survival network on statistics of plain pruning runs
+    and compare learned-proposal pruning with plain pruning on held-out
+    series.
+
+    ``make_series(seed, inject)`` returns a TimeSeries (with an injected pulsar
+    when ``inject``). Recall is the fraction of held-out injected series whose
+    best final score under the learned proposal is within 1e-3 of the plain
+    run's; the false-alarm rate is the fraction of noise-only series whose
+    best final score reaches ``det_snr`` (plain and learned)."""
+    import time
+
+    from pyloki_gb300.ffa import DynamicProgramming
+
+    dev = torch.device(device) if device is not None else torch.device(
+        "cuda", torch.cuda.current_device())
+
+    def dyp_of(ts):
+        d = DynamicProgramming(ts, cfg, device=dev)
+        d.initialize()
+        d.execute()
+        return d
+
+    ref = None
+    xs, ys = [], []
+    t_rec = time.perf_counter()
+    for sd in train_seeds:
+        ts = make_series(sd, True)
+        rec = Recorder(per_level=per_level, seed=sd)
+        d = dyp_of(ts)
+        ref = d.nsegments // 2 if ref is None else ref
+        prn, _, _ = _prune_run(lambda _t, d=d: d, ts, cfg, thresholds, ref, rec, dev,
+                               max_sugg, batch_size)
+        x, y = rec.labels(prn, lookahead)
+        xs.append(x)
+        ys.append(y)
+    x = torch.cat(xs)
+    y = torch.cat(ys)
+    pos = float(y.mean())
+    wt = torch.where(y > 0.5, 0.5 / max(pos, 1e-6), 0.5 / max(1 - pos, 1e-6))
+    rec_s = time.perf_counter() - t_rec
+    net = BranchMLP(device=dev, seed=seed)
+    t_fit = time.perf_counter()
+    hist = net.fit(x, y, wt, epochs=epochs, batch=8192, lr=2e-3, seed=seed)
+    torch.cuda.synchronize(dev)
+    fit_s = time.perf_counter() - t_fit
+    with torch.no_grad():
+        pred = net.predict(x) > 0.5
+    train_acc = float((pred == (y > 0.5)).float().mean())
+
+    def compare(seeds, inject):
+        rows = []
+        for sd in seeds:
+            ts = make_series(sd, inject)
+            d = dyp_of(ts)
+            p0, l0, ms0 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, None, dev,
+                                     max_sugg, batch_size)
+            b0 = float(p0.world_tree.scores.max()) if p0.world_tree.valid_size else float("-inf")
+            prop = BranchProposal(net, budget)
+            p1, l1, ms1 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, prop, dev,
+                                     max_sugg, batch_size)
+            b1 = float(p1.world_tree.scores.max()) if p1.world_tree.valid_size else float("-inf")
+            rows.append({"seed": int(sd), "plain_best": b0, "learned_best": b1,
+                         "plain_leaves": int(l0), "learned_leaves": int(l1),
+                         "plain_ms": ms0, "learned_ms": ms1, "levels_cut": prop.levels_cut,
+                         "parents_skipped": int(p1.parents_skipped)})
+        return rows
+
+    inj = compare(test_seeds, True)
+    noise = compare(noise_seeds, False)
+    l0 = sum(r["plain_leaves"] for r in inj + noise)
+    l1 = sum(r["learned_leaves"] for r in inj + noise)
+    ms0 = sum(r["plain_ms"] for r in inj + noise)
+    ms1 = sum(r["learned_ms"] for r in inj + noise)
+    return {
+        "train_series": len(train_seeds), "train_samples": int(x.shape[0]),
+        "positive_fraction": pos, "lookahead_levels": lookahead, "epochs": epochs,
+        "loss_per_epoch": hist, "train_accuracy": train_acc, "record_s": rec_s, "fit_s": fit_s,
+        "budget_parents": budget,
+        "recall_vs_plain": float(np.mean([r["learned_best"] >= r["plain_best"] - 1e-3
+                                          for r in inj])) if inj else None,
+        "false_alarm_plain": float(np.mean([r["plain_best"] >= det_snr for r in noise]))
+        if noise else None,
+        "false_alarm_learned": float(np.mean([r["learned_best"] >= det_snr for r in noise]))
+        if noise else None,
+        "det_snr": det_snr,
+        "plain_leaves_per_s": l0 / (ms0 * 1e-3), "learned_leaves_per_s": l1 / (ms1 * 1e-3),
+        "plain_equivalent_leaves_per_s": l0 / (ms1 * 1e-3), "speedup": ms0 / ms1,
+        "leaves_fraction": l1 / max(l0, 1), "injected": inj, "noise": noise,
+    }
+
+
+__all__ = ["BranchMLP", "BranchProposal", "NPARAMS", "Recorder", "SHAPES", "init_params",
+           "parent_features", "study"]

@@ -126,6 +126,11 @@ class WorldTree:
     def score_min(self) -> float:
         return float(self.scores.min().item()) if self.valid_size else 0.0
 
+    def take(self, idx: torch.Tensor) -> WorldTree:
+        """Rows ``idx`` (device int64, ascending) as a new tree."""
+        return WorldTree(self.leaves[idx], self.folds[idx], self.scores[idx],
+                         self.backtracks[idx], self.scores_ep[idx])
+
     def get_best_k(self, k: int) -> tuple[np.ndarray, np.ndarray]:
         """Top-k leaves by score, descending (``world_tree.py:441-459``)."""
         leaves_out = np.zeros((k, *self.leaves.shape[1:]), dtype=np.float64)
@@ -231,6 +236,14 @@ class Pruning:
         #: if a list, every level appends (start, end) CUDA events recorded on
         #: the launch stream around its loki_prune_score call
         self.score_events: list | None = None
+        #: optional ``hook(pruning, tree, level) -> idx | None`` called with the
+        #: parents of each Taylor level before branching; a returned ascending
+        #: index tensor restricts the level to those parents (their children
+        #: still face the exact threshold; backtracks keep the full-tree
+        #: parent indices). None keeps every parent: the plain algorithm.
+        self.parent_hook = None
+        #: parents the hook left out, summed over the run
+        self.parents_skipped = 0
 
     # ---- reference properties -----------------------------------------------
     @property
@@ -477,6 +490,10 @@ class Pruning:
         threshold = float(self.threshold_scheme[level - 1])
         d = self.level_desc(level)
         tree = self._world_tree
+        keep = self.parent_hook(self, tree, level) if self.parent_hook is not None else None
+        if keep is not None:
+            self.parents_skipped += tree.valid_size - int(keep.numel())
+            tree = tree.take(keep)
         n_par = tree.valid_size
         P = self.poly_order
         offsets = self._buf.get("offsets", n_par + 1, torch.int64)
@@ -536,6 +553,8 @@ class Pruning:
                                        _lib.ptr(new.scores), _lib.ptr(new.scores_ep),
                                        _lib.ptr(new.backtracks), stream))
         self.launches += 1
+        if keep is not None and n_surv:  # parent indices back into the full tree
+            new.backtracks[:, 0] = keep[new.backtracks[:, 0].long()].to(torch.int32)
         st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
                         score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
                         n_leaves=n_child, n_leaves_phy=n_child, n_leaves_surv=n_surv)
