@@ -491,9 +491,40 @@ def bench_gpu(args) -> dict | None:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
             out["prune"]["cpu_baseline"] = prune_cpu()
+        if not args.no_learned:
+            out["prune"]["learned"] = bench_learned(args, dev)
     if dist is not None:
         dist.destroy_process_group()
     return out
+
+
+def bench_learned(args, dev) -> dict:
+    """Learned branch proposal on the pruning workload: the MLP is trained on
+    the GPU on branch statistics of plain runs over seeded injections, then
+    plain and learned pruning run on held-out injections and noise-only
+    series (a bounded sample of the 10,000 / 1,000 / 1,000 design)."""
+    from pyloki_gb300.learned import study
+    from pyloki_gb300.simulation import make_series as ms
+
+    cfg = make_prune_cfg()
+
+    def series(seed: int, inject: bool):
+        if inject:
+            return make_prune_series(seed)[0]
+        return ms(2**22, 64e-6, seed=seed)
+
+    nseg = cfg.nsamps // cfg.bseg_ffa
+    n_tr, n_te = args.learned_train, args.learned_test
+    res = study(cfg, prune_thresholds(nseg), series,
+                train_seeds=list(range(10_000, 10_000 + n_tr)),
+                test_seeds=list(range(20_000, 20_000 + n_te)),
+                noise_seeds=list(range(30_000, 30_000 + n_te)),
+                budget=args.learned_budget, lookahead=16, per_level=2048, epochs=6,
+                max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH, device=dev)
+    res["workload"] = PRUNE_WORKLOAD
+    res["sample"] = (f"{n_tr} training injections, {n_te} held-out injections, {n_te} "
+                     "noise-only series (seeded)")
+    return res
 
 
 def batch_cfg(n: int):
@@ -753,6 +784,12 @@ def main() -> None:
                     help="skip the batched multi-series measurement")
     ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
                     help="series of the seeded 256-series batch to search")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned branch proposal study")
+    ap.add_argument("--learned-train", type=int, default=16)
+    ap.add_argument("--learned-test", type=int, default=8)
+    ap.add_argument("--learned-budget", type=int, nargs="+", default=[16384, 65536],
+                    help="parents expanded per level under the learned proposal")
     ap.add_argument("--no-prune", action="store_true",
                     help="skip the enumerate-prune (leaves/s) measurement")
     ap.add_argument("--profile-once", action="store_true",

@@ -425,6 +425,16 @@ int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* leaves, const 
                          double* leaves_out, float* folds_out, float* scores_out,
                          float* scores_ep_out, int32_t* bt_out, void* stream);
 
+/* loki_prune_branch restricted to the parents with parent_mask[i] != 0
+ * (device uint8): the others get no children (their offsets repeat), so the
+ * score, select and emit calls of the level skip them while backtracks keep
+ * the full tree's parent indices. No reference counterpart: it backs the
+ * learned branch proposal; with every mask byte set it is loki_prune_branch. */
+int loki_prune_branch_masked(const LokiPruneLevel* lvl, const double* leaves,
+                             int64_t n_parents, const uint8_t* parent_mask,
+                             LokiBranchInfo* info, int64_t* offsets, void* scan_scratch,
+                             int64_t scan_scratch_bytes, int32_t* dev_err, void* stream);
+
 /* Scratch bytes for the internal scans over n elements. */
 int64_t loki_scan_scratch_bytes(int64_t n);
 
@@ -489,6 +499,15 @@ int loki_mlp_forward(const LokiMLP* w, const float* x, int64_t n, float* logits,
 int loki_mlp_backward(const LokiMLP* w, const float* x, const float* y, const float* wt,
                       int64_t n, float scale, const LokiMLPGrad* grad, float* logits,
                       int32_t* dev_err, void* stream);
+
+/* Branch statistics of n pruning-tree parents into features (n, 16) float32
+ * (16-byte aligned): scores (n,), folds (n, 2, nbins) float32; thresholds the
+ * parents passed and their children face; level / levels; 1 / sqrt(level + 1);
+ * score_stats = device (mean, std) of the scores. */
+int loki_branch_features(const float* scores, const float* folds, int64_t n, int32_t nbins,
+                         float thr_prev, float thr_next, float level_frac,
+                         float inv_sqrt_level, const float* score_stats, float* features,
+                         void* stream);
 
 /* One Adam step over n float32 parameters (bias-corrected, step >= 1). */
 int loki_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,

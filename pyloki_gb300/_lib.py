@@ -165,6 +165,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_f32_to_bf16": (C.c_int, [_P, _I64, _P, _P]),
     "loki_mlp_smem_bytes": (C.c_int64, []),
+    "loki_branch_features": (C.c_int, [_P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float,
+                                       C.c_float, _P, _P, _P]),
     "loki_mlp_forward": (C.c_int, [C.POINTER(LokiMLP), _P, _I64, _P, _P, _P]),
     "loki_mlp_backward": (C.c_int, [C.POINTER(LokiMLP), _P, _P, _P, _I64, C.c_float,
                                     C.POINTER(LokiMLPGrad), _P, _P, _P]),
@@ -178,6 +180,7 @@ SIGNATURES: dict[str, tuple] = {
     "loki_fold_norm_complex": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_scan_scratch_bytes": (C.c_int64, [_I64]),
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
+    "loki_prune_branch_masked": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_score": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _I64, _P,
                                    C.POINTER(LokiScoreSpec), _P, _P, _P, _P, _P, _P]),
     "loki_prune_select": (C.c_int, [_P, _I64, _D, _P, _P, _P, _I64, _P]),

@@ -429,6 +429,68 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g,
   }
 }
 
+// Branch statistics of n parents (warp per parent): score against the
+// threshold passed and the next one, level, score z within the level, and the
+// shape of the normalised fold e / sqrt(v) (peak, mean, spread, peak
+// significance, fraction of bins above mean + 2 sigma). Approximate math: the
+// statistics only rank branches for the network.
+__global__ void branch_features_kernel(const float* __restrict__ scores,
+                                       const float* __restrict__ folds, int64_t n, int nbins,
+                                       float thr_prev, float thr_next, float level_frac,
+                                       float inv_sqrt_level, float log_n,
+                                       const float* __restrict__ score_stats,
+                                       float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= n) return;
+  const float* e = folds + p * 2 * nbins;
+  const float* v = e + nbins;
+  float mx = -INFINITY, sum = 0.0f, sq = 0.0f;
+  for (int j = lane; j < nbins; j += 32) {
+    const float x = e[j] * rsqrtf(fmaxf(v[j], 1e-30f));
+    mx = fmaxf(mx, x);
+    sum += x;
+    sq += x * x;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmaxf(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+    sum += __shfl_xor_sync(0xFFFFFFFFu, sum, o);
+    sq += __shfl_xor_sync(0xFFFFFFFFu, sq, o);
+  }
+  const float mean = sum / nbins;
+  const float sd = sqrtf(fmaxf(sq / nbins - mean * mean, 1e-12f));
+  int above = 0;
+  for (int j = lane; j < nbins; j += 32) {
+    const float x = e[j] * rsqrtf(fmaxf(v[j], 1e-30f));
+    above += x > mean + 2.0f * sd;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) above += __shfl_xor_sync(0xFFFFFFFFu, above, o);
+  if (lane == 0) {
+    const float s = scores[p];
+    float f[kF];
+    f[0] = s;
+    f[1] = s - thr_prev;
+    f[2] = thr_next - s;
+    f[3] = level_frac;
+    f[4] = s * inv_sqrt_level;
+    f[5] = mx;
+    f[6] = mean;
+    f[7] = sd;
+    f[8] = (mx - mean) / sd;
+    f[9] = (s - score_stats[0]) / fmaxf(score_stats[1], 1e-6f);
+    f[10] = log_n;
+    f[11] = thr_next;
+    f[12] = (float)above / nbins;
+    f[13] = f[14] = f[15] = 0.0f;
+    float4* o = reinterpret_cast<float4*>(out + p * kF);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2],
+                                                   f[4 * q + 3]);
+  }
+}
+
 static int check_mlp(const LokiMLP* W) {
   if (!W || !W->w1 || !W->b1 || !W->w2 || !W->b2 || !W->w3 || !W->b3)
     return set_error(LOKI_ERR_INVALID, "null MLP parameter pointer");
@@ -498,4 +560,23 @@ extern "C" int loki_mlp_adam(float* params, const float* grads, float* m, float*
   adam_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0,
                 (cudaStream_t)stream>>>(params, grads, m, v, n, lr, beta1, beta2, eps, c1, c2);
   return check_launch("mlp_adam");
+}
+
+extern "C" int loki_branch_features(const float* scores, const float* folds, int64_t n,
+                                    int32_t nbins, float thr_prev, float thr_next,
+                                    float level_frac, float inv_sqrt_level,
+                                    const float* score_stats, float* features, void* stream) {
+  if (n < 0 || nbins < 1) return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (n == 0) return LOKI_OK;
+  if (!scores || !folds || !score_stats || !features)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if ((reinterpret_cast<uintptr_t>(features) & 15) != 0)
+    return set_error(LOKI_ERR_INVALID, "features must be 16-byte aligned");
+  const float log_n = (float)(log2((double)n) / 20.0);
+  const int64_t threads = n * 32;
+  note_launch();
+  branch_features_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      scores, folds, n, nbins, thr_prev, thr_next, level_frac, inv_sqrt_level, log_n,
+      score_stats, features);
+  return check_launch("branch_features");
 }

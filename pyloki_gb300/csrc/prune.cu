@@ -238,7 +238,8 @@ __device__ __forceinline__ ChildRes resolve_child(const LokiPruneLevel& D, const
 
 __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                                     int64_t n, LokiBranchInfo* __restrict__ info,
-                                    int64_t* __restrict__ counts, int32_t* __restrict__ err) {
+                                    int64_t* __restrict__ counts, int32_t* __restrict__ err,
+                                    const uint8_t* __restrict__ mask) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int P = D.poly_order, m = P + 1;
@@ -306,7 +307,7 @@ __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__
     total *= num;
   }
   info[i] = B;
-  counts[i] = total;
+  counts[i] = (mask && !mask[i]) ? 0 : total;  // a masked-out parent has no children
 }
 
 // ---------------------------------------------------------------------------
@@ -1490,10 +1491,33 @@ extern "C" int64_t loki_scan_scratch_bytes(int64_t n) {
   return std::max<int64_t>(1, (n + kScanBlock - 1) / kScanBlock) * (int64_t)sizeof(int64_t);
 }
 
+static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
+                             int64_t n_parents, const uint8_t* mask, LokiBranchInfo* info,
+                             int64_t* offsets, void* scan_scratch, int64_t scan_scratch_bytes,
+                             int32_t* dev_err, void* stream);
+
 extern "C" int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves,
                                  int64_t n_parents, LokiBranchInfo* info, int64_t* offsets,
                                  void* scan_scratch, int64_t scan_scratch_bytes,
                                  int32_t* dev_err, void* stream) {
+  return prune_branch_impl(lvl, leaves, n_parents, nullptr, info, offsets, scan_scratch,
+                           scan_scratch_bytes, dev_err, stream);
+}
+
+extern "C" int loki_prune_branch_masked(const LokiPruneLevel* lvl, const double* leaves,
+                                        int64_t n_parents, const uint8_t* parent_mask,
+                                        LokiBranchInfo* info, int64_t* offsets,
+                                        void* scan_scratch, int64_t scan_scratch_bytes,
+                                        int32_t* dev_err, void* stream) {
+  if (n_parents > 0 && !parent_mask) return set_error(LOKI_ERR_INVALID, "null parent mask");
+  return prune_branch_impl(lvl, leaves, n_parents, parent_mask, info, offsets, scan_scratch,
+                           scan_scratch_bytes, dev_err, stream);
+}
+
+static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
+                             int64_t n_parents, const uint8_t* mask, LokiBranchInfo* info,
+                             int64_t* offsets, void* scan_scratch, int64_t scan_scratch_bytes,
+                             int32_t* dev_err, void* stream) {
   int rc = check_prune(lvl);
   if (rc) return rc;
   if (n_parents < 0) return set_error(LOKI_ERR_INVALID, "n_parents < 0");
@@ -1504,7 +1528,7 @@ extern "C" int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves
     // child counts go to offsets[0..n), scanned in place
     note_launch();
     prune_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
-        *lvl, leaves, n_parents, info, offsets, dev_err);
+        *lvl, leaves, n_parents, info, offsets, dev_err, mask);
     rc = check_launch("prune_branch");
     if (rc) return rc;
   }

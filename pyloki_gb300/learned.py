@@ -159,90 +159,94 @@ class BranchMLP:
 
 # ---- branch statistics ------------------------------------------------------
 def parent_features(prn, tree, level: int) -> torch.Tensor:
-    """(n, 16) float32 statistics of the parents entering ``level``: their
-    score against the threshold they passed and the one their children face,
-    the level, and the shape of their normalised fold (peak, mean, spread)."""
+    """(n, 16) float32 statistics of the parents entering ``level``
+    (``loki_branch_features``): score against the threshold they passed and
+    the one their children face, the level, the score's z within the level
+    and the shape of the normalised fold (peak, mean, spread)."""
     thr = prn.threshold_scheme
-    nlev = len(thr)
     n = tree.valid_size
     dev = tree.scores.device
-    s = tree.scores.float()
+    out = torch.empty((n, F), dtype=torch.float32, device=dev)
+    if n == 0:
+        return out
+    folds = tree.folds
+    if folds.is_complex():
+        mag = folds.abs().float().contiguous()
+        folds = mag
+    std, mean = torch.std_mean(tree.scores.float()) if n > 1 else (
+        torch.ones((), device=dev), tree.scores.float().mean())
+    stats = torch.stack([mean, std]).contiguous()
     t_prev = float(thr[level - 2]) if level >= 2 else 0.0
-    t_next = float(thr[level - 1])
-    f = tree.folds
-    if f.is_complex():
-        mag = f.abs().float()
-        norm = mag[:, 0, :] / torch.sqrt(mag[:, 1, :].clamp_min(1e-30))
-    else:
-        norm = f[:, 0, :].float() / torch.sqrt(f[:, 1, :].float().clamp_min(1e-30))
-    mx = norm.amax(dim=1)
-    mean = norm.mean(dim=1)
-    std = norm.std(dim=1).clamp_min(1e-6)
-    rank = torch.empty(n, dtype=torch.float32, device=dev)
-    rank[torch.argsort(s)] = torch.arange(n, dtype=torch.float32, device=dev) / max(n - 1, 1)
-    out = torch.zeros((n, F), dtype=torch.float32, device=dev)
-    out[:, 0] = s
-    out[:, 1] = s - t_prev
-    out[:, 2] = t_next - s
-    out[:, 3] = level / nlev
-    out[:, 4] = s / float(np.sqrt(level + 1))
-    out[:, 5] = mx
-    out[:, 6] = mean
-    out[:, 7] = std
-    out[:, 8] = (mx - mean) / std
-    out[:, 9] = rank
-    out[:, 10] = float(np.log2(max(n, 1))) / 20.0
-    out[:, 11] = t_next
-    out[:, 12] = (norm > (mean + 2 * std)[:, None]).float().mean(dim=1)
+    _lib.check(_lib.load().loki_branch_features(
+        tree.scores.data_ptr(), folds.data_ptr(), n, folds.shape[-1], t_prev,
+        float(thr[level - 1]), level / len(thr), 1.0 / float(np.sqrt(level + 1)),
+        stats.data_ptr(), out.data_ptr(),
+        _lib.stream_ptr(torch.cuda.current_stream(dev))))
     return out
 
 
 class Recorder:
-    """Parent hook that samples (features, tree index) of every level of a
-    plain run; ``labels`` then marks the sampled parents that still have a
-    descendant ``lookahead`` levels later (or in the last tree)."""
+    """Parent hook that keeps the statistics of every parent of every level of
+    a plain run; ``labels`` then marks the parents that lead to the run's best
+    final leaves (or that are still alive some levels later) and returns every
+    positive plus ``per_level`` random negatives of each level."""
 
     def __init__(self, per_level: int = 4096, seed: int = 0) -> None:
         self.per_level = per_level
-        self.rng = torch.Generator(device="cpu").manual_seed(seed)
-        self.samples: list[tuple[int, torch.Tensor, torch.Tensor]] = []
+        self.rng = np.random.default_rng(seed)
+        self.samples: list[tuple[int, torch.Tensor]] = []
         self.sizes: list[int] = []
 
     def __call__(self, prn, tree, level: int):
-        n = tree.valid_size
-        self.sizes.append(n)
-        if n == 0:
-            return None
-        feats = parent_features(prn, tree, level)
-        if n > self.per_level:
-            idx = torch.randperm(n, generator=self.rng)[: self.per_level].to(tree.scores.device)
-            feats = feats[idx]
-        else:
-            idx = torch.arange(n, device=tree.scores.device)
-        self.samples.append((level, idx, feats))
+        self.sizes.append(tree.valid_size)
+        if tree.valid_size:
+            self.samples.append((level, parent_features(prn, tree, level)))
         return None
 
-    def labels(self, prn, lookahead: int) -> tuple[torch.Tensor, torch.Tensor]:
-        """Features and 0/1 labels of every sampled parent of the finished run."""
+    def labels(self, prn, lookahead: int, top_k: int | None = None
+               ) -> tuple[torch.Tensor, torch.Tensor]:
+        """Features and 0/1 labels of the finished run: a descendant among the
+        last tree's ``top_k`` best leaves, or (``top_k`` None) a descendant
+        ``lookahead`` levels later or in the last tree."""
         hist = [bt[:, 0].long().cpu().numpy() for bt in prn.backtrack_hist]
-        # sizes[t] = parents entering level t + 1 = size of tree T_t
+        last = len(hist)  # T_last: the deepest tree with survivors
         sizes = list(self.sizes) + [len(hist[-1]) if hist else 0]
-        last = len(hist)  # deepest tree index T_last with survivors
-        reach = [None] * (last + 1)
-        reach[last] = np.full(sizes[last], last, np.int64)
-        for t in range(last - 1, -1, -1):
-            r = np.full(sizes[t], t, np.int64)
-            np.maximum.at(r, hist[t], reach[t + 1])
-            reach[t] = r
+        if top_k is not None:
+            mark = np.zeros(sizes[last], bool)
+            if sizes[last]:
+                sc = prn.world_tree.scores.float().cpu().numpy()
+                mark[np.argsort(-sc, kind="stable")[:top_k]] = True
+            lab = [None] * (last + 1)
+            lab[last] = mark
+            for t in range(last - 1, -1, -1):
+                m = np.zeros(sizes[t], bool)
+                m[hist[t][lab[t + 1]]] = True
+                lab[t] = m
+        else:
+            reach = [None] * (last + 1)
+            reach[last] = np.full(sizes[last], last, np.int64)
+            for t in range(last - 1, -1, -1):
+                r = np.full(sizes[t], t, np.int64)
+                np.maximum.at(r, hist[t], reach[t + 1])
+                reach[t] = r
+            lab = [reach[t] >= min(t + lookahead, last) for t in range(last + 1)]
         xs, ys = [], []
-        for level, idx, feats in self.samples:
+        for level, feats in self.samples:
             t = level - 1
             if t > last:
                 continue
-            horizon = min(t + lookahead, last)
-            y = reach[t][idx.cpu().numpy()] >= horizon
-            xs.append(feats)
-            ys.append(torch.from_numpy(y.astype(np.float32)).to(feats.device))
+            y = lab[t]
+            pos = np.flatnonzero(y)
+            neg = np.flatnonzero(~y)
+            if len(neg) > self.per_level:
+                neg = self.rng.choice(neg, self.per_level, replace=False)
+            if len(pos) > self.per_level:
+                pos = self.rng.choice(pos, self.per_level, replace=False)
+            idx = np.sort(np.concatenate([pos, neg]))
+            it = torch.from_numpy(idx).to(feats.device)
+            xs.append(feats[it])
+            ys.append(torch.from_numpy(y[idx].astype(np.float32)).to(feats.device))
+        self.samples = []
         if not xs:
             return torch.zeros((0, F)), torch.zeros(0)
         return torch.cat(xs), torch.cat(ys)
@@ -250,8 +254,8 @@ class Recorder:
 
 class BranchProposal:
     """Parent hook: when a level has more than ``budget`` parents, expand the
-    ``budget`` ones the network ranks most likely to survive (kept in tree
-    order); below the budget the level is the plain algorithm."""
+    ``budget`` ones the network ranks most likely to survive (ties at the cut
+    are all kept); below the budget the level is the plain algorithm."""
 
     def __init__(self, net: BranchMLP, budget: int) -> None:
         self.net = net
@@ -263,9 +267,9 @@ class BranchProposal:
         if n <= self.budget:
             return None
         z = self.net.logits(parent_features(prn, tree, level))
-        keep = torch.topk(z, self.budget).indices
+        kth = torch.topk(z, self.budget, sorted=False).values.min()
         self.levels_cut += 1
-        return torch.sort(keep).values
+        return (z >= kth).to(torch.uint8)
 
 
 def _prune_run(dyp_of, ts, cfg, thresholds, ref, hook, device, max_sugg, batch_size):
@@ -292,7 +296,8 @@ def _prune_run(dyp_of, ts, cfg, thresholds, ref, hook, device, max_sugg, batch_s
 
 
 def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
-          budget: int, lookahead: int = 16, per_level: int = 2048, epochs: int = 6,
+          budget, lookahead: int = 16, top_k: int | None = 64, per_level: int = 2048,
+          epochs: int = 6,
           det_snr: float = 8.0, max_sugg: int = 2**18, batch_size: int = 1024,
           device=None, seed: int = 0) -> dict:
     """Train the branch-survival network on statistics of plain pruning runs
@@ -300,7 +305,9 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
     series.
 
     ``make_series(seed, inject)`` returns a TimeSeries (with an injected pulsar
-    when ``inject``). Recall is the fraction of held-out injected series whose
+    when ``inject``). Labels mark the sampled parents with a descendant among
+    the run's ``top_k`` best final leaves (or, with ``top_k`` None, alive
+    ``lookahead`` levels later). Recall is the fraction of held-out injected series whose
     best final score under the learned proposal is within 1e-3 of the plain
     run's; the false-alarm rate is the fraction of noise-only series whose
     best final score reaches ``det_snr`` (plain and learned)."""
@@ -327,7 +334,7 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
         ref = d.nsegments // 2 if ref is None else ref
         prn, _, _ = _prune_run(lambda _t, d=d: d, ts, cfg, thresholds, ref, rec, dev,
                                max_sugg, batch_size)
-        x, y = rec.labels(prn, lookahead)
+        x, y = rec.labels(prn, lookahead, top_k)
         xs.append(x)
         ys.append(y)
     x = torch.cat(xs)
@@ -344,7 +351,7 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
         pred = net.predict(x) > 0.5
     train_acc = float((pred == (y > 0.5)).float().mean())
 
-    def compare(seeds, inject):
+    def compare(seeds, inject, budgets):
         rows = []
         for sd in seeds:
             ts = make_series(sd, inject)
@@ -352,37 +359,49 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
             p0, l0, ms0 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, None, dev,
                                      max_sugg, batch_size)
             b0 = float(p0.world_tree.scores.max()) if p0.world_tree.valid_size else float("-inf")
-            prop = BranchProposal(net, budget)
-            p1, l1, ms1 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, prop, dev,
-                                     max_sugg, batch_size)
-            b1 = float(p1.world_tree.scores.max()) if p1.world_tree.valid_size else float("-inf")
-            rows.append({"seed": int(sd), "plain_best": b0, "learned_best": b1,
-                         "plain_leaves": int(l0), "learned_leaves": int(l1),
-                         "plain_ms": ms0, "learned_ms": ms1, "levels_cut": prop.levels_cut,
-                         "parents_skipped": int(p1.parents_skipped)})
+            row = {"seed": int(sd), "plain_best": b0, "plain_leaves": int(l0), "plain_ms": ms0,
+                   "learned": {}}
+            for bud in budgets:
+                prop = BranchProposal(net, bud)
+                p1, l1, ms1 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, prop, dev,
+                                         max_sugg, batch_size)
+                b1 = (float(p1.world_tree.scores.max()) if p1.world_tree.valid_size
+                      else float("-inf"))
+                row["learned"][bud] = {"best": b1, "leaves": int(l1), "ms": ms1,
+                                       "levels_cut": prop.levels_cut,
+                                       "parents_skipped": int(p1.parents_skipped)}
+            rows.append(row)
         return rows
 
-    inj = compare(test_seeds, True)
-    noise = compare(noise_seeds, False)
-    l0 = sum(r["plain_leaves"] for r in inj + noise)
-    l1 = sum(r["learned_leaves"] for r in inj + noise)
-    ms0 = sum(r["plain_ms"] for r in inj + noise)
-    ms1 = sum(r["learned_ms"] for r in inj + noise)
+    budgets = [int(b) for b in (budget if np.ndim(budget) else [budget])]
+    inj = compare(test_seeds, True, budgets)
+    noise = compare(noise_seeds, False, budgets)
+    rows = inj + noise
+    l0 = sum(r["plain_leaves"] for r in rows)
+    ms0 = sum(r["plain_ms"] for r in rows)
+    per_budget = {}
+    for bud in budgets:
+        l1 = sum(r["learned"][bud]["leaves"] for r in rows)
+        ms1 = sum(r["learned"][bud]["ms"] for r in rows)
+        per_budget[str(bud)] = {
+            "recall_vs_plain": float(np.mean([r["learned"][bud]["best"] >= r["plain_best"] - 1e-3
+                                              for r in inj])) if inj else None,
+            "false_alarm_learned": float(np.mean([r["learned"][bud]["best"] >= det_snr
+                                                  for r in noise])) if noise else None,
+            "learned_leaves_per_s": l1 / (ms1 * 1e-3),
+            "plain_equivalent_leaves_per_s": l0 / (ms1 * 1e-3), "speedup": ms0 / ms1,
+            "leaves_fraction": l1 / max(l0, 1),
+        }
     return {
         "train_series": len(train_seeds), "train_samples": int(x.shape[0]),
-        "positive_fraction": pos, "lookahead_levels": lookahead, "epochs": epochs,
-        "loss_per_epoch": hist, "train_accuracy": train_acc, "record_s": rec_s, "fit_s": fit_s,
-        "budget_parents": budget,
-        "recall_vs_plain": float(np.mean([r["learned_best"] >= r["plain_best"] - 1e-3
-                                          for r in inj])) if inj else None,
+        "positive_fraction": pos, "label": (f"ancestor of the final top {top_k}"
+                                            if top_k else f"alive {lookahead} levels later"),
+        "epochs": epochs, "loss_per_epoch": hist, "train_accuracy": train_acc,
+        "record_s": rec_s, "fit_s": fit_s, "det_snr": det_snr,
         "false_alarm_plain": float(np.mean([r["plain_best"] >= det_snr for r in noise]))
         if noise else None,
-        "false_alarm_learned": float(np.mean([r["learned_best"] >= det_snr for r in noise]))
-        if noise else None,
-        "det_snr": det_snr,
-        "plain_leaves_per_s": l0 / (ms0 * 1e-3), "learned_leaves_per_s": l1 / (ms1 * 1e-3),
-        "plain_equivalent_leaves_per_s": l0 / (ms1 * 1e-3), "speedup": ms0 / ms1,
-        "leaves_fraction": l1 / max(l0, 1), "injected": inj, "noise": noise,
+        "plain_leaves_per_s": l0 / (ms0 * 1e-3),
+        "budgets": per_budget, "injected": inj, "noise": noise,
     }
 
 

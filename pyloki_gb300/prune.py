@@ -236,10 +236,10 @@ class Pruning:
         #: if a list, every level appends (start, end) CUDA events recorded on
         #: the launch stream around its loki_prune_score call
         self.score_events: list | None = None
-        #: optional ``hook(pruning, tree, level) -> idx | None`` called with the
-        #: parents of each Taylor level before branching; a returned ascending
-        #: index tensor restricts the level to those parents (their children
-        #: still face the exact threshold; backtracks keep the full-tree
+        #: optional ``hook(pruning, tree, level) -> mask | None`` called with the
+        #: parents of each Taylor level before branching; a returned device
+        #: uint8 mask restricts the level to the parents it marks (their
+        #: children still face the exact threshold; backtracks keep the tree's
         #: parent indices). None keeps every parent: the plain algorithm.
         self.parent_hook = None
         #: parents the hook left out, summed over the run
@@ -490,19 +490,24 @@ class Pruning:
         threshold = float(self.threshold_scheme[level - 1])
         d = self.level_desc(level)
         tree = self._world_tree
-        keep = self.parent_hook(self, tree, level) if self.parent_hook is not None else None
-        if keep is not None:
-            self.parents_skipped += tree.valid_size - int(keep.numel())
-            tree = tree.take(keep)
+        mask = self.parent_hook(self, tree, level) if self.parent_hook is not None else None
         n_par = tree.valid_size
+        n_expand = n_par
         P = self.poly_order
         offsets = self._buf.get("offsets", n_par + 1, torch.int64)
         info = self._buf.get("info", n_par * _lib.BRANCH_INFO_BYTES, torch.uint8)
         sb = int(lib.loki_scan_scratch_bytes(n_par + 1))
         scan = self._buf.get("scan", sb, torch.uint8)
-        _lib.check(lib.loki_prune_branch(d, _lib.ptr(tree.leaves), n_par, _lib.ptr(info),
-                                         _lib.ptr(offsets), _lib.ptr(scan), sb,
-                                         _lib.ptr(self._err), stream))
+        if mask is None:
+            _lib.check(lib.loki_prune_branch(d, _lib.ptr(tree.leaves), n_par, _lib.ptr(info),
+                                             _lib.ptr(offsets), _lib.ptr(scan), sb,
+                                             _lib.ptr(self._err), stream))
+        else:
+            _lib.check(lib.loki_prune_branch_masked(
+                d, _lib.ptr(tree.leaves), n_par, _lib.ptr(mask), _lib.ptr(info),
+                _lib.ptr(offsets), _lib.ptr(scan), sb, _lib.ptr(self._err), stream))
+            n_expand = int(mask.sum().item())
+            self.parents_skipped += n_par - n_expand
         n_child = int(offsets[n_par].item())
         _lib.check_dev_err(self._err)
         scores = self._buf.get("cscores", n_child, torch.float32)
@@ -553,10 +558,8 @@ class Pruning:
                                        _lib.ptr(new.scores), _lib.ptr(new.scores_ep),
                                        _lib.ptr(new.backtracks), stream))
         self.launches += 1
-        if keep is not None and n_surv:  # parent indices back into the full tree
-            new.backtracks[:, 0] = keep[new.backtracks[:, 0].long()].to(torch.int32)
         st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
-                        score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_par,
+                        score_min=float(mm[0]), score_max=float(mm[1]), n_branches=n_expand,
                         n_leaves=n_child, n_leaves_phy=n_child, n_leaves_surv=n_surv)
         self._pstats.append(st)
         if log_file is not None:
