@@ -72,6 +72,8 @@ def cpu_band_cfg(band_hz: float):
 
 PRUNE_WORKLOAD = "taylor4_prune_circular_orbit_2^22"
 PRUNE_MAX_SUGG = 2**18
+PRUNE_MULTI_RUNS = 8   # reference segments of the multi-run measurement
+PRUNE_WORKERS = 4      # concurrent runs (host threads and CUDA streams)
 PRUNE_BATCH = 1024
 PRUNE_THRESHOLD_FINAL = 4.0
 # HBM bytes per leaf of prune_score_kernel: the parent fold (2 x 64 f32) read
@@ -201,8 +203,30 @@ def bench_prune_gpu(args, dev) -> dict:
         d2h = res["param_sets"].nbytes + res["scores"].nbytes + res["scores_ep"].nbytes
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
+    # several reference segments at once (prune_dyp_tree's n_workers): runs on
+    # concurrent host threads and streams overlap one another's host waits
+    from pyloki_gb300.prune import run_many
+
+    refs = [int(r) for r in np.linspace(8, nseg - 8, PRUNE_MULTI_RUNS).round()]
+    multi = {}
+    for nw in (1, PRUNE_WORKERS):
+        run_many(dyp, thr, refs[:nw], n_workers=nw, max_sugg=PRUNE_MAX_SUGG,
+                 batch_size=PRUNE_BATCH)  # warm-up of the worker streams
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = run_many(dyp, thr, refs, n_workers=nw, max_sugg=PRUNE_MAX_SUGG,
+                       batch_size=PRUNE_BATCH)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+        nl = sum(st.n_leaves for r in res.values() for st in r["level_stats"][1:])
+        multi[f"workers_{nw}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
+    multi["runs"] = len(refs)
+    multi["ref_segments"] = refs
+    multi["speedup"] = (multi[f"workers_{PRUNE_WORKERS}"]["leaves_per_s"]
+                        / multi["workers_1"]["leaves_per_s"])
     return {
         "metric": "prune leaves/s", "value": leaves / (ms * 1e-3), "unit": "leaves/s",
+        "multi_run": multi,
         "ms_per_step": ms / args.steps, "leaves_per_step": leaves // args.steps,
         "dtype": "f32 folds, f64 parameters",
         "data": "synthetic (seeded N(0,1) noise + 3 ms pulsar in a circular orbit, S/N 10)",

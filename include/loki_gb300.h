@@ -435,6 +435,71 @@ int loki_prune_branch_masked(const LokiPruneLevel* lvl, const double* leaves,
                              LokiBranchInfo* info, int64_t* offsets, void* scan_scratch,
                              int64_t scan_scratch_bytes, int32_t* dev_err, void* stream);
 
+/* ---- native level driver ---------------------------------------------- */
+
+/* A pruning tree on the device: n rows in use of cap. */
+typedef struct {
+  double* leaves;      /* (cap, poly_order + 2, 2) */
+  float* folds;        /* (cap, 2, nbins) */
+  float* scores;       /* (cap,) */
+  float* scores_ep;    /* (cap,) */
+  int32_t* backtracks; /* (cap, poly_order + 2) */
+  int64_t n;
+  int64_t cap;
+} LokiPruneTree;
+
+/* Caller-owned workspace of loki_prune_level (device unless noted). */
+typedef struct {
+  void* info;              /* par_cap LokiBranchInfo */
+  int64_t* offsets;        /* par_cap + 1 */
+  void* scan;              /* loki_scan_scratch_bytes(par_cap + 1) */
+  int64_t scan_bytes;
+  int64_t par_cap;
+  float* child_scores;     /* child_cap */
+  int32_t* child_idx;      /* 2 * child_cap */
+  double* child_phase;     /* child_cap */
+  int64_t* surv;           /* child_cap */
+  void* sscan;             /* loki_scan_scratch_bytes(child_cap) + 8 (child_cap + 1) */
+  int64_t sscan_bytes;
+  int64_t child_cap;
+  int64_t* n_surv;         /* 1 */
+  float* minmax;           /* 2 */
+  int64_t* ovf_ids;        /* ovf_cap */
+  float* ovf_keys;         /* ovf_cap */
+  double* ovf_thr;         /* 1 */
+  int64_t ovf_cap;
+  int64_t* host_words;     /* pinned host memory, 4 words */
+  void* ev_score_begin;    /* optional cudaEvent_t recorded before / after the */
+  void* ev_score_end;      /* score launch (NULL: none) */
+} LokiPruneWork;
+
+/* What one level did; need_* > 0 names the capacity to grow to after a
+ * LOKI_ERR_CAPACITY return (the level can then be run again as is). */
+typedef struct {
+  int64_t n_parents;
+  int64_t n_children;
+  int64_t n_surv;
+  float score_min;
+  float score_max;
+  int32_t overflow;        /* the overflow rule ran */
+  int32_t dev_err;         /* non-zero: error word set by branch (nothing else ran) */
+  int64_t need_par_cap;
+  int64_t need_child_cap;
+  int64_t need_ovf_cap;
+  int64_t need_tree_cap;
+} LokiPruneLevelResult;
+
+/* One pruning level of the Taylor or Chebyshev plugin on real folds
+ * (prune.py:165-332): branch (restricted to parent_mask when not NULL),
+ * score, select with the overflow rule at max_sugg survivors, emit into out.
+ * The same calls as loki_prune_branch / _score / _select / _select_overflow /
+ * _emit in sequence, with two host waits on w->host_words. */
+int loki_prune_level(const LokiPruneLevel* lvl, const LokiPruneTree* in, LokiPruneTree* out,
+                     const LokiPruneWork* w, const float* fold_segment,
+                     const LokiScoreSpec* spec, double threshold, int64_t max_sugg,
+                     int64_t batch_size, const uint8_t* parent_mask, LokiPruneLevelResult* res,
+                     int32_t* dev_err, void* stream);
+
 /* Scratch bytes for the internal scans over n elements. */
 int64_t loki_scan_scratch_bytes(int64_t n);
 

@@ -132,6 +132,31 @@ _D = C.c_double
 _PL = C.POINTER(LokiPruneLevel)
 
 #: name -> (restype, argtypes); the exported C ABI.
+class LokiPruneTree(C.Structure):
+    _fields_ = [("leaves", C.c_void_p), ("folds", C.c_void_p), ("scores", C.c_void_p),
+                ("scores_ep", C.c_void_p), ("backtracks", C.c_void_p), ("n", C.c_int64),
+                ("cap", C.c_int64)]
+
+
+class LokiPruneWork(C.Structure):
+    _fields_ = [("info", C.c_void_p), ("offsets", C.c_void_p), ("scan", C.c_void_p),
+                ("scan_bytes", C.c_int64), ("par_cap", C.c_int64),
+                ("child_scores", C.c_void_p), ("child_idx", C.c_void_p),
+                ("child_phase", C.c_void_p), ("surv", C.c_void_p), ("sscan", C.c_void_p),
+                ("sscan_bytes", C.c_int64), ("child_cap", C.c_int64), ("n_surv", C.c_void_p),
+                ("minmax", C.c_void_p), ("ovf_ids", C.c_void_p), ("ovf_keys", C.c_void_p),
+                ("ovf_thr", C.c_void_p), ("ovf_cap", C.c_int64), ("host_words", C.c_void_p),
+                ("ev_score_begin", C.c_void_p), ("ev_score_end", C.c_void_p)]
+
+
+class LokiPruneLevelResult(C.Structure):
+    _fields_ = [("n_parents", C.c_int64), ("n_children", C.c_int64), ("n_surv", C.c_int64),
+                ("score_min", C.c_float), ("score_max", C.c_float), ("overflow", C.c_int32),
+                ("dev_err", C.c_int32), ("need_par_cap", C.c_int64),
+                ("need_child_cap", C.c_int64), ("need_ovf_cap", C.c_int64),
+                ("need_tree_cap", C.c_int64)]
+
+
 class LokiMLP(C.Structure):
     _fields_ = [("w1", C.c_void_p), ("b1", C.c_void_p), ("w2", C.c_void_p),
                 ("b2", C.c_void_p), ("w3", C.c_void_p), ("b3", C.c_void_p)]
@@ -181,6 +206,9 @@ SIGNATURES: dict[str, tuple] = {
     "loki_scan_scratch_bytes": (C.c_int64, [_I64]),
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_branch_masked": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
+    "loki_prune_level": (C.c_int, [_PL, C.POINTER(LokiPruneTree), C.POINTER(LokiPruneTree),
+                                   C.POINTER(LokiPruneWork), _P, C.POINTER(LokiScoreSpec), _D,
+                                   _I64, _I64, _P, C.POINTER(LokiPruneLevelResult), _P, _P]),
     "loki_prune_score": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _I64, _P,
                                    C.POINTER(LokiScoreSpec), _P, _P, _P, _P, _P, _P]),
     "loki_prune_select": (C.c_int, [_P, _I64, _D, _P, _P, _P, _I64, _P]),

@@ -23,6 +23,7 @@ tree of order 5 (``PruneCircTaylorDPFuncts``, its own branch / map / validate
 
 from __future__ import annotations
 
+import ctypes as C
 import dataclasses
 import math
 from pathlib import Path
@@ -125,6 +126,16 @@ class WorldTree:
     @property
     def score_min(self) -> float:
         return float(self.scores.min().item()) if self.valid_size else 0.0
+
+    def best_k_device(self, k: int) -> tuple[torch.Tensor, torch.Tensor]:
+        """Top-k leaves and scores by score, descending, left on the device
+        (no host synchronisation); ``get_best_k`` is the host version."""
+        k_take = min(k, self.valid_size)
+        if k_take == 0:
+            return self.leaves[:0], self.scores[:0]
+        idx = (torch.argmax(self.scores).reshape(1) if k_take == 1
+               else torch.topk(self.scores, k_take).indices)
+        return self.leaves[idx], self.scores[idx]
 
     def take(self, idx: torch.Tensor) -> WorldTree:
         """Rows ``idx`` (device int64, ascending) as a new tree."""
@@ -296,7 +307,25 @@ class Pruning:
 
     @property
     def best_intermediate_arr(self) -> np.ndarray:
+        self._flush_best()
         return self._best_intermediate_arr
+
+    def _flush_best(self) -> None:
+        """Copy the per-level best leaves recorded on the device to the host
+        array (one synchronisation for the whole run)."""
+        for row, leaves, scores in self._pending_best:
+            slot = self._best_intermediate_arr[row]
+            k = int(scores.shape[0])
+            slot["param_sets"][:] = 0
+            slot["scores"][:] = 0
+            if k:
+                slot["param_sets"][:k] = leaves.cpu().numpy()
+                slot["scores"][:k] = scores.cpu().numpy()
+        self._pending_best = []
+
+    def _record_best(self, level: int, tree: WorldTree) -> None:
+        leaves, scores = tree.best_k_device(self.intermediate_k)
+        self._pending_best.append((level - 1, leaves, scores))
 
     def _stream(self) -> int:
         return _lib.stream_ptr(torch.cuda.current_stream(self._device))
@@ -348,6 +377,16 @@ class Pruning:
         self._prune_level = 0
         self._world_tree = self._seed(self._fold_segment(self.scheme.ref_idx))
         self._backtrack_hist: list[torch.Tensor] = []
+        self._pending_best: list = []
+        self._slots: list = [None, None]
+        self._slot_next = 0
+        self._work_desc = None
+        self._child_cap = max(1 << 20, 64 * self.max_sugg)
+        self._ovf_cap = 0
+        self._host_words = torch.zeros(4, dtype=torch.int64, pin_memory=True)
+        self._pin_n = torch.empty(1, dtype=torch.int64, pin_memory=True)
+        self._pin_mm = torch.empty(2, dtype=torch.float32, pin_memory=True)
+        self._pin_err = torch.empty(1, dtype=torch.int32, pin_memory=True)
         self._best_intermediate_arr = np.zeros(
             (self.dyp.nsegments - 1, self.intermediate_k),
             dtype=np.dtype([("param_sets", np.float64, (self.poly_order + 2, 2)),
@@ -481,6 +520,9 @@ class Pruning:
         if self.circular:
             self._execute_iter_circ(log_file)
             return
+        if not self.fourier:
+            self._execute_iter_native(log_file)
+            return
         self._prune_level += 1
         level = self._prune_level
         lib = self._lib
@@ -508,8 +550,13 @@ class Pruning:
                 _lib.ptr(offsets), _lib.ptr(scan), sb, _lib.ptr(self._err), stream))
             n_expand = int(mask.sum().item())
             self.parents_skipped += n_par - n_expand
-        n_child = int(offsets[n_par].item())
-        _lib.check_dev_err(self._err)
+        # child count and the error word in one wait
+        self._pin_n.copy_(offsets[n_par:n_par + 1], non_blocking=True)
+        self._pin_err.copy_(self._err, non_blocking=True)
+        torch.cuda.current_stream(self._device).synchronize()
+        n_child = int(self._pin_n[0])
+        if int(self._pin_err[0]):
+            _lib.check_dev_err(self._err)
         scores = self._buf.get("cscores", n_child, torch.float32)
         cidx = self._buf.get("cidx", 2 * n_child, torch.int32)
         cphase = self._buf.get("cphase", n_child, torch.float64)
@@ -533,10 +580,13 @@ class Pruning:
         n_surv_d = self._buf.get("nsurv", 1, torch.int64)
         _lib.check(lib.loki_prune_select(_lib.ptr(scores), n_child, threshold, _lib.ptr(surv),
                                          _lib.ptr(n_surv_d), _lib.ptr(sscan), ssb, stream))
-        n_surv = int(n_surv_d.item())
-        # score min/max is final once the selection is: read it now so that
-        # the emit below runs while the host prepares the next level
-        mm = minmax.cpu().numpy() if n_child else np.zeros(2, np.float32)
+        # survivor count and score min/max in one transfer and one wait
+        self._pin_n.copy_(n_surv_d, non_blocking=True)
+        if n_child:
+            self._pin_mm.copy_(minmax[:2], non_blocking=True)
+        torch.cuda.current_stream(self._device).synchronize()
+        n_surv = int(self._pin_n[0])
+        mm = self._pin_mm.numpy().copy() if n_child else np.zeros(2, np.float32)
         self.launches += 9
         if n_surv > self.max_sugg:
             n_surv = self._select_overflow(scores, offsets, n_par, n_child, threshold, surv,
@@ -569,9 +619,127 @@ class Pruning:
             self._prune_complete = True
             self._world_tree = new
             return
-        slot = self._best_intermediate_arr[level - 1]
-        slot["param_sets"], slot["scores"] = new.get_best_k(self.intermediate_k)
+        self._record_best(level, new)
         self._backtrack_hist.append(new.backtracks)
+        self._world_tree = new
+
+    # ---- native level driver (loki_prune_level) ------------------------------
+    def _tree_slot(self, k: int, cap: int) -> dict:
+        """Ping-pong output tree buffers (capacity ``cap`` rows)."""
+        slots = self._slots
+        t = slots[k]
+        if t is None or t["cap"] < cap:
+            P, nb, dev = self.poly_order, self.dyp.cfg.nbins, self._device
+            t = slots[k] = {
+                "cap": cap,
+                "leaves": torch.empty((cap, P + 2, 2), dtype=torch.float64, device=dev),
+                "folds": torch.empty((cap, 2, nb), dtype=torch.float32, device=dev),
+                "scores": torch.empty(cap, dtype=torch.float32, device=dev),
+                "scores_ep": torch.empty(cap, dtype=torch.float32, device=dev),
+                "bt": torch.empty((cap, P + 2), dtype=torch.int32, device=dev)}
+        return t
+
+    def _work(self, par_cap: int, child_cap: int, ovf_cap: int) -> _lib.LokiPruneWork:
+        """The driver's workspace, grown to at least the given capacities."""
+        w = self._work_desc
+        if (w is not None and w.par_cap >= par_cap and w.child_cap >= child_cap
+                and w.ovf_cap >= ovf_cap):
+            return w
+        lib, b = self._lib, self._buf
+        par_cap = max(par_cap, w.par_cap if w is not None else 0)
+        child_cap = max(child_cap, w.child_cap if w is not None else 0)
+        ovf_cap = max(ovf_cap, w.ovf_cap if w is not None else 0)
+        w = _lib.LokiPruneWork()
+        w.par_cap, w.child_cap, w.ovf_cap = par_cap, child_cap, ovf_cap
+        w.info = b.get("info", par_cap * _lib.BRANCH_INFO_BYTES, torch.uint8).data_ptr()
+        w.offsets = b.get("offsets", par_cap + 1, torch.int64).data_ptr()
+        w.scan_bytes = int(lib.loki_scan_scratch_bytes(par_cap + 1))
+        w.scan = b.get("scan", w.scan_bytes, torch.uint8).data_ptr()
+        w.child_scores = b.get("cscores", child_cap, torch.float32).data_ptr()
+        w.child_idx = b.get("cidx", 2 * child_cap, torch.int32).data_ptr()
+        w.child_phase = b.get("cphase", child_cap, torch.float64).data_ptr()
+        w.surv = b.get("surv", max(child_cap, 1), torch.int64).data_ptr()
+        w.sscan_bytes = int(lib.loki_scan_scratch_bytes(child_cap)) + 8 * (child_cap + 1)
+        w.sscan = b.get("sscan", w.sscan_bytes, torch.uint8).data_ptr()
+        w.n_surv = b.get("nsurv", 1, torch.int64).data_ptr()
+        w.minmax = b.get("minmax", 2, torch.float32).data_ptr()
+        w.ovf_ids = b.get("ovf_ids", ovf_cap, torch.int64).data_ptr()
+        w.ovf_keys = b.get("ovf_keys", ovf_cap, torch.float32).data_ptr()
+        w.ovf_thr = b.get("ovf_thr", 1, torch.float64).data_ptr()
+        w.host_words = self._host_words.data_ptr()
+        self._work_desc = w
+        return w
+
+    def _execute_iter_native(self, log_file: Path | None = None) -> None:
+        self._prune_level += 1
+        level = self._prune_level
+        seg_idx = self.scheme.get_segment_idx(level)
+        fold_segment = self._fold_segment(seg_idx)
+        threshold = float(self.threshold_scheme[level - 1])
+        d = self.level_desc(level)
+        tree = self._world_tree
+        mask = self.parent_hook(self, tree, level) if self.parent_hook is not None else None
+        n_par = tree.valid_size
+        tin = _lib.LokiPruneTree(tree.leaves.data_ptr(), tree.folds.data_ptr(),
+                                 tree.scores.data_ptr(), tree.scores_ep.data_ptr(),
+                                 tree.backtracks.data_ptr(), n_par, n_par)
+        slot = self._tree_slot(self._slot_next, self.max_sugg)
+        tout = _lib.LokiPruneTree(slot["leaves"].data_ptr(), slot["folds"].data_ptr(),
+                                  slot["scores"].data_ptr(), slot["scores_ep"].data_ptr(),
+                                  slot["bt"].data_ptr(), 0, slot["cap"])
+        res = _lib.LokiPruneLevelResult()
+        w = self._work(max(n_par, self.max_sugg), self._child_cap, self._ovf_cap)
+        events = None
+        if self.score_events is not None:
+            cur = torch.cuda.current_stream(self._device)
+            events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for e in events:  # created on first record; the driver records them again
+                e.record(cur)
+        while True:
+            w.ev_score_begin = events[0].cuda_event if events else None
+            w.ev_score_end = events[1].cuda_event if events else None
+            rc = self._lib.loki_prune_level(
+                d, C.byref(tin), C.byref(tout), C.byref(w), _lib.ptr(fold_segment), self.spec,
+                threshold, self.max_sugg, self.batch_size, _lib.ptr(mask), C.byref(res),
+                _lib.ptr(self._err), self._stream())
+            if rc == _lib.LOKI_ERR_CAPACITY and (res.need_par_cap or res.need_child_cap
+                                                 or res.need_ovf_cap):
+                self._child_cap = max(self._child_cap, int(res.need_child_cap * 1.25))
+                self._ovf_cap = max(self._ovf_cap, int(res.need_ovf_cap * 1.25))
+                w = self._work(max(n_par, res.need_par_cap), self._child_cap, self._ovf_cap)
+                continue
+            _lib.check(rc)
+            break
+        if res.dev_err:
+            _lib.check_dev_err(self._err)
+        w.ev_score_begin = w.ev_score_end = None
+        if events is not None:
+            self.score_events.append((int(res.n_children), events[0], events[1]))
+        self.launches += 8 + (1 if res.overflow else 0)
+        n_surv = int(res.n_surv)
+        n_expand = n_par
+        if mask is not None:
+            n_expand = int(mask.sum().item())
+            self.parents_skipped += n_par - n_expand
+        new = WorldTree(slot["leaves"][:n_surv], slot["folds"][:n_surv], slot["scores"][:n_surv],
+                        slot["bt"][:n_surv], slot["scores_ep"][:n_surv])
+        self._slot_next ^= 1
+        n_child = int(res.n_children)
+        st = PruneStats(level=level, seg_idx=seg_idx, threshold=threshold,
+                        score_min=float(res.score_min) if n_child else 0.0,
+                        score_max=float(res.score_max) if n_child else 0.0,
+                        n_branches=n_expand, n_leaves=n_child, n_leaves_phy=n_child,
+                        n_leaves_surv=n_surv)
+        self._pstats.append(st)
+        if log_file is not None:
+            with Path(log_file).open("a") as f:
+                f.write(st.get_summary())
+        if n_surv == 0:
+            self._prune_complete = True
+            self._world_tree = new
+            return
+        self._record_best(level, new)
+        self._backtrack_hist.append(new.backtracks.clone())
         self._world_tree = new
 
     def _execute_iter_circ(self, log_file: Path | None = None) -> None:
@@ -664,8 +832,7 @@ class Pruning:
             self._prune_complete = True
             self._world_tree = new
             return
-        slot = self._best_intermediate_arr[st.level - 1]
-        slot["param_sets"], slot["scores"] = new.get_best_k(self.intermediate_k)
+        self._record_best(st.level, new)
         self._backtrack_hist.append(new.backtracks)
         self._world_tree = new
 
@@ -815,8 +982,9 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
                    use_moving_grid: bool = True, n_workers: int = 4) -> str:
     """Prune from several reference segments (``prune.py:824-932``).
 
-    Runs are executed one after another on the device (``n_workers`` is
-    validated like the reference but a single GPU needs no process pool).
+    ``n_workers`` runs proceed at once, each on its own host thread and CUDA
+    stream (``run_many``), so one run's host work and waits overlap the
+    others' kernels; every run is the same computation as on its own.
     Results are written as one ``.npz`` with the reference's per-run groups
     (``runs/<ref:03d>_<task:02d>/{scheme, param_sets, scores, scores_ep}``).
     """
@@ -845,12 +1013,15 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     log_file.write_text("Pruning log\n")
     out = {"param_names": np.asarray(dyp.cfg.param_names), "nsegments": dyp.nsegments,
            "max_sugg": max_sugg, "threshold_scheme": np.asarray(threshold_scheme)}
-    prn = Pruning(dyp, threshold_scheme, max_sugg=max_sugg, batch_size=batch_size,
-                  poly_basis=poly_basis, use_moving_grid=use_moving_grid)
+    results = run_many(dyp, threshold_scheme, ref_segs, n_workers=n_workers,
+                       ascend_levels=ascend_levels, max_sugg=max_sugg, batch_size=batch_size,
+                       poly_basis=poly_basis, use_moving_grid=use_moving_grid)
     for ref_seg in ref_segs:
+        res = results[ref_seg]
         with log_file.open("a") as f:
             f.write(f"Pruning log for ref segment: {ref_seg}\n")
-        res = prn.execute(ref_seg, ascend_levels=ascend_levels, log_file=log_file)
+            for st in res["level_stats"]:
+                f.write(st.get_summary())
         g = f"runs/{res['run_name']}"
         out[f"{g}/scheme"] = res["scheme"]
         out[f"{g}/param_sets"] = res["param_sets"]
@@ -862,6 +1033,55 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
             dtype=np.float64)
     np.savez_compressed(result_file, **out)
     return result_file.as_posix()
+
+
+def run_many(dyp, threshold_scheme, ref_segs, *, n_workers: int = 4,
+             ascend_levels: list[int] | None = None, **kwargs) -> dict[int, dict]:
+    """``Pruning.execute`` for every reference segment, ``n_workers`` at a
+    time on separate host threads and CUDA streams; results by segment."""
+    import threading
+
+    ref_segs = list(ref_segs)
+    dev = dyp.device
+    producer = torch.cuda.current_stream(dev)
+    work = list(ref_segs)
+    results: dict[int, dict] = {}
+    errors: list[BaseException] = []
+    lock = threading.Lock()
+    streams = [torch.cuda.Stream(dev) for _ in range(max(1, min(n_workers, len(ref_segs))))]
+
+    def worker(stream) -> None:
+        try:
+            stream.wait_stream(producer)  # the fold is ready before any run reads it
+            with torch.cuda.device(dev), torch.cuda.stream(stream):
+                prn = Pruning(dyp, threshold_scheme, **kwargs)
+                while True:
+                    with lock:
+                        if not work or errors:
+                            return
+                        ref = work.pop(0)
+                    before = prn.launches
+                    res = prn.execute(ref, ascend_levels=ascend_levels)
+                    res["launches"] = prn.launches - before
+                    with lock:
+                        results[ref] = res
+        except BaseException as e:  # noqa: BLE001 - re-raised in the caller
+            with lock:
+                errors.append(e)
+
+    if len(streams) == 1:
+        worker(streams[0])
+    else:
+        threads = [threading.Thread(target=worker, args=(st,)) for st in streams]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    for st in streams:
+        producer.wait_stream(st)
+    if errors:
+        raise errors[0]
+    return results
 
 
 def leaves_per_second(stats: list[PruneStats], seconds: float) -> float:

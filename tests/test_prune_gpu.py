@@ -137,3 +137,19 @@ def test_prune_dyp_tree_writes_results(cuda_device, tmp_path):
         prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=2, outdir=tmp_path, n_workers=1)
     with pytest.raises(ValueError):
         prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=0, outdir=tmp_path / "x")
+
+
+def test_prune_dyp_tree_concurrent_workers_match_serial(cuda_device, tmp_path):
+    """Four runs on three worker threads and streams write the same results as
+    one after another."""
+    from pyloki_gb300.prune import prune_dyp_tree
+
+    d, prn = _run("prune_taylor", cuda_device)
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
+    a = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "a",
+                               n_workers=1, **kw))
+    b = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "b",
+                               n_workers=3, **kw))
+    assert sorted(a.files) == sorted(b.files)
+    for k in a.files:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
