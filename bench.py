@@ -793,6 +793,30 @@ def profile_once(args) -> None:
                       "launches": dyp.launches, "snr_shape": list(snr.shape)}))
 
 
+def profile_prune_once(args) -> None:
+    """One pruning run of the pruning workload after one warm-up run, with no
+    timing; the command the pruning ncu summaries are captured from."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import Pruning
+
+    dev = torch.device("cuda", 0)
+    cfg = make_prune_cfg()
+    ts, _ = make_prune_series(seed=2000)
+    dyp = DynamicProgramming(ts, cfg, device=dev)
+    dyp.initialize()
+    dyp.execute()
+    nseg = dyp.nsegments
+    prn = Pruning(dyp, prune_thresholds(nseg), max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
+    for _ in range(2):
+        res = prn.execute(nseg // 2)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_prune_once": True, "levels": nseg - 1,
+                      "leaves": sum(st.n_leaves for st in res["level_stats"][1:]),
+                      "launches_per_run": prn.launches // 2}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -818,11 +842,16 @@ def main() -> None:
                     help="skip the enumerate-prune (leaves/s) measurement")
     ap.add_argument("--profile-once", action="store_true",
                     help="run exactly one search (for ncu captures) and exit")
+    ap.add_argument("--profile-prune-once", action="store_true",
+                    help="run the pruning workload twice (warm-up + one run) and exit")
     ap.add_argument("--nsamps-log2", type=int, default=23,
                     help="series length for --profile-once (smaller ncu cases)")
     args = ap.parse_args()
     if args.profile_once:
         profile_once(args)
+        return
+    if args.profile_prune_once:
+        profile_prune_once(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

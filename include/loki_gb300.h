@@ -500,6 +500,12 @@ int loki_prune_level(const LokiPruneLevel* lvl, const LokiPruneTree* in, LokiPru
                      int64_t batch_size, const uint8_t* parent_mask, LokiPruneLevelResult* res,
                      int32_t* dev_err, void* stream);
 
+/* Best leaf of a tree (utils/world_tree.py:441-459 get_best_k with k = 1):
+ * the leaf row (row_len float64) and score of the maximum score, first index
+ * on ties; nothing is written for n = 0. */
+int loki_prune_best(const float* scores, int64_t n, const double* leaves, int32_t row_len,
+                    double* leaf_out, float* score_out, void* stream);
+
 /* Scratch bytes for the internal scans over n elements. */
 int64_t loki_scan_scratch_bytes(int64_t n);
 

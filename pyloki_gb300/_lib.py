@@ -206,6 +206,7 @@ SIGNATURES: dict[str, tuple] = {
     "loki_scan_scratch_bytes": (C.c_int64, [_I64]),
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_branch_masked": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
+    "loki_prune_best": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P]),
     "loki_prune_level": (C.c_int, [_PL, C.POINTER(LokiPruneTree), C.POINTER(LokiPruneTree),
                                    C.POINTER(LokiPruneWork), _P, C.POINTER(LokiScoreSpec), _D,
                                    _I64, _I64, _P, C.POINTER(LokiPruneLevelResult), _P, _P]),

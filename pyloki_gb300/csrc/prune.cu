@@ -1496,6 +1496,68 @@ static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
                              int64_t* offsets, void* scan_scratch, int64_t scan_scratch_bytes,
                              int32_t* dev_err, void* stream);
 
+// Best leaf of a tree (max score, first index on ties, as torch.argmax):
+// one block reduces (score, index), then copies the leaf row and its score.
+__global__ void __launch_bounds__(1024)
+prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __restrict__ leaves,
+                  int row, double* __restrict__ leaf_out, float* __restrict__ score_out) {
+  __shared__ float sv[32];
+  __shared__ int64_t si[32];
+  float bv = -INFINITY;
+  int64_t bi = -1;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float v = scores[i];
+    if (bi < 0 || v > bv) {  // strided order: the first maximum of this thread
+      bv = v;
+      bi = i;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_down_sync(0xFFFFFFFFu, bv, o);
+    const int64_t oi = __shfl_down_sync(0xFFFFFFFFu, bi, o);
+    if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+      bv = ov;
+      bi = oi;
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sv[warp] = bv;
+    si[warp] = bi;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    bv = lane < nw ? sv[lane] : -INFINITY;
+    bi = lane < nw ? si[lane] : -1;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_down_sync(0xFFFFFFFFu, bv, o);
+      const int64_t oi = __shfl_down_sync(0xFFFFFFFFu, bi, o);
+      if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    bi = __shfl_sync(0xFFFFFFFFu, bi, 0);
+    if (bi >= 0)
+      for (int j = lane; j < row; j += 32) leaf_out[j] = leaves[bi * row + j];
+    if (lane == 0 && bi >= 0) *score_out = scores[bi];
+  }
+}
+
+extern "C" int loki_prune_best(const float* scores, int64_t n, const double* leaves,
+                               int32_t row_len, double* leaf_out, float* score_out,
+                               void* stream) {
+  if (n < 0 || row_len < 1) return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (n == 0) return LOKI_OK;
+  if (!scores || !leaves || !leaf_out || !score_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  prune_best_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, n, leaves, row_len, leaf_out,
+                                                         score_out);
+  return check_launch("prune_best");
+}
+
 extern "C" int loki_prune_branch(const LokiPruneLevel* lvl, const double* leaves,
                                  int64_t n_parents, LokiBranchInfo* info, int64_t* offsets,
                                  void* scan_scratch, int64_t scan_scratch_bytes,

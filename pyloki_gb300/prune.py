@@ -313,17 +313,32 @@ class Pruning:
     def _flush_best(self) -> None:
         """Copy the per-level best leaves recorded on the device to the host
         array (one synchronisation for the whole run)."""
+        if self._pending_best:
+            bl = self._best_leaves.cpu().numpy()
+            bs = self._best_scores.cpu().numpy()
         for row, leaves, scores in self._pending_best:
             slot = self._best_intermediate_arr[row]
             k = int(scores.shape[0])
             slot["param_sets"][:] = 0
             slot["scores"][:] = 0
-            if k:
+            if k and leaves.data_ptr() == self._best_leaves[row].data_ptr():
+                slot["param_sets"][0] = bl[row]
+                slot["scores"][0] = bs[row]
+            elif k:
                 slot["param_sets"][:k] = leaves.cpu().numpy()
                 slot["scores"][:k] = scores.cpu().numpy()
         self._pending_best = []
 
     def _record_best(self, level: int, tree: WorldTree) -> None:
+        if self.intermediate_k == 1 and tree.valid_size:  # one native launch
+            row = int(np.prod(tree.leaves.shape[1:]))
+            leaf = self._best_leaves[level - 1]
+            score = self._best_scores[level - 1:level]
+            _lib.check(self._lib.loki_prune_best(
+                tree.scores.data_ptr(), tree.valid_size, tree.leaves.data_ptr(), row,
+                leaf.data_ptr(), score.data_ptr(), self._stream()))
+            self._pending_best.append((level - 1, leaf[None], score))
+            return
         leaves, scores = tree.best_k_device(self.intermediate_k)
         self._pending_best.append((level - 1, leaves, scores))
 
@@ -378,6 +393,10 @@ class Pruning:
         self._world_tree = self._seed(self._fold_segment(self.scheme.ref_idx))
         self._backtrack_hist: list[torch.Tensor] = []
         self._pending_best: list = []
+        nlev = max(self.dyp.nsegments - 1, 1)
+        self._best_leaves = torch.zeros((nlev, self.poly_order + 2, 2), dtype=torch.float64,
+                                        device=self._device)
+        self._best_scores = torch.zeros(nlev, dtype=torch.float32, device=self._device)
         self._slots: list = [None, None]
         self._slot_next = 0
         self._work_desc = None

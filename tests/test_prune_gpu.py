@@ -153,3 +153,20 @@ def test_prune_dyp_tree_concurrent_workers_match_serial(cuda_device, tmp_path):
     assert sorted(a.files) == sorted(b.files)
     for k in a.files:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+def test_best_intermediate_matches_get_best_k(cuda_device):
+    """The per-level best leaf recorded on the device equals the host
+    get_best_k of every level's tree."""
+    d, prn = _run("prune_taylor", cuda_device)
+    prn.initialize(int(d["ref_seg"]))
+    want = []
+    for _ in range(int(d["levels_done"])):
+        prn.execute_iter()
+        if prn.prune_complete:
+            break
+        want.append(prn.world_tree.get_best_k(prn.intermediate_k))
+    arr = prn.best_intermediate_arr
+    for lvl, (leaves, scores) in enumerate(want):
+        np.testing.assert_array_equal(arr[lvl]["param_sets"], leaves)
+        np.testing.assert_array_equal(arr[lvl]["scores"], scores)
