@@ -184,6 +184,8 @@ def bench_prune_gpu(args, dev) -> dict:
     achieved = score_leaves * PRUNE_SCORE_BYTES_PER_LEAF / (score_ms * 1e-3) / 1e9
     survivors = int(prn.world_tree.valid_size)
     best = float(prn.world_tree.scores.max().item()) if survivors else float("nan")
+    # children per parent of every level of the plain run (threshold design input)
+    bpat = [max(1, int(round(st.n_leaves / max(st.n_branches, 1)))) for st in prn.pstats[1:]]
 
     # end to end: pinned host series -> FFA -> pruning run -> results on the host
     from pyloki_gb300.timeseries import TimeSeries as TS
@@ -249,6 +251,7 @@ def bench_prune_gpu(args, dev) -> dict:
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches,
         "survivors": survivors, "best_score": best,
+        "branching_pattern": bpat,
     }
 
 
@@ -517,9 +520,40 @@ def bench_gpu(args) -> dict | None:
             out["prune"]["cpu_baseline"] = prune_cpu()
         if not args.no_learned:
             out["prune"]["learned"] = bench_learned(args, dev)
+        if not args.no_thresholds:
+            out["threshold_design"] = bench_thresholds(args, dev,
+                                                       out["prune"]["branching_pattern"])
     if dist is not None:
         dist.destroy_process_group()
     return out
+
+
+def bench_thresholds(args, dev, branching_pattern) -> dict:
+    """Dynamic threshold-scheme design for the pruning workload's branching
+    pattern, with the design parameters of the reference's threshold notebook:
+    100 thresholds, 30 probability bins, 1024 trials per fold set, S/N 10,
+    beam 2.5, improved mode, 11 neighbours."""
+    import torch
+
+    from pyloki_gb300.thresholds import DynamicThresholdScheme
+
+    bp = np.asarray(branching_pattern, np.float64)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    ds = DynamicThresholdScheme(bp, 0.1, 64, ntrials=1024, nprobs=30, prob_min=0.05,
+                                snr_final=10.0, nthresholds=100, ducy_max=0.3, wtsp=1.5,
+                                beam_width=2.5, mode="improved", seed=1, device=dev)
+    ds.run(thres_neigh=11)
+    torch.cuda.synchronize(dev)
+    dt = time.perf_counter() - t0
+    path = ds.best_path()
+    return {"metric": "threshold design seconds", "value": dt, "unit": "s",
+            "higher_is_better": False, "stages": len(bp), "nthresholds": 100, "nprobs": 30,
+            "ntrials": 1024, "mode": "improved", "simulate_launches": ds.sim.launches,
+            "final_states": int((~ds.states[-1]["is_empty"]).sum()),
+            "best_path_stages": len(path),
+            "note": "the reference's notebook reports 121.5 s for a 127-stage design with "
+                    "these parameters on its CPU (numba)"}
 
 
 def bench_learned(args, dev) -> dict:
@@ -832,6 +866,8 @@ def main() -> None:
                     help="skip the batched multi-series measurement")
     ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
                     help="series of the seeded 256-series batch to search")
+    ap.add_argument("--no-thresholds", action="store_true",
+                    help="skip the threshold-scheme design measurement")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned branch proposal study")
     ap.add_argument("--learned-train", type=int, default=16)

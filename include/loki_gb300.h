@@ -527,6 +527,24 @@ int loki_snr_score_batch(const float* folds, int64_t n, int32_t nbins,
 int loki_fold_norm(const float* folds, int64_t n, int32_t nbins, float* out,
                    void* stream);
 
+/* ---- threshold-scheme design (Monte-Carlo folds) ------------------------ */
+
+/* simulate_folds + fold_max_scores (detection/thresholding.py:46-96, 484-500)
+ * for nrows rows at once: folds_out[r] = folds_in[src_row[r]] (zeros when
+ * folds_in is NULL) + bias[r] * profile + N(0, noise_std^2) per bin, from a
+ * Philox-4x32-10 stream keyed by seed and (r, bin); scores[r] = max over the
+ * spec's widths of the boxcar S/N of folds_out[r] / sqrt_var (float32
+ * division, as prune_folds normalises, thresholding.py:99-135). spec->mode
+ * must be 1. */
+int loki_sim_score_folds(const float* folds_in, const int64_t* src_row, const float* bias,
+                         int64_t nrows, const float* profile, int32_t nbins, float noise_std,
+                         float sqrt_var, uint64_t seed, const LokiScoreSpec* spec,
+                         float* folds_out, float* scores, void* stream);
+
+/* dst[i] = src[idx[i]] for n rows of row_len float32 (survivor compaction). */
+int loki_gather_rows(const float* src, const int64_t* idx, int64_t n, int64_t row_len,
+                     float* dst, void* stream);
+
 /* ---- learned branch proposal (tensor cores) ----------------------------
  * A 16 -> 128 -> 128 -> 1 MLP (ReLU) scoring per-branch statistics of the
  * pruning tree. No reference counterpart: the reference has no learned

@@ -189,6 +189,9 @@ SIGNATURES: dict[str, tuple] = {
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_f32_to_bf16": (C.c_int, [_P, _I64, _P, _P]),
+    "loki_sim_score_folds": (C.c_int, [_P, _P, _P, _I64, _P, _I32, C.c_float, C.c_float,
+                                       C.c_uint64, C.POINTER(LokiScoreSpec), _P, _P, _P]),
+    "loki_gather_rows": (C.c_int, [_P, _P, _I64, _I64, _P, _P]),
     "loki_mlp_smem_bytes": (C.c_int64, []),
     "loki_branch_features": (C.c_int, [_P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float,
                                        C.c_float, _P, _P, _P]),
