@@ -183,6 +183,38 @@ class FoldSim:
             o += c
         return folds, host
 
+    def run_bank(self, bank: torch.Tensor, offs: np.ndarray, cnts: np.ndarray,
+                 biases: np.ndarray, var_add: float, var_next: float, *,
+                 host_scores: bool = True) -> tuple[torch.Tensor, object, np.ndarray,
+                                                    np.ndarray]:
+        """``run`` for sets given as row ranges [offs, offs + cnts) of one bank:
+        returns the simulated rows, their scores (host, or the device tensor
+        with ``host_scores=False``) and each set's output offsets and counts."""
+        cnts = np.asarray(cnts, np.int64)
+        if np.any(cnts <= 0):
+            msg = "No trials in the input folds"
+            raise ValueError(msg)
+        n_sim = cnts * np.ceil(self.ntrials / cnts).astype(np.int64)
+        out_off = np.concatenate([[0], np.cumsum(n_sim)[:-1]]).astype(np.int64)
+        total = int(n_sim.sum())
+        set_of_row = np.repeat(np.arange(len(cnts)), n_sim)
+        local = np.arange(total, dtype=np.int64) - out_off[set_of_row]
+        src_row = np.asarray(offs, np.int64)[set_of_row] + local % cnts[set_of_row]
+        bias = np.asarray(biases, np.float32)[set_of_row]
+        dev = self.device
+        src_d = torch.from_numpy(src_row).to(dev)
+        bias_d = torch.from_numpy(bias).to(dev)
+        out = torch.empty((total, self.nbins), dtype=torch.float32, device=dev)
+        scores = torch.empty(total, dtype=torch.float32, device=dev)
+        seed = (self.seed * 0x9E3779B97F4A7C15 + self.calls) & 0xFFFFFFFFFFFFFFFF
+        self.calls += 1
+        _lib.check(self._lib.loki_sim_score_folds(
+            _lib.ptr(bank), _lib.ptr(src_d), _lib.ptr(bias_d), total, _lib.ptr(self.profile),
+            self.nbins, float(np.sqrt(var_add)), float(np.sqrt(np.float32(var_next))),
+            C.c_uint64(seed), self.spec, _lib.ptr(out), _lib.ptr(scores), self._stream()))
+        self.launches += 1
+        return out, (scores.cpu().numpy() if host_scores else scores), out_off, n_sim
+
     def take(self, folds: torch.Tensor, idx: np.ndarray) -> torch.Tensor:
         """Rows ``idx`` of ``folds`` (survivor compaction, one launch)."""
         n = len(idx)
@@ -301,8 +333,13 @@ class DynamicThresholdScheme:
         empty["threshold"] = -1.0
         empty["threshold_prev"] = -1.0
         self.states = np.full((self.nstages, self.nthresholds, self.nprobs), empty)
-        self.guess_path = np.minimum(bound_scheme(self.nstages, self.snr_final),
-                                     trials_scheme(self.branching_pattern, trials_start=1))
+        # A cumulative branching of 1 gives trials_scheme = isf(1) = -inf, whose
+        # beam (guess +- beam_width) holds no threshold and ends the design at
+        # that stage; the guess is held at the lowest threshold instead.
+        self.guess_path = np.maximum(
+            np.minimum(bound_scheme(self.nstages, self.snr_final),
+                       trials_scheme(self.branching_pattern, trials_start=1)),
+            self.thresholds[0])
         self.sim = FoldSim(self.profile, ntrials, ducy_max, wtsp, seed=seed, device=device)
         self.folds_in: dict[tuple[int, int], _FoldState] = {}
         self._init_stage0()
@@ -376,61 +413,131 @@ class DynamicThresholdScheme:
         self.folds_in = self._materialise(pending)
 
     def run(self, thres_neigh: int = 11) -> None:
-        """Fill every stage after the first (``thresholding.py:904-963``)."""
+        """Fill every stage after the first (``thresholding.py:904-963``).
+
+        Each stage simulates all its fold sets in one launch, evaluates every
+        (threshold, neighbour, probability bin) transition at once from the
+        sorted scores, keeps per (threshold, bin) the first transition of least
+        cumulative complexity in the reference's loop order, and compacts the
+        winners' survivors with one gather."""
         for istage in range(1, self.nstages):
-            beam_cur = self.get_current_thresholds_idx(istage)
-            beam_prev = self.get_current_thresholds_idx(istage - 1)
-            prev_states = self.states[istage - 1]
-            # the fold sets this stage draws from, simulated in one launch
-            keys = []
-            for j in beam_prev:
+            self._stage(istage, thres_neigh)
+
+    def _bank_of(self) -> tuple[torch.Tensor, dict]:
+        """The current fold states as one bank and (h0, h1) row ranges."""
+        keys = sorted(self.folds_in)
+        parts, ranges, o = [], {}, 0
+        for key in keys:
+            fs = self.folds_in[key]
+            if fs.is_empty:
+                continue
+            parts += [fs.h0, fs.h1]
+            ranges[key] = (o, fs.h0.shape[0], o + fs.h0.shape[0], fs.h1.shape[0])
+            o += fs.h0.shape[0] + fs.h1.shape[0]
+        bank = torch.cat(parts).contiguous() if parts else None
+        return bank, ranges
+
+    def _stage(self, istage: int, thres_neigh: int) -> None:
+        beam_cur = self.get_current_thresholds_idx(istage)
+        beam_prev = self.get_current_thresholds_idx(istage - 1)
+        prev = self.states[istage - 1]
+        bank, ranges = self._bank_of()
+        keys = [(int(j), k) for j in beam_prev for k in range(self.nprobs)
+                if not prev[j, k]["is_empty"] and (int(j), k) in ranges]
+        if not keys:
+            self.folds_in = {}
+            return
+        kidx = {key: n for n, key in enumerate(keys)}
+        # candidates in the reference's loop order: ithres, neighbour j, kprob
+        c_thr, c_key = [], []
+        for ithres in beam_cur:
+            for j in neighbouring_indices(beam_prev, int(ithres), thres_neigh):
                 for k in range(self.nprobs):
-                    fs = self.folds_in.get((int(j), k))
-                    if not prev_states[j, k]["is_empty"] and fs is not None and not fs.is_empty:
-                        keys.append((int(j), k))
-            sims: dict = {}
-            if self.mode == "improved":
-                sets = [s for key in keys for s in ((self.folds_in[key].h0, 0.0),
-                                                    (self.folds_in[key].h1, self.bias_snr))]
-                if sets:
-                    var = self.folds_in[keys[0]].variance
-                    folds, scores = self.sim.run(sets, 1.0, var + 1.0)
-                    for n, key in enumerate(keys):
-                        sims[key] = _FoldState(folds[2 * n], folds[2 * n + 1], var + 1.0,
-                                               scores[2 * n], scores[2 * n + 1])
-            else:  # legacy: one simulation per (ithres, neighbour, kprob) transition
-                trans = [(int(i), key) for i in beam_cur
-                         for j in neighbouring_indices(beam_prev, int(i), thres_neigh)
-                         for key in keys if key[0] == int(j)]
-                sets = [s for _, key in trans for s in ((self.folds_in[key].h0, 0.0),
-                                                        (self.folds_in[key].h1, self.bias_snr))]
-                if sets:
-                    var = self.folds_in[keys[0]].variance
-                    folds, scores = self.sim.run(sets, 1.0, var + 1.0)
-                    for n, tk in enumerate(trans):
-                        sims[tk] = _FoldState(folds[2 * n], folds[2 * n + 1], var + 1.0,
-                                              scores[2 * n], scores[2 * n + 1])
-            pending = {}
-            keyset = set(keys)
-            for ithres in beam_cur:
-                for j in neighbouring_indices(beam_prev, int(ithres), thres_neigh):
-                    for k in range(self.nprobs):
-                        key = (int(j), k)
-                        if key not in keyset:
-                            continue
-                        sim_state = sims[key] if self.mode == "improved" else sims[
-                            (int(ithres), key)]
-                        cur, fold = self._transition(prev_states[j, k], sim_state,
-                                                     float(self.thresholds[ithres]),
-                                                     float(self.branching_pattern[istage]))
-                        iprob = self._iprob(cur)
-                        if iprob < 0 or iprob >= self.nprobs:
-                            continue
-                        ex = self.states[istage, ithres, iprob]
-                        if ex["is_empty"] or cur["complexity_cumul"] < ex["complexity_cumul"]:
-                            self.states[istage, ithres, iprob] = cur
-                            pending[(int(ithres), iprob)] = fold
-            self.folds_in = self._materialise(pending)
+                    n = kidx.get((int(j), k))
+                    if n is not None:
+                        c_thr.append(int(ithres))
+                        c_key.append(n)
+        if not c_thr:
+            self.folds_in = {}
+            return
+        c_thr = np.asarray(c_thr, np.int64)
+        c_key = np.asarray(c_key, np.int64)
+        # one simulation per key (improved) or per candidate (legacy)
+        c_sim = c_key if self.mode == "improved" else np.arange(len(c_thr))
+        sim_key = np.arange(len(keys)) if self.mode == "improved" else c_key
+        offs, cnts, biases = [], [], []
+        for n in sim_key:
+            o0, n0, o1, n1 = ranges[keys[int(n)]]
+            offs += [o0, o1]
+            cnts += [n0, n1]
+            biases += [0.0, self.bias_snr]
+        var = self.folds_in[keys[0]].variance
+        out, scores_d, out_off, n_sim = self.sim.run_bank(bank, np.array(offs), np.array(cnts),
+                                                          np.array(biases), 1.0, var + 1.0,
+                                                          host_scores=False)
+        dev = self.sim.device
+        # scores as a padded (set, row) matrix on the device (-inf pads)
+        maxlen = int(n_sim.max())
+        col = torch.arange(maxlen, device=dev)
+        off_d = torch.from_numpy(out_off).to(dev)
+        nsim_d = torch.from_numpy(n_sim).to(dev)
+        valid = col[None, :] < nsim_d[:, None]
+        pos = (off_d[:, None] + col[None, :]).clamp_max(scores_d.numel() - 1)
+        smat = torch.where(valid, scores_d[pos], torch.full((), float("-inf"), device=dev))
+        # survival of every candidate at its threshold, H0 and H1
+        thr_c = self.thresholds[c_thr]
+        thr_d = torch.from_numpy(thr_c.astype(np.float32)).to(dev)
+        sets = torch.from_numpy(np.stack([2 * c_sim, 2 * c_sim + 1])).to(dev)  # (2, ncand)
+        above = (smat[sets] > thr_d[None, :, None]).sum(dim=2)
+        succ = (above.double() / nsim_d[sets].double()).cpu().numpy()
+        # next states (get_next_state, vectorised; float32 fields as stored)
+        pj = np.array([keys[int(n)] for n in c_key])
+        pst = prev[pj[:, 0], pj[:, 1]]
+        nbr = float(self.branching_pattern[istage])
+        nleaves_next = pst["complexity"].astype(np.float64) * nbr
+        cc64 = pst["complexity_cumul"].astype(np.float64) + nleaves_next
+        sh64 = pst["success_h1_cumul"].astype(np.float64) * succ[1]
+        cc = cc64.astype(np.float32)
+        sh1c = sh64.astype(np.float32)
+        iprob = np.digitize(sh1c, self.probs) - 1
+        ok = np.flatnonzero((iprob >= 0) & (iprob < self.nprobs))
+        # per (ithres, iprob): the first candidate (loop order) of least complexity
+        grp = c_thr[ok] * self.nprobs + iprob[ok]
+        srt = np.lexsort((ok, cc[ok], grp))
+        first = np.unique(grp[srt], return_index=True)[1]
+        winners = ok[srt[first]]
+        if not len(winners):
+            self.folds_in = {}
+            return
+        st = np.zeros(len(winners), dtype=state_dtype)
+        st["success_h0"], st["success_h1"] = succ[0, winners], succ[1, winners]
+        st["complexity"] = nleaves_next[winners] * succ[0, winners]
+        st["complexity_cumul"] = cc[winners]
+        st["success_h1_cumul"] = sh1c[winners]
+        st["nbranches"] = nbr
+        st["threshold"] = thr_c[winners]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            st["cost"] = cc64[winners] / sh64[winners]
+        st["threshold_prev"] = pst["threshold"][winners]
+        st["success_h1_cumul_prev"] = pst["success_h1_cumul"][winners]
+        st["is_empty"] = False
+        self.states[istage, c_thr[winners], iprob[winners]] = st
+        # survivors of the winners, H0 then H1 each, compacted in one gather
+        wsets = torch.from_numpy(np.stack([2 * c_sim[winners], 2 * c_sim[winners] + 1],
+                                          axis=1).reshape(-1)).to(dev)
+        wthr = torch.from_numpy(np.repeat(thr_c[winners].astype(np.float32), 2)).to(dev)
+        keep = smat[wsets] > wthr[:, None]
+        counts = keep.sum(dim=1).cpu().numpy()
+        r, cidx = torch.nonzero(keep, as_tuple=True)
+        rows = off_d[wsets[r]] + cidx
+        newbank = out[rows]
+        starts = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        self.folds_in = {}
+        for n, w in enumerate(winners):
+            o0, n0 = int(starts[2 * n]), int(counts[2 * n])
+            o1, n1 = int(starts[2 * n + 1]), int(counts[2 * n + 1])
+            self.folds_in[(int(c_thr[w]), int(iprob[w]))] = _FoldState(
+                newbank[o0:o0 + n0], newbank[o1:o1 + n1], var + 1.0)
 
     def best_path(self) -> np.ndarray:
         """Thresholds of the least-cost final state, traced back stage by stage

@@ -127,3 +127,16 @@ def test_dynamic_scheme_designs_a_path(cuda_device, mode, tmp_path):
     path = ds.best_path()
     assert 1 <= len(path) <= ds.nstages
     assert ds.save(str(tmp_path)).endswith(".npz")
+
+
+def test_dynamic_scheme_with_unit_first_branching(cuda_device):
+    """A pattern that starts with no branching (cumulative trials 1) still
+    designs a path: the guess is held at the lowest threshold."""
+    from pyloki_gb300.thresholds import DynamicThresholdScheme
+
+    bp = np.array([1.0, 1.0, 3.0, 1.0, 2.0, 3.0])
+    ds = DynamicThresholdScheme(bp, 0.1, ntrials=512, nprobs=5, nthresholds=30, snr_final=6.0,
+                                beam_width=1.0, mode="improved", seed=4, device=cuda_device)
+    ds.run(thres_neigh=5)
+    assert (~ds.states[-1]["is_empty"]).any()
+    assert 1 <= len(ds.best_path()) <= len(bp)
