@@ -369,19 +369,60 @@ prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     my_row = (int64_t)r.ia * D.n_freq + r.iff;
     my_shift = round_shift(r.phase, nb);
   }
-  for (int k = 0; k < kmax; ++k) {
-    const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
-    const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
-    const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
-    const float* pf = folds + par * 2 * nb;
-    const float* sf = seg + row * 2 * nb;
-    float* trow = tile + k * stride;
-    for (int j = lane; j < nb; j += 32) {
-      int js = j - sh;
-      js += (js < 0) ? nb : 0;
-      const float e = __fadd_rn(pf[j], sf[js]);
-      const float v = __fadd_rn(pf[nb + j], sf[nb + js]);
-      trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
+  if (nb == 64) {
+    // eight children's rows in flight per lane (bins lane and lane + 32)
+    constexpr int kU = 8;
+    for (int k0 = 0; k0 < kmax; k0 += kU) {
+      float pe[kU][2], pw[kU][2], se[kU][2], sw[kU][2];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + u;
+        const int src = k < kmax ? k : 0;
+        const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, src);
+        const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, src);
+        const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, src);
+        if (k < kmax) {
+          const float* pf = folds + par * 128;
+          const float* sf = seg + row * 128;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const int j = lane + 32 * c;
+            const int js = (j - sh) & 63;
+            pe[u][c] = __ldg(pf + j);
+            pw[u][c] = __ldg(pf + 64 + j);
+            se[u][c] = __ldg(sf + js);
+            sw[u][c] = __ldg(sf + 64 + js);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + u;
+        if (k >= kmax) break;
+        float* trow = tile + k * stride;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const float e = __fadd_rn(pe[u][c], se[u][c]);
+          const float v = __fadd_rn(pw[u][c], sw[u][c]);
+          trow[lane + 32 * c] = __fdiv_rn(e, __fsqrt_rn(v));
+        }
+      }
+    }
+  } else {
+    for (int k = 0; k < kmax; ++k) {
+      const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
+      const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
+      const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
+      const float* pf = folds + par * 2 * nb;
+      const float* sf = seg + row * 2 * nb;
+      float* trow = tile + k * stride;
+      for (int j = lane; j < nb; j += 32) {
+        int js = j - sh;
+        js += (js < 0) ? nb : 0;
+        const float e = __fadd_rn(pf[j], sf[js]);
+        const float v = __fadd_rn(pf[nb + j], sf[nb + js]);
+        trow[j] = __fdiv_rn(e, __fsqrt_rn(v));
+      }
     }
   }
   __syncwarp();
@@ -664,6 +705,46 @@ prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
     my_par = par;
     my_row = (int64_t)ia * D.n_freq + iff;
     my_shift = round_shift(cphase[c], nb);
+  }
+  if (nb == 64) {
+    // four survivors' rows in flight per lane (bins lane and lane + 32)
+    constexpr int kU = 4;
+    for (int k0 = 0; k0 < kmax; k0 += kU) {
+      float pe[kU][2], pw[kU][2], se[kU][2], sw[kU][2];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + u;
+        const int src = k < kmax ? k : 0;
+        const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, src);
+        const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, src);
+        const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, src);
+        if (k < kmax) {
+          const float* pf = folds + par * 128;
+          const float* sf = seg + row * 128;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const int j = lane + 32 * c;
+            const int js = (j - sh) & 63;
+            pe[u][c] = __ldg(pf + j);
+            pw[u][c] = __ldg(pf + 64 + j);
+            se[u][c] = __ldg(sf + js);
+            sw[u][c] = __ldg(sf + 64 + js);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int k = k0 + u;
+        if (k >= kmax) break;
+        float* o = fout + (s0 + k) * 128;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          o[lane + 32 * c] = __fadd_rn(pe[u][c], se[u][c]);
+          o[64 + lane + 32 * c] = __fadd_rn(pw[u][c], sw[u][c]);
+        }
+      }
+    }
+    return;
   }
   for (int k = 0; k < kmax; ++k) {
     const int64_t par = __shfl_sync(0xFFFFFFFFu, my_par, k);
