@@ -374,6 +374,13 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
         return rows
 
     budgets = [int(b) for b in (budget if np.ndim(budget) else [budget])]
+    # untimed warm-up of both paths (first launches of the MLP, feature and
+    # selection kernels) on a series outside the evaluation
+    warm = make_series(int(train_seeds[0]), True)
+    dw = dyp_of(warm)
+    _prune_run(lambda _t: dw, warm, cfg, thresholds, ref, None, dev, max_sugg, batch_size)
+    _prune_run(lambda _t: dw, warm, cfg, thresholds, ref, BranchProposal(net, min(budgets)),
+               dev, max_sugg, batch_size)
     inj = compare(test_seeds, True, budgets)
     noise = compare(noise_seeds, False, budgets)
     rows = inj + noise
