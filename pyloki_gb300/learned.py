@@ -6,7 +6,7 @@ The network maps 16 per-branch statistics of the pruning tree to the logit
 of "this branch still has a descendant above threshold some levels later".
 ``Pruning`` can use it to order the parents of a level and, when a level
 exceeds its budget, to expand the most promising parents first; the exact
-per-level threshold still judges every emitted leaf, and without a model (or
+per-level threshold still decides every emitted leaf, and without a model (or
 within budget) pruning is the plain algorithm. The reference has no learned
 part; nothing here changes results unless a budget is set.
 """
@@ -254,12 +254,15 @@ class Recorder:
 
 class BranchProposal:
     """Parent hook: when a level has more than ``budget`` parents, expand the
-    ``budget`` ones the network ranks most likely to survive (ties at the cut
-    are all kept); below the budget the level is the plain algorithm."""
+    ones the network ranks most likely to survive (ties at the cut are all
+    kept); below the budget the level is the plain algorithm. With
+    ``score_share`` > 0 that share of the budget goes to the highest-scoring
+    parents whatever the network says, so strong paths are never dropped."""
 
-    def __init__(self, net: BranchMLP, budget: int) -> None:
+    def __init__(self, net: BranchMLP, budget: int, score_share: float = 0.0) -> None:
         self.net = net
         self.budget = int(budget)
+        self.score_share = float(score_share)
         self.levels_cut = 0
 
     def __call__(self, prn, tree, level: int):
@@ -267,9 +270,14 @@ class BranchProposal:
         if n <= self.budget:
             return None
         z = self.net.logits(parent_features(prn, tree, level))
-        kth = torch.topk(z, self.budget, sorted=False).values.min()
+        k_score = int(self.budget * self.score_share)
+        k_net = self.budget - k_score
+        keep = z >= torch.topk(z, k_net, sorted=False).values.min()
+        if k_score:
+            s = torch.nan_to_num(tree.scores, nan=float("-inf"))
+            keep |= s >= torch.topk(s, k_score, sorted=False).values.min()
         self.levels_cut += 1
-        return (z >= kth).to(torch.uint8)
+        return keep.to(torch.uint8)
 
 
 def _prune_run(dyp_of, ts, cfg, thresholds, ref, hook, device, max_sugg, batch_size):
@@ -297,7 +305,7 @@ def _prune_run(dyp_of, ts, cfg, thresholds, ref, hook, device, max_sugg, batch_s
 
 def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
           budget, lookahead: int = 16, top_k: int | None = 64, per_level: int = 2048,
-          epochs: int = 6,
+          epochs: int = 6, score_share: float = 0.0,
           det_snr: float = 8.0, max_sugg: int = 2**18, batch_size: int = 1024,
           device=None, seed: int = 0) -> dict:
     """Train the branch-survival network on statistics of plain pruning runs
@@ -362,7 +370,7 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
             row = {"seed": int(sd), "plain_best": b0, "plain_leaves": int(l0), "plain_ms": ms0,
                    "learned": {}}
             for bud in budgets:
-                prop = BranchProposal(net, bud)
+                prop = BranchProposal(net, bud, score_share)
                 p1, l1, ms1 = _prune_run(lambda _t: d, ts, cfg, thresholds, ref, prop, dev,
                                          max_sugg, batch_size)
                 b1 = (float(p1.world_tree.scores.max()) if p1.world_tree.valid_size
@@ -379,8 +387,8 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
     warm = make_series(int(train_seeds[0]), True)
     dw = dyp_of(warm)
     _prune_run(lambda _t: dw, warm, cfg, thresholds, ref, None, dev, max_sugg, batch_size)
-    _prune_run(lambda _t: dw, warm, cfg, thresholds, ref, BranchProposal(net, min(budgets)),
-               dev, max_sugg, batch_size)
+    _prune_run(lambda _t: dw, warm, cfg, thresholds, ref,
+               BranchProposal(net, min(budgets), score_share), dev, max_sugg, batch_size)
     inj = compare(test_seeds, True, budgets)
     noise = compare(noise_seeds, False, budgets)
     rows = inj + noise
@@ -404,7 +412,7 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
         "positive_fraction": pos, "label": (f"ancestor of the final top {top_k}"
                                             if top_k else f"alive {lookahead} levels later"),
         "epochs": epochs, "loss_per_epoch": hist, "train_accuracy": train_acc,
-        "record_s": rec_s, "fit_s": fit_s, "det_snr": det_snr,
+        "record_s": rec_s, "fit_s": fit_s, "det_snr": det_snr, "score_share": score_share,
         "false_alarm_plain": float(np.mean([r["plain_best"] >= det_snr for r in noise]))
         if noise else None,
         "plain_leaves_per_s": l0 / (ms0 * 1e-3),
