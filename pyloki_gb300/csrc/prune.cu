@@ -272,6 +272,8 @@ __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__
       perr[k] = lf[2 * k + 1];
     }
   }
+  // Halving is exact, so x / 2 is computed as x * 0.5 (the same rounded
+  // value as the reference's division).
   LokiBranchInfo B;
   B.d0 = pval[P];
   int64_t total = 1;
@@ -293,8 +295,8 @@ __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__
         num = D.branch_max;
       }
       dact = __ddiv_rn(dcur, (double)num);
-      const double pmin = __dsub_rn(pcur, __ddiv_rn(dcur, 2.0));
-      first = __dadd_rn(pmin, __ddiv_rn(dact, 2.0));
+      const double pmin = __dsub_rn(pcur, __dmul_rn(dcur, 0.5));
+      first = __dadd_rn(pmin, __dmul_rn(dact, 0.5));
     }
     if (shift < D.eta_m) {
       num = 1;
@@ -871,6 +873,42 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
       my_shift = round_shift(ph, nb);
     }
     const float* fseg = ffa + (int64_t)seg_idx[sg] * seg_stride;
+    if (nb == 64) {
+      // eight survivors' segment rows in flight per lane (bins lane, lane + 32)
+      constexpr int kU = 8;
+      for (int k0 = 0; k0 < kmax; k0 += kU) {
+        float se[kU][2], sw[kU][2];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int k = k0 + u;
+          const int src = k < kmax ? k : 0;
+          const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, src);
+          const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, src);
+          if (k < kmax) {
+            const float* sf = fseg + row * 128;
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+              const int js = (lane + 32 * c - sh) & 63;
+              se[u][c] = __ldg(sf + js);
+              sw[u][c] = __ldg(sf + 64 + js);
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int k = k0 + u;
+          if (k >= kmax) break;
+          float* a = acc + k * 128;
+#pragma unroll
+          for (int c = 0; c < 2; ++c) {
+            const int j = lane + 32 * c;
+            a[j] = __fadd_rn(a[j], se[u][c]);
+            a[64 + j] = __fadd_rn(a[64 + j], sw[u][c]);
+          }
+        }
+      }
+      continue;
+    }
     for (int k = 0; k < kmax; ++k) {
       const int64_t row = __shfl_sync(0xFFFFFFFFu, my_row, k);
       const int sh = __shfl_sync(0xFFFFFFFFu, my_shift, k);
@@ -946,8 +984,8 @@ __device__ __forceinline__ void circ_child(const LokiBranchInfo& B, const double
   ev[P] = 0.0;
   if (ch.crackle >= 0) {  // branch_param_padded on the parent crackle cell
     const double dact = B.dact[0];
-    const double first = __dadd_rn(__dsub_rn(lf[0], __ddiv_rn(lf[1], 2.0)),
-                                   __ddiv_rn(dact, 2.0));
+    const double first = __dadd_rn(__dsub_rn(lf[0], __dmul_rn(lf[1], 0.5)),
+                                   __dmul_rn(dact, 0.5));
     pv[0] = __dadd_rn(first, __dmul_rn((double)ch.crackle, dact));
   }
 }
@@ -989,7 +1027,7 @@ __global__ void circ_branch_kernel(LokiPruneLevel D, const double* __restrict__ 
         num = D.branch_max;
       }
       dact = __ddiv_rn(dcur, (double)num);
-      first = __dadd_rn(__dsub_rn(pcur, __ddiv_rn(dcur, 2.0)), __ddiv_rn(dact, 2.0));
+      first = __dadd_rn(__dsub_rn(pcur, __dmul_rn(dcur, 0.5)), __dmul_rn(dact, 0.5));
     }
     if (j == 0) {  // crackle keeps the parent value; its step is the would-be child step
       needs0 = needs;
