@@ -425,6 +425,27 @@ int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* leaves, const 
                          double* leaves_out, float* folds_out, float* scores_out,
                          float* scores_ep_out, int32_t* bt_out, void* stream);
 
+/* loki_prune_circ_score / loki_prune_circ_emit over complex folds
+ * (PruneCircTaylorComplexDPFuncts, dynamic/dyn_circular_taylor.py:168-330):
+ * tree folds and segment rows are (2, nbins / 2 + 1) complex64; the children's
+ * folds are the phasor-rotated segment row plus the parent fold
+ * (core/common.py:403-429), scored through their irfft
+ * (detection/scoring.py:285-292). nbins must be even. */
+int loki_prune_circ_score_complex(
+    const LokiPruneLevel* lvl, const double* leaves, const void* folds, int64_t n_parents,
+    int64_t batch_size, const LokiBranchInfo* info, const void* child_map,
+    const int64_t* keep_off, const int64_t* exp_off, const int64_t* valid_ids, int64_t n_valid,
+    const void* fold_segment, const LokiScoreSpec* spec, float* child_scores,
+    int32_t* child_idx, double* child_phase, int8_t* child_class, int32_t* batch_taylor,
+    int64_t* batch_offsets, float* score_minmax, int32_t* dev_err, void* stream);
+int loki_prune_circ_emit_complex(
+    const LokiPruneLevel* lvl, const double* leaves, const void* folds, int64_t batch_size,
+    const LokiBranchInfo* info, const void* child_map, const int64_t* valid_ids,
+    const void* fold_segment, const int64_t* surv_ids, int64_t n_surv,
+    const float* child_scores, const int32_t* child_idx, const double* child_phase,
+    const int8_t* child_class, const int32_t* batch_taylor, double* leaves_out,
+    void* folds_out, float* scores_out, float* scores_ep_out, int32_t* bt_out, void* stream);
+
 /* loki_prune_branch restricted to the parents with parent_mask[i] != 0
  * (device uint8): the others get no children (their offsets repeat), so the
  * score, select and emit calls of the level skip them while backtracks keep

@@ -235,6 +235,11 @@ SIGNATURES: dict[str, tuple] = {
                                         _P, _P]),
     "loki_prune_circ_emit": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P,
                                        _P, _P, _P, _P, _P, _P, _P, _P]),
+    "loki_prune_circ_score_complex": (C.c_int, [_PL, _P, _P, _I64, _I64, _P, _P, _P, _P, _P,
+                                                _I64, _P, C.POINTER(LokiScoreSpec), _P, _P, _P,
+                                                _P, _P, _P, _P, _P, _P]),
+    "loki_prune_circ_emit_complex": (C.c_int, [_PL, _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P,
+                                               _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
 }
 
 #: bytes of one circular-tree child record (parent, cartesian index, crackle index, pad)

@@ -1532,9 +1532,14 @@ prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   const int64_t r = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
   if (r >= n) return;
   const double* lf = leaves + r * (P + 2) * 2;
-  double pv[LOKI_MAX_PARAMS + 1];
-  for (int i = 0; i < m; ++i) pv[i] = lf[2 * i];
+  double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
+  for (int i = 0; i < m; ++i) {
+    pv[i] = lf[2 * i];
+    ev[i] = lf[2 * i + 1];
+  }
   const double f0 = lf[2 * m];
+  // circular tree: class of the survivor (core/circular.py:597-666)
+  const int cls = D.basis == 2 ? circ_class(pv, ev, D.circ_sig_prop) : 0;
   for (int k = 0; k < 2 * nbf; ++k) comb[k] = make_float2(0.0f, 0.0f);
   for (int sg = 0; sg < nseg; ++sg) {
     const double(*T)[LOKI_MAX_PARAMS + 1] =
@@ -1544,6 +1549,12 @@ prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
       double a[LOKI_MAX_PARAMS + 1];
       for (int i = 0; i < m; ++i) a[i] = tdot(pv, T, i, m);
       cheby_low3(D, a, m, &accel, &vel, &dd);
+    } else if (cls != 0) {  // circular survivors: closed-form propagation
+      double a[6];
+      circ_shift(pv, dt_seg[sg], cls == 2, a);
+      accel = a[3];
+      vel = a[4];
+      dd = a[5];
     } else {
       accel = tdot(pv, T, P - 2, m);
       vel = tdot(pv, T, P - 1, m);
@@ -1574,6 +1585,133 @@ prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   float s;
   score_row(trow, nb, sp, &s);
   scores[r] = s;
+}
+
+// ---------------------------------------------------------------------------
+// circular-orbit tree over complex folds (PruneCircTaylorComplexDPFuncts,
+// dynamic/dyn_circular_taylor.py:168-330): the circular branch, validation,
+// resolve and transform of the real-fold circular kernels, with the complex
+// shift-add (core/common.py:403-429) and irfft scoring
+// (detection/scoring.py:285-292) of the complex Taylor kernels.
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                          const float2* __restrict__ folds, int64_t batch,
+                          const LokiBranchInfo* __restrict__ info,
+                          const CircChild* __restrict__ map,
+                          const int64_t* __restrict__ valid_ids, int64_t n_valid,
+                          const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                          float* __restrict__ scores, int32_t* __restrict__ cidx,
+                          double* __restrict__ cphase, int8_t* __restrict__ ccls,
+                          int32_t* __restrict__ batch_taylor,
+                          unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1, P = 5;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t v = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (v >= n_valid) return;
+  const CircChild ch = map[valid_ids[v]];
+  const LokiBranchInfo B = info[ch.parent];
+  const double* lf = leaves + (int64_t)ch.parent * (P + 2) * 2;
+  double pv[6], ev[6];
+  circ_child(B, lf, ch, pv, ev);
+  ChildRes r;
+  const int cls = circ_resolve(D, pv, ev, lf[(P + 1) * 2], &r);
+  if (cls == 0) atomicOr(batch_taylor + ch.parent / batch, 1);
+  cidx[2 * v] = r.ia;
+  cidx[2 * v + 1] = r.iff;
+  cphase[v] = r.phase;
+  ccls[v] = (int8_t)cls;
+  const int64_t row = (int64_t)r.ia * D.n_freq + r.iff;
+  rotate_add(seg + row * 2 * nbf, folds + (int64_t)ch.parent * 2 * nbf,
+             prune_phasor(r.phase, nb), nbf, comb);
+  float* trow = tile + lane * stride;
+  irfft_norm(comb, nb, nbf, tw, trow);
+  float s;
+  score_row(trow, nb, sp, &s);
+  scores[v] = s;
+  if (s == s) {
+    atomicMin(minmax_keys, float_key(s));
+    atomicMax(minmax_keys + 1, float_key(s));
+  }
+}
+
+// Survivors of the complex circular tree: leaves, basis flag and backtracks as
+// circ_emit_kernel, the fold written as the complex sum.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                         const float2* __restrict__ folds, int64_t batch,
+                         const LokiBranchInfo* __restrict__ info,
+                         const CircChild* __restrict__ map,
+                         const int64_t* __restrict__ valid_ids, const float2* __restrict__ seg,
+                         const int64_t* __restrict__ surv, int64_t n_surv,
+                         const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
+                         const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
+                         const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
+                         float2* __restrict__ fout, float* __restrict__ sout,
+                         float* __restrict__ seout, int32_t* __restrict__ bout) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n_surv) return;
+  const int nb = D.nbins, nbf = nb / 2 + 1, P = 5, m = 6;
+  const int64_t v = surv[s];
+  const CircChild ch = map[valid_ids[v]];
+  const LokiBranchInfo B = info[ch.parent];
+  const double* lf = leaves + (int64_t)ch.parent * (P + 2) * 2;
+  double pv[6], ev[6];
+  circ_child(B, lf, ch, pv, ev);
+  const int cls = ccls[v];
+  double* lo = lout + s * (P + 2) * 2;
+  double flag = lf[2 * m + 1];
+  if (D.moving) {
+    if (cls == 1) flag = 1.0;
+    else if (cls == 2) flag = batch_taylor[ch.parent / batch] ? 0.0 : 2.0;
+    if (cls != 0) {
+      double o[6];
+      circ_shift(pv, D.circ_dt_next, cls == 2, o);
+      for (int i = 0; i < m; ++i) {
+        lo[2 * i] = o[i];
+        lo[2 * i + 1] = ev[i];
+      }
+    } else {
+      for (int i = 0; i < m; ++i) lo[2 * i] = tdot(pv, D.tm_n, i, m);
+      if (D.tiling == 0) {
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dmul_rn(ev[i], fabs(D.tm_n[i][i]));
+      } else if (D.tiling == 2) {
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = tdot(ev, D.tm_e, i, m);
+      } else {
+        double e2[6];
+        for (int j = 0; j < m; ++j) e2[j] = __dmul_rn(ev[j], ev[j]);
+        for (int i = 0; i < m; ++i) lo[2 * i + 1] = __dsqrt_rn(tdot(e2, D.tm_e, i, m));
+      }
+    }
+  } else {
+    for (int i = 0; i < m; ++i) {
+      lo[2 * i] = pv[i];
+      lo[2 * i + 1] = ev[i];
+    }
+  }
+  lo[2 * m] = lf[2 * m];
+  lo[2 * m + 1] = flag;
+  sout[s] = cscores[v];
+  seout[s] = cscores[v];
+  int32_t* bt = bout + s * (P + 2);
+  const int ia = cidx[2 * v], iff = cidx[2 * v + 1];
+  bt[0] = ch.parent;
+  for (int j = 1; j < P + 1; ++j) bt[j] = 0;
+  bt[D.nparams_ffa - 1] = ia;
+  bt[D.nparams_ffa] = iff;
+  bt[P + 1] = (int32_t)cphase[v];
+  const int64_t row = (int64_t)ia * D.n_freq + iff;
+  rotate_add(seg + row * 2 * nbf, folds + (int64_t)ch.parent * 2 * nbf,
+             prune_phasor(cphase[v], nb), nbf, fout + s * 2 * nbf);
 }
 
 // ---------------------------------------------------------------------------
@@ -1997,6 +2135,87 @@ extern "C" int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* lea
   return check_launch("prune_circ_emit");
 }
 
+static int cplx_smem(const LokiPruneLevel* lvl, const LokiScoreSpec& sp, int* smem);
+
+extern "C" int loki_prune_circ_score_complex(
+    const LokiPruneLevel* lvl, const double* leaves, const void* folds, int64_t n_parents,
+    int64_t batch_size, const LokiBranchInfo* info, const void* child_map,
+    const int64_t* keep_off, const int64_t* exp_off, const int64_t* valid_ids, int64_t n_valid,
+    const void* fold_segment, const LokiScoreSpec* spec, float* child_scores,
+    int32_t* child_idx, double* child_phase, int8_t* child_class, int32_t* batch_taylor,
+    int64_t* batch_offsets, float* score_minmax, int32_t* dev_err, void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (batch_size < 1 || n_parents < 0 || n_valid < 0)
+    return set_error(LOKI_ERR_INVALID, "bad circular score arguments");
+  if (!score_minmax || !dev_err || !batch_taylor || !batch_offsets || !keep_off || !exp_off)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nbatch = (n_parents + batch_size - 1) / batch_size;
+  if (nbatch > 0 && cudaMemsetAsync(batch_taylor, 0, nbatch * sizeof(int32_t), s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
+  unsigned* keys = reinterpret_cast<unsigned*>(score_minmax);
+  note_launch();
+  minmax_init_kernel<<<1, 1, 0, s>>>(keys);
+  if (n_valid > 0) {
+    if (!leaves || !folds || !info || !child_map || !valid_ids || !fold_segment ||
+        !child_scores || !child_idx || !child_phase || !child_class)
+      return set_error(LOKI_ERR_INVALID, "null pointer argument");
+    LokiScoreSpec sp = *spec;
+    sp.mode = 1;
+    const ScoreK SK = make_score_k(sp, lvl->nbins);
+    int smem = 0;
+    rc = cplx_smem(lvl, sp, &smem);
+    if (rc) return rc;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(circ_score_complex_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+      return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+    const int64_t blocks = (n_valid + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+    if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
+    note_launch();
+    circ_score_complex_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
+        *lvl, leaves, static_cast<const float2*>(folds), batch_size, info,
+        reinterpret_cast<const CircChild*>(child_map), valid_ids, n_valid,
+        static_cast<const float2*>(fold_segment), sp, SK, child_scores, child_idx,
+        child_phase, child_class, batch_taylor, keys);
+  }
+  note_launch();
+  minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
+  note_launch();
+  circ_boff_kernel<<<(unsigned)((n_parents + 1 + 255) / 256), 256, 0, s>>>(
+      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets);
+  return check_launch("prune_circ_score_complex");
+}
+
+extern "C" int loki_prune_circ_emit_complex(
+    const LokiPruneLevel* lvl, const double* leaves, const void* folds, int64_t batch_size,
+    const LokiBranchInfo* info, const void* child_map, const int64_t* valid_ids,
+    const void* fold_segment, const int64_t* surv_ids, int64_t n_surv,
+    const float* child_scores, const int32_t* child_idx, const double* child_phase,
+    const int8_t* child_class, const int32_t* batch_taylor, double* leaves_out,
+    void* folds_out, float* scores_out, float* scores_ep_out, int32_t* bt_out, void* stream) {
+  int rc = check_circ(lvl);
+  if (rc) return rc;
+  if (lvl->nbins % 2) return set_error(LOKI_ERR_INVALID, "complex folds need an even nbins");
+  if (n_surv <= 0) return LOKI_OK;
+  if (batch_size < 1) return set_error(LOKI_ERR_INVALID, "bad batch size");
+  if (!leaves || !folds || !info || !child_map || !valid_ids || !fold_segment || !surv_ids ||
+      !child_scores || !child_idx || !child_phase || !child_class || !batch_taylor ||
+      !leaves_out || !folds_out || !scores_out || !scores_ep_out || !bt_out)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  circ_emit_complex_kernel<<<(unsigned)((n_surv + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      *lvl, leaves, static_cast<const float2*>(folds), batch_size, info,
+      reinterpret_cast<const CircChild*>(child_map), valid_ids,
+      static_cast<const float2*>(fold_segment), surv_ids, n_surv, child_scores, child_idx,
+      child_phase, child_class, batch_taylor, leaves_out, static_cast<float2*>(folds_out),
+      scores_out, scores_ep_out, bt_out);
+  return check_launch("prune_circ_emit_complex");
+}
+
 // ---- complex (Fourier) folds -----------------------------------------------
 
 static int cplx_smem(const LokiPruneLevel* lvl, const LokiScoreSpec& sp, int* smem) {
@@ -2092,8 +2311,6 @@ extern "C" int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double
   if (nseg < 1 || !leaves || !folds || !scores || !scores_ep || !tm_seg || !dt_seg ||
       !seg_idx || !ffa_fold || !dev_err)
     return set_error(LOKI_ERR_INVALID, "bad ascend arguments");
-  if (lvl->basis == 2)
-    return set_error(LOKI_ERR_UNSUPPORTED, "complex folds of the circular tree");
   LokiScoreSpec sp = *spec;
   sp.mode = 1;
   const ScoreK SK = make_score_k(sp, lvl->nbins);

@@ -213,9 +213,6 @@ class Pruning:
                        (False, "chebyshev", True), (False, "chebyshev", False)}:
             msg = f"Invalid pruning configuration: {key}"
             raise ValueError(msg)
-        if key == (True, "taylor", True):
-            msg = "the circular-orbit tree over complex (Fourier) folds is not built yet"
-            raise NotImplementedError(msg)
         self.poly_basis = poly_basis
         #: folds are complex (Fourier domain): (n, 2, nbins / 2 + 1) complex64
         self.fourier = bool(cfg.use_fourier)
@@ -807,7 +804,9 @@ class Pruning:
         btay = self._buf.get("btay", max(nbatch, 1), torch.int32)
         boff = self._buf.get("boff", n_par + 1, torch.int64)
         minmax = self._buf.get("minmax", 2, torch.float32)
-        _lib.check(lib.loki_prune_circ_score(
+        circ_score = (lib.loki_prune_circ_score_complex if self.fourier
+                      else lib.loki_prune_circ_score)
+        _lib.check(circ_score(
             d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), n_par, bs, _lib.ptr(info),
             _lib.ptr(cmap), _lib.ptr(keep), _lib.ptr(expd), _lib.ptr(valid), n_valid,
             _lib.ptr(fold_segment), self.spec, _lib.ptr(scores), _lib.ptr(cidx),
@@ -826,12 +825,14 @@ class Pruning:
                                            n_surv_d, batch_size=bs)
         nb = self.dyp.cfg.nbins
         dev = self._device
+        fold_shape = (n_surv, 2, nb // 2 + 1) if self.fourier else (n_surv, 2, nb)
         new = WorldTree(torch.empty((n_surv, P + 2, 2), dtype=torch.float64, device=dev),
-                        torch.empty((n_surv, 2, nb), dtype=torch.float32, device=dev),
+                        torch.empty(fold_shape, dtype=tree.folds.dtype, device=dev),
                         torch.empty(n_surv, dtype=torch.float32, device=dev),
                         torch.empty((n_surv, P + 2), dtype=torch.int32, device=dev),
                         torch.empty(n_surv, dtype=torch.float32, device=dev))
-        _lib.check(lib.loki_prune_circ_emit(
+        circ_emit = lib.loki_prune_circ_emit_complex if self.fourier else lib.loki_prune_circ_emit
+        _lib.check(circ_emit(
             d, _lib.ptr(tree.leaves), _lib.ptr(tree.folds), bs, _lib.ptr(info), _lib.ptr(cmap),
             _lib.ptr(valid), _lib.ptr(fold_segment), _lib.ptr(surv), n_surv, _lib.ptr(scores),
             _lib.ptr(cidx), _lib.ptr(cphase), _lib.ptr(ccls), _lib.ptr(btay),

@@ -333,6 +333,9 @@ def main() -> None:
     if "--fourier-prune-only" in sys.argv:
         fourier_prune_cases()
         return
+    if "--circ-fourier-only" in sys.argv:
+        circ_fourier_cases()
+        return
     if "--prune-only" in sys.argv:
         prune_cases()
         cheby_cases()
@@ -353,6 +356,10 @@ def fourier_cases() -> None:
 def fourier_prune_cases() -> None:
     prune_case("prune_taylor_fourier", fourier=True, fold_levels=(5, 11))
     prune_case("prune_cheby_fourier", fourier=True, basis="chebyshev", fold_levels=())
+
+
+def circ_fourier_cases() -> None:
+    prune_case("prune_circ_fourier", circular=True, fourier=True, fold_levels=(8,))
 
 
 def circ_cases() -> None:
