@@ -779,7 +779,7 @@ def bench_reference(args) -> dict | None:
         dt, nt = run_cpu_oracle(cfg_b, ts_b)
         times.append(dt)
     value = nt / (sum(times) / len(times))
-    return {
+    out = {
         "metric": METRIC, "value": value, "unit": "trials/s", "impl": "reference",
         "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
