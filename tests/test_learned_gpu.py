@@ -106,3 +106,41 @@ def test_study_runs_end_to_end(cuda_device):
     assert 0.0 <= b["recall_vs_plain"] <= 1.0
     assert res["plain_leaves_per_s"] > 0 and b["learned_leaves_per_s"] > 0
     assert b["leaves_fraction"] <= 1.0
+
+
+def test_trained_network_beats_untrained_at_equal_budget(cuda_device):
+    """What training buys: at the same parent budget, a network trained on
+    plain runs keeps more of the plain run's best final leaves (held-out
+    injections) than the same network before training."""
+    from pyloki_gb300.learned import BranchMLP, BranchProposal, Recorder
+
+    cfg = _cfg()
+    xs, ys = [], []
+    for sd in (41, 42, 43, 44, 45, 46):
+        rec = Recorder(per_level=1024, seed=sd)
+        prn, _ = _run(cfg, _series(sd), rec, cuda_device)
+        x, y = rec.labels(prn, lookahead=4, top_k=16)
+        xs.append(x)
+        ys.append(y)
+    x, y = torch.cat(xs), torch.cat(ys)
+    pos = float(y.mean())
+    wt = torch.where(y > 0.5, 0.5 / pos, 0.5 / (1 - pos))
+    trained = BranchMLP(device=cuda_device, seed=5)
+    trained.fit(x, y, wt, epochs=6, batch=4096, lr=2e-3)
+    untrained = BranchMLP(device=cuda_device, seed=5)
+
+    def recovered(net, sd, budget):
+        plain, _ = _run(cfg, _series(sd), None, cuda_device)
+        wt0 = plain.world_tree
+        top = torch.topk(wt0.scores, min(16, wt0.valid_size)).indices
+        want = {r.tobytes() for r in wt0.leaves[top].cpu().numpy()}
+        got, _ = _run(cfg, _series(sd), BranchProposal(net, budget), cuda_device)
+        have = {r.tobytes() for r in got.world_tree.leaves.cpu().numpy()}
+        return len(want & have) / max(len(want), 1)
+
+    plain, _ = _run(cfg, _series(61), None, cuda_device)
+    budget = max(64, int(np.median([s.n_branches for s in plain.pstats[1:]])) // 4)
+    rec_t = [recovered(trained, sd, budget) for sd in (61, 62, 63, 64)]
+    rec_u = [recovered(untrained, sd, budget) for sd in (61, 62, 63, 64)]
+    print(f"budget {budget}: recovered top-16 trained {rec_t} untrained {rec_u}")
+    assert np.mean(rec_t) > np.mean(rec_u), (rec_t, rec_u)
