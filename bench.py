@@ -857,7 +857,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--band-bytes", type=int, default=96 << 20)
+    ap.add_argument("--band-bytes", type=int, default=1 << 30)
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bf16", action="store_true",

@@ -86,7 +86,7 @@ class Tuner:
     """
 
     def __init__(self, path: str | os.PathLike | None = None,
-                 band_choices: Sequence[int] = (32 << 20, 96 << 20, 256 << 20)) -> None:
+                 band_choices: Sequence[int] = (128 << 20, 384 << 20, 1 << 30)) -> None:
         self.path = path
         self.band_choices = tuple(band_choices)
         self.table: dict[str, dict] = {}
@@ -247,7 +247,7 @@ class BatchedSearch:
     def __init__(self, series: Sequence[TimeSeries],
                  cfg_for: Callable[[int], PulsarSearchConfig], *, device=None, k: int = 16,
                  storage: str = "f32", rescore: bool = False, use_graphs: bool = True,
-                 tuner: Tuner | None = None, chunk: int = 8, band_bytes: int = 96 << 20,
+                 tuner: Tuner | None = None, chunk: int = 8, band_bytes: int = 1 << 30,
                  mem_fraction: float = 0.5) -> None:
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
@@ -367,7 +367,7 @@ class BatchedSearch:
 
 def sequential_search(series: Sequence[TimeSeries],
                       cfg_for: Callable[[int], PulsarSearchConfig], *, device=None,
-                      k: int = 16, band_bytes: int = 96 << 20) -> list[Candidates]:
+                      k: int = 16, band_bytes: int = 1 << 30) -> list[Candidates]:
     """The plain path: one ``DynamicProgramming.search`` per series, FP32,
     eager launches (the reference's one-series-per-call structure)."""
     dev = torch.device(device) if device is not None else torch.device(

@@ -421,7 +421,7 @@ class DynamicProgramming:
         return 2 if self._storage else 4
 
     def search(self, widths=None, stdnoise: float = 1.0, *, mode: int = 0,
-               banded: bool | None = None, band_bytes: int = 96 << 20,
+               banded: bool | None = None, band_bytes: int = 1 << 30,
                phase_events: list | None = None, check: bool = True) -> torch.Tensor:
         """S/N of every final-level parameter set (segment 0 of each series),
         never writing the final fold. Returns ``(*counts_final, nwidths)`` (or

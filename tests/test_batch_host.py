@@ -52,7 +52,8 @@ def test_tuner_picks_fastest_within_budget_and_persists(tmp_path):
         return chunk * per * (0.9 if band == 32 << 20 else 1.0)
 
     path = tmp_path / "tune.json"
-    t = Tuner(path)
+    bands = (32 << 20, 96 << 20, 256 << 20)
+    t = Tuner(path, band_choices=bands)
     dev = torch.device("cpu")
     big = _peak_bytes(cfg, 16, 256 << 20, 4)
     res = t.tune(cfg, "f32", dev, 16, big, time_fn)
@@ -60,11 +61,11 @@ def test_tuner_picks_fastest_within_budget_and_persists(tmp_path):
     assert (16, 96 << 20) not in calls  # stopped once chunks got slower
     # a second tuner reads the file instead of timing again
     calls.clear()
-    res2 = Tuner(path).tune(cfg, "f32", dev, 16, big, time_fn)
+    res2 = Tuner(path, band_choices=bands).tune(cfg, "f32", dev, 16, big, time_fn)
     assert calls == [] and (res2.chunk, res2.band_bytes) == (4, 32 << 20)
     # a memory budget below two series limits the chunk to one
     small = _peak_bytes(cfg, 1, 256 << 20, 2)
-    res3 = Tuner().tune(cfg, "bf16", dev, 16, small, time_fn)
+    res3 = Tuner(band_choices=bands).tune(cfg, "bf16", dev, 16, small, time_fn)
     assert res3.chunk == 1
     with pytest.raises(MemoryError):
-        Tuner().tune(cfg, "f32", dev, 4, 1024, time_fn)
+        Tuner(band_choices=bands).tune(cfg, "f32", dev, 4, 1024, time_fn)
