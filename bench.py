@@ -514,6 +514,8 @@ def bench_gpu(args) -> dict | None:
                                      ms_per_step)
     if not args.no_batch:
         out["batch"] = bench_batch(args, dev)
+    if not args.no_injections:
+        out["injection"] = bench_injections(args, dev, peak)
     if not args.no_prune:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
@@ -526,6 +528,97 @@ def bench_gpu(args) -> dict | None:
     if dist is not None:
         dist.destroy_process_group()
     return out
+
+
+INJ_NSAMPS = 2**21
+
+
+def injection_cfgs(n: int, seed: int = 4000):
+    """Seeded injection set: periods 2-50 ms, S/N 8-30, duty cycles 0.02-0.3,
+    accelerations +-50 m/s^2 and jerks +-0.1 m/s^3 (Taylor modulation), 2^21
+    samples of 64 us; shapes and pulse phases per injection."""
+    from pyloki_gb300.pulse import PulseSignalConfig
+
+    rng = np.random.default_rng(seed)
+    cfgs = [PulseSignalConfig(period=float(p), dt=64e-6, nsamps=INJ_NSAMPS, snr=float(s),
+                              ducy=float(d), mod_kwargs={"acc": float(a), "jerk": float(j)})
+            for p, s, d, a, j in zip(rng.uniform(2e-3, 5e-2, n), rng.uniform(8, 30, n),
+                                     rng.uniform(0.02, 0.3, n), rng.uniform(-50, 50, n),
+                                     rng.uniform(-0.1, 0.1, n))]
+    shapes = [("gaussian", "von_mises", "boxcar")[i % 3] for i in range(n)]
+    return cfgs, shapes, rng.uniform(0, 1, n)
+
+
+def bench_injections(args, dev, peak: float) -> dict:
+    """Synthetic injection set on the device (PulseSignalConfig.generate for
+    every injection): proper time, template, noise and calibration folds in
+    one pass (which also stores noise and template in the output arrays), the
+    calibration, and the in-place scaling to the float32 series, kept in HBM. Device time per
+    kernel phase from CUDA events; wall time of the public call (host
+    preparation of the CDF tables included). CPU baseline: the numpy port on
+    two injections of the same set."""
+    import torch
+
+    from oracle import pulse_oracle as PO
+    from pyloki_gb300 import _lib
+    from pyloki_gb300.pulse import _Batch, generate_injections
+
+    n = args.injections
+    cfgs, shapes, phis = injection_cfgs(n)
+    ts_e = torch.empty((n, INJ_NSAMPS), dtype=torch.float32, device=dev)
+    ts_v = torch.empty_like(ts_e)
+    generate_injections(cfgs[:8], shapes[:8], phis[:8], seed=1, device=dev)  # warm-up
+    stream = torch.cuda.current_stream(dev)
+    times = {}
+    for rep in range(2):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        batch = _Batch(cfgs, shapes, phis, 1, dev)
+        t_prep = time.perf_counter() - t0
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        before = _lib.load().loki_launch_count()
+        ev[0].record(stream)
+        folds = batch.fold(None, keep=(ts_e, ts_v))
+        ev[1].record(stream)
+        scales = batch.calibrate(folds, 5, 1e-2)
+        ev[2].record(stream)
+        batch.apply(scales, ts_e, ts_v)
+        ev[3].record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        launches = _lib.load().loki_launch_count() - before
+        times = {"fold_ms": ev[0].elapsed_time(ev[1]), "calibrate_ms": ev[1].elapsed_time(ev[2]),
+                 "apply_ms": ev[2].elapsed_time(ev[3]), "device_ms": ev[0].elapsed_time(ev[3]),
+                 "host_prep_ms": t_prep * 1e3, "wall_ms": wall * 1e3, "launches": launches}
+    samples = n * INJ_NSAMPS
+    meas = scales[:, 3].cpu().numpy()
+    # apply: noise and template read, ts_e and ts_v written, 4 bytes each
+    apply_bytes = 16 * samples
+    apply_gbs = apply_bytes / (times["apply_ms"] * 1e-3) / 1e9
+    # CPU: the numpy port of generate() on two injections of the set
+    rng = np.random.default_rng(9)
+    t0 = time.perf_counter()
+    for i in range(2):
+        c = cfgs[i]
+        noise = rng.standard_normal(INJ_NSAMPS, dtype=np.float32)
+        PO.generate(c.period, c.dt, c.nsamps, c.snr, c.ducy, noise, shape=shapes[i],
+                    phi0=float(phis[i]), kind="derivative", params=c.mod_kwargs,
+                    exact_folds=True)
+    cpu_per = (time.perf_counter() - t0) / 2
+    return {"metric": "injections/s", "value": n / (times["wall_ms"] * 1e-3),
+            "unit": "injections/s", "device_injections_per_s": n / (times["device_ms"] * 1e-3),
+            "samples_per_s_device": samples / (times["device_ms"] * 1e-3),
+            "injections": n, "nsamps": INJ_NSAMPS, **times,
+            "calibrated_snr_abs_err_median": float(np.median(np.abs(
+                meas - np.array([c.snr for c in cfgs])))),
+            "roofline_apply": {"bound": "hbm", "achieved": apply_gbs, "peak": peak,
+                               "unit": "GB/s", "frac": apply_gbs / peak,
+                               "algorithmic_bytes": apply_bytes},
+            "fold_samples_per_s": samples / (times["fold_ms"] * 1e-3),
+            "cpu_baseline": {"value": 1.0 / cpu_per, "unit": "injections/s", "cores": 1,
+                             "kind": "port",
+                             "sample": "numpy port of generate() on 2 injections of the set"},
+            "workload": f"{n} injections x 2^21 samples (Taylor modulation, three shapes)"}
 
 
 def bench_thresholds(args, dev, branching_pattern) -> dict:
@@ -866,6 +959,10 @@ def main() -> None:
                     help="skip the batched multi-series measurement")
     ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
                     help="series of the seeded 256-series batch to search")
+    ap.add_argument("--no-injections", action="store_true",
+                    help="skip the synthetic injection-set section")
+    ap.add_argument("--injections", type=int, default=1024,
+                    help="injections of 2^21 samples in the injection-set section")
     ap.add_argument("--no-thresholds", action="store_true",
                     help="skip the threshold-scheme design measurement")
     ap.add_argument("--no-learned", action="store_true",

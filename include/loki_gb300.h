@@ -623,6 +623,89 @@ int loki_branch_features(const float* scores, const float* folds, int64_t n, int
 int loki_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
                   float beta1, float beta2, float eps, int64_t step, void* stream);
 
+/* ---- synthetic pulsar series (injection generator) -----------------------
+ * PulseSignalConfig.generate (simulation/pulse.py:310-406) for many
+ * injections at once: proper time of a modulation model
+ * (simulation/modulate.py), a CDF-lookup pulse template
+ * (generate_pulse_template, pulse.py:38-68), white noise, the calibration
+ * folds at the pulse period and the S/N calibration on those folds
+ * (calibrate_scale_on_folds, pulse.py:71-118). */
+#define LOKI_MOD_MAX_COEFFS 16
+#define LOKI_MOD_DERIVATIVE 0  /* c = shift, vel, acc, jerk, snap (m / s^k) */
+#define LOKI_MOD_SERIES 1      /* c[k] = d^(k) / k! for k < ncoeff */
+#define LOKI_MOD_CIRCULAR 2    /* c = x_orb (lt-s), omega (rad/s), psi (rad) */
+#define LOKI_MOD_CIRCULAR_T0 3 /* c = a, omega (rad/s), phi (rad) */
+#define LOKI_MOD_KEPLERIAN 4   /* c = p_orb, |ecc|, phi, a (1-ecc^2), aop, sin(inc),
+                                  sqrt((1+ecc)/(1-ecc)), 1 / p_orb */
+#define LOKI_MOD_TABLE 5       /* proper times read from a device table */
+#define LOKI_PULSE_MAX_NBINS 12288 /* calibration fold bins (shared-memory bound) */
+
+typedef struct {
+  int32_t kind;   /* LOKI_MOD_* */
+  int32_t ncoeff; /* used terms of c (LOKI_MOD_SERIES) */
+  double t_ref;   /* reference epoch (s) */
+  double c[LOKI_MOD_MAX_COEFFS];
+} LokiModulation;
+
+/* One injection. Sample i is at t = i * dt; its proper time comes from mod
+ * (or pt_table[inj * nsamps + i] for LOKI_MOD_TABLE). */
+typedef struct {
+  double dt;        /* sample spacing (s) */
+  double period;    /* pulse period (s) */
+  double snr;       /* target folded S/N */
+  double ducy;      /* duty cycle (on-pulse window of the calibration) */
+  double phi0;      /* pulse phase */
+  int32_t nbins;    /* calibration fold bins, int(period / dt) */
+  int32_t ngrid;    /* CDF table intervals; the table holds ngrid + 1 values */
+  int64_t lut_off;  /* offset of this injection's CDF table in luts */
+  uint64_t seed;    /* noise stream */
+  LokiModulation mod;
+} LokiPulseSpec;
+
+/* specs: device array of ninj LokiPulseSpec. luts: float32 CDF tables.
+ * pt_table: float64 (ninj, nsamps) proper times, or NULL when no spec is
+ * LOKI_MOD_TABLE. noise: float32 (ninj, nsamps) standard normals, or NULL to
+ * draw them from each spec's seed (Philox-4x32-10, Box-Muller). */
+
+/* Template (ninj, nsamps) float32 and, if proper_time is not NULL, the
+ * proper times (ninj, nsamps) float64. */
+int loki_pulse_template(const LokiPulseSpec* specs, int32_t ninj, int64_t nsamps,
+                        const float* luts, const double* pt_table, float* tmpl,
+                        double* proper_time, void* stream);
+
+/* Calibration folds (ninj, 3, fold_stride) float64, overwritten by the call:
+ * [0] sum of noise, [1] samples per bin (unit variance), [2] sum of template,
+ * binned by get_phase_idx_int (utils/psr_utils.py:50-56) at 1 / period.
+ * Sums are exact in 2^-32 fixed point (independent of summation order;
+ * caller noise must stay below 2^20 in magnitude). noise_out and tmpl_out
+ * (both or neither, (ninj, nsamps) float32) receive the unit noise and the
+ * template for loki_pulse_apply. */
+int loki_pulse_fold(const LokiPulseSpec* specs, int32_t ninj, int64_t nsamps,
+                    const float* luts, const double* pt_table, const float* noise,
+                    double* folds, int32_t fold_stride, float* noise_out, float* tmpl_out,
+                    void* stream);
+
+/* Noise scale and calibrated signal scale per injection from the folds
+ * (ninj, 3, fold_stride) float64, rounded to float32 as the reference holds them:
+ * out (ninj, 4) float64 = noise_scale, signal scale, template S/N, last
+ * measured S/N. Stops when |S/N - snr| < tol or after max_iter steps. */
+int loki_pulse_calibrate(const LokiPulseSpec* specs, int32_t ninj, const double* folds,
+                         int32_t fold_stride, int32_t max_iter, double tol, double* out,
+                         void* stream);
+
+/* In place on the noise_out / tmpl_out arrays of loki_pulse_fold:
+ * ts_e = noise_scale * noise + scale * template, ts_v = noise_scale^2
+ * (float32 arithmetic, as pulse.py:402-405), scales from loki_pulse_calibrate. */
+int loki_pulse_apply(const double* scales, int32_t ninj, int64_t nsamps, float* ts_e,
+                     float* ts_v, void* stream);
+
+/* The same series as fold + calibrate + apply, regenerating noise and
+ * template instead of reading them back (no (ninj, nsamps) buffers needed
+ * before the scales are known). */
+int loki_pulse_emit(const LokiPulseSpec* specs, int32_t ninj, int64_t nsamps,
+                    const float* luts, const double* pt_table, const float* noise,
+                    const double* scales, float* ts_e, float* ts_v, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

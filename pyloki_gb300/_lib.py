@@ -168,6 +168,24 @@ class LokiMLPGrad(C.Structure):
                 ("loss", C.c_void_p)]
 
 
+MOD_MAX_COEFFS = 16
+PULSE_MAX_NBINS = 12288
+MOD_KINDS = {"derivative": 0, "derivative_series": 1, "circular": 2, "circular_t0": 3,
+             "keplerian": 4, "table": 5}
+
+
+class LokiModulation(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ncoeff", C.c_int32), ("t_ref", C.c_double),
+                ("c", C.c_double * MOD_MAX_COEFFS)]
+
+
+class LokiPulseSpec(C.Structure):
+    _fields_ = [("dt", C.c_double), ("period", C.c_double), ("snr", C.c_double),
+                ("ducy", C.c_double), ("phi0", C.c_double), ("nbins", C.c_int32),
+                ("ngrid", C.c_int32), ("lut_off", C.c_int64), ("seed", C.c_uint64),
+                ("mod", LokiModulation)]
+
+
 SIGNATURES: dict[str, tuple] = {
     "loki_version": (C.c_int, []),
     "loki_last_error": (C.c_char_p, []),
@@ -192,6 +210,11 @@ SIGNATURES: dict[str, tuple] = {
     "loki_sim_score_folds": (C.c_int, [_P, _P, _P, _I64, _P, _I32, C.c_float, C.c_float,
                                        C.c_uint64, C.POINTER(LokiScoreSpec), _P, _P, _P]),
     "loki_gather_rows": (C.c_int, [_P, _P, _I64, _I64, _P, _P]),
+    "loki_pulse_template": (C.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P]),
+    "loki_pulse_fold": (C.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _I32, _P, _P, _P]),
+    "loki_pulse_apply": (C.c_int, [_P, _I32, _I64, _P, _P, _P]),
+    "loki_pulse_calibrate": (C.c_int, [_P, _I32, _P, _I32, _I32, _D, _P, _P]),
+    "loki_pulse_emit": (C.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P, _P, _P]),
     "loki_mlp_smem_bytes": (C.c_int64, []),
     "loki_branch_features": (C.c_int, [_P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float,
                                        C.c_float, _P, _P, _P]),

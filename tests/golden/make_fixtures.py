@@ -1,4 +1,5 @@
-"""Generate the golden FFA / scoring fixtures by running the pyloki reference.
+"""Generate the golden FFA / scoring / pruning / generator fixtures by running
+the pyloki reference.
 
 Run in a container where the pyloki source tree is available (it is not on the
 GPU test machines, which only read the committed ``.npz`` files):
@@ -264,13 +265,91 @@ def prune_case(name: str, *, tiling: str = "aggressive", moving: bool = True,
     print(name, "levels", prn.prune_level, "survivors", v)
 
 
+PULSE_CASES = [
+    # name, mod_type, mod_kwargs, period, snr, ducy, shape, phi0, seed
+    ("taylor", "derivative", {"acc": 30.0, "jerk": 0.1}, 5.2e-3, 20.0, 0.08, "gaussian", 0.4, 3),
+    ("circular", "circular", {"p_orb": 3600.0, "x_orb": 0.5, "psi": 0.3}, 5.2e-3, 20.0, 0.08,
+     "gaussian", 0.4, 4),
+    ("vonmises", "derivative", {"acc": -5.0}, 7.7e-3, 15.0, 0.2, "von_mises", 0.5, 5),
+    ("boxcar", "derivative", {}, 3.3e-3, 25.0, 0.1, "boxcar", 0.25, 6),
+    ("keplerian", "keplerian", {"p_orb": 5000.0, "ecc": 0.3, "phi": 0.7, "a": 3.0e8,
+                                "om": 1.1, "inc": 1.2}, 5.2e-3, 20.0, 0.08, "gaussian", 0.5, 7),
+    ("series", "derivative_series", {"coeffs": [0.0, 0.0, 20.0, 0.05, 1e-4]}, 4.1e-3, 18.0,
+     0.06, "gaussian", 0.6, 8),
+    ("circular_t0", "circular_t0", {"a": 1.0e8, "p_orb": 4000.0, "t0": 50.0}, 6.0e-3, 22.0, 0.1,
+     "gaussian", 0.3, 9),
+]
+
+
+def pulse_case(name: str, kind: str, params: dict, period: float, snr: float, ducy: float,
+               shape: str, phi0: float, seed: int, n: int = 4096, dt: float = 64e-6) -> None:
+    """PulseSignalConfig.generate with a seeded generator, and the pieces it
+    computes on the way (template, folds, scales)."""
+    from pyloki.core import brutefold
+    from pyloki.detection.scoring import boxcar_snr_1d
+    from pyloki.simulation import pulse as P
+
+    cfg = P.PulseSignalConfig(period=period, dt=dt, nsamps=n, snr=snr, ducy=ducy,
+                              mod_type=kind, mod_kwargs=dict(params))
+    orig = np.random.default_rng
+    np.random.default_rng = lambda *a, **k: orig(seed)
+    try:
+        ts = cfg.generate(shape=shape, phi0=phi0)
+    finally:
+        np.random.default_rng = orig
+    noise = orig(seed).standard_normal(size=n, dtype=np.float32)
+    pt = cfg.proper_time
+    lut = P.build_cdf_lut(shape, ducy, phi0, ngrid=max(4096, int(100 / ducy)))
+    tmpl = P.generate_pulse_template(pt, dt, period, lut)
+    nbins = cfg.fold_bins_ideal
+    unit = np.ones(n, np.float32)
+    fn = brutefold(noise, unit, pt, 1.0 / period, 1, nbins).squeeze()
+    ft = brutefold(tmpl, unit, pt, 1.0 / period, 1, nbins).squeeze()
+    center = round(phi0 * nbins) % nbins
+    width = max(1, round(ducy * nbins))
+    off = np.ones(nbins, dtype=bool)
+    off[(center - width // 2 + np.arange(width)) % nbins] = False
+    ns = 1.0 / np.std(fn[0][off])
+    var_s = fn[1] * ns**2
+    snr_t = np.max(boxcar_snr_1d(ft[0] / np.sqrt(var_s), np.arange(1, nbins // 2), 1))
+    init = (snr / snr_t) * ns
+    scale = P.calibrate_scale_on_folds((fn[0] * ns).astype(np.float32),
+                                       var_s.astype(np.float32), ft[0].astype(np.float32),
+                                       snr, init, 5, 1e-2, damping=0.8)
+    final = (ns * noise + scale * tmpl).astype(np.float32)
+    assert np.array_equal(final, ts.ts_e), name
+    pnames = sorted(params)
+    pvals = [np.atleast_1d(np.asarray(params[k], np.float64)) for k in pnames]
+    np.savez_compressed(
+        HERE / f"pulse_{name}.npz", kind=np.array(kind), shape=np.array(shape),
+        param_names=np.array(pnames), param_sizes=np.array([len(v) for v in pvals]),
+        param_values=np.concatenate(pvals) if pvals else np.zeros(0),
+        period=np.float64(period), dt=np.float64(dt), nsamps=np.int64(n), snr=np.float64(snr),
+        ducy=np.float64(ducy), phi0=np.float64(phi0), t_ref=np.float64(cfg.mod_tref),
+        nbins=np.int64(nbins), noise=noise, proper_time=pt, lut=lut, template=tmpl,
+        folds=np.stack([fn[0], fn[1], ft[0]]).astype(np.float32), noise_scale=np.float64(ns),
+        initial_scale=np.float64(init), scale=np.float64(scale),
+        snr_template=np.float64(snr_t), ts_e=ts.ts_e, ts_v=ts.ts_v)
+
+
+def pulse_cases() -> None:
+    for case in PULSE_CASES:
+        pulse_case(*case)
+
+
 def main() -> None:
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     ref_src = args[0] if args else "/root/reference/src"
     sys.path.insert(0, str(HERE))
     import refshim
 
-    refshim.install(ref_src)
+    # The generator fixtures need numba's scalar typing of the calibration
+    # (float64 scale inside calibrate_scale_on_folds); the others were made
+    # without it.
+    refshim.install(ref_src, cast_signatures="--pulse-only" in sys.argv)
+    if "--pulse-only" in sys.argv:
+        pulse_cases()
+        return
     # numba types `float32_array >= float64` as a float64 comparison. Under
     # plain numpy 2 the overflow threshold that world_tree derives with
     # math.nextafter is a Python float, i.e. a weak scalar, so numpy would

@@ -20,9 +20,59 @@ import types as _t
 import numpy as np
 
 
+# Inside compiled numba code scalars have strong types (float32 * float64 is
+# float64), so arguments become numpy scalars; results are boxed into Python
+# scalars on return, as numba returns them.
+_ARG_CASTS = {"f8": np.float64, "float64": np.float64, "f4": np.float32,
+              "float32": np.float32, "i8": np.int64, "int64": np.int64, "i4": np.int32,
+              "int32": np.int32, "b1": bool}
+_RESULT_CASTS = {"f8": float, "float64": float, "f4": float, "float32": float, "i8": int,
+                 "int64": int, "i4": int, "int32": int, "b1": bool}
+_CAST_SIGNATURES = False
+
+
+def _split_args(text: str) -> list[str]:
+    out, depth, cur = [], 0, ""
+    for ch in text:
+        if ch in "[(":
+            depth += 1
+        elif ch in "])":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def _typed(sig: str, f):
+    """Cast scalar arguments and a scalar result to the types of a numba
+    signature string ``ret(arg, ...)``, as compiled numba code would."""
+    ret, _, rest = sig.partition("(")
+    casts = [_ARG_CASTS.get(t) for t in _split_args(rest[:-1])]
+    rcast = _RESULT_CASTS.get(ret.strip())
+
+    def call(*args, **kw):
+        args = [c(x) if c is not None and i < len(casts) else x
+                for i, (x, c) in enumerate(zip(args, casts + [None] * len(args)))]
+        r = f(*args, **kw)
+        return rcast(r) if rcast is not None else r
+
+    call.__name__ = f.__name__
+    return call
+
+
 def _deco(*a, **k):
     if len(a) == 1 and callable(a[0]) and not k:
         return a[0]
+    sig = a[0] if a else None
+    if isinstance(sig, list) and len(sig) == 1:
+        sig = sig[0]
+    if _CAST_SIGNATURES and isinstance(sig, str):
+        return lambda f: _typed(sig, f)
     return lambda f: f
 
 
@@ -78,8 +128,12 @@ def _define_boxing(tmpl, proxy):
             delattr(proxy, name)
 
 
-def install(reference_src: str) -> None:
-    """Install the stand-ins and put ``reference_src`` first on sys.path."""
+def install(reference_src: str, cast_signatures: bool = False) -> None:
+    """Install the stand-ins and put ``reference_src`` first on sys.path.
+    ``cast_signatures`` makes functions with an explicit numba signature
+    string cast their scalar arguments and result to its types."""
+    global _CAST_SIGNATURES
+    _CAST_SIGNATURES = cast_signatures
     numba = _t.ModuleType("numba")
     numba.njit = _deco
     numba.jit = _deco
