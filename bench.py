@@ -39,9 +39,10 @@ if str(ROOT) not in sys.path:
 METRIC = "period-trials/s"
 WORKLOAD = "ffa_accel_search_2^23"
 # DRAM bytes (read + write) per final trial of band_union64_kernel: ncu
-# capture of three launches of the same search at 2^21 samples (122.75 MB per
-# launch, 474k trials per launch); profiles/band_union64_kernel_ffa_accel_2^21.md.
-UNION_DRAM_BYTES_PER_TRIAL = 259.0
+# capture of three full-band launches of this search with 1 GiB bands
+# (1.940 GB per launch, 193 x 32098 trials per launch);
+# profiles/band_union64_kernel_ffa_accel_2^23.md.
+UNION_DRAM_BYTES_PER_TRIAL = 313.2
 BF16_TOP = 64        # candidates re-scored in FP64 and checked against the FP64 oracle
 BF16_SAMPLE = 192    # random trials added to the FP64 error sample
 BATCH_WORKLOAD = "ffa_jerk_batch_2^20-2^23"
@@ -487,8 +488,9 @@ def bench_gpu(args) -> dict | None:
                      "launches_per_step": dom_launches,
                      "algorithmic_bytes_per_launch": ab / dom_launches,
                      "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read+write of band_union64_kernel at "
-                                       "2^21 samples, scaled per final trial"
+                     "traffic_source": "ncu dram__bytes_read+write of band_union64_kernel, "
+                                       "three full-band launches of this search at 1 GiB "
+                                       "bands, per final trial x trials per launch"
                                        if traffic is not None else None},
         "e2e": {"value": world * trials / (e2e_ms * 1e-3), "unit": "trials/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 4 * cfg.nsamps,
@@ -920,6 +922,24 @@ def profile_once(args) -> None:
                       "launches": dyp.launches, "snr_shape": list(snr.shape)}))
 
 
+def profile_inject_once(args) -> None:
+    """One injection set of 64 x 2^21 samples after a warm-up, with no timing;
+    the command the generator's ncu summaries are captured from."""
+    import torch
+
+    from pyloki_gb300.pulse import generate_injections
+
+    dev = torch.device("cuda", 0)
+    cfgs, shapes, phis = injection_cfgs(64)
+    generate_injections(cfgs[:4], shapes[:4], phis[:4], seed=1, device=dev)
+    b = generate_injections(cfgs, shapes, phis, seed=1, device=dev)
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"profile_inject_once": True, "injections": len(cfgs),
+                      "nsamps": INJ_NSAMPS,
+                      "median_snr_err": float(np.median(np.abs(
+                          b.scales[:, 3].cpu().numpy() - [c.snr for c in cfgs])))}))
+
+
 def profile_prune_once(args) -> None:
     """One pruning run of the pruning workload after one warm-up run, with no
     timing; the command the pruning ncu summaries are captured from."""
@@ -959,6 +979,8 @@ def main() -> None:
                     help="skip the batched multi-series measurement")
     ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
                     help="series of the seeded 256-series batch to search")
+    ap.add_argument("--profile-inject-once", action="store_true",
+                    help="one untimed 64-injection set (the generator ncu command)")
     ap.add_argument("--no-injections", action="store_true",
                     help="skip the synthetic injection-set section")
     ap.add_argument("--injections", type=int, default=1024,
@@ -985,6 +1007,9 @@ def main() -> None:
         return
     if args.profile_prune_once:
         profile_prune_once(args)
+        return
+    if args.profile_inject_once:
+        profile_inject_once(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
