@@ -706,6 +706,49 @@ int loki_pulse_emit(const LokiPulseSpec* specs, int32_t ninj, int64_t nsamps,
                     const float* luts, const double* pt_table, const float* noise,
                     const double* scales, float* ts_e, float* ts_v, void* stream);
 
+/* ---- alternative profile scorers (detection/scoring.py) ------------------
+ * None of these is on a search path of the reference; they score candidate
+ * profiles (n, nbins) float32 on request. */
+
+/* kadane_circular_normalized_1d (scoring.py:675-755) per profile: the best
+ * mean-subtracted circular window over the biases, float64, with its width
+ * and start. Bit-identical to the reference. */
+int loki_kadane_circular(const float* profiles, int64_t n, int32_t nbins, const float* biases,
+                         int32_t nbias, double* snr, int64_t* width, int64_t* start,
+                         void* stream);
+
+/* The matched-filter bank (MatchedFilter + compute_snr_e_mat_2d,
+ * scoring.py:295-357,491-524): e_mat (nfilt, nbins) holds, per template,
+ * shifts_per_template circularly shifted rows; snr (n, nfilt /
+ * shifts_per_template) = max projection / stdnoise; projections (n, nfilt)
+ * is optional (NULL: not written). */
+int loki_matched_filter(const float* profiles, int64_t n, int32_t nbins, const float* e_mat,
+                        int32_t nfilt, int32_t shifts_per_template, float stdnoise, float* snr,
+                        float* projections, void* stream);
+
+/* _compute_snr_double (scoring.py:561-627): per profile, the larger of the
+ * single-filter and the best two-filter chi-square score among the n_corr
+ * largest projections, less its look-elsewhere penalty, mapped to a normal
+ * S/N. inner = e_mat e_mat^T (nfilt, nfilt). chi_table is the
+ * (df_max + 2, nchi) table of -log sf of chi-square (utils/maths.py:61-77,
+ * a zero row appended), isf_table the normal ISF of exp(-x) (nisf entries,
+ * the last repeated once). */
+int loki_matched_filter_double(const float* profiles, int64_t n, int32_t nbins,
+                               const float* e_mat, int32_t nfilt, const float* inner,
+                               int32_t n_corr, const double* chi_table, int32_t nchi,
+                               double chi_res, double chi_max, const double* isf_table,
+                               int32_t nisf, double isf_res, double isf_max, float* out,
+                               void* stream);
+
+/* harmonic_summing_score_func (scoring.py:630-642) per fold (n, 2, nbins):
+ * cumulative power of harmonics 1..n_harmonics of e / sqrt(v), best
+ * chi-square score over the prefix, as a normal S/N (float64). chi_rows =
+ * rows of chi_table. */
+int loki_harmonic_sum(const float* folds, int64_t n, int32_t nbins, int32_t n_harmonics,
+                      const double* chi_table, int32_t chi_rows, int32_t nchi, double chi_res,
+                      double chi_max, const double* isf_table, int32_t nisf, double isf_res,
+                      double isf_max, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -594,6 +594,31 @@ def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segme
     return fold
 
 
+def brutefold_bucketed(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor,
+                       segment_len: int, nbins: int, tsamp: float,
+                       t_ref: float = 0.0) -> torch.Tensor:
+    """``core/fold.py:174-276``. The reference gathers each (frequency, bin)
+    bucket and sums it in sample order: the same sums, in the same order, as
+    ``brutefold``, which computes them. Like the reference it requires whole
+    segments."""
+    if ts_e.numel() % segment_len:
+        msg = "The number of samples must be a multiple of the segment length."
+        raise ValueError(msg)
+    return brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref)
+
+
+def brutefold_complex_oversampled(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor,
+                                  segment_len: int, nbins: int, tsamp: float,
+                                  t_ref: float = 0.0,
+                                  oversample_factor: int = 4) -> torch.Tensor:
+    """``core/fold.py:484-524``: the fold on ``nbins * oversample_factor``
+    bins, transformed along the bins (cuFFT) and cut to the first
+    ``nbins // 2 + 1`` coefficients, complex64 ``(nseg, nfreq, 2, nbins//2+1)``."""
+    fine = brutefold_bucketed(ts_e, ts_v, freqs, segment_len, nbins * oversample_factor, tsamp,
+                              t_ref)
+    return torch.fft.rfft(fine, dim=-1)[..., :nbins // 2 + 1].to(torch.complex64).contiguous()
+
+
 class FFAPlan:
     """Per-level coordinate plan (``ffa.py:53-193``), resolved on the GPU."""
 

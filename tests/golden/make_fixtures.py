@@ -332,6 +332,65 @@ def pulse_case(name: str, kind: str, params: dict, period: float, snr: float, du
         snr_template=np.float64(snr_t), ts_e=ts.ts_e, ts_v=ts.ts_v)
 
 
+def scorer_case(name: str, nbins: int, n: int, seed: int, shift: int) -> None:
+    """The alternative scorers of detection/scoring.py on seeded profiles with
+    one or two peaks: circular Kadane, the matched-filter bank (boxcar and
+    Gaussian templates), the two-peak score and harmonic summing; plus the
+    bucketed and the oversampled complex brute folds (core/fold.py)."""
+    from pyloki.core import fold as F
+    from pyloki.detection import scoring as S
+
+    rng = np.random.default_rng(seed)
+    x = np.arange(nbins)
+    prof = rng.standard_normal((n, nbins)).astype(np.float32)
+    for i in range(n):
+        for _ in range(1 + (i % 3 == 0)):
+            c, w, a = rng.uniform(0, nbins), rng.uniform(0.6, 5.0), rng.uniform(0, 7)
+            d = np.minimum(np.abs(x - c), nbins - np.abs(x - c))
+            prof[i] += (a * np.exp(-0.5 * (d / w) ** 2)).astype(np.float32)
+    biases = np.array([0.0, 0.05, 0.2, 0.5], np.float32)
+    kad = [S.kadane_circular_normalized_1d(prof[i], biases) for i in range(n)]
+    out = {"profiles": prof, "biases": biases,
+           "kadane_snr": np.array([k[0] for k in kad], np.float64),
+           "kadane_width": np.array([k[1] for k in kad], np.int64),
+           "kadane_start": np.array([k[2] for k in kad], np.int64)}
+    widths = np.array([1, 2, 3, 5, 8, 12, 16], np.int64)
+    out["mf_widths"] = widths
+    for kind in ("boxcar", "gaussian"):
+        mf = S.MatchedFilter(widths, nbins, shift=1, kind=kind)
+        out[f"{kind}_templates"] = mf.templates
+        out[f"{kind}_e_mat"] = mf.e_mat
+        out[f"{kind}_snr"] = S.compute_snr_e_mat_2d(prof, mf.e_mat, mf.shifts)
+        out[f"{kind}_dot"] = np.asarray(mf.compute_dot(prof.T), np.float32)
+        out[f"{kind}_double"] = np.asarray(mf.compute_dot_double(prof), np.float32)
+    # _get_e_mat sizes its bank as nbins // shift rows per template, so the
+    # shift has to divide nbins (other shifts overrun it in the reference)
+    mf2 = S.MatchedFilter(np.array([2, 6], np.int64), nbins, shift=shift, kind="boxcar")
+    out["shift"] = np.int64(shift)
+    out["shift_e_mat"] = mf2.e_mat
+    out["shift_snr"] = S.compute_snr_e_mat_2d(prof, mf2.e_mat, mf2.shifts)
+    var = rng.uniform(0.5, 2.0, (n, nbins)).astype(np.float32)
+    folds = np.stack([prof * np.sqrt(var), var], axis=1).astype(np.float32)
+    out["harm_folds"] = folds
+    out["harm_nh"] = np.array([1, 3, 8], np.int64)
+    out["harmonic"] = np.array([[S.harmonic_summing_score_func(folds[i], nh)
+                                 for nh in (1, 3, 8)] for i in range(n)], np.float64)
+    ts_e = rng.standard_normal(4096).astype(np.float32)
+    ts_v = rng.uniform(0.5, 1.5, 4096).astype(np.float32)
+    freqs = np.array([3.1, 7.7, 12.25, 40.0], np.float64)
+    out.update(bf_ts_e=ts_e, bf_ts_v=ts_v, bf_freqs=freqs, bf_tsamp=np.float64(1e-3),
+               bf_t_ref=np.float64(0.3), bf_segment_len=np.int64(1024))
+    out["bucketed"] = F.brutefold_bucketed(ts_e, ts_v, freqs, 1024, nbins, 1e-3, 0.3)
+    out["oversampled"] = F.brutefold_complex_oversampled(ts_e, ts_v, freqs, 1024, nbins,
+                                                         1e-3, 0.3, 4)
+    np.savez_compressed(HERE / f"{name}.npz", nbins=np.int64(nbins), **out)
+
+
+def scorer_cases() -> None:
+    scorer_case("scorers_nb64", 64, 48, 31, 4)
+    scorer_case("scorers_nb50", 50, 36, 32, 5)
+
+
 def pulse_cases() -> None:
     for case in PULSE_CASES:
         pulse_case(*case)
@@ -343,12 +402,16 @@ def main() -> None:
     sys.path.insert(0, str(HERE))
     import refshim
 
-    # The generator fixtures need numba's scalar typing of the calibration
-    # (float64 scale inside calibrate_scale_on_folds); the others were made
-    # without it.
-    refshim.install(ref_src, cast_signatures="--pulse-only" in sys.argv)
+    # The generator and scorer fixtures need numba's scalar typing (float64
+    # scale inside calibrate_scale_on_folds, typed scorer arguments); the
+    # others were made without it.
+    refshim.install(ref_src, cast_signatures="--pulse-only" in sys.argv
+                    or "--scorers-only" in sys.argv)
     if "--pulse-only" in sys.argv:
         pulse_cases()
+        return
+    if "--scorers-only" in sys.argv:
+        scorer_cases()
         return
     # numba types `float32_array >= float64` as a float64 comparison. Under
     # plain numpy 2 the overflow threshold that world_tree derives with

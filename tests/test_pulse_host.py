@@ -111,3 +111,16 @@ def test_batched_cdf_tables_equal_single_builds():
     tables = cdf_tables(keys)
     for k in keys:
         np.testing.assert_array_equal(tables[k], build_cdf_lut(k[0], k[1], k[2], k[3]))
+
+
+def test_matched_filter_host_checks():
+    from pyloki_gb300.scoring import MatchedFilter
+
+    with pytest.raises(ValueError, match="must divide"):
+        MatchedFilter([2, 6], 50, shift=4)
+    with pytest.raises(ValueError, match="greater than 0"):
+        MatchedFilter([2], 64, shift=0)
+    with pytest.raises(ValueError, match="Unknown template"):
+        MatchedFilter([2], 64, kind="sinc")
+    mf = MatchedFilter([1, 3], 64, shift=2, kind="gaussian")
+    assert mf.e_mat.shape == (64, 64) and np.allclose((mf.e_mat**2).sum(1), 1, atol=1e-5)
