@@ -731,8 +731,8 @@ int loki_matched_filter(const float* profiles, int64_t n, int32_t nbins, const f
  * largest projections, less its look-elsewhere penalty, mapped to a normal
  * S/N. inner = e_mat e_mat^T (nfilt, nfilt). chi_table is the
  * (df_max + 2, nchi) table of -log sf of chi-square (utils/maths.py:61-77,
- * a zero row appended), isf_table the normal ISF of exp(-x) (nisf entries,
- * the last repeated once). */
+ * a zero row appended), isf_table the normal ISF of exp(-x): the reference's
+ * nisf entries plus the last repeated once (nisf + 1 values). */
 int loki_matched_filter_double(const float* profiles, int64_t n, int32_t nbins,
                                const float* e_mat, int32_t nfilt, const float* inner,
                                int32_t n_corr, const double* chi_table, int32_t nchi,
@@ -743,7 +743,7 @@ int loki_matched_filter_double(const float* profiles, int64_t n, int32_t nbins,
 /* harmonic_summing_score_func (scoring.py:630-642) per fold (n, 2, nbins):
  * cumulative power of harmonics 1..n_harmonics of e / sqrt(v), best
  * chi-square score over the prefix, as a normal S/N (float64). chi_rows =
- * rows of chi_table. */
+ * rows of chi_table; tables as for loki_matched_filter_double. */
 int loki_harmonic_sum(const float* folds, int64_t n, int32_t nbins, int32_t n_harmonics,
                       const double* chi_table, int32_t chi_rows, int32_t nchi, double chi_res,
                       double chi_max, const double* isf_table, int32_t nisf, double isf_res,

@@ -38,6 +38,8 @@ def chi_minus_logsf(chi: np.ndarray, x: float, df: int) -> float:
 
 
 def norm_isf(isf: np.ndarray, m: float) -> float:
+    """Negative positions index from the end of the table, as the reference's
+    do (a weak candidate's score wraps to the top of the table)."""
     if m < ISF_MAX:
         pos = m / ISF_RES
         fr = pos % 1
@@ -89,13 +91,19 @@ def snr_e_mat_2d(prof: np.ndarray, e_mat: np.ndarray, shifts: np.ndarray,
 
 
 def snr_double(prof: np.ndarray, e_mat: np.ndarray, n_corr: int = 10) -> np.ndarray:
+    scores = np.stack([np.dot(e_mat, x.astype(np.float32)) for x in prof])
+    return snr_double_from_scores(scores, np.dot(e_mat, e_mat.T), n_corr)
+
+
+def snr_double_from_scores(scores: np.ndarray, inner: np.ndarray,
+                           n_corr: int = 10) -> np.ndarray:
+    """The two-peak score from given projections (n, nfilt)."""
     chi, isf = tables()
-    nf = e_mat.shape[0]
+    nf = scores.shape[1]
     lee_d, lee_s = np.log2((nf * nf - 1) / 2), np.log2(nf)
-    inner = np.dot(e_mat, e_mat.T)
-    out = np.empty(len(prof), np.float32)
-    for p, x in enumerate(prof):
-        sc = np.dot(e_mat, x.astype(np.float32)).astype(np.float64)
+    out = np.empty(len(scores), np.float32)
+    for p, row in enumerate(scores):
+        sc = np.asarray(row, np.float32).astype(np.float64)
         single = float(sc.max()) ** 2
         good = np.argsort(sc, kind="stable")[-n_corr:]
         dbl, s = single, 0.0

@@ -139,8 +139,11 @@ __device__ __forceinline__ double chi_minus_logsf(const double* tab, int nchi, d
   return __ddiv_rn(__dmul_rn(row[nchi - 1], x), xmax);
 }
 
-// norm_isf_func (utils/maths.py:80-89); negative positions wrap to the end
-// of the table as the reference's array indexing does.
+// norm_isf_func (utils/maths.py:80-89) on the reference's nisf-entry table
+// plus one repeated entry (tab[nisf]) for the read one past the end. A
+// negative position (a score whose chi-square term is below its look-
+// elsewhere penalty) wraps to the end of the table, as the reference's
+// array indexing does.
 __device__ __forceinline__ double norm_isf(const double* tab, int nisf, double m, double res,
                                            double mmax) {
   if (m < mmax) {
@@ -151,8 +154,8 @@ __device__ __forceinline__ double norm_isf(const double* tab, int nisf, double m
     int64_t j = i + 1;
     if (i < 0) i += nisf;
     if (j < 0) j += nisf;
-    i = i < 0 ? 0 : (i >= nisf ? nisf - 1 : i);  // stay in the table
-    j = j < 0 ? 0 : (j >= nisf ? nisf - 1 : j);
+    i = i < 0 ? 0 : (i > nisf ? nisf : i);  // stay in the nisf + 1 entries
+    j = j < 0 ? 0 : (j > nisf ? nisf : j);
     return __dadd_rn(__dmul_rn(tab[i], __dsub_rn(1.0, fr)), __dmul_rn(tab[j], fr));
   }
   return __dmul_rn(tab[nisf - 1], sqrt(__ddiv_rn(m, mmax)));

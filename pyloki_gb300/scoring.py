@@ -68,7 +68,8 @@ def score_tables_host() -> tuple[np.ndarray, np.ndarray]:
     """-log sf of chi-square (rows df = 0..64, plus a zero row) and the normal
     ISF of exp(-x) (plus the last value repeated), as the reference builds
     them (utils/maths.py:55-77). The extra row and value keep the one-past-
-    the-end reads of the interpolation inside the tables."""
+    the-end reads of the interpolation inside the tables; the device wraps
+    negative positions with the reference's table length."""
     from scipy import stats
 
     x = np.arange(0, CHI_SQ_MAX, CHI_SQ_RES)
@@ -210,7 +211,7 @@ class MatchedFilter:
         _lib.check(_lib.load().loki_matched_filter_double(
             _lib.ptr(flat), flat.shape[0], self.nbins, _lib.ptr(e), e.shape[0],
             _lib.ptr(inner), int(n_corr), _lib.ptr(chi), chi.shape[1], CHI_SQ_RES, CHI_SQ_MAX,
-            _lib.ptr(isf), isf.numel(), MINUS_LOGSF_RES, MAX_MINUS_LOGSF, _lib.ptr(out),
+            _lib.ptr(isf), isf.numel() - 1, MINUS_LOGSF_RES, MAX_MINUS_LOGSF, _lib.ptr(out),
             _lib.stream_ptr(torch.cuda.current_stream(x.device))))
         out = out.reshape(x.shape[:-1])
         return out.cpu().numpy() if host else out
@@ -247,7 +248,7 @@ def harmonic_summing_score(folds, n_harmonics: int, *, device=None):
     out = torch.empty(flat.shape[0], dtype=torch.float64, device=x.device)
     _lib.check(_lib.load().loki_harmonic_sum(
         _lib.ptr(flat), flat.shape[0], nb, int(n_harmonics), _lib.ptr(chi), chi.shape[0],
-        chi.shape[1], CHI_SQ_RES, CHI_SQ_MAX, _lib.ptr(isf), isf.numel(), MINUS_LOGSF_RES,
+        chi.shape[1], CHI_SQ_RES, CHI_SQ_MAX, _lib.ptr(isf), isf.numel() - 1, MINUS_LOGSF_RES,
         MAX_MINUS_LOGSF, _lib.ptr(out), _lib.stream_ptr(torch.cuda.current_stream(x.device))))
     out = out.reshape(x.shape[:-2])
     return out.cpu().numpy() if host else out

@@ -34,3 +34,19 @@ def test_scorer_oracle_against_reference(path):
                                rtol=1e-6, atol=1e-6)
     got = np.array([[O.harmonic(f, nh) for nh in z["harm_nh"]] for f in z["harm_folds"]])
     np.testing.assert_allclose(got, z["harmonic"], rtol=2e-5)
+
+
+@pytest.mark.parametrize("path", CASES, ids=[p.stem for p in CASES])
+def test_template_banks_equal_reference(path):
+    """Host-built banks against the reference's on this host (numpy's mean
+    and BLAS dot set the last ulps, so another host may differ by a few)."""
+    from pyloki_gb300.scoring import MatchedFilter
+
+    z = np.load(path)
+    nb = int(z["nbins"])
+    for kind in ("boxcar", "gaussian"):
+        mf = MatchedFilter(z["mf_widths"], nb, 1, kind)
+        np.testing.assert_array_equal(mf.templates, z[f"{kind}_templates"])
+        np.testing.assert_array_equal(mf.e_mat, z[f"{kind}_e_mat"])
+    mf = MatchedFilter(np.array([2, 6]), nb, int(z["shift"]), "boxcar")
+    np.testing.assert_array_equal(mf.e_mat, z["shift_e_mat"])
