@@ -706,6 +706,22 @@ int loki_pulse_emit(const LokiPulseSpec* specs, int32_t ninj, int64_t nsamps,
                     const float* luts, const double* pt_table, const float* noise,
                     const double* scales, float* ts_e, float* ts_v, void* stream);
 
+/* TimeSeries.fold_ephem (io/timeseries.py:45-83): the series folded at freq
+ * over the proper times of mod (t = i dt; pt_table for LOKI_MOD_TABLE) into
+ * fold (nsubints, 2, nbins) float32, each (subint, bin) summed in sample
+ * order as core/fold.py:57-105 brutefold does (bit-identical); norm
+ * (nsubints, nbins), if not NULL, = e / sqrt(v), or 0 where |v| <= 1e-5.
+ * bins: nsamps uint32 scratch. Trailing samples past nsubints whole
+ * subints are not folded. */
+int loki_fold_ephem(const float* ts_e, const float* ts_v, int64_t nsamps, double dt,
+                    const LokiModulation* mod, const double* pt_table, double freq,
+                    int32_t nbins, int32_t nsubints, uint32_t* bins, float* fold, float* norm,
+                    void* stream);
+
+/* Mean of each group of factor samples, n / factor outputs
+ * (utils/np_utils.py:119-122 downsample_1d). */
+int loki_downsample(const float* x, int64_t n, int32_t factor, float* out, void* stream);
+
 /* ---- alternative profile scorers (detection/scoring.py) ------------------
  * None of these is on a search path of the reference; they score candidate
  * profiles (n, nbins) float32 on request. */

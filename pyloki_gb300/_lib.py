@@ -213,6 +213,9 @@ SIGNATURES: dict[str, tuple] = {
     "loki_pulse_template": (C.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _P]),
     "loki_pulse_fold": (C.c_int, [_P, _I32, _I64, _P, _P, _P, _P, _I32, _P, _P, _P]),
     "loki_pulse_apply": (C.c_int, [_P, _I32, _I64, _P, _P, _P]),
+    "loki_fold_ephem": (C.c_int, [_P, _P, _I64, _D, C.POINTER(LokiModulation), _P, _D, _I32,
+                                  _I32, _P, _P, _P, _P]),
+    "loki_downsample": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_kadane_circular": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P, _P, _P]),
     "loki_matched_filter": (C.c_int, [_P, _I64, _I32, _P, _I32, _I32, C.c_float, _P, _P, _P]),
     "loki_matched_filter_double": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _I32, _P, _I32, _D,

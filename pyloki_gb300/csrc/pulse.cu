@@ -569,3 +569,100 @@ extern "C" int loki_pulse_apply(const double* scales, int32_t ninj, int64_t nsam
       nsamps, scales, ts_e, ts_v, vec4);
   return check_launch("pulse_apply");
 }
+
+// ---------------------------------------------------------------------------
+// TimeSeries.fold_ephem (io/timeseries.py:45-83): the series folded at one
+// frequency over the proper times of a modulation model, in nsub
+// subintegrations (core/fold.py:57-105 brutefold): every (subint, bin) sum
+// in sample order in float32, so the fold is the reference's bit for bit.
+// Pass 1 bins every sample; pass 2 gives each (subint, bin) one thread that
+// walks its subint in order.
+// ---------------------------------------------------------------------------
+namespace loki {
+
+__global__ void ephem_bins_kernel(LokiPulseSpec s, const double* __restrict__ table,
+                                  int64_t n, double freq, int nbins,
+                                  uint32_t* __restrict__ bins) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double pt = proper_time_at(s, i, table, 0);
+    bins[i] = (uint32_t)round_shift(phase_idx(pt, freq, nbins, 0.0), nbins);
+  }
+}
+
+__global__ void __launch_bounds__(256)
+ephem_fold_kernel(const float* __restrict__ ts_e, const float* __restrict__ ts_v,
+                  const uint32_t* __restrict__ bins, int64_t seg_len, int nbins,
+                  float* __restrict__ fold, float* __restrict__ norm) {
+  const int64_t seg = blockIdx.y;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i0 = seg * seg_len;
+  float e = 0.0f, v = 0.0f;
+  if (b < nbins) {
+    for (int64_t i = i0; i < i0 + seg_len; ++i) {
+      if (bins[i] == (uint32_t)b) {
+        e = __fadd_rn(e, ts_e[i]);
+        v = __fadd_rn(v, ts_v[i]);
+      }
+    }
+    fold[(seg * 2) * nbins + b] = e;
+    fold[(seg * 2 + 1) * nbins + b] = v;
+    if (norm)  // zero where the variance is within 1e-5 of zero (np.isclose)
+      norm[seg * nbins + b] = fabsf(v) <= 1e-5f ? 0.0f : __fdiv_rn(e, __fsqrt_rn(v));
+  }
+}
+
+// Mean of each group of `factor` samples (np_utils.downsample_1d).
+__global__ void downsample_kernel(const float* __restrict__ x, int64_t nout, int factor,
+                                  float* __restrict__ out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nout;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j < factor; ++j) acc += (double)x[k * factor + j];
+    out[k] = __double2float_rn(acc / factor);
+  }
+}
+
+}  // namespace loki
+
+extern "C" int loki_fold_ephem(const float* ts_e, const float* ts_v, int64_t nsamps, double dt,
+                               const LokiModulation* mod, const double* pt_table, double freq,
+                               int32_t nbins, int32_t nsubints, uint32_t* bins, float* fold,
+                               float* norm, void* stream) {
+  if (nsamps < 1 || !(dt > 0.0) || !(freq > 0.0) || nbins < 1 || nsubints < 1 ||
+      nsubints > nsamps)
+    return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (nsubints > 65535) return set_error(LOKI_ERR_UNSUPPORTED, "more than 65535 subints");
+  if (!ts_e || !ts_v || !mod || !bins || !fold)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if (mod->kind < LOKI_MOD_DERIVATIVE || mod->kind > LOKI_MOD_TABLE ||
+      (mod->kind == LOKI_MOD_TABLE && !pt_table) || mod->ncoeff < 0 ||
+      mod->ncoeff > LOKI_MOD_MAX_COEFFS)
+    return set_error(LOKI_ERR_INVALID, "bad modulation");
+  LokiPulseSpec s{};
+  s.dt = dt;
+  s.mod = *mod;
+  const int64_t seg_len = nsamps / nsubints;
+  const int64_t nfold = seg_len * nsubints;  // trailing samples are not folded
+  note_launch();
+  ephem_bins_kernel<<<(unsigned)std::min<int64_t>((nfold + 255) / 256, 152 * 16), 256, 0,
+                      (cudaStream_t)stream>>>(s, pt_table, nfold, freq, nbins, bins);
+  int rc = check_launch("fold_ephem (bins)");
+  if (rc) return rc;
+  note_launch();
+  ephem_fold_kernel<<<dim3((unsigned)((nbins + 255) / 256), (unsigned)nsubints), 256, 0,
+                      (cudaStream_t)stream>>>(ts_e, ts_v, bins, seg_len, nbins, fold, norm);
+  return check_launch("fold_ephem");
+}
+
+extern "C" int loki_downsample(const float* x, int64_t n, int32_t factor, float* out,
+                               void* stream) {
+  if (n < 0 || factor < 1) return set_error(LOKI_ERR_INVALID, "bad sizes");
+  const int64_t nout = n / factor;
+  if (nout == 0) return LOKI_OK;
+  if (!x || !out) return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  note_launch();
+  downsample_kernel<<<(unsigned)std::min<int64_t>((nout + 255) / 256, 152 * 16), 256, 0,
+                      (cudaStream_t)stream>>>(x, nout, factor, out);
+  return check_launch("downsample");
+}

@@ -386,6 +386,33 @@ def scorer_case(name: str, nbins: int, n: int, seed: int, shift: int) -> None:
     np.savez_compressed(HERE / f"{name}.npz", nbins=np.int64(nbins), **out)
 
 
+def timeseries_case() -> None:
+    """TimeSeries.fold_ephem and downsample (io/timeseries.py:40-83) on a
+    seeded accelerated pulsar."""
+    from pyloki.io.timeseries import TimeSeries
+
+    rng = np.random.default_rng(41)
+    n, dt, f0 = 2**15, 2e-4, 37.3
+    t = np.arange(n) * dt
+    ph = (t - 12.0 * (t - n * dt / 2) ** 2 / 2 / 299792458.0) * f0
+    ts_e = (rng.standard_normal(n) + 0.8 * np.exp(6 * (np.cos(2 * np.pi * ph) - 1))).astype(
+        np.float32)
+    ts_v = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    ts_v[::97] = 0.0
+    ts = TimeSeries(ts_e, ts_v, dt)
+    out = {"ts_e": ts_e, "ts_v": ts_v, "dt": np.float64(dt), "freq": np.float64(f0)}
+    kw = {"mod_kwargs": {"acc": 12.0, "jerk": 0.3}}
+    out["fold1"] = ts.fold_ephem(f0, 64, 1, normalize=False, **kw)
+    out["norm1"] = ts.fold_ephem(f0, 64, 1, **kw)
+    out["fold8"] = ts.fold_ephem(f0, 50, 8, normalize=False, **kw)
+    out["norm8"] = ts.fold_ephem(f0, 50, 8, **kw)
+    out["fold_circ"] = ts.fold_ephem(f0, 32, 3, normalize=False, mod_type="circular",
+                                     mod_kwargs={"p_orb": 600.0, "x_orb": 0.01, "psi": 0.2})
+    ds = ts.downsample(4)
+    out.update(ds_e=ds.ts_e, ds_v=ds.ts_v, ds_dt=np.float64(ds.dt))
+    np.savez_compressed(HERE / "timeseries_ephem.npz", **out)
+
+
 def scorer_cases() -> None:
     scorer_case("scorers_nb64", 64, 48, 31, 4)
     scorer_case("scorers_nb50", 50, 36, 32, 5)
@@ -406,12 +433,15 @@ def main() -> None:
     # scale inside calibrate_scale_on_folds, typed scorer arguments); the
     # others were made without it.
     refshim.install(ref_src, cast_signatures="--pulse-only" in sys.argv
-                    or "--scorers-only" in sys.argv)
+                    or "--scorers-only" in sys.argv or "--timeseries-only" in sys.argv)
     if "--pulse-only" in sys.argv:
         pulse_cases()
         return
     if "--scorers-only" in sys.argv:
         scorer_cases()
+        return
+    if "--timeseries-only" in sys.argv:
+        timeseries_case()
         return
     # numba types `float32_array >= float64` as a float64 comparison. Under
     # plain numpy 2 the overflow threshold that world_tree derives with
