@@ -742,6 +742,13 @@ int loki_matched_filter(const float* profiles, int64_t n, int32_t nbins, const f
                         int32_t nfilt, int32_t shifts_per_template, float stdnoise, float* snr,
                         float* projections, void* stream);
 
+/* MatchedFilter.compute_fft (_compute_snr_fft, scoring.py:527-558): per
+ * (profile, template) the max over the first nbins lags of the circular
+ * convolution of the profile, circularly padded to the next power of two,
+ * with the zero-padded template (ntemp, nbins). out (n, ntemp). */
+int loki_matched_filter_conv(const float* profiles, int64_t n, int32_t nbins,
+                             const float* templates, int32_t ntemp, float* out, void* stream);
+
 /* _compute_snr_double (scoring.py:561-627): per profile, the larger of the
  * single-filter and the best two-filter chi-square score among the n_corr
  * largest projections, less its look-elsewhere penalty, mapped to a normal

@@ -130,3 +130,15 @@ def harmonic(fold: np.ndarray, n_harmonics: int) -> float:
         raw += abs(ft[i]) ** 2
         best = max(chi_minus_logsf(chi, raw * 2, 2 * i), best)
     return norm_isf(isf, best)
+
+
+def snr_fft(prof: np.ndarray, templates: np.ndarray) -> np.ndarray:
+    """``_compute_snr_fft``: circular pad to a power of two, zero-padded
+    templates, irfft(rfft(x) rfft(t)), max over the first nbins lags."""
+    nb = prof.shape[-1]
+    n = 1 << int(np.ceil(np.log2(nb)))
+    xx = np.concatenate([prof, prof[:, :n - nb]], axis=1).astype(np.float32)
+    yy = np.concatenate([templates, np.zeros((len(templates), n - nb))], axis=1)
+    fx, fy = np.fft.rfft(xx), np.fft.rfft(yy)
+    return np.array([[np.fft.irfft(fx[p] * fy[t], n)[:nb].max() for t in range(len(templates))]
+                     for p in range(len(prof))], np.float32)

@@ -218,6 +218,7 @@ SIGNATURES: dict[str, tuple] = {
     "loki_downsample": (C.c_int, [_P, _I64, _I32, _P, _P]),
     "loki_kadane_circular": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P, _P, _P]),
     "loki_matched_filter": (C.c_int, [_P, _I64, _I32, _P, _I32, _I32, C.c_float, _P, _P, _P]),
+    "loki_matched_filter_conv": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P]),
     "loki_matched_filter_double": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _I32, _P, _I32, _D,
                                              _D, _P, _I32, _D, _D, _P, _P]),
     "loki_harmonic_sum": (C.c_int, [_P, _I64, _I32, _I32, _P, _I32, _I32, _D, _D, _P, _I32,

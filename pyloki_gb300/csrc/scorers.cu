@@ -255,6 +255,33 @@ harmonic_kernel(const float* __restrict__ folds, int64_t n, int nb, int nh, Scor
   out[p] = norm_isf(T.isf, T.nisf, best, T.isf_res, T.isf_max);
 }
 
+// _compute_snr_fft (scoring.py:527-558): the profile circularly padded to
+// the next power of two N (np_utils.cpadpow2), the template zero-padded to N,
+// their circular convolution c[k] = sum_m t[m] x[(k - m) mod N] (what the
+// reference's irfft(rfft(x) rfft(t)) computes), max over k < nbins. Direct
+// float64 sums; thread per (profile, template).
+__global__ void __launch_bounds__(128)
+mf_conv_kernel(const float* __restrict__ prof, int64_t n, int nb, int npad,
+               const float* __restrict__ templates, int ntemp, float* __restrict__ out) {
+  const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (q >= n * ntemp) return;
+  const int64_t p = q / ntemp;
+  const int t = (int)(q - p * ntemp);
+  const float* x = prof + p * nb;
+  const float* tm = templates + (size_t)t * nb;
+  double best = -INFINITY;
+  for (int k = 0; k < nb; ++k) {
+    double c = 0.0;
+    for (int m = 0; m < nb; ++m) {
+      int j = k - m;
+      j += j < 0 ? npad : 0;              // index into the padded profile
+      c += (double)tm[m] * (double)x[j < nb ? j : j - nb];
+    }
+    best = fmax(best, c);
+  }
+  out[q] = __double2float_rn(best);
+}
+
 ScoreTables tables_of(const double* chi, int32_t nchi, double chi_res, double chi_max,
                       const double* isf, int32_t nisf, double isf_res, double isf_max) {
   return ScoreTables{chi, nchi, chi_res, chi_max, isf, nisf, isf_res, isf_max};
@@ -343,4 +370,19 @@ extern "C" int loki_harmonic_sum(const float* folds, int64_t n, int32_t nbins,
       folds, n, nbins, n_harmonics,
       tables_of(chi_table, nchi, chi_res, chi_max, isf_table, nisf, isf_res, isf_max), out);
   return check_launch("harmonic_sum");
+}
+
+extern "C" int loki_matched_filter_conv(const float* profiles, int64_t n, int32_t nbins,
+                                        const float* templates, int32_t ntemp, float* out,
+                                        void* stream) {
+  if (n < 0 || nbins < 1 || ntemp < 1) return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (n == 0) return LOKI_OK;
+  if (!profiles || !templates || !out) return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  int npad = 1;
+  while (npad < nbins) npad <<= 1;
+  const int64_t work = n * ntemp;
+  note_launch();
+  mf_conv_kernel<<<(unsigned)((work + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      profiles, n, nbins, npad, templates, ntemp, out);
+  return check_launch("matched_filter_conv");
 }

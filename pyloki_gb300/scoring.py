@@ -200,6 +200,24 @@ class MatchedFilter:
         proj = proj.T if t.ndim == 2 else proj[0]
         return proj.cpu().numpy() if host else proj.contiguous()
 
+    def compute_fft(self, folds, *, device=None):
+        """Max over the first nbins lags of the circular convolution of each
+        profile (circularly padded to a power of two) with each template,
+        ``(..., nbins) -> (..., ntemp)`` (``_compute_snr_fft``)."""
+        device = device or (folds.device if isinstance(folds, torch.Tensor) else "cuda")
+        x, host = _to_device(folds, device)
+        flat = x.reshape(-1, self.nbins).contiguous()
+        key = f"templates:{x.device}"
+        if key not in self._dev:
+            self._dev[key] = torch.from_numpy(self.templates).to(x.device)
+        tm = self._dev[key]
+        out = torch.empty((flat.shape[0], self.ntemp), dtype=torch.float32, device=x.device)
+        _lib.check(_lib.load().loki_matched_filter_conv(
+            _lib.ptr(flat), flat.shape[0], self.nbins, _lib.ptr(tm), self.ntemp, _lib.ptr(out),
+            _lib.stream_ptr(torch.cuda.current_stream(x.device))))
+        out = out.reshape(*x.shape[:-1], self.ntemp)
+        return out.cpu().numpy() if host else out
+
     def compute_dot_double(self, folds, n_corr: int = 10, *, device=None):
         """Two-peak score per profile (``_compute_snr_double``)."""
         device = device or (folds.device if isinstance(folds, torch.Tensor) else "cuda")

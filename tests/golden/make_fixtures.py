@@ -363,6 +363,7 @@ def scorer_case(name: str, nbins: int, n: int, seed: int, shift: int) -> None:
         out[f"{kind}_snr"] = S.compute_snr_e_mat_2d(prof, mf.e_mat, mf.shifts)
         out[f"{kind}_dot"] = np.asarray(mf.compute_dot(prof.T), np.float32)
         out[f"{kind}_double"] = np.asarray(mf.compute_dot_double(prof), np.float32)
+        out[f"{kind}_fft"] = np.asarray(mf.compute_fft(prof), np.float32)
     # _get_e_mat sizes its bank as nbins // shift rows per template, so the
     # shift has to divide nbins (other shifts overrun it in the reference)
     mf2 = S.MatchedFilter(np.array([2, 6], np.int64), nbins, shift=shift, kind="boxcar")

@@ -29,6 +29,8 @@ def test_scorer_oracle_against_reference(path):
         np.testing.assert_allclose(O.snr_e_mat_2d(prof, e, np.ones(7, np.int64)),
                                    z[f"{kind}_snr"], rtol=1e-6, atol=1e-6)
         np.testing.assert_allclose(O.snr_double(prof, e), z[f"{kind}_double"], rtol=2e-5)
+        np.testing.assert_allclose(O.snr_fft(prof, z[f"{kind}_templates"]), z[f"{kind}_fft"],
+                                   rtol=0, atol=1e-5)
     sh = np.full(2, int(z["shift"]), np.int64)
     np.testing.assert_allclose(O.snr_e_mat_2d(prof, z["shift_e_mat"], sh), z["shift_snr"],
                                rtol=1e-6, atol=1e-6)

@@ -70,6 +70,9 @@ def test_matched_filter_bank(cuda_device, path):
                                    rtol=0, atol=PROJ_ATOL)
         np.testing.assert_allclose(mf.compute_dot(prof.T, device=cuda_device),
                                    z[f"{kind}_dot"], rtol=0, atol=PROJ_ATOL)
+        mf.templates = z[f"{kind}_templates"]
+        np.testing.assert_allclose(mf.compute_fft(prof, device=cuda_device), z[f"{kind}_fft"],
+                                   rtol=0, atol=PROJ_ATOL)
         dbl = mf.compute_dot_double(prof, device=cuda_device)
         # from the GPU's own projections the oracle gives the same score
         proj = mf.compute_dot(prof.T, device=cuda_device).T
