@@ -220,6 +220,9 @@ class _Batch:
             msg = "all injections of a batch need the same nsamps"
             raise ValueError(msg)
         shapes = [shape] * n if isinstance(shape, str) else list(shape)
+        if len(shapes) != n:
+            msg = f"{len(shapes)} shapes for {n} injections"
+            raise ValueError(msg)
         phis = np.broadcast_to(np.asarray(phi0, dtype=np.float64), (n,))
         for s in shapes:
             if s not in SHAPES:

@@ -79,6 +79,10 @@ def test_validation_before_any_kernel():
                             device="cpu")
     with pytest.raises(ValueError, match="Unknown shape"):
         _Batch([a], "sawtooth", 0.5, 0, "cpu")
+    with pytest.raises(ValueError, match="2 shapes for 1 injections"):
+        _Batch([a], ["gaussian", "boxcar"], 0.5, 0, "cpu")
+    with pytest.raises(ValueError):
+        _Batch([a, a], "gaussian", [0.1, 0.2, 0.3], 0, "cpu")
     with pytest.raises(ValueError, match="calibration bins"):
         _Batch([PulseSignalConfig(period=1.0, dt=64e-6, nsamps=4096)], "gaussian", 0.5, 0,
                "cpu").fold(None)
