@@ -673,6 +673,7 @@ def bench_learned(args, dev) -> dict:
                 test_seeds=list(range(20_000, 20_000 + n_te)),
                 noise_seeds=list(range(30_000, 30_000 + n_te)),
                 budget=args.learned_budget, lookahead=16, per_level=2048, epochs=6,
+                score_share=args.learned_score_share,
                 max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH, device=dev)
     res["workload"] = PRUNE_WORKLOAD
     res["sample"] = (f"{n_tr} training injections, {n_te} held-out injections, {n_te} "
@@ -990,8 +991,11 @@ def main() -> None:
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned branch proposal study")
     ap.add_argument("--learned-train", type=int, default=16)
-    ap.add_argument("--learned-test", type=int, default=8)
-    ap.add_argument("--learned-budget", type=int, nargs="+", default=[16384, 65536],
+    ap.add_argument("--learned-test", type=int, default=16)
+    ap.add_argument("--learned-score-share", type=float, default=0.5,
+                    help="share of each level's parent budget given to the best-scoring "
+                         "parents (the rest is ranked by the network)")
+    ap.add_argument("--learned-budget", type=int, nargs="+", default=[16384, 65536, 131072],
                     help="parents expanded per level under the learned proposal")
     ap.add_argument("--no-prune", action="store_true",
                     help="skip the enumerate-prune (leaves/s) measurement")

@@ -407,7 +407,12 @@ def study(cfg, thresholds, make_series, *, train_seeds, test_seeds, noise_seeds,
             "plain_equivalent_leaves_per_s": l0 / (ms1 * 1e-3), "speedup": ms0 / ms1,
             "leaves_fraction": l1 / max(l0, 1),
         }
+    ok = [b for b in budgets if inj and per_budget[str(b)]["recall_vs_plain"] >= 0.99]
+    at99 = ({"budget": min(ok), **{k: per_budget[str(min(ok))][k]
+                                   for k in ("recall_vs_plain", "speedup", "leaves_fraction")}}
+            if ok else None)
     return {
+        "at_recall_0.99": at99,
         "train_series": len(train_seeds), "train_samples": int(x.shape[0]),
         "positive_fraction": pos, "label": (f"ancestor of the final top {top_k}"
                                             if top_k else f"alive {lookahead} levels later"),
