@@ -44,6 +44,14 @@ def taylor_matrix(delta_t: float, n: int) -> np.ndarray:
     return delta_t**powers / fact(powers) * np.tril(np.ones_like(powers))
 
 
+def taylor_matrices(delta_t: np.ndarray, n: int) -> np.ndarray:
+    """``taylor_matrix`` for every entry of ``delta_t`` at once (the same
+    element-wise operations), shape ``(len(delta_t), n, n)``."""
+    powers = np.tril(np.arange(n)[:, np.newaxis] - np.arange(n))
+    dt = np.asarray(delta_t, dtype=np.float64)[:, np.newaxis, np.newaxis]
+    return dt**powers / fact(powers) * np.tril(np.ones_like(powers))
+
+
 def shift_factors(poly_order: int, tobs: float, nbins: int) -> np.ndarray:
     """Bin-shift factors of poly_taylor_shift_d_vec (``utils/psr_utils.py:227-248``)."""
     k = np.arange(poly_order - 1, -1, -1)
@@ -315,13 +323,14 @@ class Pruning:
             bs = self._best_scores.cpu().numpy()
         for row, leaves, scores in self._pending_best:
             slot = self._best_intermediate_arr[row]
-            k = int(scores.shape[0])
             slot["param_sets"][:] = 0
             slot["scores"][:] = 0
-            if k and leaves.data_ptr() == self._best_leaves[row].data_ptr():
+            if leaves is None:  # written by loki_prune_best into the run's arrays
                 slot["param_sets"][0] = bl[row]
                 slot["scores"][0] = bs[row]
-            elif k:
+                continue
+            k = int(scores.shape[0])
+            if k:
                 slot["param_sets"][:k] = leaves.cpu().numpy()
                 slot["scores"][:k] = scores.cpu().numpy()
         self._pending_best = []
@@ -329,18 +338,23 @@ class Pruning:
     def _record_best(self, level: int, tree: WorldTree) -> None:
         if self.intermediate_k == 1 and tree.valid_size:  # one native launch
             row = int(np.prod(tree.leaves.shape[1:]))
-            leaf = self._best_leaves[level - 1]
-            score = self._best_scores[level - 1:level]
+            # rows level - 1 of the run's (levels, row) float64 and (levels,)
+            # float32 arrays, addressed directly
+            leaf_ptr = self._best_leaves.data_ptr() + (level - 1) * row * 8
+            score_ptr = self._best_scores.data_ptr() + (level - 1) * 4
             _lib.check(self._lib.loki_prune_best(
                 tree.scores.data_ptr(), tree.valid_size, tree.leaves.data_ptr(), row,
-                leaf.data_ptr(), score.data_ptr(), self._stream()))
-            self._pending_best.append((level - 1, leaf[None], score))
+                leaf_ptr, score_ptr, self._stream()))
+            self._pending_best.append((level - 1, None, None))
             return
         leaves, scores = tree.best_k_device(self.intermediate_k)
         self._pending_best.append((level - 1, leaves, scores))
 
     def _stream(self) -> int:
-        return _lib.stream_ptr(torch.cuda.current_stream(self._device))
+        """The run's stream: the current stream when ``initialize`` ran."""
+        ptr = self.__dict__.get("_stream_ptr")
+        return ptr if ptr is not None else _lib.stream_ptr(
+            torch.cuda.current_stream(self._device))
 
     def _fold_segment(self, seg: int) -> torch.Tensor:
         f = self.dyp.fold[seg]
@@ -384,6 +398,8 @@ class Pruning:
         return WorldTree(torch.from_numpy(leaves).to(self._device), folds, scores, bt)
 
     def initialize(self, ref_seg: int, log_file: Path | None = None) -> None:
+        self._stream_ptr = None
+        self._stream_ptr = self._stream()
         self._scheme = MiddleOutScheme(self.dyp.nsegments, ref_seg, self.dyp.tseg, 1)
         self._prune_complete = False
         self._prune_level = 0
@@ -884,24 +900,31 @@ class Pruning:
         coord_end = sc.get_previous_coord(self.prune_level + 1, self.use_moving_grid)
         seg_idx, seg_coords = sc.get_segment_coords_so_far(self.prune_level)
         nseg = len(seg_idx)
-        tm = np.zeros((nseg, 6, 6), np.float64)
-        dts = np.zeros(nseg, np.float64)
         cheby = self.poly_basis == "chebyshev"
-        for s in range(nseg):
-            dt = seg_coords[s, 0] - coord_end[0]
-            if cheby:  # core/chebyshev.py:280-320 (shift at the end-domain scale)
-                tm[s, : P + 1, : P + 1] = chebyshev.transform_matrix(
-                    P, coord_end[0], coord_end[1], seg_coords[s, 0], coord_end[1]).T
-            else:
-                tm[s, : P + 1, : P + 1] = taylor_matrix(dt, P + 1)
-            dts[s] = dt
         dev = self._device
-        tm_d = torch.from_numpy(tm).to(dev)
-        dt_d = torch.from_numpy(dts).to(dev)
-        si_d = torch.from_numpy(seg_idx.astype(np.int32)).to(dev)
+        # the tables depend only on the reference segment and the level
+        key = ("ascend", sc.ref_idx, self.prune_level, self.poly_basis, self.use_moving_grid,
+               str(dev))
+        cache = self.__dict__.setdefault("_desc_cache", {})
+        if key not in cache:
+            dts = seg_coords[:, 0] - coord_end[0]
+            tm = np.zeros((nseg, 6, 6), np.float64)
+            if cheby:  # core/chebyshev.py:280-320 (shift at the end-domain scale)
+                for s in range(nseg):
+                    tm[s, : P + 1, : P + 1] = chebyshev.transform_matrix(
+                        P, coord_end[0], coord_end[1], seg_coords[s, 0], coord_end[1]).T
+            else:
+                tm[:, : P + 1, : P + 1] = taylor_matrices(dts, P + 1)
+            cache[key] = (torch.from_numpy(tm).to(dev),
+                          torch.from_numpy(np.ascontiguousarray(dts, np.float64)).to(dev),
+                          torch.from_numpy(seg_idx.astype(np.int32)).to(dev))
+        tm_d, dt_d, si_d = cache[key]
         fold = self.dyp.fold
         stride = int(np.prod(fold.shape[1:]))
-        d = self._level_desc(self.prune_level)  # a fresh copy: modified below
+        dkey = ("ascend_desc",) + key[1:]
+        if dkey not in cache:
+            cache[dkey] = self._level_desc(self.prune_level)
+        d = _lib.LokiPruneLevel.from_buffer_copy(cache[dkey])  # a copy: modified below
         if cheby:
             self._cheby_scale(d, coord_end[1])
         wt = self.world_tree
