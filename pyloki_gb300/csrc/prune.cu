@@ -1762,9 +1762,47 @@ prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __r
   __shared__ int64_t si[32];
   float bv = -INFINITY;
   int64_t bi = -1;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  // each thread visits its elements in increasing index order, so it keeps
+  // its first maximum; float4 loads, four in flight, when the scores are
+  // 16-byte aligned
+  int64_t head = 0;
+  if ((reinterpret_cast<uintptr_t>(scores) & 15) == 0) {
+    const float4* s4 = reinterpret_cast<const float4*>(scores);
+    const int64_t n4 = n >> 2;
+    const int64_t step = blockDim.x;
+    int64_t q = threadIdx.x;
+    for (; q + 3 * step < n4; q += 4 * step) {
+      float4 a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = s4[q + u * step];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float c[4] = {a[u].x, a[u].y, a[u].z, a[u].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (bi < 0 || c[k] > bv) {
+            bv = c[k];
+            bi = 4 * (q + u * step) + k;
+          }
+        }
+      }
+    }
+    for (; q < n4; q += step) {
+      const float4 a = s4[q];
+      const float c[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (bi < 0 || c[k] > bv) {
+          bv = c[k];
+          bi = 4 * q + k;
+        }
+      }
+    }
+    head = n4 << 2;
+  }
+  for (int64_t i = head + threadIdx.x; i < n; i += blockDim.x) {
     const float v = scores[i];
-    if (bi < 0 || v > bv) {  // strided order: the first maximum of this thread
+    if (bi < 0 || v > bv) {
       bv = v;
       bi = i;
     }
