@@ -437,12 +437,72 @@ class Pruning:
     # ---- per-level constants ---------------------------------------------------
     def level_desc(self, level: int) -> _lib.LokiPruneLevel:
         """Constants of one level; they depend only on the reference segment
-        and the level, so repeated runs from the same segment reuse them."""
-        key = (self.scheme.ref_idx, level)
+        and the level, so repeated runs from the same segment reuse them. For
+        the Taylor basis every level of the segment is built at once
+        (``_level_descs_taylor``)."""
         cache = self.__dict__.setdefault("_desc_cache", {})
+        if self.poly_basis == "taylor" and not self.circular:
+            akey = ("taylor_all", self.scheme.ref_idx, self.use_moving_grid)
+            if akey not in cache:
+                cache[akey] = self._level_descs_taylor(max(self.dyp.nsegments - 1, 1))
+            return cache[akey][level - 1]
+        key = (self.scheme.ref_idx, level)
         if key not in cache:
             cache[key] = self._level_desc(level)
         return cache[key]
+
+    def _level_descs_taylor(self, nlev: int):
+        """``_level_desc`` for levels 1..nlev of the Taylor basis in one
+        vectorised pass (the same element-wise operations, so the same
+        values), as a ctypes array of descriptors."""
+        cfg = self.dyp.cfg
+        sc = self.scheme
+        moving = self.use_moving_grid
+        P = self.poly_order
+        levels = range(1, nlev + 1)
+        c_init = sc.get_coord(0)
+        cur = np.array([sc.get_current_coord(L, moving) for L in levels], dtype=np.float64)
+        nxt = np.array([sc.get_coord(L) for L in levels], dtype=np.float64)
+        add = np.array([sc.get_segment_coord(L) for L in levels], dtype=np.float64)
+        arr = (_lib.LokiPruneLevel * nlev)()
+        v = np.ctypeslib.as_array(arr)
+        v["poly_order"] = P
+        v["nbins"] = cfg.nbins
+        v["nparams_ffa"] = self.nparams_ffa
+        v["moving"] = 1 if moving else 0
+        v["tiling"] = _TILING[cfg.tiling_strategy]
+        v["branch_max"] = cfg.branch_max
+        v["eta_m"] = cfg.eta - FLOAT_EPSILON
+        tobs = cur[:, 1]
+        # poly_taylor_step_f (t_ref 0, Chebyshev-scaled), times c
+        k = np.arange(P)
+        step = cfg.eta / cfg.nbins * fact(k + 1) / (tobs[:, None] - 0) ** (k + 1)
+        step = (2**k * step)[:, ::-1] * C_VAL
+        # shift_factors
+        kk = np.arange(P - 1, -1, -1)
+        fac = (tobs[:, None] - 0) ** (kk + 1) * cfg.nbins / fact(kk + 1) / 2**kk
+        v["dfc"][:, :P] = step
+        v["fac"][:, :P] = fac
+        n = P + 1
+        if moving:
+            v["tm_a"][:, :n, :n] = taylor_matrices(add[:, 0] - cur[:, 0], n)
+            v["tm_i"][:, :n, :n] = taylor_matrices(c_init[0] - cur[:, 0], n)
+            tn = taylor_matrices(nxt[:, 0] - cur[:, 0], n)
+            v["tm_n"][:, :n, :n] = tn
+            v["tm_e"][:, :n, :n] = tn**2 if cfg.tiling_strategy == "quadrature" else np.abs(tn)
+        else:
+            v["tm_a"][:, :n, :n] = taylor_matrices(add[:, 0] - c_init[0], n)
+        v["dt_phase"] = add[:, 0] - c_init[0]
+        counts = self.param_grid_count_init
+        lim = cfg.param_limits
+        v["n_accel"], v["n_freq"] = int(counts[-2]), int(counts[-1])
+        a_min, a_max = lim[-2]
+        f_min, f_max = lim[-1]
+        v["accel_min"] = float(a_min)
+        v["accel_inv"] = float(counts[-2] / (a_max - a_min)) if a_max > a_min else 0.0
+        v["freq_min"] = float(f_min)
+        v["freq_inv"] = float(counts[-1] / (f_max - f_min)) if f_max > f_min else 0.0
+        return arr
 
     def _level_desc(self, level: int) -> _lib.LokiPruneLevel:
         cfg = self.dyp.cfg
