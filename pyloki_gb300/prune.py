@@ -441,7 +441,7 @@ class Pruning:
         the Taylor basis every level of the segment is built at once
         (``_level_descs_taylor``)."""
         cache = self.__dict__.setdefault("_desc_cache", {})
-        if self.poly_basis == "taylor" and not self.circular:
+        if self.poly_basis == "taylor":
             akey = ("taylor_all", self.scheme.ref_idx, self.use_moving_grid)
             if akey not in cache:
                 cache[akey] = self._level_descs_taylor(max(self.dyp.nsegments - 1, 1))
@@ -452,9 +452,9 @@ class Pruning:
         return cache[key]
 
     def _level_descs_taylor(self, nlev: int):
-        """``_level_desc`` for levels 1..nlev of the Taylor basis in one
-        vectorised pass (the same element-wise operations, so the same
-        values), as a ctypes array of descriptors."""
+        """``_level_desc`` for levels 1..nlev of the Taylor basis (plain or
+        circular-orbit tree) in one vectorised pass (the same element-wise
+        operations, so the same values), as a ctypes array of descriptors."""
         cfg = self.dyp.cfg
         sc = self.scheme
         moving = self.use_moving_grid
@@ -493,6 +493,18 @@ class Pruning:
         else:
             v["tm_a"][:, :n, :n] = taylor_matrices(add[:, 0] - c_init[0], n)
         v["dt_phase"] = add[:, 0] - c_init[0]
+        if self.circular:  # dynamic/dyn_circular_taylor.py:341-385, config.py:475-481
+            v["basis"] = 2
+            v["circ_sig_prop"] = float(cfg.propagator_significance)
+            v["circ_sig_valid"] = float(cfg.validation_significance)
+            v["circ_omega_max_sq"] = float((2 * np.pi / cfg.p_orb_min) ** 2)
+            v["circ_x_mass"] = float(cfg.x_mass_const)
+            if moving:
+                v["circ_dt_add"] = add[:, 0] - cur[:, 0]
+                v["circ_dt_init"] = c_init[0] - cur[:, 0]
+                v["circ_dt_next"] = nxt[:, 0] - cur[:, 0]
+            else:
+                v["circ_dt_add"] = add[:, 0] - c_init[0]
         counts = self.param_grid_count_init
         lim = cfg.param_limits
         v["n_accel"], v["n_freq"] = int(counts[-2]), int(counts[-1])
