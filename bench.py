@@ -73,7 +73,7 @@ def cpu_band_cfg(band_hz: float):
 
 PRUNE_WORKLOAD = "taylor4_prune_circular_orbit_2^22"
 PRUNE_MAX_SUGG = 2**18
-PRUNE_MULTI_RUNS = 8   # reference segments of the multi-run measurement
+PRUNE_MULTI_RUNS = 16   # reference segments of the multi-run measurement
 PRUNE_WORKERS = 4      # concurrent runs (host threads and CUDA streams)
 PRUNE_BATCH = 1024
 PRUNE_THRESHOLD_FINAL = 4.0
@@ -214,9 +214,9 @@ def bench_prune_gpu(args, dev) -> dict:
     # concurrent host threads and streams overlap one another's host waits
     from pyloki_gb300.prune import run_many
 
-    refs = [int(r) for r in np.linspace(8, nseg - 8, PRUNE_MULTI_RUNS).round()]
+    refs = [int(r) for r in np.linspace(8, nseg - 8, args.prune_runs).round()]
     multi = {}
-    for nw in (1, PRUNE_WORKERS):
+    for nw in (1, args.prune_workers):
         run_many(dyp, thr, refs[:nw], n_workers=nw, max_sugg=PRUNE_MAX_SUGG,
                  batch_size=PRUNE_BATCH)  # warm-up of the worker streams
         torch.cuda.synchronize(dev)
@@ -229,7 +229,7 @@ def bench_prune_gpu(args, dev) -> dict:
         multi[f"workers_{nw}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
     multi["runs"] = len(refs)
     multi["ref_segments"] = refs
-    multi["speedup"] = (multi[f"workers_{PRUNE_WORKERS}"]["leaves_per_s"]
+    multi["speedup"] = (multi[f"workers_{args.prune_workers}"]["leaves_per_s"]
                         / multi["workers_1"]["leaves_per_s"])
     return {
         "metric": "prune leaves/s", "value": leaves / (ms * 1e-3), "unit": "leaves/s",
@@ -986,6 +986,10 @@ def main() -> None:
                     help="series of the seeded 256-series batch to search")
     ap.add_argument("--profile-inject-once", action="store_true",
                     help="one untimed 64-injection set (the generator ncu command)")
+    ap.add_argument("--prune-workers", type=int, default=PRUNE_WORKERS,
+                    help="host threads (each with its own stream) of the multi-run pruning")
+    ap.add_argument("--prune-runs", type=int, default=PRUNE_MULTI_RUNS,
+                    help="reference segments of the multi-run pruning")
     ap.add_argument("--no-injections", action="store_true",
                     help="skip the synthetic injection-set section")
     ap.add_argument("--injections", type=int, default=1024,
