@@ -110,6 +110,19 @@ int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
                    void* phase_scratch, int64_t scratch_bytes,
                    float* fold_out, void* stream);
 
+/* loki_brutefold for a series whose ts_v is all ones (the normalised series
+ * io/timeseries.py:198-236 from_tim produces). Every variance sum of the
+ * reference is then the bin's sample count, exact in float32, and the same
+ * for every full segment: it is written from one histogram of the phase map
+ * per frequency, and only the ts_e sums run sample by sample (half the
+ * shared memory per thread). The fold is bit-identical to loki_brutefold's
+ * with ts_v = 1. segment_len < 2^24. No reference counterpart as an entry
+ * point. */
+int loki_brutefold_unit_variance(const float* ts_e, int64_t nsamps, const double* freqs,
+                                 int64_t nfreqs, int64_t segment_len, int32_t nbins,
+                                 double tsamp, double t_ref, void* phase_scratch,
+                                 int64_t scratch_bytes, float* fold_out, void* stream);
+
 /* loki_brutefold without a caller-supplied phase scratch and without any
  * device allocation: no counterpart in the reference. For callers that may
  * not allocate device memory: cudaMalloc and cudaFree synchronise the whole

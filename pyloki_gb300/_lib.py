@@ -191,6 +191,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_last_error": (C.c_char_p, []),
     "loki_launch_count": (C.c_int64, []),
     "loki_brutefold": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _I64, _P, _P]),
+    "loki_brutefold_unit_variance": (C.c_int, [_P, _I64, _P, _I64, _I64, _I32, _D, _D, _P,
+                                                _I64, _P, _P]),
     "loki_brutefold_noalloc": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
     "loki_brutefold_noalloc_scratch_bytes": (C.c_int64, []),
     "loki_ffa_plan": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P]),

@@ -162,13 +162,17 @@ class _ChunkGraph:
     its top-k captured in a CUDA graph."""
 
     def __init__(self, cfg: PulsarSearchConfig, nbatch: int, k: int, band_bytes: int,
-                 storage: str, device: torch.device, use_graph: bool) -> None:
+                 storage: str, device: torch.device, use_graph: bool,
+                 unit_variance: bool = False) -> None:
         self.cfg, self.nbatch, self.k = cfg, nbatch, k
         self.band_bytes, self.storage, self.device = band_bytes, storage, device
         self.ts_e = torch.zeros(nbatch * cfg.nsamps, dtype=torch.float32, device=device)
         self.ts_v = torch.ones(nbatch * cfg.nsamps, dtype=torch.float32, device=device)
+        # the flag holds for every series this graph will see (decided by the
+        # caller over all of them), not just the warm-up buffers
         self.dyp = DynamicProgramming(TimeSeries(self.ts_e, self.ts_v, cfg.tsamp), cfg,
-                                      device=device, storage=storage, nbatch=nbatch)
+                                      device=device, storage=storage, nbatch=nbatch,
+                                      unit_variance=unit_variance)
         # grids referenced by raw pointers in the captured launches stay alive here
         self._grids = [self.dyp._grid(level) for level in range(cfg.niters_ffa + 1)]
         self.graph: torch.cuda.CUDAGraph | None = None
@@ -256,6 +260,9 @@ class BatchedSearch:
         self.k, self.storage, self.rescore = k, storage, rescore
         self.use_graphs, self.tuner = use_graphs, tuner
         self.chunk, self.band_bytes, self.mem_fraction = chunk, band_bytes, mem_fraction
+        # every series has ts_v all ones: the brute folds count instead of summing
+        self.unit_variance = all(bool(np.all(np.asarray(
+            ts.ts_v.cpu() if torch.is_tensor(ts.ts_v) else ts.ts_v) == 1.0)) for ts in self.series)
         self.groups: dict[int, list[int]] = {}
         for i, ts in enumerate(self.series):
             self.groups.setdefault(pow2_length(len(ts.ts_e)), []).append(i)
@@ -280,7 +287,8 @@ class BatchedSearch:
         g = self._graphs.get(key)
         if g is None:
             g = self._graphs[key] = _ChunkGraph(self._cfgs[n], nbatch, self.k, band_bytes,
-                                                self.storage, self.device, self.use_graphs)
+                                                self.storage, self.device, self.use_graphs,
+                                                self.unit_variance)
         return g
 
     def prepare(self) -> None:
@@ -292,7 +300,7 @@ class BatchedSearch:
             if self.tuner is not None:
                 def time_fn(c: int, b: int, n=n) -> float:
                     g = _ChunkGraph(cfg, c, self.k, b, self.storage, self.device,
-                                    use_graph=False)
+                                    use_graph=False, unit_variance=self.unit_variance)
                     g.load([self.series[i] for i in ids[:c]])
                     torch.cuda.synchronize(self.device)
                     t0 = torch.cuda.Event(enable_timing=True)

@@ -136,7 +136,8 @@ class DynamicProgramming:
     """
 
     def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None,
-                 storage: str = "f32", nbatch: int = 1) -> None:
+                 storage: str = "f32", nbatch: int = 1,
+                 unit_variance: bool | None = None) -> None:
         if cfg.use_fourier and cfg.nbins % 2:
             msg = "the Fourier-domain FFA needs an even nbins (irfft length)"
             raise ValueError(msg)
@@ -148,6 +149,9 @@ class DynamicProgramming:
             raise ValueError(msg)
         self._storage, self._fold_dtype = STORAGES[storage]
         self.storage = storage
+        # ts_v all ones: the brute fold takes the variance sums from sample
+        # counts. None: decided from the series at the first initialize.
+        self._unit_var = unit_variance
         if nbatch < 1:
             msg = "nbatch must be >= 1"
             raise ValueError(msg)
@@ -289,10 +293,15 @@ class DynamicProgramming:
             self._err.zero_()
             self._ffa_level = 0
             return
+        if self._unit_var is None:
+            src = self.ts_data.ts_v
+            self._unit_var = (bool((ts_v == 1.0).all()) if torch.is_tensor(src)
+                              else bool(np.all(np.asarray(src) == 1.0)))
         self._fold, nl = _brutefold(ts_e, ts_v, g0.dev[-1], cfg.bseg_brute, cfg.nbins,
                                     cfg.tsamp, 0.0 if cfg.nparams == 1 else
                                     cfg.bseg_brute * cfg.tsamp / 2,
-                                    scratch_bytes=self.phase_scratch_bytes)
+                                    scratch_bytes=self.phase_scratch_bytes,
+                                    unit_variance=self._unit_var)
         self.launches += nl
         nseg, nfreq = self._fold.shape[:2]
         if self._storage:
@@ -562,21 +571,22 @@ _BAND_CACHE: dict[tuple, tuple] = {}
 
 
 def _brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref=0.0, *,
-               scratch_bytes=_GIB) -> tuple[torch.Tensor, int]:
+               scratch_bytes=_GIB, unit_variance: bool = False) -> tuple[torch.Tensor, int]:
     """Brute fold plus the number of kernels it launched."""
     lib = _lib.load()
     before = lib.loki_launch_count()
     fold = brutefold(ts_e, ts_v, freqs, segment_len, nbins, tsamp, t_ref,
-                     scratch_bytes=scratch_bytes)
+                     scratch_bytes=scratch_bytes, unit_variance=unit_variance)
     return fold, lib.loki_launch_count() - before
 
 
 def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segment_len: int,
               nbins: int, tsamp: float, t_ref: float = 0.0, *,
-              scratch_bytes: int = _GIB) -> torch.Tensor:
+              scratch_bytes: int = _GIB, unit_variance: bool = False) -> torch.Tensor:
     """Fold ``(nsegments, nfreqs, 2, nbins)`` (``core/fold.py:108-171``).
     ``scratch_bytes`` bounds the phase map; frequencies beyond it are folded
-    in chunks."""
+    in chunks. ``unit_variance``: the caller asserts ``ts_v`` is all ones,
+    and the variance sums come from sample counts (the same values)."""
     lib = _lib.load()
     nsamps = ts_e.numel()
     nseg = math.ceil(nsamps / segment_len)
@@ -587,6 +597,11 @@ def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segme
                           dtype=torch.uint8, device=ts_e.device)
     fold = torch.empty((nseg, nfreq, 2, nbins), dtype=torch.float32, device=ts_e.device)
     stream = _lib.stream_ptr(torch.cuda.current_stream(ts_e.device))
+    if unit_variance:
+        _lib.check(lib.loki_brutefold_unit_variance(
+            _lib.ptr(ts_e), nsamps, _lib.ptr(freqs), nfreq, segment_len, nbins, tsamp, t_ref,
+            _lib.ptr(scratch), scratch.numel(), _lib.ptr(fold), stream))
+        return fold
     _lib.check(lib.loki_brutefold(_lib.ptr(ts_e), _lib.ptr(ts_v), nsamps, _lib.ptr(freqs),
                                   nfreq, segment_len, nbins, tsamp, t_ref,
                                   _lib.ptr(scratch), scratch.numel(), _lib.ptr(fold),
