@@ -50,13 +50,14 @@ BATCH_SERIES = 32    # bounded sample of the 256-series batch (first series of t
 BATCH_K = 16         # candidates kept per series
 
 
-def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0):
+def make_cfg(freq_lo: float = 50.0, freq_hi: float = 500.0, nsamps: int = 2**23,
+             use_fourier: bool = False):
     from pyloki_gb300 import ParamLimits, PulsarSearchConfig
 
     return PulsarSearchConfig(
-        nsamps=2**23, tsamp=64e-6, nbins=64, eta=1.0,
+        nsamps=nsamps, tsamp=64e-6, nbins=64, eta=1.0,
         param_limits=ParamLimits.from_taylor((freq_lo, freq_hi), accel=(-50.0, 50.0)).limits,
-        ducy_max=0.25, wtsp=2.0, use_fourier=False, bseg_brute=16384)
+        ducy_max=0.25, wtsp=2.0, use_fourier=use_fourier, bseg_brute=16384)
 
 
 def make_series(seed: int):
@@ -522,6 +523,8 @@ def bench_gpu(args) -> dict | None:
         out["batch"] = bench_batch(args, dev)
     if not args.no_injections:
         out["injection"] = bench_injections(args, dev, peak)
+    if not args.no_fourier:
+        out["ffa_fourier"] = bench_fourier(args, dev)
     if not args.no_prune:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
@@ -537,6 +540,51 @@ def bench_gpu(args) -> dict | None:
 
 
 INJ_NSAMPS = 2**21
+FOURIER_NSAMPS = 2**20
+
+
+def bench_fourier(args, dev) -> dict:
+    """The Fourier-domain FFA (the reference's default, use_fourier=True) on
+    the benchmark's acceleration grid at 2^20 samples, where every level can
+    be materialised: complex brute fold, complex shift-add levels, irfft
+    normalisation and boxcar S/N of every final trial. The time-domain search
+    of the same grid is timed beside it."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.simulation import make_series as ms
+
+    ts = ms(FOURIER_NSAMPS, 64e-6, freq=200.0, snr=15.0, ducy=0.05, accel=20.0, seed=1001)
+    out = {"workload": "ffa_accel_search_2^20 (50-500 Hz, +-50 m/s^2, 64 bins)"}
+    for name, fourier in (("fourier", True), ("time_domain", False)):
+        cfg = make_cfg(nsamps=FOURIER_NSAMPS, use_fourier=fourier)
+        dyp = DynamicProgramming(ts, cfg, device=dev)
+        trials = int(np.prod(cfg.get_param_grid_count(cfg.niters_ffa)))
+
+        def step():
+            dyp.reset()
+            return dyp.search(mode=1)
+
+        for _ in range(max(args.warmup, 1)):
+            step()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            snr = step()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        ms_step = e0.elapsed_time(e1) / args.steps
+        best = float(torch.nan_to_num(snr, nan=float("-inf")).max())
+        marks: list = []
+        dyp.reset()
+        dyp.search(mode=1, phase_events=marks)
+        torch.cuda.synchronize(dev)
+        phases = {marks[i][0]: marks[i - 1][1].elapsed_time(marks[i][1])
+                  for i in range(1, len(marks))}
+        out[name] = {"trials_per_s": trials / (ms_step * 1e-3), "ms_per_step": ms_step,
+                     "trials": trials, "best_snr": best, "phases_ms": phases}
+    return out
 
 
 def injection_cfgs(n: int, seed: int = 4000):
@@ -990,6 +1038,8 @@ def main() -> None:
                     help="host threads (each with its own stream) of the multi-run pruning")
     ap.add_argument("--prune-runs", type=int, default=PRUNE_MULTI_RUNS,
                     help="reference segments of the multi-run pruning")
+    ap.add_argument("--no-fourier", action="store_true",
+                    help="skip the Fourier-domain FFA section")
     ap.add_argument("--no-injections", action="store_true",
                     help="skip the synthetic injection-set section")
     ap.add_argument("--injections", type=int, default=1024,

@@ -18,7 +18,7 @@ namespace loki {
 // f_h * float32(t * float32(-2 pi tsamp)); then the t_ref phase correction
 // exp(i float32(2 pi t_ref) f_h). One thread owns one (frequency, harmonic)
 // and kSegs segments, so each basis value serves kSegs segments.
-constexpr int kSegs = 8;
+constexpr int kSegs = 16;
 
 __global__ void __launch_bounds__(128)
 brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict__ ts_v,
@@ -57,7 +57,9 @@ brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict
   const float th = __fmul_rn(corr_factor, fh);
   float cs_c, sn_c;
   sincosf(th, &sn_c, &cs_c);
-  for (int k = 0; k < ns; ++k) {
+#pragma unroll
+  for (int k = 0; k < kSegs; ++k) {  // constant indices keep the sums in registers
+    if (k >= ns) break;
     float2* row = fold + ((s0 + k) * nfreq + fi) * 2 * nbf;
     row[h] = make_float2(__fsub_rn(__fmul_rn(er[k], cs_c), __fmul_rn(ei[k], sn_c)),
                          __fadd_rn(__fmul_rn(er[k], sn_c), __fmul_rn(ei[k], cs_c)));
@@ -112,8 +114,22 @@ __global__ void ffa_level_complex_kernel(const LokiFFACoord* __restrict__ plan, 
 // get_fold_norm for Fourier folds (ffa.py:401-411): irfft of each component
 // (nbins real samples from nbins_f coefficients, computed in float64 with
 // exact twiddles and rounded to float32), then e / sqrt(v).
+// irfft (numpy, n = nbins) of each component, then e / sqrt(v). Twiddle
+// factors cos/sin(2 pi r / nbins) depend only on r = (m j) mod nbins: a block
+// fills a float32 table of nbins entries (float64 sincospi, rounded once) and
+// every term reads it; the sums run in float32 with fused multiply-adds, as
+// numpy's float32 transform of a complex64 fold does (float64 sums would
+// leave the FP64 pipe, a small fraction of GB300's float32 rate, the limit).
 __global__ void fold_norm_complex_kernel(const float2* __restrict__ folds, int64_t n, int nbins,
                                          int nbf, float* __restrict__ out) {
+  extern __shared__ float tw[];  // [nbins] cos, [nbins] sin
+  for (int r = threadIdx.x; r < nbins; r += blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)r / (double)nbins, &s, &c);
+    tw[r] = (float)c;
+    tw[nbins + r] = (float)s;
+  }
+  __syncthreads();
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= n * nbins) return;
   const int64_t p = k / nbins;
@@ -121,18 +137,23 @@ __global__ void fold_norm_complex_kernel(const float2* __restrict__ folds, int64
   float val[2];
   for (int c = 0; c < 2; ++c) {
     const float2* x = folds + (p * 2 + c) * nbf;
-    double acc = (double)x[0].x;
+    float acc = x[0].x;
+    int r = 0;
     for (int m = 1; m < nbf; ++m) {
-      // irfft (numpy, n = nbins): the imaginary parts of the DC and (for even
-      // nbins) Nyquist terms are ignored; other terms count twice.
-      const bool edge = (2 * m == nbins);
-      double s, cth;
-      sincospi(2.0 * (double)((int64_t)m * j % nbins) / (double)nbins, &s, &cth);
-      const double re = (double)x[m].x, im = (double)x[m].y;
-      const double term = edge ? re * cth : 2.0 * (re * cth - im * s);
-      acc += term;
+      // the imaginary parts of the DC and (for even nbins) Nyquist terms are
+      // ignored; other terms count twice
+      r += j;
+      if (r >= nbins) r -= nbins;
+      const float cth = tw[r], s = tw[nbins + r];
+      const float2 xm = x[m];
+      if (2 * m == nbins) {
+        acc = __fmaf_rn(xm.x, cth, acc);
+      } else {
+        acc = __fmaf_rn(2.0f * xm.x, cth, acc);
+        acc = __fmaf_rn(-2.0f * xm.y, s, acc);
+      }
     }
-    val[c] = (float)(acc / (double)nbins);
+    val[c] = __fdiv_rn(acc, (float)nbins);
   }
   out[k] = __fdiv_rn(val[0], __fsqrt_rn(val[1]));
 }
@@ -196,8 +217,10 @@ extern "C" int loki_fold_norm_complex(const void* folds, int64_t n, int32_t nbin
   if (n == 0) return LOKI_OK;
   if (!folds || !out) return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const int64_t total = n * nbins;
+  if (nbins > 8192) return set_error(LOKI_ERR_UNSUPPORTED, "nbins above 8192");
   note_launch();
-  fold_norm_complex_kernel<<<(unsigned)((total + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+  fold_norm_complex_kernel<<<(unsigned)((total + 255) / 256), 256, 8 * nbins,
+                             (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(folds), n, nbins, nbins / 2 + 1, out);
   return check_launch("fold_norm_complex");
 }
