@@ -975,6 +975,25 @@ def profile_once(args) -> None:
                       "launches": dyp.launches, "snr_shape": list(snr.shape)}))
 
 
+def profile_fourier_once(args) -> None:
+    """One Fourier-domain search of the benchmark grid at 2^20 samples after a
+    warm-up, with no timing; the command the Fourier ncu summaries use."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.simulation import make_series as ms
+
+    cfg = make_cfg(nsamps=FOURIER_NSAMPS, use_fourier=True)
+    ts = ms(FOURIER_NSAMPS, 64e-6, freq=200.0, snr=15.0, ducy=0.05, accel=20.0, seed=1001)
+    dyp = DynamicProgramming(ts, cfg, device=torch.device("cuda", 0))
+    for _ in range(2):
+        dyp.reset()
+        snr = dyp.search(mode=1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_fourier_once": True, "nsamps": FOURIER_NSAMPS,
+                      "best_snr": float(torch.nan_to_num(snr, nan=-1.0).max())}))
+
+
 def profile_inject_once(args) -> None:
     """One injection set of 64 x 2^21 samples after a warm-up, with no timing;
     the command the generator's ncu summaries are captured from."""
@@ -1032,6 +1051,8 @@ def main() -> None:
                     help="skip the batched multi-series measurement")
     ap.add_argument("--batch-series", type=int, default=BATCH_SERIES,
                     help="series of the seeded 256-series batch to search")
+    ap.add_argument("--profile-fourier-once", action="store_true",
+                    help="two untimed Fourier-domain searches at 2^20 (the Fourier ncu command)")
     ap.add_argument("--profile-inject-once", action="store_true",
                     help="one untimed 64-injection set (the generator ncu command)")
     ap.add_argument("--prune-workers", type=int, default=PRUNE_WORKERS,
@@ -1072,6 +1093,9 @@ def main() -> None:
         return
     if args.profile_inject_once:
         profile_inject_once(args)
+        return
+    if args.profile_fourier_once:
+        profile_fourier_once(args)
         return
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
