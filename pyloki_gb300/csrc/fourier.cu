@@ -20,6 +20,26 @@ namespace loki {
 // and kSegs segments, so each basis value serves kSegs segments.
 constexpr int kSegs = 16;
 
+// sin and cos of a float32 angle by Cody and Waite's additive reduction
+// ("Software Manual for the Elementary Functions", 1980): 2 pi split into
+// three float32 parts, the first two with 8 significant bits so that k times
+// them is exact for |k| < 2^15 (angles up to about 2e5 rad), subtracted with
+// fused multiply-adds; sincosf of the reduced angle then stays on its short
+// path. The parts come from 2 pi to 60 digits: 0x1.92p+2 + 0x1.fbp-10 +
+// 0x1.5110b4p-20 (their sum is 2 pi to 2e-14).
+__device__ __forceinline__ void sincos_reduced(float a, float* s, float* c) {
+  constexpr float kC1 = 0x1.92p+2f, kC2 = 0x1.fbp-10f, kC3 = 0x1.5110b4p-20f;
+  const float k = rintf(__fmul_rn(a, 0.15915494f));
+  if (fabsf(k) < 32768.0f) {
+    float r = __fmaf_rn(-k, kC1, a);
+    r = __fmaf_rn(-k, kC2, r);
+    r = __fmaf_rn(-k, kC3, r);
+    sincosf(r, s, c);
+  } else {
+    sincosf(a, s, c);
+  }
+}
+
 __global__ void __launch_bounds__(128)
 brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict__ ts_v,
                          const double* __restrict__ freqs, int64_t nfreq, int64_t seg_len,
@@ -40,7 +60,7 @@ brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict
     const float tv = __fmul_rn((float)t, tfac);
     const float ang = __fmul_rn(fh, tv);
     float sn, cs;
-    sincosf(ang, &sn, &cs);
+    sincos_reduced(ang, &sn, &cs);
 #pragma unroll
     for (int k = 0; k < kSegs; ++k) {
       if (k < ns) {
@@ -56,7 +76,7 @@ brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict
   // correction phasor exp(i * float32(corr_factor * f_h)), complex64 multiply
   const float th = __fmul_rn(corr_factor, fh);
   float cs_c, sn_c;
-  sincosf(th, &sn_c, &cs_c);
+  sincos_reduced(th, &sn_c, &cs_c);
 #pragma unroll
   for (int k = 0; k < kSegs; ++k) {  // constant indices keep the sums in registers
     if (k >= ns) break;
