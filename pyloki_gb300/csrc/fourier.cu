@@ -56,7 +56,39 @@ brutefold_complex_kernel(const float* __restrict__ ts_e, const float* __restrict
   float er[kSegs], ei[kSegs], vr[kSegs], vi[kSegs];
 #pragma unroll
   for (int k = 0; k < kSegs; ++k) er[k] = ei[k] = vr[k] = vi[k] = 0.0f;
-  for (int64_t t = 0; t < seg_len; ++t) {
+  int64_t t = 0;
+  // four samples per step with 16-byte (broadcast) loads of each segment;
+  // every accumulator still takes its terms in sample order
+  const bool vec = (seg_len & 3) == 0 &&
+                   ((reinterpret_cast<uintptr_t>(ts_e) | reinterpret_cast<uintptr_t>(ts_v)) &
+                    15) == 0;
+  if (vec) {
+    for (; t < seg_len; t += 4) {
+      float sn[4], cs[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float tv = __fmul_rn((float)(t + q), tfac);
+        sincos_reduced(__fmul_rn(fh, tv), &sn[q], &cs[q]);
+      }
+#pragma unroll
+      for (int k = 0; k < kSegs; ++k) {
+        if (k < ns) {
+          const int64_t at = (s0 + k) * seg_len + t;
+          const float4 xe = __ldg(reinterpret_cast<const float4*>(ts_e + at));
+          const float4 xv = __ldg(reinterpret_cast<const float4*>(ts_v + at));
+          const float e4[4] = {xe.x, xe.y, xe.z, xe.w}, v4[4] = {xv.x, xv.y, xv.z, xv.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            er[k] = fmaf(e4[q], cs[q], er[k]);
+            ei[k] = fmaf(e4[q], sn[q], ei[k]);
+            vr[k] = fmaf(v4[q], cs[q], vr[k]);
+            vi[k] = fmaf(v4[q], sn[q], vi[k]);
+          }
+        }
+      }
+    }
+  }
+  for (; t < seg_len; ++t) {
     const float tv = __fmul_rn((float)t, tfac);
     const float ang = __fmul_rn(fh, tv);
     float sn, cs;
