@@ -228,7 +228,9 @@ int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, const float* t
 /* Complex brute fold (core/fold.py:395-481 brutefold_start_complex_opt, via
  * ffa_taylor_init_complex 572-614): the DFT of every segment at the
  * harmonics h * f, h = 0 .. nbins / 2, with the t_ref phase correction.
- * nsamps must be a multiple of segment_len. */
+ * nsamps must be a multiple of segment_len. ts_v may be NULL, meaning all
+ * ones: the variance sums are then the same for every segment and are taken
+ * once (the same values). */
 int loki_brutefold_complex(const float* ts_e, const float* ts_v, int64_t nsamps,
                            const double* freqs, int64_t nfreqs, int64_t segment_len,
                            int32_t nbins, double tsamp, double t_ref, void* fold_out,

@@ -280,23 +280,24 @@ class DynamicProgramming:
             raise ValueError(msg)
         self._ts_dev = (ts_e, ts_v)
         t_ref = 0.0 if cfg.nparams == 1 else cfg.bseg_brute * cfg.tsamp / 2
+        if self._unit_var is None:
+            src = self.ts_data.ts_v
+            self._unit_var = (bool((ts_v == 1.0).all()) if torch.is_tensor(src)
+                              else bool(np.all(np.asarray(src) == 1.0)))
         if cfg.use_fourier:  # core/fold.py:395-481,572-614
             nseg = ts_e.numel() // cfg.bseg_brute
             nfreq = g0.dev[-1].numel()
             nbf = cfg.nbins // 2 + 1
             fold = torch.empty((nseg, nfreq, 2, nbf), dtype=torch.complex64, device=dev)
             _lib.check(self._lib.loki_brutefold_complex(
-                _lib.ptr(ts_e), _lib.ptr(ts_v), ts_e.numel(), _lib.ptr(g0.dev[-1]), nfreq,
+                _lib.ptr(ts_e), 0 if self._unit_var else _lib.ptr(ts_v), ts_e.numel(),
+                _lib.ptr(g0.dev[-1]), nfreq,
                 cfg.bseg_brute, cfg.nbins, cfg.tsamp, t_ref, _lib.ptr(fold), self._stream()))
             self.launches += 1
             self._fold = fold.reshape(nseg, *([1] * (cfg.nparams - 1)), nfreq, 2, nbf)
             self._err.zero_()
             self._ffa_level = 0
             return
-        if self._unit_var is None:
-            src = self.ts_data.ts_v
-            self._unit_var = (bool((ts_v == 1.0).all()) if torch.is_tensor(src)
-                              else bool(np.all(np.asarray(src) == 1.0)))
         self._fold, nl = _brutefold(ts_e, ts_v, g0.dev[-1], cfg.bseg_brute, cfg.nbins,
                                     cfg.tsamp, 0.0 if cfg.nparams == 1 else
                                     cfg.bseg_brute * cfg.tsamp / 2,

@@ -60,3 +60,23 @@ def test_dynamic_programming_detects_unit_variance(cuda_device):
                                device=cuda_device)
     dev_v.initialize()
     assert dev_v._unit_var
+
+
+def test_complex_fold_unit_variance_equals_general(cuda_device):
+    """ts_v NULL (all ones) gives the same complex fold as ts_v = ones."""
+    from pyloki_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(9)
+    n, seg, nbins = 2**14 * 5, 2**14, 64
+    e = torch.from_numpy(rng.standard_normal(n).astype(np.float32)).to(cuda_device)
+    v = torch.ones(n, dtype=torch.float32, device=cuda_device)
+    freqs = torch.from_numpy(np.linspace(5.0, 60.0, 23)).to(cuda_device)
+    out = [torch.empty((n // seg, 23, 2, nbins // 2 + 1), dtype=torch.complex64,
+                       device=cuda_device) for _ in range(2)]
+    stream = _lib.stream_ptr(torch.cuda.current_stream(cuda_device))
+    for vp, o in ((v, out[0]), (None, out[1])):
+        _lib.check(lib.loki_brutefold_complex(_lib.ptr(e), _lib.ptr(vp), n, _lib.ptr(freqs), 23,
+                                              seg, nbins, 1e-3, 0.5 * seg * 1e-3, _lib.ptr(o),
+                                              stream))
+    assert torch.equal(out[0], out[1])
