@@ -133,6 +133,14 @@ class DynamicProgramming:
         per series. Each series must end in one final segment
         (``nsamps == bseg_brute * 2**niters_ffa``), so no segment pair spans
         two series.
+    unit_variance : bool or None
+        ``ts_v`` is all ones: the brute folds take the variance sums from
+        sample counts (time domain) or once for all segments (Fourier
+        domain), the same values. None (default) checks the series once at
+        the first ``initialize``. True asserts the property without checking,
+        for callers that reuse the object for other series (``BatchedSearch``
+        decides over all of its series); with a ``ts_v`` that is not all ones
+        the variance sums would be wrong.
     """
 
     def __init__(self, ts_data: TimeSeries, cfg: PulsarSearchConfig, *, device=None,
