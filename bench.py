@@ -1082,6 +1082,8 @@ def main() -> None:
                     help="run exactly one search (for ncu captures) and exit")
     ap.add_argument("--profile-prune-once", action="store_true",
                     help="run the pruning workload twice (warm-up + one run) and exit")
+    ap.add_argument("--detail-out", default=None,
+                    help="also write the full result (every side study) to this JSON file")
     ap.add_argument("--nsamps-log2", type=int, default=23,
                     help="series length for --profile-once (smaller ncu cases)")
     args = ap.parse_args()
@@ -1100,8 +1102,77 @@ def main() -> None:
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     out = bench_reference(args) if args.impl == "reference" else bench_gpu(args)
-    if out is not None:
-        print(json.dumps(out), flush=True)
+    if out is None:
+        return
+    if args.detail_out:
+        Path(args.detail_out).parent.mkdir(parents=True, exist_ok=True)
+        Path(args.detail_out).write_text(json.dumps(out, indent=1))
+    # one line per side study first, the compact headline last
+    for key in SECTIONS:
+        if key in out:
+            print(json.dumps({"section": key, **_compact_section(out[key])}), flush=True)
+    if isinstance(out.get("prune"), dict):
+        for key in ("multi_run", "learned"):
+            if isinstance(out["prune"].get(key), dict):
+                print(json.dumps({"section": f"prune.{key}",
+                                  **_compact_section(out["prune"][key])}), flush=True)
+    print(json.dumps(headline(out)), flush=True)
+
+
+# side studies printed on their own lines before the headline
+SECTIONS = ("ffa_bf16", "ffa_precision", "batch", "injection", "ffa_fourier", "threshold_design")
+HEADLINE_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "impl",
+                 "gpu_launches", "clocks")
+
+
+def _round(x):
+    if isinstance(x, float):
+        return float(f"{x:.6g}")
+    if isinstance(x, dict):
+        return {k: _round(v) for k, v in x.items()}
+    if isinstance(x, list):
+        return [_round(v) for v in x]
+    return x
+
+
+def _compact_section(sec: dict) -> dict:
+    """A side study without its long per-item lists (kept in the detail file)."""
+    return _round({k: v for k, v in sec.items()
+                   if not (isinstance(v, list) and len(v) > 8)})
+
+
+def headline(out: dict) -> dict:
+    """The last stdout line: the period-trials/s headline with its roofline,
+    CPU baseline and end-to-end figures, and the prune leaves/s headline as a
+    small sub-object; a few hundred bytes to about 2 KB."""
+    h = {k: out[k] for k in HEADLINE_KEYS if k in out}
+    cfg = out.get("config", {})
+    h["config"] = {k: cfg[k] for k in ("workload", "nsamps", "trials_per_step", "final_grid",
+                                       "widths", "l2", "parallelism", "sample_band_hz")
+                   if k in cfg}
+    for k in ("roofline", "cpu_baseline", "e2e"):
+        if k in out:
+            h[k] = {kk: vv for kk, vv in out[k].items()
+                    if kk not in ("traffic_source", "sample") or k == "cpu_baseline"}
+    if "prune" in out:
+        p = out["prune"]
+        sub = {k: p[k] for k in ("metric", "value", "unit", "ms_per_step", "leaves_per_step")
+               if k in p}
+        pc = p.get("config", {})
+        sub["config"] = {k: pc[k] for k in ("workload", "thresholds", "ref_segment") if k in pc}
+        for k in ("roofline", "cpu_baseline", "e2e"):
+            if k in p:
+                sub[k] = {kk: vv for kk, vv in p[k].items()
+                          if kk in ("kernel", "bound", "achieved", "peak", "unit", "frac",
+                                    "traffic", "value", "cores", "kind", "ms_per_step",
+                                    "h2d_bytes_per_step", "d2h_bytes_per_step", "sample")}
+        if "learned" in p and isinstance(p["learned"], dict):
+            lh = p["learned"].get("headline")
+            if lh:
+                sub["learned"] = lh
+        h["prune"] = sub
+    return _round(h)
 
 
 if __name__ == "__main__":

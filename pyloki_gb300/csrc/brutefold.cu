@@ -14,7 +14,6 @@
 // addresses). Blocks are ordered segment-fastest so that the map rows of the
 // frequencies in flight stay in L2 while every segment consumes them.
 #include <algorithm>
-#include <mutex>
 
 #include "loki_common.cuh"
 
@@ -233,10 +232,8 @@ static int brutefold_impl(const float* ts_e, const float* ts_v, bool unit, int64
   auto k8 = unit ? brutefold_seq_kernel<uint8_t, true> : brutefold_seq_kernel<uint8_t, false>;
   auto k16 =
       unit ? brutefold_seq_kernel<uint16_t, true> : brutefold_seq_kernel<uint16_t, false>;
-  if (cudaFuncSetAttribute(k8, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
+  if (set_smem_limit(k8, (int)smem) != cudaSuccess ||
+      set_smem_limit(k16, (int)smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int hsmem = 2 * nbins * (int)sizeof(int);
   for (int64_t f0 = 0; f0 < nfreqs; f0 += chunk) {
@@ -302,28 +299,16 @@ static constexpr int64_t kNoAllocScratchBytes = int64_t(16) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_phase_scratch[kNoAllocScratchBytes];
 
 namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices];
-
-// Device address of the array on the current device, looked up once per device.
+// Device address of the array in the current context. Looked up on every call
+// (the lookup allocates nothing): an address cached per device ordinal would
+// go stale after cudaDeviceReset or under a non-primary context.
 int noalloc_scratch(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess)
-    return set_error(LOKI_ERR_CUDA, "cudaGetDevice failed: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return set_error(LOKI_ERR_UNSUPPORTED, "device ordinal %d above %d", dev, kMaxDevices - 1);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_phase_scratch);
-    if (e != cudaSuccess || !p)
-      return set_error(LOKI_ERR_CUDA, "cudaGetSymbolAddress of the phase scratch failed: %s",
-                       cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_phase_scratch);
+  if (e != cudaSuccess || !p)
+    return set_error(LOKI_ERR_CUDA, "cudaGetSymbolAddress of the phase scratch failed: %s",
+                     cudaGetErrorString(e));
+  *out = p;
   return LOKI_OK;
 }
 }  // namespace

@@ -2,6 +2,10 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "loki_common.cuh"
 
 namespace loki {
@@ -17,6 +21,24 @@ int set_error(int code, const char* fmt, ...) {
   vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
   va_end(ap);
   return code;
+}
+
+// Largest dynamic shared-memory limit set so far per (device, kernel). The
+// limit is only ever raised, under one lock, so a host thread launching a
+// kernel with a smaller tile can never lower it below what another thread's
+// launch of the same kernel needs. The attribute is set on every call (a
+// context created after a device reset starts from the default again).
+static std::mutex g_smem_mu;
+static std::map<std::pair<int, const void*>, int> g_smem_limit;
+
+cudaError_t raise_smem_limit(const void* func, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  int& cur = g_smem_limit[{dev, func}];
+  if (bytes > cur) cur = bytes;
+  return cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, cur);
 }
 
 int check_launch(const char* what) {

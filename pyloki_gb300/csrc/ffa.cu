@@ -668,7 +668,7 @@ static int launch_level_score_t(const LokiFFALevel& L, const LevelK& K, const S*
   const int smem = score_smem_bytes(L.nbins, sp.wmax, warps);
   auto kern = fast ? ffa_level_score64_kernel<S> : ffa_level_score_kernel<S>;
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      set_smem_limit(kern, smem) !=
           cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t Q = n_out_params(L);
@@ -843,10 +843,8 @@ extern "C" int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel
     const int smem = score_smem_bytes(64, spec->wmax, kScoreWarps);
     const bool bf16 = fin->storage == 1;
     if (smem > 48 * 1024 &&
-        (bf16 ? cudaFuncSetAttribute(band_union64_kernel<__nv_bfloat16>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-              : cudaFuncSetAttribute(band_union64_kernel<float>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+        (bf16 ? set_smem_limit(band_union64_kernel<__nv_bfloat16>, smem)
+              : set_smem_limit(band_union64_kernel<float>, smem)) !=
             cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     P.out_start = win_lo[0];

@@ -23,6 +23,13 @@ int set_error(int code, const char* fmt, ...);
 int check_launch(const char* what);
 // Counts one kernel launch of this host thread (read by loki_launch_count).
 void note_launch();
+// Raises (never lowers) a kernel's dynamic shared-memory limit on the current
+// device to at least `bytes`; thread-safe (defined in capi.cu).
+cudaError_t raise_smem_limit(const void* func, int bytes);
+template <typename F>
+inline cudaError_t set_smem_limit(F* func, int bytes) {
+  return raise_smem_limit(reinterpret_cast<const void*>(func), bytes);
+}
 
 // Division by a runtime-constant 32-bit divisor d >= 1 with a precomputed
 // multiplier (Granlund & Montgomery 1994): q = (t + ((n - t) >> 1)) >> (l - 1),

@@ -518,8 +518,7 @@ extern "C" int loki_mlp_forward(const LokiMLP* w, const float* x, int64_t n, flo
   if (n == 0) return LOKI_OK;
   if (!x || !logits || !dev_err) return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const int smem = (int)sizeof(MlpSmem);
-  if (cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+  if (set_smem_limit(mlp_forward_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   note_launch();
   mlp_forward_kernel<<<mlp_grid(n), kTile, smem, (cudaStream_t)stream>>>(*w, x, n, logits,
@@ -539,8 +538,7 @@ extern "C" int loki_mlp_backward(const LokiMLP* w, const float* x, const float* 
       !grad->w3 || !grad->b3 || !grad->loss)
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   const int smem = (int)sizeof(MlpSmem);
-  if (cudaFuncSetAttribute(mlp_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+  if (set_smem_limit(mlp_backward_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   note_launch();
   mlp_backward_kernel<<<mlp_grid(n), kTile, smem, (cudaStream_t)stream>>>(

@@ -1920,8 +1920,7 @@ extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
     if (smem > 200 * 1024)
       return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(prune_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
+        set_smem_limit(prune_score_kernel, smem) != cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     const int64_t blocks = (n_children + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
@@ -2027,8 +2026,7 @@ extern "C" int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves
   const int smem = kPruneWarps * 32 * (2 * nb + score_stride(nb, sp.wmax)) * (int)sizeof(float);
   if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for ascend");
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(prune_ascend_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+      set_smem_limit(prune_ascend_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t blocks = (n + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
   note_launch();
@@ -2127,8 +2125,7 @@ extern "C" int loki_prune_circ_score(const LokiPruneLevel* lvl, const double* le
     if (smem > 200 * 1024)
       return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(circ_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
+        set_smem_limit(circ_score_kernel, smem) != cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     const int64_t blocks = (n_valid + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
@@ -2208,8 +2205,7 @@ extern "C" int loki_prune_circ_score_complex(
     rc = cplx_smem(lvl, sp, &smem);
     if (rc) return rc;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(circ_score_complex_kernel,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        set_smem_limit(circ_score_complex_kernel, smem) != cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     const int64_t blocks = (n_valid + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
@@ -2294,8 +2290,7 @@ extern "C" int loki_prune_score_complex(const LokiPruneLevel* lvl, const double*
     int smem = 0;
     rc = cplx_smem(lvl, sp, &smem);
     if (rc) return rc;
-    if (cudaFuncSetAttribute(prune_score_complex_kernel,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (set_smem_limit(prune_score_complex_kernel, smem) != cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     const int64_t blocks = (n_children + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
     if (blocks > 0x7FFFFFFF) return set_error(LOKI_ERR_UNSUPPORTED, "grid too large");
@@ -2355,8 +2350,7 @@ extern "C" int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double
   int smem = 0;
   rc = cplx_smem(lvl, sp, &smem);
   if (rc) return rc;
-  if (cudaFuncSetAttribute(prune_ascend_complex_kernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+  if (set_smem_limit(prune_ascend_complex_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t blocks = (n + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
   note_launch();

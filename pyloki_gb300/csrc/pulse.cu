@@ -497,8 +497,7 @@ extern "C" int loki_pulse_fold(const LokiPulseSpec* specs, int32_t ninj, int64_t
     const int use_smem = fold_stride <= kFoldSmemBins;
     const int smem = use_smem ? 20 * fold_stride : 0;
     if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(pulse_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
+        set_smem_limit(pulse_fold_kernel, smem) != cudaSuccess)
       return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
     // enough samples per block that the flush (3 * nbins atomics) stays small
     const int64_t pb =
@@ -529,8 +528,7 @@ extern "C" int loki_pulse_calibrate(const LokiPulseSpec* specs, int32_t ninj, co
   // nn, tn, prefix (n + n / 2) and the combined profile (n)
   const int smem = (4 * fold_stride + fold_stride / 2) * (int)sizeof(float);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(pulse_calibrate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+      set_smem_limit(pulse_calibrate_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   note_launch();
   pulse_calibrate_kernel<<<dim3(1, (unsigned)ninj), kCalibThreads, smem,

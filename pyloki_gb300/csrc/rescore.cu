@@ -200,9 +200,7 @@ extern "C" int loki_ffa_rescore(const LokiFFALevel* levels, int32_t nlevels, con
   A.t_ref = n == 1 ? 0.0 : (double)bseg_brute * tsamp / 2.0;  // ffa.py t_ref of the brute fold
   A.freqs0 = freqs0;
   const int smem = rescore_smem(nb, spec->wmax);
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(rescore_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               smem) != cudaSuccess)
+  if (smem > 48 * 1024 && set_smem_limit(rescore_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const unsigned grid = (unsigned)std::min<int64_t>(ncand, 152 * 8);
   note_launch();

@@ -65,8 +65,7 @@ static int launch_score(const float* in, int64_t nprof, int nbins, LokiScoreSpec
   const int warps = score_warps_per_block(nbins, sp.wmax);
   const int smem = score_smem_bytes(nbins, sp.wmax, warps);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(score_kernel<FROM_EV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+      set_smem_limit(score_kernel<FROM_EV>, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const int64_t nw = (nprof + 31) / 32;
   const int64_t blocks = (nw + warps - 1) / warps;

@@ -315,7 +315,7 @@ extern "C" int loki_matched_filter(const float* profiles, int64_t n, int32_t nbi
   const int smem = kMfWarps * (nbins + nfilt) * (int)sizeof(float);
   if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins + filters too large");
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(mf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+      set_smem_limit(mf_kernel, smem) !=
           cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   note_launch();
@@ -339,8 +339,7 @@ extern "C" int loki_matched_filter_double(const float* profiles, int64_t n, int3
   const int smem = kMfWarps * (nbins + nfilt + n_corr) * (int)sizeof(float);
   if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins + filters too large");
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(mf_double_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+      set_smem_limit(mf_double_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const double lee_double = log2(((double)nfilt * nfilt - 1.0) / 2.0);
   const double lee_single = log2((double)nfilt);

@@ -88,8 +88,7 @@ extern "C" int loki_sim_score_folds(const float* folds_in, const int64_t* src_ro
   const int warps = score_warps_per_block(nbins, spec->wmax);
   const int smem = score_smem_bytes(nbins, spec->wmax, warps);
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(sim_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           smem) != cudaSuccess)
+      set_smem_limit(sim_score_kernel, smem) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   const ScoreK SK = make_score_k(*spec, nbins);
   const int64_t blocks = (nrows + warps * 32 - 1) / (warps * 32);
