@@ -401,7 +401,8 @@ def bench_gpu(args) -> dict | None:
 
     def one_step(events=None, storage="f32"):
         dyp = DynamicProgramming(ts_dev, cfg, device=dev, storage=storage)
-        snr = dyp.search(band_bytes=args.band_bytes, phase_events=events)
+        snr = dyp.search(band_bytes=args.band_bytes, phase_events=events, final=args.final,
+                         norm=args.norm)
         return dyp, snr
 
     for _ in range(args.warmup):
@@ -437,13 +438,13 @@ def bench_gpu(args) -> dict | None:
     # ---- end to end through the public API, host buffers ------------------
     ts_pinned = TimeSeries(ts_e_pin, ts_v_pin, cfg.tsamp)
     for _ in range(max(1, args.warmup // 2)):
-        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
+        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev, norm=args.norm)
         pg.find_best_params(ignore_nan=True)
     barrier()
     t0 = time.perf_counter()
     best = None
     for _ in range(args.steps):
-        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev)
+        _, pg = ffa_search(ts_pinned, cfg, materialize=False, device=dev, norm=args.norm)
         best = pg.find_best_params(ignore_nan=True)
         del pg
     barrier()
@@ -1043,6 +1044,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--band-bytes", type=int, default=1 << 30)
+    ap.add_argument("--final", choices=["auto", "tiled", "banded", "level"], default="auto",
+                    help="how the last two FFA levels run")
+    ap.add_argument("--norm", choices=["exact", "fast"], default="exact",
+                    help="profile normalisation of the tiled final levels")
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bf16", action="store_true",

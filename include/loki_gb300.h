@@ -192,6 +192,27 @@ int loki_ffa_final_banded(const LokiFFALevel* pen, const LokiFFALevel* fin,
 int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin,
                                       int64_t max_window);
 
+/* Last two FFA levels fused in one persistent launch: the penultimate and the
+ * final unify_fold (dynamic/dyn_pffa.py:435-489) plus get_fold_norm
+ * (ffa.py:382-411) and boxcar_snr_nd (detection/scoring.py:156-165), with
+ * neither level written to global memory. Each CTA takes a tile (output
+ * segment, run of final "other" parameter sets that resolve to the same
+ * penultimate others, 64 final frequencies), builds the penultimate rows the
+ * tile reads in shared memory from fold_pp (the materialised level before the
+ * penultimate), and scores the tile's trials from there. pen / fin describe
+ * the full (unwindowed) penultimate and final levels. nbins must be 64 and the
+ * widths 1, 2, 4, ..., 2^(nw-1) with nw <= 6 (else LOKI_ERR_UNSUPPORTED: use
+ * loki_ffa_final_banded). fast_norm 0 normalises with correctly rounded
+ * division and square root (S/N bit-identical to the reference); 1 uses
+ * e * rsqrt(v) (S/N within 1e-5 of the reference relative to max(|S/N|, 1)).
+ * scratch (64-byte aligned, loki_ffa_final_tiled_scratch bytes) holds the
+ * per-level resolve tables and the tile groups. */
+int loki_ffa_final_tiled(const LokiFFALevel* pen, const LokiFFALevel* fin, const void* fold_pp,
+                         void* scratch, int64_t scratch_bytes, const LokiScoreSpec* spec,
+                         int32_t fast_norm, float* snr, int32_t* dev_err, void* stream);
+/* Bytes of scratch loki_ffa_final_tiled needs; -1 for invalid descriptors. */
+int64_t loki_ffa_final_tiled_scratch(const LokiFFALevel* pen, const LokiFFALevel* fin);
+
 /* Round n float32 values to bfloat16 (nearest even): the brute fold, summed
  * in float32, enters a bfloat16-stored FFA (LokiFFALevel.storage = 1).
  * No reference counterpart: the reference stores float32 only. */

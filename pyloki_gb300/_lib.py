@@ -205,6 +205,10 @@ SIGNATURES: dict[str, tuple] = {
                                         _P]),
     "loki_ffa_final_banded_scratch": (C.c_int64, [C.POINTER(LokiFFALevel),
                                                   C.POINTER(LokiFFALevel), _I64]),
+    "loki_ffa_final_tiled": (C.c_int, [C.POINTER(LokiFFALevel), C.POINTER(LokiFFALevel), _P,
+                                       _P, _I64, C.POINTER(LokiScoreSpec), _I32, _P, _P, _P]),
+    "loki_ffa_final_tiled_scratch": (C.c_int64, [C.POINTER(LokiFFALevel),
+                                                 C.POINTER(LokiFFALevel)]),
     "loki_boxcar_snr": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_snr_score_batch": (C.c_int, [_P, _I64, _I32, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_fold_norm": (C.c_int, [_P, _I64, _I32, _P, _P]),

@@ -523,6 +523,310 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in,
   score_out(L, K, sp, SK, tile, stride, lane, q0, kmax, snr, seg);
 }
 
+// ---------------------------------------------------------------------------
+// Last two levels fused per tile (nbins == 64, widths 1, 2, 4, ..., 2^(NW-1)).
+//
+// A tile is (output segment b, group of final "others", block of kTileF final
+// frequencies). A group is a run of consecutive final others (every parameter
+// but frequency) whose tail and head resolve to the same penultimate others,
+// so its trials read one run of penultimate rows for the tail (penultimate
+// segment 2b) and one for the head (segment 2b + 1). The CTA builds those rows
+// in shared memory from the materialised level before them (the penultimate
+// unify_fold, dynamic/dyn_pffa.py:435-489, restricted to the tile's window),
+// then scores every final trial of the tile lane-per-trial from shared memory:
+// the final shift-add, get_fold_norm (ffa.py:382-411) and the boxcar S/N
+// (detection/scoring.py:99-165). Neither of the last two levels is written to
+// global memory. Tiles are ordered frequency-block-major, so CTAs in flight
+// share the rows of the level before (L2 hits) and each of its profiles comes
+// from DRAM about once.
+//
+// Shared row layout: 128 float2 (e, v) per penultimate row, position p holding
+// bin p mod 64, so the roll by a trial's shift s reads positions 64 - s + j,
+// j = 0..63, with no wrap and compile-time offsets. Consecutive lanes hold
+// consecutive final frequencies, whose rows and shifts advance by about half a
+// row and half a bin per lane, so the lanes of a warp spread over the banks.
+//
+// FAST: the profile is normalised as e * rsqrtf(v) (at most a few ulp from the
+// reference's e / sqrt(v)); otherwise with correctly rounded division and
+// square root, which makes the S/N bit-identical to the reference.
+// ---------------------------------------------------------------------------
+
+constexpr int kTileF = 64;        // final frequencies per tile
+constexpr int kTileWarps = 8;
+constexpr int kTileRows = 48;     // shared penultimate rows per side (tail, head)
+constexpr int kTileMembers = 8;   // final others per chunk of a group
+constexpr int kTileSmem = 2 * kTileRows * 128 * (int)sizeof(float2);
+
+// Final others grouped by their (tail, head) penultimate other: groups[0] is
+// the group count G, groups[1 + g] the first other of group g, groups[1 + G] =
+// n_other. One block; a block-wide scan of the boundary flags.
+__global__ void __launch_bounds__(1024) tile_groups_kernel(const OtherRes* __restrict__ tab,
+                                                           int64_t n_other,
+                                                           int32_t* __restrict__ groups) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < n_other; base += blockDim.x) {
+    const int64_t o = base + threadIdx.x;
+    bool flag = false;
+    if (o < n_other)
+      flag = o == 0 || tab[o].prefix != tab[o - 1].prefix ||
+             tab[n_other + o].prefix != tab[n_other + o - 1].prefix;
+    const unsigned bal = __ballot_sync(0xFFFFFFFFu, flag);
+    if (lane == 0) warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    if (warp == 0) {
+      int v = lane < nwarps ? warp_tot[lane] : 0;
+      for (int d = 1; d < 32; d <<= 1) {
+        const int u = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        if (lane >= d) v += u;
+      }
+      if (lane < nwarps) warp_tot[lane] = v;  // inclusive
+    }
+    __syncthreads();
+    const int before = (warp ? warp_tot[warp - 1] : 0) + __popc(bal & lanemask_lt());
+    if (flag) groups[1 + carry + before] = (int32_t)o;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_tot[nwarps - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    groups[0] = carry;
+    groups[1 + carry] = (int32_t)n_other;
+  }
+}
+
+// Previous-level index (of the last, frequency, dimension; window not
+// applied) of final frequency fidx for one other.
+__device__ __forceinline__ int64_t tile_index(const LokiFFALevel& L, const LevelK& K,
+                                              const OtherRes& o, int64_t fidx) {
+  const double f = L.param_arr[L.nparams - 1][fidx];
+  float f_hi, f_lo;
+  if (L.last_split) {
+    const float2 fs = reinterpret_cast<const float2*>(L.last_split)[fidx];
+    f_hi = fs.x;
+    f_lo = fs.y;
+  } else {
+    split2(f, &f_hi, &f_lo);
+  }
+  return trial_index(o, f, f_hi, f_lo, L, K);
+}
+
+template <typename S>
+__device__ __forceinline__ float round_store(float x) {
+  return x;
+}
+template <>
+__device__ __forceinline__ float round_store<__nv_bfloat16>(float x) {
+  return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+// Builds penultimate rows [row0, row1) of the tile (row r < nt: tail side,
+// frequency lo_t + r of penultimate other pt in segment s_t; else head side)
+// into shared memory. Warp w owns a contiguous run of rows; lane k resolves
+// row k of the run and the warp then gathers row by row.
+template <typename S>
+__device__ __forceinline__ void tile_build(const LokiFFALevel& P, const LevelK& KP,
+                                           const S* __restrict__ fold_pp,
+                                           const OtherRes* __restrict__ tab_p, int64_t no_p,
+                                           float2* rows, int nt, int nh, int64_t lo_t,
+                                           int64_t lo_h, int64_t pt, int64_t ph, int64_t s_t,
+                                           int64_t s_h, int32_t* err) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int R = nt + nh;
+  const int per = (R + kTileWarps - 1) / kTileWarps;  // <= 2 * kTileRows / 8 = 12
+  const int r0 = warp * per;
+  const int r1 = std::min(R, r0 + per);
+  const int64_t P_in = n_in_params(P);
+  // lane k: row r0 + k
+  int32_t my_t = 0, my_h = 0, my_sh = 0;
+  bool my_ok = false;
+  if (r0 + lane < r1) {
+    const int r = r0 + lane;
+    const bool tail = r < nt;
+    const int64_t po = tail ? pt : ph;
+    const int64_t f8 = tail ? lo_t + r : lo_h + (r - nt);
+    const TrialRes tr = resolve_trial(P, KP, tab_p[po], tab_p[no_p + po], f8);
+    my_t = (int32_t)tr.in_tail;
+    my_h = (int32_t)tr.in_head;
+    my_sh = tr.s_tail | (tr.s_head << 8);
+    my_ok = tr.ok;
+    if (!tr.ok) atomicOr(err, LOKI_DEVERR_WINDOW);
+  }
+  for (int r = r0; r < r1; ++r) {
+    const int k = r - r0;
+    const int32_t it = __shfl_sync(0xFFFFFFFFu, my_t, k);
+    const int32_t ih = __shfl_sync(0xFFFFFFFFu, my_h, k);
+    const int32_t sh2 = __shfl_sync(0xFFFFFFFFu, my_sh, k);
+    const bool ok = __shfl_sync(0xFFFFFFFFu, my_ok, k);
+    float2* dst = rows + (size_t)(r < nt ? r : kTileRows + (r - nt)) * 128;
+    if (!ok) {
+      dst[lane] = dst[lane + 32] = dst[lane + 64] = dst[lane + 96] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const int64_t seg8 = r < nt ? s_t : s_h;
+    const S* t = fold_pp + ((size_t)(2 * seg8) * P_in + it) * 128;
+    const S* h = fold_pp + ((size_t)(2 * seg8 + 1) * P_in + ih) * 128;
+    const int st = sh2 & 0xFF, shh = sh2 >> 8;
+    const int jt0 = (lane - st) & 63, jt1 = (lane + 32 - st) & 63;
+    const int jh0 = (lane - shh) & 63, jh1 = (lane + 32 - shh) & 63;
+    const float e0 = round_store<S>(__fadd_rn(Store<S>::load(t + jt0), Store<S>::load(h + jh0)));
+    const float e1 = round_store<S>(__fadd_rn(Store<S>::load(t + jt1), Store<S>::load(h + jh1)));
+    const float v0 =
+        round_store<S>(__fadd_rn(Store<S>::load(t + 64 + jt0), Store<S>::load(h + 64 + jh0)));
+    const float v1 =
+        round_store<S>(__fadd_rn(Store<S>::load(t + 64 + jt1), Store<S>::load(h + 64 + jh1)));
+    dst[lane] = dst[lane + 64] = make_float2(e0, v0);
+    dst[lane + 32] = dst[lane + 96] = make_float2(e1, v1);
+  }
+}
+
+// S/N of one final trial from its rolled tail and head rows (lane-per-trial).
+template <bool FAST, int NW>
+__device__ __forceinline__ void tile_score_trial(const float2* __restrict__ bt,
+                                                 const float2* __restrict__ bh,
+                                                 const LokiScoreSpec& sp, const ScoreK& SK,
+                                                 float* __restrict__ out) {
+  constexpr int WMAX = 1 << (NW - 1);
+  float pf[64];
+  float m[NW];
+#pragma unroll
+  for (int iw = 0; iw < NW; ++iw) m[iw] = -FLT_MAX;
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 64; ++j) {
+    const float2 a = bt[j], c = bh[j];
+    const float e = __fadd_rn(a.x, c.x);
+    const float v = __fadd_rn(a.y, c.y);
+    const float nv = FAST ? __fmul_rn(e, rsqrtf(v)) : __fdiv_rn(e, __fsqrt_rn(v));
+    s = j == 0 ? nv : __fadd_rn(s, nv);
+    pf[j] = s;
+#pragma unroll
+    for (int iw = 0; iw < NW; ++iw)
+      if (j >= (1 << iw)) m[iw] = fmaxf(m[iw], __fsub_rn(pf[j], pf[j - (1 << iw)]));
+  }
+  const float total = s;
+  // circular extension P[64 + k] = P[k] + total (scoring.py:42-71), k-major so
+  // that P[k] and P[64 - w + k] are dead once used
+#pragma unroll
+  for (int k = 0; k < WMAX; ++k) {
+    const float ext = __fadd_rn(pf[k], total);
+#pragma unroll
+    for (int iw = 0; iw < NW; ++iw)
+      if (k < (1 << iw)) m[iw] = fmaxf(m[iw], __fsub_rn(ext, pf[64 - (1 << iw) + k]));
+  }
+  float best = -FLT_MAX;
+#pragma unroll
+  for (int iw = 0; iw < NW; ++iw) {
+    float r;
+    if (SK.inv_one) {
+      r = snr_fast(m[iw], total, SK.hb_hi[iw], SK.hb_lo[iw], SK.b_hi[iw], SK.b_lo[iw],
+                   sp.hb[iw], sp.b[iw]);
+    } else {
+      const double x = __dsub_rn(__dmul_rn(sp.hb[iw], (double)m[iw]),
+                                 __dmul_rn(sp.b[iw], (double)total));
+      r = __double2float_rn(__dmul_rn(x, sp.inv_stdnoise));
+    }
+    if (sp.mode == 0) out[iw] = r;
+    else if (r > best) best = r;
+  }
+  if (sp.mode != 0) out[0] = best;
+}
+
+template <typename S, bool FAST, int NW>
+__global__ void __launch_bounds__(kTileWarps * 32, 2)
+ffa_final_tiled64_kernel(LokiFFALevel P, LevelK KP, const S* __restrict__ fold_pp,
+                         const OtherRes* __restrict__ tab_p, int64_t no_p, LokiFFALevel F,
+                         LevelK KF, const OtherRes* __restrict__ tab_f, int64_t no_f,
+                         const int32_t* __restrict__ groups, LokiScoreSpec sp, ScoreK SK,
+                         float* __restrict__ snr, int32_t* __restrict__ err) {
+  extern __shared__ float2 rows[];  // [2][kTileRows][128]
+  __shared__ int64_t win[4];        // tail lo, tail hi, head lo, head hi
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = F.nparams;
+  const int64_t nlast = F.counts_cur[n - 1];
+  const int64_t nfb = (nlast + kTileF - 1) / kTileF;
+  const int64_t ngroups = groups[0];
+  const int64_t nseg_out = n_score_segs(sp);
+  const int64_t total = nseg_out * nfb * ngroups;
+  const int64_t n_full = n_full_params(F);
+  const int nout = sp.mode == 0 ? NW : 1;
+  for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+    const int64_t g = t % ngroups;
+    const int64_t rest = t / ngroups;
+    const int64_t fb = rest % nfb;
+    const int64_t b = rest / nfb;
+    const int64_t o0 = groups[1 + g], o1 = groups[2 + g];
+    const int64_t f0 = fb * kTileF;
+    const int nf = (int)std::min<int64_t>(kTileF, nlast - f0);
+    const int64_t pt = tab_f[o0].prefix, ph = tab_f[no_f + o0].prefix;
+    int64_t c0 = o0;
+    int step = kTileMembers;
+    while (c0 < o1) {
+      const int64_t c1 = std::min<int64_t>(c0 + step, o1);
+      const int m = (int)(c1 - c0);
+      __syncthreads();  // the previous chunk's rows and windows are no longer read
+      if (threadIdx.x == 0) {
+        win[0] = INT64_MAX;  // minima; indices are >= 0, so the maxima start at 0
+        win[1] = 0;
+        win[2] = INT64_MAX;
+        win[3] = 0;
+      }
+      __syncthreads();
+      if (threadIdx.x < 4 * m) {  // corners: (member, tail|head, first|last frequency)
+        const int i = threadIdx.x >> 2, side = (threadIdx.x >> 1) & 1, last = threadIdx.x & 1;
+        const int64_t o = c0 + i;
+        const int64_t idx = tile_index(F, KF, tab_f[side * no_f + o], last ? f0 + nf - 1 : f0);
+        atomicMin(reinterpret_cast<unsigned long long*>(&win[2 * side]),
+                  (unsigned long long)idx);
+        atomicMax(reinterpret_cast<unsigned long long*>(&win[2 * side + 1]),
+                  (unsigned long long)idx);
+      }
+      __syncthreads();
+      const int64_t lo_t = win[0], lo_h = win[2];
+      const int nt = (int)(win[1] - win[0] + 1), nh = (int)(win[3] - win[2] + 1);
+      if (nt > kTileRows || nh > kTileRows) {  // uniform across the block
+        if (step > 1) {
+          step = 1;  // redo this chunk one member at a time
+          continue;
+        }
+        if (threadIdx.x == 0) atomicOr(err, LOKI_DEVERR_WINDOW);
+        c0 = c1;
+        continue;
+      }
+      tile_build<S>(P, KP, fold_pp, tab_p, no_p, rows, nt, nh, lo_t, lo_h, pt, ph, 2 * b,
+                    2 * b + 1, err);
+      __syncthreads();
+      // trials: member-major, 32 consecutive frequencies per warp task
+      const int tasks = m * (kTileF / 32);
+      for (int q = warp; q < tasks; q += kTileWarps) {
+        const int i = q / (kTileF / 32);
+        const int fi = (q % (kTileF / 32)) * 32 + lane;
+        if (fi >= nf) continue;
+        const int64_t o = c0 + i;
+        const int64_t fidx = f0 + fi;
+        const OtherRes ot = tab_f[o], oh = tab_f[no_f + o];
+        const TrialRes tr = resolve_trial(F, KF, ot, oh, fidx);
+        const int64_t rt = tr.in_tail - ot.prefix * F.in_width - lo_t;
+        const int64_t rh = tr.in_head - oh.prefix * F.in_width - lo_h;
+        float* out = snr + (size_t)(b * n_full + o * nlast + fidx) * nout;
+        if (!tr.ok || rt < 0 || rt >= nt || rh < 0 || rh >= nh) {
+          atomicOr(err, LOKI_DEVERR_WINDOW);
+          for (int k = 0; k < nout; ++k) out[k] = __int_as_float(0x7fc00000);
+          continue;
+        }
+        const float2* bt = rows + (size_t)rt * 128 + (64 - tr.s_tail);
+        const float2* bh = rows + (size_t)(kTileRows + rh) * 128 + (64 - tr.s_head);
+        tile_score_trial<FAST, NW>(bt, bh, sp, SK, out);
+      }
+      c0 = c1;
+    }
+  }
+}
+
 // Previous-level frequency window needed by each band of current-level
 // frequencies. The resolved frequency index is monotone in the current
 // frequency for fixed other parameters (f_new = f * (1 - v/c)), so a band
@@ -906,6 +1210,131 @@ extern "C" int64_t loki_ffa_final_banded_scratch(const LokiFFALevel* pen, const 
   // two band buffers (the banded pipeline double-buffers) plus the tables
   const int64_t band = fin->nseg_in * n_other_of(*pen) * max_window * 2 * (int64_t)fin->nbins;
   return 2 * (((band + 15) / 16) * 16) + table_floats(*pen) + table_floats(*fin);
+}
+
+namespace loki {
+
+// ---- fused tiled last two levels --------------------------------------------
+
+template <typename S, bool FAST, int NW>
+static int launch_tiled_t(const LokiFFALevel& P, const LevelK& KP, const void* fold_pp,
+                          const OtherRes* tab_p, int64_t no_p, const LokiFFALevel& F,
+                          const LevelK& KF, const OtherRes* tab_f, int64_t no_f,
+                          const int32_t* groups, const LokiScoreSpec& sp, const ScoreK& SK,
+                          float* snr, int32_t* err, cudaStream_t s) {
+  auto kern = ffa_final_tiled64_kernel<S, FAST, NW>;
+  if (set_smem_limit(kern, kTileSmem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileWarps * 32,
+                                                    kTileSmem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "occupancy query failed");
+  const int grid = std::max(1, nsm * std::max(1, per_sm));
+  note_launch();
+  kern<<<grid, kTileWarps * 32, kTileSmem, s>>>(P, KP, static_cast<const S*>(fold_pp), tab_p,
+                                                no_p, F, KF, tab_f, no_f, groups, sp, SK, snr,
+                                                err);
+  return LOKI_OK;
+}
+
+template <typename S, bool FAST>
+static int launch_tiled_nw(int nw, const LokiFFALevel& P, const LevelK& KP, const void* pp,
+                           const OtherRes* tp, int64_t np_, const LokiFFALevel& F,
+                           const LevelK& KF, const OtherRes* tf, int64_t nf_,
+                           const int32_t* groups, const LokiScoreSpec& sp, const ScoreK& SK,
+                           float* snr, int32_t* err, cudaStream_t s) {
+  switch (nw) {
+    case 1: return launch_tiled_t<S, FAST, 1>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+    case 2: return launch_tiled_t<S, FAST, 2>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+    case 3: return launch_tiled_t<S, FAST, 3>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+    case 4: return launch_tiled_t<S, FAST, 4>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+    case 5: return launch_tiled_t<S, FAST, 5>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+    default: return launch_tiled_t<S, FAST, 6>(P, KP, pp, tp, np_, F, KF, tf, nf_, groups, sp, SK, snr, err, s);
+  }
+}
+
+static int64_t tiled_scratch_bytes(const LokiFFALevel& pen, const LokiFFALevel& fin) {
+  return (int64_t)sizeof(float) * (table_floats(pen) + table_floats(fin)) +
+         (int64_t)sizeof(int32_t) * (n_other_of(fin) + 2);
+}
+
+}  // namespace loki
+
+extern "C" int64_t loki_ffa_final_tiled_scratch(const LokiFFALevel* pen,
+                                                const LokiFFALevel* fin) {
+  if (check_level(pen) || check_level(fin)) return -1;
+  return tiled_scratch_bytes(*pen, *fin);
+}
+
+extern "C" int loki_ffa_final_tiled(const LokiFFALevel* pen, const LokiFFALevel* fin,
+                                    const void* fold_pp, void* scratch, int64_t scratch_bytes,
+                                    const LokiScoreSpec* spec, int32_t fast_norm, float* snr,
+                                    int32_t* dev_err, void* stream) {
+  int rc = check_level(pen);
+  if (rc) return rc;
+  rc = check_level(fin);
+  if (rc) return rc;
+  rc = check_spec(spec, fin->nbins);
+  if (rc) return rc;
+  rc = check_score_segs(fin, spec);
+  if (rc) return rc;
+  if (!fold_pp || !scratch || !snr || !dev_err)
+    return set_error(LOKI_ERR_INVALID, "null pointer argument");
+  if (fin->level != pen->level + 1 || pen->nseg_in != 2 * fin->nseg_in ||
+      fin->nparams != pen->nparams || fin->storage != pen->storage)
+    return set_error(LOKI_ERR_INVALID, "pen/fin descriptors are not consecutive levels");
+  const int n = fin->nparams;
+  if (pen->out_start != 0 || pen->out_width != pen->counts_cur[n - 1] || pen->in_start != 0 ||
+      pen->in_width != pen->counts_prev[n - 1] || fin->out_start != 0 ||
+      fin->out_width != fin->counts_cur[n - 1] || fin->in_start != 0 ||
+      fin->in_width != pen->counts_cur[n - 1])
+    return set_error(LOKI_ERR_INVALID, "the tiled final levels take full (unwindowed) grids");
+  if (fin->nbins != 64)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the tiled final levels need nbins == 64");
+  const ScoreK SK = make_score_k(*spec, fin->nbins);
+  if (!SK.pow2_64)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the tiled final levels need widths 1, 2, 4, ... 32");
+  if (n_in_params(*pen) >= (int64_t(1) << 31) || n_other_of(*fin) >= (int64_t(1) << 31))
+    return set_error(LOKI_ERR_UNSUPPORTED, "grids above 2^31 parameter sets per segment");
+  if (scratch_bytes < tiled_scratch_bytes(*pen, *fin))
+    return set_error(LOKI_ERR_CAPACITY, "scratch of %lld bytes below the %lld needed",
+                     (long long)scratch_bytes, (long long)tiled_scratch_bytes(*pen, *fin));
+  if ((reinterpret_cast<uintptr_t>(scratch) & 63) != 0)
+    return set_error(LOKI_ERR_INVALID, "scratch must be 64-byte aligned");
+  cudaStream_t s = (cudaStream_t)stream;
+  const LevelK KP = make_level_k(*pen);
+  const LevelK KF = make_level_k(*fin);
+  float* sc = static_cast<float*>(scratch);
+  OtherRes* tab_p = reinterpret_cast<OtherRes*>(sc);
+  OtherRes* tab_f = reinterpret_cast<OtherRes*>(sc + table_floats(*pen));
+  int32_t* groups = reinterpret_cast<int32_t*>(sc + table_floats(*pen) + table_floats(*fin));
+  const int64_t no_p = n_other_of(*pen), no_f = n_other_of(*fin);
+  note_launch();
+  note_launch();
+  note_launch();
+  other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_p + 127) / 128, 1024), 128, 0, s>>>(
+      *pen, KP, tab_p, no_p);
+  other_table_kernel<<<(unsigned)std::min<int64_t>((2 * no_f + 127) / 128, 1024), 128, 0, s>>>(
+      *fin, KF, tab_f, no_f);
+  tile_groups_kernel<<<1, 1024, 0, s>>>(tab_f, no_f, groups);
+  const int nw = spec->nwidths;
+  if (fin->storage == 1)
+    rc = fast_norm ? launch_tiled_nw<__nv_bfloat16, true>(nw, *pen, KP, fold_pp, tab_p, no_p,
+                                                          *fin, KF, tab_f, no_f, groups, *spec,
+                                                          SK, snr, dev_err, s)
+                   : launch_tiled_nw<__nv_bfloat16, false>(nw, *pen, KP, fold_pp, tab_p, no_p,
+                                                           *fin, KF, tab_f, no_f, groups, *spec,
+                                                           SK, snr, dev_err, s);
+  else
+    rc = fast_norm ? launch_tiled_nw<float, true>(nw, *pen, KP, fold_pp, tab_p, no_p, *fin, KF,
+                                                  tab_f, no_f, groups, *spec, SK, snr, dev_err, s)
+                   : launch_tiled_nw<float, false>(nw, *pen, KP, fold_pp, tab_p, no_p, *fin, KF,
+                                                   tab_f, no_f, groups, *spec, SK, snr, dev_err,
+                                                   s);
+  if (rc) return rc;
+  return check_launch("ffa_final_tiled");
 }
 
 namespace loki {

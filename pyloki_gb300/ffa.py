@@ -440,6 +440,7 @@ class DynamicProgramming:
 
     def search(self, widths=None, stdnoise: float = 1.0, *, mode: int = 0,
                banded: bool | None = None, band_bytes: int = 1 << 30,
+               final: str = "auto", norm: str = "exact",
                phase_events: list | None = None, check: bool = True) -> torch.Tensor:
         """S/N of every final-level parameter set (segment 0 of each series),
         never writing the final fold. Returns ``(*counts_final, nwidths)`` (or
@@ -448,7 +449,27 @@ class DynamicProgramming:
         ``(name, cuda.Event)`` marks recorded on the launch stream after the
         brute fold, the materialised levels and the final levels. ``check=False``
         leaves the device error word unread (no host synchronisation, as CUDA
-        graph capture requires); read it later with ``check_errors``."""
+        graph capture requires); read it later with ``check_errors``.
+
+        ``final`` picks how the last levels run: ``"tiled"`` fuses the last
+        two into one persistent launch that builds the penultimate rows of
+        each tile in shared memory (64 bins, widths 1, 2, 4, ...);
+        ``"banded"`` writes the penultimate level band by band to a scratch
+        buffer; ``"level"`` materialises the penultimate level and fuses only
+        the final one with scoring. ``"auto"`` takes the tiled path where it
+        applies, else banded when the penultimate level is above
+        ``8 * band_bytes``, else level. ``banded=True`` / ``False`` (with
+        ``final="auto"``) asks for banded / level. ``norm`` applies to the
+        tiled path: ``"exact"`` divides by the correctly rounded square root
+        (S/N bit-identical to the reference); ``"fast"`` multiplies by the
+        reciprocal square root (S/N within 1e-5 of it, relative to
+        max(|S/N|, 1))."""
+        if final not in ("auto", "tiled", "banded", "level"):
+            msg = f"final must be 'auto', 'tiled', 'banded' or 'level', got {final!r}"
+            raise ValueError(msg)
+        if norm not in ("exact", "fast"):
+            msg = f"norm must be 'exact' or 'fast', got {norm!r}"
+            raise ValueError(msg)
         cfg = self.cfg
         n = cfg.niters_ffa
         widths = cfg.score_widths if widths is None else np.asarray(widths, np.int64)
@@ -483,15 +504,31 @@ class DynamicProgramming:
             return snr
         snr = torch.empty((self.nbatch, fin.size, nout), dtype=torch.float32,
                           device=self._device)
-        if banded is None:
-            banded = n >= 2 and self.level_bytes(n - 1) > 8 * band_bytes
-        if banded and n < 2:
-            banded = False
-        last_mat = n - 2 if banded else n - 1
+        widths_arr = np.asarray(widths, np.int64)
+        tiled_ok = (n >= 2 and cfg.nbins == 64 and len(widths_arr) <= 6
+                    and np.array_equal(widths_arr, 2 ** np.arange(len(widths_arr))))
+        if final == "tiled" and not tiled_ok:
+            msg = "the tiled final levels need >= 2 levels, 64 bins and widths 1, 2, 4, ..."
+            raise ValueError(msg)
+        if final == "auto":
+            if banded is not None:
+                final = "banded" if banded else "level"
+            elif tiled_ok:
+                final = "tiled"
+            else:
+                final = ("banded" if n >= 2 and self.level_bytes(n - 1) > 8 * band_bytes
+                         else "level")
+        if final == "banded" and n < 2:
+            final = "level"
+        tiled = final == "tiled"
+        banded = final == "banded"
+        last_mat = n - 2 if (banded or tiled) else n - 1
         while self.ffa_level < last_mat:
             self._execute_iter()
         mark("levels")
-        if not banded:
+        if tiled:
+            self._search_tiled(fin, spec, snr, fast=norm == "fast")
+        elif not banded:
             prev = self._grid(n - 1)
             desc = level_desc(cfg, fin, prev, self.nsegments, storage=self._storage)
             _lib.check(self._lib.loki_ffa_level_score(
@@ -550,6 +587,24 @@ class DynamicProgramming:
                 return width, lo_h, hi_h
             width = max(32, width // 2)
         return width, lo_h, hi_h
+
+    def _search_tiled(self, fin: _Grid, spec, snr: torch.Tensor, *, fast: bool) -> None:
+        cfg = self.cfg
+        n = cfg.niters_ffa
+        pen, pp = self._grid(n - 1), self._grid(n - 2)
+        nseg_pp = self.nsegments
+        d_pen = level_desc(cfg, pen, pp, nseg_pp, storage=self._storage)
+        d_fin = level_desc(cfg, fin, pen, nseg_pp // 2, storage=self._storage)
+        nbytes = int(self._lib.loki_ffa_final_tiled_scratch(d_pen, d_fin))
+        if nbytes <= 0:
+            msg = "invalid tiled level descriptors"
+            raise ValueError(msg)
+        scratch = torch.empty((nbytes + 7) // 8, dtype=torch.float64, device=self._device)
+        before = self._lib.loki_launch_count()
+        _lib.check(self._lib.loki_ffa_final_tiled(
+            d_pen, d_fin, _lib.ptr(self.fold), _lib.ptr(scratch), scratch.numel() * 8, spec,
+            1 if fast else 0, _lib.ptr(snr), _lib.ptr(self._err), self._stream()))
+        self.launches += self._lib.loki_launch_count() - before
 
     def _search_banded(self, fin: _Grid, spec, snr: torch.Tensor, band_bytes: int) -> None:
         cfg = self.cfg

@@ -69,13 +69,15 @@ class Periodogram:
 
 def ffa_search(tseries: TimeSeries, search_cfg: PulsarSearchConfig, *, quiet: bool = False,
                show_progress: bool = False, materialize: bool | None = None,
-               device=None) -> tuple[DynamicProgramming, Periodogram]:
+               device=None, norm: str = "exact") -> tuple[DynamicProgramming, Periodogram]:
     """FFA search: brute fold, DP levels, boxcar S/N of segment 0.
 
     With ``materialize`` (default: when the final fold is at most 1 GiB) every
     level is kept, as in the reference, and ``dyp.fold`` is the final fold;
-    otherwise the final level is fused with scoring (``dyp.search``) and only
-    the S/N array is produced. Both paths give identical S/N.
+    otherwise the last levels are fused with scoring (``dyp.search``) and only
+    the S/N array is produced. Both paths give identical S/N. ``norm="fast"``
+    (fused path only) normalises profiles with the reciprocal square root:
+    S/N within 1e-5 of the reference relative to max(|S/N|, 1).
     """
     dyp = DynamicProgramming(tseries, search_cfg, device=device)
     widths = search_cfg.score_widths
@@ -88,7 +90,7 @@ def ffa_search(tseries: TimeSeries, search_cfg: PulsarSearchConfig, *, quiet: bo
 
         snrs = boxcar_snr_nd(dyp.get_fold_norm(), widths, 1.0)
     else:
-        snrs = dyp.search(widths, 1.0)
+        snrs = dyp.search(widths, 1.0, norm=norm)
     pgram = Periodogram(params={"width": widths, **dyp.param_arr_dict}, snrs=snrs,
                         tobs=tseries.tobs)
     return dyp, pgram

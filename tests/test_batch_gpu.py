@@ -35,9 +35,9 @@ def _many(n, count, seed0=10):
 
 
 @pytest.mark.parametrize("storage", ["f32", "bf16"])
-@pytest.mark.parametrize("banded", [False, True])
+@pytest.mark.parametrize("final", ["level", "banded", "tiled"])
 @pytest.mark.parametrize("jerk", [False, True])
-def test_nbatch_search_equals_one_search_per_series(cuda_device, storage, banded, jerk):
+def test_nbatch_search_equals_one_search_per_series(cuda_device, storage, final, jerk):
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.timeseries import TimeSeries
 
@@ -47,12 +47,12 @@ def test_nbatch_search_equals_one_search_per_series(cuda_device, storage, banded
     v = np.concatenate([s[1] for s in ser])
     dyp = DynamicProgramming(TimeSeries(e, v, cfg.tsamp), cfg, device=cuda_device,
                              storage=storage, nbatch=3)
-    got = dyp.search(banded=banded, band_bytes=8192).cpu().numpy()
+    got = dyp.search(final=final, band_bytes=8192).cpu().numpy()
     assert got.shape[0] == 3
     for i, (se, sv) in enumerate(ser):
         one = DynamicProgramming(TimeSeries(se, sv, cfg.tsamp), cfg, device=cuda_device,
                                  storage=storage)
-        np.testing.assert_array_equal(got[i], one.search(banded=banded,
+        np.testing.assert_array_equal(got[i], one.search(final=final,
                                                          band_bytes=8192).cpu().numpy())
     if storage == "f32" and not jerk:  # and against the oracle
         ref = O.boxcar_snr(O.fold_norm(O.ffa_execute(ser[1][0], ser[1][1], cfg)[0]),

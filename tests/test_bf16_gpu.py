@@ -64,8 +64,8 @@ def test_bf16_levels_bit_exact_vs_rounded_oracle(cuda_device, name):
 
 
 @pytest.mark.parametrize("name", FFA_CASES)
-@pytest.mark.parametrize("banded", [False, True])
-def test_bf16_search_bit_exact_vs_oracle_on_stored_levels(cuda_device, name, banded):
+@pytest.mark.parametrize("final", ["level", "banded", "tiled"])
+def test_bf16_search_bit_exact_vs_oracle_on_stored_levels(cuda_device, name, final):
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.timeseries import TimeSeries
 
@@ -81,7 +81,7 @@ def test_bf16_search_bit_exact_vs_oracle_on_stored_levels(cuda_device, name, ban
     want = O.boxcar_snr(O.fold_norm(fin[0]), cfg.score_widths)
     dyp = DynamicProgramming(ts, cfg, device=cuda_device, storage="bf16")
     dyp.initialize()
-    got = dyp.search(banded=banded, band_bytes=4096).cpu().numpy()
+    got = dyp.search(final=final, band_bytes=4096).cpu().numpy()
     np.testing.assert_array_equal(got, want.reshape(got.shape))
 
 

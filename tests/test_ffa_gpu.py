@@ -68,7 +68,7 @@ def test_plan_matches_reference(cuda_device, name):
 
 
 @pytest.mark.parametrize("name", FFA_CASES)
-@pytest.mark.parametrize("path", ["materialize", "fused", "banded"])
+@pytest.mark.parametrize("path", ["materialize", "level", "banded", "tiled"])
 def test_ffa_search_snrs(cuda_device, name, path):
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.search import ffa_search
@@ -84,8 +84,53 @@ def test_ffa_search_snrs(cuda_device, name, path):
         dyp = DynamicProgramming(ts, cfg, device=cuda_device)
         dyp.initialize()
         # a tiny band budget forces many narrow bands with halos
-        snrs = dyp.search(banded=(path == "banded"), band_bytes=4096).cpu().numpy()
+        snrs = dyp.search(final=path, band_bytes=4096).cpu().numpy()
     np.testing.assert_array_equal(snrs, d["snrs"])
+
+
+# Tolerance of the fast normalisation (e * rsqrt(v)): the benchmark spec's 1e-5
+# relative bound on FP32 results, taken relative to max(|S/N|, 1).
+FAST_TOL = 1e-5
+
+
+def _rel_err(got, ref):
+    fin = np.isfinite(ref)
+    assert np.array_equal(fin, np.isfinite(got)), "NaN/inf pattern differs"
+    return float((np.abs(got[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1.0)).max())
+
+
+@pytest.mark.parametrize("name", FFA_CASES)
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tiled_fast_norm_within_tolerance(cuda_device, name, mode):
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden(name)
+    cfg = cfg_from_golden(d)
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg, device=cuda_device)
+    got = dyp.search(final="tiled", norm="fast", mode=mode).cpu().numpy()
+    ref = d["snrs"] if mode == 0 else d["snrs"].max(axis=-1)
+    assert _rel_err(got, ref) <= FAST_TOL
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_tiled_matches_banded_general_variance(cuda_device, storage):
+    """A general ts_v (not all ones) and both storages: the tiled last two
+    levels equal the banded ones bit for bit (exact normalisation), including
+    the bfloat16 rounding of every stored penultimate value."""
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d = load_golden("ffa_accel")
+    cfg = cfg_from_golden(d)
+    rng = np.random.default_rng(5)
+    ts_v = rng.uniform(0.5, 2.0, d["ts_e"].size).astype(np.float32)
+    ts = TimeSeries(d["ts_e"], ts_v, cfg.tsamp)
+    out = {}
+    for final in ("tiled", "banded"):
+        dyp = DynamicProgramming(ts, cfg, device=cuda_device, storage=storage)
+        out[final] = dyp.search(final=final, band_bytes=8192).cpu().numpy()
+    np.testing.assert_array_equal(out["tiled"], out["banded"])
 
 
 def test_search_max_mode(cuda_device):
@@ -160,9 +205,10 @@ def test_accel_search_spot_trials_vs_oracle(cuda_device):
     # every trial against the oracle's fully materialised search
     full = O.boxcar_snr(O.fold_norm(O.ffa_execute(ts_e, ts_v, cfg)[0]), cfg.score_widths)
     np.testing.assert_array_equal(snrs, full)
-    # unbanded fused path gives the same array
-    dyp2 = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
-    np.testing.assert_array_equal(dyp2.search(banded=False).cpu().numpy(), snrs)
+    # the level and tiled paths give the same array
+    for final in ("level", "tiled"):
+        dyp2 = DynamicProgramming(TimeSeries(ts_e, ts_v, cfg.tsamp), cfg, device=cuda_device)
+        np.testing.assert_array_equal(dyp2.search(final=final).cpu().numpy(), snrs)
 
 
 def test_brutefold_chunked_scratch_and_wide_bins(cuda_device):

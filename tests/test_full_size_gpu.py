@@ -45,6 +45,13 @@ def test_benchmark_accel_search_2e23_spot_trials_bit_exact(cuda_device):
     snr = dyp.search()
     assert tuple(snr.shape) == (193, 7730942, 5)
     _check(snr, ts.ts_e, ts.ts_v, cfg)
+    # the fast normalisation: every trial within 1e-5 of the exact search
+    # (relative to max(|S/N|, 1)), the same NaN pattern (empty-bin trials)
+    fast = DynamicProgramming(ts, cfg, device=cuda_device).search(norm="fast")
+    fin = torch.isfinite(snr)
+    assert torch.equal(fin, torch.isfinite(fast))
+    err = ((fast - snr).abs() / snr.abs().clamp(min=1.0))[fin].max().item()
+    assert err <= 1e-5, err
 
 
 def test_jerk_search_2e21_spot_trials_bit_exact_single_and_stacked(cuda_device):
