@@ -969,7 +969,7 @@ def profile_once(args) -> None:
         bseg_brute=16384 if n == 2**23 else 0)
     ts = ms(n, 64e-6, freq=200.0, snr=15.0, ducy=0.05, accel=20.0, seed=1000)
     dyp = DynamicProgramming(ts, cfg, device=torch.device("cuda", 0))
-    snr = dyp.search(band_bytes=args.band_bytes)
+    snr = dyp.search(band_bytes=args.band_bytes, final=args.final, norm=args.norm)
     torch.cuda.synchronize()
     print(json.dumps({"profile_once": True, "nsamps": n, "levels": cfg.niters_ffa,
                       "final_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
