@@ -561,6 +561,11 @@ class DynamicThresholdScheme:
             path.append(float(s["threshold"]))
         return np.array(path[::-1], np.float32)
 
+    def backtrack_best(self, min_probs: list[float] | None = None) -> list[np.ndarray]:
+        """Least-cost complete schemes reaching each ``min_probs`` H1 survival
+        (``detection/schemes.py:225-277``); see :func:`backtrack_best`."""
+        return backtrack_best(self.states, self.thresholds, self.probs, min_probs)
+
     def save(self, outdir: str = ".") -> str:
         """The design as ``.npz`` with the reference's attribute and dataset
         names (``thresholding.py:965-1008``; h5py is not used)."""
@@ -577,6 +582,50 @@ class DynamicThresholdScheme:
         return path.as_posix()
 
 
-__all__ = ["DynamicThresholdScheme", "FoldSim", "bound_scheme", "determine_scheme",
+def backtrack_best(states: np.ndarray, thresholds: np.ndarray, probs: np.ndarray,
+                   min_probs: list[float] | None = None) -> list[np.ndarray]:
+    """Best threshold paths of a finished design
+    (``DynamicThresholdSchemeAnalyser.backtrack_best``, ``detection/schemes.py:225-277``).
+
+    For each ``min_prob``: among the non-empty final states whose cumulative
+    H1 survival is at least ``min_prob``, the one of least ``cost``, traced
+    back stage by stage to the state at (nearest threshold to
+    ``threshold_prev``, probability bin of ``success_h1_cumul_prev``). Each
+    result is the path's states (``state_dtype``, one per stage; its
+    ``threshold`` field is the scheme), empty when no final state qualifies.
+    Raises ``ValueError`` when the design has no complete scheme or the trace
+    reaches an empty state.
+    """
+    if min_probs is None:
+        min_probs = [probs[0]]
+    final = states[-1]
+    cloud = final[~final["is_empty"]]
+    if len(cloud) == 0:
+        msg = "No non-empty final states to plot"
+        raise ValueError(msg)
+    nstages = states.shape[0]
+    out = []
+    for min_prob in min_probs:
+        ok = cloud[cloud["success_h1_cumul"] >= min_prob]
+        if len(ok) == 0:
+            out.append(np.zeros(0, dtype=states.dtype))
+            continue
+        path = [ok[np.argmin(ok["cost"])]]
+        for istage in range(nstages - 2, -1, -1):
+            prev_thr = path[0]["threshold_prev"]
+            prev_prob = path[0]["success_h1_cumul_prev"]
+            ithres = np.argmin(np.abs(thresholds - prev_thr))
+            iprob = np.digitize(prev_prob, probs) - 1
+            if iprob < 0 or states[istage, ithres, iprob]["is_empty"]:
+                msg = (f"Backtracking failed at stage {istage} for threshold {prev_thr} "
+                       f"and success probability {prev_prob}")
+                raise ValueError(msg)
+            path.insert(0, states[istage, ithres, iprob])
+        out.append(np.array(path, dtype=states.dtype))
+    return out
+
+
+__all__ = ["DynamicThresholdScheme", "FoldSim", "backtrack_best", "bound_scheme",
+           "determine_scheme",
            "evaluate_scheme", "generate_folded_profile", "get_next_state",
            "neighbouring_indices", "state_dtype", "trials_scheme"]

@@ -414,6 +414,91 @@ def timeseries_case() -> None:
     np.savez_compressed(HERE / "timeseries_ephem.npz", **out)
 
 
+def branching_case() -> None:
+    """PulsarSearchConfig.generate_branching_pattern (config.py:758-819) of the
+    circular-orbit benchmark search (Taylor tree to the 4th derivative, 2^22
+    samples, 128 segments): moving grid for three reference segments, the
+    fixed grid, and the quadrature and conservative tilings."""
+    from pyloki.config import ParamLimits, PulsarSearchConfig
+
+    n = 2**22
+    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=4)
+    out = {}
+    cases = [("moving_64", "aggressive", "poly_taylor_moving", 64),
+             ("moving_0", "aggressive", "poly_taylor_moving", 0),
+             ("moving_100", "aggressive", "poly_taylor_moving", 100),
+             ("fixed_64", "aggressive", "poly_taylor_fixed", 64),
+             ("quad_64", "quadrature", "poly_taylor_moving", 64),
+             ("cons_64", "conservative", "poly_taylor_moving", 64)]
+    for key, tiling, kind, ref in cases:
+        cfg = PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
+                                 param_limits=lim.limits, use_fourier=False, bseg_ffa=n // 128,
+                                 prune_poly_order=4, tiling_strategy=tiling)
+        out[key] = cfg.generate_branching_pattern(kind, ref_seg=ref)
+    out["param_limits"] = np.asarray(lim.limits, dtype=np.float64)
+    np.savez_compressed(HERE / "branching_taylor4.npz", **out)
+
+
+def synthetic_states(nstages: int, nthr: int, nprob: int, seed: int):
+    """A seeded threshold-design table (thresholding.py state records) whose
+    non-empty cells each point back to a non-empty cell of the stage before."""
+    # the field layout of thresholding.state_dtype (thresholding.py:333-347);
+    # that module cannot be imported under the shim (structref types)
+    state_dtype = np.dtype(
+        [("success_h0", np.float32), ("success_h1", np.float32), ("complexity", np.float32),
+         ("complexity_cumul", np.float32), ("success_h1_cumul", np.float32),
+         ("nbranches", np.float32), ("threshold", np.float32), ("cost", np.float32),
+         ("threshold_prev", np.float32), ("success_h1_cumul_prev", np.float32),
+         ("is_empty", np.bool_)])
+    rng = np.random.default_rng(seed)
+    thresholds = np.linspace(0.1, 10.0, nthr).astype(np.float32)
+    probs = np.logspace(np.log10(0.05), 0, nprob)
+    states = np.zeros((nstages, nthr, nprob), dtype=state_dtype)
+    states["is_empty"] = True
+    for st in range(nstages):
+        full = rng.random((nthr, nprob)) < 0.4
+        for i, k in zip(*np.nonzero(full)):
+            rec = states[st, i, k]
+            rec["is_empty"] = False
+            rec["threshold"] = thresholds[i]
+            hi = probs[k + 1] if k + 1 < nprob else 1.0
+            rec["success_h1_cumul"] = rng.uniform(probs[k], hi)
+            rec["success_h1"] = rng.uniform(0.5, 1.0)
+            rec["success_h0"] = rng.uniform(0.0, 0.5)
+            rec["complexity"] = rng.uniform(1, 100)
+            rec["complexity_cumul"] = rng.uniform(1, 1e4)
+            rec["nbranches"] = rng.integers(1, 5)
+            rec["cost"] = rng.uniform(1, 1e3) * (1 + 100 * rec["success_h1_cumul"])
+            if st > 0:
+                prev = np.argwhere(~states[st - 1]["is_empty"])
+                pi, pk = prev[rng.integers(len(prev))]
+                rec["threshold_prev"] = thresholds[pi] + np.float32(1e-3)
+                rec["success_h1_cumul_prev"] = states[st - 1, pi, pk]["success_h1_cumul"]
+            else:
+                rec["threshold_prev"] = -1.0
+                rec["success_h1_cumul_prev"] = 1.0
+            states[st, i, k] = rec
+    return states, thresholds, probs
+
+
+def schemes_case() -> None:
+    """DynamicThresholdSchemeAnalyser.backtrack_best (detection/schemes.py:225-277)
+    on a seeded synthetic design table, for four minimum H1 survivals."""
+    from pyloki.detection import schemes
+
+    states, thresholds, probs = synthetic_states(12, 25, 8, seed=77)
+    an = schemes.DynamicThresholdSchemeAnalyser(states, thresholds, probs,
+                                                np.ones(12, np.float32), np.ones(12), 1.0)
+    min_probs = [0.06, 0.2, 0.5, 0.9]
+    paths = an.backtrack_best(min_probs=min_probs)
+    out = {"states": states, "thresholds": thresholds, "probs": probs,
+           "min_probs": np.asarray(min_probs)}
+    for i, p in enumerate(paths):
+        out[f"path_{i}"] = p.thresholds
+        out[f"cost_{i}"] = p.get_info("cost")
+    np.savez_compressed(HERE / "schemes_backtrack.npz", **out)
+
+
 def scorer_cases() -> None:
     scorer_case("scorers_nb64", 64, 48, 31, 4)
     scorer_case("scorers_nb50", 50, 36, 32, 5)
@@ -426,7 +511,9 @@ def pulse_cases() -> None:
 
 def main() -> None:
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    ref_src = args[0] if args else "/root/reference/src"
+    if not args:
+        sys.exit("usage: make_fixtures.py PYLOKI_SRC_DIR [--only-flags]")
+    ref_src = args[0]
     sys.path.insert(0, str(HERE))
     import refshim
 
@@ -443,6 +530,24 @@ def main() -> None:
         return
     if "--timeseries-only" in sys.argv:
         timeseries_case()
+        return
+    if "--branching-only" in sys.argv:
+        branching_case()
+        return
+    if "--schemes-only" in sys.argv:
+        import types as _types
+
+        # detection/schemes.py imports tkinter and matplotlib's Tk backend for
+        # its viewer only
+        for name in ("tkinter", "tkinter.ttk", "tkinter.filedialog", "tkinter.messagebox",
+                     "matplotlib.backends", "matplotlib.backends.backend_tkagg",
+                     "matplotlib.ticker"):
+            sys.modules[name] = _types.ModuleType(name)
+        sys.modules["tkinter"].Tk = object
+        sys.modules["matplotlib.backends.backend_tkagg"].FigureCanvasTkAgg = object
+        sys.modules["matplotlib.backends.backend_tkagg"].NavigationToolbar2Tk = object
+        sys.modules["matplotlib.ticker"].FormatStrFormatter = object
+        schemes_case()
         return
     # numba types `float32_array >= float64` as a float64 comparison. Under
     # plain numpy 2 the overflow threshold that world_tree derives with

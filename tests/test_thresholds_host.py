@@ -45,3 +45,23 @@ def test_neighbouring_indices_window():
     np.testing.assert_array_equal(neighbouring_indices(beam, 10, 5), [10, 11, 12, 13, 14])
     np.testing.assert_array_equal(neighbouring_indices(beam, 29, 5), [25, 26, 27, 28, 29])
     np.testing.assert_array_equal(neighbouring_indices(beam, 50, 3), [27, 28, 29])
+
+
+def test_backtrack_best_matches_reference_analyser():
+    """backtrack_best against the reference's DynamicThresholdSchemeAnalyser on
+    a seeded synthetic design table (tests/golden/schemes_backtrack.npz, made
+    by make_fixtures.py --schemes-only)."""
+    from conftest import load_golden
+
+    from pyloki_gb300.thresholds import backtrack_best, state_dtype
+
+    d = load_golden("schemes_backtrack")
+    states = d["states"].astype(state_dtype)
+    paths = backtrack_best(states, d["thresholds"], d["probs"], list(d["min_probs"]))
+    assert len(paths) == len(d["min_probs"])
+    for i, p in enumerate(paths):
+        np.testing.assert_array_equal(p["threshold"], d[f"path_{i}"])
+        cost = (p["complexity_cumul"] / p["success_h1_cumul"]).astype(np.float32)
+        np.testing.assert_allclose(cost, d[f"cost_{i}"], rtol=1e-6)
+    # no final state reaches a survival above 1: empty path, like the reference
+    assert len(backtrack_best(states, d["thresholds"], d["probs"], [1.5])[0]) == 0
