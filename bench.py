@@ -38,11 +38,16 @@ if str(ROOT) not in sys.path:
 
 METRIC = "period-trials/s"
 WORKLOAD = "ffa_accel_search_2^23"
-# DRAM bytes (read + write) per final trial of band_union64_kernel: ncu
-# capture of three full-band launches of this search with 1 GiB bands
-# (1.940 GB per launch, 193 x 32098 trials per launch);
-# profiles/band_union64_kernel_ffa_accel_2^23.md.
-UNION_DRAM_BYTES_PER_TRIAL = 313.2
+# DRAM bytes (read + write) per final trial of the fused last two levels:
+# ncu capture of one launch of the same search at 2^21 samples (13 x 1932736
+# trials); profiles/ffa_final_tiled64_kernel_ffa_accel_2^21.md. The banded
+# path's figure comes from three full-band launches at 2^21
+# (profiles/band_union64_kernel_ffa_accel_2^21.md).
+FINAL_DRAM_BYTES_PER_TRIAL = {"tiled": 60.2, "banded": 259.0}
+FINAL_KERNEL = {"tiled": "ffa_final_tiled64_kernel (last two levels fused per tile: "
+                         "penultimate rows built in shared memory, lane-per-trial scoring)",
+                "banded": "band_union64_kernel (penultimate band + fused final-level scoring)",
+                "level": "ffa_level_score_kernel (final level fused with scoring)"}
 BF16_TOP = 64        # candidates re-scored in FP64 and checked against the FP64 oracle
 BF16_SAMPLE = 192    # random trials added to the FP64 error sample
 BATCH_WORKLOAD = "ffa_jerk_batch_2^20-2^23"
@@ -74,10 +79,13 @@ def cpu_band_cfg(band_hz: float):
 
 PRUNE_WORKLOAD = "taylor4_prune_circular_orbit_2^22"
 PRUNE_MAX_SUGG = 2**18
-PRUNE_MULTI_RUNS = 16   # reference segments of the multi-run measurement
+PRUNE_MULTI_RUNS = 64   # reference segments of the multi-run measurement
 PRUNE_WORKERS = 4      # concurrent runs (host threads and CUDA streams)
+PRUNE_STREAMS = 16     # concurrent device-resident runs (CUDA streams, one host thread)
 PRUNE_BATCH = 1024
-PRUNE_THRESHOLD_FINAL = 4.0
+PRUNE_SCHEME = ROOT / "tests" / "golden" / "prune_scheme_taylor4.npz"
+PRUNE_SCHEME_NOTE = ("designed: DynamicThresholdScheme over the tree's branching pattern, "
+                     "least-cost path keeping 90% of S/N-10 signals")
 # HBM bytes per leaf of prune_score_kernel: the parent fold (2 x 64 f32) read
 # once, the score (f32), grid indices (2 x i32) and phase (f64) written. The
 # added segment's fold (146 rows, 75 KB) stays in L2.
@@ -106,9 +114,17 @@ def make_prune_series(seed: int):
     return ms(2**22, 64e-6, freq=333.33, snr=10.0, orbit=orbit, seed=seed), orbit
 
 
-def prune_thresholds(nseg: int, final: float = PRUNE_THRESHOLD_FINAL) -> np.ndarray:
-    """Per-level thresholds rising as sqrt(segments folded), reaching ``final``."""
-    return final * np.sqrt(np.arange(1, nseg) / (nseg - 1))
+def prune_thresholds(nseg: int) -> np.ndarray:
+    """The designed per-level thresholds of the pruning workload: the
+    reference's threshold-design workflow (DynamicThresholdScheme over the
+    tree's branching pattern, least-cost path keeping 90 % of S/N-10 signals,
+    rounded to 0.1), made by tests/golden/make_prune_scheme.py."""
+    with np.load(PRUNE_SCHEME) as d:
+        thr = d["thresholds"].astype(np.float64)
+    if len(thr) != nseg - 1:
+        msg = f"the threshold scheme has {len(thr)} levels, the search {nseg - 1}"
+        raise ValueError(msg)
+    return thr
 
 
 def prune_cpu(nthreads: int = 0) -> dict:
@@ -155,7 +171,9 @@ def bench_prune_gpu(args, dev) -> dict:
     ref = nseg // 2
     prn = Pruning(dyp, thr, max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
 
-    def one_run(events=None) -> int:
+    def level_run(events=None) -> int:
+        """The level-by-level path: one host wait per level for the child
+        count and one for the survivor count."""
         prn.score_events = events
         prn.initialize(ref)
         for _ in range(nseg - 1):
@@ -165,12 +183,25 @@ def bench_prune_gpu(args, dev) -> dict:
         prn._do_ascend()
         return sum(st.n_leaves for st in prn.pstats[1:])
 
+    def one_run() -> int:
+        """Device-resident: every level in one CUDA graph (counts on the
+        device), then the ascend."""
+        prn.run_device(ref, graph=True)
+        prn._do_ascend()
+        return sum(st.n_leaves for st in prn.pstats[1:])
+
     for _ in range(args.warmup):
         one_run()
+        level_run()
+    # kernels per run, counted on one uncaptured run (a graph replay does not
+    # pass through the library's launch counter)
+    c0 = lib.loki_launch_count()
+    prn.run_device(ref, graph=False)
+    prn._do_ascend()
+    run_launches = lib.loki_launch_count() - c0
     torch.cuda.synchronize(dev)
     leaves = 0
     score_events: list = []
-    c0 = lib.loki_launch_count()
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
     start.record()
@@ -178,11 +209,18 @@ def bench_prune_gpu(args, dev) -> dict:
         leaves += one_run()
     end.record()
     torch.cuda.synchronize(dev)
-    launches = lib.loki_launch_count() - c0
+    launches = run_launches * args.steps
     ms = start.elapsed_time(end)
+    lstart = torch.cuda.Event(enable_timing=True)
+    lend = torch.cuda.Event(enable_timing=True)
+    lstart.record()
+    lleaves = sum(level_run() for _ in range(args.steps))
+    lend.record()
+    torch.cuda.synchronize(dev)
+    level_ms = lstart.elapsed_time(lend)
     # the score kernel's own time for the roofline: one more run with CUDA
     # events around every score launch, outside the timed runs
-    one_run(score_events)
+    level_run(score_events)
     torch.cuda.synchronize(dev)
     score_ms = sum(e0.elapsed_time(e1) for _, e0, e1 in score_events)
     score_leaves = sum(n for n, _, _ in score_events)
@@ -228,12 +266,35 @@ def bench_prune_gpu(args, dev) -> dict:
         dt = time.perf_counter() - t0
         nl = sum(st.n_leaves for r in res.values() for st in r["level_stats"][1:])
         multi[f"workers_{nw}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
+    # batched: the same runs device-resident, one CUDA graph per run, one
+    # stream per concurrent run, enqueued from one host thread
+    from pyloki_gb300.prune import run_batch
+
+    for ns in (1, args.prune_streams):
+        jobs = [(dyp, r) for r in refs]
+        run_batch(jobs, thr, n_streams=ns, max_sugg=PRUNE_MAX_SUGG,
+                  batch_size=PRUNE_BATCH)  # capture of every run's graph
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        res = run_batch(jobs, thr, n_streams=ns, max_sugg=PRUNE_MAX_SUGG,
+                        batch_size=PRUNE_BATCH)
+        torch.cuda.synchronize(dev)
+        dt = time.perf_counter() - t0
+        nl = sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+        multi[f"batched_streams_{ns}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
     multi["runs"] = len(refs)
     multi["ref_segments"] = refs
     multi["speedup"] = (multi[f"workers_{args.prune_workers}"]["leaves_per_s"]
                         / multi["workers_1"]["leaves_per_s"])
+    multi["batched_speedup_vs_plain"] = (
+        multi[f"batched_streams_{args.prune_streams}"]["leaves_per_s"]
+        / (lleaves / (level_ms * 1e-3)))
     return {
         "metric": "prune leaves/s", "value": leaves / (ms * 1e-3), "unit": "leaves/s",
+        "path": "device-resident levels, one CUDA graph per run (loki_prune_run)",
+        "level_path": {"value": lleaves / (level_ms * 1e-3),
+                       "ms_per_step": level_ms / args.steps,
+                       "note": "level by level with two host waits per level"},
         "multi_run": multi,
         "ms_per_step": ms / args.steps, "leaves_per_step": leaves // args.steps,
         "dtype": "f32 folds, f64 parameters",
@@ -243,7 +304,7 @@ def bench_prune_gpu(args, dev) -> dict:
                    "ffa_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
                    "widths": cfg.score_widths.tolist(), "max_sugg": PRUNE_MAX_SUGG,
                    "batch_size": PRUNE_BATCH, "ref_segment": ref,
-                   "thresholds": f"{PRUNE_THRESHOLD_FINAL} * sqrt(level / {nseg - 1})",
+                   "thresholds": PRUNE_SCHEME_NOTE,
                    "orbit": {"p_orb_h": orbit[0] / 3600, "x_lts": orbit[1], "psi": orbit[2]},
                    "l2": "segment folds (75 KB) are L2-resident; tree folds stream"},
         "roofline": {"kernel": "prune_score_kernel (resolve + gather + shift-add + score)",
@@ -399,10 +460,13 @@ def bench_gpu(args) -> dict | None:
         if dist is not None:
             dist.barrier()
 
-    def one_step(events=None, storage="f32"):
+    final_path = {}
+
+    def one_step(events=None, storage="f32", norm=None):
         dyp = DynamicProgramming(ts_dev, cfg, device=dev, storage=storage)
         snr = dyp.search(band_bytes=args.band_bytes, phase_events=events, final=args.final,
-                         norm=args.norm)
+                         norm=norm or args.norm)
+        final_path["path"] = dyp.final_path
         return dyp, snr
 
     for _ in range(args.warmup):
@@ -450,6 +514,21 @@ def bench_gpu(args) -> dict | None:
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps, dist, dev)
 
+    # the bit-exact normalisation, same search, for comparison (not the headline)
+    norm_exact = None
+    if args.norm == "fast":
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            _, snr = one_step(norm="exact")
+            del snr
+        e1.record()
+        barrier()
+        ex_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, dev)
+        norm_exact = {"value": world * trials / (ex_ms * 1e-3), "ms_per_step": ex_ms}
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -462,8 +541,10 @@ def bench_gpu(args) -> dict | None:
     achieved = ab / (dom_ms * 1e-3) / 1e9
     dom_launches = max(1, phase_launches[dom] // args.steps)
     traffic = None
-    if dom == "final":  # DRAM bytes per final trial from the ncu capture, x trials per launch
-        traffic = UNION_DRAM_BYTES_PER_TRIAL * trials / dom_launches
+    fpath = final_path["path"]
+    if dom == "final" and fpath in FINAL_DRAM_BYTES_PER_TRIAL:
+        # DRAM bytes per final trial from the ncu capture, x trials per launch
+        traffic = FINAL_DRAM_BYTES_PER_TRIAL[fpath] * trials / dom_launches
     out = {
         "metric": METRIC,
         "value": world * trials / (ms_per_step * 1e-3),
@@ -482,21 +563,22 @@ def bench_gpu(args) -> dict | None:
                    "widths": cfg.score_widths.tolist(), "levels": cfg.niters_ffa,
                    "final_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
                    "trials_per_step": trials, "band_bytes": args.band_bytes,
+                   "final_path": fpath,
+                   "norm": ("fast: e * rsqrt(v), S/N within 1e-5 of the bit-exact search"
+                            if args.norm == "fast" else "exact: bit-identical S/N"),
                    "l2": "inputs larger than L2 (>51 GB read per step)",
                    "parallelism": f"replicas x{world}"},
         "phases_ms": {k: v / args.steps for k, v in phases.items()},
         "roofline": {"kernel": {"brutefold": "brutefold_seq_kernel (+phase_map_kernel)",
                                 "levels": "ffa_level64_kernel (materialised levels)",
-                                "final": "band_union64_kernel (penultimate band + fused "
-                                         "final-level scoring)"}[dom],
+                                "final": FINAL_KERNEL[fpath]}[dom],
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "launches_per_step": dom_launches,
                      "algorithmic_bytes_per_launch": ab / dom_launches,
                      "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read+write of band_union64_kernel, "
-                                       "three full-band launches of this search at 1 GiB "
-                                       "bands, per final trial x trials per launch"
+                     "traffic_source": "ncu dram__bytes_read+write per final trial at 2^21 "
+                                       "samples x trials per launch"
                                        if traffic is not None else None},
         "e2e": {"value": world * trials / (e2e_ms * 1e-3), "unit": "trials/s",
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": 2 * 4 * cfg.nsamps,
@@ -506,6 +588,8 @@ def bench_gpu(args) -> dict | None:
         "clocks": clocks.summary(),
         "best_candidate": {k: float(v) for k, v in best.items()},
     }
+    if norm_exact is not None:
+        out["norm_exact"] = norm_exact
     if world == 1 and not args.no_cpu_baseline:
         cfg_b = cpu_band_cfg(args.cpu_band_hz)
         from oracle import oracle as O
@@ -704,33 +788,91 @@ def bench_thresholds(args, dev, branching_pattern) -> dict:
                     "these parameters on its CPU (numba)"}
 
 
+class PruneInjections:
+    """Series of the pruning workload made on the GPU by the reference's
+    generator (``pulse.PulseSignalConfig``: folded S/N calibrated on the
+    folds, ``simulation/pulse.py:71-118``): a 3 ms pulsar (von Mises, 5 %
+    duty, S/N 10) in a circular orbit with P_orb 2-10 h, x 0.1-2 lt-s and an
+    orbital phase drawn from the seed; or the same noise alone. 2^22 samples
+    of 64 us, made ``batch`` seeds at a time."""
+
+    def __init__(self, dev, batch: int = 32) -> None:
+        self.dev = dev
+        self.batch = batch
+        self._cache: dict = {}
+
+    @staticmethod
+    def signal(seed: int):
+        from pyloki_gb300.pulse import PulseSignalConfig
+
+        rng = np.random.default_rng(seed)
+        orb = {"p_orb": rng.uniform(2.0, 10.0) * 3600.0, "x_orb": rng.uniform(0.1, 2.0),
+               "psi": rng.uniform(0.0, 2 * np.pi)}
+        return PulseSignalConfig(period=3e-3, dt=64e-6, nsamps=2**22, snr=10.0, ducy=0.05,
+                                 mod_type="circular", mod_kwargs=orb)
+
+    def __call__(self, seed: int, inject: bool):
+        from pyloki_gb300.pulse import generate_injections
+        from pyloki_gb300.timeseries import TimeSeries
+
+        if not inject:
+            return self.signal(seed).generate_noise(seed=seed, device=self.dev)
+        base = seed - seed % self.batch
+        hit = self._cache.get("inj")
+        if hit is None or hit[0] != base:
+            cfgs = [self.signal(s) for s in range(base, base + self.batch)]
+            b = generate_injections(cfgs, shape="von_mises", seed=base, device=self.dev)
+            hit = self._cache["inj"] = (base, b)
+        b = hit[1]
+        i = seed - base
+        return TimeSeries(b.ts_e[i], b.ts_v[i], b.dt)
+
+
+def clopper_pearson(k: int, n: int, conf: float = 0.95) -> tuple[float, float]:
+    """Exact binomial confidence interval of k successes in n trials."""
+    from scipy import stats
+
+    a = (1 - conf) / 2
+    lo = 0.0 if k == 0 else float(stats.beta.ppf(a, k, n - k + 1))
+    hi = 1.0 if k == n else float(stats.beta.ppf(1 - a, k + 1, n - k))
+    return lo, hi
+
+
 def bench_learned(args, dev) -> dict:
     """Learned branch proposal on the pruning workload: the MLP is trained on
     the GPU on branch statistics of plain runs over seeded injections, then
     plain and learned pruning run on held-out injections and noise-only
-    series (a bounded sample of the 10,000 / 1,000 / 1,000 design)."""
+    series. The full design is 10,000 / 1,000 / 1,000 series; the default run
+    takes a bounded sample (--learned-train / --learned-test)."""
     from pyloki_gb300.learned import study
-    from pyloki_gb300.simulation import make_series as ms
 
     cfg = make_prune_cfg()
-
-    def series(seed: int, inject: bool):
-        if inject:
-            return make_prune_series(seed)[0]
-        return ms(2**22, 64e-6, seed=seed)
-
     nseg = cfg.nsamps // cfg.bseg_ffa
     n_tr, n_te = args.learned_train, args.learned_test
-    res = study(cfg, prune_thresholds(nseg), series,
+    gen = PruneInjections(dev)
+    res = study(cfg, prune_thresholds(nseg), gen,
                 train_seeds=list(range(10_000, 10_000 + n_tr)),
                 test_seeds=list(range(20_000, 20_000 + n_te)),
                 noise_seeds=list(range(30_000, 30_000 + n_te)),
                 budget=args.learned_budget, lookahead=16, per_level=2048, epochs=6,
                 score_share=args.learned_score_share,
                 max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH, device=dev)
+    inj, noise = res["injected"], res["noise"]
+    for bud, row in res["budgets"].items():
+        k = sum(r["learned"][int(bud)]["best"] >= r["plain_best"] - 1e-3 for r in inj)
+        row["recall_ci95"] = clopper_pearson(int(k), len(inj)) if inj else None
+        fa = sum(r["learned"][int(bud)]["best"] >= res["det_snr"] for r in noise)
+        row["false_alarm_ci95"] = clopper_pearson(int(fa), len(noise)) if noise else None
+    det = sum(r["plain_best"] >= res["det_snr"] for r in inj)
+    res["plain_detection"] = {"rate": det / max(len(inj), 1),
+                              "ci95": clopper_pearson(int(det), len(inj)) if inj else None}
     res["workload"] = PRUNE_WORKLOAD
     res["sample"] = (f"{n_tr} training injections, {n_te} held-out injections, {n_te} "
-                     "noise-only series (seeded)")
+                     "noise-only series (seeded; GPU generator with the reference's S/N "
+                     "calibration)")
+    if len(inj) >= 100:  # per-series records stay in the detail file only for small studies
+        res.pop("injected")
+        res.pop("noise")
     return res
 
 
@@ -1046,8 +1188,9 @@ def main() -> None:
     ap.add_argument("--band-bytes", type=int, default=1 << 30)
     ap.add_argument("--final", choices=["auto", "tiled", "banded", "level"], default="auto",
                     help="how the last two FFA levels run")
-    ap.add_argument("--norm", choices=["exact", "fast"], default="exact",
-                    help="profile normalisation of the tiled final levels")
+    ap.add_argument("--norm", choices=["exact", "fast"], default="fast",
+                    help="profile normalisation of the tiled final levels: fast = e * rsqrt(v) "
+                         "(S/N within 1e-5 of exact), exact = bit-identical to the reference")
     ap.add_argument("--cpu-band-hz", type=float, default=4.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-bf16", action="store_true",
@@ -1062,6 +1205,8 @@ def main() -> None:
                     help="one untimed 64-injection set (the generator ncu command)")
     ap.add_argument("--prune-workers", type=int, default=PRUNE_WORKERS,
                     help="host threads (each with its own stream) of the multi-run pruning")
+    ap.add_argument("--prune-streams", type=int, default=PRUNE_STREAMS,
+                    help="concurrent device-resident runs of the batched pruning measurement")
     ap.add_argument("--prune-runs", type=int, default=PRUNE_MULTI_RUNS,
                     help="reference segments of the multi-run pruning")
     ap.add_argument("--no-fourier", action="store_true",
@@ -1079,7 +1224,7 @@ def main() -> None:
     ap.add_argument("--learned-score-share", type=float, default=0.5,
                     help="share of each level's parent budget given to the best-scoring "
                          "parents (the rest is ranked by the network)")
-    ap.add_argument("--learned-budget", type=int, nargs="+", default=[16384, 65536, 131072],
+    ap.add_argument("--learned-budget", type=int, nargs="+", default=[4096, 8192, 16384],
                     help="parents expanded per level under the learned proposal")
     ap.add_argument("--no-prune", action="store_true",
                     help="skip the enumerate-prune (leaves/s) measurement")
@@ -1154,8 +1299,10 @@ def headline(out: dict) -> dict:
     h = {k: out[k] for k in HEADLINE_KEYS if k in out}
     cfg = out.get("config", {})
     h["config"] = {k: cfg[k] for k in ("workload", "nsamps", "trials_per_step", "final_grid",
-                                       "widths", "l2", "parallelism", "sample_band_hz")
+                                       "widths", "norm", "l2", "parallelism", "sample_band_hz")
                    if k in cfg}
+    if "norm_exact" in out:
+        h["norm_exact"] = out["norm_exact"]
     for k in ("roofline", "cpu_baseline", "e2e"):
         if k in out:
             h[k] = {kk: vv for kk, vv in out[k].items()

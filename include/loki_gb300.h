@@ -35,6 +35,7 @@ extern "C" {
 #define LOKI_DEVERR_WINDOW 1   /* resolved index outside the input window */
 #define LOKI_DEVERR_BRANCH 2   /* branch count above branch_max */
 #define LOKI_DEVERR_TIMEOUT 4  /* a bounded wait on the tensor cores gave up */
+#define LOKI_DEVERR_CAPACITY 8 /* a device-counted run outgrew a workspace */
 
 #define LOKI_MAX_PARAMS 5
 #define LOKI_MAX_WIDTHS 64
@@ -556,6 +557,53 @@ int loki_prune_level(const LokiPruneLevel* lvl, const LokiPruneTree* in, LokiPru
                      const LokiScoreSpec* spec, double threshold, int64_t max_sugg,
                      int64_t batch_size, const uint8_t* parent_mask, LokiPruneLevelResult* res,
                      int32_t* dev_err, void* stream);
+
+/* Per-level record of a device-resident run (loki_prune_run). n_children is
+ * the count the level asked for, also when it exceeded the workspace. */
+typedef struct {
+  int64_t n_parents;
+  int64_t n_children;
+  int64_t n_surv;
+  float score_min;
+  float score_max;
+  int32_t overflow;        /* the overflow rule ran */
+  int32_t reserved;
+} LokiPruneLevelStats;
+
+/* Buffers of loki_prune_run (device unless noted; all caller-owned). */
+typedef struct {
+  LokiPruneTree trees[2];       /* ping-pong trees, cap >= max_sugg; trees[0] holds the seed */
+  LokiPruneWork work;           /* par_cap >= max_sugg, ovf_cap >= max_sugg + child_cap + 1;
+                                   host_words and the events are not used */
+  int64_t* counts;              /* 4 words: parents, children, survivors of the level */
+  int32_t* ovf_flag;            /* 1 word */
+  LokiPruneLevelStats* stats;   /* nlevels records */
+  double* best_leaves;          /* nlevels rows of (poly_order + 2) * 2, or NULL */
+  float* best_scores;           /* nlevels, or NULL */
+  int32_t* bt_hist;             /* bt_rows x (poly_order + 2): every level's survivors'
+                                   backtracks in level order, or NULL */
+  int64_t bt_rows;
+} LokiPruneRun;
+
+/* Every level of one reference segment (prune.py:526-613 Pruning.execute
+ * without the ascend; the same kernels as loki_prune_level) enqueued on the
+ * stream with all counts kept on the device: no host wait, so a whole run
+ * can be captured in a CUDA graph and replayed. Level l (1-based) reads
+ * trees[(l - 1) & 1], writes trees[l & 1], adds segment seg_idx[l - 1] of
+ * ffa_folds (segment stride seg_stride floats) at threshold
+ * thresholds[l - 1]; stats[l - 1] records it, best_* its best leaf and
+ * bt_hist its survivors' backtracks (after those of the levels before). A
+ * level without survivors leaves every later level empty. A workspace that
+ * is too small sets LOKI_DEVERR_CAPACITY in *dev_err (the run's results are
+ * then void: grow work.child_cap to the largest stats[].n_children, or
+ * bt_rows to the sum of stats[].n_surv, and run again); a branch count above
+ * branch_max sets LOKI_DEVERR_BRANCH. No reference counterpart
+ * as one call: it replaces the per-level loop of Pruning.execute. */
+int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const float* ffa_folds,
+                   int64_t seg_stride, const int32_t* seg_idx, const double* thresholds,
+                   const LokiScoreSpec* spec, int64_t seed_n, int64_t max_sugg,
+                   int64_t batch_size, const LokiPruneRun* run, int32_t* dev_err,
+                   void* stream);
 
 /* Best leaf of a tree (utils/world_tree.py:441-459 get_best_k with k = 1):
  * the leaf row (row_len float64) and score of the maximum score, first index

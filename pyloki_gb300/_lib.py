@@ -21,6 +21,7 @@ LOKI_ERR_CAPACITY = -4
 LOKI_DEVERR_WINDOW = 1
 LOKI_DEVERR_BRANCH = 2
 LOKI_DEVERR_TIMEOUT = 4
+LOKI_DEVERR_CAPACITY = 8
 
 MAX_PARAMS = 5
 MAX_WIDTHS = 64
@@ -157,6 +158,25 @@ class LokiPruneLevelResult(C.Structure):
                 ("need_tree_cap", C.c_int64)]
 
 
+class LokiPruneLevelStats(C.Structure):
+    _fields_ = [("n_parents", C.c_int64), ("n_children", C.c_int64), ("n_surv", C.c_int64),
+                ("score_min", C.c_float), ("score_max", C.c_float), ("overflow", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class LokiPruneRun(C.Structure):
+    _fields_ = [("trees", LokiPruneTree * 2), ("work", LokiPruneWork), ("counts", C.c_void_p),
+                ("ovf_flag", C.c_void_p), ("stats", C.c_void_p), ("best_leaves", C.c_void_p),
+                ("best_scores", C.c_void_p), ("bt_hist", C.c_void_p), ("bt_rows", C.c_int64)]
+
+
+#: numpy view of an array of LokiPruneLevelStats records
+PRUNE_STATS_DTYPE = np.dtype([("n_parents", np.int64), ("n_children", np.int64),
+                              ("n_surv", np.int64), ("score_min", np.float32),
+                              ("score_max", np.float32), ("overflow", np.int32),
+                              ("reserved", np.int32)])
+
+
 class LokiMLP(C.Structure):
     _fields_ = [("w1", C.c_void_p), ("b1", C.c_void_p), ("w2", C.c_void_p),
                 ("b2", C.c_void_p), ("w3", C.c_void_p), ("b3", C.c_void_p)]
@@ -249,6 +269,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_branch_masked": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_best": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P]),
+    "loki_prune_run": (C.c_int, [_PL, _I32, _P, _I64, _P, _P, C.POINTER(LokiScoreSpec), _I64,
+                                 _I64, _I64, C.POINTER(LokiPruneRun), _P, _P]),
     "loki_prune_level": (C.c_int, [_PL, C.POINTER(LokiPruneTree), C.POINTER(LokiPruneTree),
                                    C.POINTER(LokiPruneWork), _P, C.POINTER(LokiScoreSpec), _D,
                                    _I64, _I64, _P, C.POINTER(LokiPruneLevelResult), _P, _P]),
@@ -340,6 +362,9 @@ def check_dev_err(err_word) -> None:
         raise ValueError(msg)
     if v & LOKI_DEVERR_TIMEOUT:
         msg = "a bounded wait for the tensor cores timed out"
+        raise LokiError(msg)
+    if v & LOKI_DEVERR_CAPACITY:
+        msg = "a device-counted run outgrew its workspace"
         raise LokiError(msg)
     if v:
         msg = f"device error word {v}"

@@ -540,11 +540,16 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in,
 // share the rows of the level before (L2 hits) and each of its profiles comes
 // from DRAM about once.
 //
-// Shared row layout: 128 float2 (e, v) per penultimate row, position p holding
-// bin p mod 64, so the roll by a trial's shift s reads positions 64 - s + j,
-// j = 0..63, with no wrap and compile-time offsets. Consecutive lanes hold
-// consecutive final frequencies, whose rows and shifts advance by about half a
-// row and half a bin per lane, so the lanes of a warp spread over the banks.
+// Shared row layout: 64 float2 (e, v) per penultimate row (512 bytes, rows
+// 512-byte aligned), so a trial rolled by shift s reads bin (j - s) mod 64 at
+// byte (8 * (64 - s + j)) mod 512 of the row: one add and one and-or per load.
+// Compact rows let six 4-warp CTAs share an SM (36 rows per side: one final
+// other's 64 frequencies span at most 34 penultimate rows), and a chunk of two
+// final others (the usual group size of an acceleration search) is exactly
+// one 32-trial task per warp, so no warp idles while the others score.
+// Consecutive lanes hold consecutive final frequencies, whose rows and shifts
+// advance by about half a row and half a bin per lane, so the lanes of a warp
+// spread over the banks.
 //
 // FAST: the profile is normalised as e * rsqrtf(v) (at most a few ulp from the
 // reference's e / sqrt(v)); otherwise with correctly rounded division and
@@ -552,10 +557,10 @@ ffa_level_score_kernel(LokiFFALevel L, LevelK K, const S* __restrict__ in,
 // ---------------------------------------------------------------------------
 
 constexpr int kTileF = 64;        // final frequencies per tile
-constexpr int kTileWarps = 8;
-constexpr int kTileRows = 48;     // shared penultimate rows per side (tail, head)
+constexpr int kTileWarps = 4;
+constexpr int kTileRows = 36;     // shared penultimate rows per side (tail, head)
 constexpr int kTileMembers = 8;   // final others per chunk of a group
-constexpr int kTileSmem = 2 * kTileRows * 128 * (int)sizeof(float2);
+constexpr int kTileRowBytes = 64 * (int)sizeof(float2);
 
 // Final others grouped by their (tail, head) penultimate other: groups[0] is
 // the group count G, groups[1 + g] the first other of group g, groups[1 + G] =
@@ -624,10 +629,10 @@ __device__ __forceinline__ float round_store<__nv_bfloat16>(float x) {
   return __bfloat162float(__float2bfloat16_rn(x));
 }
 
-// Builds penultimate rows [row0, row1) of the tile (row r < nt: tail side,
-// frequency lo_t + r of penultimate other pt in segment s_t; else head side)
-// into shared memory. Warp w owns a contiguous run of rows; lane k resolves
-// row k of the run and the warp then gathers row by row.
+// Builds the tile's penultimate rows (row r < nt: tail side, frequency lo_t + r
+// of penultimate other pt in segment s_t; else head side) into shared memory.
+// Warp w owns a contiguous run of rows; lane k resolves row k of the run and
+// the warp then gathers row by row.
 template <typename S>
 __device__ __forceinline__ void tile_build(const LokiFFALevel& P, const LevelK& KP,
                                            const S* __restrict__ fold_pp,
@@ -637,7 +642,7 @@ __device__ __forceinline__ void tile_build(const LokiFFALevel& P, const LevelK& 
                                            int64_t s_h, int32_t* err) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int R = nt + nh;
-  const int per = (R + kTileWarps - 1) / kTileWarps;  // <= 2 * kTileRows / 8 = 12
+  const int per = (R + kTileWarps - 1) / kTileWarps;  // <= 2 * kTileRows / 4 = 20
   const int r0 = warp * per;
   const int r1 = std::min(R, r0 + per);
   const int64_t P_in = n_in_params(P);
@@ -662,9 +667,9 @@ __device__ __forceinline__ void tile_build(const LokiFFALevel& P, const LevelK& 
     const int32_t ih = __shfl_sync(0xFFFFFFFFu, my_h, k);
     const int32_t sh2 = __shfl_sync(0xFFFFFFFFu, my_sh, k);
     const bool ok = __shfl_sync(0xFFFFFFFFu, my_ok, k);
-    float2* dst = rows + (size_t)(r < nt ? r : kTileRows + (r - nt)) * 128;
+    float2* dst = rows + (size_t)(r < nt ? r : kTileRows + (r - nt)) * 64;
     if (!ok) {
-      dst[lane] = dst[lane + 32] = dst[lane + 64] = dst[lane + 96] = make_float2(0.f, 0.f);
+      dst[lane] = dst[lane + 32] = make_float2(0.f, 0.f);
       continue;
     }
     const int64_t seg8 = r < nt ? s_t : s_h;
@@ -679,44 +684,88 @@ __device__ __forceinline__ void tile_build(const LokiFFALevel& P, const LevelK& 
         round_store<S>(__fadd_rn(Store<S>::load(t + 64 + jt0), Store<S>::load(h + 64 + jh0)));
     const float v1 =
         round_store<S>(__fadd_rn(Store<S>::load(t + 64 + jt1), Store<S>::load(h + 64 + jh1)));
-    dst[lane] = dst[lane + 64] = make_float2(e0, v0);
-    dst[lane + 32] = dst[lane + 96] = make_float2(e1, v1);
+    dst[lane] = make_float2(e0, v0);
+    dst[lane + 32] = make_float2(e1, v1);
   }
 }
 
-// S/N of one final trial from its rolled tail and head rows (lane-per-trial).
+// (e, v) of bin j of a compact row whose roll starts at byte offset `off`
+// (= 8 * ((64 - s) mod 64)); `base` is the row's 512-aligned shared address.
+__device__ __forceinline__ float2 tile_ld(uint32_t base, uint32_t off, int j) {
+  const uint32_t a = base | ((off + 8u * (uint32_t)j) & 511u);
+  float2 r;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "r"(a));
+  return r;
+}
+
+// S/N of one final trial from its tail and head rows (lane-per-trial). The
+// prefix sum runs sequentially in float32 as circular_prefix_sum does and is
+// kept as register pairs P2[k] = (P[2k], P[2k + 1]); every even width's
+// window differences are packed f32x2 subtractions of two pairs, folded into
+// the running maximum three at a time. The differences and the maximum are
+// the reference's, so the S/N is unchanged.
 template <bool FAST, int NW>
-__device__ __forceinline__ void tile_score_trial(const float2* __restrict__ bt,
-                                                 const float2* __restrict__ bh,
-                                                 const LokiScoreSpec& sp, const ScoreK& SK,
-                                                 float* __restrict__ out) {
+__device__ __forceinline__ void tile_score_trial(uint32_t bt, uint32_t ot, uint32_t bh,
+                                                 uint32_t oh, const LokiScoreSpec& sp,
+                                                 const ScoreK& SK, float* __restrict__ out) {
   constexpr int WMAX = 1 << (NW - 1);
-  float pf[64];
+  unsigned long long P2[32];
   float m[NW];
 #pragma unroll
   for (int iw = 0; iw < NW; ++iw) m[iw] = -FLT_MAX;
-  float s = 0.0f;
+  float s = 0.0f, prev = 0.0f;
 #pragma unroll
-  for (int j = 0; j < 64; ++j) {
-    const float2 a = bt[j], c = bh[j];
-    const float e = __fadd_rn(a.x, c.x);
-    const float v = __fadd_rn(a.y, c.y);
-    const float nv = FAST ? __fmul_rn(e, rsqrtf(v)) : __fdiv_rn(e, __fsqrt_rn(v));
-    s = j == 0 ? nv : __fadd_rn(s, nv);
-    pf[j] = s;
+  for (int k = 0; k < 32; ++k) {
+    float nv[2];
 #pragma unroll
-    for (int iw = 0; iw < NW; ++iw)
-      if (j >= (1 << iw)) m[iw] = fmaxf(m[iw], __fsub_rn(pf[j], pf[j - (1 << iw)]));
+    for (int q = 0; q < 2; ++q) {
+      const float2 a = tile_ld(bt, ot, 2 * k + q), c = tile_ld(bh, oh, 2 * k + q);
+      const float e = __fadd_rn(a.x, c.x);
+      const float v = __fadd_rn(a.y, c.y);
+      nv[q] = FAST ? __fmul_rn(e, rsqrtf(v)) : __fdiv_rn(e, __fsqrt_rn(v));
+    }
+    const float s0 = k == 0 ? nv[0] : __fadd_rn(s, nv[0]);
+    s = __fadd_rn(s0, nv[1]);
+    P2[k] = pack2(s0, s);
+    // width 1: P[2k] - P[2k - 1] and P[2k + 1] - P[2k]
+    if (k == 0) m[0] = fmaxf(m[0], __fsub_rn(s, s0));
+    else m[0] = max3(m[0], __fsub_rn(s0, prev), __fsub_rn(s, s0));
+    prev = s;
+#pragma unroll
+    for (int iw = 1; iw < NW; ++iw) {
+      const int H = 1 << (iw - 1);  // width 2H
+      if (k >= H) {
+        unsigned long long d;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(P2[k]), "l"(P2[k - H]));
+        float d0, d1;
+        unpack2(d, d0, d1);
+        m[iw] = max3(m[iw], d0, d1);
+      }
+    }
   }
   const float total = s;
-  // circular extension P[64 + k] = P[k] + total (scoring.py:42-71), k-major so
-  // that P[k] and P[64 - w + k] are dead once used
+  // circular extension P[64 + i] = P[i] + total (scoring.py:42-71)
+  {
+    float p0, p1;
+    unpack2(P2[0], p0, p1);
+    m[0] = fmaxf(m[0], __fsub_rn(__fadd_rn(p0, total), prev));  // P[64] - P[63]
+  }
+  const unsigned long long tt = pack2(total, total);
 #pragma unroll
-  for (int k = 0; k < WMAX; ++k) {
-    const float ext = __fadd_rn(pf[k], total);
+  for (int k = 0; k < WMAX / 2; ++k) {
+    unsigned long long ext;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(ext) : "l"(P2[k]), "l"(tt));
 #pragma unroll
-    for (int iw = 0; iw < NW; ++iw)
-      if (k < (1 << iw)) m[iw] = fmaxf(m[iw], __fsub_rn(ext, pf[64 - (1 << iw) + k]));
+    for (int iw = 1; iw < NW; ++iw) {
+      const int H = 1 << (iw - 1);
+      if (k < H) {
+        unsigned long long d;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(ext), "l"(P2[32 - H + k]));
+        float d0, d1;
+        unpack2(d, d0, d1);
+        m[iw] = max3(m[iw], d0, d1);
+      }
+    }
   }
   float best = -FLT_MAX;
 #pragma unroll
@@ -737,14 +786,15 @@ __device__ __forceinline__ void tile_score_trial(const float2* __restrict__ bt,
 }
 
 template <typename S, bool FAST, int NW>
-__global__ void __launch_bounds__(kTileWarps * 32, 2)
+__global__ void __launch_bounds__(kTileWarps * 32, 6)
 ffa_final_tiled64_kernel(LokiFFALevel P, LevelK KP, const S* __restrict__ fold_pp,
                          const OtherRes* __restrict__ tab_p, int64_t no_p, LokiFFALevel F,
                          LevelK KF, const OtherRes* __restrict__ tab_f, int64_t no_f,
                          const int32_t* __restrict__ groups, LokiScoreSpec sp, ScoreK SK,
                          float* __restrict__ snr, int32_t* __restrict__ err) {
-  extern __shared__ float2 rows[];  // [2][kTileRows][128]
-  __shared__ int64_t win[4];        // tail lo, tail hi, head lo, head hi
+  __shared__ __align__(512) float2 rows[2 * kTileRows * 64];  // [side][row][bin]
+  __shared__ int64_t win[4];  // tail lo, tail hi, head lo, head hi
+  const uint32_t rows_sh = (uint32_t)__cvta_generic_to_shared(rows);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n = F.nparams;
   const int64_t nlast = F.counts_cur[n - 1];
@@ -818,9 +868,11 @@ ffa_final_tiled64_kernel(LokiFFALevel P, LevelK KP, const S* __restrict__ fold_p
           for (int k = 0; k < nout; ++k) out[k] = __int_as_float(0x7fc00000);
           continue;
         }
-        const float2* bt = rows + (size_t)rt * 128 + (64 - tr.s_tail);
-        const float2* bh = rows + (size_t)(kTileRows + rh) * 128 + (64 - tr.s_head);
-        tile_score_trial<FAST, NW>(bt, bh, sp, SK, out);
+        const uint32_t bt = rows_sh + (uint32_t)rt * kTileRowBytes;
+        const uint32_t bh = rows_sh + (uint32_t)(kTileRows + rh) * kTileRowBytes;
+        const uint32_t offt = 8u * (uint32_t)((64 - tr.s_tail) & 63);
+        const uint32_t offh = 8u * (uint32_t)((64 - tr.s_head) & 63);
+        tile_score_trial<FAST, NW>(bt, offt, bh, offh, sp, SK, out);
       }
       c0 = c1;
     }
@@ -1223,19 +1275,16 @@ static int launch_tiled_t(const LokiFFALevel& P, const LevelK& KP, const void* f
                           const int32_t* groups, const LokiScoreSpec& sp, const ScoreK& SK,
                           float* snr, int32_t* err, cudaStream_t s) {
   auto kern = ffa_final_tiled64_kernel<S, FAST, NW>;
-  if (set_smem_limit(kern, kTileSmem) != cudaSuccess)
-    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileWarps * 32,
-                                                    kTileSmem) != cudaSuccess)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTileWarps * 32, 0) !=
+          cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "occupancy query failed");
   const int grid = std::max(1, nsm * std::max(1, per_sm));
   note_launch();
-  kern<<<grid, kTileWarps * 32, kTileSmem, s>>>(P, KP, static_cast<const S*>(fold_pp), tab_p,
-                                                no_p, F, KF, tab_f, no_f, groups, sp, SK, snr,
-                                                err);
+  kern<<<grid, kTileWarps * 32, 0, s>>>(P, KP, static_cast<const S*>(fold_pp), tab_p, no_p, F,
+                                        KF, tab_f, no_f, groups, sp, SK, snr, err);
   return LOKI_OK;
 }
 

@@ -35,11 +35,12 @@ __device__ __forceinline__ int64_t scan_in(const void* in, int64_t i, int64_t n,
   return reinterpret_cast<const int64_t*>(in)[i];
 }
 
+// One kScanBlock-element tile of the scan: exclusive within the tile, the
+// tile's total in sums[tile].
 template <bool FLAGS>
-__global__ void __launch_bounds__(kScanBlock)
-scan_block_kernel(const void* in, int64_t n, double thr, int64_t* out, int64_t* sums) {
-  __shared__ int64_t warp_tot[32];
-  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+__device__ __forceinline__ void scan_tile(const void* in, int64_t n, double thr, int64_t* out,
+                                          int64_t* sums, int64_t tile, int64_t* warp_tot) {
+  const int64_t i = tile * kScanBlock + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t x = scan_in<FLAGS>(in, i, n, thr);
   int64_t v = x;
@@ -62,15 +63,41 @@ scan_block_kernel(const void* in, int64_t n, double thr, int64_t* out, int64_t* 
   __syncthreads();
   const int64_t incl = v + (warp ? warp_tot[warp - 1] : 0);
   if (i < n) out[i] = incl - x;  // exclusive within the block
-  if (threadIdx.x == kScanBlock - 1) sums[blockIdx.x] = incl;
+  if (threadIdx.x == kScanBlock - 1) sums[tile] = incl;
+  __syncthreads();  // warp_tot is reused by the next tile
+}
+
+// n_dev, when not null, holds the element count on the device: the blocks
+// then stride over its tiles.
+template <bool FLAGS>
+__global__ void __launch_bounds__(kScanBlock)
+scan_block_kernel(const void* in, int64_t n, const int64_t* n_dev, double thr, int64_t* out,
+                  int64_t* sums) {
+  __shared__ int64_t warp_tot[32];
+  if (!n_dev) {
+    scan_tile<FLAGS>(in, n, thr, out, sums, blockIdx.x, warp_tot);
+    return;
+  }
+  n = *n_dev;
+  const int64_t ntiles = (n + kScanBlock - 1) / kScanBlock;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x)  // uniform over the block
+    scan_tile<FLAGS>(in, n, thr, out, sums, t, warp_tot);
 }
 
 // Single block: exclusive scan of the block sums (any count), carry-chained.
+// With n_dev the block count and the total's slot (out + n) come from the
+// device count.
 __global__ void __launch_bounds__(kScanBlock)
-scan_sums_kernel(int64_t* sums, int64_t nblocks, int64_t* total) {
+scan_sums_kernel(int64_t* sums, int64_t nblocks, int64_t* total, const int64_t* n_dev,
+                 int64_t* out) {
   __shared__ int64_t warp_tot[32];
   __shared__ int64_t carry;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (n_dev) {
+    const int64_t n = *n_dev;
+    nblocks = (n + kScanBlock - 1) / kScanBlock;
+    total = out + n;
+  }
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   for (int64_t base = 0; base < nblocks; base += kScanBlock) {
@@ -104,9 +131,17 @@ scan_sums_kernel(int64_t* sums, int64_t nblocks, int64_t* total) {
   if (threadIdx.x == 0) *total = carry;
 }
 
-__global__ void scan_add_kernel(int64_t* out, int64_t n, const int64_t* sums) {
-  const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
-  if (i < n) out[i] += sums[blockIdx.x];
+__global__ void scan_add_kernel(int64_t* out, int64_t n, const int64_t* n_dev,
+                                const int64_t* sums) {
+  if (!n_dev) {
+    const int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+    return;
+  }
+  n = *n_dev;
+  for (int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kScanBlock)
+    out[i] += sums[i / kScanBlock];
 }
 
 // out[0..n) exclusive scan, out[n] = total.
@@ -123,10 +158,30 @@ static int exclusive_scan(const void* in, int64_t n, double thr, int64_t* out, v
     return LOKI_OK;
   }
   for (int i = 0; i < 3; ++i) note_launch();
-  scan_block_kernel<FLAGS><<<(unsigned)nblocks, kScanBlock, 0, s>>>(in, n, thr, out, sums);
-  scan_sums_kernel<<<1, kScanBlock, 0, s>>>(sums, nblocks, out + n);
-  scan_add_kernel<<<(unsigned)nblocks, kScanBlock, 0, s>>>(out, n, sums);
+  scan_block_kernel<FLAGS><<<(unsigned)nblocks, kScanBlock, 0, s>>>(in, n, nullptr, thr, out,
+                                                                    sums);
+  scan_sums_kernel<<<1, kScanBlock, 0, s>>>(sums, nblocks, out + n, nullptr, nullptr);
+  scan_add_kernel<<<(unsigned)nblocks, kScanBlock, 0, s>>>(out, n, nullptr, sums);
   return check_launch("exclusive_scan");
+}
+
+// The same scan over a device-held count *n_dev <= n_cap (no host wait):
+// out[0..n) exclusive scan, out[n] = total. At most `grid` blocks stride over
+// the tiles.
+template <bool FLAGS>
+static int exclusive_scan_dev(const void* in, int64_t n_cap, const int64_t* n_dev, double thr,
+                              int64_t* out, void* scratch, int64_t scratch_bytes, int grid,
+                              cudaStream_t s) {
+  const int64_t ntiles = std::max<int64_t>(1, (n_cap + kScanBlock - 1) / kScanBlock);
+  if (scratch_bytes < ntiles * (int64_t)sizeof(int64_t))
+    return set_error(LOKI_ERR_CAPACITY, "scan scratch too small");
+  const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, grid));
+  int64_t* sums = reinterpret_cast<int64_t*>(scratch);
+  for (int i = 0; i < 3; ++i) note_launch();
+  scan_block_kernel<FLAGS><<<blocks, kScanBlock, 0, s>>>(in, n_cap, n_dev, thr, out, sums);
+  scan_sums_kernel<<<1, kScanBlock, 0, s>>>(sums, ntiles, nullptr, n_dev, out);
+  scan_add_kernel<<<blocks, kScanBlock, 0, s>>>(out, n_cap, n_dev, sums);
+  return check_launch("exclusive_scan_dev");
 }
 
 // ---------------------------------------------------------------------------
@@ -239,7 +294,9 @@ __device__ __forceinline__ ChildRes resolve_child(const LokiPruneLevel& D, const
 __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                                     int64_t n, LokiBranchInfo* __restrict__ info,
                                     int64_t* __restrict__ counts, int32_t* __restrict__ err,
-                                    const uint8_t* __restrict__ mask) {
+                                    const uint8_t* __restrict__ mask,
+                                    const int64_t* __restrict__ n_dev) {
+  if (n_dev) n = *n_dev;  // parent count held on the device
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int P = D.poly_order, m = P + 1;
@@ -337,20 +394,17 @@ __device__ __forceinline__ float key_float(unsigned k) {
   return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
 }
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+// Children c0 .. c0 + 31 (those below n_children) of one warp.
+__device__ __forceinline__ void score_tile(const LokiPruneLevel& D, const double* __restrict__ leaves,
                    const float* __restrict__ folds, int64_t n_parents,
                    const LokiBranchInfo* __restrict__ info, const int64_t* __restrict__ offsets,
-                   int64_t n_children, const float* __restrict__ seg, LokiScoreSpec sp,
-                   ScoreK SK, float* __restrict__ scores, int32_t* __restrict__ cidx,
-                   double* __restrict__ cphase, unsigned* __restrict__ minmax_keys) {
-  extern __shared__ float tiles[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                   int64_t n_children, const float* __restrict__ seg, const LokiScoreSpec& sp,
+                   const ScoreK& SK, float* __restrict__ scores, int32_t* __restrict__ cidx,
+                   double* __restrict__ cphase, unsigned* __restrict__ minmax_keys,
+                   float* tile, int64_t c0) {
+  const int lane = threadIdx.x & 31;
   const int nb = D.nbins, P = D.poly_order;
   const int stride = score_stride(nb, sp.wmax);
-  float* tile = tiles + (size_t)warp * 32 * stride;
-  const int64_t c0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
-  if (c0 >= n_children) return;
   const int kmax = (int)std::min<int64_t>(32, n_children - c0);
   // lane k resolves child c0 + k
   int64_t my_par = 0, my_row = 0;
@@ -441,6 +495,36 @@ prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
 }
 
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                   const float* __restrict__ folds, int64_t n_parents,
+                   const LokiBranchInfo* __restrict__ info, const int64_t* __restrict__ offsets,
+                   int64_t n_children, const float* __restrict__ seg, LokiScoreSpec sp,
+                   ScoreK SK, float* __restrict__ scores, int32_t* __restrict__ cidx,
+                   double* __restrict__ cphase, unsigned* __restrict__ minmax_keys,
+                   const int64_t* __restrict__ cnt_dev) {
+  extern __shared__ float tiles[];
+  const int warp = threadIdx.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(D.nbins, sp.wmax);
+  if (!cnt_dev) {
+    const int64_t c0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+    if (c0 < n_children)
+      score_tile(D, leaves, folds, n_parents, info, offsets, n_children, seg, sp, SK, scores,
+                 cidx, cphase, minmax_keys, tile, c0);
+    return;
+  }
+  // device counts: cnt_dev[0] parents, cnt_dev[1] children; warps stride
+  // over the 32-child tiles
+  n_parents = cnt_dev[0];
+  n_children = cnt_dev[1];
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_children;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    score_tile(D, leaves, folds, n_parents, info, offsets, n_children, seg, sp, SK, scores,
+               cidx, cphase, minmax_keys, tile, t * 32);
+    __syncwarp();  // the tile rows are rewritten by the next tile
+  }
+}
+
 __global__ void minmax_init_kernel(unsigned* keys) {
   keys[0] = 0xFFFFFFFFu;
   keys[1] = 0u;
@@ -461,7 +545,15 @@ __global__ void minmax_finish_kernel(const unsigned* keys, float* out) {
 // ---------------------------------------------------------------------------
 
 __global__ void select_scatter_kernel(const float* __restrict__ scores, int64_t n, double thr,
-                                      const int64_t* __restrict__ pos, int64_t* __restrict__ ids) {
+                                      const int64_t* __restrict__ pos, int64_t* __restrict__ ids,
+                                      const int64_t* __restrict__ n_dev) {
+  if (n_dev) {  // device count: grid-stride walk
+    n = *n_dev;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      if ((double)scores[i] >= thr) ids[pos[i]] = i;
+    return;
+  }
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n && (double)scores[i] >= thr) ids[pos[i]] = i;
 }
@@ -530,16 +622,25 @@ __device__ unsigned block_select(const unsigned* keys, int64_t n, int64_t r, uns
   return prefix;
 }
 
+// With cnt_dev (device counts: [0] parents, [2] survivors of the plain
+// selection) the kernel does nothing unless more than cap survived, and then
+// sets *ovf_flag.
 __global__ void __launch_bounds__(kSelThreads)
 select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restrict__ offsets,
                        int64_t n_parents, int64_t batch, double thr, int64_t cap,
                        int64_t* __restrict__ ids, int64_t* __restrict__ n_out,
                        double* __restrict__ thr_out, int64_t* __restrict__ tmp_ids,
-                       unsigned* __restrict__ keys) {
+                       unsigned* __restrict__ keys, const int64_t* __restrict__ cnt_dev,
+                       int32_t* __restrict__ ovf_flag) {
   __shared__ int wsum[33];
   __shared__ unsigned hist[256];
   __shared__ long long vs_sh;
   __shared__ double cur_sh;
+  if (cnt_dev) {
+    if (cnt_dev[2] <= cap) return;  // uniform over the block
+    n_parents = cnt_dev[0];
+    if (threadIdx.x == 0) *ovf_flag = 1;
+  }
   if (threadIdx.x == 0) {
     vs_sh = 0;
     cur_sh = thr;
@@ -646,8 +747,8 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
 // emit: thread per survivor for the leaf, warp per 32 survivors for folds
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+// Survivors s0 .. s0 + 31 (those below n_surv) of one warp.
+__device__ __forceinline__ void emit_tile(const LokiPruneLevel& D, const double* __restrict__ leaves,
                   const float* __restrict__ folds, const LokiBranchInfo* __restrict__ info,
                   const int64_t* __restrict__ offsets, int64_t n_parents,
                   const float* __restrict__ seg, const int64_t* __restrict__ surv,
@@ -655,11 +756,9 @@ prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                   const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
                   double* __restrict__ lout, float* __restrict__ fout,
                   float* __restrict__ sout, float* __restrict__ seout,
-                  int32_t* __restrict__ bout) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                  int32_t* __restrict__ bout, int64_t s0) {
+  const int lane = threadIdx.x & 31;
   const int nb = D.nbins, P = D.poly_order, m = P + 1;
-  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
-  if (s0 >= n_surv) return;
   const int kmax = (int)std::min<int64_t>(32, n_surv - s0);
   int64_t my_par = 0, my_row = 0;
   int my_shift = 0;
@@ -762,6 +861,33 @@ prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
       o[nb + j] = __fadd_rn(pf[nb + j], sf[nb + js]);
     }
   }
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                  const float* __restrict__ folds, const LokiBranchInfo* __restrict__ info,
+                  const int64_t* __restrict__ offsets, int64_t n_parents,
+                  const float* __restrict__ seg, const int64_t* __restrict__ surv,
+                  int64_t n_surv, const float* __restrict__ cscores,
+                  const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
+                  double* __restrict__ lout, float* __restrict__ fout,
+                  float* __restrict__ sout, float* __restrict__ seout,
+                  int32_t* __restrict__ bout, const int64_t* __restrict__ cnt_dev) {
+  const int warp = threadIdx.x >> 5;
+  if (!cnt_dev) {
+    const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+    if (s0 < n_surv)
+      emit_tile(D, leaves, folds, info, offsets, n_parents, seg, surv, n_surv, cscores, cidx,
+                cphase, lout, fout, sout, seout, bout, s0);
+    return;
+  }
+  // device counts: cnt_dev[0] parents, cnt_dev[2] survivors
+  n_parents = cnt_dev[0];
+  n_surv = cnt_dev[2];
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_surv;
+       t += (int64_t)gridDim.x * kPruneWarps)
+    emit_tile(D, leaves, folds, info, offsets, n_parents, seg, surv, n_surv, cscores, cidx,
+              cphase, lout, fout, sout, seout, bout, t * 32);
 }
 
 // ---------------------------------------------------------------------------
@@ -1757,9 +1883,11 @@ static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
 // one block reduces (score, index), then copies the leaf row and its score.
 __global__ void __launch_bounds__(1024)
 prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __restrict__ leaves,
-                  int row, double* __restrict__ leaf_out, float* __restrict__ score_out) {
+                  int row, double* __restrict__ leaf_out, float* __restrict__ score_out,
+                  const int64_t* __restrict__ n_dev) {
   __shared__ float sv[32];
   __shared__ int64_t si[32];
+  if (n_dev) n = *n_dev;  // a count of 0 writes nothing (bi stays -1)
   float bv = -INFINITY;
   int64_t bi = -1;
   // each thread visits its elements in increasing index order, so it keeps
@@ -1849,7 +1977,7 @@ extern "C" int loki_prune_best(const float* scores, int64_t n, const double* lea
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   note_launch();
   prune_best_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, n, leaves, row_len, leaf_out,
-                                                         score_out);
+                                                         score_out, nullptr);
   return check_launch("prune_best");
 }
 
@@ -1885,7 +2013,7 @@ static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
     // child counts go to offsets[0..n), scanned in place
     note_launch();
     prune_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
-        *lvl, leaves, n_parents, info, offsets, dev_err, mask);
+        *lvl, leaves, n_parents, info, offsets, dev_err, mask, nullptr);
     rc = check_launch("prune_branch");
     if (rc) return rc;
   }
@@ -1927,7 +2055,7 @@ extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
     note_launch();
     prune_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
         *lvl, leaves, folds, n_parents, info, offsets, n_children, fold_segment, sp, SK,
-        child_scores, child_idx, child_phase, keys);
+        child_scores, child_idx, child_phase, keys, nullptr);
   }
   note_launch();
   minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
@@ -1955,7 +2083,7 @@ extern "C" int loki_prune_select(const float* child_scores, int64_t n_children,
   if (n_children > 0) note_launch();
   if (n_children > 0)
     select_scatter_kernel<<<(unsigned)((n_children + 255) / 256), 256, 0, s>>>(
-        child_scores, n_children, threshold, pos, surv_ids);
+        child_scores, n_children, threshold, pos, surv_ids, nullptr);
   if (cudaMemcpyAsync(n_surv, pos + n_children, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) !=
       cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaMemcpyAsync failed");
@@ -1976,7 +2104,7 @@ extern "C" int loki_prune_select_overflow(const float* child_scores, const int64
   note_launch();
   select_overflow_kernel<<<1, kSelThreads, 0, (cudaStream_t)stream>>>(
       child_scores, offsets, n_parents, batch_size, threshold, capacity, surv_ids, n_surv,
-      thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys));
+      thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys), nullptr, nullptr);
   (void)scratch_len;
   return check_launch("prune_select_overflow");
 }
@@ -2001,7 +2129,7 @@ extern "C" int loki_prune_emit(const LokiPruneLevel* lvl, const double* leaves,
   prune_emit_kernel<<<(unsigned)blocks, kPruneWarps * 32, 0, (cudaStream_t)stream>>>(
       *lvl, leaves, folds, info, offsets, n_parents, fold_segment, surv_ids, n_surv,
       child_scores, child_idx, child_phase, leaves_out, folds_out, scores_out, scores_ep_out,
-      bt_out);
+      bt_out, nullptr);
   return check_launch("prune_emit");
 }
 
@@ -2359,4 +2487,182 @@ extern "C" int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double
       *lvl, leaves, reinterpret_cast<float2*>(folds), scores, scores_ep, n, nseg, tm_seg, dt_seg,
       seg_idx, reinterpret_cast<const float2*>(ffa_fold), seg_stride, sp, SK);
   return check_launch("prune_ascend_complex");
+}
+
+// ---------------------------------------------------------------------------
+// device-resident run: every level of one reference segment with the counts
+// kept on the device (counts[0] parents, [1] children, [2] survivors)
+// ---------------------------------------------------------------------------
+
+namespace loki {
+
+__global__ void run_seed_kernel(int64_t* cnt, int64_t n) {
+  cnt[0] = n;
+  cnt[1] = 0;
+  cnt[2] = 0;
+  cnt[3] = 0;
+}
+
+// children of the level = offsets[parents]; above the workspace the level
+// gets none and the run is flagged
+__global__ void run_children_kernel(int64_t* cnt, const int64_t* offsets, int64_t child_cap,
+                                    LokiPruneLevelStats* st, int32_t* err) {
+  const int64_t n_par = cnt[0];
+  const int64_t n_child = offsets[n_par];
+  st->n_parents = n_par;
+  st->n_children = n_child;
+  if (n_child > child_cap) {
+    atomicOr(err, LOKI_DEVERR_CAPACITY);
+    cnt[1] = 0;
+  } else {
+    cnt[1] = n_child;
+  }
+}
+
+__global__ void run_survivors_kernel(int64_t* cnt, const int64_t* pos) { cnt[2] = pos[cnt[1]]; }
+
+// level record; the survivors are the next level's parents
+__global__ void run_level_end_kernel(int64_t* cnt, const float* minmax, int32_t* ovf_flag,
+                                     LokiPruneLevelStats* st) {
+  st->n_surv = cnt[2];
+  st->score_min = minmax[0];
+  st->score_max = minmax[1];
+  st->overflow = *ovf_flag;
+  st->reserved = 0;
+  *ovf_flag = 0;
+  cnt[3] += cnt[2];  // backtrack history rows
+  cnt[0] = cnt[2];
+}
+
+// survivors' backtracks appended to the history at row counts[3]
+__global__ void run_bt_copy_kernel(const int32_t* __restrict__ bt, const int64_t* cnt, int row,
+                                   int32_t* __restrict__ hist, int64_t hist_rows,
+                                   int32_t* err) {
+  const int64_t start = cnt[3], rows = cnt[2];
+  if (start + rows > hist_rows) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, LOKI_DEVERR_CAPACITY);
+    return;
+  }
+  int32_t* out = hist + start * row;
+  const int64_t n = rows * row;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = bt[i];
+}
+
+}  // namespace loki
+
+extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const float* ffa_folds,
+                              int64_t seg_stride, const int32_t* seg_idx,
+                              const double* thresholds, const LokiScoreSpec* spec,
+                              int64_t seed_n, int64_t max_sugg, int64_t batch_size,
+                              const LokiPruneRun* run, int32_t* dev_err, void* stream) {
+  if (!lvls || nlevels < 1 || !ffa_folds || !seg_idx || !thresholds || !spec || !run ||
+      !dev_err)
+    return set_error(LOKI_ERR_INVALID, "null pointer or no level");
+  if (max_sugg < 1 || batch_size < 1 || seed_n < 0 || seed_n > max_sugg || seg_stride < 1)
+    return set_error(LOKI_ERR_INVALID, "bad sizes");
+  const LokiPruneWork& w = run->work;
+  const LokiPruneTree* tr = run->trees;
+  if (tr[0].cap < max_sugg || tr[1].cap < max_sugg || w.par_cap < max_sugg || w.child_cap < 1 ||
+      w.ovf_cap < max_sugg + w.child_cap + 1)
+    return set_error(LOKI_ERR_CAPACITY, "run workspace below max_sugg / child_cap");
+  if (!run->counts || !run->ovf_flag || !run->stats || !w.info || !w.offsets || !w.scan ||
+      !w.child_scores || !w.child_idx || !w.child_phase || !w.surv || !w.sscan || !w.minmax ||
+      !w.ovf_ids || !w.ovf_keys || !w.ovf_thr)
+    return set_error(LOKI_ERR_INVALID, "null workspace pointer");
+  for (int l = 0; l < nlevels; ++l) {
+    int rc = check_prune(&lvls[l]);
+    if (rc) return rc;
+    if (lvls[l].basis != lvls[0].basis || lvls[l].poly_order != lvls[0].poly_order ||
+        lvls[l].nbins != lvls[0].nbins)
+      return set_error(LOKI_ERR_INVALID, "levels of different trees");
+  }
+  if (lvls[0].basis == 2)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree has its own level calls");
+  int rc = prune_spec_check(spec, lvls[0].nbins);
+  if (rc) return rc;
+  const int64_t sums_bytes = loki_scan_scratch_bytes(w.child_cap);
+  if (w.scan_bytes < loki_scan_scratch_bytes(w.par_cap + 1) ||
+      w.sscan_bytes < sums_bytes + (w.child_cap + 1) * (int64_t)sizeof(int64_t))
+    return set_error(LOKI_ERR_CAPACITY, "scan scratch below par_cap / child_cap");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = lvls[0].nbins, P = lvls[0].poly_order;
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, nb);
+  const int smem = score_smem_bytes(nb, sp.wmax, kPruneWarps);
+  if (smem > 200 * 1024)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
+  if (smem > 48 * 1024 && set_smem_limit(prune_score_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  int dev = 0, nsm = 0, occ_s = 0, occ_e = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, prune_score_kernel,
+                                                    kPruneWarps * 32, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, prune_emit_kernel,
+                                                    kPruneWarps * 32, 0) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "occupancy query failed");
+  // grids: one full wave of the score / emit kernels, and enough blocks for
+  // the parent-sized and child-sized passes to stride through
+  const unsigned g_score = (unsigned)std::max(1, nsm * std::max(1, occ_s));
+  const unsigned g_emit = (unsigned)std::max(1, nsm * std::max(1, occ_e));
+  const unsigned g_par = (unsigned)std::min<int64_t>((w.par_cap + 255) / 256, 8 * nsm);
+  const unsigned g_flat = (unsigned)(4 * nsm);
+  const int scan_grid = 2 * nsm;
+  int64_t* cnt = run->counts;
+  int64_t* pos = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(w.sscan) + sums_bytes);
+  unsigned* keys = reinterpret_cast<unsigned*>(w.minmax);
+  const int row_bt = P + 2, row_leaf = (P + 2) * 2;
+  note_launch();
+  run_seed_kernel<<<1, 1, 0, s>>>(cnt, seed_n);
+  for (int l = 1; l <= nlevels; ++l) {
+    const LokiPruneLevel& D = lvls[l - 1];
+    const LokiPruneTree& in = tr[(l - 1) & 1];
+    const LokiPruneTree& out = tr[l & 1];
+    const float* seg = ffa_folds + (int64_t)seg_idx[l - 1] * seg_stride;
+    const double thr = thresholds[l - 1];
+    LokiPruneLevelStats* st = run->stats + (l - 1);
+    LokiBranchInfo* info = reinterpret_cast<LokiBranchInfo*>(w.info);
+    for (int i = 0; i < 6; ++i) note_launch();
+    prune_branch_kernel<<<g_par, 256, 0, s>>>(D, in.leaves, w.par_cap, info, w.offsets, dev_err,
+                                              nullptr, cnt);
+    rc = exclusive_scan_dev<false>(w.offsets, w.par_cap, cnt, 0.0, w.offsets, w.scan,
+                                   w.scan_bytes, scan_grid, s);
+    if (rc) return rc;
+    run_children_kernel<<<1, 1, 0, s>>>(cnt, w.offsets, w.child_cap, st, dev_err);
+    minmax_init_kernel<<<1, 1, 0, s>>>(keys);
+    prune_score_kernel<<<g_score, kPruneWarps * 32, smem, s>>>(
+        D, in.leaves, in.folds, 0, info, w.offsets, 0, seg, sp, SK, w.child_scores, w.child_idx,
+        w.child_phase, keys, cnt);
+    minmax_finish_kernel<<<1, 1, 0, s>>>(keys, w.minmax);
+    rc = exclusive_scan_dev<true>(w.child_scores, w.child_cap, cnt + 1, thr, pos, w.sscan,
+                                  sums_bytes, scan_grid, s);
+    if (rc) return rc;
+    for (int i = 0; i < 6; ++i) note_launch();
+    select_scatter_kernel<<<g_flat, 256, 0, s>>>(w.child_scores, 0, thr, pos, w.surv, cnt + 1);
+    run_survivors_kernel<<<1, 1, 0, s>>>(cnt, pos);
+    select_overflow_kernel<<<1, kSelThreads, 0, s>>>(
+        w.child_scores, w.offsets, 0, batch_size, thr, max_sugg, w.surv, cnt + 2, w.ovf_thr,
+        w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys), cnt, run->ovf_flag);
+    prune_emit_kernel<<<g_emit, kPruneWarps * 32, 0, s>>>(
+        D, in.leaves, in.folds, info, w.offsets, 0, seg, w.surv, 0, w.child_scores, w.child_idx,
+        w.child_phase, out.leaves, out.folds, out.scores, out.scores_ep, out.backtracks, cnt);
+    if (run->best_leaves && run->best_scores) {
+      note_launch();
+      prune_best_kernel<<<1, 1024, 0, s>>>(out.scores, 0, out.leaves, row_leaf,
+                                           run->best_leaves + (int64_t)(l - 1) * row_leaf,
+                                           run->best_scores + (l - 1), cnt + 2);
+    }
+    if (run->bt_hist) {
+      note_launch();
+      run_bt_copy_kernel<<<g_flat, 256, 0, s>>>(out.backtracks, cnt, row_bt, run->bt_hist,
+                                                run->bt_rows, dev_err);
+    }
+    run_level_end_kernel<<<1, 1, 0, s>>>(cnt, w.minmax, run->ovf_flag, st);
+    rc = check_launch("prune_run");
+    if (rc) return rc;
+  }
+  return LOKI_OK;
 }

@@ -177,8 +177,10 @@ __device__ __forceinline__ int64_t trial_index(const OtherRes& o, double f, floa
   const float fr = (s - fs) + r;
   const float fl = floorf(fr);
   const float frac = fr - fl;
-  if (frac > 1e-4f && frac < 1.0f - 1e-4f && fabsf(p) < 1.0e9f) {
-    int64_t idx = (int64_t)fs + (int64_t)fl;
+  if (frac > 1e-4f && frac < 1.0f - 1e-4f && fabsf(p) < 1.0e9f && fabsf(s) < 2.0e9f) {
+    // fs and fl (in {-1, 0, 1, 2}) fit 32-bit integers, whose conversions
+    // avoid the slow 64-bit conversion path
+    int64_t idx = (int64_t)((int)fs + (int)fl);
     if (idx < 0) idx = 0;
     else if (idx >= n_grid) idx = n_grid - 1;
     return idx;

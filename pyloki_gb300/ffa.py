@@ -520,6 +520,7 @@ class DynamicProgramming:
                          else "level")
         if final == "banded" and n < 2:
             final = "level"
+        self.final_path = final
         tiled = final == "tiled"
         banded = final == "banded"
         last_mat = n - 2 if (banded or tiled) else n - 1

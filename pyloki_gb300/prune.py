@@ -260,6 +260,9 @@ class Pruning:
         self.parent_hook = None
         #: parents the hook left out, summed over the run
         self.parents_skipped = 0
+        #: first child capacity of ``run_device`` (None: max(2^20, 8 max_sugg));
+        #: a run that needs more grows it and runs again
+        self.device_child_cap: int | None = None
 
     # ---- reference properties -----------------------------------------------
     @property
@@ -963,6 +966,54 @@ class Pruning:
         self.launches += 1
         return int(n_surv_d.item())
 
+    # ---- device-resident runs (loki_prune_run) ---------------------------------
+    @property
+    def device_run_supported(self) -> bool:
+        """``run_device`` covers this configuration: Taylor or Chebyshev basis
+        on time-domain folds, one best leaf per level, no parent hook."""
+        return (not self.circular and not self.fourier and self.intermediate_k == 1
+                and self.parent_hook is None)
+
+    def run_device(self, ref_seg: int, *, graph: bool = False, levels: int | None = None) -> None:
+        """Every level of one reference segment with the counts kept on the
+        device (``loki_prune_run``): the run is enqueued without a host wait
+        and read back once at the end (level statistics, survivors, per-level
+        best leaves and backtracks), leaving the object as ``initialize`` +
+        ``execute_iter`` over all levels (or the first ``levels``) would, before
+        the ascend. With
+        ``graph=True`` the first run from ``ref_seg`` is captured in a CUDA
+        graph that later runs from it replay. The results are those of the
+        level-by-level path, kernel for kernel.
+        """
+        self._device_finish(self._device_enqueue(ref_seg, graph, levels), graph)
+
+    def _device_enqueue(self, ref_seg: int, graph: bool, levels: int | None = None):
+        """Enqueue a device-resident run on the current stream (no wait)."""
+        if not self.device_run_supported:
+            msg = "run_device covers Taylor / Chebyshev time-domain trees without a parent hook"
+            raise ValueError(msg)
+        self._stream_ptr = None  # the current stream
+        nlev = self.dyp.nsegments - 1 if levels is None else int(levels)
+        if not 0 <= nlev <= self.dyp.nsegments - 1:
+            msg = f"levels must be in [0, {self.dyp.nsegments - 1}], got {levels}"
+            raise ValueError(msg)
+        key = (ref_seg, nlev)
+        dr = self.__dict__.setdefault("_device_runs", {}).get(key)
+        if dr is None:
+            dr = _DeviceRun(self, ref_seg, nlev)
+            self.__dict__.setdefault("_device_runs", {})[key] = dr
+        dr.launch(graph)
+        return dr
+
+    def _device_finish(self, dr, graph: bool) -> None:
+        """Read an enqueued run back; repeat it with grown workspaces if it
+        outgrew them."""
+        while not dr.finish(self):
+            key = (dr.ref_seg, dr.nlev)
+            dr = _DeviceRun(self, dr.ref_seg, dr.nlev, grow=dr)
+            self.__dict__.setdefault("_device_runs", {})[key] = dr
+            dr.launch(graph)
+
     # ---- ascend (prune.py:671-693, dyn_poly_taylor.py:587-628) -----------------
     def _do_ascend(self) -> None:
         if self.prune_complete or self.world_tree.valid_size == 0:
@@ -1022,13 +1073,21 @@ class Pruning:
     def execute(self, ref_seg: int, ascend_levels: list[int] | None = None,
                 outdir: str | Path = "./", log_file: Path | None = None,
                 result_file: Path | None = None, task_id: int = 0) -> dict:
-        """Full run for one reference segment; returns the run's results."""
+        """Full run for one reference segment; returns the run's results.
+        Without intermediate ascends the levels run device-resident
+        (``run_device``) where the configuration allows, else level by level."""
         asc = frozenset(ascend_levels) if ascend_levels is not None else None
-        self.initialize(ref_seg, log_file)
-        for _ in range(self.dyp.nsegments - 1):
-            self.execute_iter(log_file)
-            if asc is not None and self.prune_level in asc:
-                self._do_ascend()
+        if asc is None and self.device_run_supported:
+            self.run_device(ref_seg)
+            if log_file is not None:
+                with Path(log_file).open("a") as f:
+                    f.writelines(st.get_summary() for st in self.pstats)
+        else:
+            self.initialize(ref_seg, log_file)
+            for _ in range(self.dyp.nsegments - 1):
+                self.execute_iter(log_file)
+                if asc is not None and self.prune_level in asc:
+                    self._do_ascend()
         if asc is None or self.prune_level not in asc:
             self._do_ascend()
         return {
@@ -1071,6 +1130,205 @@ class Pruning:
             idx = int(bt[0])
             lvl -= 1
         return steps[::-1]
+
+
+class _DeviceBuffers:
+    """Trees and workspace of device-resident runs on one Pruning object."""
+
+    def __init__(self, prn: Pruning, child_cap: int, bt_rows: int) -> None:
+        dev = prn._device
+        P, nb, cap = prn.poly_order, prn.dyp.cfg.nbins, prn.max_sugg
+        nlev = max(prn.dyp.nsegments - 1, 1)
+        lib = prn._lib
+        t64, t32, f32, f64, u8 = torch.int64, torch.int32, torch.float32, torch.float64, torch.uint8
+        self.child_cap, self.bt_rows = child_cap, bt_rows
+        self.trees = [{"leaves": torch.empty((cap, P + 2, 2), dtype=f64, device=dev),
+                       "folds": torch.empty((cap, 2, nb), dtype=f32, device=dev),
+                       "scores": torch.empty(cap, dtype=f32, device=dev),
+                       "scores_ep": torch.empty(cap, dtype=f32, device=dev),
+                       "bt": torch.empty((cap, P + 2), dtype=t32, device=dev)} for _ in range(2)]
+        scan_bytes = int(lib.loki_scan_scratch_bytes(cap + 1))
+        sscan_bytes = int(lib.loki_scan_scratch_bytes(child_cap)) + 8 * (child_cap + 1)
+        ovf_cap = cap + child_cap + 1
+        self.mem = {
+            "info": torch.empty(cap * _lib.BRANCH_INFO_BYTES, dtype=u8, device=dev),
+            "offsets": torch.empty(cap + 1, dtype=t64, device=dev),
+            "scan": torch.empty(scan_bytes, dtype=u8, device=dev),
+            "cscores": torch.empty(child_cap, dtype=f32, device=dev),
+            "cidx": torch.empty(2 * child_cap, dtype=t32, device=dev),
+            "cphase": torch.empty(child_cap, dtype=f64, device=dev),
+            "surv": torch.empty(child_cap, dtype=t64, device=dev),
+            "sscan": torch.empty(sscan_bytes, dtype=u8, device=dev),
+            "minmax": torch.empty(2, dtype=f32, device=dev),
+            "ovf_ids": torch.empty(ovf_cap, dtype=t64, device=dev),
+            "ovf_keys": torch.empty(ovf_cap, dtype=f32, device=dev),
+            "ovf_thr": torch.empty(1, dtype=f64, device=dev),
+            "counts": torch.zeros(4, dtype=t64, device=dev),
+            "ovf_flag": torch.zeros(1, dtype=t32, device=dev),
+            "stats": torch.zeros(nlev * _lib.PRUNE_STATS_DTYPE.itemsize, dtype=u8, device=dev),
+            "best_leaves": torch.zeros((nlev, P + 2, 2), dtype=f64, device=dev),
+            "best_scores": torch.zeros(nlev, dtype=f32, device=dev),
+            "bt_hist": torch.empty((bt_rows, P + 2), dtype=t32, device=dev),
+        }
+        m = self.mem
+        r = _lib.LokiPruneRun()
+        for k, t in enumerate(self.trees):
+            r.trees[k] = _lib.LokiPruneTree(t["leaves"].data_ptr(), t["folds"].data_ptr(),
+                                            t["scores"].data_ptr(), t["scores_ep"].data_ptr(),
+                                            t["bt"].data_ptr(), 0, cap)
+        w = r.work
+        w.info, w.offsets, w.scan = (m["info"].data_ptr(), m["offsets"].data_ptr(),
+                                     m["scan"].data_ptr())
+        w.scan_bytes, w.par_cap = scan_bytes, cap
+        w.child_scores, w.child_idx = m["cscores"].data_ptr(), m["cidx"].data_ptr()
+        w.child_phase, w.surv = m["cphase"].data_ptr(), m["surv"].data_ptr()
+        w.sscan, w.sscan_bytes, w.child_cap = m["sscan"].data_ptr(), sscan_bytes, child_cap
+        w.n_surv, w.minmax = None, m["minmax"].data_ptr()
+        w.ovf_ids, w.ovf_keys = m["ovf_ids"].data_ptr(), m["ovf_keys"].data_ptr()
+        w.ovf_thr, w.ovf_cap = m["ovf_thr"].data_ptr(), ovf_cap
+        r.counts, r.ovf_flag, r.stats = (m["counts"].data_ptr(), m["ovf_flag"].data_ptr(),
+                                         m["stats"].data_ptr())
+        r.best_leaves, r.best_scores = m["best_leaves"].data_ptr(), m["best_scores"].data_ptr()
+        r.bt_hist, r.bt_rows = m["bt_hist"].data_ptr(), bt_rows
+        self.run = r
+
+
+class _DeviceRun:
+    """One reference segment's device-resident run: level descriptors,
+    segment order, thresholds, the seed (copied into the first tree at the
+    start of every run) and, once captured, the run's CUDA graph."""
+
+    def __init__(self, prn: Pruning, ref_seg: int, nlev: int,
+                 grow: _DeviceRun | None = None) -> None:
+        dyp = prn.dyp
+        nseg = dyp.nsegments
+        self.nlev = nlev
+        self.ref_seg = ref_seg
+        self.scheme = MiddleOutScheme(nseg, ref_seg, dyp.tseg, 1)
+        prn._scheme = self.scheme
+        self.seed = prn._seed(prn._fold_segment(ref_seg))
+        if self.seed.size > prn.max_sugg:
+            msg = "the seed tree is larger than max_sugg"
+            raise ValueError(msg)
+        cap = prn.max_sugg
+        bufs = prn.__dict__.get("_device_bufs")
+        child_cap = prn.device_child_cap or max(1 << 20, 8 * cap)
+        bt_rows = max(1, min(self.nlev * cap, max(1 << 22, 16 * cap)))
+        if grow is not None:
+            child_cap = max(child_cap, grow.need_child, bufs.child_cap if bufs else 0)
+            bt_rows = max(bt_rows, grow.need_bt, bufs.bt_rows if bufs else 0)
+        if bufs is None or bufs.child_cap < child_cap or bufs.bt_rows < bt_rows:
+            prn.__dict__.pop("_device_runs", None)  # their graphs hold the old buffers
+            bufs = prn._device_bufs = _DeviceBuffers(prn, child_cap, bt_rows)
+        self.bufs = bufs
+        self.descs = (_lib.LokiPruneLevel * max(self.nlev, 1))()
+        for lvl in range(1, self.nlev + 1):
+            C.memmove(C.byref(self.descs, (lvl - 1) * C.sizeof(_lib.LokiPruneLevel)),
+                      C.byref(prn.level_desc(lvl)), C.sizeof(_lib.LokiPruneLevel))
+        self.seg_idx = np.ascontiguousarray(
+            [self.scheme.get_segment_idx(lvl) for lvl in range(1, self.nlev + 1)], np.int32)
+        self.thresholds = np.ascontiguousarray(prn.threshold_scheme[: self.nlev], np.float64)
+        self.prn = prn
+        self.graph = None
+        self.need_child = self.need_bt = 0
+
+    def _enqueue(self) -> None:
+        prn, b = self.prn, self.bufs
+        t0, seed = b.trees[0], self.seed
+        n = seed.size
+        t0["leaves"][:n].copy_(seed.leaves)
+        t0["folds"][:n].copy_(seed.folds)
+        t0["scores"][:n].copy_(seed.scores)
+        t0["scores_ep"][:n].copy_(seed.scores_ep)
+        t0["bt"][:n].copy_(seed.backtracks)
+        prn._err.zero_()
+        if self.nlev == 0:
+            return
+        fold = prn.dyp.fold
+        stride = int(np.prod(fold.shape[1:]))
+        _lib.check(prn._lib.loki_prune_run(
+            self.descs, self.nlev, _lib.ptr(fold), stride, self.seg_idx.ctypes.data,
+            self.thresholds.ctypes.data, prn.spec, n, prn.max_sugg, prn.batch_size,
+            C.byref(b.run), _lib.ptr(prn._err), prn._stream()))
+
+    def launch(self, graph: bool) -> None:
+        if not graph:
+            self._enqueue()
+            return
+        if self.graph is None:
+            self._enqueue()  # uncaptured first run: kernel attributes, lazy loading
+            cur = torch.cuda.current_stream(self.prn._device)
+            side = torch.cuda.Stream(self.prn._device)
+            side.wait_stream(cur)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side):
+                self.prn._stream_ptr = _lib.stream_ptr(side)
+                with torch.cuda.graph(g, stream=side):
+                    self._enqueue()
+            cur.wait_stream(side)
+            self.prn._stream_ptr = _lib.stream_ptr(cur)
+            self.graph = g
+        self.graph.replay()
+
+    def finish(self, prn: Pruning) -> bool:
+        """Read the run back (one wait) and set ``prn``'s state; False when a
+        workspace has to grow (``need_*`` set) and the run must be repeated."""
+        b = self.bufs
+        stats = b.mem["stats"].cpu().numpy().view(_lib.PRUNE_STATS_DTYPE)
+        err = int(prn._err.item())
+        if err & _lib.LOKI_DEVERR_CAPACITY:
+            self.need_child = int(stats["n_children"].max() * 1.25) + 1
+            self.need_bt = int(stats["n_surv"].sum() * 1.25) + 1
+            prn._err.zero_()
+            return False
+        if err:
+            _lib.check_dev_err(prn._err)
+        sc = self.scheme
+        prn._scheme = sc
+        seed = self.seed
+        st0 = PruneStats(level=0, seg_idx=sc.get_segment_idx(0), threshold=0,
+                         score_min=seed.score_min, score_max=seed.score_max,
+                         n_branches=seed.size, n_leaves=seed.size, n_leaves_phy=seed.size,
+                         n_leaves_surv=seed.size)
+        pstats = [st0]
+        bt_hist = []
+        off = 0
+        bt = b.mem["bt_hist"]
+        last = 0
+        for lvl in range(1, self.nlev + 1):
+            r = stats[lvl - 1]
+            n_child, n_surv = int(r["n_children"]), int(r["n_surv"])
+            pstats.append(PruneStats(
+                level=lvl, seg_idx=int(self.seg_idx[lvl - 1]),
+                threshold=float(self.thresholds[lvl - 1]),
+                score_min=float(r["score_min"]) if n_child else 0.0,
+                score_max=float(r["score_max"]) if n_child else 0.0,
+                n_branches=int(r["n_parents"]), n_leaves=n_child, n_leaves_phy=n_child,
+                n_leaves_surv=n_surv))
+            last = lvl
+            if n_surv == 0:
+                break
+            bt_hist.append(bt[off:off + n_surv])
+            off += n_surv
+        n_final = int(stats[last - 1]["n_surv"]) if last else seed.size
+        t = b.trees[last & 1]
+        prn._pstats = pstats
+        prn._prune_level = last
+        prn._prune_complete = n_final == 0
+        prn._world_tree = WorldTree(t["leaves"][:n_final], t["folds"][:n_final],
+                                    t["scores"][:n_final], t["bt"][:n_final],
+                                    t["scores_ep"][:n_final])
+        prn._backtrack_hist = bt_hist
+        nkeep = len(bt_hist)
+        prn._best_leaves = b.mem["best_leaves"]
+        prn._best_scores = b.mem["best_scores"]
+        prn._pending_best = [(lvl - 1, None, None) for lvl in range(1, nkeep + 1)]
+        prn._best_intermediate_arr = np.zeros(
+            (prn.dyp.nsegments - 1, prn.intermediate_k),
+            dtype=np.dtype([("param_sets", np.float64, (prn.poly_order + 2, 2)),
+                            ("scores", np.float32)]))
+        prn.launches += 1 + 13 * self.nlev
+        return True
 
 
 def poly_taylor_report_batch(leaves: np.ndarray) -> np.ndarray:
@@ -1148,6 +1406,59 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
             dtype=np.float64)
     np.savez_compressed(result_file, **out)
     return result_file.as_posix()
+
+
+def run_batch(jobs, threshold_scheme, *, n_streams: int = 8, graph: bool = True,
+              ascend: bool = True, **kwargs) -> list[dict]:
+    """Device-resident runs of many (fold, reference segment) jobs at once from
+    one host thread. ``jobs`` is a list of ``(dyp, ref_seg)``. Each of
+    ``n_streams`` CUDA streams has its own run buffers; a round enqueues one
+    run per stream (a CUDA-graph replay with ``graph``) with no host wait, so
+    the streams' small per-level kernels overlap on the GPU, then reads the
+    round back (one wait per run) and, with ``ascend``, re-folds the
+    survivors over all segments. Every run is the same computation as
+    ``Pruning.execute`` on its own; the results come in job order as
+    ``execute``'s dictionaries."""
+    jobs = list(jobs)
+    if not jobs:
+        return []
+    dev = jobs[0][0].device
+    producer = torch.cuda.current_stream(dev)
+    n_streams = max(1, min(int(n_streams), len(jobs)))
+    streams = [torch.cuda.Stream(dev) for _ in range(n_streams)]
+    prns: list[dict] = [{} for _ in range(n_streams)]  # per stream: dyp id -> Pruning
+    bufs: list = [None] * n_streams
+    out: list[dict] = [{} for _ in jobs]
+    for r0 in range(0, len(jobs), n_streams):
+        round_jobs = list(enumerate(jobs[r0:r0 + n_streams]))
+        started = []
+        for k, (dyp, ref) in round_jobs:
+            st = streams[k]
+            st.wait_stream(producer)
+            with torch.cuda.stream(st):
+                prn = prns[k].get(id(dyp))
+                if prn is None:
+                    prn = prns[k][id(dyp)] = Pruning(dyp, threshold_scheme, **kwargs)
+                    if bufs[k] is not None:
+                        prn._device_bufs = bufs[k]
+                started.append((k, prn, prn._device_enqueue(ref, graph)))
+        for k, prn, dr in started:
+            with torch.cuda.stream(streams[k]):
+                prn._device_finish(dr, graph)
+                bufs[k] = prn._device_bufs
+                if ascend:
+                    prn._do_ascend()
+        for k, prn, dr in started:
+            with torch.cuda.stream(streams[k]):
+                out[r0 + k] = {
+                    "run_name": f"{dr.ref_seg:03d}_00", "scheme": prn.scheme.data.copy(),
+                    "param_sets": prn.report(),
+                    "scores": prn.world_tree.scores.cpu().numpy(),
+                    "scores_ep": prn.world_tree.scores_ep.cpu().numpy(),
+                    "level_stats": prn.pstats}
+    for st in streams:
+        producer.wait_stream(st)
+    return out
 
 
 def run_many(dyp, threshold_scheme, ref_segs, *, n_workers: int = 4,

@@ -1,0 +1,136 @@
+"""Device-resident pruning runs (loki_prune_run) against the reference and
+against the level-by-level path.
+
+``Pruning.run_device`` enqueues every level of a reference segment with the
+counts kept on the device; the level statistics, the surviving tree, the
+per-level backtracks and best leaves, and the ascend that follows must equal
+the reference's runs (the same fixtures as test_prune_gpu.py) and the
+level-by-level path, with and without CUDA-graph capture and replay.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.test_prune_gpu import _leaves_close, _run
+
+pytestmark = pytest.mark.gpu
+CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
+         "prune_taylor_overflow", "prune_cheby", "prune_cheby_fixed", "prune_cheby_cons",
+         "prune_cheby_quad"]
+
+
+def _check_against_fixture(d, prn, levels):
+    for lvl in range(1, levels + 1):
+        if lvl >= len(prn.pstats):
+            break
+        st = prn.pstats[lvl]
+        np.testing.assert_array_equal(
+            [st.n_branches, st.n_leaves, st.n_leaves_phy, st.n_leaves_surv],
+            d[f"stats_{lvl}"], err_msg=f"stats level {lvl}")
+        np.testing.assert_array_equal([st.score_min, st.score_max],
+                                      d[f"smm_{lvl}"].astype(np.float32).astype(np.float64),
+                                      err_msg=f"score min/max level {lvl}")
+    last = prn.prune_level
+    wt = prn.world_tree
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d[f"scores_{last}"])
+    if f"leaves_{last}" in d:
+        _leaves_close(wt.leaves.cpu().numpy(), d[f"leaves_{last}"], "final leaves")
+    if f"folds_{last}" in d:
+        np.testing.assert_array_equal(wt.folds.cpu().numpy(), d[f"folds_{last}"])
+    prn._do_ascend()
+    wt = prn.world_tree
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["asc_scores"])
+    np.testing.assert_array_equal(wt.scores_ep.cpu().numpy(), d["asc_scores_ep"])
+    if "asc_folds" in d:
+        np.testing.assert_array_equal(wt.folds.cpu().numpy(), d["asc_folds"])
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("name", CASES)
+def test_device_run_matches_reference(cuda_device, name, graph):
+    d, prn = _run(name, cuda_device)
+    levels = int(d["levels_done"])
+    ref = int(d["ref_seg"])
+    for _ in range(2):  # the second run replays the captured graph
+        prn.run_device(ref, graph=graph, levels=levels)
+        np.testing.assert_array_equal(prn.scheme.data, d["scheme"])
+        _check_against_fixture(d, prn, levels)
+
+
+@pytest.mark.parametrize("name", ["prune_taylor", "prune_taylor_overflow", "prune_cheby"])
+def test_device_run_matches_level_path(cuda_device, name):
+    """Backtrack history, per-level best leaves and statistics equal the
+    level-by-level path's."""
+    d, prn = _run(name, cuda_device)
+    levels = int(d["levels_done"])
+    ref = int(d["ref_seg"])
+    prn.initialize(ref)
+    for _ in range(levels):
+        prn.execute_iter()
+    want_stats = [(s.n_branches, s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+                  for s in prn.pstats]
+    want_bt = [b.cpu().numpy() for b in prn.backtrack_hist]
+    want_best = prn.best_intermediate_arr.copy()
+    want_tree = prn.world_tree.leaves.cpu().numpy()
+    prn.run_device(ref, graph=True, levels=levels)
+    got_stats = [(s.n_branches, s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+                 for s in prn.pstats]
+    assert got_stats == want_stats
+    got_bt = [b.cpu().numpy() for b in prn.backtrack_hist]
+    assert len(got_bt) == len(want_bt)
+    for lvl, (a, b) in enumerate(zip(got_bt, want_bt, strict=True)):
+        np.testing.assert_array_equal(a, b, err_msg=f"backtracks level {lvl + 1}")
+    got_best = prn.best_intermediate_arr
+    np.testing.assert_array_equal(got_best["scores"], want_best["scores"])
+    np.testing.assert_array_equal(got_best["param_sets"], want_best["param_sets"])
+    np.testing.assert_array_equal(prn.world_tree.leaves.cpu().numpy(), want_tree)
+
+
+def test_device_run_grows_its_workspace(cuda_device):
+    """A child workspace that is too small is detected on the device, grown
+    and the run repeated: the results do not change."""
+    d, prn = _run("prune_taylor", cuda_device)
+    levels = int(d["levels_done"])
+    ref = int(d["ref_seg"])
+    prn.device_child_cap = 64
+    prn.run_device(ref, levels=levels)
+    assert max(s.n_leaves for s in prn.pstats[1:]) > 64
+    assert prn._device_bufs.child_cap > 64
+    _check_against_fixture(d, prn, levels)
+
+
+def test_device_run_rejects_unsupported(cuda_device):
+    d, prn = _run("prune_circ", cuda_device)
+    assert not prn.device_run_supported
+    with pytest.raises(ValueError):
+        prn.run_device(int(d["ref_seg"]))
+
+
+@pytest.mark.parametrize("n_streams", [1, 3])
+def test_run_batch_matches_level_path(cuda_device, n_streams):
+    """Batched device-resident runs of several reference segments (one graph
+    per run, runs on concurrent streams) equal level-by-level runs."""
+    from pyloki_gb300.prune import Pruning, run_batch
+
+    d, prn = _run("prune_taylor", cuda_device)
+    dyp = prn.dyp
+    refs = [0, 3, 7, dyp.nsegments - 1, 5]
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
+    got = run_batch([(dyp, r) for r in refs], d["thresholds"], n_streams=n_streams, **kw)
+    again = run_batch([(dyp, r) for r in refs], d["thresholds"], n_streams=n_streams, **kw)
+    for ref, g, a in zip(refs, got, again, strict=True):
+        p = Pruning(dyp, d["thresholds"], **kw)
+        p.initialize(ref)
+        for _ in range(dyp.nsegments - 1):
+            p.execute_iter()
+        p._do_ascend()
+        want_stats = [(s.n_branches, s.n_leaves, s.n_leaves_surv) for s in p.pstats]
+        for res in (g, a):
+            assert [(s.n_branches, s.n_leaves, s.n_leaves_surv)
+                    for s in res["level_stats"]] == want_stats
+            np.testing.assert_array_equal(res["scores"], p.world_tree.scores.cpu().numpy())
+            np.testing.assert_array_equal(res["scores_ep"],
+                                          p.world_tree.scores_ep.cpu().numpy())
+            np.testing.assert_array_equal(res["param_sets"], p.report())

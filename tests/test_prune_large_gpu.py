@@ -1,10 +1,11 @@
 """GPU enumerate-prune against the CPU oracle on the benchmark workload.
 
 The circular-orbit search with a Taylor tree to the 4th derivative (2^22
-samples, 128 segments, FFA grid (1, 1, 1, 146)), run for every level from the
-middle reference segment: per-level statistics, survivor scores, backtracks
-and folds bit-exact, FP64 leaves to 1e-13 relative, then the ascend. The
-oracle is pinned to the reference by test_prune_oracle_golden.py.
+samples, 128 segments, FFA grid (1, 1, 1, 146)) with its designed per-level
+thresholds (tests/golden/prune_scheme_taylor4.npz), run for every level from
+the middle reference segment: per-level statistics, survivor scores,
+backtracks and folds bit-exact, FP64 leaves to 1e-13 relative, then the
+ascend. The oracle is pinned to the reference by test_prune_oracle_golden.py.
 """
 
 from __future__ import annotations
@@ -60,7 +61,7 @@ def test_prune_taylor4_circular_matches_oracle(cuda_device):
             np.testing.assert_allclose(wt.leaves.cpu().numpy(), run.leaves, rtol=1e-13, atol=0)
         if not alive:
             break
-    assert sum(s[1] for s in run.stats) > 10**6  # the tree really branched
+    assert sum(s[1] for s in run.stats) > 10**5  # the tree really branched
     prn._do_ascend()
     run.ascend()
     np.testing.assert_array_equal(prn.world_tree.scores.cpu().numpy(), run.scores)
