@@ -43,7 +43,7 @@ WORKLOAD = "ffa_accel_search_2^23"
 # trials); profiles/ffa_final_tiled64_kernel_ffa_accel_2^21.md. The banded
 # path's figure comes from three full-band launches at 2^21
 # (profiles/band_union64_kernel_ffa_accel_2^21.md).
-FINAL_DRAM_BYTES_PER_TRIAL = {"tiled": 60.2, "banded": 259.0}
+FINAL_DRAM_BYTES_PER_TRIAL = {"tiled": 70.2, "banded": 259.0}
 FINAL_KERNEL = {"tiled": "ffa_final_tiled64_kernel (last two levels fused per tile: "
                          "penultimate rows built in shared memory, lane-per-trial scoring)",
                 "banded": "band_union64_kernel (penultimate band + fused final-level scoring)",
@@ -84,8 +84,7 @@ PRUNE_WORKERS = 4      # concurrent runs (host threads and CUDA streams)
 PRUNE_STREAMS = 16     # concurrent device-resident runs (CUDA streams, one host thread)
 PRUNE_BATCH = 1024
 PRUNE_SCHEME = ROOT / "tests" / "golden" / "prune_scheme_taylor4.npz"
-PRUNE_SCHEME_NOTE = ("designed: DynamicThresholdScheme over the tree's branching pattern, "
-                     "least-cost path keeping 90% of S/N-10 signals")
+PRUNE_SCHEME_NOTE = "designed (DynamicThresholdScheme, least-cost path at 90% of S/N 10)"
 # HBM bytes per leaf of prune_score_kernel: the parent fold (2 x 64 f32) read
 # once, the score (f32), grid indices (2 x i32) and phase (f64) written. The
 # added segment's fold (146 rows, 75 KB) stays in L2.
@@ -147,12 +146,16 @@ def prune_cpu(nthreads: int = 0) -> dict:
 
 
 def bench_prune_gpu(args, dev) -> dict:
-    """Prune leaves/s of one enumerate-prune run per step (device-resident
-    FFA fold), plus the same run end to end from a pinned host series."""
+    """Prune leaves/s of the pruning workload run from PRUNE_MULTI_RUNS
+    reference segments per step (prune_dyp_tree's n_runs), batched: every run
+    device-resident in its own CUDA graph, PRUNE_STREAMS runs at once on
+    their own streams. Beside it: one run device-resident, one run level by
+    level (the plain path), and the batched job end to end from a pinned host
+    series."""
     import torch
 
     from pyloki_gb300.ffa import DynamicProgramming
-    from pyloki_gb300.prune import Pruning
+    from pyloki_gb300.prune import PruneBatch, Pruning
     from pyloki_gb300.timeseries import TimeSeries
 
     from pyloki_gb300 import _lib
@@ -169,11 +172,13 @@ def bench_prune_gpu(args, dev) -> dict:
     nseg = dyp.nsegments
     thr = prune_thresholds(nseg)
     ref = nseg // 2
-    prn = Pruning(dyp, thr, max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
+    refs = [int(r) for r in np.linspace(4, nseg - 5, args.prune_runs).round()]
+    kw = {"max_sugg": PRUNE_MAX_SUGG, "batch_size": PRUNE_BATCH}
+    prn = Pruning(dyp, thr, **kw)
 
     def level_run(events=None) -> int:
-        """The level-by-level path: one host wait per level for the child
-        count and one for the survivor count."""
+        """The plain path: level by level, one host wait per level for the
+        child count and one for the survivor count."""
         prn.score_events = events
         prn.initialize(ref)
         for _ in range(nseg - 1):
@@ -183,142 +188,108 @@ def bench_prune_gpu(args, dev) -> dict:
         prn._do_ascend()
         return sum(st.n_leaves for st in prn.pstats[1:])
 
-    def one_run() -> int:
-        """Device-resident: every level in one CUDA graph (counts on the
-        device), then the ascend."""
+    def device_run() -> int:
+        """One run device-resident: every level in one CUDA graph."""
         prn.run_device(ref, graph=True)
         prn._do_ascend()
         return sum(st.n_leaves for st in prn.pstats[1:])
 
+    runner = PruneBatch(thr, n_streams=args.prune_streams, **kw)
+
+    def batched(d=dyp) -> int:
+        res = runner.run([(d, r) for r in refs])
+        return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+
+    def timed(fn, steps):
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        n = sum(fn() for _ in range(steps))
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return n, e0.elapsed_time(e1)
+
     for _ in range(args.warmup):
-        one_run()
         level_run()
-    # kernels per run, counted on one uncaptured run (a graph replay does not
+        device_run()
+        batched()
+    # kernels per step, counted on uncaptured runs (a graph replay does not
     # pass through the library's launch counter)
     c0 = lib.loki_launch_count()
-    prn.run_device(ref, graph=False)
-    prn._do_ascend()
-    run_launches = lib.loki_launch_count() - c0
-    torch.cuda.synchronize(dev)
-    leaves = 0
+    for r in refs:
+        prn.run_device(r, graph=False)
+        prn._do_ascend()
+    step_launches = lib.loki_launch_count() - c0
+    with ClockSampler(dev.index) as clocks:
+        leaves, ms = timed(batched, args.steps)
+    single_leaves, single_ms = timed(device_run, args.steps)
+    plain_leaves, plain_ms = timed(level_run, args.steps)
+    # the score kernel's own time for the roofline: one more level-by-level
+    # run with CUDA events around every score launch, outside the timed runs
     score_events: list = []
-    start = torch.cuda.Event(enable_timing=True)
-    end = torch.cuda.Event(enable_timing=True)
-    start.record()
-    for _ in range(args.steps):
-        leaves += one_run()
-    end.record()
-    torch.cuda.synchronize(dev)
-    launches = run_launches * args.steps
-    ms = start.elapsed_time(end)
-    lstart = torch.cuda.Event(enable_timing=True)
-    lend = torch.cuda.Event(enable_timing=True)
-    lstart.record()
-    lleaves = sum(level_run() for _ in range(args.steps))
-    lend.record()
-    torch.cuda.synchronize(dev)
-    level_ms = lstart.elapsed_time(lend)
-    # the score kernel's own time for the roofline: one more run with CUDA
-    # events around every score launch, outside the timed runs
     level_run(score_events)
     torch.cuda.synchronize(dev)
     score_ms = sum(e0.elapsed_time(e1) for _, e0, e1 in score_events)
     score_leaves = sum(n for n, _, _ in score_events)
     peak, peak_kind = measured_peak_hbm()
     achieved = score_leaves * PRUNE_SCORE_BYTES_PER_LEAF / (score_ms * 1e-3) / 1e9
-    survivors = int(prn.world_tree.valid_size)
-    best = float(prn.world_tree.scores.max().item()) if survivors else float("nan")
-    # children per parent of every level of the plain run (threshold design input)
-    bpat = [max(1, int(round(st.n_leaves / max(st.n_branches, 1)))) for st in prn.pstats[1:]]
+    value = leaves / (ms * 1e-3)
+    plain_value = plain_leaves / (plain_ms * 1e-3)
 
-    # end to end: pinned host series -> FFA -> pruning run -> results on the host
+    # end to end: pinned host series -> FFA -> the batched runs -> results on
+    # the host (every run's surviving parameters and scores)
     from pyloki_gb300.timeseries import TimeSeries as TS
 
     host_ts = TS(e_pin, v_pin, cfg.tsamp)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    d2h = 0
     e2e_leaves = 0
+    d2h = 0
     for _ in range(args.steps):
         dp = DynamicProgramming(host_ts, cfg, device=dev)
         dp.initialize()
         dp.execute()
-        pr = Pruning(dp, thr, max_sugg=PRUNE_MAX_SUGG, batch_size=PRUNE_BATCH)
-        res = pr.execute(ref)
-        e2e_leaves += sum(st.n_leaves for st in res["level_stats"][1:])
-        d2h = res["param_sets"].nbytes + res["scores"].nbytes + res["scores_ep"].nbytes
+        res = runner.run([(dp, r) for r in refs])  # graphs rebound to the new fold
+        e2e_leaves += sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+        d2h = sum(r["param_sets"].nbytes + r["scores"].nbytes + r["scores_ep"].nbytes
+                  for r in res)
     torch.cuda.synchronize(dev)
     e2e_s = time.perf_counter() - t0
-    # several reference segments at once (prune_dyp_tree's n_workers): runs on
-    # concurrent host threads and streams overlap one another's host waits
-    from pyloki_gb300.prune import run_many
-
-    refs = [int(r) for r in np.linspace(8, nseg - 8, args.prune_runs).round()]
-    multi = {}
-    for nw in (1, args.prune_workers):
-        run_many(dyp, thr, refs[:nw], n_workers=nw, max_sugg=PRUNE_MAX_SUGG,
-                 batch_size=PRUNE_BATCH)  # warm-up of the worker streams
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        res = run_many(dyp, thr, refs, n_workers=nw, max_sugg=PRUNE_MAX_SUGG,
-                       batch_size=PRUNE_BATCH)
-        torch.cuda.synchronize(dev)
-        dt = time.perf_counter() - t0
-        nl = sum(st.n_leaves for r in res.values() for st in r["level_stats"][1:])
-        multi[f"workers_{nw}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
-    # batched: the same runs device-resident, one CUDA graph per run, one
-    # stream per concurrent run, enqueued from one host thread
-    from pyloki_gb300.prune import run_batch
-
-    for ns in (1, args.prune_streams):
-        jobs = [(dyp, r) for r in refs]
-        run_batch(jobs, thr, n_streams=ns, max_sugg=PRUNE_MAX_SUGG,
-                  batch_size=PRUNE_BATCH)  # capture of every run's graph
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        res = run_batch(jobs, thr, n_streams=ns, max_sugg=PRUNE_MAX_SUGG,
-                        batch_size=PRUNE_BATCH)
-        torch.cuda.synchronize(dev)
-        dt = time.perf_counter() - t0
-        nl = sum(st.n_leaves for r in res for st in r["level_stats"][1:])
-        multi[f"batched_streams_{ns}"] = {"leaves_per_s": nl / dt, "seconds": dt, "leaves": nl}
-    multi["runs"] = len(refs)
-    multi["ref_segments"] = refs
-    multi["speedup"] = (multi[f"workers_{args.prune_workers}"]["leaves_per_s"]
-                        / multi["workers_1"]["leaves_per_s"])
-    multi["batched_speedup_vs_plain"] = (
-        multi[f"batched_streams_{args.prune_streams}"]["leaves_per_s"]
-        / (lleaves / (level_ms * 1e-3)))
     return {
-        "metric": "prune leaves/s", "value": leaves / (ms * 1e-3), "unit": "leaves/s",
-        "path": "device-resident levels, one CUDA graph per run (loki_prune_run)",
-        "level_path": {"value": lleaves / (level_ms * 1e-3),
-                       "ms_per_step": level_ms / args.steps,
-                       "note": "level by level with two host waits per level"},
-        "multi_run": multi,
+        "metric": "prune leaves/s", "value": value, "unit": "leaves/s",
+        "path": (f"batched: {len(refs)} reference segments per step, each run device-resident "
+                 f"in one CUDA graph, {args.prune_streams} runs at once on their own streams"),
         "ms_per_step": ms / args.steps, "leaves_per_step": leaves // args.steps,
+        "single_run": {"value": single_leaves / (single_ms * 1e-3),
+                       "ms_per_run": single_ms / args.steps,
+                       "leaves_per_run": single_leaves // args.steps,
+                       "note": "one run (reference segment 64) device-resident, one graph"},
+        "plain": {"value": plain_value, "ms_per_run": plain_ms / args.steps,
+                  "leaves_per_run": plain_leaves // args.steps,
+                  "note": "one run level by level with two host waits per level"},
+        "speedup_vs_plain": value / plain_value,
         "dtype": "f32 folds, f64 parameters",
         "data": "synthetic (seeded N(0,1) noise + 3 ms pulsar in a circular orbit, S/N 10)",
         "config": {"workload": PRUNE_WORKLOAD, "nsamps": cfg.nsamps, "tsamp": cfg.tsamp,
                    "nbins": cfg.nbins, "poly_order": 4, "segments": nseg,
                    "ffa_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
                    "widths": cfg.score_widths.tolist(), "max_sugg": PRUNE_MAX_SUGG,
-                   "batch_size": PRUNE_BATCH, "ref_segment": ref,
-                   "thresholds": PRUNE_SCHEME_NOTE,
+                   "batch_size": PRUNE_BATCH, "ref_segments": len(refs),
+                   "streams": args.prune_streams, "thresholds": PRUNE_SCHEME_NOTE,
                    "orbit": {"p_orb_h": orbit[0] / 3600, "x_lts": orbit[1], "psi": orbit[2]},
                    "l2": "segment folds (75 KB) are L2-resident; tree folds stream"},
         "roofline": {"kernel": "prune_score_kernel (resolve + gather + shift-add + score)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "bytes_per_leaf": PRUNE_SCORE_BYTES_PER_LEAF,
-                     "kernel_ms_per_step": score_ms,
-                     "launches_per_step": len(score_events), "traffic": None},
+                     "kernel_ms_per_run": score_ms,
+                     "launches_per_run": len(score_events), "traffic": None},
         "e2e": {"value": e2e_leaves / e2e_s, "unit": "leaves/s",
                 "ms_per_step": e2e_s * 1e3 / args.steps, "h2d_bytes_per_step": 8 * cfg.nsamps,
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": launches,
-        "survivors": survivors, "best_score": best,
-        "branching_pattern": bpat,
+        "gpu_launches": step_launches * args.steps,
+        "clocks": clocks.summary(),
+        "survivors": int(prn.world_tree.valid_size),
     }
 
 
@@ -540,6 +511,8 @@ def bench_gpu(args) -> dict | None:
     peak, peak_kind = measured_peak_hbm()
     achieved = ab / (dom_ms * 1e-3) / 1e9
     dom_launches = max(1, phase_launches[dom] // args.steps)
+    if dom == "final" and final_path["path"] == "tiled":
+        dom_launches = 1  # the phase's other launches are its small table kernels
     traffic = None
     fpath = final_path["path"]
     if dom == "final" and fpath in FINAL_DRAM_BYTES_PER_TRIAL:
@@ -564,7 +537,7 @@ def bench_gpu(args) -> dict | None:
                    "final_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
                    "trials_per_step": trials, "band_bytes": args.band_bytes,
                    "final_path": fpath,
-                   "norm": ("fast: e * rsqrt(v), S/N within 1e-5 of the bit-exact search"
+                   "norm": ("rsqrt: S/N within 1e-5 of the bit-exact search"
                             if args.norm == "fast" else "exact: bit-identical S/N"),
                    "l2": "inputs larger than L2 (>51 GB read per step)",
                    "parallelism": f"replicas x{world}"},
@@ -610,6 +583,8 @@ def bench_gpu(args) -> dict | None:
         out["injection"] = bench_injections(args, dev, peak)
     if not args.no_fourier:
         out["ffa_fourier"] = bench_fourier(args, dev)
+    if world == 1:
+        out["ffa_freq"] = bench_ffa_freq(args, dev)
     if not args.no_prune:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
@@ -617,8 +592,10 @@ def bench_gpu(args) -> dict | None:
         if not args.no_learned:
             out["prune"]["learned"] = bench_learned(args, dev)
         if not args.no_thresholds:
-            out["threshold_design"] = bench_thresholds(args, dev,
-                                                       out["prune"]["branching_pattern"])
+            from pyloki_gb300.branching import generate_branching_pattern
+
+            out["threshold_design"] = bench_thresholds(
+                args, dev, generate_branching_pattern(make_prune_cfg(), ref_seg=64))
     if dist is not None:
         dist.destroy_process_group()
     return out
@@ -669,6 +646,59 @@ def bench_fourier(args, dev) -> dict:
                   for i in range(1, len(marks))}
         out[name] = {"trials_per_s": trials / (ms_step * 1e-3), "ms_per_step": ms_step,
                      "trials": trials, "best_snr": best, "phases_ms": phases}
+    return out
+
+
+def bench_ffa_freq(args, dev) -> dict:
+    """The plain FFA frequency search that the reference can run on a CPU:
+    one series of 2^20 samples at 64 us with a von Mises pulse (5 % duty,
+    P = 0.5 s, folded S/N 12 by the reference's calibration), periods
+    0.1-1 s, 64 bins, widths 1-32. The GPU search and the CPU oracle (all
+    host threads) of the whole search; the best candidate of each."""
+    import torch
+
+    from pyloki_gb300 import ParamLimits, PulsarSearchConfig
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.pulse import PulseSignalConfig
+    from pyloki_gb300.timeseries import TimeSeries
+
+    cfg = PulsarSearchConfig(nsamps=2**20, tsamp=64e-6, nbins=64, eta=1.0,
+                             param_limits=ParamLimits.from_taylor((1.0, 10.0)).limits,
+                             ducy_max=0.5, wtsp=2.0, use_fourier=False)
+    sig = PulseSignalConfig(period=0.5, dt=64e-6, nsamps=2**20, snr=12.0, ducy=0.05)
+    ts = sig.generate(shape="von_mises", seed=1100, device=dev)
+    trials = final_trials(cfg)
+    dyp = DynamicProgramming(ts, cfg, device=dev)
+
+    def step():
+        dyp.reset()
+        return dyp.search(norm=args.norm)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        snr = step()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / args.steps
+    best = snr.reshape(-1, snr.shape[-1]).amax(dim=1)
+    i = int(torch.argmax(best))
+    f = cfg.get_param_arr(cfg.get_dparams(cfg.niters_ffa))[-1]
+    out = {"workload": "ffa_freq_search_2^20 (periods 0.1-1 s, 64 bins, widths 1-32)",
+           "value": trials / (ms * 1e-3), "unit": "trials/s", "ms_per_step": ms,
+           "trials": trials, "final_path": dyp.final_path,
+           "best": {"snr": float(best[i]), "period_s": float(1 / f[i])}}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+
+        host = TimeSeries(ts.ts_e.cpu().numpy(), ts.ts_v.cpu().numpy(), cfg.tsamp)
+        dt, nt = run_cpu_oracle(cfg, host)
+        out["cpu_baseline"] = {"value": nt / dt, "unit": "trials/s", "cores": O.max_threads(),
+                               "kind": "port", "sample": f"the whole search ({nt} trials)",
+                               "seconds": dt}
     return out
 
 
@@ -1306,19 +1336,27 @@ def headline(out: dict) -> dict:
     for k in ("roofline", "cpu_baseline", "e2e"):
         if k in out:
             h[k] = {kk: vv for kk, vv in out[k].items()
-                    if kk not in ("traffic_source", "sample") or k == "cpu_baseline"}
+                    if kk not in ("traffic_source", "sample", "peak_kind",
+                                  "algorithmic_bytes_per_launch") or k == "cpu_baseline"}
+    if "roofline" in h:  # the kernel's name only; the detail file has the description
+        h["roofline"]["kernel"] = h["roofline"]["kernel"].split(" (")[0]
     if "prune" in out:
         p = out["prune"]
-        sub = {k: p[k] for k in ("metric", "value", "unit", "ms_per_step", "leaves_per_step")
-               if k in p}
+        sub = {k: p[k] for k in ("metric", "value", "unit", "ms_per_step", "leaves_per_step",
+                                 "speedup_vs_plain") if k in p}
+        if "plain" in p:
+            sub["plain"] = {"value": p["plain"]["value"], "ms_per_run": p["plain"]["ms_per_run"]}
         pc = p.get("config", {})
-        sub["config"] = {k: pc[k] for k in ("workload", "thresholds", "ref_segment") if k in pc}
+        sub["config"] = {k: pc[k] for k in ("workload", "thresholds", "ref_segments", "streams")
+                         if k in pc}
         for k in ("roofline", "cpu_baseline", "e2e"):
             if k in p:
                 sub[k] = {kk: vv for kk, vv in p[k].items()
                           if kk in ("kernel", "bound", "achieved", "peak", "unit", "frac",
                                     "traffic", "value", "cores", "kind", "ms_per_step",
-                                    "h2d_bytes_per_step", "d2h_bytes_per_step", "sample")}
+                                    "h2d_bytes_per_step", "d2h_bytes_per_step")}
+        if "roofline" in sub:
+            sub["roofline"]["kernel"] = sub["roofline"]["kernel"].split(" (")[0]
         if "learned" in p and isinstance(p["learned"], dict):
             lh = p["learned"].get("headline")
             if lh:

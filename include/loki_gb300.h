@@ -683,6 +683,13 @@ typedef struct {
 /* Shared memory one MLP block uses (bytes). */
 int64_t loki_mlp_smem_bytes(void);
 
+/* Test hook for the bounded tensor-core waits of the MLP kernels: with on != 0
+ * (current device) every completed MMA wait is treated as expired, so the
+ * kernels take their timeout path (tensor memory freed, LOKI_DEVERR_TIMEOUT in
+ * the error word) with nothing left in flight; 0 restores normal operation.
+ * Synchronous. No reference counterpart (error-path testing only). */
+int loki_mlp_force_timeout(int32_t on);
+
 /* logits[i] for features x (n, 16) float32 (rounded to bfloat16 on load). */
 int loki_mlp_forward(const LokiMLP* w, const float* x, int64_t n, float* logits,
                      int32_t* dev_err, void* stream);

@@ -254,6 +254,7 @@ SIGNATURES: dict[str, tuple] = {
     "loki_mlp_smem_bytes": (C.c_int64, []),
     "loki_branch_features": (C.c_int, [_P, _P, _I64, _I32, C.c_float, C.c_float, C.c_float,
                                        C.c_float, _P, _P, _P]),
+    "loki_mlp_force_timeout": (C.c_int, [_I32]),
     "loki_mlp_forward": (C.c_int, [C.POINTER(LokiMLP), _P, _I64, _P, _P, _P]),
     "loki_mlp_backward": (C.c_int, [C.POINTER(LokiMLP), _P, _P, _P, _I64, C.c_float,
                                     C.POINTER(LokiMLPGrad), _P, _P, _P]),

@@ -208,6 +208,12 @@ __device__ void stage_weights(MlpSmem& S, const LokiMLP& W, bool backward) {
   }
 }
 
+// Test hook (loki_mlp_force_timeout): when set, an MMA wait that completed is
+// treated as one that gave up. The commit has landed, so no tensor-core work
+// is left in flight; the kernel then takes its timeout path (TMEM freed,
+// LOKI_DEVERR_TIMEOUT reported) exactly as after a real bounded-wait expiry.
+__device__ int g_mlp_force_timeout = 0;
+
 // One MMA group: thread 0 issues, commits; everyone waits (bounded).
 template <typename F>
 __device__ __forceinline__ bool mma_sync(MlpSmem& S, uint32_t& phase, F issue) {
@@ -219,7 +225,7 @@ __device__ __forceinline__ bool mma_sync(MlpSmem& S, uint32_t& phase, F issue) {
     issue();
     mma_commit(&S.bar);
   }
-  const bool ok = mbar_wait(&S.bar, phase);
+  const bool ok = mbar_wait(&S.bar, phase) && !g_mlp_force_timeout;
   phase ^= 1u;
   tc_fence_after();
   if (!ok) S.failed = 1;
@@ -509,6 +515,13 @@ static int mlp_grid(int64_t n) {
 using namespace loki;
 
 extern "C" int64_t loki_mlp_smem_bytes(void) { return (int64_t)sizeof(MlpSmem); }
+
+extern "C" int loki_mlp_force_timeout(int32_t on) {
+  const int v = on ? 1 : 0;
+  if (cudaMemcpyToSymbol(g_mlp_force_timeout, &v, sizeof(v)) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaMemcpyToSymbol failed");
+  return LOKI_OK;
+}
 
 extern "C" int loki_mlp_forward(const LokiMLP* w, const float* x, int64_t n, float* logits,
                                 int32_t* dev_err, void* stream) {

@@ -2496,11 +2496,13 @@ extern "C" int loki_prune_ascend_complex(const LokiPruneLevel* lvl, const double
 
 namespace loki {
 
-__global__ void run_seed_kernel(int64_t* cnt, int64_t n) {
+__global__ void run_seed_kernel(int64_t* cnt, int64_t n, unsigned* keys) {
   cnt[0] = n;
   cnt[1] = 0;
   cnt[2] = 0;
   cnt[3] = 0;
+  keys[0] = 0xFFFFFFFFu;  // score min / max keys of the first level
+  keys[1] = 0u;
 }
 
 // children of the level = offsets[parents]; above the workspace the level
@@ -2521,15 +2523,19 @@ __global__ void run_children_kernel(int64_t* cnt, const int64_t* offsets, int64_
 
 __global__ void run_survivors_kernel(int64_t* cnt, const int64_t* pos) { cnt[2] = pos[cnt[1]]; }
 
-// level record; the survivors are the next level's parents
-__global__ void run_level_end_kernel(int64_t* cnt, const float* minmax, int32_t* ovf_flag,
+// level record (score range from the ordered keys, as minmax_finish_kernel);
+// the survivors are the next level's parents, the keys restart
+__global__ void run_level_end_kernel(int64_t* cnt, unsigned* keys, int32_t* ovf_flag,
                                      LokiPruneLevelStats* st) {
   st->n_surv = cnt[2];
-  st->score_min = minmax[0];
-  st->score_max = minmax[1];
+  const bool none = keys[0] == 0xFFFFFFFFu;  // no finite score
+  st->score_min = none ? 0.0f : key_float(keys[0]);
+  st->score_max = none ? 0.0f : key_float(keys[1]);
   st->overflow = *ovf_flag;
   st->reserved = 0;
   *ovf_flag = 0;
+  keys[0] = 0xFFFFFFFFu;
+  keys[1] = 0u;
   cnt[3] += cnt[2];  // backtrack history rows
   cnt[0] = cnt[2];
 }
@@ -2616,7 +2622,7 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
   unsigned* keys = reinterpret_cast<unsigned*>(w.minmax);
   const int row_bt = P + 2, row_leaf = (P + 2) * 2;
   note_launch();
-  run_seed_kernel<<<1, 1, 0, s>>>(cnt, seed_n);
+  run_seed_kernel<<<1, 1, 0, s>>>(cnt, seed_n, keys);
   for (int l = 1; l <= nlevels; ++l) {
     const LokiPruneLevel& D = lvls[l - 1];
     const LokiPruneTree& in = tr[(l - 1) & 1];
@@ -2625,22 +2631,20 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
     const double thr = thresholds[l - 1];
     LokiPruneLevelStats* st = run->stats + (l - 1);
     LokiBranchInfo* info = reinterpret_cast<LokiBranchInfo*>(w.info);
-    for (int i = 0; i < 6; ++i) note_launch();
+    for (int i = 0; i < 3; ++i) note_launch();
     prune_branch_kernel<<<g_par, 256, 0, s>>>(D, in.leaves, w.par_cap, info, w.offsets, dev_err,
                                               nullptr, cnt);
     rc = exclusive_scan_dev<false>(w.offsets, w.par_cap, cnt, 0.0, w.offsets, w.scan,
                                    w.scan_bytes, scan_grid, s);
     if (rc) return rc;
     run_children_kernel<<<1, 1, 0, s>>>(cnt, w.offsets, w.child_cap, st, dev_err);
-    minmax_init_kernel<<<1, 1, 0, s>>>(keys);
     prune_score_kernel<<<g_score, kPruneWarps * 32, smem, s>>>(
         D, in.leaves, in.folds, 0, info, w.offsets, 0, seg, sp, SK, w.child_scores, w.child_idx,
         w.child_phase, keys, cnt);
-    minmax_finish_kernel<<<1, 1, 0, s>>>(keys, w.minmax);
     rc = exclusive_scan_dev<true>(w.child_scores, w.child_cap, cnt + 1, thr, pos, w.sscan,
                                   sums_bytes, scan_grid, s);
     if (rc) return rc;
-    for (int i = 0; i < 6; ++i) note_launch();
+    for (int i = 0; i < 5; ++i) note_launch();
     select_scatter_kernel<<<g_flat, 256, 0, s>>>(w.child_scores, 0, thr, pos, w.surv, cnt + 1);
     run_survivors_kernel<<<1, 1, 0, s>>>(cnt, pos);
     select_overflow_kernel<<<1, kSelThreads, 0, s>>>(
@@ -2660,7 +2664,7 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
       run_bt_copy_kernel<<<g_flat, 256, 0, s>>>(out.backtracks, cnt, row_bt, run->bt_hist,
                                                 run->bt_rows, dev_err);
     }
-    run_level_end_kernel<<<1, 1, 0, s>>>(cnt, w.minmax, run->ovf_flag, st);
+    run_level_end_kernel<<<1, 1, 0, s>>>(cnt, keys, run->ovf_flag, st);
     rc = check_launch("prune_run");
     if (rc) return rc;
   }

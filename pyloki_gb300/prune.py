@@ -966,6 +966,24 @@ class Pruning:
         self.launches += 1
         return int(n_surv_d.item())
 
+    def rebind(self, dyp) -> None:
+        """Prune the fold of another ``DynamicProgramming`` of the same
+        configuration and shape, keeping this object's buffers, level
+        constants and captured run graphs (they read the fold through a copy
+        made before every device-resident run)."""
+        a, b = self.dyp, dyp
+        same = (a.fold.shape == b.fold.shape and a.fold.dtype == b.fold.dtype
+                and a.device == b.device and a.nsegments == b.nsegments
+                and np.array_equal(a.cfg.param_limits, b.cfg.param_limits)
+                and all(getattr(a.cfg, k) == getattr(b.cfg, k)
+                        for k in ("nsamps", "tsamp", "nbins", "eta", "bseg_brute", "bseg_ffa",
+                                  "prune_poly_order", "ducy_max", "wtsp", "use_fourier",
+                                  "branch_max", "tiling_strategy")))
+        if not same:
+            msg = "rebind needs a fold of the same configuration and shape"
+            raise ValueError(msg)
+        self._dyp = dyp
+
     # ---- device-resident runs (loki_prune_run) ---------------------------------
     @property
     def device_run_supported(self) -> bool:
@@ -1169,6 +1187,10 @@ class _DeviceBuffers:
             "best_leaves": torch.zeros((nlev, P + 2, 2), dtype=f64, device=dev),
             "best_scores": torch.zeros(nlev, dtype=f32, device=dev),
             "bt_hist": torch.empty((bt_rows, P + 2), dtype=t32, device=dev),
+            # the FFA fold the runs read: a copy made on the stream before each
+            # run, so a captured graph serves any fold of the same shape
+            "mirror": torch.empty(int(prn.dyp.fold.numel()), dtype=f32, device=dev),
+            "seed_scores": torch.empty(cap, dtype=f32, device=dev),
         }
         m = self.mem
         r = _lib.LokiPruneRun()
@@ -1217,7 +1239,8 @@ class _DeviceRun:
         if grow is not None:
             child_cap = max(child_cap, grow.need_child, bufs.child_cap if bufs else 0)
             bt_rows = max(bt_rows, grow.need_bt, bufs.bt_rows if bufs else 0)
-        if bufs is None or bufs.child_cap < child_cap or bufs.bt_rows < bt_rows:
+        if (bufs is None or bufs.child_cap < child_cap or bufs.bt_rows < bt_rows
+                or bufs.mem["mirror"].numel() < dyp.fold.numel()):
             prn.__dict__.pop("_device_runs", None)  # their graphs hold the old buffers
             bufs = prn._device_bufs = _DeviceBuffers(prn, child_cap, bt_rows)
         self.bufs = bufs
@@ -1233,25 +1256,33 @@ class _DeviceRun:
         self.need_child = self.need_bt = 0
 
     def _enqueue(self) -> None:
+        """The run from the fold mirror: seed (leaves from the grid, folds
+        and scores from the mirror), then every level."""
         prn, b = self.prn, self.bufs
         t0, seed = b.trees[0], self.seed
         n = seed.size
+        nb = prn.dyp.cfg.nbins
+        stride = int(np.prod(prn.dyp.fold.shape[1:]))
+        mirror = b.mem["mirror"]
         t0["leaves"][:n].copy_(seed.leaves)
-        t0["folds"][:n].copy_(seed.folds)
-        t0["scores"][:n].copy_(seed.scores)
-        t0["scores_ep"][:n].copy_(seed.scores_ep)
-        t0["bt"][:n].copy_(seed.backtracks)
+        t0["folds"][:n].copy_(mirror[self.ref_seg * stride:(self.ref_seg + 1) * stride]
+                              .view(n, 2, nb))
+        _lib.check(prn._lib.loki_snr_score_batch(
+            _lib.ptr(t0["folds"]), n, nb, prn.spec, _lib.ptr(t0["scores"]), prn._stream()))
+        t0["scores_ep"][:n].copy_(t0["scores"][:n])
+        b.mem["seed_scores"][:n].copy_(t0["scores"][:n])  # level-0 statistics
+        t0["bt"][:n].zero_()
         prn._err.zero_()
         if self.nlev == 0:
             return
-        fold = prn.dyp.fold
-        stride = int(np.prod(fold.shape[1:]))
         _lib.check(prn._lib.loki_prune_run(
-            self.descs, self.nlev, _lib.ptr(fold), stride, self.seg_idx.ctypes.data,
+            self.descs, self.nlev, _lib.ptr(mirror), stride, self.seg_idx.ctypes.data,
             self.thresholds.ctypes.data, prn.spec, n, prn.max_sugg, prn.batch_size,
             C.byref(b.run), _lib.ptr(prn._err), prn._stream()))
 
     def launch(self, graph: bool) -> None:
+        fold = self.prn.dyp.fold.reshape(-1)
+        self.bufs.mem["mirror"][: fold.numel()].copy_(fold)  # outside any graph
         if not graph:
             self._enqueue()
             return
@@ -1286,8 +1317,10 @@ class _DeviceRun:
         sc = self.scheme
         prn._scheme = sc
         seed = self.seed
+        s0 = b.mem["seed_scores"][: seed.size]
         st0 = PruneStats(level=0, seg_idx=sc.get_segment_idx(0), threshold=0,
-                         score_min=seed.score_min, score_max=seed.score_max,
+                         score_min=float(s0.min()) if seed.size else 0.0,
+                         score_max=float(s0.max()) if seed.size else 0.0,
                          n_branches=seed.size, n_leaves=seed.size, n_leaves_phy=seed.size,
                          n_leaves_surv=seed.size)
         pstats = [st0]
@@ -1408,57 +1441,96 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     return result_file.as_posix()
 
 
+class PruneBatch:
+    """Device-resident runs of many (fold, reference segment) jobs at once
+    from one host thread (``loki_prune_run``).
+
+    Job i of a call goes to stream i mod ``n_streams``; every stream keeps
+    one ``Pruning`` (rebound to each job's fold of the same configuration),
+    its run buffers and, per reference segment, the run's CUDA graph (with
+    ``graph``), so repeated calls, over the same or new folds, only copy the
+    fold and replay graphs. A round enqueues one run per stream with no host wait, so the
+    streams' small per-level kernels overlap on the GPU, then reads the round
+    back (one wait per run) and, with ``ascend``, re-folds the survivors over
+    all segments. Every run is the same computation as ``Pruning.execute``
+    on its own.
+    """
+
+    def __init__(self, threshold_scheme, *, n_streams: int = 8, graph: bool = True,
+                 **kwargs) -> None:
+        if int(n_streams) < 1:
+            msg = f"n_streams must be greater than 0, got {n_streams}"
+            raise ValueError(msg)
+        self.threshold_scheme = threshold_scheme
+        self.n_streams = int(n_streams)
+        self.graph = graph
+        self.kwargs = kwargs
+        self._streams: list = []
+        self._prns: list[dict] = []  # per stream: {"prn": Pruning}
+        self._bufs: list = []
+
+    def _stream(self, k: int, dev):
+        while len(self._streams) <= k:
+            self._streams.append(torch.cuda.Stream(dev))
+            self._prns.append({})
+            self._bufs.append(None)
+        return self._streams[k]
+
+    def _pruning(self, k: int, dyp) -> Pruning:
+        prn = self._prns[k].get("prn")
+        if prn is not None and prn.dyp is not dyp:
+            try:
+                prn.rebind(dyp)
+            except ValueError:
+                prn = None
+        if prn is None:
+            prn = self._prns[k]["prn"] = Pruning(dyp, self.threshold_scheme, **self.kwargs)
+            if self._bufs[k] is not None:
+                prn._device_bufs = self._bufs[k]
+        return prn
+
+    def run(self, jobs, *, ascend: bool = True) -> list[dict]:
+        """``jobs``: a list of ``(dyp, ref_seg)``; returns ``execute``'s
+        dictionaries in job order."""
+        jobs = list(jobs)
+        if not jobs:
+            return []
+        dev = jobs[0][0].device
+        producer = torch.cuda.current_stream(dev)
+        ns = min(self.n_streams, len(jobs))
+        out: list[dict] = [{} for _ in jobs]
+        for r0 in range(0, len(jobs), ns):
+            started = []
+            for k, (dyp, ref) in enumerate(jobs[r0:r0 + ns]):
+                st = self._stream(k, dev)
+                st.wait_stream(producer)
+                with torch.cuda.stream(st):
+                    prn = self._pruning(k, dyp)
+                    started.append((k, prn, prn._device_enqueue(ref, self.graph)))
+            for k, prn, dr in started:
+                with torch.cuda.stream(self._streams[k]):
+                    prn._device_finish(dr, self.graph)
+                    self._bufs[k] = prn._device_bufs
+                    if ascend:
+                        prn._do_ascend()
+            for k, prn, dr in started:
+                with torch.cuda.stream(self._streams[k]):
+                    out[r0 + k] = {
+                        "run_name": f"{dr.ref_seg:03d}_00", "scheme": prn.scheme.data.copy(),
+                        "param_sets": prn.report(),
+                        "scores": prn.world_tree.scores.cpu().numpy(),
+                        "scores_ep": prn.world_tree.scores_ep.cpu().numpy(),
+                        "level_stats": prn.pstats}
+        for st in self._streams[:ns]:
+            producer.wait_stream(st)
+        return out
+
+
 def run_batch(jobs, threshold_scheme, *, n_streams: int = 8, graph: bool = True,
               ascend: bool = True, **kwargs) -> list[dict]:
-    """Device-resident runs of many (fold, reference segment) jobs at once from
-    one host thread. ``jobs`` is a list of ``(dyp, ref_seg)``. Each of
-    ``n_streams`` CUDA streams has its own run buffers; a round enqueues one
-    run per stream (a CUDA-graph replay with ``graph``) with no host wait, so
-    the streams' small per-level kernels overlap on the GPU, then reads the
-    round back (one wait per run) and, with ``ascend``, re-folds the
-    survivors over all segments. Every run is the same computation as
-    ``Pruning.execute`` on its own; the results come in job order as
-    ``execute``'s dictionaries."""
-    jobs = list(jobs)
-    if not jobs:
-        return []
-    dev = jobs[0][0].device
-    producer = torch.cuda.current_stream(dev)
-    n_streams = max(1, min(int(n_streams), len(jobs)))
-    streams = [torch.cuda.Stream(dev) for _ in range(n_streams)]
-    prns: list[dict] = [{} for _ in range(n_streams)]  # per stream: dyp id -> Pruning
-    bufs: list = [None] * n_streams
-    out: list[dict] = [{} for _ in jobs]
-    for r0 in range(0, len(jobs), n_streams):
-        round_jobs = list(enumerate(jobs[r0:r0 + n_streams]))
-        started = []
-        for k, (dyp, ref) in round_jobs:
-            st = streams[k]
-            st.wait_stream(producer)
-            with torch.cuda.stream(st):
-                prn = prns[k].get(id(dyp))
-                if prn is None:
-                    prn = prns[k][id(dyp)] = Pruning(dyp, threshold_scheme, **kwargs)
-                    if bufs[k] is not None:
-                        prn._device_bufs = bufs[k]
-                started.append((k, prn, prn._device_enqueue(ref, graph)))
-        for k, prn, dr in started:
-            with torch.cuda.stream(streams[k]):
-                prn._device_finish(dr, graph)
-                bufs[k] = prn._device_bufs
-                if ascend:
-                    prn._do_ascend()
-        for k, prn, dr in started:
-            with torch.cuda.stream(streams[k]):
-                out[r0 + k] = {
-                    "run_name": f"{dr.ref_seg:03d}_00", "scheme": prn.scheme.data.copy(),
-                    "param_sets": prn.report(),
-                    "scores": prn.world_tree.scores.cpu().numpy(),
-                    "scores_ep": prn.world_tree.scores_ep.cpu().numpy(),
-                    "level_stats": prn.pstats}
-    for st in streams:
-        producer.wait_stream(st)
-    return out
+    """``PruneBatch(...).run(jobs)`` once (graphs and buffers are not kept)."""
+    return PruneBatch(threshold_scheme, n_streams=n_streams, graph=graph,
+                      **kwargs).run(jobs, ascend=ascend)
 
 
 def run_many(dyp, threshold_scheme, ref_segs, *, n_workers: int = 4,

@@ -70,3 +70,34 @@ def test_training_reduces_loss_and_learns(cuda_device):
     xt, yt, _ = _data(8192, 10)
     acc = ((net.predict(xt).cpu().numpy() > 0.5) == (yt > 0.5)).mean()
     assert acc > 0.9
+
+
+def test_timeout_path_reports_and_recovers(cuda_device):
+    """The MLP kernels' give-up path after a bounded tensor-core wait: with
+    the test hook on, completed waits count as expired (nothing is left in
+    flight), the kernels free their tensor memory and set
+    LOKI_DEVERR_TIMEOUT, and the host raises LokiError. With the hook off
+    the next forward pass is correct again."""
+    from pyloki_gb300 import _lib
+    from pyloki_gb300.learned import BranchMLP, init_params
+
+    lib = _lib.load()
+    flat = init_params(7)
+    net = BranchMLP(flat, device=cuda_device)
+    x, y, w = _data(300, 3)
+    try:
+        _lib.check(lib.loki_mlp_force_timeout(1))
+        net.logits(x)
+        with pytest.raises(_lib.LokiError, match="timed out"):
+            net.check_errors()
+        net.err.zero_()
+        net.loss_and_grads(x, y, w)
+        with pytest.raises(_lib.LokiError, match="timed out"):
+            net.check_errors()
+    finally:
+        _lib.check(lib.loki_mlp_force_timeout(0))
+    net.err.zero_()
+    got = net.logits(x).cpu().numpy()
+    net.check_errors()
+    ref = M.forward(M.split(flat), x)["logit"]
+    np.testing.assert_allclose(got, ref, atol=LOGIT_ABS_TOL, rtol=1e-3)

@@ -134,3 +134,35 @@ def test_run_batch_matches_level_path(cuda_device, n_streams):
             np.testing.assert_array_equal(res["scores_ep"],
                                           p.world_tree.scores_ep.cpu().numpy())
             np.testing.assert_array_equal(res["param_sets"], p.report())
+
+
+def test_prune_batch_rebinds_to_new_folds(cuda_device):
+    """A PruneBatch keeps its graphs across folds of the same configuration:
+    runs over a second series (the first one's noise reversed) equal the
+    level-by-level runs of that series."""
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import PruneBatch, Pruning
+    from pyloki_gb300.timeseries import TimeSeries
+
+    d, prn = _run("prune_taylor", cuda_device)
+    cfg = prn.dyp.cfg
+    dyp2 = DynamicProgramming(TimeSeries(d["ts_e"][::-1].copy(), d["ts_v"], cfg.tsamp), cfg,
+                              device=cuda_device)
+    dyp2.initialize()
+    dyp2.execute()
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
+    runner = PruneBatch(d["thresholds"], n_streams=2, **kw)
+    refs = [1, 6, 9]
+    for dyp in (prn.dyp, dyp2, prn.dyp, dyp2):
+        got = runner.run([(dyp, r) for r in refs])
+        for ref, g in zip(refs, got, strict=True):
+            p = Pruning(dyp, d["thresholds"], **kw)
+            p.initialize(ref)
+            for _ in range(dyp.nsegments - 1):
+                p.execute_iter()
+            p._do_ascend()
+            assert [(s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+                    for s in g["level_stats"]] == [
+                (s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max) for s in p.pstats]
+            np.testing.assert_array_equal(g["scores"], p.world_tree.scores.cpu().numpy())
+            np.testing.assert_array_equal(g["param_sets"], p.report())
