@@ -33,6 +33,10 @@ from pathlib import Path
 import numpy as np
 
 ROOT = Path(__file__).resolve().parent
+# the batched pruning runs put many streams of small kernels in flight: give
+# each of them its own hardware queue (a per-process setting, read at CUDA
+# initialisation)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 

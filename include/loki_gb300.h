@@ -391,6 +391,15 @@ int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves, float* fo
                       const float* ffa_fold, int64_t seg_stride, const LokiScoreSpec* spec,
                       int32_t* dev_err, void* stream);
 
+/* loki_prune_ascend with the survivor count on the device (*n_dev <= n_cap),
+ * for a run whose counts never reach the host (loki_prune_run); Taylor and
+ * Chebyshev trees. Same reference function as loki_prune_ascend. */
+int loki_prune_ascend_dev(const LokiPruneLevel* lvl, const double* leaves, float* folds,
+                          float* scores, float* scores_ep, const int64_t* n_dev, int64_t n_cap,
+                          int32_t nseg, const double* tm_seg, const double* dt_seg,
+                          const int32_t* seg_idx, const float* ffa_fold, int64_t seg_stride,
+                          const LokiScoreSpec* spec, int32_t* dev_err, void* stream);
+
 /* ---- complex (Fourier) folds ---------------------------------------------
  * The same steps for trees over Fourier-domain FFA folds
  * (PrunePolyTaylorComplexDPFuncts / PrunePolyChebyshevComplexDPFuncts):
@@ -563,6 +572,7 @@ int loki_prune_level(const LokiPruneLevel* lvl, const LokiPruneTree* in, LokiPru
 typedef struct {
   int64_t n_parents;
   int64_t n_children;
+  int64_t n_valid;         /* children past validation (the circular tree); n_children otherwise */
   int64_t n_surv;
   float score_min;
   float score_max;
@@ -575,7 +585,8 @@ typedef struct {
   LokiPruneTree trees[2];       /* ping-pong trees, cap >= max_sugg; trees[0] holds the seed */
   LokiPruneWork work;           /* par_cap >= max_sugg, ovf_cap >= max_sugg + child_cap + 1;
                                    host_words and the events are not used */
-  int64_t* counts;              /* 4 words: parents, children, survivors of the level */
+  int64_t* counts;              /* 8 words: parents, children, survivors, backtrack rows,
+                                   valid children of the level */
   int32_t* ovf_flag;            /* 1 word */
   LokiPruneLevelStats* stats;   /* nlevels records */
   double* best_leaves;          /* nlevels rows of (poly_order + 2) * 2, or NULL */
@@ -583,6 +594,14 @@ typedef struct {
   int32_t* bt_hist;             /* bt_rows x (poly_order + 2): every level's survivors'
                                    backtracks in level order, or NULL */
   int64_t bt_rows;
+  /* circular-orbit tree only (basis 2), else NULL: */
+  int64_t* exp_off;             /* par_cap + 1: crackle-expansion children per parent */
+  void* child_map;              /* child_cap x 16 B: the children in batch order */
+  float* valid_flags;           /* child_cap */
+  int64_t* valid_ids;           /* child_cap */
+  int8_t* child_class;          /* child_cap */
+  int32_t* batch_taylor;        /* par_cap / batch_size + 1 */
+  int64_t* batch_offsets;       /* par_cap + 1 */
 } LokiPruneRun;
 
 /* Every level of one reference segment (prune.py:526-613 Pruning.execute

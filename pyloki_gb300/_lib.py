@@ -159,22 +159,25 @@ class LokiPruneLevelResult(C.Structure):
 
 
 class LokiPruneLevelStats(C.Structure):
-    _fields_ = [("n_parents", C.c_int64), ("n_children", C.c_int64), ("n_surv", C.c_int64),
-                ("score_min", C.c_float), ("score_max", C.c_float), ("overflow", C.c_int32),
-                ("reserved", C.c_int32)]
+    _fields_ = [("n_parents", C.c_int64), ("n_children", C.c_int64), ("n_valid", C.c_int64),
+                ("n_surv", C.c_int64), ("score_min", C.c_float), ("score_max", C.c_float),
+                ("overflow", C.c_int32), ("reserved", C.c_int32)]
 
 
 class LokiPruneRun(C.Structure):
     _fields_ = [("trees", LokiPruneTree * 2), ("work", LokiPruneWork), ("counts", C.c_void_p),
                 ("ovf_flag", C.c_void_p), ("stats", C.c_void_p), ("best_leaves", C.c_void_p),
-                ("best_scores", C.c_void_p), ("bt_hist", C.c_void_p), ("bt_rows", C.c_int64)]
+                ("best_scores", C.c_void_p), ("bt_hist", C.c_void_p), ("bt_rows", C.c_int64),
+                ("exp_off", C.c_void_p), ("child_map", C.c_void_p), ("valid_flags", C.c_void_p),
+                ("valid_ids", C.c_void_p), ("child_class", C.c_void_p),
+                ("batch_taylor", C.c_void_p), ("batch_offsets", C.c_void_p)]
 
 
 #: numpy view of an array of LokiPruneLevelStats records
 PRUNE_STATS_DTYPE = np.dtype([("n_parents", np.int64), ("n_children", np.int64),
-                              ("n_surv", np.int64), ("score_min", np.float32),
-                              ("score_max", np.float32), ("overflow", np.int32),
-                              ("reserved", np.int32)])
+                              ("n_valid", np.int64), ("n_surv", np.int64),
+                              ("score_min", np.float32), ("score_max", np.float32),
+                              ("overflow", np.int32), ("reserved", np.int32)])
 
 
 class LokiMLP(C.Structure):
@@ -270,6 +273,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_prune_branch": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_branch_masked": (C.c_int, [_PL, _P, _I64, _P, _P, _P, _P, _I64, _P, _P]),
     "loki_prune_best": (C.c_int, [_P, _I64, _P, _I32, _P, _P, _P]),
+    "loki_prune_ascend_dev": (C.c_int, [_PL, _P, _P, _P, _P, _P, _I64, _I32, _P, _P, _P, _P,
+                                        _I64, C.POINTER(LokiScoreSpec), _P, _P]),
     "loki_prune_run": (C.c_int, [_PL, _I32, _P, _I64, _P, _P, C.POINTER(LokiScoreSpec), _I64,
                                  _I64, _I64, C.POINTER(LokiPruneRun), _P, _P]),
     "loki_prune_level": (C.c_int, [_PL, C.POINTER(LokiPruneTree), C.POINTER(LokiPruneTree),

@@ -502,7 +502,8 @@ prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                    int64_t n_children, const float* __restrict__ seg, LokiScoreSpec sp,
                    ScoreK SK, float* __restrict__ scores, int32_t* __restrict__ cidx,
                    double* __restrict__ cphase, unsigned* __restrict__ minmax_keys,
-                   const int64_t* __restrict__ cnt_dev) {
+                   int64_t* cnt_dev, int64_t child_cap, LokiPruneLevelStats* st,
+                   int32_t* err) {
   extern __shared__ float tiles[];
   const int warp = threadIdx.x >> 5;
   float* tile = tiles + (size_t)warp * 32 * score_stride(D.nbins, sp.wmax);
@@ -513,10 +514,20 @@ prune_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                  cidx, cphase, minmax_keys, tile, c0);
     return;
   }
-  // device counts: cnt_dev[0] parents, cnt_dev[1] children; warps stride
-  // over the 32-child tiles
+  // device counts: cnt_dev[0] parents; the children are offsets[parents],
+  // none when they exceed the workspace (the run is then flagged). Block 0
+  // records them for the later kernels of the level. Warps stride over the
+  // 32-child tiles.
   n_parents = cnt_dev[0];
-  n_children = cnt_dev[1];
+  const int64_t total = offsets[n_parents];
+  n_children = total > child_cap ? 0 : total;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt_dev[1] = n_children;
+    st->n_parents = n_parents;
+    st->n_children = total;
+    st->n_valid = total;
+    if (total > child_cap) atomicOr(err, LOKI_DEVERR_CAPACITY);
+  }
   for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_children;
        t += (int64_t)gridDim.x * kPruneWarps) {
     score_tile(D, leaves, folds, n_parents, info, offsets, n_children, seg, sp, SK, scores,
@@ -622,23 +633,29 @@ __device__ unsigned block_select(const unsigned* keys, int64_t n, int64_t r, uns
   return prefix;
 }
 
-// With cnt_dev (device counts: [0] parents, [2] survivors of the plain
-// selection) the kernel does nothing unless more than cap survived, and then
-// sets *ovf_flag.
+// With cnt_dev (device counts: [0] parents) the plain selection's survivor
+// count is pos[*n_in] (n_in: its inputs, the children): it is stored at *n_out, and
+// the kernel does nothing more unless it exceeds cap (then *ovf_flag is set
+// and the overflow rule rewrites the selection and *n_out). n_out points into
+// the same counters, so neither pointer is restrict.
 __global__ void __launch_bounds__(kSelThreads)
 select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restrict__ offsets,
                        int64_t n_parents, int64_t batch, double thr, int64_t cap,
-                       int64_t* __restrict__ ids, int64_t* __restrict__ n_out,
+                       int64_t* __restrict__ ids, int64_t* n_out,
                        double* __restrict__ thr_out, int64_t* __restrict__ tmp_ids,
-                       unsigned* __restrict__ keys, const int64_t* __restrict__ cnt_dev,
-                       int32_t* __restrict__ ovf_flag) {
+                       unsigned* __restrict__ keys, const int64_t* cnt_dev,
+                       int32_t* __restrict__ ovf_flag, const int64_t* __restrict__ pos,
+                       const int64_t* n_in) {
   __shared__ int wsum[33];
   __shared__ unsigned hist[256];
   __shared__ long long vs_sh;
   __shared__ double cur_sh;
   if (cnt_dev) {
-    if (cnt_dev[2] <= cap) return;  // uniform over the block
+    const int64_t n_sel = pos[*n_in];  // the selection's total over its n_in inputs
     n_parents = cnt_dev[0];
+    __syncthreads();  // every thread has read the counters
+    if (threadIdx.x == 0) *n_out = n_sel;
+    if (n_sel <= cap) return;  // uniform over the block
     if (threadIdx.x == 0) *ovf_flag = 1;
   }
   if (threadIdx.x == 0) {
@@ -935,22 +952,18 @@ __device__ __forceinline__ void circ_shift(const double* p, double dt, bool hole
 // ascend: warp per 32 survivors, segments accumulated in order
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+// Survivors s0 .. s0 + 31 (those below n) of one warp; acc and tile are the
+// warp's accumulators (32 x 2 nb) and score tile.
+__device__ __forceinline__ void ascend_tile(const LokiPruneLevel& D, const double* __restrict__ leaves,
                     float* __restrict__ folds, float* __restrict__ scores,
                     float* __restrict__ scores_ep, int64_t n, int nseg,
                     const double* __restrict__ tm_seg, const double* __restrict__ dt_seg,
                     const int32_t* __restrict__ seg_idx, const float* __restrict__ ffa,
-                    int64_t seg_stride, LokiScoreSpec sp, ScoreK SK) {
-  extern __shared__ float tiles[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                    int64_t seg_stride, const LokiScoreSpec& sp, const ScoreK& SK, float* acc,
+                    float* tile, int64_t s0) {
+  const int lane = threadIdx.x & 31;
   const int nb = D.nbins, P = D.poly_order, m = P + 1;
-  // per warp: the 32 accumulators (2 * nb each) followed by the score tile
   const int stride = score_stride(nb, sp.wmax);
-  float* acc = tiles + (size_t)warp * 32 * (2 * nb + stride);
-  float* tile = acc + 32 * 2 * nb;
-  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
-  if (s0 >= n) return;
   const int kmax = (int)std::min<int64_t>(32, n - s0);
   for (int k = 0; k < kmax; ++k)
     for (int j = lane; j < 2 * nb; j += 32) acc[k * 2 * nb + j] = 0.0f;
@@ -1070,6 +1083,36 @@ prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
 }
 
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                    float* __restrict__ folds, float* __restrict__ scores,
+                    float* __restrict__ scores_ep, int64_t n, int nseg,
+                    const double* __restrict__ tm_seg, const double* __restrict__ dt_seg,
+                    const int32_t* __restrict__ seg_idx, const float* __restrict__ ffa,
+                    int64_t seg_stride, LokiScoreSpec sp, ScoreK SK,
+                    const int64_t* __restrict__ n_dev) {
+  extern __shared__ float tiles[];
+  const int warp = threadIdx.x >> 5;
+  // per warp: the 32 accumulators (2 * nb each) followed by the score tile
+  const int stride = score_stride(D.nbins, sp.wmax);
+  float* acc = tiles + (size_t)warp * 32 * (2 * D.nbins + stride);
+  float* tile = acc + 32 * 2 * D.nbins;
+  if (!n_dev) {
+    const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+    if (s0 < n)
+      ascend_tile(D, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa,
+                  seg_stride, sp, SK, acc, tile, s0);
+    return;
+  }
+  n = *n_dev;  // survivors held on the device: warps stride over their tiles
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    ascend_tile(D, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa,
+                seg_stride, sp, SK, acc, tile, t * 32);
+    __syncwarp();  // the accumulators are reused by the next tile
+  }
+}
+
 // ---------------------------------------------------------------------------
 // circular-orbit Taylor tree (core/circular.py, dynamic/dyn_circular_taylor.py)
 //
@@ -1119,12 +1162,35 @@ __device__ __forceinline__ void circ_child(const LokiBranchInfo& B, const double
 // Branch every parent (circ_taylor_branch_batch): per-parameter branching of
 // d4..d1 as in the Taylor tree, crackle deferred; counts the children that
 // keep the parent crackle and those produced by crackle expansion.
+__device__ __forceinline__ void circ_branch_one(const LokiPruneLevel& D,
+                                                const double* __restrict__ leaves, int64_t i,
+                                                LokiBranchInfo* __restrict__ info,
+                                                int64_t* __restrict__ n_keep,
+                                                int64_t* __restrict__ n_exp,
+                                                int32_t* __restrict__ err);
+
+// n_dev, when not null, holds the parent count on the device (grid-stride).
 __global__ void circ_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                                    int64_t n, LokiBranchInfo* __restrict__ info,
                                    int64_t* __restrict__ n_keep, int64_t* __restrict__ n_exp,
-                                   int32_t* __restrict__ err) {
+                                   int32_t* __restrict__ err, const int64_t* __restrict__ n_dev) {
+  if (n_dev) {
+    n = *n_dev;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      circ_branch_one(D, leaves, i, info, n_keep, n_exp, err);
+    return;
+  }
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i < n) circ_branch_one(D, leaves, i, info, n_keep, n_exp, err);
+}
+
+__device__ __forceinline__ void circ_branch_one(const LokiPruneLevel& D,
+                                                const double* __restrict__ leaves, int64_t i,
+                                                LokiBranchInfo* __restrict__ info,
+                                                int64_t* __restrict__ n_keep,
+                                                int64_t* __restrict__ n_exp,
+                                                int32_t* __restrict__ err) {
   const int P = 5;
   const double* lf = leaves + i * (P + 2) * 2;
   const double f0 = lf[(P + 1) * 2];
@@ -1193,13 +1259,51 @@ __global__ void circ_branch_kernel(LokiPruneLevel D, const double* __restrict__ 
 
 // Children of every parent at their batch-ordered positions, plus a validity
 // flag (1.0 / 0.0) per child for the compaction.
+__device__ __forceinline__ void circ_map_one(const LokiPruneLevel& D,
+                                             const double* __restrict__ leaves, int64_t n,
+                                             int64_t batch, const LokiBranchInfo* __restrict__ info,
+                                             const int64_t* __restrict__ keep_off,
+                                             const int64_t* __restrict__ exp_off,
+                                             CircChild* __restrict__ map,
+                                             float* __restrict__ validf, int64_t i);
+
+// With cnt (device counts) the parents are cnt[0] and the children
+// keep_off[n] + exp_off[n]; block 0 records the children in cnt[1] and the
+// level's statistics, and above child_cap the level gets none (flagged).
 __global__ void circ_map_kernel(LokiPruneLevel D, const double* __restrict__ leaves, int64_t n,
                                 int64_t batch, const LokiBranchInfo* __restrict__ info,
                                 const int64_t* __restrict__ keep_off,
                                 const int64_t* __restrict__ exp_off,
-                                CircChild* __restrict__ map, float* __restrict__ validf) {
+                                CircChild* __restrict__ map, float* __restrict__ validf,
+                                int64_t* cnt, int64_t child_cap, LokiPruneLevelStats* st,
+                                int32_t* err) {
+  if (cnt) {
+    n = cnt[0];
+    const int64_t total = keep_off[n] + exp_off[n];
+    const bool fits = total <= child_cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      cnt[1] = fits ? total : 0;
+      st->n_parents = n;
+      st->n_children = total;
+      if (!fits) atomicOr(err, LOKI_DEVERR_CAPACITY);
+    }
+    if (!fits) return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+      circ_map_one(D, leaves, n, batch, info, keep_off, exp_off, map, validf, i);
+    return;
+  }
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i < n) circ_map_one(D, leaves, n, batch, info, keep_off, exp_off, map, validf, i);
+}
+
+__device__ __forceinline__ void circ_map_one(const LokiPruneLevel& D,
+                                             const double* __restrict__ leaves, int64_t n,
+                                             int64_t batch, const LokiBranchInfo* __restrict__ info,
+                                             const int64_t* __restrict__ keep_off,
+                                             const int64_t* __restrict__ exp_off,
+                                             CircChild* __restrict__ map,
+                                             float* __restrict__ validf, int64_t i) {
   const int P = 5;
   const int64_t b0 = (i / batch) * batch, b1 = std::min(b0 + batch, n);
   int64_t pk = keep_off[i] + exp_off[b0];
@@ -1250,7 +1354,15 @@ __device__ __forceinline__ int64_t lower_bound64(const int64_t* a, int64_t n, in
 __global__ void circ_boff_kernel(const int64_t* __restrict__ keep_off,
                                  const int64_t* __restrict__ exp_off, int64_t n,
                                  const int64_t* __restrict__ valid_ids, int64_t n_valid,
-                                 int64_t* __restrict__ boff) {
+                                 int64_t* __restrict__ boff, const int64_t* __restrict__ cnt) {
+  if (cnt) {  // device counts: cnt[0] parents, cnt[4] valid children
+    n = cnt[0];
+    n_valid = cnt[4];
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n;
+         p += (int64_t)gridDim.x * blockDim.x)
+      boff[p] = lower_bound64(valid_ids, n_valid, keep_off[p] + exp_off[p]);
+    return;
+  }
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p > n) return;
   boff[p] = lower_bound64(valid_ids, n_valid, keep_off[p] + exp_off[p]);
@@ -1292,22 +1404,19 @@ __device__ __forceinline__ int circ_resolve(const LokiPruneLevel& D, const doubl
   return cls;
 }
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-circ_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+// Valid children v0 .. v0 + 31 (those below n_valid) of one warp.
+__device__ __forceinline__ void circ_score_tile(const LokiPruneLevel& D, const double* __restrict__ leaves,
                   const float* __restrict__ folds, int64_t batch,
                   const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
                   const int64_t* __restrict__ valid_ids, int64_t n_valid,
-                  const float* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                  const float* __restrict__ seg, const LokiScoreSpec& sp, const ScoreK& SK,
                   float* __restrict__ scores, int32_t* __restrict__ cidx,
                   double* __restrict__ cphase, int8_t* __restrict__ ccls,
-                  int32_t* __restrict__ batch_taylor, unsigned* __restrict__ minmax_keys) {
-  extern __shared__ float tiles[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                  int32_t* __restrict__ batch_taylor, unsigned* __restrict__ minmax_keys,
+                  float* tile, int64_t v0) {
+  const int lane = threadIdx.x & 31;
   const int nb = D.nbins, P = 5;
   const int stride = score_stride(nb, sp.wmax);
-  float* tile = tiles + (size_t)warp * 32 * stride;
-  const int64_t v0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
-  if (v0 >= n_valid) return;
   const int kmax = (int)std::min<int64_t>(32, n_valid - v0);
   int64_t my_par = 0, my_row = 0;
   int my_shift = 0;
@@ -1358,13 +1467,48 @@ circ_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
 }
 
+// With cnt (device counts) the valid children are pos_v[cnt[1]] (the
+// validity compaction's total); block 0 records them in cnt[4] and st.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_score_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                  const float* __restrict__ folds, int64_t batch,
+                  const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+                  const int64_t* __restrict__ valid_ids, int64_t n_valid,
+                  const float* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                  float* __restrict__ scores, int32_t* __restrict__ cidx,
+                  double* __restrict__ cphase, int8_t* __restrict__ ccls,
+                  int32_t* __restrict__ batch_taylor, unsigned* __restrict__ minmax_keys,
+                  int64_t* cnt, const int64_t* __restrict__ pos_v, LokiPruneLevelStats* st) {
+  extern __shared__ float tiles[];
+  const int warp = threadIdx.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(D.nbins, sp.wmax);
+  if (!cnt) {
+    const int64_t v0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+    if (v0 < n_valid)
+      circ_score_tile(D, leaves, folds, batch, info, map, valid_ids, n_valid, seg, sp, SK,
+                      scores, cidx, cphase, ccls, batch_taylor, minmax_keys, tile, v0);
+    return;
+  }
+  n_valid = pos_v[cnt[1]];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[4] = n_valid;
+    st->n_valid = n_valid;
+  }
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_valid;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    circ_score_tile(D, leaves, folds, batch, info, map, valid_ids, n_valid, seg, sp, SK, scores,
+                    cidx, cphase, ccls, batch_taylor, minmax_keys, tile, t * 32);
+    __syncwarp();
+  }
+}
+
 // New tree from the survivors: circ_taylor_transform_batch
 // (core/circular.py:669-705, moving grid), the basis flag written by the
 // moving-grid resolve (core/circular.py:478-509: 1 snap, 2 crackle, and 0 for
 // the crackle children of a batch that also holds Taylor children), backtracks
 // and folds.
-__global__ void __launch_bounds__(kPruneWarps * 32)
-circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+// Survivors s0 .. s0 + 31 (those below n_surv) of one warp.
+__device__ __forceinline__ void circ_emit_tile(const LokiPruneLevel& D, const double* __restrict__ leaves,
                  const float* __restrict__ folds, int64_t batch,
                  const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
                  const int64_t* __restrict__ valid_ids, const float* __restrict__ seg,
@@ -1373,11 +1517,9 @@ circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
                  const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
                  const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
                  float* __restrict__ fout, float* __restrict__ sout,
-                 float* __restrict__ seout, int32_t* __restrict__ bout) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                 float* __restrict__ seout, int32_t* __restrict__ bout, int64_t s0) {
+  const int lane = threadIdx.x & 31;
   const int nb = D.nbins, P = 5, m = 6;
-  const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
-  if (s0 >= n_surv) return;
   const int kmax = (int)std::min<int64_t>(32, n_surv - s0);
   int64_t my_par = 0, my_row = 0;
   int my_shift = 0;
@@ -1450,6 +1592,33 @@ circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
       o[nb + j] = __fadd_rn(pf[nb + j], sf[nb + js]);
     }
   }
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_emit_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                 const float* __restrict__ folds, int64_t batch,
+                 const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+                 const int64_t* __restrict__ valid_ids, const float* __restrict__ seg,
+                 const int64_t* __restrict__ surv, int64_t n_surv,
+                 const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
+                 const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
+                 const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
+                 float* __restrict__ fout, float* __restrict__ sout,
+                 float* __restrict__ seout, int32_t* __restrict__ bout,
+                 const int64_t* __restrict__ cnt) {
+  const int warp = threadIdx.x >> 5;
+  if (!cnt) {
+    const int64_t s0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32;
+    if (s0 < n_surv)
+      circ_emit_tile(D, leaves, folds, batch, info, map, valid_ids, seg, surv, n_surv, cscores,
+                     cidx, cphase, ccls, batch_taylor, lout, fout, sout, seout, bout, s0);
+    return;
+  }
+  n_surv = cnt[2];  // device counts: warps stride over the survivors' tiles
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_surv;
+       t += (int64_t)gridDim.x * kPruneWarps)
+    circ_emit_tile(D, leaves, folds, batch, info, map, valid_ids, seg, surv, n_surv, cscores,
+                   cidx, cphase, ccls, batch_taylor, lout, fout, sout, seout, bout, t * 32);
 }
 
 // ---------------------------------------------------------------------------
@@ -1879,15 +2048,34 @@ static int prune_branch_impl(const LokiPruneLevel* lvl, const double* leaves,
                              int64_t* offsets, void* scan_scratch, int64_t scan_scratch_bytes,
                              int32_t* dev_err, void* stream);
 
+// End of a device-resident level (single thread): the level's record (score
+// range from the ordered keys, as minmax_finish_kernel), then the survivors
+// become the next level's parents and the keys restart.
+__device__ __forceinline__ void level_end(int64_t* cnt, unsigned* keys, int32_t* ovf_flag,
+                                          LokiPruneLevelStats* st) {
+  st->n_surv = cnt[2];
+  const bool none = keys[0] == 0xFFFFFFFFu;  // no finite score
+  st->score_min = none ? 0.0f : key_float(keys[0]);
+  st->score_max = none ? 0.0f : key_float(keys[1]);
+  st->overflow = *ovf_flag;
+  st->reserved = 0;
+  *ovf_flag = 0;
+  keys[0] = 0xFFFFFFFFu;
+  keys[1] = 0u;
+  cnt[3] += cnt[2];  // backtrack history rows
+  cnt[0] = cnt[2];
+}
+
 // Best leaf of a tree (max score, first index on ties, as torch.argmax):
 // one block reduces (score, index), then copies the leaf row and its score.
 __global__ void __launch_bounds__(1024)
 prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __restrict__ leaves,
                   int row, double* __restrict__ leaf_out, float* __restrict__ score_out,
-                  const int64_t* __restrict__ n_dev) {
+                  int64_t* lvl_cnt, unsigned* lvl_keys, int32_t* lvl_ovf,
+                  LokiPruneLevelStats* lvl_st) {
   __shared__ float sv[32];
   __shared__ int64_t si[32];
-  if (n_dev) n = *n_dev;  // a count of 0 writes nothing (bi stays -1)
+  if (lvl_cnt) n = lvl_cnt[2];  // the level's survivors; 0 writes nothing (bi stays -1)
   float bv = -INFINITY;
   int64_t bi = -1;
   // each thread visits its elements in increasing index order, so it keeps
@@ -1965,6 +2153,7 @@ prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __r
     if (bi >= 0)
       for (int j = lane; j < row; j += 32) leaf_out[j] = leaves[bi * row + j];
     if (lane == 0 && bi >= 0) *score_out = scores[bi];
+    if (lane == 0 && lvl_cnt) level_end(lvl_cnt, lvl_keys, lvl_ovf, lvl_st);
   }
 }
 
@@ -1977,7 +2166,8 @@ extern "C" int loki_prune_best(const float* scores, int64_t n, const double* lea
     return set_error(LOKI_ERR_INVALID, "null pointer argument");
   note_launch();
   prune_best_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(scores, n, leaves, row_len, leaf_out,
-                                                         score_out, nullptr);
+                                                         score_out, nullptr, nullptr, nullptr,
+                                                         nullptr);
   return check_launch("prune_best");
 }
 
@@ -2055,7 +2245,7 @@ extern "C" int loki_prune_score(const LokiPruneLevel* lvl, const double* leaves,
     note_launch();
     prune_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
         *lvl, leaves, folds, n_parents, info, offsets, n_children, fold_segment, sp, SK,
-        child_scores, child_idx, child_phase, keys, nullptr);
+        child_scores, child_idx, child_phase, keys, nullptr, 0, nullptr, nullptr);
   }
   note_launch();
   minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
@@ -2104,7 +2294,8 @@ extern "C" int loki_prune_select_overflow(const float* child_scores, const int64
   note_launch();
   select_overflow_kernel<<<1, kSelThreads, 0, (cudaStream_t)stream>>>(
       child_scores, offsets, n_parents, batch_size, threshold, capacity, surv_ids, n_surv,
-      thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys), nullptr, nullptr);
+      thr_out, scratch_ids, reinterpret_cast<unsigned*>(scratch_keys), nullptr, nullptr,
+      nullptr, nullptr);
   (void)scratch_len;
   return check_launch("prune_select_overflow");
 }
@@ -2160,8 +2351,46 @@ extern "C" int loki_prune_ascend(const LokiPruneLevel* lvl, const double* leaves
   note_launch();
   prune_ascend_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, (cudaStream_t)stream>>>(
       *lvl, leaves, folds, scores, scores_ep, n, nseg, tm_seg, dt_seg, seg_idx, ffa_fold,
-      seg_stride, sp, SK);
+      seg_stride, sp, SK, nullptr);
   return check_launch("prune_ascend");
+}
+
+extern "C" int loki_prune_ascend_dev(const LokiPruneLevel* lvl, const double* leaves,
+                                     float* folds, float* scores, float* scores_ep,
+                                     const int64_t* n_dev, int64_t n_cap, int32_t nseg,
+                                     const double* tm_seg, const double* dt_seg,
+                                     const int32_t* seg_idx, const float* ffa_fold,
+                                     int64_t seg_stride, const LokiScoreSpec* spec,
+                                     int32_t* dev_err, void* stream) {
+  int rc = check_prune(lvl);
+  if (rc) return rc;
+  rc = prune_spec_check(spec, lvl->nbins);
+  if (rc) return rc;
+  if (n_cap < 1 || nseg < 1 || !n_dev || !leaves || !folds || !scores || !scores_ep ||
+      !tm_seg || !dt_seg || !seg_idx || !ffa_fold || !dev_err)
+    return set_error(LOKI_ERR_INVALID, "bad ascend arguments");
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, lvl->nbins);
+  const int nb = lvl->nbins;
+  const int smem = kPruneWarps * 32 * (2 * nb + score_stride(nb, sp.wmax)) * (int)sizeof(float);
+  if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for ascend");
+  if (smem > 48 * 1024 && set_smem_limit(prune_ascend_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  int dev = 0, nsm = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune_ascend_kernel,
+                                                    kPruneWarps * 32, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "occupancy query failed");
+  const int64_t need = (n_cap + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  const unsigned blocks = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(need, (int64_t)nsm * std::max(1, occ)));
+  note_launch();
+  prune_ascend_kernel<<<blocks, kPruneWarps * 32, smem, (cudaStream_t)stream>>>(
+      *lvl, leaves, folds, scores, scores_ep, 0, nseg, tm_seg, dt_seg, seg_idx, ffa_fold,
+      seg_stride, sp, SK, n_dev);
+  return check_launch("prune_ascend_dev");
 }
 
 // ---- circular-orbit tree --------------------------------------------------
@@ -2188,7 +2417,7 @@ extern "C" int loki_prune_circ_branch(const LokiPruneLevel* lvl, const double* l
   if (n_parents > 0) {
     note_launch();
     circ_branch_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, s>>>(
-        *lvl, leaves, n_parents, info, keep_off, exp_off, dev_err);
+        *lvl, leaves, n_parents, info, keep_off, exp_off, dev_err, nullptr);
     rc = check_launch("prune_circ_branch");
     if (rc) return rc;
   }
@@ -2213,7 +2442,7 @@ extern "C" int loki_prune_circ_map(const LokiPruneLevel* lvl, const double* leav
   note_launch();
   circ_map_kernel<<<(unsigned)((n_parents + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
       *lvl, leaves, n_parents, batch_size, info, keep_off, exp_off,
-      reinterpret_cast<CircChild*>(child_map), valid_flags);
+      reinterpret_cast<CircChild*>(child_map), valid_flags, nullptr, 0, nullptr, nullptr);
   return check_launch("prune_circ_map");
 }
 
@@ -2261,13 +2490,13 @@ extern "C" int loki_prune_circ_score(const LokiPruneLevel* lvl, const double* le
     circ_score_kernel<<<(unsigned)blocks, kPruneWarps * 32, smem, s>>>(
         *lvl, leaves, folds, batch_size, info, reinterpret_cast<const CircChild*>(child_map),
         valid_ids, n_valid, fold_segment, sp, SK, child_scores, child_idx, child_phase,
-        child_class, batch_taylor, keys);
+        child_class, batch_taylor, keys, nullptr, nullptr, nullptr);
   }
   note_launch();
   minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
   note_launch();
   circ_boff_kernel<<<(unsigned)((n_parents + 1 + 255) / 256), 256, 0, s>>>(
-      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets);
+      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets, nullptr);
   return check_launch("prune_circ_score");
 }
 
@@ -2294,7 +2523,8 @@ extern "C" int loki_prune_circ_emit(const LokiPruneLevel* lvl, const double* lea
   circ_emit_kernel<<<(unsigned)blocks, kPruneWarps * 32, 0, (cudaStream_t)stream>>>(
       *lvl, leaves, folds, batch_size, info, reinterpret_cast<const CircChild*>(child_map),
       valid_ids, fold_segment, surv_ids, n_surv, child_scores, child_idx, child_phase,
-      child_class, batch_taylor, leaves_out, folds_out, scores_out, scores_ep_out, bt_out);
+      child_class, batch_taylor, leaves_out, folds_out, scores_out, scores_ep_out, bt_out,
+      nullptr);
   return check_launch("prune_circ_emit");
 }
 
@@ -2348,7 +2578,7 @@ extern "C" int loki_prune_circ_score_complex(
   minmax_finish_kernel<<<1, 1, 0, s>>>(keys, score_minmax);
   note_launch();
   circ_boff_kernel<<<(unsigned)((n_parents + 1 + 255) / 256), 256, 0, s>>>(
-      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets);
+      keep_off, exp_off, n_parents, valid_ids, n_valid, batch_offsets, nullptr);
   return check_launch("prune_circ_score_complex");
 }
 
@@ -2498,46 +2728,14 @@ namespace loki {
 
 __global__ void run_seed_kernel(int64_t* cnt, int64_t n, unsigned* keys) {
   cnt[0] = n;
-  cnt[1] = 0;
-  cnt[2] = 0;
-  cnt[3] = 0;
+  for (int k = 1; k < 8; ++k) cnt[k] = 0;
   keys[0] = 0xFFFFFFFFu;  // score min / max keys of the first level
   keys[1] = 0u;
 }
 
-// children of the level = offsets[parents]; above the workspace the level
-// gets none and the run is flagged
-__global__ void run_children_kernel(int64_t* cnt, const int64_t* offsets, int64_t child_cap,
-                                    LokiPruneLevelStats* st, int32_t* err) {
-  const int64_t n_par = cnt[0];
-  const int64_t n_child = offsets[n_par];
-  st->n_parents = n_par;
-  st->n_children = n_child;
-  if (n_child > child_cap) {
-    atomicOr(err, LOKI_DEVERR_CAPACITY);
-    cnt[1] = 0;
-  } else {
-    cnt[1] = n_child;
-  }
-}
-
-__global__ void run_survivors_kernel(int64_t* cnt, const int64_t* pos) { cnt[2] = pos[cnt[1]]; }
-
-// level record (score range from the ordered keys, as minmax_finish_kernel);
-// the survivors are the next level's parents, the keys restart
 __global__ void run_level_end_kernel(int64_t* cnt, unsigned* keys, int32_t* ovf_flag,
                                      LokiPruneLevelStats* st) {
-  st->n_surv = cnt[2];
-  const bool none = keys[0] == 0xFFFFFFFFu;  // no finite score
-  st->score_min = none ? 0.0f : key_float(keys[0]);
-  st->score_max = none ? 0.0f : key_float(keys[1]);
-  st->overflow = *ovf_flag;
-  st->reserved = 0;
-  *ovf_flag = 0;
-  keys[0] = 0xFFFFFFFFu;
-  keys[1] = 0u;
-  cnt[3] += cnt[2];  // backtrack history rows
-  cnt[0] = cnt[2];
+  level_end(cnt, keys, ovf_flag, st);
 }
 
 // survivors' backtracks appended to the history at row counts[3]
@@ -2557,6 +2755,62 @@ __global__ void run_bt_copy_kernel(const int32_t* __restrict__ bt, const int64_t
 }
 
 }  // namespace loki
+
+// One circular-orbit level with device counts (counts[4] = valid children):
+// branch (kept and crackle-expanded children per parent), the two scans, the
+// batch-ordered child map, validation compaction, resolve + score, batch
+// offsets of the valid children, selection with the overflow rule, emit.
+static int circ_level_dev(const LokiPruneLevel& D, const LokiPruneTree& in,
+                          const LokiPruneTree& out, const LokiPruneWork& w,
+                          const LokiPruneRun* run, const float* seg, double thr,
+                          const LokiScoreSpec& sp, const ScoreK& SK, int smem, int64_t max_sugg,
+                          int64_t batch, unsigned g_par, unsigned g_flat, unsigned g_score,
+                          unsigned g_emit, int scan_grid, int64_t* cnt, int64_t* pos,
+                          int64_t sums_bytes, unsigned* keys, LokiPruneLevelStats* st,
+                          int32_t* dev_err, cudaStream_t s) {
+  LokiBranchInfo* info = reinterpret_cast<LokiBranchInfo*>(w.info);
+  CircChild* map = reinterpret_cast<CircChild*>(run->child_map);
+  note_launch();
+  circ_branch_kernel<<<g_par, 256, 0, s>>>(D, in.leaves, 0, info, w.offsets, run->exp_off,
+                                           dev_err, cnt);
+  int rc = exclusive_scan_dev<false>(w.offsets, w.par_cap, cnt, 0.0, w.offsets, w.scan,
+                                     w.scan_bytes, scan_grid, s);
+  if (rc) return rc;
+  rc = exclusive_scan_dev<false>(run->exp_off, w.par_cap, cnt, 0.0, run->exp_off, w.scan,
+                                 w.scan_bytes, scan_grid, s);
+  if (rc) return rc;
+  note_launch();
+  circ_map_kernel<<<g_par, 256, 0, s>>>(D, in.leaves, 0, batch, info, w.offsets, run->exp_off,
+                                        map, run->valid_flags, cnt, w.child_cap, st, dev_err);
+  // validation compaction: valid flags are 1.0 / 0.0
+  rc = exclusive_scan_dev<true>(run->valid_flags, w.child_cap, cnt + 1, 0.5, pos, w.sscan,
+                                sums_bytes, scan_grid, s);
+  if (rc) return rc;
+  for (int i = 0; i < 3; ++i) note_launch();
+  select_scatter_kernel<<<g_flat, 256, 0, s>>>(run->valid_flags, 0, 0.5, pos, run->valid_ids,
+                                               cnt + 1);
+  if (cudaMemsetAsync(run->batch_taylor, 0,
+                      (size_t)(w.par_cap / batch + 1) * sizeof(int32_t), s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaMemsetAsync failed");
+  circ_score_kernel<<<g_score, kPruneWarps * 32, smem, s>>>(
+      D, in.leaves, in.folds, batch, info, map, run->valid_ids, 0, seg, sp, SK, w.child_scores,
+      w.child_idx, w.child_phase, run->child_class, run->batch_taylor, keys, cnt, pos, st);
+  circ_boff_kernel<<<g_par, 256, 0, s>>>(w.offsets, run->exp_off, 0, run->valid_ids, 0,
+                                         run->batch_offsets, cnt);
+  rc = exclusive_scan_dev<true>(w.child_scores, w.child_cap, cnt + 4, thr, pos, w.sscan,
+                                sums_bytes, scan_grid, s);
+  if (rc) return rc;
+  for (int i = 0; i < 3; ++i) note_launch();
+  select_scatter_kernel<<<g_flat, 256, 0, s>>>(w.child_scores, 0, thr, pos, w.surv, cnt + 4);
+  select_overflow_kernel<<<1, kSelThreads, 0, s>>>(
+      w.child_scores, run->batch_offsets, 0, batch, thr, max_sugg, w.surv, cnt + 2, w.ovf_thr,
+      w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys), cnt, run->ovf_flag, pos, cnt + 4);
+  circ_emit_kernel<<<g_emit, kPruneWarps * 32, 0, s>>>(
+      D, in.leaves, in.folds, batch, info, map, run->valid_ids, seg, w.surv, 0, w.child_scores,
+      w.child_idx, w.child_phase, run->child_class, run->batch_taylor, out.leaves, out.folds,
+      out.scores, out.scores_ep, out.backtracks, cnt);
+  return LOKI_OK;
+}
 
 extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const float* ffa_folds,
                               int64_t seg_stride, const int32_t* seg_idx,
@@ -2584,8 +2838,12 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
         lvls[l].nbins != lvls[0].nbins)
       return set_error(LOKI_ERR_INVALID, "levels of different trees");
   }
-  if (lvls[0].basis == 2)
-    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree has its own level calls");
+  const bool circ = lvls[0].basis == 2;
+  if (circ && (lvls[0].poly_order != 5 || !run->exp_off || !run->child_map ||
+               !run->valid_flags || !run->valid_ids || !run->child_class ||
+               !run->batch_taylor || !run->batch_offsets))
+    return set_error(LOKI_ERR_INVALID, "the circular-orbit tree needs poly_order 5 and its "
+                                       "workspace");
   int rc = prune_spec_check(spec, lvls[0].nbins);
   if (rc) return rc;
   const int64_t sums_bytes = loki_scan_scratch_bytes(w.child_cap);
@@ -2600,15 +2858,22 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
   const int smem = score_smem_bytes(nb, sp.wmax, kPruneWarps);
   if (smem > 200 * 1024)
     return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
-  if (smem > 48 * 1024 && set_smem_limit(prune_score_kernel, smem) != cudaSuccess)
+  if (smem > 48 * 1024 && (set_smem_limit(prune_score_kernel, smem) != cudaSuccess ||
+                           set_smem_limit(circ_score_kernel, smem) != cudaSuccess))
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0, occ_s = 0, occ_e = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, prune_score_kernel,
-                                                    kPruneWarps * 32, smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, prune_emit_kernel,
-                                                    kPruneWarps * 32, 0) != cudaSuccess)
+      (circ ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, circ_score_kernel,
+                                                            kPruneWarps * 32, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, prune_score_kernel,
+                                                            kPruneWarps * 32, smem)) !=
+          cudaSuccess ||
+      (circ ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, circ_emit_kernel,
+                                                            kPruneWarps * 32, 0)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_e, prune_emit_kernel,
+                                                            kPruneWarps * 32, 0)) !=
+          cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "occupancy query failed");
   // grids: one full wave of the score / emit kernels, and enough blocks for
   // the parent-sized and child-sized passes to stride through
@@ -2631,40 +2896,48 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
     const double thr = thresholds[l - 1];
     LokiPruneLevelStats* st = run->stats + (l - 1);
     LokiBranchInfo* info = reinterpret_cast<LokiBranchInfo*>(w.info);
-    for (int i = 0; i < 3; ++i) note_launch();
+    if (circ) {
+      rc = circ_level_dev(D, in, out, w, run, seg, thr, sp, SK, smem, max_sugg, batch_size,
+                          g_par, g_flat, g_score, g_emit, scan_grid, cnt, pos, sums_bytes, keys,
+                          st, dev_err, s);
+      if (rc) return rc;
+    } else {
+    note_launch();
     prune_branch_kernel<<<g_par, 256, 0, s>>>(D, in.leaves, w.par_cap, info, w.offsets, dev_err,
                                               nullptr, cnt);
     rc = exclusive_scan_dev<false>(w.offsets, w.par_cap, cnt, 0.0, w.offsets, w.scan,
                                    w.scan_bytes, scan_grid, s);
     if (rc) return rc;
-    run_children_kernel<<<1, 1, 0, s>>>(cnt, w.offsets, w.child_cap, st, dev_err);
+    note_launch();
     prune_score_kernel<<<g_score, kPruneWarps * 32, smem, s>>>(
         D, in.leaves, in.folds, 0, info, w.offsets, 0, seg, sp, SK, w.child_scores, w.child_idx,
-        w.child_phase, keys, cnt);
+        w.child_phase, keys, cnt, w.child_cap, st, dev_err);
     rc = exclusive_scan_dev<true>(w.child_scores, w.child_cap, cnt + 1, thr, pos, w.sscan,
                                   sums_bytes, scan_grid, s);
     if (rc) return rc;
-    for (int i = 0; i < 5; ++i) note_launch();
+    for (int i = 0; i < 3; ++i) note_launch();
     select_scatter_kernel<<<g_flat, 256, 0, s>>>(w.child_scores, 0, thr, pos, w.surv, cnt + 1);
-    run_survivors_kernel<<<1, 1, 0, s>>>(cnt, pos);
     select_overflow_kernel<<<1, kSelThreads, 0, s>>>(
         w.child_scores, w.offsets, 0, batch_size, thr, max_sugg, w.surv, cnt + 2, w.ovf_thr,
-        w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys), cnt, run->ovf_flag);
+        w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys), cnt, run->ovf_flag, pos, cnt + 1);
     prune_emit_kernel<<<g_emit, kPruneWarps * 32, 0, s>>>(
         D, in.leaves, in.folds, info, w.offsets, 0, seg, w.surv, 0, w.child_scores, w.child_idx,
         w.child_phase, out.leaves, out.folds, out.scores, out.scores_ep, out.backtracks, cnt);
-    if (run->best_leaves && run->best_scores) {
-      note_launch();
-      prune_best_kernel<<<1, 1024, 0, s>>>(out.scores, 0, out.leaves, row_leaf,
-                                           run->best_leaves + (int64_t)(l - 1) * row_leaf,
-                                           run->best_scores + (l - 1), cnt + 2);
     }
-    if (run->bt_hist) {
+    if (run->bt_hist) {  // before the level end moves the counters on
       note_launch();
       run_bt_copy_kernel<<<g_flat, 256, 0, s>>>(out.backtracks, cnt, row_bt, run->bt_hist,
                                                 run->bt_rows, dev_err);
     }
-    run_level_end_kernel<<<1, 1, 0, s>>>(cnt, keys, run->ovf_flag, st);
+    note_launch();
+    if (run->best_leaves && run->best_scores) {  // best leaf, then the level end
+      prune_best_kernel<<<1, 1024, 0, s>>>(out.scores, 0, out.leaves, row_leaf,
+                                           run->best_leaves + (int64_t)(l - 1) * row_leaf,
+                                           run->best_scores + (l - 1), cnt, keys,
+                                           run->ovf_flag, st);
+    } else {
+      run_level_end_kernel<<<1, 1, 0, s>>>(cnt, keys, run->ovf_flag, st);
+    }
     rc = check_launch("prune_run");
     if (rc) return rc;
   }

@@ -987,10 +987,10 @@ class Pruning:
     # ---- device-resident runs (loki_prune_run) ---------------------------------
     @property
     def device_run_supported(self) -> bool:
-        """``run_device`` covers this configuration: Taylor or Chebyshev basis
-        on time-domain folds, one best leaf per level, no parent hook."""
-        return (not self.circular and not self.fourier and self.intermediate_k == 1
-                and self.parent_hook is None)
+        """``run_device`` covers this configuration: the Taylor, Chebyshev and
+        circular-orbit trees on time-domain folds, one best leaf per level, no
+        parent hook."""
+        return not self.fourier and self.intermediate_k == 1 and self.parent_hook is None
 
     def run_device(self, ref_seg: int, *, graph: bool = False, levels: int | None = None) -> None:
         """Every level of one reference segment with the counts kept on the
@@ -1005,20 +1005,22 @@ class Pruning:
         """
         self._device_finish(self._device_enqueue(ref_seg, graph, levels), graph)
 
-    def _device_enqueue(self, ref_seg: int, graph: bool, levels: int | None = None):
-        """Enqueue a device-resident run on the current stream (no wait)."""
+    def _device_enqueue(self, ref_seg: int, graph: bool, levels: int | None = None,
+                        ascend: bool = False):
+        """Enqueue a device-resident run on the current stream (no wait);
+        with ``ascend`` the run ends with the ascend over its survivors."""
         if not self.device_run_supported:
-            msg = "run_device covers Taylor / Chebyshev time-domain trees without a parent hook"
+            msg = "run_device covers time-domain trees without a parent hook"
             raise ValueError(msg)
         self._stream_ptr = None  # the current stream
         nlev = self.dyp.nsegments - 1 if levels is None else int(levels)
         if not 0 <= nlev <= self.dyp.nsegments - 1:
             msg = f"levels must be in [0, {self.dyp.nsegments - 1}], got {levels}"
             raise ValueError(msg)
-        key = (ref_seg, nlev)
+        key = (ref_seg, nlev, ascend)
         dr = self.__dict__.setdefault("_device_runs", {}).get(key)
         if dr is None:
-            dr = _DeviceRun(self, ref_seg, nlev)
+            dr = _DeviceRun(self, ref_seg, nlev, ascend=ascend)
             self.__dict__.setdefault("_device_runs", {})[key] = dr
         dr.launch(graph)
         return dr
@@ -1027,25 +1029,24 @@ class Pruning:
         """Read an enqueued run back; repeat it with grown workspaces if it
         outgrew them."""
         while not dr.finish(self):
-            key = (dr.ref_seg, dr.nlev)
-            dr = _DeviceRun(self, dr.ref_seg, dr.nlev, grow=dr)
+            key = (dr.ref_seg, dr.nlev, dr.ascend)
+            dr = _DeviceRun(self, dr.ref_seg, dr.nlev, grow=dr, ascend=dr.ascend)
             self.__dict__.setdefault("_device_runs", {})[key] = dr
             dr.launch(graph)
+        return dr
 
     # ---- ascend (prune.py:671-693, dyn_poly_taylor.py:587-628) -----------------
-    def _do_ascend(self) -> None:
-        if self.prune_complete or self.world_tree.valid_size == 0:
-            return
+    def _ascend_tables(self, level: int):
+        """Level descriptor and per-segment tables of the ascend after
+        ``level`` (they depend only on the reference segment and the level)."""
         sc = self.scheme
         P = self.poly_order
-        coord_end = sc.get_previous_coord(self.prune_level + 1, self.use_moving_grid)
-        seg_idx, seg_coords = sc.get_segment_coords_so_far(self.prune_level)
+        coord_end = sc.get_previous_coord(level + 1, self.use_moving_grid)
+        seg_idx, seg_coords = sc.get_segment_coords_so_far(level)
         nseg = len(seg_idx)
         cheby = self.poly_basis == "chebyshev"
         dev = self._device
-        # the tables depend only on the reference segment and the level
-        key = ("ascend", sc.ref_idx, self.prune_level, self.poly_basis, self.use_moving_grid,
-               str(dev))
+        key = ("ascend", sc.ref_idx, level, self.poly_basis, self.use_moving_grid, str(dev))
         cache = self.__dict__.setdefault("_desc_cache", {})
         if key not in cache:
             dts = seg_coords[:, 0] - coord_end[0]
@@ -1060,14 +1061,20 @@ class Pruning:
                           torch.from_numpy(np.ascontiguousarray(dts, np.float64)).to(dev),
                           torch.from_numpy(seg_idx.astype(np.int32)).to(dev))
         tm_d, dt_d, si_d = cache[key]
-        fold = self.dyp.fold
-        stride = int(np.prod(fold.shape[1:]))
         dkey = ("ascend_desc",) + key[1:]
         if dkey not in cache:
-            cache[dkey] = self._level_desc(self.prune_level)
-        d = _lib.LokiPruneLevel.from_buffer_copy(cache[dkey])  # a copy: modified below
-        if cheby:
-            self._cheby_scale(d, coord_end[1])
+            d = _lib.LokiPruneLevel.from_buffer_copy(self._level_desc(level))
+            if cheby:
+                self._cheby_scale(d, coord_end[1])
+            cache[dkey] = d
+        return cache[dkey], tm_d, dt_d, si_d, nseg
+
+    def _do_ascend(self) -> None:
+        if self.prune_complete or self.world_tree.valid_size == 0:
+            return
+        d, tm_d, dt_d, si_d, nseg = self._ascend_tables(self.prune_level)
+        fold = self.dyp.fold
+        stride = int(np.prod(fold.shape[1:]))
         wt = self.world_tree
         ascend_fn = (self._lib.loki_prune_ascend_complex if self.fourier
                      else self._lib.loki_prune_ascend)
@@ -1080,7 +1087,9 @@ class Pruning:
 
     # ---- report (core/taylor.py:342-360, dyn_poly_cheby.py:824-840) ------------
     def report(self) -> np.ndarray:
-        leaves = self.world_tree.leaves.cpu().numpy()
+        return self._report_host(self.world_tree.leaves.cpu().numpy())
+
+    def _report_host(self, leaves: np.ndarray) -> np.ndarray:
         if self.poly_basis == "chebyshev":
             # The reference's fixed-grid branch computes a shift to the report
             # domain and discards it, so both grids report the leaves as held.
@@ -1160,6 +1169,7 @@ class _DeviceBuffers:
         lib = prn._lib
         t64, t32, f32, f64, u8 = torch.int64, torch.int32, torch.float32, torch.float64, torch.uint8
         self.child_cap, self.bt_rows = child_cap, bt_rows
+        self.host: dict = {}  # pinned readback buffers, grown on demand
         self.trees = [{"leaves": torch.empty((cap, P + 2, 2), dtype=f64, device=dev),
                        "folds": torch.empty((cap, 2, nb), dtype=f32, device=dev),
                        "scores": torch.empty(cap, dtype=f32, device=dev),
@@ -1181,7 +1191,7 @@ class _DeviceBuffers:
             "ovf_ids": torch.empty(ovf_cap, dtype=t64, device=dev),
             "ovf_keys": torch.empty(ovf_cap, dtype=f32, device=dev),
             "ovf_thr": torch.empty(1, dtype=f64, device=dev),
-            "counts": torch.zeros(4, dtype=t64, device=dev),
+            "counts": torch.zeros(8, dtype=t64, device=dev),
             "ovf_flag": torch.zeros(1, dtype=t32, device=dev),
             "stats": torch.zeros(nlev * _lib.PRUNE_STATS_DTYPE.itemsize, dtype=u8, device=dev),
             "best_leaves": torch.zeros((nlev, P + 2, 2), dtype=f64, device=dev),
@@ -1212,6 +1222,20 @@ class _DeviceBuffers:
                                          m["stats"].data_ptr())
         r.best_leaves, r.best_scores = m["best_leaves"].data_ptr(), m["best_scores"].data_ptr()
         r.bt_hist, r.bt_rows = m["bt_hist"].data_ptr(), bt_rows
+        if prn.circular:  # the circular tree's own child bookkeeping
+            nbatch = cap // max(1, prn.batch_size) + 1
+            m.update({
+                "exp_off": torch.empty(cap + 1, dtype=t64, device=dev),
+                "cmap": torch.empty(child_cap * _lib.CIRC_CHILD_BYTES, dtype=u8, device=dev),
+                "validf": torch.empty(child_cap, dtype=f32, device=dev),
+                "valid": torch.empty(child_cap, dtype=t64, device=dev),
+                "ccls": torch.empty(child_cap, dtype=torch.int8, device=dev),
+                "btay": torch.empty(nbatch, dtype=t32, device=dev),
+                "boff": torch.empty(cap + 1, dtype=t64, device=dev)})
+            r.exp_off, r.child_map = m["exp_off"].data_ptr(), m["cmap"].data_ptr()
+            r.valid_flags, r.valid_ids = m["validf"].data_ptr(), m["valid"].data_ptr()
+            r.child_class, r.batch_taylor = m["ccls"].data_ptr(), m["btay"].data_ptr()
+            r.batch_offsets = m["boff"].data_ptr()
         self.run = r
 
 
@@ -1221,7 +1245,7 @@ class _DeviceRun:
     start of every run) and, once captured, the run's CUDA graph."""
 
     def __init__(self, prn: Pruning, ref_seg: int, nlev: int,
-                 grow: _DeviceRun | None = None) -> None:
+                 grow: _DeviceRun | None = None, ascend: bool = False) -> None:
         dyp = prn.dyp
         nseg = dyp.nsegments
         self.nlev = nlev
@@ -1251,6 +1275,8 @@ class _DeviceRun:
         self.seg_idx = np.ascontiguousarray(
             [self.scheme.get_segment_idx(lvl) for lvl in range(1, self.nlev + 1)], np.int32)
         self.thresholds = np.ascontiguousarray(prn.threshold_scheme[: self.nlev], np.float64)
+        self.ascend = bool(ascend) and self.nlev > 0
+        self.asc = prn._ascend_tables(self.nlev) if self.ascend else None
         self.prn = prn
         self.graph = None
         self.need_child = self.need_bt = 0
@@ -1279,6 +1305,14 @@ class _DeviceRun:
             self.descs, self.nlev, _lib.ptr(mirror), stride, self.seg_idx.ctypes.data,
             self.thresholds.ctypes.data, prn.spec, n, prn.max_sugg, prn.batch_size,
             C.byref(b.run), _lib.ptr(prn._err), prn._stream()))
+        if self.ascend:  # survivors of the last level: counts[0] after the run
+            d, tm_d, dt_d, si_d, nseg = self.asc
+            t = b.trees[self.nlev & 1]
+            _lib.check(prn._lib.loki_prune_ascend_dev(
+                d, _lib.ptr(t["leaves"]), _lib.ptr(t["folds"]), _lib.ptr(t["scores"]),
+                _lib.ptr(t["scores_ep"]), _lib.ptr(b.mem["counts"]), prn.max_sugg, nseg,
+                _lib.ptr(tm_d), _lib.ptr(dt_d), _lib.ptr(si_d), _lib.ptr(mirror), stride,
+                prn.spec, _lib.ptr(prn._err), prn._stream()))
 
     def launch(self, graph: bool) -> None:
         fold = self.prn.dyp.fold.reshape(-1)
@@ -1300,6 +1334,71 @@ class _DeviceRun:
             self.prn._stream_ptr = _lib.stream_ptr(cur)
             self.graph = g
         self.graph.replay()
+
+    def _pinned(self, name: str, numel: int, dtype) -> torch.Tensor:
+        """Grow-only pinned host buffer of the run's buffers."""
+        b = self.bufs
+        t = b.host.get(name)
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = b.host[name] = torch.empty(max(numel, 1), dtype=dtype, pin_memory=True)
+        return t[:numel]
+
+    def copy_stats_async(self) -> None:
+        """Enqueue the copies of the level records, error word and seed
+        scores to pinned host memory on the current stream."""
+        prn, b = self.prn, self.bufs
+        nbytes = self.nlev * _lib.PRUNE_STATS_DTYPE.itemsize
+        self._h_stats = self._pinned("stats", nbytes, torch.uint8)
+        self._h_stats.copy_(b.mem["stats"][:nbytes], non_blocking=True)
+        self._h_err = self._pinned("err", 1, torch.int32)
+        self._h_err.copy_(prn._err, non_blocking=True)
+        self._h_seed = self._pinned("seed", self.seed.size, torch.float32)
+        self._h_seed.copy_(b.mem["seed_scores"][: self.seed.size], non_blocking=True)
+
+    def stats_host(self):
+        """(level records, error word, last level, survivors of it) from the
+        pinned copies (after the stream has been waited on)."""
+        stats = self._h_stats.numpy().view(_lib.PRUNE_STATS_DTYPE)
+        err = int(self._h_err[0])
+        last, n_final = 0, self.seed.size
+        for lvl in range(1, self.nlev + 1):
+            last = lvl
+            n_final = int(stats[lvl - 1]["n_surv"])
+            if n_final == 0:
+                break
+        return stats, err, last, n_final
+
+    def copy_tree_async(self, n: int) -> None:
+        """Enqueue the copies of the final tree's first n rows (leaves, scores,
+        scores_ep) to pinned host memory on the current stream."""
+        t = self.bufs.trees[self.nlev & 1]
+        P = self.prn.poly_order
+        self._h_leaves = self._pinned("leaves", n * (P + 2) * 2, torch.float64)
+        self._h_leaves.copy_(t["leaves"][:n].reshape(-1), non_blocking=True)
+        self._h_scores = self._pinned("scores", n, torch.float32)
+        self._h_scores.copy_(t["scores"][:n], non_blocking=True)
+        self._h_scores_ep = self._pinned("scores_ep", n, torch.float32)
+        self._h_scores_ep.copy_(t["scores_ep"][:n], non_blocking=True)
+
+    def level_stats(self, stats, last: int) -> list[PruneStats]:
+        sc, seed = self.scheme, self.seed
+        s0 = self._h_seed.numpy()
+        out = [PruneStats(level=0, seg_idx=sc.get_segment_idx(0), threshold=0,
+                          score_min=float(s0.min()) if seed.size else 0.0,
+                          score_max=float(s0.max()) if seed.size else 0.0,
+                          n_branches=seed.size, n_leaves=seed.size, n_leaves_phy=seed.size,
+                          n_leaves_surv=seed.size)]
+        for lvl in range(1, last + 1):
+            r = stats[lvl - 1]
+            n_child = int(r["n_children"])
+            out.append(PruneStats(
+                level=lvl, seg_idx=int(self.seg_idx[lvl - 1]),
+                threshold=float(self.thresholds[lvl - 1]),
+                score_min=float(r["score_min"]) if n_child else 0.0,
+                score_max=float(r["score_max"]) if n_child else 0.0,
+                n_branches=int(r["n_parents"]), n_leaves=n_child,
+                n_leaves_phy=int(r["n_valid"]), n_leaves_surv=int(r["n_surv"])))
+        return out
 
     def finish(self, prn: Pruning) -> bool:
         """Read the run back (one wait) and set ``prn``'s state; False when a
@@ -1336,8 +1435,8 @@ class _DeviceRun:
                 threshold=float(self.thresholds[lvl - 1]),
                 score_min=float(r["score_min"]) if n_child else 0.0,
                 score_max=float(r["score_max"]) if n_child else 0.0,
-                n_branches=int(r["n_parents"]), n_leaves=n_child, n_leaves_phy=n_child,
-                n_leaves_surv=n_surv))
+                n_branches=int(r["n_parents"]), n_leaves=n_child,
+                n_leaves_phy=int(r["n_valid"]), n_leaves_surv=n_surv))
             last = lvl
             if n_surv == 0:
                 break
@@ -1506,21 +1605,35 @@ class PruneBatch:
                 st.wait_stream(producer)
                 with torch.cuda.stream(st):
                     prn = self._pruning(k, dyp)
-                    started.append((k, prn, prn._device_enqueue(ref, self.graph)))
+                    dr = prn._device_enqueue(ref, self.graph, ascend=ascend)
+                    dr.copy_stats_async()
+                started.append((k, prn, dr))
+            # one wait per run for its records, then the surviving rows
+            ready = []
             for k, prn, dr in started:
-                with torch.cuda.stream(self._streams[k]):
-                    prn._device_finish(dr, self.graph)
-                    self._bufs[k] = prn._device_bufs
-                    if ascend:
-                        prn._do_ascend()
-            for k, prn, dr in started:
-                with torch.cuda.stream(self._streams[k]):
-                    out[r0 + k] = {
-                        "run_name": f"{dr.ref_seg:03d}_00", "scheme": prn.scheme.data.copy(),
-                        "param_sets": prn.report(),
-                        "scores": prn.world_tree.scores.cpu().numpy(),
-                        "scores_ep": prn.world_tree.scores_ep.cpu().numpy(),
-                        "level_stats": prn.pstats}
+                st = self._streams[k]
+                st.synchronize()
+                stats, err, last, n = dr.stats_host()
+                with torch.cuda.stream(st):
+                    if err:  # a workspace to grow, or a device error to raise
+                        dr = prn._device_finish(dr, self.graph)
+                        dr.copy_stats_async()
+                        st.synchronize()
+                        stats, err, last, n = dr.stats_host()
+                    dr.copy_tree_async(n)
+                self._bufs[k] = prn._device_bufs
+                ready.append((k, prn, dr, stats, last, n))
+            P = ready[0][1].poly_order
+            for k, prn, dr, stats, last, n in ready:
+                self._streams[k].synchronize()
+                prn._scheme = dr.scheme
+                leaves = dr._h_leaves.numpy().reshape(n, P + 2, 2).copy()
+                out[r0 + k] = {
+                    "run_name": f"{dr.ref_seg:03d}_00", "scheme": dr.scheme.data.copy(),
+                    "param_sets": prn._report_host(leaves),
+                    "scores": dr._h_scores.numpy().copy(),
+                    "scores_ep": dr._h_scores_ep.numpy().copy(),
+                    "level_stats": dr.level_stats(stats, last)}
         for st in self._streams[:ns]:
             producer.wait_stream(st)
         return out

@@ -499,6 +499,82 @@ def schemes_case() -> None:
     np.savez_compressed(HERE / "schemes_backtrack.npz", **out)
 
 
+def prune_large_case(basis: str = "chebyshev") -> None:
+    """One full run of the benchmark pruning workload (2^22 samples, 128
+    segments, Taylor grid to the 4th derivative, reference segment 64, the
+    designed thresholds) with the given basis, by the reference's own
+    Pruning. The FFA fold comes from the C oracle (bit-exact to the
+    reference's DynamicProgramming on the FFA fixtures), because the shimmed
+    FFA would take hours at this size; the series is regenerated from its
+    seed by bench.make_prune_series. Recorded: every level's statistics,
+    the surviving scores after the last level, the ascend and the report."""
+    import time
+
+    sys.path.insert(0, str(HERE.parents[1]))
+    import bench
+    from oracle import oracle as O
+    from pyloki.config import ParamLimits, PulsarSearchConfig
+    from pyloki.ffa import DynamicProgramming
+    from pyloki.io.timeseries import TimeSeries
+    from pyloki.prune import Pruning
+
+    ours = bench.make_prune_cfg()
+    n = ours.nsamps
+    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=4).limits
+    cfg = PulsarSearchConfig(nsamps=n, tsamp=ours.tsamp, nbins=ours.nbins, eta=ours.eta,
+                             param_limits=lim, use_fourier=False, bseg_ffa=n // 128,
+                             prune_poly_order=4)
+    ts, _ = bench.make_prune_series(seed=2000)
+    fold = O.ffa_execute(ts.ts_e, ts.ts_v, ours)
+    dyp = DynamicProgramming(TimeSeries(ts.ts_e, ts.ts_v, ours.tsamp), cfg)
+    lvl = cfg.niters_ffa
+    dparams = cfg.get_dparams(lvl)
+    dyp._ffa_level = lvl
+    dyp._param_arr = cfg.get_param_arr(dparams)
+    dyp._param_grid_count = cfg.get_param_grid_count(lvl)
+    dyp._dparams = dparams
+    dyp._dparams_actual = cfg.get_dparams_actual(lvl)
+    dyp._tseg = cfg.tseg_ffa
+    dyp._fold = fold.reshape(fold.shape[0], *dyp._param_grid_count.tolist(), 2, cfg.nbins)
+    thr = bench.prune_thresholds(dyp.nsegments)
+    prn = Pruning(dyp, thr, max_sugg=bench.PRUNE_MAX_SUGG, batch_size=bench.PRUNE_BATCH,
+                  poly_basis=basis)
+    ref = dyp.nsegments // 2
+    log = Path("/tmp") / f"prune_large_{basis}_log.txt"
+    log.write_text("")
+    prn.initialize(ref, log)
+    out = {"basis": np.str_(basis), "ref_seg": np.int64(ref), "seed": np.int64(2000),
+           "thresholds": thr}
+    t0 = time.time()
+    stats = []
+    for level in range(1, dyp.nsegments):
+        prn.execute_iter(log)
+        st = prn.pstats.stats_list[-1]
+        stats.append([st.n_branches, st.n_leaves, st.n_leaves_phy, st.n_leaves_surv])
+        out[f"smm_{level}"] = np.array([st.score_min, st.score_max], np.float64)
+        if level % 8 == 0:
+            print(basis, "level", level, stats[-1], f"{time.time() - t0:.0f} s", flush=True)
+        if prn.prune_complete:
+            break
+    out["stats"] = np.array(stats, np.int64)
+    out["levels_done"] = np.int64(prn.prune_level)
+    wt = prn.world_tree
+    v = wt.valid_size
+    out["scores_last"] = wt.scores[:v].copy()
+    bt = wt.backtracks[:v]
+    out["bt_last"] = np.concatenate([bt[:, : cfg.nparams + 1], bt[:, -1:]], axis=1).copy()
+    prn._do_ascend()
+    wt = prn.world_tree
+    out["asc_scores"] = wt.scores[:v].copy()
+    out["asc_scores_ep"] = wt.scores_ep[:v].copy()
+    coord_end = prn.scheme.get_previous_coord(prn.prune_level + 1, prn.use_moving_grid)
+    coord_report = prn.scheme.get_report_coord(prn.use_moving_grid)
+    out["report"] = prn.prune_funcs.report(wt.leaves[:v].copy(), coord_report, coord_end)
+    np.savez_compressed(HERE / f"prune_large_{basis}.npz", **out)
+    print("prune_large", basis, "levels", prn.prune_level, "survivors", v,
+          "leaves", int(out["stats"][:, 1].sum()), f"{time.time() - t0:.0f} s")
+
+
 def scorer_cases() -> None:
     scorer_case("scorers_nb64", 64, 48, 31, 4)
     scorer_case("scorers_nb50", 50, 36, 32, 5)
@@ -601,6 +677,9 @@ def main() -> None:
         scoring_case("score_nb100", 100, 128, 0.3, 1.3, 13)
     if "--cheby-only" in sys.argv:
         cheby_cases()
+        return
+    if "--cheby-large" in sys.argv:
+        prune_large_case("chebyshev")
         return
     if "--circ-only" in sys.argv:
         circ_cases()

@@ -18,10 +18,12 @@ from tests.test_prune_gpu import _leaves_close, _run
 pytestmark = pytest.mark.gpu
 CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
          "prune_taylor_overflow", "prune_cheby", "prune_cheby_fixed", "prune_cheby_cons",
-         "prune_cheby_quad"]
+         "prune_cheby_quad", "prune_circ", "prune_circ_b4", "prune_circ_quad",
+         "prune_circ_fixed"]
 
 
 def _check_against_fixture(d, prn, levels):
+    circ = int(d["poly_order"]) == 5
     for lvl in range(1, levels + 1):
         if lvl >= len(prn.pstats):
             break
@@ -36,7 +38,7 @@ def _check_against_fixture(d, prn, levels):
     wt = prn.world_tree
     np.testing.assert_array_equal(wt.scores.cpu().numpy(), d[f"scores_{last}"])
     if f"leaves_{last}" in d:
-        _leaves_close(wt.leaves.cpu().numpy(), d[f"leaves_{last}"], "final leaves")
+        _leaves_close(wt.leaves.cpu().numpy(), d[f"leaves_{last}"], "final leaves", circ)
     if f"folds_{last}" in d:
         np.testing.assert_array_equal(wt.folds.cpu().numpy(), d[f"folds_{last}"])
     prn._do_ascend()
@@ -45,6 +47,8 @@ def _check_against_fixture(d, prn, levels):
     np.testing.assert_array_equal(wt.scores_ep.cpu().numpy(), d["asc_scores_ep"])
     if "asc_folds" in d:
         np.testing.assert_array_equal(wt.folds.cpu().numpy(), d["asc_folds"])
+        _leaves_close(wt.leaves.cpu().numpy(), d["final_leaves"], "ascended leaves", circ)
+        _leaves_close(prn.report(), d["report"], "report", circ)
 
 
 @pytest.mark.parametrize("graph", [False, True])
@@ -59,7 +63,8 @@ def test_device_run_matches_reference(cuda_device, name, graph):
         _check_against_fixture(d, prn, levels)
 
 
-@pytest.mark.parametrize("name", ["prune_taylor", "prune_taylor_overflow", "prune_cheby"])
+@pytest.mark.parametrize("name", ["prune_taylor", "prune_taylor_overflow", "prune_cheby",
+                                  "prune_circ", "prune_circ_b4"])
 def test_device_run_matches_level_path(cuda_device, name):
     """Backtrack history, per-level best leaves and statistics equal the
     level-by-level path's."""
@@ -88,10 +93,11 @@ def test_device_run_matches_level_path(cuda_device, name):
     np.testing.assert_array_equal(prn.world_tree.leaves.cpu().numpy(), want_tree)
 
 
-def test_device_run_grows_its_workspace(cuda_device):
+@pytest.mark.parametrize("name", ["prune_taylor", "prune_circ"])
+def test_device_run_grows_its_workspace(cuda_device, name):
     """A child workspace that is too small is detected on the device, grown
     and the run repeated: the results do not change."""
-    d, prn = _run("prune_taylor", cuda_device)
+    d, prn = _run(name, cuda_device)
     levels = int(d["levels_done"])
     ref = int(d["ref_seg"])
     prn.device_child_cap = 64
@@ -102,10 +108,19 @@ def test_device_run_grows_its_workspace(cuda_device):
 
 
 def test_device_run_rejects_unsupported(cuda_device):
+    """A parent hook or more than one best leaf per level stays on the
+    level-by-level path."""
+    from pyloki_gb300.prune import Pruning
+
     d, prn = _run("prune_circ", cuda_device)
+    assert prn.device_run_supported
+    prn.parent_hook = lambda p, tree, level: None
     assert not prn.device_run_supported
     with pytest.raises(ValueError):
         prn.run_device(int(d["ref_seg"]))
+    p2 = Pruning(prn.dyp, d["thresholds"], max_sugg=int(d["max_sugg"]),
+                 batch_size=int(d["batch_size"]), intermediate_k=2)
+    assert not p2.device_run_supported
 
 
 @pytest.mark.parametrize("n_streams", [1, 3])

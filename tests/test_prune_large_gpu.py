@@ -66,3 +66,52 @@ def test_prune_taylor4_circular_matches_oracle(cuda_device):
     run.ascend()
     np.testing.assert_array_equal(prn.world_tree.scores.cpu().numpy(), run.scores)
     np.testing.assert_array_equal(prn.world_tree.folds.cpu().numpy(), run.folds)
+
+
+@pytest.mark.parametrize("device_run", [False, True])
+def test_prune_chebyshev_full_size_matches_reference(cuda_device, device_run):
+    """The same workload with the Chebyshev basis against a full run of the
+    reference's own Pruning (tests/golden/prune_large_chebyshev.npz, made by
+    make_fixtures.py --cheby-large from the C oracle's FFA fold of the same
+    seeded series): every level's statistics and score range, the surviving
+    scores and backtracks after the last level, the ascend and the report."""
+    import bench
+    from conftest import load_golden
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import Pruning
+
+    d = load_golden("prune_large_chebyshev")
+    cfg = bench.make_prune_cfg()
+    ts, _ = bench.make_prune_series(seed=int(d["seed"]))
+    dyp = DynamicProgramming(ts, cfg, device=cuda_device)
+    dyp.initialize()
+    dyp.execute()
+    prn = Pruning(dyp, d["thresholds"], max_sugg=bench.PRUNE_MAX_SUGG,
+                  batch_size=bench.PRUNE_BATCH, poly_basis="chebyshev")
+    ref = int(d["ref_seg"])
+    levels = int(d["levels_done"])
+    if device_run:
+        prn.run_device(ref, graph=True, levels=levels)
+    else:
+        prn.initialize(ref)
+        for _ in range(levels):
+            prn.execute_iter()
+    got = np.array([[s.n_branches, s.n_leaves, s.n_leaves_phy, s.n_leaves_surv]
+                    for s in prn.pstats[1:]], np.int64)
+    np.testing.assert_array_equal(got, d["stats"])
+    for lvl in range(1, levels + 1):
+        st = prn.pstats[lvl]
+        np.testing.assert_array_equal([st.score_min, st.score_max],
+                                      d[f"smm_{lvl}"].astype(np.float32).astype(np.float64),
+                                      err_msg=f"score range level {lvl}")
+    wt = prn.world_tree
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["scores_last"])
+    nparams = cfg.nparams
+    bt = wt.backtracks.cpu().numpy()
+    np.testing.assert_array_equal(np.concatenate([bt[:, : nparams + 1], bt[:, -1:]], axis=1),
+                                  d["bt_last"])
+    prn._do_ascend()
+    wt = prn.world_tree
+    np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["asc_scores"])
+    np.testing.assert_array_equal(wt.scores_ep.cpu().numpy(), d["asc_scores_ep"])
+    np.testing.assert_allclose(prn.report(), d["report"], rtol=1e-13, atol=0)
