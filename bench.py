@@ -95,16 +95,19 @@ PRUNE_SCHEME_NOTE = "designed (DynamicThresholdScheme, least-cost path at 90% of
 PRUNE_SCORE_BYTES_PER_LEAF = 2 * 64 * 4 + 4 + 8 + 8
 
 
-def make_prune_cfg():
+def make_prune_cfg(circular: bool = False):
     """Circular-orbit search with a Taylor tree to the 4th derivative: 2^22
-    samples at 64 us, 128 segments, 64 bins, FFA grid (1, 1, 1, 146)."""
+    samples at 64 us, 128 segments, 64 bins, FFA grid (1, 1, 1, 146). With
+    ``circular``, the circular-orbit tree of order 5 on the same series (FFA
+    grid (1, 1, 1, 1, 146), P_orb_min 2 h)."""
     from pyloki_gb300 import ParamLimits, PulsarSearchConfig
 
     n = 2**22
-    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=4)
+    order = 5 if circular else 4
+    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=order)
     return PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
                               param_limits=lim.limits, use_fourier=False, bseg_ffa=n // 128,
-                              prune_poly_order=4)
+                              prune_poly_order=order, p_orb_min=7200.0 if circular else 0.0)
 
 
 def make_prune_series(seed: int):

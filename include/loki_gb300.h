@@ -111,6 +111,15 @@ int loki_brutefold(const float* ts_e, const float* ts_v, int64_t nsamps,
                    void* phase_scratch, int64_t scratch_bytes,
                    float* fold_out, void* stream);
 
+/* Scratch bytes with which loki_brutefold / loki_brutefold_unit_variance fold
+ * all nfreqs frequencies in one pass. With nbins <= 256 that is the phase
+ * map plus the chain layout (per frequency: segment_len bytes of map, then
+ * per 512-sample time chunk the chunk's positions sorted by bin, 1 KiB, and
+ * the bin starts); a smaller scratch folds in frequency chunks, and one too
+ * small for a single frequency of the chain layout uses the map alone. No
+ * reference counterpart. */
+int64_t loki_brutefold_scratch_bytes(int64_t nfreqs, int64_t segment_len, int32_t nbins);
+
 /* loki_brutefold for a series whose ts_v is all ones (the normalised series
  * io/timeseries.py:198-236 from_tim produces). Every variance sum of the
  * reference is then the bin's sample count, exact in float32, and the same

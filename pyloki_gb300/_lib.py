@@ -218,6 +218,7 @@ SIGNATURES: dict[str, tuple] = {
                                                 _I64, _P, _P]),
     "loki_brutefold_noalloc": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
     "loki_brutefold_noalloc_scratch_bytes": (C.c_int64, []),
+    "loki_brutefold_scratch_bytes": (C.c_int64, [_I64, _I64, _I32]),
     "loki_ffa_plan": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P]),
     "loki_ffa_level": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
     "loki_ffa_level_score": (C.c_int, [C.POINTER(LokiFFALevel), _P, C.POINTER(LokiScoreSpec),

@@ -649,15 +649,16 @@ def brutefold(ts_e: torch.Tensor, ts_v: torch.Tensor, freqs: torch.Tensor, segme
               nbins: int, tsamp: float, t_ref: float = 0.0, *,
               scratch_bytes: int = _GIB, unit_variance: bool = False) -> torch.Tensor:
     """Fold ``(nsegments, nfreqs, 2, nbins)`` (``core/fold.py:108-171``).
-    ``scratch_bytes`` bounds the phase map; frequencies beyond it are folded
-    in chunks. ``unit_variance``: the caller asserts ``ts_v`` is all ones,
-    and the variance sums come from sample counts (the same values)."""
+    ``scratch_bytes`` bounds the phase map and chain layout; frequencies
+    beyond it are folded in chunks. ``unit_variance``: the caller asserts
+    ``ts_v`` is all ones, and the variance sums come from sample counts (the
+    same values)."""
     lib = _lib.load()
     nsamps = ts_e.numel()
     nseg = math.ceil(nsamps / segment_len)
     nfreq = freqs.numel()
     elem = 1 if nbins <= 256 else 2
-    need = nfreq * segment_len * elem
+    need = int(lib.loki_brutefold_scratch_bytes(nfreq, segment_len, nbins))
     scratch = torch.empty(min(need, max(scratch_bytes, segment_len * elem)),
                           dtype=torch.uint8, device=ts_e.device)
     fold = torch.empty((nseg, nfreq, 2, nbins), dtype=torch.float32, device=ts_e.device)

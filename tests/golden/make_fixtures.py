@@ -499,11 +499,12 @@ def schemes_case() -> None:
     np.savez_compressed(HERE / "schemes_backtrack.npz", **out)
 
 
-def prune_large_case(basis: str = "chebyshev") -> None:
+def prune_large_case(basis: str = "chebyshev", circular: bool = False) -> None:
     """One full run of the benchmark pruning workload (2^22 samples, 128
     segments, Taylor grid to the 4th derivative, reference segment 64, the
     designed thresholds) with the given basis, by the reference's own
-    Pruning. The FFA fold comes from the C oracle (bit-exact to the
+    Pruning; with ``circular``, the circular-orbit tree of order 5 (crackle
+    added, FFA limits from_circular(poly_order=5), P_orb_min 2 h) instead. The FFA fold comes from the C oracle (bit-exact to the
     reference's DynamicProgramming on the FFA fixtures), because the shimmed
     FFA would take hours at this size; the series is regenerated from its
     seed by bench.make_prune_series. Recorded: every level's statistics,
@@ -518,12 +519,15 @@ def prune_large_case(basis: str = "chebyshev") -> None:
     from pyloki.io.timeseries import TimeSeries
     from pyloki.prune import Pruning
 
-    ours = bench.make_prune_cfg()
+    ours = bench.make_prune_cfg(circular=circular)
     n = ours.nsamps
-    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=4).limits
+    order = 5 if circular else 4
+    p_orb_min = 7200.0 if circular else 0.0
+    lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=order).limits
     cfg = PulsarSearchConfig(nsamps=n, tsamp=ours.tsamp, nbins=ours.nbins, eta=ours.eta,
                              param_limits=lim, use_fourier=False, bseg_ffa=n // 128,
-                             prune_poly_order=4)
+                             prune_poly_order=order, p_orb_min=p_orb_min)
+    name = "circular" if circular else basis
     ts, _ = bench.make_prune_series(seed=2000)
     fold = O.ffa_execute(ts.ts_e, ts.ts_v, ours)
     dyp = DynamicProgramming(TimeSeries(ts.ts_e, ts.ts_v, ours.tsamp), cfg)
@@ -540,7 +544,7 @@ def prune_large_case(basis: str = "chebyshev") -> None:
     prn = Pruning(dyp, thr, max_sugg=bench.PRUNE_MAX_SUGG, batch_size=bench.PRUNE_BATCH,
                   poly_basis=basis)
     ref = dyp.nsegments // 2
-    log = Path("/tmp") / f"prune_large_{basis}_log.txt"
+    log = Path("/tmp") / f"prune_large_{name}_log.txt"
     log.write_text("")
     prn.initialize(ref, log)
     out = {"basis": np.str_(basis), "ref_seg": np.int64(ref), "seed": np.int64(2000),
@@ -553,7 +557,7 @@ def prune_large_case(basis: str = "chebyshev") -> None:
         stats.append([st.n_branches, st.n_leaves, st.n_leaves_phy, st.n_leaves_surv])
         out[f"smm_{level}"] = np.array([st.score_min, st.score_max], np.float64)
         if level % 8 == 0:
-            print(basis, "level", level, stats[-1], f"{time.time() - t0:.0f} s", flush=True)
+            print(name, "level", level, stats[-1], f"{time.time() - t0:.0f} s", flush=True)
         if prn.prune_complete:
             break
     out["stats"] = np.array(stats, np.int64)
@@ -570,8 +574,8 @@ def prune_large_case(basis: str = "chebyshev") -> None:
     coord_end = prn.scheme.get_previous_coord(prn.prune_level + 1, prn.use_moving_grid)
     coord_report = prn.scheme.get_report_coord(prn.use_moving_grid)
     out["report"] = prn.prune_funcs.report(wt.leaves[:v].copy(), coord_report, coord_end)
-    np.savez_compressed(HERE / f"prune_large_{basis}.npz", **out)
-    print("prune_large", basis, "levels", prn.prune_level, "survivors", v,
+    np.savez_compressed(HERE / f"prune_large_{name}.npz", **out)
+    print("prune_large", name, "levels", prn.prune_level, "survivors", v,
           "leaves", int(out["stats"][:, 1].sum()), f"{time.time() - t0:.0f} s")
 
 
@@ -680,6 +684,9 @@ def main() -> None:
         return
     if "--cheby-large" in sys.argv:
         prune_large_case("chebyshev")
+        return
+    if "--circ-large" in sys.argv:
+        prune_large_case("taylor", circular=True)
         return
     if "--circ-only" in sys.argv:
         circ_cases()

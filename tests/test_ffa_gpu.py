@@ -263,6 +263,41 @@ def test_brutefold_many_segments_ragged(cuda_device):
         np.testing.assert_array_equal(out.cpu().numpy(), ref, err_msg=f"n={n} nbins={nbins}")
 
 
+@pytest.mark.parametrize("n,seg,nbins,lo,hi,nfreq,per_chunk", [
+    (70 * 2048 + 333, 2048, 64, 40.0, 47.0, 29, 0),   # ragged last segment, 70 segments
+    (33 * 1000, 1000, 50, 300.0, 700.0, 23, 2),       # chunk of 512 not dividing the segment
+    (5 * 1536 + 7, 1536, 100, 0.5, 3.0, 17, 0),       # long bin runs (low frequencies)
+    (40 * 4096, 4096, 256, 9000.0, 9100.0, 9, 4),     # several bins skipped per sample
+    (31 * 512, 512, 37, 60.0, 61.0, 41, 0),           # fewer than 32 segments
+])
+@pytest.mark.parametrize("unit", [False, True])
+def test_brutefold_chain_path_against_oracle(cuda_device, n, seg, nbins, lo, hi, nfreq,
+                                             per_chunk, unit):
+    """The chain path (per-frequency sample order by bin, one lane per
+    segment) against the oracle: ragged segments and chunks, segment counts
+    around a multiple of 32, frequency groups cut by the scratch (per_chunk
+    frequencies per pass; 0 = all at once), bins visited for hundreds of
+    samples or skipped several per sample, unit and general variance."""
+    import torch
+
+    from pyloki_gb300 import _lib
+    from pyloki_gb300.ffa import brutefold
+
+    lib = _lib.load()
+    rng = np.random.default_rng(n + nbins)
+    ts_e = rng.standard_normal(n).astype(np.float32)
+    ts_v = np.ones(n, np.float32) if unit else (1 + rng.random(n)).astype(np.float32)
+    freqs = np.linspace(lo, hi, nfreq)
+    tsamp = 64e-6 if hi < 1000 else 1e-5
+    ref = O.brutefold(ts_e, ts_v, freqs, seg, nbins, tsamp, 0.011)
+    per_freq = int(lib.loki_brutefold_scratch_bytes(1, seg, nbins)) - 768
+    scratch = per_chunk * per_freq + 768 if per_chunk else 1 << 30
+    out = brutefold(torch.from_numpy(ts_e).to(cuda_device), torch.from_numpy(ts_v).to(cuda_device),
+                    torch.from_numpy(freqs).to(cuda_device), seg, nbins, tsamp, 0.011,
+                    scratch_bytes=scratch, unit_variance=unit)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
 def test_window_violation_is_reported_not_faulted(cuda_device):
     """A level whose input window misses the resolved indices sets the device
     error word (the access is skipped) and the host raises."""

@@ -69,25 +69,32 @@ def test_prune_taylor4_circular_matches_oracle(cuda_device):
 
 
 @pytest.mark.parametrize("device_run", [False, True])
-def test_prune_chebyshev_full_size_matches_reference(cuda_device, device_run):
-    """The same workload with the Chebyshev basis against a full run of the
-    reference's own Pruning (tests/golden/prune_large_chebyshev.npz, made by
-    make_fixtures.py --cheby-large from the C oracle's FFA fold of the same
-    seeded series): every level's statistics and score range, the surviving
-    scores and backtracks after the last level, the ascend and the report."""
+@pytest.mark.parametrize("tree", ["chebyshev", "circular"])
+def test_prune_full_size_matches_reference(cuda_device, tree, device_run):
+    """The same workload with the Chebyshev basis, or with the circular-orbit
+    tree of order 5 (crackle added; FFA limits for order 5), against a full
+    run of the reference's own Pruning (tests/golden/prune_large_{tree}.npz,
+    made by make_fixtures.py --cheby-large / --circ-large from the C oracle's
+    FFA fold of the same seeded series): every level's statistics and score
+    range, the surviving scores and backtracks after the last level, the
+    ascend and the report (the circular tree's to 1e-9 of each column's
+    largest magnitude: its propagation calls cos/sin)."""
     import bench
     from conftest import load_golden
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.prune import Pruning
+    from tests.test_prune_gpu import _leaves_close
 
-    d = load_golden("prune_large_chebyshev")
-    cfg = bench.make_prune_cfg()
+    d = load_golden(f"prune_large_{tree}")
+    circ = tree == "circular"
+    cfg = bench.make_prune_cfg(circular=circ)
     ts, _ = bench.make_prune_series(seed=int(d["seed"]))
     dyp = DynamicProgramming(ts, cfg, device=cuda_device)
     dyp.initialize()
     dyp.execute()
     prn = Pruning(dyp, d["thresholds"], max_sugg=bench.PRUNE_MAX_SUGG,
-                  batch_size=bench.PRUNE_BATCH, poly_basis="chebyshev")
+                  batch_size=bench.PRUNE_BATCH, poly_basis="taylor" if circ else tree)
+    assert prn.circular == circ
     ref = int(d["ref_seg"])
     levels = int(d["levels_done"])
     if device_run:
@@ -114,4 +121,7 @@ def test_prune_chebyshev_full_size_matches_reference(cuda_device, device_run):
     wt = prn.world_tree
     np.testing.assert_array_equal(wt.scores.cpu().numpy(), d["asc_scores"])
     np.testing.assert_array_equal(wt.scores_ep.cpu().numpy(), d["asc_scores_ep"])
-    np.testing.assert_allclose(prn.report(), d["report"], rtol=1e-13, atol=0)
+    if circ:
+        _leaves_close(prn.report(), d["report"], "report", circular=True)
+    else:
+        np.testing.assert_allclose(prn.report(), d["report"], rtol=1e-13, atol=0)
