@@ -841,6 +841,34 @@ int loki_fold_ephem(const float* ts_e, const float* ts_v, int64_t nsamps, double
  * (utils/np_utils.py:119-122 downsample_1d). */
 int loki_downsample(const float* x, int64_t n, int32_t factor, float* out, void* stream);
 
+/* ---- series conditioning (io/timeseries.py:198-236 TimeSeries.from_tim) ---
+ * from_tim dereddens the series with sigpyproc's median filter and
+ * normalises it with sigpyproc's location and scale estimates. sigpyproc is
+ * a git dependency of the reference (pyproject.toml:41) outside its tree, so
+ * the steps are defined here:
+ * loki_running_median: out[i] = the order statistic of rank window / 2 of
+ * x[i - window/2 .. i - window/2 + window - 1] with half-sample symmetric
+ * reflection at the ends (scipy.ndimage.median_filter, mode "reflect"), or
+ * x[i] minus it when subtract != 0. 1 <= window <= 32768; x finite (no NaN).
+ * No allocation. */
+int loki_running_median(const float* x, int64_t n, int32_t window, int32_t subtract,
+                        float* out, void* stream);
+
+/* k-th smallest element (0-based) of x into *out (device), by a radix select
+ * over the float order; scratch of loki_select_scratch_bytes() device bytes. */
+int loki_select_kth(const float* x, int64_t n, int64_t k, float* out, void* scratch,
+                    int64_t scratch_bytes, void* stream);
+int64_t loki_select_scratch_bytes(void);
+
+/* Sum of x (square == 0) or of x^2 (square != 0) accumulated in float64 into
+ * *out (device); scratch of at least min(ceil(n / 256), 1024) doubles. */
+int loki_sum_f64(const float* x, int64_t n, int32_t square, double* out, void* scratch,
+                 int64_t scratch_bytes, void* stream);
+
+/* y = (x - loc) / scale in float32, or y = |x - loc| when scale == 0 (the
+ * absolute deviations of a median-absolute-deviation scale). */
+int loki_affine(const float* x, int64_t n, float loc, float scale, float* y, void* stream);
+
 /* ---- alternative profile scorers (detection/scoring.py) ------------------
  * None of these is on a search path of the reference; they score candidate
  * profiles (n, nbins) float32 on request. */

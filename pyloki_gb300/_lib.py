@@ -246,6 +246,11 @@ SIGNATURES: dict[str, tuple] = {
     "loki_fold_ephem": (C.c_int, [_P, _P, _I64, _D, C.POINTER(LokiModulation), _P, _D, _I32,
                                   _I32, _P, _P, _P, _P]),
     "loki_downsample": (C.c_int, [_P, _I64, _I32, _P, _P]),
+    "loki_running_median": (C.c_int, [_P, _I64, _I32, _I32, _P, _P]),
+    "loki_select_kth": (C.c_int, [_P, _I64, _I64, _P, _P, _I64, _P]),
+    "loki_select_scratch_bytes": (C.c_int64, []),
+    "loki_sum_f64": (C.c_int, [_P, _I64, _I32, _P, _P, _I64, _P]),
+    "loki_affine": (C.c_int, [_P, _I64, C.c_float, C.c_float, _P, _P]),
     "loki_kadane_circular": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P, _P, _P]),
     "loki_matched_filter": (C.c_int, [_P, _I64, _I32, _P, _I32, _I32, C.c_float, _P, _P, _P]),
     "loki_matched_filter_conv": (C.c_int, [_P, _I64, _I32, _P, _I32, _P, _P]),

@@ -9,6 +9,78 @@ def _is_tensor(x) -> bool:
     return type(x).__module__.startswith("torch")
 
 
+class _Stats:
+    """Order statistics, sums and moments of one device array (float32),
+    each computed by the library's kernels and read back as a float."""
+
+    def __init__(self, x, dev) -> None:
+        import torch
+
+        from pyloki_gb300 import _lib
+
+        self.x, self.dev, self.n = x, dev, int(x.numel())
+        if self.n < 1:
+            msg = "statistics of an empty series"
+            raise ValueError(msg)
+        self.lib = _lib.load()
+        self.stream = _lib.stream_ptr(torch.cuda.current_stream(dev))
+        self._scratch = torch.empty(max(int(self.lib.loki_select_scratch_bytes()), 8192),
+                                    dtype=torch.uint8, device=dev)
+        self._val = torch.empty(1, dtype=torch.float32, device=dev)
+        self._dval = torch.empty(1, dtype=torch.float64, device=dev)
+
+    def kth(self, k: int, x=None) -> float:
+        from pyloki_gb300 import _lib
+
+        x = self.x if x is None else x
+        _lib.check(self.lib.loki_select_kth(_lib.ptr(x), x.numel(), int(k), _lib.ptr(self._val),
+                                            _lib.ptr(self._scratch), self._scratch.numel(),
+                                            self.stream))
+        return float(self._val.item())
+
+    def _sum(self, x, square: bool) -> float:
+        from pyloki_gb300 import _lib
+
+        _lib.check(self.lib.loki_sum_f64(_lib.ptr(x), x.numel(), int(square),
+                                         _lib.ptr(self._dval), _lib.ptr(self._scratch),
+                                         self._scratch.numel(), self.stream))
+        return float(self._dval.item())
+
+    def mean(self) -> float:
+        return self._sum(self.x, False) / self.n
+
+    def median(self, x=None) -> float:
+        n = self.n if x is None else int(x.numel())
+        lo = self.kth((n - 1) // 2, x)
+        hi = lo if n % 2 else self.kth(n // 2, x)
+        return float(np.float32((np.float64(lo) + np.float64(hi)) / 2.0))
+
+    def percentile(self, q: float) -> float:
+        """numpy's ``percentile`` (linear interpolation) of the array."""
+        pos = (self.n - 1) * q / 100.0
+        k = int(np.floor(pos))
+        t = pos - k
+        a = np.float64(self.kth(k))
+        b = np.float64(self.kth(min(k + 1, self.n - 1))) if t > 0 else a
+        return float(a + (b - a) * t) if t < 0.5 else float(b - (b - a) * (1.0 - t))
+
+    def _dev(self, loc: float, absolute: bool):
+        import torch
+
+        from pyloki_gb300 import _lib
+
+        d = torch.empty_like(self.x)
+        _lib.check(self.lib.loki_affine(_lib.ptr(self.x), self.n, float(np.float32(loc)),
+                                        0.0 if absolute else 1.0, _lib.ptr(d), self.stream))
+        return d
+
+    def std(self) -> float:
+        return float(np.sqrt(self._sum(self._dev(self.mean(), False), True) / self.n))
+
+    def mad(self) -> float:
+        return self.median(self._dev(self.median(), True))
+
+
 class TimeSeries:
     """A time series as pyloki holds it.
 
@@ -138,6 +210,111 @@ class TimeSeries:
         res = (norm if normalize else fold).squeeze(0) if nsubints == 1 else (
             norm if normalize else fold)
         return res.cpu().numpy() if host else res
+
+    def deredden(self, method: str = "median", window: float = 0.5, *, fast: bool = False,
+                 device=None) -> TimeSeries:
+        """``ts_e`` minus its running median over ``window`` seconds
+        (``int(window / tsamp)`` samples, as the reference's call into
+        sigpyproc's ``TimeSeries.deredden``, ``io/timeseries.py:231``), on the
+        GPU: the order statistic of rank ``window // 2`` of the centred window
+        with half-sample symmetric reflection at the ends (the definition of
+        ``scipy.ndimage.median_filter``, mode ``"reflect"``). ``fast`` is
+        accepted for the reference's signature; the filter is always exact.
+        ``ts_v`` is kept."""
+        import torch
+
+        from pyloki_gb300 import _lib
+
+        del fast
+        if method != "median":
+            msg = f"deredden method must be 'median', got {method!r}"
+            raise ValueError(msg)
+        nwin = int(window / self.tsamp)
+        if nwin < 1:
+            msg = f"window {window} s is shorter than one sample ({self.tsamp} s)"
+            raise ValueError(msg)
+        e, v, dev, host = self._device_arrays(device)
+        if not bool(torch.isfinite(e).all()):
+            msg = "deredden needs a finite series (no NaN or inf)"
+            raise ValueError(msg)
+        out = torch.empty_like(e)
+        _lib.check(_lib.load().loki_running_median(
+            _lib.ptr(e), e.numel(), nwin, 1, _lib.ptr(out),
+            _lib.stream_ptr(torch.cuda.current_stream(dev))))
+        return TimeSeries(out.cpu().numpy() if host else out,
+                          v.cpu().numpy() if host else v, self.tsamp)
+
+    def normalise(self, loc_method: str = "mean", scale_method: str = "std", *,
+                  device=None) -> TimeSeries:
+        """``(ts_e - loc) / scale`` in float32 (the reference's call into
+        sigpyproc's ``TimeSeries.normalise``, ``io/timeseries.py:232``), with
+        the statistics taken on the GPU:
+
+        - ``loc_method``: ``"mean"`` (float64 sum / n) or ``"median"`` (the
+          mean of the two middle order statistics for an even count);
+        - ``scale_method``: ``"std"`` (population standard deviation about
+          the mean, float64), ``"iqr"`` (interquartile range of numpy's
+          linearly interpolated percentiles / 1.3489795003921634, the normal
+          consistency factor) or ``"mad"`` (median absolute deviation about
+          the median x 1.482602218505602).
+
+        ``ts_v`` is kept."""
+        import torch
+
+        from pyloki_gb300 import _lib
+
+        e, v, dev, host = self._device_arrays(device)
+        st = _Stats(e, dev)
+        if loc_method == "mean":
+            loc = st.mean()
+        elif loc_method == "median":
+            loc = st.median()
+        else:
+            msg = f"loc_method must be 'mean' or 'median', got {loc_method!r}"
+            raise ValueError(msg)
+        if scale_method == "std":
+            scale = st.std()
+        elif scale_method == "iqr":
+            scale = (st.percentile(75.0) - st.percentile(25.0)) / 1.3489795003921634
+        elif scale_method == "mad":
+            scale = st.mad() * 1.482602218505602
+        else:
+            msg = f"scale_method must be 'std', 'iqr' or 'mad', got {scale_method!r}"
+            raise ValueError(msg)
+        if not scale > 0 or not np.isfinite(scale):
+            msg = f"the series has scale {scale}: it cannot be normalised"
+            raise ValueError(msg)
+        out = torch.empty_like(e)
+        _lib.check(_lib.load().loki_affine(_lib.ptr(e), e.numel(), float(np.float32(loc)),
+                                           float(np.float32(scale)), _lib.ptr(out),
+                                           st.stream))
+        return TimeSeries(out.cpu().numpy() if host else out,
+                          v.cpu().numpy() if host else v, self.tsamp)
+
+    @classmethod
+    def from_tim(cls, timfile, tim_type: str = "dat", filter_window: float = 1.0,
+                 norm_scale_method: str = "iqr", *, device=None) -> TimeSeries:
+        """Load a ``.dat`` (PRESTO, with its ``.inf``) or ``.tim`` (SIGPROC)
+        series, deredden it with a running median of ``filter_window``
+        seconds, normalise it to zero mean and unit ``norm_scale_method``
+        scale, and pair it with unit variance
+        (``io/timeseries.py:198-236``). The filters run on the GPU."""
+        from pyloki_gb300 import sigproc
+
+        if tim_type == "dat":
+            data, info = sigproc.read_dat(timfile)
+            tsamp = info["tsamp"]
+        elif tim_type == "tim":
+            data, hdr = sigproc.read_tim(timfile)
+            tsamp = hdr["tsamp"]
+        else:
+            msg = f"Invalid tim type: {tim_type}"
+            raise ValueError(msg)
+        ts = cls(data, np.ones_like(data), tsamp)
+        ts = ts.deredden(method="median", window=filter_window, fast=True, device=device)
+        ts = ts.normalise(loc_method="mean", scale_method=norm_scale_method, device=device)
+        return cls(ts.ts_e, np.ones_like(ts.ts_e) if not _is_tensor(ts.ts_e)
+                   else ts.ts_e.new_ones(ts.ts_e.shape), tsamp)
 
     def __str__(self) -> str:
         return (f"{type(self).__name__} {{nsamps = {self.nsamps:d}, tsamp = {self.tsamp:.4e}, "
