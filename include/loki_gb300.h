@@ -633,6 +633,103 @@ int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const float* ffa
                    int64_t batch_size, const LokiPruneRun* run, int32_t* dev_err,
                    void* stream);
 
+/* One job of loki_prune_run_blocks: a reference segment of a fold, its
+ * buffers and its device error word. */
+typedef struct {
+  const float* ffa_fold;   /* segment rows of this job's FFA fold */
+  int64_t seg_stride;      /* floats between segments */
+  int64_t seed_n;          /* parents already in run.trees[0] (leaves, folds, scores) */
+  LokiPruneRun run;        /* as for loki_prune_run (Taylor / Chebyshev: no circular fields) */
+  int32_t* dev_err;        /* device error word */
+} LokiPruneJob;
+
+/* loki_prune_run for njobs jobs at once: one thread block per job runs every
+ * level with block barriers between the steps (the same branch, score,
+ * select, overflow and emit code), so the whole batch is one launch. Job j's
+ * level l uses levels[j * nlevels + l - 1], seg_idx[j * nlevels + l - 1] and
+ * thresholds[j * nlevels + l - 1] (host arrays, checked and copied with the
+ * jobs into dev_scratch of loki_prune_run_blocks_scratch_bytes bytes).
+ * Results, counters and LOKI_DEVERR_* flags per job as loki_prune_run
+ * writes them. Taylor and Chebyshev trees (not basis 2). No reference
+ * counterpart as one call: it replaces the per-segment loop of
+ * prune_dyp_tree (prune.py:696-780) over Pruning.execute. */
+int loki_prune_run_blocks(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
+                          const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
+                          const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                          void* dev_scratch, int64_t dev_scratch_bytes, void* stream);
+int64_t loki_prune_run_blocks_scratch_bytes(int32_t njobs, int32_t nlevels);
+
+/* The same jobs, arguments and results as loki_prune_run_blocks, run level
+ * by level over all jobs at once: every step of a level (branch, the two
+ * scans, score, select, overflow rule, emit, backtrack history, best leaf
+ * and record) is one launch whose blocks cover every job (grid y = job), so
+ * a batch costs the launches of a single run and each step spreads over the
+ * whole GPU; no host wait, so the enqueue can be captured in a CUDA graph.
+ * dev_scratch of loki_prune_run_blocks_scratch_bytes bytes; njobs <= 65535.
+ * Taylor and Chebyshev trees (not basis 2). */
+int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
+                         const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
+                         const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                         void* dev_scratch, int64_t dev_scratch_bytes, void* stream);
+
+/* loki_prune_run_batch in two halves, so that the kernels can be captured
+ * in a CUDA graph once and replayed: loki_prune_batch_tables checks the jobs
+ * and copies the tables into dev_scratch (host memory is read: not inside a
+ * capture) and writes the batch's shape (4 words: nbins, poly_order, largest
+ * par_cap, largest child_cap); loki_prune_batch_enqueue enqueues the kernels
+ * over the tables in dev_scratch for that shape. A replay after
+ * loki_prune_batch_tables with new jobs of the same count, levels and shape
+ * runs the new jobs. */
+int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
+                            const LokiPruneLevel* levels, const int32_t* seg_idx,
+                            const double* thresholds, int32_t nlevels,
+                            const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                            void* dev_scratch, int64_t dev_scratch_bytes, int64_t* shape_out,
+                            void* stream);
+int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
+                             const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                             const int64_t* shape_in, void* stream);
+
+/* One job of loki_prune_ascend_batch: the ascend of loki_prune_ascend_dev
+ * (its level descriptor, final tree, device survivor count and per-segment
+ * tables) for one run. */
+typedef struct {
+  LokiPruneLevel lvl;
+  const double* leaves;
+  float* folds;
+  float* scores;
+  float* scores_ep;
+  const int64_t* n_dev;    /* survivors (device), <= n_cap */
+  const double* tm_seg;
+  const double* dt_seg;
+  const int32_t* seg_idx;
+  const float* ffa_fold;
+  int64_t seg_stride;
+  int32_t* dev_err;
+} LokiAscendJob;
+
+/* loki_prune_ascend_dev for njobs runs in one launch (grid y = job): the
+ * jobs (host array) are checked and copied into dev_scratch of at least
+ * njobs * sizeof(LokiAscendJob) bytes. Every job has nseg segments and at
+ * most n_cap survivors. Taylor and Chebyshev trees. */
+int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs, int32_t nseg,
+                            const LokiScoreSpec* spec, int64_t n_cap, void* dev_scratch,
+                            int64_t dev_scratch_bytes, void* stream);
+
+/* A device byte range and its place in a packed destination. */
+typedef struct {
+  const void* src;
+  int64_t bytes;
+  int64_t dst_off;
+} LokiGatherPart;
+
+/* Copy every part into dst (device, dst_bytes) at its offset in one launch
+ * (the parts, a host array, are checked and copied into dev_scratch of at
+ * least nparts * sizeof(LokiGatherPart) bytes): many small device ranges
+ * become one packed buffer for a single device-to-host copy. */
+int loki_gather_parts(const LokiGatherPart* parts, int32_t nparts, void* dst, int64_t dst_bytes,
+                      void* dev_scratch, int64_t dev_scratch_bytes, void* stream);
+
 /* Best leaf of a tree (utils/world_tree.py:441-459 get_best_k with k = 1):
  * the leaf row (row_len float64) and score of the maximum score, first index
  * on ties; nothing is written for n = 0. */

@@ -173,6 +173,22 @@ class LokiPruneRun(C.Structure):
                 ("batch_taylor", C.c_void_p), ("batch_offsets", C.c_void_p)]
 
 
+class LokiPruneJob(C.Structure):
+    _fields_ = [("ffa_fold", C.c_void_p), ("seg_stride", C.c_int64), ("seed_n", C.c_int64),
+                ("run", LokiPruneRun), ("dev_err", C.c_void_p)]
+
+
+class LokiAscendJob(C.Structure):
+    _fields_ = [("lvl", LokiPruneLevel), ("leaves", C.c_void_p), ("folds", C.c_void_p),
+                ("scores", C.c_void_p), ("scores_ep", C.c_void_p), ("n_dev", C.c_void_p),
+                ("tm_seg", C.c_void_p), ("dt_seg", C.c_void_p), ("seg_idx", C.c_void_p),
+                ("ffa_fold", C.c_void_p), ("seg_stride", C.c_int64), ("dev_err", C.c_void_p)]
+
+
+class LokiGatherPart(C.Structure):
+    _fields_ = [("src", C.c_void_p), ("bytes", C.c_int64), ("dst_off", C.c_int64)]
+
+
 #: numpy view of an array of LokiPruneLevelStats records
 PRUNE_STATS_DTYPE = np.dtype([("n_parents", np.int64), ("n_children", np.int64),
                               ("n_valid", np.int64), ("n_surv", np.int64),
@@ -219,6 +235,19 @@ SIGNATURES: dict[str, tuple] = {
     "loki_brutefold_noalloc": (C.c_int, [_P, _P, _I64, _P, _I64, _I64, _I32, _D, _D, _P, _P]),
     "loki_brutefold_noalloc_scratch_bytes": (C.c_int64, []),
     "loki_brutefold_scratch_bytes": (C.c_int64, [_I64, _I64, _I32]),
+    "loki_prune_run_blocks": (C.c_int, [_P, _I32, _P, _P, _P, _I32, C.POINTER(LokiScoreSpec),
+                                        _I64, _I64, _P, _I64, _P]),
+    "loki_prune_run_blocks_scratch_bytes": (C.c_int64, [_I32, _I32]),
+    "loki_prune_run_batch": (C.c_int, [_P, _I32, _P, _P, _P, _I32, C.POINTER(LokiScoreSpec),
+                                       _I64, _I64, _P, _I64, _P]),
+    "loki_prune_batch_tables": (C.c_int, [_P, _I32, _P, _P, _P, _I32,
+                                          C.POINTER(LokiScoreSpec), _I64, _I64, _P, _I64, _P,
+                                          _P]),
+    "loki_prune_batch_enqueue": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64,
+                                           _I64, _P, _P]),
+    "loki_prune_ascend_batch": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64, _P,
+                                          _I64, _P]),
+    "loki_gather_parts": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "loki_ffa_plan": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P]),
     "loki_ffa_level": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
     "loki_ffa_level_score": (C.c_int, [C.POINTER(LokiFFALevel), _P, C.POINTER(LokiScoreSpec),

@@ -291,14 +291,14 @@ __device__ __forceinline__ ChildRes resolve_child(const LokiPruneLevel& D, const
 // branch
 // ---------------------------------------------------------------------------
 
-__global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                                    int64_t n, LokiBranchInfo* __restrict__ info,
-                                    int64_t* __restrict__ counts, int32_t* __restrict__ err,
-                                    const uint8_t* __restrict__ mask,
-                                    const int64_t* __restrict__ n_dev) {
-  if (n_dev) n = *n_dev;  // parent count held on the device
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// Parent i: per-parameter child counts, steps and first values (info[i]) and
+// its child count (counts[i]).
+__device__ __forceinline__ void branch_one(const LokiPruneLevel& D,
+                                           const double* __restrict__ leaves, int64_t i,
+                                           LokiBranchInfo* __restrict__ info,
+                                           int64_t* __restrict__ counts,
+                                           int32_t* __restrict__ err,
+                                           const uint8_t* __restrict__ mask) {
   const int P = D.poly_order, m = P + 1;
   const double* lf = leaves + i * (P + 2) * 2;
   const double f0 = lf[(P + 1) * 2];
@@ -367,6 +367,17 @@ __global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__
   }
   info[i] = B;
   counts[i] = (mask && !mask[i]) ? 0 : total;  // a masked-out parent has no children
+}
+
+__global__ void prune_branch_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                                    int64_t n, LokiBranchInfo* __restrict__ info,
+                                    int64_t* __restrict__ counts, int32_t* __restrict__ err,
+                                    const uint8_t* __restrict__ mask,
+                                    const int64_t* __restrict__ n_dev) {
+  if (n_dev) n = *n_dev;  // parent count held on the device
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  branch_one(D, leaves, i, info, counts, err, mask);
 }
 
 // ---------------------------------------------------------------------------
@@ -584,7 +595,7 @@ __device__ __forceinline__ int block_scan_flag(int f, int* total, int* wsum) {
   if (lane == 0) wsum[warp] = __popc(b);
   __syncthreads();
   if (warp == 0) {
-    int w = wsum[lane];
+    int w = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
     int v = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -633,31 +644,22 @@ __device__ unsigned block_select(const unsigned* keys, int64_t n, int64_t r, uns
   return prefix;
 }
 
-// With cnt_dev (device counts: [0] parents) the plain selection's survivor
-// count is pos[*n_in] (n_in: its inputs, the children): it is stored at *n_out, and
-// the kernel does nothing more unless it exceeds cap (then *ovf_flag is set
-// and the overflow rule rewrites the selection and *n_out). n_out points into
-// the same counters, so neither pointer is restrict.
-__global__ void __launch_bounds__(kSelThreads)
-select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restrict__ offsets,
-                       int64_t n_parents, int64_t batch, double thr, int64_t cap,
-                       int64_t* __restrict__ ids, int64_t* n_out,
-                       double* __restrict__ thr_out, int64_t* __restrict__ tmp_ids,
-                       unsigned* __restrict__ keys, const int64_t* cnt_dev,
-                       int32_t* __restrict__ ovf_flag, const int64_t* __restrict__ pos,
-                       const int64_t* n_in) {
+// The overflow rule over the whole selection, by one block (any multiple of
+// 32 threads up to 1024): batch by batch of parents, the passing children are
+// appended while they fit, otherwise prune_on_overload raises the threshold.
+// Writes ids[0 .. *n_out) and the final threshold.
+__device__ void select_overflow_block(const float* __restrict__ scores,
+                                      const int64_t* __restrict__ offsets, int64_t n_parents,
+                                      int64_t batch, double thr, int64_t cap,
+                                      int64_t* __restrict__ ids, int64_t* n_out,
+                                      double* __restrict__ thr_out,
+                                      int64_t* __restrict__ tmp_ids,
+                                      unsigned* __restrict__ keys) {
   __shared__ int wsum[33];
   __shared__ unsigned hist[256];
   __shared__ long long vs_sh;
   __shared__ double cur_sh;
-  if (cnt_dev) {
-    const int64_t n_sel = pos[*n_in];  // the selection's total over its n_in inputs
-    n_parents = cnt_dev[0];
-    __syncthreads();  // every thread has read the counters
-    if (threadIdx.x == 0) *n_out = n_sel;
-    if (n_sel <= cap) return;  // uniform over the block
-    if (threadIdx.x == 0) *ovf_flag = 1;
-  }
+  const int nthr = blockDim.x;  // the loops stride by the block
   if (threadIdx.x == 0) {
     vs_sh = 0;
     cur_sh = thr;
@@ -670,7 +672,7 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
     const double eff_in = fmax(thr, cur_sh);
     // pass 1: count passing children of the batch
     int64_t m = 0;
-    for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+    for (int64_t base = c_lo; base < c_hi; base += nthr) {
       const int64_t c = base + threadIdx.x;
       const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
       int tot;
@@ -680,7 +682,7 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
     int64_t vs = vs_sh;
     if (m <= cap - vs) {  // fast path: append in order
       int64_t w = vs;
-      for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+      for (int64_t base = c_lo; base < c_hi; base += nthr) {
         const int64_t c = base + threadIdx.x;
         const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
         int tot;
@@ -694,8 +696,8 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
     }
     // prune_on_overload: keys of the current tree and of the passing batch
     int64_t w = vs;
-    for (int64_t i = threadIdx.x; i < vs; i += kSelThreads) keys[i] = float_key(scores[ids[i]]);
-    for (int64_t base = c_lo; base < c_hi; base += kSelThreads) {
+    for (int64_t i = threadIdx.x; i < vs; i += nthr) keys[i] = float_key(scores[ids[i]]);
+    for (int64_t base = c_lo; base < c_hi; base += nthr) {
       const int64_t c = base + threadIdx.x;
       const int f = (c < c_hi && (double)scores[c] >= eff_in) ? 1 : 0;
       int tot;
@@ -716,7 +718,7 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
     eff = fmax(eff, fmax(tk, tm));
     // keep tree entries >= eff (stable)
     int64_t kept = 0;
-    for (int64_t base = 0; base < vs; base += kSelThreads) {
+    for (int64_t base = 0; base < vs; base += nthr) {
       const int64_t i = base + threadIdx.x;
       int64_t id = 0;
       int f = 0;
@@ -730,12 +732,12 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
       kept += tot;
     }
     __syncthreads();
-    for (int64_t i = threadIdx.x; i < kept; i += kSelThreads) ids[i] = tmp_ids[m + i];
+    for (int64_t i = threadIdx.x; i < kept; i += nthr) ids[i] = tmp_ids[m + i];
     __syncthreads();
     // pending batch entries >= eff, in order, up to the free space
     const int64_t space = cap - kept;
     int64_t added = 0;
-    for (int64_t base = 0; base < m; base += kSelThreads) {
+    for (int64_t base = 0; base < m; base += nthr) {
       const int64_t i = base + threadIdx.x;
       int64_t id = 0;
       int f = 0;
@@ -758,6 +760,32 @@ select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restri
     *n_out = vs_sh;
     *thr_out = cur_sh;
   }
+  __syncthreads();
+}
+
+// With cnt_dev (device counts: [0] parents) the plain selection's survivor
+// count is pos[*n_in] (n_in: its inputs, the children): it is stored at
+// *n_out, and the kernel does nothing more unless it exceeds cap (then
+// *ovf_flag is set and the overflow rule rewrites the selection and *n_out).
+// n_out points into the same counters, so neither pointer is restrict.
+__global__ void __launch_bounds__(kSelThreads)
+select_overflow_kernel(const float* __restrict__ scores, const int64_t* __restrict__ offsets,
+                       int64_t n_parents, int64_t batch, double thr, int64_t cap,
+                       int64_t* __restrict__ ids, int64_t* n_out,
+                       double* __restrict__ thr_out, int64_t* __restrict__ tmp_ids,
+                       unsigned* __restrict__ keys, const int64_t* cnt_dev,
+                       int32_t* __restrict__ ovf_flag, const int64_t* __restrict__ pos,
+                       const int64_t* n_in) {
+  if (cnt_dev) {
+    const int64_t n_sel = pos[*n_in];  // the selection's total over its n_in inputs
+    n_parents = cnt_dev[0];
+    __syncthreads();  // every thread has read the counters
+    if (threadIdx.x == 0) *n_out = n_sel;
+    if (n_sel <= cap) return;  // uniform over the block
+    if (threadIdx.x == 0) *ovf_flag = 1;
+  }
+  select_overflow_block(scores, offsets, n_parents, batch, thr, cap, ids, n_out, thr_out, tmp_ids,
+                        keys);
 }
 
 // ---------------------------------------------------------------------------
@@ -2068,14 +2096,11 @@ __device__ __forceinline__ void level_end(int64_t* cnt, unsigned* keys, int32_t*
 
 // Best leaf of a tree (max score, first index on ties, as torch.argmax):
 // one block reduces (score, index), then copies the leaf row and its score.
-__global__ void __launch_bounds__(1024)
-prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __restrict__ leaves,
-                  int row, double* __restrict__ leaf_out, float* __restrict__ score_out,
-                  int64_t* lvl_cnt, unsigned* lvl_keys, int32_t* lvl_ovf,
-                  LokiPruneLevelStats* lvl_st) {
+__device__ void block_best(const float* __restrict__ scores, int64_t n,
+                           const double* __restrict__ leaves, int row,
+                           double* __restrict__ leaf_out, float* __restrict__ score_out) {
   __shared__ float sv[32];
   __shared__ int64_t si[32];
-  if (lvl_cnt) n = lvl_cnt[2];  // the level's survivors; 0 writes nothing (bi stays -1)
   float bv = -INFINITY;
   int64_t bi = -1;
   // each thread visits its elements in increasing index order, so it keeps
@@ -2153,8 +2178,18 @@ prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __r
     if (bi >= 0)
       for (int j = lane; j < row; j += 32) leaf_out[j] = leaves[bi * row + j];
     if (lane == 0 && bi >= 0) *score_out = scores[bi];
-    if (lane == 0 && lvl_cnt) level_end(lvl_cnt, lvl_keys, lvl_ovf, lvl_st);
   }
+}
+
+__global__ void __launch_bounds__(1024)
+prune_best_kernel(const float* __restrict__ scores, int64_t n, const double* __restrict__ leaves,
+                  int row, double* __restrict__ leaf_out, float* __restrict__ score_out,
+                  int64_t* lvl_cnt, unsigned* lvl_keys, int32_t* lvl_ovf,
+                  LokiPruneLevelStats* lvl_st) {
+  if (lvl_cnt) n = lvl_cnt[2];  // the level's survivors; 0 writes nothing
+  block_best(scores, n, leaves, row, leaf_out, score_out);
+  // every thread read the count before block_best's barrier
+  if (threadIdx.x == 0 && lvl_cnt) level_end(lvl_cnt, lvl_keys, lvl_ovf, lvl_st);
 }
 
 extern "C" int loki_prune_best(const float* scores, int64_t n, const double* leaves,
@@ -2942,4 +2977,812 @@ extern "C" int loki_prune_run(const LokiPruneLevel* lvls, int32_t nlevels, const
     if (rc) return rc;
   }
   return LOKI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// block-per-run driver: one thread block runs every level of one job (a
+// reference segment of a fold) with block barriers between the steps, so a
+// batch of jobs is one launch instead of ~13 dependent launches per level
+// and job. The steps are those of loki_prune_run (Taylor and Chebyshev
+// trees): branch, scan, score, select (with the overflow rule), emit,
+// backtrack history, best leaf and level record.
+// ---------------------------------------------------------------------------
+
+namespace loki {
+
+constexpr int kRunThreads = 512;  // 16 warps a job
+
+// Exclusive scan of in[0..n) (int64 counts, or score >= thr flags) into
+// out[0..n), out[n] = total, by one block; in may be out. Returns the total.
+template <bool FLAGS>
+__device__ int64_t block_scan64(const void* in, int64_t n, double thr, int64_t* out,
+                                int64_t* warp_tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int64_t carry = 0;
+  for (int64_t base = 0; base < n; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t x = scan_in<FLAGS>(in, i, n, thr);
+    int64_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_tot[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = lane < nw ? warp_tot[lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int64_t incl = v + (warp ? warp_tot[warp - 1] : 0);
+    if (i < n) out[i] = carry + incl - x;
+    carry += warp_tot[nw - 1];
+    __syncthreads();  // warp_tot is rewritten by the next tile
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+  __syncthreads();
+  return carry;
+}
+
+__global__ void __launch_bounds__(kRunThreads, 1)
+prune_block_run_kernel(const LokiPruneJob* __restrict__ jobs,
+                       const LokiPruneLevel* __restrict__ levels,
+                       const int32_t* __restrict__ seg_idx, const double* __restrict__ thr_all,
+                       int32_t nlevels, LokiScoreSpec sp, ScoreK SK, int64_t max_sugg,
+                       int64_t batch) {
+  extern __shared__ float tiles[];
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t n_sh;
+  const LokiPruneJob& J = jobs[blockIdx.x];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const int tid = threadIdx.x, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(levels[0].nbins, sp.wmax);
+  int64_t* cnt = R.counts;
+  unsigned* keys = reinterpret_cast<unsigned*>(w.minmax);
+  LokiBranchInfo* info = reinterpret_cast<LokiBranchInfo*>(w.info);
+  // selection positions after the scan sums, as loki_prune_run places them
+  const int64_t sums_bytes = (int64_t)max((int64_t)1, (w.child_cap + kScanBlock - 1) / kScanBlock) * 8;
+  int64_t* pos = reinterpret_cast<int64_t*>(reinterpret_cast<char*>(w.sscan) + sums_bytes);
+  const int P = levels[0].poly_order;
+  const int row_bt = P + 2, row_leaf = (P + 2) * 2;
+  if (tid == 0) {
+    cnt[0] = J.seed_n;
+    for (int k = 1; k < 8; ++k) cnt[k] = 0;
+    keys[0] = 0xFFFFFFFFu;
+    keys[1] = 0u;
+    *R.ovf_flag = 0;
+  }
+  __syncthreads();
+  int64_t n_par = J.seed_n;
+  for (int l = 1; l <= nlevels; ++l) {
+    const LokiPruneLevel& D = levels[(size_t)blockIdx.x * nlevels + (l - 1)];
+    const LokiPruneTree& in = R.trees[(l - 1) & 1];
+    const LokiPruneTree& out = R.trees[l & 1];
+    const float* seg = J.ffa_fold + (int64_t)seg_idx[(size_t)blockIdx.x * nlevels + (l - 1)] *
+                                        J.seg_stride;
+    const double thr = thr_all[(size_t)blockIdx.x * nlevels + (l - 1)];
+    LokiPruneLevelStats* st = R.stats + (l - 1);
+    // branch and the child offsets
+    for (int64_t i = tid; i < n_par; i += blockDim.x)
+      branch_one(D, in.leaves, i, info, w.offsets, J.dev_err, nullptr);
+    __syncthreads();
+    const int64_t total = block_scan64<false>(w.offsets, n_par, 0.0, w.offsets, warp_tot);
+    const int64_t n_child = total > w.child_cap ? 0 : total;
+    if (tid == 0) {
+      cnt[1] = n_child;
+      st->n_parents = n_par;
+      st->n_children = total;
+      st->n_valid = total;
+      if (total > w.child_cap) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+    }
+    // score every child
+    for (int64_t t = warp; t * 32 < n_child; t += nwarps) {
+      score_tile(D, in.leaves, in.folds, n_par, info, w.offsets, n_child, seg, sp, SK,
+                 w.child_scores, w.child_idx, w.child_phase, keys, tile, t * 32);
+      __syncwarp();  // the tile rows are rewritten by the next tile
+    }
+    __syncthreads();
+    // select: survivors in order, then the overflow rule when they exceed max_sugg
+    const int64_t n_sel = block_scan64<true>(w.child_scores, n_child, thr, pos, warp_tot);
+    for (int64_t i = tid; i < n_child; i += blockDim.x)
+      if ((double)w.child_scores[i] >= thr) w.surv[pos[i]] = i;
+    if (tid == 0) n_sh = n_sel;
+    __syncthreads();
+    if (n_sel > max_sugg) {  // uniform over the block
+      if (tid == 0) *R.ovf_flag = 1;
+      select_overflow_block(w.child_scores, w.offsets, n_par, batch, thr, max_sugg, w.surv,
+                            &n_sh, w.ovf_thr, w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys));
+    }
+    const int64_t n_surv = n_sh;
+    // the next tree
+    for (int64_t t = warp; t * 32 < n_surv; t += nwarps)
+      emit_tile(D, in.leaves, in.folds, info, w.offsets, n_par, seg, w.surv, n_surv,
+                w.child_scores, w.child_idx, w.child_phase, out.leaves, out.folds, out.scores,
+                out.scores_ep, out.backtracks, t * 32);
+    __syncthreads();
+    // backtrack history, best leaf, level record
+    if (R.bt_hist) {
+      const int64_t start = cnt[3];
+      if (start + n_surv > R.bt_rows) {
+        if (tid == 0) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+      } else {
+        int32_t* h = R.bt_hist + start * row_bt;
+        for (int64_t i = tid; i < n_surv * row_bt; i += blockDim.x) h[i] = out.backtracks[i];
+      }
+    }
+    if (R.best_leaves && R.best_scores)
+      block_best(out.scores, n_surv, out.leaves, row_leaf,
+                 R.best_leaves + (int64_t)(l - 1) * row_leaf, R.best_scores + (l - 1));
+    __syncthreads();
+    if (tid == 0) {
+      cnt[2] = n_surv;
+      level_end(cnt, keys, R.ovf_flag, st);
+    }
+    __syncthreads();
+    n_par = n_surv;
+  }
+}
+
+}  // namespace loki
+
+extern "C" int64_t loki_prune_run_blocks_scratch_bytes(int32_t njobs, int32_t nlevels) {
+  if (njobs < 1 || nlevels < 1) return 0;
+  const int64_t nl = (int64_t)njobs * nlevels;
+  return ((int64_t)njobs * sizeof(LokiPruneJob) + 255) / 256 * 256 +
+         (nl * (int64_t)sizeof(LokiPruneLevel) + 255) / 256 * 256 +
+         (nl * 4 + 255) / 256 * 256 + nl * 8;
+}
+
+extern "C" int loki_prune_run_blocks(const LokiPruneJob* jobs, int32_t njobs,
+                                     const LokiPruneLevel* levels, const int32_t* seg_idx,
+                                     const double* thresholds, int32_t nlevels,
+                                     const LokiScoreSpec* spec, int64_t max_sugg,
+                                     int64_t batch_size, void* dev_scratch,
+                                     int64_t dev_scratch_bytes, void* stream) {
+  if (!jobs || njobs < 1 || !levels || !seg_idx || !thresholds || nlevels < 1 || !spec ||
+      !dev_scratch)
+    return set_error(LOKI_ERR_INVALID, "null pointer, no job or no level");
+  if (max_sugg < 1 || batch_size < 1)
+    return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (dev_scratch_bytes < loki_prune_run_blocks_scratch_bytes(njobs, nlevels))
+    return set_error(LOKI_ERR_CAPACITY, "job scratch below %lld bytes",
+                     (long long)loki_prune_run_blocks_scratch_bytes(njobs, nlevels));
+  const int nb = levels[0].nbins;
+  for (int64_t k = 0; k < (int64_t)njobs * nlevels; ++k) {
+    int rc = check_prune(&levels[k]);
+    if (rc) return rc;
+    if (levels[k].basis != levels[0].basis || levels[k].poly_order != levels[0].poly_order ||
+        levels[k].nbins != nb)
+      return set_error(LOKI_ERR_INVALID, "levels of different trees");
+  }
+  if (levels[0].basis == 2)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree runs in loki_prune_run");
+  for (int j = 0; j < njobs; ++j) {
+    const LokiPruneJob& J = jobs[j];
+    const LokiPruneRun& R = J.run;
+    const LokiPruneWork& w = R.work;
+    if (!J.ffa_fold || J.seg_stride < 1 || !J.dev_err || J.seed_n < 0 || J.seed_n > max_sugg)
+      return set_error(LOKI_ERR_INVALID, "job %d: bad fold, error word or seed", j);
+    if (R.trees[0].cap < max_sugg || R.trees[1].cap < max_sugg || w.par_cap < max_sugg ||
+        w.child_cap < 1 || w.ovf_cap < max_sugg + w.child_cap + 1)
+      return set_error(LOKI_ERR_CAPACITY, "job %d: workspace below max_sugg / child_cap", j);
+    if (!R.counts || !R.ovf_flag || !R.stats || !w.info || !w.offsets || !w.child_scores ||
+        !w.child_idx || !w.child_phase || !w.surv || !w.sscan || !w.minmax || !w.ovf_ids ||
+        !w.ovf_keys || !w.ovf_thr)
+      return set_error(LOKI_ERR_INVALID, "job %d: null workspace pointer", j);
+    if (w.sscan_bytes <
+        loki_scan_scratch_bytes(w.child_cap) + (w.child_cap + 1) * (int64_t)sizeof(int64_t))
+      return set_error(LOKI_ERR_CAPACITY, "job %d: selection scratch below child_cap", j);
+    for (int t = 0; t < 2; ++t)
+      if (!R.trees[t].leaves || !R.trees[t].folds || !R.trees[t].scores ||
+          !R.trees[t].scores_ep || !R.trees[t].backtracks)
+        return set_error(LOKI_ERR_INVALID, "job %d: null tree pointer", j);
+  }
+  int rc = prune_spec_check(spec, nb);
+  if (rc) return rc;
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, nb);
+  const int smem = (kRunThreads / 32) * 32 * score_stride(nb, sp.wmax) * (int)sizeof(float);
+  if (smem > 200 * 1024)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for the block driver");
+  if (set_smem_limit(prune_block_run_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  const int64_t nl = (int64_t)njobs * nlevels;
+  char* base = reinterpret_cast<char*>(dev_scratch);
+  const int64_t o_lv = ((int64_t)njobs * sizeof(LokiPruneJob) + 255) / 256 * 256;
+  const int64_t o_si = o_lv + (nl * (int64_t)sizeof(LokiPruneLevel) + 255) / 256 * 256;
+  const int64_t o_th = o_si + (nl * 4 + 255) / 256 * 256;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(base, jobs, njobs * sizeof(LokiPruneJob), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(base + o_lv, levels, nl * sizeof(LokiPruneLevel), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess ||
+      cudaMemcpyAsync(base + o_si, seg_idx, nl * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(base + o_th, thresholds, nl * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "copy of the job tables failed");
+  note_launch();
+  prune_block_run_kernel<<<(unsigned)njobs, kRunThreads, smem, s>>>(
+      reinterpret_cast<const LokiPruneJob*>(base),
+      reinterpret_cast<const LokiPruneLevel*>(base + o_lv),
+      reinterpret_cast<const int32_t*>(base + o_si), reinterpret_cast<const double*>(base + o_th),
+      nlevels, sp, SK, max_sugg, batch_size);
+  return check_launch("prune_block_run");
+}
+
+// ---------------------------------------------------------------------------
+// level-synchronous batch: every step of a level is one launch over all jobs
+// (blockIdx.y = job), so a batch of jobs costs the launches of one run and
+// each step spreads over the whole GPU. The device code is that of
+// loki_prune_run; the counters, records and results of job j are those a
+// loki_prune_run of job j writes.
+// ---------------------------------------------------------------------------
+
+namespace loki {
+
+struct BatchTabs {
+  const LokiPruneJob* jobs;
+  const LokiPruneLevel* levels;  // [job][level]
+  const int32_t* seg_idx;        // [job][level]
+  const double* thr;             // [job][level]
+  int32_t nlevels;
+};
+
+__device__ __forceinline__ int64_t* job_pos(const LokiPruneWork& w) {
+  const int64_t sums = (int64_t)max((int64_t)1, (w.child_cap + kScanBlock - 1) / kScanBlock) * 8;
+  return reinterpret_cast<int64_t*>(reinterpret_cast<char*>(w.sscan) + sums);
+}
+
+__global__ void bj_seed_kernel(BatchTabs T) {
+  const LokiPruneJob& J = T.jobs[blockIdx.x];
+  int64_t* cnt = J.run.counts;
+  cnt[0] = J.seed_n;
+  for (int k = 1; k < 8; ++k) cnt[k] = 0;
+  unsigned* keys = reinterpret_cast<unsigned*>(J.run.work.minmax);
+  keys[0] = 0xFFFFFFFFu;
+  keys[1] = 0u;
+  *J.run.ovf_flag = 0;
+}
+
+__global__ void bj_branch_kernel(BatchTabs T, int l) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneLevel& D = T.levels[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  const LokiPruneWork& w = J.run.work;
+  const int64_t n = J.run.counts[0];
+  const double* leaves = J.run.trees[(l - 1) & 1].leaves;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    branch_one(D, leaves, i, reinterpret_cast<LokiBranchInfo*>(w.info), w.offsets, J.dev_err,
+               nullptr);
+}
+
+// The two scans of a level, per job: mode 0 the child counts of the parents
+// (in place in offsets, scratch w.scan), mode 1 the score >= threshold flags
+// of the children (into the positions after w.sscan's sums).
+__device__ __forceinline__ void bj_scan_args(const BatchTabs& T, int l, int mode,
+                                             const void** in, int64_t** out, int64_t** sums,
+                                             int64_t* n, double* thr) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneWork& w = J.run.work;
+  if (mode == 0) {
+    *in = w.offsets;
+    *out = w.offsets;
+    *sums = reinterpret_cast<int64_t*>(w.scan);
+    *n = J.run.counts[0];
+    *thr = 0.0;
+  } else {
+    *in = w.child_scores;
+    *out = job_pos(w);
+    *sums = reinterpret_cast<int64_t*>(w.sscan);
+    *n = J.run.counts[1];
+    *thr = T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  }
+}
+
+template <bool FLAGS>
+__global__ void __launch_bounds__(kScanBlock) bj_scan_block_kernel(BatchTabs T, int l) {
+  __shared__ int64_t warp_tot[32];
+  const void* in;
+  int64_t *out, *sums, n;
+  double thr;
+  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  const int64_t ntiles = (n + kScanBlock - 1) / kScanBlock;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+    scan_tile<FLAGS>(in, n, thr, out, sums, t, warp_tot);
+}
+
+template <bool FLAGS>
+__global__ void __launch_bounds__(kScanBlock) bj_scan_sums_kernel(BatchTabs T, int l) {
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t carry;
+  const void* in;
+  int64_t *out, *sums, n;
+  double thr;
+  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nblocks = (n + kScanBlock - 1) / kScanBlock;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nblocks; base += kScanBlock) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t x = i < nblocks ? sums[i] : 0;
+    int64_t v = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+      if (lane >= o) v += y;
+    }
+    if (lane == 31) warp_tot[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const int64_t incl = v + (warp ? warp_tot[warp - 1] : 0);
+    const int64_t c = carry;
+    if (i < nblocks) sums[i] = c + incl - x;
+    __syncthreads();
+    if (threadIdx.x == kScanBlock - 1) carry = c + incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+template <bool FLAGS>
+__global__ void __launch_bounds__(kScanBlock) bj_scan_add_kernel(BatchTabs T, int l) {
+  const void* in;
+  int64_t *out, *sums, n;
+  double thr;
+  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  for (int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kScanBlock)
+    out[i] += sums[i / kScanBlock];
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_score_kernel(BatchTabs T, int l, LokiScoreSpec sp, ScoreK SK) {
+  extern __shared__ float tiles[];
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const float* seg = J.ffa_fold + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int warp = threadIdx.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(D.nbins, sp.wmax);
+  int64_t* cnt = R.counts;
+  const int64_t n_par = cnt[0];
+  const int64_t total = w.offsets[n_par];
+  const int64_t n_child = total > w.child_cap ? 0 : total;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[1] = n_child;
+    LokiPruneLevelStats* st = R.stats + (l - 1);
+    st->n_parents = n_par;
+    st->n_children = total;
+    st->n_valid = total;
+    if (total > w.child_cap) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+  }
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_child;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    score_tile(D, in.leaves, in.folds, n_par, reinterpret_cast<LokiBranchInfo*>(w.info),
+               w.offsets, n_child, seg, sp, SK, w.child_scores, w.child_idx, w.child_phase,
+               reinterpret_cast<unsigned*>(w.minmax), tile, t * 32);
+    __syncwarp();
+  }
+}
+
+__global__ void bj_scatter_kernel(BatchTabs T, int l) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneWork& w = J.run.work;
+  const double thr = T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  const int64_t n = J.run.counts[1];
+  const int64_t* pos = job_pos(w);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if ((double)w.child_scores[i] >= thr) w.surv[pos[i]] = i;
+}
+
+// one block per job: the survivor count, and the overflow rule when it
+// exceeds max_sugg
+__global__ void __launch_bounds__(kSelThreads)
+bj_overflow_kernel(BatchTabs T, int l, int64_t max_sugg, int64_t batch) {
+  const LokiPruneJob& J = T.jobs[blockIdx.x];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  int64_t* cnt = R.counts;
+  const int64_t n_sel = job_pos(w)[cnt[1]];
+  const int64_t n_par = cnt[0];
+  __syncthreads();  // every thread has read the counters
+  if (threadIdx.x == 0) cnt[2] = n_sel;
+  if (n_sel <= max_sugg) return;  // uniform over the block
+  if (threadIdx.x == 0) *R.ovf_flag = 1;
+  select_overflow_block(w.child_scores, w.offsets, n_par, batch,
+                        T.thr[(size_t)blockIdx.x * T.nlevels + (l - 1)], max_sugg, w.surv,
+                        cnt + 2, w.ovf_thr, w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys));
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32) bj_emit_kernel(BatchTabs T, int l) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const LokiPruneTree& out = R.trees[l & 1];
+  const float* seg = J.ffa_fold + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int warp = threadIdx.x >> 5;
+  const int64_t n_par = R.counts[0], n_surv = R.counts[2];
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_surv;
+       t += (int64_t)gridDim.x * kPruneWarps)
+    emit_tile(D, in.leaves, in.folds, reinterpret_cast<LokiBranchInfo*>(w.info), w.offsets,
+              n_par, seg, w.surv, n_surv, w.child_scores, w.child_idx, w.child_phase,
+              out.leaves, out.folds, out.scores, out.scores_ep, out.backtracks, t * 32);
+}
+
+__global__ void bj_bt_kernel(BatchTabs T, int l, int row) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneRun& R = J.run;
+  if (!R.bt_hist) return;
+  const int64_t start = R.counts[3], rows = R.counts[2];
+  if (start + rows > R.bt_rows) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+    return;
+  }
+  const int32_t* bt = R.trees[l & 1].backtracks;
+  int32_t* h = R.bt_hist + start * row;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows * row;
+       i += (int64_t)gridDim.x * blockDim.x)
+    h[i] = bt[i];
+}
+
+// one block per job: the best leaf of the new tree, then the level's end
+__global__ void __launch_bounds__(1024) bj_best_kernel(BatchTabs T, int l, int row_leaf) {
+  const LokiPruneJob& J = T.jobs[blockIdx.x];
+  const LokiPruneRun& R = J.run;
+  int64_t* cnt = R.counts;
+  const int64_t n = cnt[2];
+  if (R.best_leaves && R.best_scores)
+    block_best(R.trees[l & 1].scores, n, R.trees[l & 1].leaves, row_leaf,
+               R.best_leaves + (int64_t)(l - 1) * row_leaf, R.best_scores + (l - 1));
+  __syncthreads();  // every thread has read the count
+  if (threadIdx.x == 0)
+    level_end(cnt, reinterpret_cast<unsigned*>(R.work.minmax), R.ovf_flag, R.stats + (l - 1));
+}
+
+}  // namespace loki
+
+// Host checks of a batch and the copy of its tables into dev_scratch; fills
+// the grid sizes of the enqueue.
+struct BatchShape {
+  int nbins, poly_order;
+  int64_t max_par, max_child;
+};
+
+static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
+                        const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
+                        const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                        void* dev_scratch, int64_t dev_scratch_bytes, cudaStream_t s,
+                        BatchShape* shape) {
+  if (!jobs || njobs < 1 || njobs > 65535 || !levels || !seg_idx || !thresholds ||
+      nlevels < 1 || !spec || !dev_scratch)
+    return set_error(LOKI_ERR_INVALID, "null pointer, no job (or above 65535) or no level");
+  if (max_sugg < 1 || batch_size < 1) return set_error(LOKI_ERR_INVALID, "bad sizes");
+  if (dev_scratch_bytes < loki_prune_run_blocks_scratch_bytes(njobs, nlevels))
+    return set_error(LOKI_ERR_CAPACITY, "job scratch below %lld bytes",
+                     (long long)loki_prune_run_blocks_scratch_bytes(njobs, nlevels));
+  const int nb = levels[0].nbins, P = levels[0].poly_order;
+  int64_t max_par = 0, max_child = 0;
+  for (int64_t k = 0; k < (int64_t)njobs * nlevels; ++k) {
+    int rc = check_prune(&levels[k]);
+    if (rc) return rc;
+    if (levels[k].basis != levels[0].basis || levels[k].poly_order != P ||
+        levels[k].nbins != nb)
+      return set_error(LOKI_ERR_INVALID, "levels of different trees");
+  }
+  if (levels[0].basis == 2)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree runs in loki_prune_run");
+  for (int j = 0; j < njobs; ++j) {
+    const LokiPruneJob& J = jobs[j];
+    const LokiPruneRun& R = J.run;
+    const LokiPruneWork& w = R.work;
+    if (!J.ffa_fold || J.seg_stride < 1 || !J.dev_err || J.seed_n < 0 || J.seed_n > max_sugg)
+      return set_error(LOKI_ERR_INVALID, "job %d: bad fold, error word or seed", j);
+    if (R.trees[0].cap < max_sugg || R.trees[1].cap < max_sugg || w.par_cap < max_sugg ||
+        w.child_cap < 1 || w.ovf_cap < max_sugg + w.child_cap + 1)
+      return set_error(LOKI_ERR_CAPACITY, "job %d: workspace below max_sugg / child_cap", j);
+    if (!R.counts || !R.ovf_flag || !R.stats || !w.info || !w.offsets || !w.scan ||
+        !w.child_scores || !w.child_idx || !w.child_phase || !w.surv || !w.sscan || !w.minmax ||
+        !w.ovf_ids || !w.ovf_keys || !w.ovf_thr)
+      return set_error(LOKI_ERR_INVALID, "job %d: null workspace pointer", j);
+    if (w.scan_bytes < loki_scan_scratch_bytes(w.par_cap + 1) ||
+        w.sscan_bytes <
+            loki_scan_scratch_bytes(w.child_cap) + (w.child_cap + 1) * (int64_t)sizeof(int64_t))
+      return set_error(LOKI_ERR_CAPACITY, "job %d: scan scratch below par_cap / child_cap", j);
+    for (int t = 0; t < 2; ++t)
+      if (!R.trees[t].leaves || !R.trees[t].folds || !R.trees[t].scores ||
+          !R.trees[t].scores_ep || !R.trees[t].backtracks)
+        return set_error(LOKI_ERR_INVALID, "job %d: null tree pointer", j);
+    max_par = std::max(max_par, w.par_cap);
+    max_child = std::max(max_child, w.child_cap);
+  }
+  int rc = prune_spec_check(spec, nb);
+  if (rc) return rc;
+  const int64_t nl = (int64_t)njobs * nlevels;
+  char* base = reinterpret_cast<char*>(dev_scratch);
+  const int64_t o_lv = ((int64_t)njobs * sizeof(LokiPruneJob) + 255) / 256 * 256;
+  const int64_t o_si = o_lv + (nl * (int64_t)sizeof(LokiPruneLevel) + 255) / 256 * 256;
+  const int64_t o_th = o_si + (nl * 4 + 255) / 256 * 256;
+  if (cudaMemcpyAsync(base, jobs, njobs * sizeof(LokiPruneJob), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(base + o_lv, levels, nl * sizeof(LokiPruneLevel), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess ||
+      cudaMemcpyAsync(base + o_si, seg_idx, nl * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(base + o_th, thresholds, nl * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "copy of the job tables failed");
+  shape->nbins = nb;
+  shape->poly_order = P;
+  shape->max_par = max_par;
+  shape->max_child = max_child;
+  return LOKI_OK;
+}
+
+// The kernels of a batch over tables already in dev_scratch (no host
+// access to them: the enqueue can be captured in a CUDA graph and replayed
+// after new tables of the same shape are copied in).
+static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
+                         const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
+                         const BatchShape& shape, cudaStream_t s) {
+  const int nb = shape.nbins, P = shape.poly_order;
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, nb);
+  const int smem = score_smem_bytes(nb, sp.wmax, kPruneWarps);
+  if (smem > 200 * 1024)
+    return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
+  if (smem > 48 * 1024 && set_smem_limit(bj_score_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "device query failed");
+  const int64_t nl = (int64_t)njobs * nlevels;
+  char* base = reinterpret_cast<char*>(dev_scratch);
+  const int64_t o_lv = ((int64_t)njobs * sizeof(LokiPruneJob) + 255) / 256 * 256;
+  const int64_t o_si = o_lv + (nl * (int64_t)sizeof(LokiPruneLevel) + 255) / 256 * 256;
+  const int64_t o_th = o_si + (nl * 4 + 255) / 256 * 256;
+  BatchTabs T;
+  T.jobs = reinterpret_cast<const LokiPruneJob*>(base);
+  T.levels = reinterpret_cast<const LokiPruneLevel*>(base + o_lv);
+  T.seg_idx = reinterpret_cast<const int32_t*>(base + o_si);
+  T.thr = reinterpret_cast<const double*>(base + o_th);
+  T.nlevels = nlevels;
+  // per-job grids of a few waves of the GPU in total, at least one block
+  auto per_job = [&](int64_t waves_blocks, int64_t cap_blocks) {
+    return (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>(cap_blocks, (waves_blocks + njobs - 1) / njobs));
+  };
+  const int64_t max_par = shape.max_par, max_child = shape.max_child;
+  const unsigned g_par = per_job(8 * nsm, (max_par + 255) / 256);
+  const unsigned g_scan_p = per_job(2 * nsm, (max_par + 1 + kScanBlock - 1) / kScanBlock);
+  const unsigned g_scan_c = per_job(2 * nsm, (max_child + kScanBlock - 1) / kScanBlock);
+  const unsigned g_score =
+      per_job(6 * nsm, (max_child + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
+  const unsigned g_flat = per_job(8 * nsm, (max_child + 255) / 256);
+  const unsigned g_emit =
+      per_job(6 * nsm, (max_par + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
+  const int row_bt = P + 2, row_leaf = (P + 2) * 2;
+  note_launch();
+  bj_seed_kernel<<<(unsigned)njobs, 1, 0, s>>>(T);
+  for (int l = 1; l <= nlevels; ++l) {
+    for (int i = 0; i < 13; ++i) note_launch();
+    bj_branch_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l);
+    bj_scan_block_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_scan_sums_kernel<false><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_scan_add_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
+    bj_scan_block_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_scan_sums_kernel<true><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_scan_add_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
+    bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l);
+    bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size);
+    bj_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+    bj_bt_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, row_bt);
+    bj_best_kernel<<<(unsigned)njobs, 1024, 0, s>>>(T, l, row_leaf);
+    int rc = check_launch("prune_run_batch");
+    if (rc) return rc;
+  }
+  return LOKI_OK;
+}
+
+extern "C" int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs,
+                                    const LokiPruneLevel* levels, const int32_t* seg_idx,
+                                    const double* thresholds, int32_t nlevels,
+                                    const LokiScoreSpec* spec, int64_t max_sugg,
+                                    int64_t batch_size, void* dev_scratch,
+                                    int64_t dev_scratch_bytes, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  BatchShape shape;
+  int rc = batch_tables(jobs, njobs, levels, seg_idx, thresholds, nlevels, spec, max_sugg,
+                        batch_size, dev_scratch, dev_scratch_bytes, s, &shape);
+  if (rc) return rc;
+  return batch_enqueue(dev_scratch, njobs, nlevels, spec, max_sugg, batch_size, shape, s);
+}
+
+extern "C" int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
+                                       const LokiPruneLevel* levels, const int32_t* seg_idx,
+                                       const double* thresholds, int32_t nlevels,
+                                       const LokiScoreSpec* spec, int64_t max_sugg,
+                                       int64_t batch_size, void* dev_scratch,
+                                       int64_t dev_scratch_bytes, int64_t* shape_out,
+                                       void* stream) {
+  if (!shape_out) return set_error(LOKI_ERR_INVALID, "null shape pointer");
+  BatchShape shape;
+  int rc = batch_tables(jobs, njobs, levels, seg_idx, thresholds, nlevels, spec, max_sugg,
+                        batch_size, dev_scratch, dev_scratch_bytes, (cudaStream_t)stream,
+                        &shape);
+  if (rc) return rc;
+  shape_out[0] = shape.nbins;
+  shape_out[1] = shape.poly_order;
+  shape_out[2] = shape.max_par;
+  shape_out[3] = shape.max_child;
+  return LOKI_OK;
+}
+
+extern "C" int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
+                                        const LokiScoreSpec* spec, int64_t max_sugg,
+                                        int64_t batch_size, const int64_t* shape_in,
+                                        void* stream) {
+  if (!dev_scratch || !spec || !shape_in || njobs < 1 || njobs > 65535 || nlevels < 1 ||
+      max_sugg < 1 || batch_size < 1)
+    return set_error(LOKI_ERR_INVALID, "bad batch enqueue arguments");
+  BatchShape shape;
+  shape.nbins = (int)shape_in[0];
+  shape.poly_order = (int)shape_in[1];
+  shape.max_par = shape_in[2];
+  shape.max_child = shape_in[3];
+  if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
+      shape.max_par < 1 || shape.max_child < 1)
+    return set_error(LOKI_ERR_INVALID, "bad batch shape");
+  int rc = prune_spec_check(spec, shape.nbins);
+  if (rc) return rc;
+  return batch_enqueue(dev_scratch, njobs, nlevels, spec, max_sugg, batch_size, shape,
+                       (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// batched ascend and read-back of many jobs' final trees
+// ---------------------------------------------------------------------------
+
+namespace loki {
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_batch_kernel(const LokiAscendJob* __restrict__ jobs, int nseg, LokiScoreSpec sp,
+                          ScoreK SK) {
+  extern __shared__ float tiles[];
+  const LokiAscendJob& J = jobs[blockIdx.y];
+  const LokiPruneLevel& D = J.lvl;
+  const int warp = threadIdx.x >> 5;
+  const int stride = score_stride(D.nbins, sp.wmax);
+  float* acc = tiles + (size_t)warp * 32 * (2 * D.nbins + stride);
+  float* tile = acc + 32 * 2 * D.nbins;
+  const int64_t n = *J.n_dev;
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    ascend_tile(D, J.leaves, J.folds, J.scores, J.scores_ep, n, nseg, J.tm_seg, J.dt_seg,
+                J.seg_idx, J.ffa_fold, J.seg_stride, sp, SK, acc, tile, t * 32);
+    __syncwarp();  // the accumulators are reused by the next tile
+  }
+}
+
+// Block y copies part y: src[y][0 .. bytes[y]) to dst + off[y] (16-byte
+// words where both ends allow, else bytes).
+__global__ void gather_parts_kernel(const LokiGatherPart* __restrict__ parts,
+                                    char* __restrict__ dst) {
+  const LokiGatherPart& P = parts[blockIdx.y];
+  const char* src = reinterpret_cast<const char*>(P.src);
+  char* d = dst + P.dst_off;
+  const int64_t nb = P.bytes;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(d)) & 15) == 0) {
+    const int64_t n16 = nb >> 4;
+    for (int64_t i = i0; i < n16; i += step)
+      reinterpret_cast<uint4*>(d)[i] = reinterpret_cast<const uint4*>(src)[i];
+    for (int64_t i = (n16 << 4) + i0; i < nb; i += step) d[i] = src[i];
+  } else {
+    for (int64_t i = i0; i < nb; i += step) d[i] = src[i];
+  }
+}
+
+}  // namespace loki
+
+extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs, int32_t nseg,
+                                       const LokiScoreSpec* spec, int64_t n_cap,
+                                       void* dev_scratch, int64_t dev_scratch_bytes,
+                                       void* stream) {
+  if (!jobs || njobs < 1 || njobs > 65535 || nseg < 1 || !spec || n_cap < 1 || !dev_scratch)
+    return set_error(LOKI_ERR_INVALID, "bad batched ascend arguments");
+  if (dev_scratch_bytes < (int64_t)njobs * (int64_t)sizeof(LokiAscendJob))
+    return set_error(LOKI_ERR_CAPACITY, "ascend job scratch below %lld bytes",
+                     (long long)njobs * (long long)sizeof(LokiAscendJob));
+  const int nb = jobs[0].lvl.nbins;
+  for (int j = 0; j < njobs; ++j) {
+    const LokiAscendJob& J = jobs[j];
+    int rc = check_prune(&J.lvl);
+    if (rc) return rc;
+    if (J.lvl.nbins != nb || J.lvl.basis != jobs[0].lvl.basis)
+      return set_error(LOKI_ERR_INVALID, "ascend jobs of different trees");
+    if (!J.n_dev || !J.leaves || !J.folds || !J.scores || !J.scores_ep || !J.tm_seg ||
+        !J.dt_seg || !J.seg_idx || !J.ffa_fold || J.seg_stride < 1 || !J.dev_err)
+      return set_error(LOKI_ERR_INVALID, "ascend job %d: null pointer or bad stride", j);
+  }
+  if (jobs[0].lvl.basis == 2)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit ascend runs per job");
+  int rc = prune_spec_check(spec, nb);
+  if (rc) return rc;
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, nb);
+  const int smem = kPruneWarps * 32 * (2 * nb + score_stride(nb, sp.wmax)) * (int)sizeof(float);
+  if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for ascend");
+  if (smem > 48 * 1024 && set_smem_limit(prune_ascend_batch_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  int dev = 0, nsm = 0, occ = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune_ascend_batch_kernel,
+                                                    kPruneWarps * 32, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "occupancy query failed");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(dev_scratch, jobs, njobs * sizeof(LokiAscendJob), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "copy of the ascend jobs failed");
+  const int64_t need = (n_cap + kPruneWarps * 32 - 1) / (kPruneWarps * 32);
+  const int64_t wave = ((int64_t)nsm * std::max(1, occ) + njobs - 1) / njobs;
+  const unsigned bx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, wave));
+  note_launch();
+  prune_ascend_batch_kernel<<<dim3(bx, njobs), kPruneWarps * 32, smem, s>>>(
+      reinterpret_cast<const LokiAscendJob*>(dev_scratch), nseg, sp, SK);
+  return check_launch("prune_ascend_batch");
+}
+
+extern "C" int loki_gather_parts(const LokiGatherPart* parts, int32_t nparts, void* dst,
+                                 int64_t dst_bytes, void* dev_scratch,
+                                 int64_t dev_scratch_bytes, void* stream) {
+  if (!parts || nparts < 1 || nparts > 65535 || !dst || !dev_scratch)
+    return set_error(LOKI_ERR_INVALID, "bad gather arguments");
+  if (dev_scratch_bytes < (int64_t)nparts * (int64_t)sizeof(LokiGatherPart))
+    return set_error(LOKI_ERR_CAPACITY, "gather scratch below %lld bytes",
+                     (long long)nparts * (long long)sizeof(LokiGatherPart));
+  int64_t maxb = 0;
+  for (int i = 0; i < nparts; ++i) {
+    if (parts[i].bytes < 0 || parts[i].dst_off < 0 ||
+        parts[i].dst_off + parts[i].bytes > dst_bytes || (parts[i].bytes > 0 && !parts[i].src))
+      return set_error(LOKI_ERR_INVALID, "gather part %d outside the destination", i);
+    maxb = std::max(maxb, parts[i].bytes);
+  }
+  if (maxb == 0) return LOKI_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(dev_scratch, parts, nparts * sizeof(LokiGatherPart),
+                      cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "copy of the gather parts failed");
+  const unsigned bx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(64, (maxb / 16 + 255) / 256));
+  note_launch();
+  gather_parts_kernel<<<dim3(bx, nparts), 256, 0, s>>>(
+      reinterpret_cast<const LokiGatherPart*>(dev_scratch), reinterpret_cast<char*>(dst));
+  return check_launch("gather_parts");
 }

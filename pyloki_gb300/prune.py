@@ -1017,12 +1017,17 @@ class Pruning:
         if not 0 <= nlev <= self.dyp.nsegments - 1:
             msg = f"levels must be in [0, {self.dyp.nsegments - 1}], got {levels}"
             raise ValueError(msg)
+        dr = self._device_run_obj(ref_seg, nlev, ascend)
+        dr.launch(graph)
+        return dr
+
+    def _device_run_obj(self, ref_seg: int, nlev: int, ascend: bool):
+        """The cached ``_DeviceRun`` of (reference segment, levels, ascend)."""
         key = (ref_seg, nlev, ascend)
         dr = self.__dict__.setdefault("_device_runs", {}).get(key)
         if dr is None:
             dr = _DeviceRun(self, ref_seg, nlev, ascend=ascend)
             self.__dict__.setdefault("_device_runs", {})[key] = dr
-        dr.launch(graph)
         return dr
 
     def _device_finish(self, dr, graph: bool) -> None:
@@ -1281,17 +1286,23 @@ class _DeviceRun:
         self.graph = None
         self.need_child = self.need_bt = 0
 
-    def _enqueue(self) -> None:
-        """The run from the fold mirror: seed (leaves from the grid, folds
-        and scores from the mirror), then every level."""
+    def _fold_src(self):
+        """The FFA fold the run reads: the run's mirror (a captured graph
+        keeps its address across folds) or, for the batched drivers, the
+        fold itself."""
+        return self.__dict__.get("_direct_fold", self.bufs.mem["mirror"])
+
+    def _seed_enqueue(self) -> None:
+        """The seed tree from the fold: leaves from the grid, folds and
+        scores from the reference segment's rows."""
         prn, b = self.prn, self.bufs
         t0, seed = b.trees[0], self.seed
         n = seed.size
         nb = prn.dyp.cfg.nbins
         stride = int(np.prod(prn.dyp.fold.shape[1:]))
-        mirror = b.mem["mirror"]
+        src = self._fold_src()
         t0["leaves"][:n].copy_(seed.leaves)
-        t0["folds"][:n].copy_(mirror[self.ref_seg * stride:(self.ref_seg + 1) * stride]
+        t0["folds"][:n].copy_(src[self.ref_seg * stride:(self.ref_seg + 1) * stride]
                               .view(n, 2, nb))
         _lib.check(prn._lib.loki_snr_score_batch(
             _lib.ptr(t0["folds"]), n, nb, prn.spec, _lib.ptr(t0["scores"]), prn._stream()))
@@ -1299,22 +1310,75 @@ class _DeviceRun:
         b.mem["seed_scores"][:n].copy_(t0["scores"][:n])  # level-0 statistics
         t0["bt"][:n].zero_()
         prn._err.zero_()
+
+    def _ascend_enqueue(self) -> None:
+        """The ascend over the last level's survivors (counts[0] after the run)."""
+        prn, b = self.prn, self.bufs
+        stride = int(np.prod(prn.dyp.fold.shape[1:]))
+        d, tm_d, dt_d, si_d, nseg = self.asc
+        t = b.trees[self.nlev & 1]
+        _lib.check(prn._lib.loki_prune_ascend_dev(
+            d, _lib.ptr(t["leaves"]), _lib.ptr(t["folds"]), _lib.ptr(t["scores"]),
+            _lib.ptr(t["scores_ep"]), _lib.ptr(b.mem["counts"]), prn.max_sugg, nseg,
+            _lib.ptr(tm_d), _lib.ptr(dt_d), _lib.ptr(si_d), _lib.ptr(self._fold_src()), stride,
+            prn.spec, _lib.ptr(prn._err), prn._stream()))
+
+    def ascend_job(self) -> _lib.LokiAscendJob:
+        """This run's ascend as a job of ``loki_prune_ascend_batch``."""
+        prn, b = self.prn, self.bufs
+        d, tm_d, dt_d, si_d, _ = self.asc
+        t = b.trees[self.nlev & 1]
+        j = _lib.LokiAscendJob()
+        j.lvl = d
+        j.leaves, j.folds = _lib.ptr(t["leaves"]), _lib.ptr(t["folds"])
+        j.scores, j.scores_ep = _lib.ptr(t["scores"]), _lib.ptr(t["scores_ep"])
+        j.n_dev = _lib.ptr(b.mem["counts"])
+        j.tm_seg, j.dt_seg, j.seg_idx = _lib.ptr(tm_d), _lib.ptr(dt_d), _lib.ptr(si_d)
+        j.ffa_fold = _lib.ptr(self._fold_src())
+        j.seg_stride = int(np.prod(prn.dyp.fold.shape[1:]))
+        j.dev_err = _lib.ptr(prn._err)
+        return j
+
+    def tree_parts(self, n: int):
+        """(device tensor, bytes) of the final tree's first n rows: leaves,
+        scores, scores_ep."""
+        t = self.bufs.trees[self.nlev & 1]
+        P = self.prn.poly_order
+        return [(t["leaves"], n * (P + 2) * 2 * 8), (t["scores"], n * 4),
+                (t["scores_ep"], n * 4)]
+
+    def job(self) -> _lib.LokiPruneJob:
+        """This run as a job of the batched drivers (after the seed)."""
+        prn, b = self.prn, self.bufs
+        j = _lib.LokiPruneJob()
+        j.ffa_fold = _lib.ptr(self._fold_src())
+        j.seg_stride = int(np.prod(prn.dyp.fold.shape[1:]))
+        j.seed_n = self.seed.size
+        j.run = b.run
+        j.dev_err = _lib.ptr(prn._err)
+        return j
+
+    def prepare_block(self) -> None:
+        """The seed, read from the fold itself, for a batched driver."""
+        self._direct_fold = self.prn.dyp.fold.reshape(-1)
+        self._seed_enqueue()
+
+    def _enqueue(self) -> None:
+        """The run from the fold mirror: the seed, then every level."""
+        prn, b = self.prn, self.bufs
+        self._seed_enqueue()
         if self.nlev == 0:
             return
+        stride = int(np.prod(prn.dyp.fold.shape[1:]))
         _lib.check(prn._lib.loki_prune_run(
-            self.descs, self.nlev, _lib.ptr(mirror), stride, self.seg_idx.ctypes.data,
-            self.thresholds.ctypes.data, prn.spec, n, prn.max_sugg, prn.batch_size,
-            C.byref(b.run), _lib.ptr(prn._err), prn._stream()))
-        if self.ascend:  # survivors of the last level: counts[0] after the run
-            d, tm_d, dt_d, si_d, nseg = self.asc
-            t = b.trees[self.nlev & 1]
-            _lib.check(prn._lib.loki_prune_ascend_dev(
-                d, _lib.ptr(t["leaves"]), _lib.ptr(t["folds"]), _lib.ptr(t["scores"]),
-                _lib.ptr(t["scores_ep"]), _lib.ptr(b.mem["counts"]), prn.max_sugg, nseg,
-                _lib.ptr(tm_d), _lib.ptr(dt_d), _lib.ptr(si_d), _lib.ptr(mirror), stride,
-                prn.spec, _lib.ptr(prn._err), prn._stream()))
+            self.descs, self.nlev, _lib.ptr(b.mem["mirror"]), stride, self.seg_idx.ctypes.data,
+            self.thresholds.ctypes.data, prn.spec, self.seed.size, prn.max_sugg,
+            prn.batch_size, C.byref(b.run), _lib.ptr(prn._err), prn._stream()))
+        if self.ascend:
+            self._ascend_enqueue()
 
     def launch(self, graph: bool) -> None:
+        self.__dict__.pop("_direct_fold", None)  # the graphs read the mirror
         fold = self.prn.dyp.fold.reshape(-1)
         self.bufs.mem["mirror"][: fold.numel()].copy_(fold)  # outside any graph
         if not graph:
@@ -1388,16 +1452,16 @@ class _DeviceRun:
                           score_max=float(s0.max()) if seed.size else 0.0,
                           n_branches=seed.size, n_leaves=seed.size, n_leaves_phy=seed.size,
                           n_leaves_surv=seed.size)]
-        for lvl in range(1, last + 1):
-            r = stats[lvl - 1]
-            n_child = int(r["n_children"])
+        seg, thr = self.seg_idx[:last].tolist(), self.thresholds[:last].tolist()
+        f = stats[:last]
+        for lvl, (npar, nch, nval, nsurv, smin, smax) in enumerate(
+                zip(f["n_parents"].tolist(), f["n_children"].tolist(), f["n_valid"].tolist(),
+                    f["n_surv"].tolist(), f["score_min"].tolist(), f["score_max"].tolist()),
+                start=1):
             out.append(PruneStats(
-                level=lvl, seg_idx=int(self.seg_idx[lvl - 1]),
-                threshold=float(self.thresholds[lvl - 1]),
-                score_min=float(r["score_min"]) if n_child else 0.0,
-                score_max=float(r["score_max"]) if n_child else 0.0,
-                n_branches=int(r["n_parents"]), n_leaves=n_child,
-                n_leaves_phy=int(r["n_valid"]), n_leaves_surv=int(r["n_surv"])))
+                level=lvl, seg_idx=seg[lvl - 1], threshold=thr[lvl - 1],
+                score_min=smin if nch else 0.0, score_max=smax if nch else 0.0,
+                n_branches=npar, n_leaves=nch, n_leaves_phy=nval, n_leaves_surv=nsurv))
         return out
 
     def finish(self, prn: Pruning) -> bool:
@@ -1637,6 +1701,200 @@ class PruneBatch:
         for st in self._streams[:ns]:
             producer.wait_stream(st)
         return out
+
+
+class PruneBlockBatch(PruneBatch):
+    """Device-resident runs of many (fold, reference segment) jobs enqueued
+    together. ``driver="batch"`` (``loki_prune_run_batch``): every step of a
+    level is one launch over all jobs, so the batch pays the launches of one
+    run. ``driver="blocks"`` (``loki_prune_run_blocks``): one thread block
+    per job walks every level with block barriers between the steps, a
+    single launch for the batch.
+
+    Up to ``max_jobs`` jobs go in one launch, each with its own ``Pruning``
+    and run buffers (kept across calls, rebound to each job's fold). The
+    ascend, the read-back and the results are those of ``PruneBatch``; a job
+    that outgrows its workspace is repeated with grown buffers through
+    ``loki_prune_run``. Taylor and Chebyshev trees; circular-orbit trees go
+    through ``PruneBatch``.
+    """
+
+    def __init__(self, threshold_scheme, *, max_jobs: int = 152, driver: str = "batch",
+                 **kwargs) -> None:
+        super().__init__(threshold_scheme, n_streams=1, graph=False, **kwargs)
+        if int(max_jobs) < 1:
+            msg = f"max_jobs must be greater than 0, got {max_jobs}"
+            raise ValueError(msg)
+        if driver not in ("batch", "blocks"):
+            msg = f"driver must be 'batch' or 'blocks', got {driver!r}"
+            raise ValueError(msg)
+        self.max_jobs = int(max_jobs)
+        self.driver = driver
+        self._slots: list = []
+        self._scratch = None
+
+    def _enqueue_batch(self, lib, dev, st, n: int, nlev: int, args, shape) -> None:
+        """The batch's kernels over the tables just copied: enqueued directly
+        the first time a shape is seen, then captured once in a CUDA graph
+        and replayed (the tables are read on the device, so a replay runs
+        whatever jobs were copied in)."""
+        key = (n, nlev, tuple(int(v) for v in shape), args[1], args[2])
+        graphs = self.__dict__.setdefault("_graphs", {})
+        g = graphs.get(key)
+        if g is None and key not in self.__dict__.setdefault("_seen", set()):
+            self._seen.add(key)
+            _lib.check(lib.loki_prune_batch_enqueue(_lib.ptr(self._scratch), n, nlev, *args,
+                                                    shape.ctypes.data, _lib.stream_ptr(st)))
+            return
+        if g is None:
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(st)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side), torch.cuda.graph(g, stream=side):
+                _lib.check(lib.loki_prune_batch_enqueue(
+                    _lib.ptr(self._scratch), n, nlev, *args, shape.ctypes.data,
+                    _lib.stream_ptr(side)))
+            st.wait_stream(side)
+            graphs[key] = g
+        g.replay()
+
+    def _slot(self, k: int, dyp) -> Pruning:
+        while len(self._slots) <= k:
+            self._slots.append(None)
+        prn = self._slots[k]
+        if prn is not None and prn.dyp is not dyp:
+            try:
+                prn.rebind(dyp)
+            except ValueError:
+                prn = None
+        if prn is None:
+            prn = self._slots[k] = Pruning(dyp, self.threshold_scheme, **self.kwargs)
+        return prn
+
+    def run(self, jobs, *, ascend: bool = True) -> list[dict]:
+        jobs = list(jobs)
+        if not jobs:
+            return []
+        first = self._slot(0, jobs[0][0])
+        if first.circular:
+            return PruneBatch.run(self, jobs, ascend=ascend)
+        if not first.device_run_supported:
+            msg = "the block driver covers time-domain trees without a parent hook"
+            raise ValueError(msg)
+        dev = jobs[0][0].device
+        st = torch.cuda.current_stream(dev)
+        out: list[dict] = [{} for _ in jobs]
+        lib = _lib.load()
+        for w0 in range(0, len(jobs), self.max_jobs):
+            wave = jobs[w0:w0 + self.max_jobs]
+            runs = []
+            for k, (dyp, ref) in enumerate(wave):
+                prn = self._slot(k, dyp)
+                prn._stream_ptr = None  # the current stream
+                dr = prn._device_run_obj(ref, dyp.nsegments - 1, ascend)
+                dr.prepare_block()
+                runs.append((prn, dr))
+            nlev = runs[0][1].nlev
+            n = len(runs)
+            if nlev > 0:
+                tab = (_lib.LokiPruneJob * n)()
+                lv = (_lib.LokiPruneLevel * (n * nlev))()
+                seg = np.empty((n, nlev), np.int32)
+                thr = np.empty((n, nlev), np.float64)
+                size = C.sizeof(_lib.LokiPruneLevel)
+                for i, (prn, dr) in enumerate(runs):
+                    tab[i] = dr.job()
+                    C.memmove(C.byref(lv, i * nlev * size), dr.descs, nlev * size)
+                    seg[i] = dr.seg_idx
+                    thr[i] = dr.thresholds
+                need = int(lib.loki_prune_run_blocks_scratch_bytes(n, nlev))
+                if self._scratch is None or self._scratch.numel() < need:
+                    self._scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+                    self._graphs = {}  # captured over the old scratch
+                p0 = runs[0][0]
+                args = (p0.spec, p0.max_sugg, p0.batch_size)
+                if self.driver == "blocks":
+                    _lib.check(lib.loki_prune_run_blocks(
+                        tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
+                        _lib.ptr(self._scratch), self._scratch.numel(), _lib.stream_ptr(st)))
+                else:
+                    shape = np.zeros(4, np.int64)
+                    _lib.check(lib.loki_prune_batch_tables(
+                        tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
+                        _lib.ptr(self._scratch), self._scratch.numel(), shape.ctypes.data,
+                        _lib.stream_ptr(st)))
+                    self._enqueue_batch(lib, dev, st, n, nlev, args, shape)
+            if ascend and nlev > 0:  # every job's ascend in one launch
+                ajobs = (_lib.LokiAscendJob * n)()
+                for i, (prn, dr) in enumerate(runs):
+                    ajobs[i] = dr.ascend_job()
+                p0 = runs[0][0]
+                abuf = self._dev_buf("ascend", n * C.sizeof(_lib.LokiAscendJob), dev)
+                _lib.check(lib.loki_prune_ascend_batch(
+                    ajobs, n, runs[0][1].asc[4], p0.spec, p0.max_sugg, _lib.ptr(abuf),
+                    abuf.numel(), _lib.stream_ptr(st)))
+            elif ascend:
+                for prn, dr in runs:
+                    dr._ascend_enqueue()
+            for prn, dr in runs:
+                dr.copy_stats_async()
+            st.synchronize()
+            ready = []
+            for prn, dr in runs:
+                stats, err, last, nf = dr.stats_host()
+                if err:  # a workspace to grow, or a device error to raise
+                    dr = prn._device_finish(dr, False)
+                    dr.copy_stats_async()
+                    st.synchronize()
+                    stats, err, last, nf = dr.stats_host()
+                ready.append((prn, dr, stats, last, nf))
+            host = self._read_trees(lib, dev, st, ready)
+            P = ready[0][0].poly_order
+            for i, (prn, dr, stats, last, nf) in enumerate(ready):
+                prn._scheme = dr.scheme
+                leaves_b, scores_b, ep_b = host[i]
+                leaves = np.frombuffer(leaves_b, np.float64).reshape(nf, P + 2, 2).copy()
+                out[w0 + i] = {
+                    "run_name": f"{dr.ref_seg:03d}_00", "scheme": dr.scheme.data.copy(),
+                    "param_sets": prn._report_host(leaves),
+                    "scores": np.frombuffer(scores_b, np.float32).copy(),
+                    "scores_ep": np.frombuffer(ep_b, np.float32).copy(),
+                    "level_stats": dr.level_stats(stats, last)}
+        return out
+
+    def _dev_buf(self, name: str, nbytes: int, dev):
+        bufs = self.__dict__.setdefault("_dev_bufs", {})
+        t = bufs.get(name)
+        if t is None or t.numel() < nbytes:
+            t = bufs[name] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=dev)
+        return t
+
+    def _read_trees(self, lib, dev, st, ready):
+        """Every job's final rows (leaves, scores, scores_ep) packed on the
+        device by one gather launch and read back with one copy."""
+        parts, offs, off = [], [], 0
+        for _, dr, _, _, nf in ready:
+            row = []
+            for t, nb in dr.tree_parts(nf):
+                parts.append((t, nb, off))
+                row.append((off, nb))
+                off += (nb + 15) // 16 * 16
+            offs.append(row)
+        packed = self._dev_buf("packed", off, dev)
+        pin = self.__dict__.get("_pin")
+        if pin is None or pin.numel() < off:
+            pin = self._pin = torch.empty(max(off, 256), dtype=torch.uint8, pin_memory=True)
+        tab = (_lib.LokiGatherPart * len(parts))()
+        for i, (t, nb, o) in enumerate(parts):
+            tab[i].src, tab[i].bytes, tab[i].dst_off = _lib.ptr(t), nb, o
+        pbuf = self._dev_buf("parts", len(parts) * C.sizeof(_lib.LokiGatherPart), dev)
+        _lib.check(lib.loki_gather_parts(tab, len(parts), _lib.ptr(packed), packed.numel(),
+                                         _lib.ptr(pbuf), pbuf.numel(), _lib.stream_ptr(st)))
+        if off:
+            pin[:off].copy_(packed[:off], non_blocking=True)
+        st.synchronize()
+        raw = pin.numpy()
+        return [[raw[o:o + nb].tobytes() for o, nb in row] for row in offs]
 
 
 def run_batch(jobs, threshold_scheme, *, n_streams: int = 8, graph: bool = True,

@@ -181,3 +181,79 @@ def test_prune_batch_rebinds_to_new_folds(cuda_device):
                 (s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max) for s in p.pstats]
             np.testing.assert_array_equal(g["scores"], p.world_tree.scores.cpu().numpy())
             np.testing.assert_array_equal(g["param_sets"], p.report())
+
+
+def _level_path_results(prn_factory, dyp, ref, d):
+    p = prn_factory()
+    p.initialize(ref)
+    for _ in range(dyp.nsegments - 1):
+        p.execute_iter()
+    p._do_ascend()
+    return ([(s.n_branches, s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+             for s in p.pstats], p.world_tree.scores.cpu().numpy(),
+            p.world_tree.scores_ep.cpu().numpy(), p.report())
+
+
+@pytest.mark.parametrize("name", ["prune_taylor", "prune_taylor_overflow", "prune_cheby",
+                                  "prune_taylor_quad", "prune_cheby_fixed"])
+@pytest.mark.parametrize("max_jobs", [3, 64])
+@pytest.mark.parametrize("driver", ["batch", "blocks"])
+def test_block_batch_matches_level_path(cuda_device, name, max_jobs, driver):
+    """One thread block per job (loki_prune_run_blocks): every job's level
+    records, final scores, ascend and report equal the level-by-level run's,
+    in one launch or in waves of three; the overflow fixture runs the
+    overflow rule inside the block."""
+    from pyloki_gb300.prune import PruneBlockBatch, Pruning
+
+    d, prn = _run(name, cuda_device)
+    dyp = prn.dyp
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]),
+              poly_basis=prn.poly_basis, use_moving_grid=prn.use_moving_grid)
+    refs = [0, 3, int(d["ref_seg"]), dyp.nsegments - 1, 5, 9, 12]
+    runner = PruneBlockBatch(d["thresholds"], max_jobs=max_jobs, driver=driver, **kw)
+    # the second call reuses the slots' buffers and runs; with the batch
+    # driver it captures the kernels in a CUDA graph, which the third replays
+    for _ in range(3):
+        got = runner.run([(dyp, r) for r in refs])
+        for ref, g in zip(refs, got, strict=True):
+            want = _level_path_results(lambda: Pruning(dyp, d["thresholds"], **kw), dyp, ref, d)
+            assert [(s.n_branches, s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+                    for s in g["level_stats"]] == want[0], ref
+            np.testing.assert_array_equal(g["scores"], want[1])
+            np.testing.assert_array_equal(g["scores_ep"], want[2])
+            np.testing.assert_array_equal(g["param_sets"], want[3])
+
+
+@pytest.mark.parametrize("driver", ["batch", "blocks"])
+def test_block_batch_grows_workspaces(cuda_device, driver):
+    """A job whose children outgrow the batched drivers' workspace is flagged
+    on the device and repeated with grown buffers: the results do not change."""
+    from pyloki_gb300.prune import PruneBlockBatch, Pruning
+
+    d, prn = _run("prune_taylor", cuda_device)
+    dyp = prn.dyp
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
+    runner = PruneBlockBatch(d["thresholds"], max_jobs=4, driver=driver, **kw)
+    for k in range(2):
+        runner._slot(k, dyp).device_child_cap = 64
+    refs = [int(d["ref_seg"]), 2]
+    got = runner.run([(dyp, r) for r in refs])
+    for ref, g in zip(refs, got, strict=True):
+        want = _level_path_results(lambda: Pruning(dyp, d["thresholds"], **kw), dyp, ref, d)
+        assert max(s.n_leaves for s in g["level_stats"]) > 64
+        np.testing.assert_array_equal(g["scores"], want[1])
+        np.testing.assert_array_equal(g["param_sets"], want[3])
+
+
+def test_block_batch_passes_circular_to_streams(cuda_device):
+    from pyloki_gb300.prune import PruneBlockBatch, run_batch
+
+    d, prn = _run("prune_circ", cuda_device)
+    dyp = prn.dyp
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
+    refs = [int(d["ref_seg"]), 1]
+    got = PruneBlockBatch(d["thresholds"], **kw).run([(dyp, r) for r in refs])
+    want = run_batch([(dyp, r) for r in refs], d["thresholds"], n_streams=2, **kw)
+    for g, w in zip(got, want, strict=True):
+        np.testing.assert_array_equal(g["scores"], w["scores"])
+        np.testing.assert_array_equal(g["param_sets"], w["param_sets"])
