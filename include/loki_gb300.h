@@ -690,6 +690,29 @@ int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
                              const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
                              const int64_t* shape_in, void* stream);
 
+/* One job of loki_prune_seed_batch: the seed tree of a run (the
+ * reference segment's n grid points, core/taylor.py:14-65 seeds): its leaves
+ * and fold rows are copied into the run's first tree and scored. */
+typedef struct {
+  const double* seed_leaves;  /* n x (poly_order + 2) x 2 */
+  const float* fold_rows;     /* n x 2 x nbins: the reference segment of the FFA fold */
+  int64_t n;
+  double* leaves_out;
+  float* folds_out;
+  float* scores_out;
+  float* scores_ep_out;
+  float* seed_scores_out;     /* the level-0 record */
+  int32_t* bt_out;            /* n x (poly_order + 2), cleared */
+  int32_t* dev_err;           /* cleared */
+} LokiSeedJob;
+
+/* The seeds of njobs runs in one launch (grid y = job); jobs (host array)
+ * are checked and copied into dev_scratch of at least
+ * njobs * sizeof(LokiSeedJob) bytes. */
+int loki_prune_seed_batch(const LokiSeedJob* jobs, int32_t njobs, int32_t nbins,
+                          int32_t poly_order, const LokiScoreSpec* spec, void* dev_scratch,
+                          int64_t dev_scratch_bytes, void* stream);
+
 /* One job of loki_prune_ascend_batch: the ascend of loki_prune_ascend_dev
  * (its level descriptor, final tree, device survivor count and per-segment
  * tables) for one run. */

@@ -178,6 +178,14 @@ class LokiPruneJob(C.Structure):
                 ("run", LokiPruneRun), ("dev_err", C.c_void_p)]
 
 
+class LokiSeedJob(C.Structure):
+    _fields_ = [("seed_leaves", C.c_void_p), ("fold_rows", C.c_void_p), ("n", C.c_int64),
+                ("leaves_out", C.c_void_p), ("folds_out", C.c_void_p),
+                ("scores_out", C.c_void_p), ("scores_ep_out", C.c_void_p),
+                ("seed_scores_out", C.c_void_p), ("bt_out", C.c_void_p),
+                ("dev_err", C.c_void_p)]
+
+
 class LokiAscendJob(C.Structure):
     _fields_ = [("lvl", LokiPruneLevel), ("leaves", C.c_void_p), ("folds", C.c_void_p),
                 ("scores", C.c_void_p), ("scores_ep", C.c_void_p), ("n_dev", C.c_void_p),
@@ -248,6 +256,8 @@ SIGNATURES: dict[str, tuple] = {
     "loki_prune_ascend_batch": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64, _P,
                                           _I64, _P]),
     "loki_gather_parts": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
+    "loki_prune_seed_batch": (C.c_int, [_P, _I32, _I32, _I32, C.POINTER(LokiScoreSpec), _P,
+                                        _I64, _P]),
     "loki_ffa_plan": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P]),
     "loki_ffa_level": (C.c_int, [C.POINTER(LokiFFALevel), _P, _P, _P, _P]),
     "loki_ffa_level_score": (C.c_int, [C.POINTER(LokiFFALevel), _P, C.POINTER(LokiScoreSpec),

@@ -3786,3 +3786,90 @@ extern "C" int loki_gather_parts(const LokiGatherPart* parts, int32_t nparts, vo
       reinterpret_cast<const LokiGatherPart*>(dev_scratch), reinterpret_cast<char*>(dst));
   return check_launch("gather_parts");
 }
+
+namespace loki {
+
+// Block y seeds job y: leaves copied, the segment rows copied into the tree
+// and scored (normalised e / sqrt(v), boxcar S/N as loki_snr_score_batch),
+// scores_ep and the seed record set, backtracks and the error word cleared.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_seed_batch_kernel(const LokiSeedJob* __restrict__ jobs, int nb, int P, LokiScoreSpec sp,
+                        ScoreK SK) {
+  extern __shared__ float tiles[];
+  const LokiSeedJob& J = jobs[blockIdx.y];
+  const int64_t n = J.n;
+  const int row_leaf = (P + 2) * 2, row_bt = P + 2;
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t gstep = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = gtid; i < n * row_leaf; i += gstep) J.leaves_out[i] = J.seed_leaves[i];
+  for (int64_t i = gtid; i < n * 2 * nb; i += gstep) J.folds_out[i] = J.fold_rows[i];
+  for (int64_t i = gtid; i < n * row_bt; i += gstep) J.bt_out[i] = 0;
+  if (gtid == 0) *J.dev_err = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tile = tiles + (size_t)warp * 32 * stride;
+  for (int64_t p0 = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32; p0 < n;
+       p0 += (int64_t)gridDim.x * kPruneWarps * 32) {
+    const int kmax = (int)min((int64_t)32, n - p0);
+    for (int k = 0; k < kmax; ++k) {
+      const float* src = J.fold_rows + (p0 + k) * 2 * nb;
+      float* trow = tile + k * stride;
+      for (int j = lane; j < nb; j += 32) trow[j] = __fdiv_rn(src[j], __fsqrt_rn(src[nb + j]));
+    }
+    __syncwarp();
+    if (lane < kmax) {
+      float s;
+      float* row = tile + lane * stride;
+      if (SK.pow2_64) score_row64_pow2(row, sp, SK, &s);
+      else score_row(row, nb, sp, &s);
+      J.scores_out[p0 + lane] = s;
+      J.scores_ep_out[p0 + lane] = s;
+      J.seed_scores_out[p0 + lane] = s;
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace loki
+
+extern "C" int loki_prune_seed_batch(const LokiSeedJob* jobs, int32_t njobs, int32_t nbins,
+                                     int32_t poly_order, const LokiScoreSpec* spec,
+                                     void* dev_scratch, int64_t dev_scratch_bytes,
+                                     void* stream) {
+  if (!jobs || njobs < 1 || njobs > 65535 || !spec || !dev_scratch || nbins < 2 ||
+      poly_order < 1 || poly_order > LOKI_MAX_PARAMS)
+    return set_error(LOKI_ERR_INVALID, "bad seed batch arguments");
+  if (dev_scratch_bytes < (int64_t)njobs * (int64_t)sizeof(LokiSeedJob))
+    return set_error(LOKI_ERR_CAPACITY, "seed job scratch below %lld bytes",
+                     (long long)njobs * (long long)sizeof(LokiSeedJob));
+  int64_t maxn = 0;
+  for (int j = 0; j < njobs; ++j) {
+    const LokiSeedJob& J = jobs[j];
+    if (J.n < 0 || (J.n > 0 && (!J.seed_leaves || !J.fold_rows || !J.leaves_out ||
+                                !J.folds_out || !J.scores_out || !J.scores_ep_out ||
+                                !J.seed_scores_out || !J.bt_out)) ||
+        !J.dev_err)
+      return set_error(LOKI_ERR_INVALID, "seed job %d: null pointer or negative size", j);
+    maxn = std::max(maxn, J.n);
+  }
+  int rc = prune_spec_check(spec, nbins);
+  if (rc) return rc;
+  LokiScoreSpec sp = *spec;
+  sp.mode = 1;
+  const ScoreK SK = make_score_k(sp, nbins);
+  const int smem = score_smem_bytes(nbins, sp.wmax, kPruneWarps);
+  if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large");
+  if (smem > 48 * 1024 && set_smem_limit(prune_seed_batch_kernel, smem) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(dev_scratch, jobs, njobs * sizeof(LokiSeedJob), cudaMemcpyHostToDevice,
+                      s) != cudaSuccess)
+    return set_error(LOKI_ERR_CUDA, "copy of the seed jobs failed");
+  const unsigned bx =
+      (unsigned)std::max<int64_t>(1, std::min<int64_t>(32, (maxn + kPruneWarps * 32 - 1) /
+                                                               (kPruneWarps * 32)));
+  note_launch();
+  prune_seed_batch_kernel<<<dim3(bx, njobs), kPruneWarps * 32, smem, s>>>(
+      reinterpret_cast<const LokiSeedJob*>(dev_scratch), nbins, poly_order, sp, SK);
+  return check_launch("prune_seed_batch");
+}

@@ -1363,6 +1363,24 @@ class _DeviceRun:
         self._direct_fold = self.prn.dyp.fold.reshape(-1)
         self._seed_enqueue()
 
+    def seed_job(self) -> _lib.LokiSeedJob:
+        """This run's seed as a job of ``loki_prune_seed_batch``, reading the
+        fold itself."""
+        prn, b = self.prn, self.bufs
+        self._direct_fold = prn.dyp.fold.reshape(-1)
+        t0, n = b.trees[0], self.seed.size
+        stride = int(np.prod(prn.dyp.fold.shape[1:]))
+        j = _lib.LokiSeedJob()
+        j.seed_leaves = _lib.ptr(self.seed.leaves)
+        j.fold_rows = _lib.ptr(self._direct_fold) + 4 * self.ref_seg * stride
+        j.n = n
+        j.leaves_out, j.folds_out = _lib.ptr(t0["leaves"]), _lib.ptr(t0["folds"])
+        j.scores_out, j.scores_ep_out = _lib.ptr(t0["scores"]), _lib.ptr(t0["scores_ep"])
+        j.seed_scores_out = _lib.ptr(b.mem["seed_scores"])
+        j.bt_out = _lib.ptr(t0["bt"])
+        j.dev_err = _lib.ptr(prn._err)
+        return j
+
     def _enqueue(self) -> None:
         """The run from the fold mirror: the seed, then every level."""
         prn, b = self.prn, self.bufs
@@ -1791,11 +1809,21 @@ class PruneBlockBatch(PruneBatch):
             for k, (dyp, ref) in enumerate(wave):
                 prn = self._slot(k, dyp)
                 prn._stream_ptr = None  # the current stream
-                dr = prn._device_run_obj(ref, dyp.nsegments - 1, ascend)
-                dr.prepare_block()
-                runs.append((prn, dr))
+                runs.append((prn, prn._device_run_obj(ref, dyp.nsegments - 1, ascend)))
             nlev = runs[0][1].nlev
             n = len(runs)
+            if all(prn.dyp.fold.dtype == torch.float32 for prn, _ in runs):
+                sjobs = (_lib.LokiSeedJob * n)()  # every job's seed in one launch
+                for i, (prn, dr) in enumerate(runs):
+                    sjobs[i] = dr.seed_job()
+                p0 = runs[0][0]
+                sbuf = self._dev_buf("seed", n * C.sizeof(_lib.LokiSeedJob), dev)
+                _lib.check(lib.loki_prune_seed_batch(
+                    sjobs, n, p0.dyp.cfg.nbins, p0.poly_order, p0.spec, _lib.ptr(sbuf),
+                    sbuf.numel(), _lib.stream_ptr(st)))
+            else:  # a fold stored in another type: converted by the per-job copies
+                for prn, dr in runs:
+                    dr.prepare_block()
             if nlev > 0:
                 tab = (_lib.LokiPruneJob * n)()
                 lv = (_lib.LokiPruneLevel * (n * nlev))()

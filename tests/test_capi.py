@@ -89,7 +89,8 @@ def test_struct_layouts_match_header(tmp_path):
     structs = [_lib.LokiFFALevel, _lib.LokiFFACoord, _lib.LokiScoreSpec,
                _lib.LokiPruneLevel, _lib.LokiBranchInfo, _lib.LokiPruneTree,
                _lib.LokiPruneWork, _lib.LokiPruneLevelStats, _lib.LokiPruneRun,
-               _lib.LokiPruneJob, _lib.LokiAscendJob, _lib.LokiGatherPart]
+               _lib.LokiPruneJob, _lib.LokiAscendJob, _lib.LokiGatherPart,
+               _lib.LokiSeedJob]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "loki_gb300.h"',
              "int main(void) {"]
     for st in structs:
