@@ -162,7 +162,7 @@ def bench_prune_gpu(args, dev) -> dict:
     import torch
 
     from pyloki_gb300.ffa import DynamicProgramming
-    from pyloki_gb300.prune import PruneBatch, Pruning
+    from pyloki_gb300.prune import PruneBatch, PruneBlockBatch, Pruning
     from pyloki_gb300.timeseries import TimeSeries
 
     from pyloki_gb300 import _lib
@@ -201,10 +201,19 @@ def bench_prune_gpu(args, dev) -> dict:
         prn._do_ascend()
         return sum(st.n_leaves for st in prn.pstats[1:])
 
-    runner = PruneBatch(thr, n_streams=args.prune_streams, **kw)
+    runner = PruneBlockBatch(thr, **kw)
+    streams = PruneBatch(thr, n_streams=args.prune_streams, **kw)
 
     def batched(d=dyp) -> int:
+        """Every run at once: one launch per step of a level over all runs,
+        the kernels replayed from one CUDA graph."""
         res = runner.run([(d, r) for r in refs])
+        return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+
+    def batched_streams(d=dyp) -> int:
+        """Every run device-resident in its own graph, several at once on
+        their own streams."""
+        res = streams.run([(d, r) for r in refs])
         return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
 
     def timed(fn, steps):
@@ -220,24 +229,29 @@ def bench_prune_gpu(args, dev) -> dict:
         level_run()
         device_run()
         batched()
-    # kernels per step, counted on uncaptured runs (a graph replay does not
-    # pass through the library's launch counter)
+        batched_streams()
+    # kernels per step, counted on an uncaptured step (a graph replay does
+    # not pass through the library's launch counter)
+    runner._graphs.clear()
+    runner._seen.clear()
     c0 = lib.loki_launch_count()
-    for r in refs:
-        prn.run_device(r, graph=False)
-        prn._do_ascend()
+    batched()
     step_launches = lib.loki_launch_count() - c0
+    batched()  # captures the graph again
     with ClockSampler(dev.index) as clocks:
         leaves, ms = timed(batched, args.steps)
+    streams_leaves, streams_ms = timed(batched_streams, args.steps)
     single_leaves, single_ms = timed(device_run, args.steps)
     plain_leaves, plain_ms = timed(level_run, args.steps)
-    # the score kernel's own time for the roofline: one more level-by-level
-    # run with CUDA events around every score launch, outside the timed runs
-    score_events: list = []
-    level_run(score_events)
-    torch.cuda.synchronize(dev)
-    score_ms = sum(e0.elapsed_time(e1) for _, e0, e1 in score_events)
-    score_leaves = sum(n for n, _, _ in score_events)
+    # the score kernel's own time for the roofline: one more batched step,
+    # uncaptured, with CUDA events around every level's score launch (all
+    # runs in one launch), outside the timed steps
+    runner.time_score = True
+    res = runner.run([(dyp, r) for r in refs])
+    runner.time_score = False
+    score_ms = float(runner.score_ms.sum())
+    score_leaves = sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+    score_launches = int(runner.score_ms.size)
     peak, peak_kind = measured_peak_hbm()
     achieved = score_leaves * PRUNE_SCORE_BYTES_PER_LEAF / (score_ms * 1e-3) / 1e9
     value = leaves / (ms * 1e-3)
@@ -264,9 +278,14 @@ def bench_prune_gpu(args, dev) -> dict:
     e2e_s = time.perf_counter() - t0
     return {
         "metric": "prune leaves/s", "value": value, "unit": "leaves/s",
-        "path": (f"batched: {len(refs)} reference segments per step, each run device-resident "
-                 f"in one CUDA graph, {args.prune_streams} runs at once on their own streams"),
+        "path": (f"batched: {len(refs)} reference segments per step, every step of a level "
+                 f"one launch over all runs (loki_prune_run_batch), replayed from one CUDA "
+                 f"graph; seeds, ascend and read-back one launch each"),
         "ms_per_step": ms / args.steps, "leaves_per_step": leaves // args.steps,
+        "streams": {"value": streams_leaves / (streams_ms * 1e-3),
+                    "ms_per_step": streams_ms / args.steps,
+                    "note": (f"each run device-resident in its own CUDA graph, "
+                             f"{args.prune_streams} runs at once on their own streams")},
         "single_run": {"value": single_leaves / (single_ms * 1e-3),
                        "ms_per_run": single_ms / args.steps,
                        "leaves_per_run": single_leaves // args.steps,
@@ -282,15 +301,17 @@ def bench_prune_gpu(args, dev) -> dict:
                    "ffa_grid": cfg.get_param_grid_count(cfg.niters_ffa).tolist(),
                    "widths": cfg.score_widths.tolist(), "max_sugg": PRUNE_MAX_SUGG,
                    "batch_size": PRUNE_BATCH, "ref_segments": len(refs),
-                   "streams": args.prune_streams, "thresholds": PRUNE_SCHEME_NOTE,
+                   "driver": "level-synchronous batch (loki_prune_run_batch)",
+                   "thresholds": PRUNE_SCHEME_NOTE,
                    "orbit": {"p_orb_h": orbit[0] / 3600, "x_lts": orbit[1], "psi": orbit[2]},
                    "l2": "segment folds (75 KB) are L2-resident; tree folds stream"},
-        "roofline": {"kernel": "prune_score_kernel (resolve + gather + shift-add + score)",
+        "roofline": {"kernel": "bj_score_kernel (resolve + gather + shift-add + score, "
+                               "every run of the step in one launch per level)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "bytes_per_leaf": PRUNE_SCORE_BYTES_PER_LEAF,
-                     "kernel_ms_per_run": score_ms,
-                     "launches_per_run": len(score_events), "traffic": None},
+                     "kernel_ms_per_step": score_ms,
+                     "launches_per_step": score_launches, "traffic": None},
         "e2e": {"value": e2e_leaves / e2e_s, "unit": "leaves/s",
                 "ms_per_step": e2e_s * 1e3 / args.steps, "h2d_bytes_per_step": 8 * cfg.nsamps,
                 "d2h_bytes_per_step": int(d2h)},
@@ -1354,8 +1375,11 @@ def headline(out: dict) -> dict:
         if "plain" in p:
             sub["plain"] = {"value": p["plain"]["value"], "ms_per_run": p["plain"]["ms_per_run"]}
         pc = p.get("config", {})
-        sub["config"] = {k: pc[k] for k in ("workload", "thresholds", "ref_segments", "streams")
+        sub["config"] = {k: pc[k] for k in ("workload", "thresholds", "ref_segments", "driver")
                          if k in pc}
+        if "streams" in p:
+            sub["streams"] = {"value": p["streams"]["value"],
+                              "ms_per_step": p["streams"]["ms_per_step"]}
         for k in ("roofline", "cpu_baseline", "e2e"):
             if k in p:
                 sub[k] = {kk: vv for kk, vv in p[k].items()

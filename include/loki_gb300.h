@@ -690,6 +690,14 @@ int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
                              const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
                              const int64_t* shape_in, void* stream);
 
+/* loki_prune_batch_enqueue with CUDA events around every level's score
+ * launch; waits for the stream and writes the score kernel's time of each
+ * level (ms) to score_ms (host, nlevels). For measurement. */
+int loki_prune_batch_score_times(void* dev_scratch, int32_t njobs, int32_t nlevels,
+                                 const LokiScoreSpec* spec, int64_t max_sugg,
+                                 int64_t batch_size, const int64_t* shape_in, float* score_ms,
+                                 void* stream);
+
 /* One job of loki_prune_seed_batch: the seed tree of a run (the
  * reference segment's n grid points, core/taylor.py:14-65 seeds): its leaves
  * and fold rows are copied into the run's first tree and scored. */

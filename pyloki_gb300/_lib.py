@@ -253,6 +253,8 @@ SIGNATURES: dict[str, tuple] = {
                                           _P]),
     "loki_prune_batch_enqueue": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64,
                                            _I64, _P, _P]),
+    "loki_prune_batch_score_times": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec),
+                                               _I64, _I64, _P, _P, _P]),
     "loki_prune_ascend_batch": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64, _P,
                                           _I64, _P]),
     "loki_gather_parts": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),

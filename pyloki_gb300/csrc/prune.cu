@@ -14,6 +14,7 @@
 // the BLAS matrix product, which accumulates each output with forward fused
 // multiply-adds (acc = fma(x_j, T_ij, acc), j = 0..P).
 #include <algorithm>
+#include <vector>
 
 #include "loki_common.cuh"
 #include "score.cuh"
@@ -3545,7 +3546,8 @@ static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPrune
 // after new tables of the same shape are copied in).
 static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
                          const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
-                         const BatchShape& shape, cudaStream_t s) {
+                         const BatchShape& shape, cudaStream_t s,
+                         cudaEvent_t* ev_score = nullptr) {
   const int nb = shape.nbins, P = shape.poly_order;
   LokiScoreSpec sp = *spec;
   sp.mode = 1;
@@ -3593,7 +3595,9 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
     bj_scan_block_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_sums_kernel<false><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_add_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
+    if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
     bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
+    if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
     bj_scan_block_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_sums_kernel<true><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_add_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
@@ -3640,6 +3644,42 @@ extern "C" int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
   shape_out[2] = shape.max_par;
   shape_out[3] = shape.max_child;
   return LOKI_OK;
+}
+
+extern "C" int loki_prune_batch_score_times(void* dev_scratch, int32_t njobs, int32_t nlevels,
+                                            const LokiScoreSpec* spec, int64_t max_sugg,
+                                            int64_t batch_size, const int64_t* shape_in,
+                                            float* score_ms, void* stream) {
+  if (!dev_scratch || !spec || !shape_in || !score_ms || njobs < 1 || njobs > 65535 ||
+      nlevels < 1 || max_sugg < 1 || batch_size < 1)
+    return set_error(LOKI_ERR_INVALID, "bad batch timing arguments");
+  BatchShape shape;
+  shape.nbins = (int)shape_in[0];
+  shape.poly_order = (int)shape_in[1];
+  shape.max_par = shape_in[2];
+  shape.max_child = shape_in[3];
+  if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
+      shape.max_par < 1 || shape.max_child < 1)
+    return set_error(LOKI_ERR_INVALID, "bad batch shape");
+  int rc = prune_spec_check(spec, shape.nbins);
+  if (rc) return rc;
+  std::vector<cudaEvent_t> ev(2 * (size_t)nlevels, nullptr);
+  for (auto& e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (auto& f : ev)
+        if (f) cudaEventDestroy(f);
+      return set_error(LOKI_ERR_CUDA, "cudaEventCreate failed");
+    }
+  cudaStream_t s = (cudaStream_t)stream;
+  rc = batch_enqueue(dev_scratch, njobs, nlevels, spec, max_sugg, batch_size, shape, s,
+                     ev.data());
+  if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
+    rc = set_error(LOKI_ERR_CUDA, "cudaStreamSynchronize failed");
+  for (int l = 0; l < nlevels && !rc; ++l)
+    if (cudaEventElapsedTime(&score_ms[l], ev[2 * l], ev[2 * l + 1]) != cudaSuccess)
+      rc = set_error(LOKI_ERR_CUDA, "cudaEventElapsedTime failed");
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
 }
 
 extern "C" int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,

@@ -1566,15 +1566,22 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
                    ref_segs: list[int] | None = None, ascend_levels: list[int] | None = None,
                    max_sugg: int = 2**18, batch_size: int = 1024, outdir: str | Path = "./",
                    file_prefix: str = "test", poly_basis: str = "taylor", *,
-                   use_moving_grid: bool = True, n_workers: int = 4) -> str:
+                   use_moving_grid: bool = True, n_workers: int = 4,
+                   driver: str = "auto") -> str:
     """Prune from several reference segments (``prune.py:824-932``).
 
-    ``n_workers`` runs proceed at once, each on its own host thread and CUDA
-    stream (``run_many``), so one run's host work and waits overlap the
-    others' kernels; every run is the same computation as on its own.
+    ``driver="auto"`` runs every segment at once on the device
+    (``PruneBlockBatch``: one launch per step of a level over all runs)
+    when the tree supports device-resident runs and only the final ascend is
+    asked for; otherwise, and with ``driver="threads"``, ``n_workers`` runs
+    proceed at once, each on its own host thread and CUDA stream
+    (``run_many``). Every run is the same computation as on its own.
     Results are written as one ``.npz`` with the reference's per-run groups
     (``runs/<ref:03d>_<task:02d>/{scheme, param_sets, scores, scores_ep}``).
     """
+    if driver not in ("auto", "threads"):
+        msg = f"driver must be 'auto' or 'threads', got {driver!r}"
+        raise ValueError(msg)
     if not isinstance(n_workers, int | np.integer):
         msg = f"n_workers must be an integer, got {type(n_workers)}"
         raise TypeError(msg)
@@ -1600,9 +1607,16 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     log_file.write_text("Pruning log\n")
     out = {"param_names": np.asarray(dyp.cfg.param_names), "nsegments": dyp.nsegments,
            "max_sugg": max_sugg, "threshold_scheme": np.asarray(threshold_scheme)}
-    results = run_many(dyp, threshold_scheme, ref_segs, n_workers=n_workers,
-                       ascend_levels=ascend_levels, max_sugg=max_sugg, batch_size=batch_size,
-                       poly_basis=poly_basis, use_moving_grid=use_moving_grid)
+    kw = {"max_sugg": max_sugg, "batch_size": batch_size, "poly_basis": poly_basis,
+          "use_moving_grid": use_moving_grid}
+    batched = driver == "auto" and ascend_levels is None and Pruning(
+        dyp, threshold_scheme, **kw).device_run_supported
+    if batched:
+        res_list = PruneBlockBatch(threshold_scheme, **kw).run([(dyp, r) for r in ref_segs])
+        results = dict(zip(ref_segs, res_list, strict=True))
+    else:
+        results = run_many(dyp, threshold_scheme, ref_segs, n_workers=n_workers,
+                           ascend_levels=ascend_levels, **kw)
     for ref_seg in ref_segs:
         res = results[ref_seg]
         with log_file.open("a") as f:
@@ -1756,6 +1770,13 @@ class PruneBlockBatch(PruneBatch):
         the first time a shape is seen, then captured once in a CUDA graph
         and replayed (the tables are read on the device, so a replay runs
         whatever jobs were copied in)."""
+        if self.__dict__.get("time_score"):  # measurement: uncaptured, timed score launches
+            ms = np.zeros(nlev, np.float32)
+            _lib.check(lib.loki_prune_batch_score_times(
+                _lib.ptr(self._scratch), n, nlev, *args, shape.ctypes.data, ms.ctypes.data,
+                _lib.stream_ptr(st)))
+            self.score_ms = ms
+            return
         key = (n, nlev, tuple(int(v) for v in shape), args[1], args[2])
         graphs = self.__dict__.setdefault("_graphs", {})
         g = graphs.get(key)

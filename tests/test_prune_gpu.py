@@ -139,20 +139,25 @@ def test_prune_dyp_tree_writes_results(cuda_device, tmp_path):
         prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=0, outdir=tmp_path / "x")
 
 
-def test_prune_dyp_tree_concurrent_workers_match_serial(cuda_device, tmp_path):
-    """Four runs on three worker threads and streams write the same results as
-    one after another."""
+@pytest.mark.parametrize("name", ["prune_taylor", "prune_circ"])
+def test_prune_dyp_tree_drivers_match_serial(cuda_device, tmp_path, name):
+    """Four runs on three worker threads and streams, and all four at once
+    on the device (the default driver), write the same results as one after
+    another."""
     from pyloki_gb300.prune import prune_dyp_tree
 
-    d, prn = _run("prune_taylor", cuda_device)
+    d, prn = _run(name, cuda_device)
     kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
     a = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "a",
-                               n_workers=1, **kw))
+                               n_workers=1, driver="threads", **kw))
     b = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "b",
-                               n_workers=3, **kw))
-    assert sorted(a.files) == sorted(b.files)
+                               n_workers=3, driver="threads", **kw))
+    c = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "c",
+                               **kw))
+    assert sorted(a.files) == sorted(b.files) == sorted(c.files)
     for k in a.files:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+        np.testing.assert_array_equal(a[k], c[k], err_msg=k)
 
 
 def test_best_intermediate_matches_get_best_k(cuda_device):
