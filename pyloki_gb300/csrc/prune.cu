@@ -3353,7 +3353,7 @@ __global__ void __launch_bounds__(kScanBlock) bj_scan_add_kernel(BatchTabs T, in
     out[i] += sums[i / kScanBlock];
 }
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
+__global__ void __launch_bounds__(kPruneWarps * 32, 4)
 bj_score_kernel(BatchTabs T, int l, LokiScoreSpec sp, ScoreK SK) {
   extern __shared__ float tiles[];
   const LokiPruneJob& J = T.jobs[blockIdx.y];
@@ -3572,20 +3572,24 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
   T.seg_idx = reinterpret_cast<const int32_t*>(base + o_si);
   T.thr = reinterpret_cast<const double*>(base + o_th);
   T.nlevels = nlevels;
-  // per-job grids of a few waves of the GPU in total, at least one block
+  // Per-job grids. The jobs' sizes differ from level to level, so every job
+  // gets enough blocks for several times an even share of the GPU: blocks
+  // past a job's work retire at once, and the block scheduler spreads the
+  // busy jobs' blocks over the whole GPU.
   auto per_job = [&](int64_t waves_blocks, int64_t cap_blocks) {
     return (unsigned)std::max<int64_t>(
         1, std::min<int64_t>(cap_blocks, (waves_blocks + njobs - 1) / njobs));
   };
   const int64_t max_par = shape.max_par, max_child = shape.max_child;
-  const unsigned g_par = per_job(8 * nsm, (max_par + 255) / 256);
+  const int64_t spread = std::min<int64_t>(njobs, 16);
+  const unsigned g_par = per_job(8 * nsm * spread, (max_par + 255) / 256);
   const unsigned g_scan_p = per_job(2 * nsm, (max_par + 1 + kScanBlock - 1) / kScanBlock);
   const unsigned g_scan_c = per_job(2 * nsm, (max_child + kScanBlock - 1) / kScanBlock);
   const unsigned g_score =
-      per_job(6 * nsm, (max_child + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
+      per_job(6 * nsm * spread, (max_child + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
   const unsigned g_flat = per_job(8 * nsm, (max_child + 255) / 256);
   const unsigned g_emit =
-      per_job(6 * nsm, (max_par + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
+      per_job(6 * nsm * spread, (max_par + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
   const int row_bt = P + 2, row_leaf = (P + 2) * 2;
   note_launch();
   bj_seed_kernel<<<(unsigned)njobs, 1, 0, s>>>(T);
