@@ -340,11 +340,17 @@ __device__ __forceinline__ void branch_one(const LokiPruneLevel& D,
     const double dnew = __ddiv_rn(D.dfc[j], f0);
     const double fb = __dmul_rn(D.fac[j], fscale);
     const double shift = __dmul_rn(fabs(__dsub_rn(dcur, dnew)), fb);
+    const bool split = !(shift < D.eta_m);
     int64_t num = 1;
     double dact = dcur, first = pcur;
     if (!(dcur > 0.0) || !(dnew > 0.0)) {
       atomicOr(err, LOKI_DEVERR_BRANCH);
-    } else {
+    } else if (split || dcur > __dmul_rn(dnew, 0.5 * (double)D.branch_max)) {
+      // The child count is needed for a split, and for the reference's
+      // branch_max check of every parameter; a parameter that does not
+      // split and whose step is at most half of branch_max new steps cannot
+      // exceed branch_max (ratio <= branch_max / 2 up to rounding), so its
+      // division is skipped.
       const double ratio = __ddiv_rn(dcur, dnew);
       num = (int64_t)ceil(__dsub_rn(ratio, LOKI_FLOAT_EPSILON));
       if (num < 1) num = 1;
@@ -352,11 +358,15 @@ __device__ __forceinline__ void branch_one(const LokiPruneLevel& D,
         atomicOr(err, LOKI_DEVERR_BRANCH);
         num = D.branch_max;
       }
-      dact = __ddiv_rn(dcur, (double)num);
-      const double pmin = __dsub_rn(pcur, __dmul_rn(dcur, 0.5));
-      first = __dadd_rn(pmin, __dmul_rn(dact, 0.5));
+      if (split) {  // division by 1 or a power of two is exact scaling
+        dact = num == 1                ? dcur
+               : (num & (num - 1)) == 0 ? __dmul_rn(dcur, 1.0 / (double)num)
+                                        : __ddiv_rn(dcur, (double)num);
+        const double pmin = __dsub_rn(pcur, __dmul_rn(dcur, 0.5));
+        first = __dadd_rn(pmin, __dmul_rn(dact, 0.5));
+      }
     }
-    if (shift < D.eta_m) {
+    if (!split) {
       num = 1;
       dact = dcur;
       first = pcur;
