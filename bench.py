@@ -1237,6 +1237,31 @@ def profile_prune_once(args) -> None:
                       "launches_per_run": prn.launches // 2}))
 
 
+def profile_prune_batch_once(args) -> None:
+    """One batched pruning step (``PruneBlockBatch``, the first call of a
+    fresh runner, so its kernels are launched directly) over args.prune_runs
+    reference segments, with no timing; the command the batched-pruning ncu
+    summaries are captured from."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import PruneBlockBatch
+
+    dev = torch.device("cuda", 0)
+    cfg = make_prune_cfg()
+    ts, _ = make_prune_series(seed=2000)
+    dyp = DynamicProgramming(ts, cfg, device=dev)
+    dyp.initialize()
+    dyp.execute()
+    nseg = dyp.nsegments
+    refs = [int(r) for r in np.linspace(4, nseg - 5, args.prune_runs).round()]
+    res = PruneBlockBatch(prune_thresholds(nseg), max_sugg=PRUNE_MAX_SUGG,
+                          batch_size=PRUNE_BATCH).run([(dyp, r) for r in refs])
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_prune_batch_once": True, "runs": len(refs),
+                      "leaves": sum(st.n_leaves for r in res for st in r["level_stats"][1:])}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1290,6 +1315,8 @@ def main() -> None:
                     help="run exactly one search (for ncu captures) and exit")
     ap.add_argument("--profile-prune-once", action="store_true",
                     help="run the pruning workload twice (warm-up + one run) and exit")
+    ap.add_argument("--profile-prune-batch-once", action="store_true",
+                    help="one batched pruning step over --prune-runs segments, then exit")
     ap.add_argument("--detail-out", default=None,
                     help="also write the full result (every side study) to this JSON file")
     ap.add_argument("--nsamps-log2", type=int, default=23,
@@ -1300,6 +1327,9 @@ def main() -> None:
         return
     if args.profile_prune_once:
         profile_prune_once(args)
+        return
+    if args.profile_prune_batch_once:
+        profile_prune_batch_once(args)
         return
     if args.profile_inject_once:
         profile_inject_once(args)
