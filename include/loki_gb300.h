@@ -675,17 +675,20 @@ int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPrun
 /* loki_prune_run_batch in two halves, so that the kernels can be captured
  * in a CUDA graph once and replayed: loki_prune_batch_tables checks the jobs
  * and copies the tables into dev_scratch (host memory is read: not inside a
- * capture) and writes the batch's shape (4 words: nbins, poly_order, largest
- * par_cap, largest child_cap); loki_prune_batch_enqueue enqueues the kernels
+ * capture) and writes the batch's shape (5 words: nbins, poly_order, largest
+ * par_cap, largest child_cap, fourier); loki_prune_batch_enqueue enqueues the kernels
  * over the tables in dev_scratch for that shape. A replay after
  * loki_prune_batch_tables with new jobs of the same count, levels and shape
- * runs the new jobs. */
+ * runs the new jobs. fourier != 0: complex (Fourier-domain) trees, the
+ * jobs' tree folds (cap, 2, nbins / 2 + 1) complex64, fold rows and
+ * seg_stride in complex elements (the complex level kernels' per-child code,
+ * prune.py:165-332 with PruneTaylorComplexDPFuncts). */
 int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
                             const LokiPruneLevel* levels, const int32_t* seg_idx,
                             const double* thresholds, int32_t nlevels,
                             const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
-                            void* dev_scratch, int64_t dev_scratch_bytes, int64_t* shape_out,
-                            void* stream);
+                            int32_t fourier, void* dev_scratch, int64_t dev_scratch_bytes,
+                            int64_t* shape_out, void* stream);
 int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
                              const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
                              const int64_t* shape_in, void* stream);
@@ -742,10 +745,12 @@ typedef struct {
 /* loki_prune_ascend_dev for njobs runs in one launch (grid y = job): the
  * jobs (host array) are checked and copied into dev_scratch of at least
  * njobs * sizeof(LokiAscendJob) bytes. Every job has nseg segments and at
- * most n_cap survivors. Taylor and Chebyshev trees. */
+ * most n_cap survivors. Taylor and Chebyshev trees; fourier != 0: complex
+ * trees as loki_prune_ascend_complex (folds and seg_stride in complex
+ * elements). */
 int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs, int32_t nseg,
-                            const LokiScoreSpec* spec, int64_t n_cap, void* dev_scratch,
-                            int64_t dev_scratch_bytes, void* stream);
+                            const LokiScoreSpec* spec, int64_t n_cap, int32_t fourier,
+                            void* dev_scratch, int64_t dev_scratch_bytes, void* stream);
 
 /* A device byte range and its place in a packed destination. */
 typedef struct {

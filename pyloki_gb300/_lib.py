@@ -249,14 +249,14 @@ SIGNATURES: dict[str, tuple] = {
     "loki_prune_run_batch": (C.c_int, [_P, _I32, _P, _P, _P, _I32, C.POINTER(LokiScoreSpec),
                                        _I64, _I64, _P, _I64, _P]),
     "loki_prune_batch_tables": (C.c_int, [_P, _I32, _P, _P, _P, _I32,
-                                          C.POINTER(LokiScoreSpec), _I64, _I64, _P, _I64, _P,
-                                          _P]),
+                                          C.POINTER(LokiScoreSpec), _I64, _I64, _I32, _P, _I64,
+                                          _P, _P]),
     "loki_prune_batch_enqueue": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64,
                                            _I64, _P, _P]),
     "loki_prune_batch_score_times": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec),
                                                _I64, _I64, _P, _P, _P]),
-    "loki_prune_ascend_batch": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64, _P,
-                                          _I64, _P]),
+    "loki_prune_ascend_batch": (C.c_int, [_P, _I32, _I32, C.POINTER(LokiScoreSpec), _I64,
+                                          _I32, _P, _I64, _P]),
     "loki_gather_parts": (C.c_int, [_P, _I32, _P, _I64, _P, _I64, _P]),
     "loki_prune_seed_batch": (C.c_int, [_P, _I32, _I32, _I32, C.POINTER(LokiScoreSpec), _P,
                                         _I64, _P]),

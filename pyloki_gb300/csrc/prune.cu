@@ -1739,26 +1739,16 @@ __host__ __device__ inline size_t cplx_warp_floats(int nbins, int stride) {
   return (size_t)32 * 2 * (nbins / 2 + 1) * 2 + (size_t)32 * stride;
 }
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                           const float2* __restrict__ folds, int64_t n_parents,
-                           const LokiBranchInfo* __restrict__ info,
-                           const int64_t* __restrict__ offsets, int64_t n_children,
-                           const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
-                           float* __restrict__ scores, int32_t* __restrict__ cidx,
-                           double* __restrict__ cphase, unsigned* __restrict__ minmax_keys) {
-  extern __shared__ float smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// One child of the complex tree: resolve, rotate-add the segment row onto the
+// parent fold, score the sum through its irfft (comb and trow: this lane's
+// scratch, tw: the block's twiddles).
+__device__ __forceinline__ void score_child_complex(
+    const LokiPruneLevel& D, const double* __restrict__ leaves, const float2* __restrict__ folds,
+    int64_t n_parents, const LokiBranchInfo* __restrict__ info,
+    const int64_t* __restrict__ offsets, const float2* __restrict__ seg, const LokiScoreSpec& sp,
+    float* __restrict__ scores, int32_t* __restrict__ cidx, double* __restrict__ cphase,
+    unsigned* __restrict__ minmax_keys, const float* tw, float2* comb, float* trow, int64_t c) {
   const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order;
-  const int stride = score_stride(nb, sp.wmax);
-  float* tw = smem;
-  load_twiddles(tw, nb);
-  __syncthreads();
-  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
-  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
-  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
-  const int64_t c = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
-  if (c >= n_children) return;
   const int64_t par = find_parent(offsets, n_parents, c);
   const LokiBranchInfo B = info[par];
   const double* lf = leaves + par * (P + 2) * 2;
@@ -1771,7 +1761,6 @@ prune_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   cphase[c] = r.phase;
   const int64_t row = (int64_t)r.ia * D.n_freq + r.iff;
   rotate_add(seg + row * 2 * nbf, folds + par * 2 * nbf, prune_phasor(r.phase, nb), nbf, comb);
-  float* trow = tile + lane * stride;
   irfft_norm(comb, nb, nbf, tw, trow);
   float s;
   score_row(trow, nb, sp, &s);
@@ -1782,21 +1771,42 @@ prune_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
 }
 
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                           const float2* __restrict__ folds, int64_t n_parents,
+                           const LokiBranchInfo* __restrict__ info,
+                           const int64_t* __restrict__ offsets, int64_t n_children,
+                           const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                           float* __restrict__ scores, int32_t* __restrict__ cidx,
+                           double* __restrict__ cphase, unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t c = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (c >= n_children) return;
+  score_child_complex(D, leaves, folds, n_parents, info, offsets, seg, sp, scores, cidx, cphase,
+                      minmax_keys, tw, comb, tile + lane * stride, c);
+}
+
 // Survivors of the complex tree: transform / backtrack exactly as
 // prune_emit_kernel, the fold written as the complex sum.
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                          const float2* __restrict__ folds,
-                          const LokiBranchInfo* __restrict__ info,
-                          const int64_t* __restrict__ offsets, int64_t n_parents,
-                          const float2* __restrict__ seg, const int64_t* __restrict__ surv,
-                          int64_t n_surv, const float* __restrict__ cscores,
-                          const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
-                          double* __restrict__ lout, float2* __restrict__ fout,
-                          float* __restrict__ sout, float* __restrict__ seout,
-                          int32_t* __restrict__ bout) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n_surv) return;
+// One survivor of the complex tree: transform, backtrack and the complex
+// sum of its fold.
+__device__ __forceinline__ void emit_one_complex(
+    const LokiPruneLevel& D, const double* __restrict__ leaves, const float2* __restrict__ folds,
+    const LokiBranchInfo* __restrict__ info, const int64_t* __restrict__ offsets,
+    int64_t n_parents, const float2* __restrict__ seg, const int64_t* __restrict__ surv,
+    const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
+    const double* __restrict__ cphase, double* __restrict__ lout, float2* __restrict__ fout,
+    float* __restrict__ sout, float* __restrict__ seout, int32_t* __restrict__ bout,
+    int64_t s) {
   const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order, m = P + 1;
   const int64_t c = surv[s];
   const int64_t par = find_parent(offsets, n_parents, c);
@@ -1841,30 +1851,34 @@ prune_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
              fout + s * 2 * nbf);
 }
 
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                          const float2* __restrict__ folds,
+                          const LokiBranchInfo* __restrict__ info,
+                          const int64_t* __restrict__ offsets, int64_t n_parents,
+                          const float2* __restrict__ seg, const int64_t* __restrict__ surv,
+                          int64_t n_surv, const float* __restrict__ cscores,
+                          const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
+                          double* __restrict__ lout, float2* __restrict__ fout,
+                          float* __restrict__ sout, float* __restrict__ seout,
+                          int32_t* __restrict__ bout) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n_surv) return;
+  emit_one_complex(D, leaves, folds, info, offsets, n_parents, seg, surv, cscores, cidx, cphase,
+                   lout, fout, sout, seout, bout, s);
+}
+
 // Ascend of the complex tree (dyn_poly_taylor.py:632-679 with
 // core/common.py:460-490): per survivor the rotated segment rows are summed
 // over the segments in order, then the sum is scored through its irfft.
-__global__ void __launch_bounds__(kPruneWarps * 32)
-prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                            float2* __restrict__ folds, float* __restrict__ scores,
-                            float* __restrict__ scores_ep, int64_t n, int nseg,
-                            const double* __restrict__ tm_seg,
-                            const double* __restrict__ dt_seg,
-                            const int32_t* __restrict__ seg_idx,
-                            const float2* __restrict__ ffa, int64_t seg_stride,
-                            LokiScoreSpec sp, ScoreK SK) {
-  extern __shared__ float smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Ascend of one survivor of the complex tree.
+__device__ __forceinline__ void ascend_one_complex(
+    const LokiPruneLevel& D, const double* __restrict__ leaves, float2* __restrict__ folds,
+    float* __restrict__ scores, float* __restrict__ scores_ep, int nseg,
+    const double* __restrict__ tm_seg, const double* __restrict__ dt_seg,
+    const int32_t* __restrict__ seg_idx, const float2* __restrict__ ffa, int64_t seg_stride,
+    const LokiScoreSpec& sp, const float* tw, float2* comb, float* trow, int64_t r) {
   const int nb = D.nbins, nbf = nb / 2 + 1, P = D.poly_order, m = P + 1;
-  const int stride = score_stride(nb, sp.wmax);
-  float* tw = smem;
-  load_twiddles(tw, nb);
-  __syncthreads();
-  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
-  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
-  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
-  const int64_t r = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
-  if (r >= n) return;
   const double* lf = leaves + r * (P + 2) * 2;
   double pv[LOKI_MAX_PARAMS + 1], ev[LOKI_MAX_PARAMS + 1];
   for (int i = 0; i < m; ++i) {
@@ -1913,12 +1927,36 @@ prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
   float2* o = folds + r * 2 * nbf;
   for (int k = 0; k < 2 * nbf; ++k) o[k] = comb[k];
-  float* trow = tile + lane * stride;
   irfft_norm(comb, nb, nbf, tw, trow);
   scores_ep[r] = scores[r];
   float s;
   score_row(trow, nb, sp, &s);
   scores[r] = s;
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                            float2* __restrict__ folds, float* __restrict__ scores,
+                            float* __restrict__ scores_ep, int64_t n, int nseg,
+                            const double* __restrict__ tm_seg,
+                            const double* __restrict__ dt_seg,
+                            const int32_t* __restrict__ seg_idx,
+                            const float2* __restrict__ ffa, int64_t seg_stride,
+                            LokiScoreSpec sp, ScoreK SK) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t r = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (r >= n) return;
+  ascend_one_complex(D, leaves, folds, scores, scores_ep, nseg, tm_seg, dt_seg, seg_idx, ffa,
+                     seg_stride, sp, tw, comb, tile + lane * stride, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -3444,6 +3482,69 @@ __global__ void __launch_bounds__(kPruneWarps * 32) bj_emit_kernel(BatchTabs T, 
               out.leaves, out.folds, out.scores, out.scores_ep, out.backtracks, t * 32);
 }
 
+// complex (Fourier-domain) trees: the per-child functions of the complex
+// level kernels, grid-stride over each job's device counts. The jobs' fold
+// rows and segment strides are in complex (float2) units.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_score_complex_kernel(BatchTabs T, int l, LokiScoreSpec sp) {
+  extern __shared__ float smem[];
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const float2* seg = reinterpret_cast<const float2*>(J.ffa_fold) + (int64_t)T.seg_idx[li] *
+                                                                        J.seg_stride;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* trow = wbase + (size_t)32 * 2 * nbf * 2 + lane * stride;
+  int64_t* cnt = R.counts;
+  const int64_t n_par = cnt[0];
+  const int64_t total = w.offsets[n_par];
+  const int64_t n_child = total > w.child_cap ? 0 : total;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[1] = n_child;
+    LokiPruneLevelStats* st = R.stats + (l - 1);
+    st->n_parents = n_par;
+    st->n_children = total;
+    st->n_valid = total;
+    if (total > w.child_cap) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+  }
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n_child;
+       c += (int64_t)gridDim.x * blockDim.x)
+    score_child_complex(D, in.leaves, reinterpret_cast<const float2*>(in.folds), n_par,
+                        reinterpret_cast<LokiBranchInfo*>(w.info), w.offsets, seg, sp,
+                        w.child_scores, w.child_idx, w.child_phase,
+                        reinterpret_cast<unsigned*>(w.minmax), tw, comb, trow, c);
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32) bj_emit_complex_kernel(BatchTabs T, int l) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const LokiPruneTree& out = R.trees[l & 1];
+  const float2* seg = reinterpret_cast<const float2*>(J.ffa_fold) + (int64_t)T.seg_idx[li] *
+                                                                        J.seg_stride;
+  const int64_t n_par = R.counts[0], n_surv = R.counts[2];
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_surv;
+       s += (int64_t)gridDim.x * blockDim.x)
+    emit_one_complex(D, in.leaves, reinterpret_cast<const float2*>(in.folds),
+                     reinterpret_cast<LokiBranchInfo*>(w.info), w.offsets, n_par, seg, w.surv,
+                     w.child_scores, w.child_idx, w.child_phase, out.leaves,
+                     reinterpret_cast<float2*>(out.folds), out.scores, out.scores_ep,
+                     out.backtracks, s);
+}
+
 __global__ void bj_bt_kernel(BatchTabs T, int l, int row) {
   const LokiPruneJob& J = T.jobs[blockIdx.y];
   const LokiPruneRun& R = J.run;
@@ -3481,13 +3582,14 @@ __global__ void __launch_bounds__(1024) bj_best_kernel(BatchTabs T, int l, int r
 struct BatchShape {
   int nbins, poly_order;
   int64_t max_par, max_child;
+  int fourier;  // complex (Fourier-domain) folds
 };
 
 static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
                         const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
                         const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
                         void* dev_scratch, int64_t dev_scratch_bytes, cudaStream_t s,
-                        BatchShape* shape) {
+                        BatchShape* shape, int fourier = 0) {
   if (!jobs || njobs < 1 || njobs > 65535 || !levels || !seg_idx || !thresholds ||
       nlevels < 1 || !spec || !dev_scratch)
     return set_error(LOKI_ERR_INVALID, "null pointer, no job (or above 65535) or no level");
@@ -3548,6 +3650,7 @@ static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPrune
   shape->poly_order = P;
   shape->max_par = max_par;
   shape->max_child = max_child;
+  shape->fourier = fourier ? 1 : 0;
   return LOKI_OK;
 }
 
@@ -3559,13 +3662,18 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
                          const BatchShape& shape, cudaStream_t s,
                          cudaEvent_t* ev_score = nullptr) {
   const int nb = shape.nbins, P = shape.poly_order;
+  const bool cplx = shape.fourier != 0;
   LokiScoreSpec sp = *spec;
   sp.mode = 1;
   const ScoreK SK = make_score_k(sp, nb);
-  const int smem = score_smem_bytes(nb, sp.wmax, kPruneWarps);
+  const int smem =
+      cplx ? (int)((2 * nb + kPruneWarps * cplx_warp_floats(nb, score_stride(nb, sp.wmax))) *
+                   sizeof(float))
+           : score_smem_bytes(nb, sp.wmax, kPruneWarps);
   if (smem > 200 * 1024)
     return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
-  if (smem > 48 * 1024 && set_smem_limit(bj_score_kernel, smem) != cudaSuccess)
+  if (smem > 48 * 1024 && (cplx ? set_smem_limit(bj_score_complex_kernel, smem)
+                                : set_smem_limit(bj_score_kernel, smem)) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -3610,14 +3718,20 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
     bj_scan_sums_kernel<false><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_add_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
     if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
-    bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
+    if (cplx)
+      bj_score_complex_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp);
+    else
+      bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
     if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
     bj_scan_block_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_sums_kernel<true><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scan_add_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
     bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l);
     bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size);
-    bj_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+    if (cplx)
+      bj_emit_complex_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+    else
+      bj_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
     bj_bt_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, row_bt);
     bj_best_kernel<<<(unsigned)njobs, 1024, 0, s>>>(T, l, row_leaf);
     int rc = check_launch("prune_run_batch");
@@ -3644,19 +3758,20 @@ extern "C" int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
                                        const LokiPruneLevel* levels, const int32_t* seg_idx,
                                        const double* thresholds, int32_t nlevels,
                                        const LokiScoreSpec* spec, int64_t max_sugg,
-                                       int64_t batch_size, void* dev_scratch,
+                                       int64_t batch_size, int32_t fourier, void* dev_scratch,
                                        int64_t dev_scratch_bytes, int64_t* shape_out,
                                        void* stream) {
   if (!shape_out) return set_error(LOKI_ERR_INVALID, "null shape pointer");
   BatchShape shape;
   int rc = batch_tables(jobs, njobs, levels, seg_idx, thresholds, nlevels, spec, max_sugg,
                         batch_size, dev_scratch, dev_scratch_bytes, (cudaStream_t)stream,
-                        &shape);
+                        &shape, fourier);
   if (rc) return rc;
   shape_out[0] = shape.nbins;
   shape_out[1] = shape.poly_order;
   shape_out[2] = shape.max_par;
   shape_out[3] = shape.max_child;
+  shape_out[4] = shape.fourier;
   return LOKI_OK;
 }
 
@@ -3672,6 +3787,7 @@ extern "C" int loki_prune_batch_score_times(void* dev_scratch, int32_t njobs, in
   shape.poly_order = (int)shape_in[1];
   shape.max_par = shape_in[2];
   shape.max_child = shape_in[3];
+  shape.fourier = shape_in[4] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
       shape.max_par < 1 || shape.max_child < 1)
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
@@ -3708,6 +3824,7 @@ extern "C" int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_
   shape.poly_order = (int)shape_in[1];
   shape.max_par = shape_in[2];
   shape.max_child = shape_in[3];
+  shape.fourier = shape_in[4] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
       shape.max_par < 1 || shape.max_child < 1)
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
@@ -3742,6 +3859,31 @@ prune_ascend_batch_kernel(const LokiAscendJob* __restrict__ jobs, int nseg, Loki
   }
 }
 
+// The same over complex trees (folds and segment strides in float2 units).
+__global__ void __launch_bounds__(kPruneWarps * 32)
+prune_ascend_batch_complex_kernel(const LokiAscendJob* __restrict__ jobs, int nseg,
+                                  LokiScoreSpec sp) {
+  extern __shared__ float smem[];
+  const LokiAscendJob& J = jobs[blockIdx.y];
+  const LokiPruneLevel& D = J.lvl;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* trow = wbase + (size_t)32 * 2 * nbf * 2 + lane * stride;
+  const int64_t n = *J.n_dev;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x)
+    ascend_one_complex(D, J.leaves, reinterpret_cast<float2*>(J.folds), J.scores, J.scores_ep,
+                       nseg, J.tm_seg, J.dt_seg, J.seg_idx,
+                       reinterpret_cast<const float2*>(J.ffa_fold), J.seg_stride, sp, tw, comb,
+                       trow, r);
+}
+
 // Block y copies part y: src[y][0 .. bytes[y]) to dst + off[y] (16-byte
 // words where both ends allow, else bytes).
 __global__ void gather_parts_kernel(const LokiGatherPart* __restrict__ parts,
@@ -3766,8 +3908,8 @@ __global__ void gather_parts_kernel(const LokiGatherPart* __restrict__ parts,
 
 extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs, int32_t nseg,
                                        const LokiScoreSpec* spec, int64_t n_cap,
-                                       void* dev_scratch, int64_t dev_scratch_bytes,
-                                       void* stream) {
+                                       int32_t fourier, void* dev_scratch,
+                                       int64_t dev_scratch_bytes, void* stream) {
   if (!jobs || njobs < 1 || njobs > 65535 || nseg < 1 || !spec || n_cap < 1 || !dev_scratch)
     return set_error(LOKI_ERR_INVALID, "bad batched ascend arguments");
   if (dev_scratch_bytes < (int64_t)njobs * (int64_t)sizeof(LokiAscendJob))
@@ -3791,15 +3933,23 @@ extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs,
   LokiScoreSpec sp = *spec;
   sp.mode = 1;
   const ScoreK SK = make_score_k(sp, nb);
-  const int smem = kPruneWarps * 32 * (2 * nb + score_stride(nb, sp.wmax)) * (int)sizeof(float);
+  const int stride = score_stride(nb, sp.wmax);
+  const int smem =
+      fourier ? (int)((2 * nb + kPruneWarps * cplx_warp_floats(nb, stride)) * sizeof(float))
+              : kPruneWarps * 32 * (2 * nb + stride) * (int)sizeof(float);
   if (smem > 200 * 1024) return set_error(LOKI_ERR_UNSUPPORTED, "nbins too large for ascend");
-  if (smem > 48 * 1024 && set_smem_limit(prune_ascend_batch_kernel, smem) != cudaSuccess)
+  if (smem > 48 * 1024 && (fourier ? set_smem_limit(prune_ascend_batch_complex_kernel, smem)
+                                   : set_smem_limit(prune_ascend_batch_kernel, smem)) !=
+                              cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0, occ = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune_ascend_batch_kernel,
-                                                    kPruneWarps * 32, smem) != cudaSuccess)
+      (fourier ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                     &occ, prune_ascend_batch_complex_kernel, kPruneWarps * 32, smem)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, prune_ascend_batch_kernel,
+                                                               kPruneWarps * 32, smem)) !=
+          cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "occupancy query failed");
   cudaStream_t s = (cudaStream_t)stream;
   if (cudaMemcpyAsync(dev_scratch, jobs, njobs * sizeof(LokiAscendJob), cudaMemcpyHostToDevice,
@@ -3809,8 +3959,12 @@ extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs,
   const int64_t wave = ((int64_t)nsm * std::max(1, occ) + njobs - 1) / njobs;
   const unsigned bx = (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, wave));
   note_launch();
-  prune_ascend_batch_kernel<<<dim3(bx, njobs), kPruneWarps * 32, smem, s>>>(
-      reinterpret_cast<const LokiAscendJob*>(dev_scratch), nseg, sp, SK);
+  if (fourier)
+    prune_ascend_batch_complex_kernel<<<dim3(bx, njobs), kPruneWarps * 32, smem, s>>>(
+        reinterpret_cast<const LokiAscendJob*>(dev_scratch), nseg, sp);
+  else
+    prune_ascend_batch_kernel<<<dim3(bx, njobs), kPruneWarps * 32, smem, s>>>(
+        reinterpret_cast<const LokiAscendJob*>(dev_scratch), nseg, sp, SK);
   return check_launch("prune_ascend_batch");
 }
 

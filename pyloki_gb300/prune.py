@@ -992,6 +992,15 @@ class Pruning:
         parent hook."""
         return not self.fourier and self.intermediate_k == 1 and self.parent_hook is None
 
+    @property
+    def block_batch_supported(self) -> bool:
+        """``PruneBlockBatch`` covers this configuration: every tree without
+        a parent hook and one best leaf per level, except the circular-orbit
+        tree over complex folds (the circular tree over real folds runs
+        through ``PruneBatch``)."""
+        return (self.intermediate_k == 1 and self.parent_hook is None
+                and not (self.fourier and self.circular))
+
     def run_device(self, ref_seg: int, *, graph: bool = False, levels: int | None = None) -> None:
         """Every level of one reference segment with the counts kept on the
         device (``loki_prune_run``): the run is enqueued without a host wait
@@ -1175,8 +1184,10 @@ class _DeviceBuffers:
         t64, t32, f32, f64, u8 = torch.int64, torch.int32, torch.float32, torch.float64, torch.uint8
         self.child_cap, self.bt_rows = child_cap, bt_rows
         self.host: dict = {}  # pinned readback buffers, grown on demand
+        fold_row = ((2, nb // 2 + 1), torch.complex64) if prn.fourier else ((2, nb), f32)
         self.trees = [{"leaves": torch.empty((cap, P + 2, 2), dtype=f64, device=dev),
-                       "folds": torch.empty((cap, 2, nb), dtype=f32, device=dev),
+                       "folds": torch.empty((cap, *fold_row[0]), dtype=fold_row[1],
+                                            device=dev),
                        "scores": torch.empty(cap, dtype=f32, device=dev),
                        "scores_ep": torch.empty(cap, dtype=f32, device=dev),
                        "bt": torch.empty((cap, P + 2), dtype=t32, device=dev)} for _ in range(2)]
@@ -1204,7 +1215,8 @@ class _DeviceBuffers:
             "bt_hist": torch.empty((bt_rows, P + 2), dtype=t32, device=dev),
             # the FFA fold the runs read: a copy made on the stream before each
             # run, so a captured graph serves any fold of the same shape
-            "mirror": torch.empty(int(prn.dyp.fold.numel()), dtype=f32, device=dev),
+            "mirror": torch.empty(int(prn.dyp.fold.numel()), dtype=prn.dyp.fold.dtype,
+                                  device=dev),
             "seed_scores": torch.empty(cap, dtype=f32, device=dev),
         }
         m = self.mem
@@ -1294,7 +1306,8 @@ class _DeviceRun:
 
     def _seed_enqueue(self) -> None:
         """The seed tree from the fold: leaves from the grid, folds and
-        scores from the reference segment's rows."""
+        scores from the reference segment's rows (complex rows scored
+        through their irfft, as ``Pruning._seed``)."""
         prn, b = self.prn, self.bufs
         t0, seed = b.trees[0], self.seed
         n = seed.size
@@ -1303,9 +1316,17 @@ class _DeviceRun:
         src = self._fold_src()
         t0["leaves"][:n].copy_(seed.leaves)
         t0["folds"][:n].copy_(src[self.ref_seg * stride:(self.ref_seg + 1) * stride]
-                              .view(n, 2, nb))
-        _lib.check(prn._lib.loki_snr_score_batch(
-            _lib.ptr(t0["folds"]), n, nb, prn.spec, _lib.ptr(t0["scores"]), prn._stream()))
+                              .view(n, *t0["folds"].shape[1:]))
+        if prn.fourier:
+            norm = torch.empty((n, nb), dtype=torch.float32, device=prn._device)
+            _lib.check(prn._lib.loki_fold_norm_complex(_lib.ptr(t0["folds"]), n, nb,
+                                                       _lib.ptr(norm), prn._stream()))
+            _lib.check(prn._lib.loki_boxcar_snr(_lib.ptr(norm), n, nb, prn.spec,
+                                                _lib.ptr(t0["scores"]), prn._stream()))
+        else:
+            _lib.check(prn._lib.loki_snr_score_batch(
+                _lib.ptr(t0["folds"]), n, nb, prn.spec, _lib.ptr(t0["scores"]),
+                prn._stream()))
         t0["scores_ep"][:n].copy_(t0["scores"][:n])
         b.mem["seed_scores"][:n].copy_(t0["scores"][:n])  # level-0 statistics
         t0["bt"][:n].zero_()
@@ -1609,8 +1630,9 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
            "max_sugg": max_sugg, "threshold_scheme": np.asarray(threshold_scheme)}
     kw = {"max_sugg": max_sugg, "batch_size": batch_size, "poly_basis": poly_basis,
           "use_moving_grid": use_moving_grid}
-    batched = driver == "auto" and ascend_levels is None and Pruning(
-        dyp, threshold_scheme, **kw).device_run_supported
+    probe = Pruning(dyp, threshold_scheme, **kw)
+    batched = driver == "auto" and ascend_levels is None and probe.block_batch_supported and (
+        probe.device_run_supported or not probe.circular)
     if batched:
         res_list = PruneBlockBatch(threshold_scheme, **kw).run([(dyp, r) for r in ref_segs])
         results = dict(zip(ref_segs, res_list, strict=True))
@@ -1815,10 +1837,15 @@ class PruneBlockBatch(PruneBatch):
         if not jobs:
             return []
         first = self._slot(0, jobs[0][0])
+        if not first.block_batch_supported:
+            msg = ("the batched drivers cover trees without a parent hook, one best leaf per "
+                   "level, and no circular-orbit tree over complex folds")
+            raise ValueError(msg)
         if first.circular:
             return PruneBatch.run(self, jobs, ascend=ascend)
-        if not first.device_run_supported:
-            msg = "the block driver covers time-domain trees without a parent hook"
+        fourier = first.fourier
+        if fourier and self.driver == "blocks":
+            msg = "complex (Fourier-domain) trees run with driver='batch'"
             raise ValueError(msg)
         dev = jobs[0][0].device
         st = torch.cuda.current_stream(dev)
@@ -1833,7 +1860,7 @@ class PruneBlockBatch(PruneBatch):
                 runs.append((prn, prn._device_run_obj(ref, dyp.nsegments - 1, ascend)))
             nlev = runs[0][1].nlev
             n = len(runs)
-            if all(prn.dyp.fold.dtype == torch.float32 for prn, _ in runs):
+            if not fourier and all(prn.dyp.fold.dtype == torch.float32 for prn, _ in runs):
                 sjobs = (_lib.LokiSeedJob * n)()  # every job's seed in one launch
                 for i, (prn, dr) in enumerate(runs):
                     sjobs[i] = dr.seed_job()
@@ -1842,7 +1869,7 @@ class PruneBlockBatch(PruneBatch):
                 _lib.check(lib.loki_prune_seed_batch(
                     sjobs, n, p0.dyp.cfg.nbins, p0.poly_order, p0.spec, _lib.ptr(sbuf),
                     sbuf.numel(), _lib.stream_ptr(st)))
-            else:  # a fold stored in another type: converted by the per-job copies
+            else:  # complex folds, or a fold stored in another type: per-job seeds
                 for prn, dr in runs:
                     dr.prepare_block()
             if nlev > 0:
@@ -1867,11 +1894,11 @@ class PruneBlockBatch(PruneBatch):
                         tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
                         _lib.ptr(self._scratch), self._scratch.numel(), _lib.stream_ptr(st)))
                 else:
-                    shape = np.zeros(4, np.int64)
+                    shape = np.zeros(5, np.int64)
                     _lib.check(lib.loki_prune_batch_tables(
                         tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
-                        _lib.ptr(self._scratch), self._scratch.numel(), shape.ctypes.data,
-                        _lib.stream_ptr(st)))
+                        int(fourier), _lib.ptr(self._scratch), self._scratch.numel(),
+                        shape.ctypes.data, _lib.stream_ptr(st)))
                     self._enqueue_batch(lib, dev, st, n, nlev, args, shape)
             if ascend and nlev > 0:  # every job's ascend in one launch
                 ajobs = (_lib.LokiAscendJob * n)()
@@ -1880,8 +1907,8 @@ class PruneBlockBatch(PruneBatch):
                 p0 = runs[0][0]
                 abuf = self._dev_buf("ascend", n * C.sizeof(_lib.LokiAscendJob), dev)
                 _lib.check(lib.loki_prune_ascend_batch(
-                    ajobs, n, runs[0][1].asc[4], p0.spec, p0.max_sugg, _lib.ptr(abuf),
-                    abuf.numel(), _lib.stream_ptr(st)))
+                    ajobs, n, runs[0][1].asc[4], p0.spec, p0.max_sugg, int(fourier),
+                    _lib.ptr(abuf), abuf.numel(), _lib.stream_ptr(st)))
             elif ascend:
                 for prn, dr in runs:
                     dr._ascend_enqueue()

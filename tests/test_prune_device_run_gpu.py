@@ -257,3 +257,45 @@ def test_block_batch_passes_circular_to_streams(cuda_device):
     for g, w in zip(got, want, strict=True):
         np.testing.assert_array_equal(g["scores"], w["scores"])
         np.testing.assert_array_equal(g["param_sets"], w["param_sets"])
+
+
+@pytest.mark.parametrize("name", ["prune_taylor_fourier", "prune_cheby_fourier"])
+def test_block_batch_fourier_matches_level_path(cuda_device, name):
+    """Complex (Fourier-domain) trees in the level-synchronous batch: every
+    job's level records, final scores, ascend and report equal the
+    level-by-level complex run's, uncaptured, captured and replayed; the
+    block-per-run driver declines them."""
+    from pyloki_gb300.config import PulsarSearchConfig
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import PruneBlockBatch, Pruning
+    from pyloki_gb300.timeseries import TimeSeries
+    from tests.conftest import load_golden
+
+    d = load_golden(name)
+    cfg = PulsarSearchConfig(
+        nsamps=int(d["nsamps"]), tsamp=float(d["tsamp"]), nbins=int(d["nbins"]),
+        eta=float(d["eta"]), param_limits=d["param_limits"], ducy_max=float(d["ducy_max"]),
+        wtsp=float(d["wtsp"]), use_fourier=True, bseg_ffa=int(d["bseg_ffa"]),
+        prune_poly_order=int(d["poly_order"]), branch_max=int(d["branch_max"]),
+        p_orb_min=float(d["p_orb_min"]))
+    dyp = DynamicProgramming(TimeSeries(d["ts_e"], d["ts_v"], cfg.tsamp), cfg,
+                             device=cuda_device)
+    dyp.initialize()
+    dyp.execute()
+    basis = str(d["basis"]) if "basis" in d else "taylor"
+    kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]), poly_basis=basis,
+              use_moving_grid=bool(d["moving"]))
+    assert Pruning(dyp, d["thresholds"], **kw).fourier
+    refs = [0, int(d["ref_seg"]), dyp.nsegments - 1, 6]
+    runner = PruneBlockBatch(d["thresholds"], **kw)
+    for _ in range(3):
+        got = runner.run([(dyp, r) for r in refs])
+        for ref, g in zip(refs, got, strict=True):
+            want = _level_path_results(lambda: Pruning(dyp, d["thresholds"], **kw), dyp, ref, d)
+            assert [(s.n_branches, s.n_leaves, s.n_leaves_surv, s.score_min, s.score_max)
+                    for s in g["level_stats"]] == want[0], ref
+            np.testing.assert_array_equal(g["scores"], want[1])
+            np.testing.assert_array_equal(g["scores_ep"], want[2])
+            np.testing.assert_array_equal(g["param_sets"], want[3])
+    with pytest.raises(ValueError, match="driver='batch'"):
+        PruneBlockBatch(d["thresholds"], driver="blocks", **kw).run([(dyp, refs[0])])
