@@ -95,18 +95,19 @@ PRUNE_SCHEME_NOTE = "designed (DynamicThresholdScheme, least-cost path at 90% of
 PRUNE_SCORE_BYTES_PER_LEAF = 2 * 64 * 4 + 4 + 8 + 8
 
 
-def make_prune_cfg(circular: bool = False):
+def make_prune_cfg(circular: bool = False, fourier: bool = False):
     """Circular-orbit search with a Taylor tree to the 4th derivative: 2^22
     samples at 64 us, 128 segments, 64 bins, FFA grid (1, 1, 1, 146). With
     ``circular``, the circular-orbit tree of order 5 on the same series (FFA
-    grid (1, 1, 1, 1, 146), P_orb_min 2 h)."""
+    grid (1, 1, 1, 1, 146), P_orb_min 2 h); with ``fourier``, the FFA and the
+    tree over complex (Fourier-domain) folds, the reference's default."""
     from pyloki_gb300 import ParamLimits, PulsarSearchConfig
 
     n = 2**22
     order = 5 if circular else 4
     lim = ParamLimits.from_circular(333.33, p_orb_min=7200.0, poly_order=order)
     return PulsarSearchConfig(nsamps=n, tsamp=64e-6, nbins=64, eta=1.0,
-                              param_limits=lim.limits, use_fourier=False, bseg_ffa=n // 128,
+                              param_limits=lim.limits, use_fourier=fourier, bseg_ffa=n // 128,
                               prune_poly_order=order, p_orb_min=7200.0 if circular else 0.0)
 
 
@@ -319,6 +320,64 @@ def bench_prune_gpu(args, dev) -> dict:
         "clocks": clocks.summary(),
         "survivors": int(prn.world_tree.valid_size),
     }
+
+
+def bench_prune_fourier(args, dev) -> dict:
+    """The pruning step over complex (Fourier-domain) folds, the reference's
+    default mode: the same series, thresholds and reference segments, every
+    run level-synchronously in the batch; beside it one run level by level."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import PruneBlockBatch, Pruning
+
+    cfg = make_prune_cfg(fourier=True)
+    ts, _ = make_prune_series(seed=2000)
+    dyp = DynamicProgramming(ts, cfg, device=dev)
+    dyp.initialize()
+    dyp.execute()
+    nseg = dyp.nsegments
+    thr = prune_thresholds(nseg)
+    refs = [int(r) for r in np.linspace(4, nseg - 5, args.prune_runs).round()]
+    kw = {"max_sugg": PRUNE_MAX_SUGG, "batch_size": PRUNE_BATCH}
+    runner = PruneBlockBatch(thr, **kw)
+    prn = Pruning(dyp, thr, **kw)
+
+    def batched() -> int:
+        res = runner.run([(dyp, r) for r in refs])
+        return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+
+    def level_run() -> int:
+        prn.initialize(nseg // 2)
+        for _ in range(nseg - 1):
+            prn.execute_iter()
+            if prn.prune_complete:
+                break
+        prn._do_ascend()
+        return sum(st.n_leaves for st in prn.pstats[1:])
+
+    def timed(fn, steps):
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        n = sum(fn() for _ in range(steps))
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return n, e0.elapsed_time(e1)
+
+    for _ in range(2):  # uncaptured, then captured
+        batched()
+    level_run()
+    steps = max(1, min(args.steps, 3))
+    leaves, ms = timed(batched, steps)
+    plain_leaves, plain_ms = timed(level_run, 1)
+    return {"metric": "prune leaves/s (complex folds)", "value": leaves / (ms * 1e-3),
+            "unit": "leaves/s", "ms_per_step": ms / steps, "leaves_per_step": leaves // steps,
+            "plain": {"value": plain_leaves / (plain_ms * 1e-3), "ms_per_run": plain_ms,
+                      "leaves_per_run": plain_leaves},
+            "config": {"workload": PRUNE_WORKLOAD.replace("prune", "prune_fourier"),
+                       "ref_segments": len(refs), "fold": "complex64, nbins // 2 + 1",
+                       "driver": "level-synchronous batch (loki_prune_run_batch, fourier)"}}
 
 
 def final_trials(cfg) -> int:
@@ -617,6 +676,8 @@ def bench_gpu(args) -> dict | None:
         out["prune"] = bench_prune_gpu(args, dev)
         if world == 1 and not args.no_cpu_baseline:
             out["prune"]["cpu_baseline"] = prune_cpu()
+        if not args.no_fourier and world == 1:
+            out["prune_fourier"] = bench_prune_fourier(args, dev)
         if not args.no_learned:
             out["prune"]["learned"] = bench_learned(args, dev)
         if not args.no_thresholds:
@@ -1358,7 +1419,8 @@ def main() -> None:
 
 
 # side studies printed on their own lines before the headline
-SECTIONS = ("ffa_bf16", "ffa_precision", "batch", "injection", "ffa_fourier", "threshold_design")
+SECTIONS = ("ffa_bf16", "ffa_precision", "batch", "injection", "ffa_fourier", "prune_fourier",
+            "threshold_design")
 HEADLINE_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                  "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "impl",
                  "gpu_launches", "clocks")
