@@ -1912,9 +1912,17 @@ class PruneBlockBatch(PruneBatch):
             elif ascend:
                 for prn, dr in runs:
                     dr._ascend_enqueue()
-            for prn, dr in runs:
-                dr.copy_stats_async()
-            st.synchronize()
+            # every job's level records, error word and seed scores: one
+            # gather launch and one copy
+            isz = _lib.PRUNE_STATS_DTYPE.itemsize
+            raw = self._gather_read(
+                lib, dev, st, [[(dr.bufs.mem["stats"], dr.nlev * isz), (prn._err, 4),
+                                (dr.bufs.mem["seed_scores"], dr.seed.size * 4)]
+                               for prn, dr in runs], "stats")
+            for (prn, dr), (b_st, b_err, b_seed) in zip(runs, raw, strict=True):
+                dr._h_stats = torch.from_numpy(np.frombuffer(b_st, np.uint8).copy())
+                dr._h_err = torch.from_numpy(np.frombuffer(b_err, np.int32).copy())
+                dr._h_seed = torch.from_numpy(np.frombuffer(b_seed, np.float32).copy())
             ready = []
             for prn, dr in runs:
                 stats, err, last, nf = dr.stats_host()
@@ -1946,24 +1954,31 @@ class PruneBlockBatch(PruneBatch):
         return t
 
     def _read_trees(self, lib, dev, st, ready):
-        """Every job's final rows (leaves, scores, scores_ep) packed on the
-        device by one gather launch and read back with one copy."""
+        """Every job's final rows (leaves, scores, scores_ep)."""
+        return self._gather_read(lib, dev, st, [dr.tree_parts(nf) for _, dr, _, _, nf in ready],
+                                 "trees")
+
+    def _gather_read(self, lib, dev, st, groups, name: str):
+        """Device ranges (per job a list of (tensor, bytes)) packed on the
+        device by one gather launch and read back with one copy; returns the
+        bytes of every range, per job."""
         parts, offs, off = [], [], 0
-        for _, dr, _, _, nf in ready:
+        for group in groups:
             row = []
-            for t, nb in dr.tree_parts(nf):
+            for t, nb in group:
                 parts.append((t, nb, off))
                 row.append((off, nb))
                 off += (nb + 15) // 16 * 16
             offs.append(row)
-        packed = self._dev_buf("packed", off, dev)
-        pin = self.__dict__.get("_pin")
+        packed = self._dev_buf(f"packed_{name}", off, dev)
+        pins = self.__dict__.setdefault("_pins", {})
+        pin = pins.get(name)
         if pin is None or pin.numel() < off:
-            pin = self._pin = torch.empty(max(off, 256), dtype=torch.uint8, pin_memory=True)
+            pin = pins[name] = torch.empty(max(off, 256), dtype=torch.uint8, pin_memory=True)
         tab = (_lib.LokiGatherPart * len(parts))()
         for i, (t, nb, o) in enumerate(parts):
             tab[i].src, tab[i].bytes, tab[i].dst_off = _lib.ptr(t), nb, o
-        pbuf = self._dev_buf("parts", len(parts) * C.sizeof(_lib.LokiGatherPart), dev)
+        pbuf = self._dev_buf(f"parts_{name}", len(parts) * C.sizeof(_lib.LokiGatherPart), dev)
         _lib.check(lib.loki_gather_parts(tab, len(parts), _lib.ptr(packed), packed.numel(),
                                          _lib.ptr(pbuf), pbuf.numel(), _lib.stream_ptr(st)))
         if off:
