@@ -380,6 +380,61 @@ def bench_prune_fourier(args, dev) -> dict:
                        "driver": "level-synchronous batch (loki_prune_run_batch, fourier)"}}
 
 
+def bench_prune_circ(args, dev) -> dict:
+    """The pruning step of the circular-orbit tree (order 5, crackle added)
+    on the same series and thresholds: every run level-synchronously in the
+    batch; beside it the same runs each device-resident in its own CUDA
+    graph on several streams."""
+    import torch
+
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import PruneBatch, PruneBlockBatch
+
+    cfg = make_prune_cfg(circular=True)
+    ts, _ = make_prune_series(seed=2000)
+    dyp = DynamicProgramming(ts, cfg, device=dev)
+    dyp.initialize()
+    dyp.execute()
+    nseg = dyp.nsegments
+    thr = prune_thresholds(nseg)
+    refs = [int(r) for r in np.linspace(4, nseg - 5, args.prune_runs).round()]
+    kw = {"max_sugg": PRUNE_MAX_SUGG, "batch_size": PRUNE_BATCH}
+    runner = PruneBlockBatch(thr, **kw)
+    streams = PruneBatch(thr, n_streams=args.prune_streams, **kw)
+
+    def batched() -> int:
+        res = runner.run([(dyp, r) for r in refs])
+        return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+
+    def batched_streams() -> int:
+        res = streams.run([(dyp, r) for r in refs])
+        return sum(st.n_leaves for r in res for st in r["level_stats"][1:])
+
+    def timed(fn, steps):
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        n = sum(fn() for _ in range(steps))
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return n, e0.elapsed_time(e1)
+
+    for _ in range(2):  # uncaptured, then captured
+        batched()
+        batched_streams()
+    steps = max(1, min(args.steps, 3))
+    leaves, ms = timed(batched, steps)
+    s_leaves, s_ms = timed(batched_streams, steps)
+    return {"metric": "prune leaves/s (circular-orbit tree)", "value": leaves / (ms * 1e-3),
+            "unit": "leaves/s", "ms_per_step": ms / steps, "leaves_per_step": leaves // steps,
+            "streams": {"value": s_leaves / (s_ms * 1e-3), "ms_per_step": s_ms / steps,
+                        "note": (f"each run device-resident in its own CUDA graph, "
+                                 f"{args.prune_streams} runs at once on their own streams")},
+            "config": {"workload": "circ5_prune_circular_orbit_2^22",
+                       "ref_segments": len(refs), "poly_order": 5,
+                       "driver": "level-synchronous batch (loki_prune_run_batch, basis 2)"}}
+
+
 def final_trials(cfg) -> int:
     return int(np.prod(cfg.get_param_grid_count(cfg.niters_ffa)))
 
@@ -678,6 +733,8 @@ def bench_gpu(args) -> dict | None:
             out["prune"]["cpu_baseline"] = prune_cpu()
         if not args.no_fourier and world == 1:
             out["prune_fourier"] = bench_prune_fourier(args, dev)
+        if world == 1:
+            out["prune_circ"] = bench_prune_circ(args, dev)
         if not args.no_learned:
             out["prune"]["learned"] = bench_learned(args, dev)
         if not args.no_thresholds:
@@ -1420,7 +1477,7 @@ def main() -> None:
 
 # side studies printed on their own lines before the headline
 SECTIONS = ("ffa_bf16", "ffa_precision", "batch", "injection", "ffa_fourier", "prune_fourier",
-            "threshold_design")
+            "prune_circ", "threshold_design")
 HEADLINE_KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                  "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "impl",
                  "gpu_launches", "clocks")

@@ -639,7 +639,7 @@ typedef struct {
   const float* ffa_fold;   /* segment rows of this job's FFA fold */
   int64_t seg_stride;      /* floats between segments */
   int64_t seed_n;          /* parents already in run.trees[0] (leaves, folds, scores) */
-  LokiPruneRun run;        /* as for loki_prune_run (Taylor / Chebyshev: no circular fields) */
+  LokiPruneRun run;        /* as for loki_prune_run (circular fields for basis 2 only) */
   int32_t* dev_err;        /* device error word */
 } LokiPruneJob;
 
@@ -666,7 +666,11 @@ int64_t loki_prune_run_blocks_scratch_bytes(int32_t njobs, int32_t nlevels);
  * a batch costs the launches of a single run and each step spreads over the
  * whole GPU; no host wait, so the enqueue can be captured in a CUDA graph.
  * dev_scratch of loki_prune_run_blocks_scratch_bytes bytes; njobs <= 65535.
- * Taylor and Chebyshev trees (not basis 2). */
+ * Taylor and Chebyshev trees, and the circular-orbit tree on real folds
+ * (basis 2, poly_order 5, the jobs' runs with their circular fields): its
+ * level adds the crackle-expansion scan, the batch-ordered child map, the
+ * validity compaction and the valid-child batch offsets of loki_prune_run's
+ * circular level, each one launch over every job. */
 int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
                          const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
                          const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
@@ -675,14 +679,16 @@ int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPrun
 /* loki_prune_run_batch in two halves, so that the kernels can be captured
  * in a CUDA graph once and replayed: loki_prune_batch_tables checks the jobs
  * and copies the tables into dev_scratch (host memory is read: not inside a
- * capture) and writes the batch's shape (5 words: nbins, poly_order, largest
- * par_cap, largest child_cap, fourier); loki_prune_batch_enqueue enqueues the kernels
+ * capture) and writes the batch's shape (6 words: nbins, poly_order, largest
+ * par_cap, largest child_cap, fourier, circular-orbit tree);
+ * loki_prune_batch_enqueue enqueues the kernels
  * over the tables in dev_scratch for that shape. A replay after
  * loki_prune_batch_tables with new jobs of the same count, levels and shape
  * runs the new jobs. fourier != 0: complex (Fourier-domain) trees, the
  * jobs' tree folds (cap, 2, nbins / 2 + 1) complex64, fold rows and
  * seg_stride in complex elements (the complex level kernels' per-child code,
- * prune.py:165-332 with PruneTaylorComplexDPFuncts). */
+ * prune.py:165-332 with PruneTaylorComplexDPFuncts; Taylor and Chebyshev
+ * trees). */
 int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
                             const LokiPruneLevel* levels, const int32_t* seg_idx,
                             const double* thresholds, int32_t nlevels,

@@ -3312,49 +3312,54 @@ __global__ void bj_branch_kernel(BatchTabs T, int l) {
                nullptr);
 }
 
-// The two scans of a level, per job: mode 0 the child counts of the parents
-// (in place in offsets, scratch w.scan), mode 1 the score >= threshold flags
-// of the children (into the positions after w.sscan's sums).
+// The scans of a level, per job. Counts (in place, scratch w.scan): mode 0
+// the parents' child counts (offsets), mode 2 the circular tree's crackle
+// expansion counts (exp_off), both over counts[0] parents. Flags (into the
+// positions after w.sscan's sums): mode 1 score >= threshold over counts[1]
+// children, mode 3 the circular tree's validity flags over counts[1]
+// children, mode 4 score >= threshold over counts[4] valid children.
 __device__ __forceinline__ void bj_scan_args(const BatchTabs& T, int l, int mode,
                                              const void** in, int64_t** out, int64_t** sums,
                                              int64_t* n, double* thr) {
   const LokiPruneJob& J = T.jobs[blockIdx.y];
   const LokiPruneWork& w = J.run.work;
-  if (mode == 0) {
-    *in = w.offsets;
-    *out = w.offsets;
+  if (mode == 0 || mode == 2) {
+    int64_t* a = mode == 0 ? w.offsets : J.run.exp_off;
+    *in = a;
+    *out = a;
     *sums = reinterpret_cast<int64_t*>(w.scan);
     *n = J.run.counts[0];
     *thr = 0.0;
   } else {
-    *in = w.child_scores;
+    *in = mode == 3 ? static_cast<const void*>(J.run.valid_flags)
+                    : static_cast<const void*>(w.child_scores);
     *out = job_pos(w);
     *sums = reinterpret_cast<int64_t*>(w.sscan);
-    *n = J.run.counts[1];
-    *thr = T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+    *n = J.run.counts[mode == 4 ? 4 : 1];
+    *thr = mode == 3 ? 0.5 : T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
   }
 }
 
 template <bool FLAGS>
-__global__ void __launch_bounds__(kScanBlock) bj_scan_block_kernel(BatchTabs T, int l) {
+__global__ void __launch_bounds__(kScanBlock) bj_scan_block_kernel(BatchTabs T, int l, int mode) {
   __shared__ int64_t warp_tot[32];
   const void* in;
   int64_t *out, *sums, n;
   double thr;
-  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  bj_scan_args(T, l, mode, &in, &out, &sums, &n, &thr);
   const int64_t ntiles = (n + kScanBlock - 1) / kScanBlock;
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x)
     scan_tile<FLAGS>(in, n, thr, out, sums, t, warp_tot);
 }
 
 template <bool FLAGS>
-__global__ void __launch_bounds__(kScanBlock) bj_scan_sums_kernel(BatchTabs T, int l) {
+__global__ void __launch_bounds__(kScanBlock) bj_scan_sums_kernel(BatchTabs T, int l, int mode) {
   __shared__ int64_t warp_tot[32];
   __shared__ int64_t carry;
   const void* in;
   int64_t *out, *sums, n;
   double thr;
-  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  bj_scan_args(T, l, mode, &in, &out, &sums, &n, &thr);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t nblocks = (n + kScanBlock - 1) / kScanBlock;
   if (threadIdx.x == 0) carry = 0;
@@ -3391,11 +3396,11 @@ __global__ void __launch_bounds__(kScanBlock) bj_scan_sums_kernel(BatchTabs T, i
 }
 
 template <bool FLAGS>
-__global__ void __launch_bounds__(kScanBlock) bj_scan_add_kernel(BatchTabs T, int l) {
+__global__ void __launch_bounds__(kScanBlock) bj_scan_add_kernel(BatchTabs T, int l, int mode) {
   const void* in;
   int64_t *out, *sums, n;
   double thr;
-  bj_scan_args(T, l, FLAGS ? 1 : 0, &in, &out, &sums, &n, &thr);
+  bj_scan_args(T, l, mode, &in, &out, &sums, &n, &thr);
   for (int64_t i = (int64_t)blockIdx.x * kScanBlock + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kScanBlock)
     out[i] += sums[i / kScanBlock];
@@ -3434,32 +3439,38 @@ bj_score_kernel(BatchTabs T, int l, LokiScoreSpec sp, ScoreK SK) {
   }
 }
 
-__global__ void bj_scatter_kernel(BatchTabs T, int l) {
+// mode 1: survivors among counts[1] children; mode 3: the circular tree's
+// valid children (valid_ids) among counts[1]; mode 4: survivors among
+// counts[4] valid children.
+__global__ void bj_scatter_kernel(BatchTabs T, int l, int mode) {
   const LokiPruneJob& J = T.jobs[blockIdx.y];
   const LokiPruneWork& w = J.run.work;
-  const double thr = T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
-  const int64_t n = J.run.counts[1];
+  const double thr = mode == 3 ? 0.5 : T.thr[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  const float* f = mode == 3 ? J.run.valid_flags : w.child_scores;
+  int64_t* ids = mode == 3 ? J.run.valid_ids : w.surv;
+  const int64_t n = J.run.counts[mode == 4 ? 4 : 1];
   const int64_t* pos = job_pos(w);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    if ((double)w.child_scores[i] >= thr) w.surv[pos[i]] = i;
+    if ((double)f[i] >= thr) ids[pos[i]] = i;
 }
 
 // one block per job: the survivor count, and the overflow rule when it
 // exceeds max_sugg
 __global__ void __launch_bounds__(kSelThreads)
-bj_overflow_kernel(BatchTabs T, int l, int64_t max_sugg, int64_t batch) {
+bj_overflow_kernel(BatchTabs T, int l, int64_t max_sugg, int64_t batch, int circ) {
   const LokiPruneJob& J = T.jobs[blockIdx.x];
   const LokiPruneRun& R = J.run;
   const LokiPruneWork& w = R.work;
   int64_t* cnt = R.counts;
-  const int64_t n_sel = job_pos(w)[cnt[1]];
+  const int64_t n_sel = job_pos(w)[cnt[circ ? 4 : 1]];
   const int64_t n_par = cnt[0];
   __syncthreads();  // every thread has read the counters
   if (threadIdx.x == 0) cnt[2] = n_sel;
   if (n_sel <= max_sugg) return;  // uniform over the block
   if (threadIdx.x == 0) *R.ovf_flag = 1;
-  select_overflow_block(w.child_scores, w.offsets, n_par, batch,
+  // the circular tree's batches are over its valid children
+  select_overflow_block(w.child_scores, circ ? R.batch_offsets : w.offsets, n_par, batch,
                         T.thr[(size_t)blockIdx.x * T.nlevels + (l - 1)], max_sugg, w.surv,
                         cnt + 2, w.ovf_thr, w.ovf_ids, reinterpret_cast<unsigned*>(w.ovf_keys));
 }
@@ -3545,6 +3556,116 @@ __global__ void __launch_bounds__(kPruneWarps * 32) bj_emit_complex_kernel(Batch
                      out.backtracks, s);
 }
 
+// circular-orbit tree (real folds): the steps of circ_level_dev per job
+__global__ void bj_circ_branch_kernel(BatchTabs T, int l) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneLevel& D = T.levels[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  const LokiPruneRun& R = J.run;
+  const int64_t n = R.counts[0];
+  const double* leaves = R.trees[(l - 1) & 1].leaves;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    circ_branch_one(D, leaves, i, reinterpret_cast<LokiBranchInfo*>(R.work.info),
+                    R.work.offsets, R.exp_off, J.dev_err);
+}
+
+// the batch-ordered child map and validity flags; counts[1] = every child,
+// or 0 above the workspace (flagged)
+__global__ void bj_circ_map_kernel(BatchTabs T, int l, int64_t batch) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const LokiPruneLevel& D = T.levels[(size_t)blockIdx.y * T.nlevels + (l - 1)];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  int64_t* cnt = R.counts;
+  const int64_t n = cnt[0];
+  const int64_t total = w.offsets[n] + R.exp_off[n];
+  const bool fits = total <= w.child_cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[1] = fits ? total : 0;
+    LokiPruneLevelStats* st = R.stats + (l - 1);
+    st->n_parents = n;
+    st->n_children = total;
+    if (!fits) atomicOr(J.dev_err, LOKI_DEVERR_CAPACITY);
+  }
+  if (!fits) return;
+  const double* leaves = R.trees[(l - 1) & 1].leaves;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    circ_map_one(D, leaves, n, batch, reinterpret_cast<const LokiBranchInfo*>(w.info),
+                 w.offsets, R.exp_off, reinterpret_cast<CircChild*>(R.child_map),
+                 R.valid_flags, i);
+}
+
+// the per-batch "holds Taylor children" flags of the current parents
+__global__ void bj_circ_clear_kernel(BatchTabs T, int64_t batch) {
+  const LokiPruneRun& R = T.jobs[blockIdx.y].run;
+  const int64_t nb = R.counts[0] / batch + 1;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nb;
+       i += (int64_t)gridDim.x * blockDim.x)
+    R.batch_taylor[i] = 0;
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_circ_score_kernel(BatchTabs T, int l, LokiScoreSpec sp, ScoreK SK, int64_t batch) {
+  extern __shared__ float tiles[];
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const float* seg = J.ffa_fold + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int warp = threadIdx.x >> 5;
+  float* tile = tiles + (size_t)warp * 32 * score_stride(D.nbins, sp.wmax);
+  int64_t* cnt = R.counts;
+  const int64_t n_valid = job_pos(w)[cnt[1]];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[4] = n_valid;
+    R.stats[l - 1].n_valid = n_valid;
+  }
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_valid;
+       t += (int64_t)gridDim.x * kPruneWarps) {
+    circ_score_tile(D, in.leaves, in.folds, batch,
+                    reinterpret_cast<const LokiBranchInfo*>(w.info),
+                    reinterpret_cast<const CircChild*>(R.child_map), R.valid_ids, n_valid, seg,
+                    sp, SK, w.child_scores, w.child_idx, w.child_phase, R.child_class,
+                    R.batch_taylor, reinterpret_cast<unsigned*>(w.minmax), tile, t * 32);
+    __syncwarp();
+  }
+}
+
+// valid-child offsets at the parents (the overflow rule reads those at
+// batch boundaries)
+__global__ void bj_circ_boff_kernel(BatchTabs T) {
+  const LokiPruneRun& R = T.jobs[blockIdx.y].run;
+  const int64_t n = R.counts[0], n_valid = R.counts[4];
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= n;
+       p += (int64_t)gridDim.x * blockDim.x)
+    R.batch_offsets[p] = lower_bound64(R.valid_ids, n_valid, R.work.offsets[p] + R.exp_off[p]);
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_circ_emit_kernel(BatchTabs T, int l, int64_t batch) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const LokiPruneTree& out = R.trees[l & 1];
+  const float* seg = J.ffa_fold + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int warp = threadIdx.x >> 5;
+  const int64_t n_surv = R.counts[2];
+  for (int64_t t = (int64_t)blockIdx.x * kPruneWarps + warp; t * 32 < n_surv;
+       t += (int64_t)gridDim.x * kPruneWarps)
+    circ_emit_tile(D, in.leaves, in.folds, batch,
+                   reinterpret_cast<const LokiBranchInfo*>(w.info),
+                   reinterpret_cast<const CircChild*>(R.child_map), R.valid_ids, seg, w.surv,
+                   n_surv, w.child_scores, w.child_idx, w.child_phase, R.child_class,
+                   R.batch_taylor, out.leaves, out.folds, out.scores, out.scores_ep,
+                   out.backtracks, t * 32);
+}
+
 __global__ void bj_bt_kernel(BatchTabs T, int l, int row) {
   const LokiPruneJob& J = T.jobs[blockIdx.y];
   const LokiPruneRun& R = J.run;
@@ -3583,6 +3704,7 @@ struct BatchShape {
   int nbins, poly_order;
   int64_t max_par, max_child;
   int fourier;  // complex (Fourier-domain) folds
+  int circ;     // circular-orbit tree (real folds, poly_order 5)
 };
 
 static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
@@ -3606,14 +3728,19 @@ static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPrune
         levels[k].nbins != nb)
       return set_error(LOKI_ERR_INVALID, "levels of different trees");
   }
-  if (levels[0].basis == 2)
-    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree runs in loki_prune_run");
+  const bool circ = levels[0].basis == 2;
+  if (circ && (fourier || P != 5))
+    return set_error(LOKI_ERR_UNSUPPORTED,
+                     "the circular-orbit tree runs on real folds with poly_order 5");
   for (int j = 0; j < njobs; ++j) {
     const LokiPruneJob& J = jobs[j];
     const LokiPruneRun& R = J.run;
     const LokiPruneWork& w = R.work;
     if (!J.ffa_fold || J.seg_stride < 1 || !J.dev_err || J.seed_n < 0 || J.seed_n > max_sugg)
       return set_error(LOKI_ERR_INVALID, "job %d: bad fold, error word or seed", j);
+    if (circ && (!R.exp_off || !R.child_map || !R.valid_flags || !R.valid_ids ||
+                 !R.child_class || !R.batch_taylor || !R.batch_offsets))
+      return set_error(LOKI_ERR_INVALID, "job %d: no circular-orbit workspace", j);
     if (R.trees[0].cap < max_sugg || R.trees[1].cap < max_sugg || w.par_cap < max_sugg ||
         w.child_cap < 1 || w.ovf_cap < max_sugg + w.child_cap + 1)
       return set_error(LOKI_ERR_CAPACITY, "job %d: workspace below max_sugg / child_cap", j);
@@ -3651,6 +3778,7 @@ static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPrune
   shape->max_par = max_par;
   shape->max_child = max_child;
   shape->fourier = fourier ? 1 : 0;
+  shape->circ = circ ? 1 : 0;
   return LOKI_OK;
 }
 
@@ -3673,7 +3801,9 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
   if (smem > 200 * 1024)
     return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
   if (smem > 48 * 1024 && (cplx ? set_smem_limit(bj_score_complex_kernel, smem)
-                                : set_smem_limit(bj_score_kernel, smem)) != cudaSuccess)
+                                : shape.circ ? set_smem_limit(bj_circ_score_kernel, smem)
+                                             : set_smem_limit(bj_score_kernel, smem)) !=
+                              cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -3709,29 +3839,63 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
   const unsigned g_emit =
       per_job(6 * nsm * spread, (max_par + kPruneWarps * 32 - 1) / (kPruneWarps * 32));
   const int row_bt = P + 2, row_leaf = (P + 2) * 2;
+  int l_cur = 1;
+  auto scan = [&](int mode, unsigned g) {
+    if (mode == 0 || mode == 2) {
+      bj_scan_block_kernel<false><<<dim3(g, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+      bj_scan_sums_kernel<false><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+      bj_scan_add_kernel<false><<<dim3(g, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+    } else {
+      bj_scan_block_kernel<true><<<dim3(g, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+      bj_scan_sums_kernel<true><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+      bj_scan_add_kernel<true><<<dim3(g, njobs), kScanBlock, 0, s>>>(T, l_cur, mode);
+    }
+  };
   note_launch();
   bj_seed_kernel<<<(unsigned)njobs, 1, 0, s>>>(T);
   for (int l = 1; l <= nlevels; ++l) {
-    for (int i = 0; i < 13; ++i) note_launch();
-    bj_branch_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l);
-    bj_scan_block_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
-    bj_scan_sums_kernel<false><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
-    bj_scan_add_kernel<false><<<dim3(g_scan_p, njobs), kScanBlock, 0, s>>>(T, l);
-    if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
-    if (cplx)
-      bj_score_complex_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp);
-    else
-      bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
-    if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
-    bj_scan_block_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
-    bj_scan_sums_kernel<true><<<dim3(1, njobs), kScanBlock, 0, s>>>(T, l);
-    bj_scan_add_kernel<true><<<dim3(g_scan_c, njobs), kScanBlock, 0, s>>>(T, l);
-    bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l);
-    bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size);
-    if (cplx)
-      bj_emit_complex_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
-    else
-      bj_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+    l_cur = l;
+    if (shape.circ) {
+      // circ_level_dev's steps for every job at once
+      for (int i = 0; i < 21; ++i) note_launch();
+      bj_circ_branch_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l);
+      scan(0, g_scan_p);
+      scan(2, g_scan_p);
+      bj_circ_map_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l, batch_size);
+      scan(3, g_scan_c);
+      bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, 3);
+      bj_circ_clear_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, batch_size);
+      if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
+      bj_circ_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK,
+                                                                               batch_size);
+      if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
+      bj_circ_boff_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T);
+      scan(4, g_scan_c);
+      bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, 4);
+      bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size,
+                                                                 1);
+      bj_circ_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l, batch_size);
+    } else {
+      for (int i = 0; i < 11; ++i) note_launch();
+      bj_branch_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l);
+      scan(0, g_scan_p);
+      if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
+      if (cplx)
+        bj_score_complex_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp);
+      else
+        bj_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK);
+      if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
+      scan(1, g_scan_c);
+      bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, 1);
+      bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size,
+                                                                 0);
+      if (cplx)
+        bj_emit_complex_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+      else
+        bj_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l);
+    }
+    note_launch();
+    note_launch();
     bj_bt_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, row_bt);
     bj_best_kernel<<<(unsigned)njobs, 1024, 0, s>>>(T, l, row_leaf);
     int rc = check_launch("prune_run_batch");
@@ -3772,6 +3936,7 @@ extern "C" int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
   shape_out[2] = shape.max_par;
   shape_out[3] = shape.max_child;
   shape_out[4] = shape.fourier;
+  shape_out[5] = shape.circ;
   return LOKI_OK;
 }
 
@@ -3788,8 +3953,10 @@ extern "C" int loki_prune_batch_score_times(void* dev_scratch, int32_t njobs, in
   shape.max_par = shape_in[2];
   shape.max_child = shape_in[3];
   shape.fourier = shape_in[4] != 0;
+  shape.circ = shape_in[5] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
-      shape.max_par < 1 || shape.max_child < 1)
+      shape.max_par < 1 || shape.max_child < 1 ||
+      (shape.circ && (shape.fourier || shape.poly_order != 5)))
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
   int rc = prune_spec_check(spec, shape.nbins);
   if (rc) return rc;
@@ -3825,8 +3992,10 @@ extern "C" int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_
   shape.max_par = shape_in[2];
   shape.max_child = shape_in[3];
   shape.fourier = shape_in[4] != 0;
+  shape.circ = shape_in[5] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
-      shape.max_par < 1 || shape.max_child < 1)
+      shape.max_par < 1 || shape.max_child < 1 ||
+      (shape.circ && (shape.fourier || shape.poly_order != 5)))
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
   int rc = prune_spec_check(spec, shape.nbins);
   if (rc) return rc;
@@ -3926,8 +4095,9 @@ extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs,
         !J.dt_seg || !J.seg_idx || !J.ffa_fold || J.seg_stride < 1 || !J.dev_err)
       return set_error(LOKI_ERR_INVALID, "ascend job %d: null pointer or bad stride", j);
   }
-  if (jobs[0].lvl.basis == 2)
-    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit ascend runs per job");
+  if (jobs[0].lvl.basis == 2 && fourier)
+    return set_error(LOKI_ERR_UNSUPPORTED,
+                     "the circular-orbit ascend over complex folds runs per job");
   int rc = prune_spec_check(spec, nb);
   if (rc) return rc;
   LokiScoreSpec sp = *spec;

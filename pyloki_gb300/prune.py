@@ -996,8 +996,7 @@ class Pruning:
     def block_batch_supported(self) -> bool:
         """``PruneBlockBatch`` covers this configuration: every tree without
         a parent hook and one best leaf per level, except the circular-orbit
-        tree over complex folds (the circular tree over real folds runs
-        through ``PruneBatch``)."""
+        tree over complex folds."""
         return (self.intermediate_k == 1 and self.parent_hook is None
                 and not (self.fourier and self.circular))
 
@@ -1769,8 +1768,9 @@ class PruneBlockBatch(PruneBatch):
     and run buffers (kept across calls, rebound to each job's fold). The
     ascend, the read-back and the results are those of ``PruneBatch``; a job
     that outgrows its workspace is repeated with grown buffers through
-    ``loki_prune_run``. Taylor and Chebyshev trees; circular-orbit trees go
-    through ``PruneBatch``.
+    ``loki_prune_run``. Taylor, Chebyshev and (with the level-synchronous
+    driver, real folds) circular-orbit trees; the block-per-run driver passes
+    circular-orbit trees to ``PruneBatch``.
     """
 
     def __init__(self, threshold_scheme, *, max_jobs: int = 152, driver: str = "batch",
@@ -1841,7 +1841,7 @@ class PruneBlockBatch(PruneBatch):
             msg = ("the batched drivers cover trees without a parent hook, one best leaf per "
                    "level, and no circular-orbit tree over complex folds")
             raise ValueError(msg)
-        if first.circular:
+        if first.circular and self.driver == "blocks":
             return PruneBatch.run(self, jobs, ascend=ascend)
         fourier = first.fourier
         if fourier and self.driver == "blocks":
@@ -1894,7 +1894,7 @@ class PruneBlockBatch(PruneBatch):
                         tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
                         _lib.ptr(self._scratch), self._scratch.numel(), _lib.stream_ptr(st)))
                 else:
-                    shape = np.zeros(5, np.int64)
+                    shape = np.zeros(6, np.int64)
                     _lib.check(lib.loki_prune_batch_tables(
                         tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
                         int(fourier), _lib.ptr(self._scratch), self._scratch.numel(),

@@ -195,14 +195,17 @@ def _level_path_results(prn_factory, dyp, ref, d):
 
 
 @pytest.mark.parametrize("name", ["prune_taylor", "prune_taylor_overflow", "prune_cheby",
-                                  "prune_taylor_quad", "prune_cheby_fixed"])
+                                  "prune_taylor_quad", "prune_cheby_fixed", "prune_circ",
+                                  "prune_circ_b4"])
 @pytest.mark.parametrize("max_jobs", [3, 64])
 @pytest.mark.parametrize("driver", ["batch", "blocks"])
 def test_block_batch_matches_level_path(cuda_device, name, max_jobs, driver):
-    """One thread block per job (loki_prune_run_blocks): every job's level
-    records, final scores, ascend and report equal the level-by-level run's,
-    in one launch or in waves of three; the overflow fixture runs the
-    overflow rule inside the block."""
+    """The level-synchronous batch (loki_prune_batch_*) and one thread block
+    per job (loki_prune_run_blocks): every job's level records, final scores,
+    ascend and report equal the level-by-level run's, in one launch or in
+    waves of three; the overflow fixture runs the overflow rule, the
+    circular-orbit fixtures (batch of 64 and of 4 parents) the circular
+    level's child map, validity compaction and batch offsets."""
     from pyloki_gb300.prune import PruneBlockBatch, Pruning
 
     d, prn = _run(name, cuda_device)
@@ -224,13 +227,15 @@ def test_block_batch_matches_level_path(cuda_device, name, max_jobs, driver):
             np.testing.assert_array_equal(g["param_sets"], want[3])
 
 
-@pytest.mark.parametrize("driver", ["batch", "blocks"])
-def test_block_batch_grows_workspaces(cuda_device, driver):
+@pytest.mark.parametrize(("name", "driver"), [("prune_taylor", "batch"),
+                                             ("prune_taylor", "blocks"),
+                                             ("prune_circ", "batch")])
+def test_block_batch_grows_workspaces(cuda_device, name, driver):
     """A job whose children outgrow the batched drivers' workspace is flagged
     on the device and repeated with grown buffers: the results do not change."""
     from pyloki_gb300.prune import PruneBlockBatch, Pruning
 
-    d, prn = _run("prune_taylor", cuda_device)
+    d, prn = _run(name, cuda_device)
     dyp = prn.dyp
     kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
     runner = PruneBlockBatch(d["thresholds"], max_jobs=4, driver=driver, **kw)
@@ -246,13 +251,14 @@ def test_block_batch_grows_workspaces(cuda_device, driver):
 
 
 def test_block_batch_passes_circular_to_streams(cuda_device):
+    """The block-per-run driver hands circular-orbit trees to PruneBatch."""
     from pyloki_gb300.prune import PruneBlockBatch, run_batch
 
     d, prn = _run("prune_circ", cuda_device)
     dyp = prn.dyp
     kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
     refs = [int(d["ref_seg"]), 1]
-    got = PruneBlockBatch(d["thresholds"], **kw).run([(dyp, r) for r in refs])
+    got = PruneBlockBatch(d["thresholds"], driver="blocks", **kw).run([(dyp, r) for r in refs])
     want = run_batch([(dyp, r) for r in refs], d["thresholds"], n_streams=2, **kw)
     for g, w in zip(got, want, strict=True):
         np.testing.assert_array_equal(g["scores"], w["scores"])
