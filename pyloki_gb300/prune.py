@@ -1130,7 +1130,7 @@ class Pruning:
                     self._do_ascend()
         if asc is None or self.prune_level not in asc:
             self._do_ascend()
-        return {
+        res = {
             "run_name": f"{ref_seg:03d}_{task_id:02d}",
             "scheme": self.scheme.data.copy(),
             "param_sets": self.report(),
@@ -1138,6 +1138,13 @@ class Pruning:
             "scores_ep": self.world_tree.scores_ep.cpu().numpy(),
             "level_stats": self.pstats,
         }
+        if result_file is not None:  # prune.py:599-607: the run appended to the file
+            from pyloki_gb300.results import PruneResultWriter
+
+            with PruneResultWriter(result_file, mode="a") as writer:
+                writer.write_run_results(res["run_name"], res["scheme"], res["param_sets"],
+                                         res["scores"], res["scores_ep"], res["level_stats"])
+        return res
 
     def trace_integration_path(self, survivor_idx: int,
                                level: int | None = None) -> list[PruneIntegrationStep]:
@@ -1596,8 +1603,10 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     asked for; otherwise, and with ``driver="threads"``, ``n_workers`` runs
     proceed at once, each on its own host thread and CUDA stream
     (``run_many``). Every run is the same computation as on its own.
-    Results are written as one ``.npz`` with the reference's per-run groups
-    (``runs/<ref:03d>_<task:02d>/{scheme, param_sets, scores, scores_ep}``).
+    Results are written as the reference's HDF5 result file
+    (``PruneResultWriter``: file attributes, ``threshold_scheme`` and
+    ``runs/<ref:03d>_<task:02d>/{scheme, param_sets, scores_ep, scores,
+    level_stats, timer_stats}``), runs in ``ref_segs`` order.
     """
     if driver not in ("auto", "threads"):
         msg = f"driver must be 'auto' or 'threads', got {driver!r}"
@@ -1620,13 +1629,11 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     outdir.mkdir(parents=True, exist_ok=True)
     filebase = f"{file_prefix}_pruning_nstages_{dyp.nsegments}"
     log_file = outdir / f"{filebase}_log.txt"
-    result_file = outdir / f"{filebase}_results.npz"
+    result_file = outdir / f"{filebase}_results.h5"
     if log_file.exists() or result_file.exists():
         msg = f"{log_file} or {result_file} already exists"
         raise FileExistsError(msg)
     log_file.write_text("Pruning log\n")
-    out = {"param_names": np.asarray(dyp.cfg.param_names), "nsegments": dyp.nsegments,
-           "max_sugg": max_sugg, "threshold_scheme": np.asarray(threshold_scheme)}
     kw = {"max_sugg": max_sugg, "batch_size": batch_size, "poly_basis": poly_basis,
           "use_moving_grid": use_moving_grid}
     probe = Pruning(dyp, threshold_scheme, **kw)
@@ -1638,22 +1645,18 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     else:
         results = run_many(dyp, threshold_scheme, ref_segs, n_workers=n_workers,
                            ascend_levels=ascend_levels, **kw)
-    for ref_seg in ref_segs:
-        res = results[ref_seg]
-        with log_file.open("a") as f:
-            f.write(f"Pruning log for ref segment: {ref_seg}\n")
-            for st in res["level_stats"]:
-                f.write(st.get_summary())
-        g = f"runs/{res['run_name']}"
-        out[f"{g}/scheme"] = res["scheme"]
-        out[f"{g}/param_sets"] = res["param_sets"]
-        out[f"{g}/scores"] = res["scores"]
-        out[f"{g}/scores_ep"] = res["scores_ep"]
-        out[f"{g}/level_stats"] = np.array(
-            [(s.level, s.seg_idx, s.threshold, s.score_min, s.score_max, s.n_branches,
-              s.n_leaves, s.n_leaves_phy, s.n_leaves_surv) for s in res["level_stats"]],
-            dtype=np.float64)
-    np.savez_compressed(result_file, **out)
+    from pyloki_gb300.results import PruneResultWriter
+
+    with PruneResultWriter(result_file) as writer:
+        writer.write_metadata(dyp.cfg.param_names, dyp.nsegments, max_sugg, threshold_scheme)
+        for ref_seg in ref_segs:
+            res = results[ref_seg]
+            with log_file.open("a") as f:
+                f.write(f"Pruning log for ref segment: {ref_seg}\n")
+                for st in res["level_stats"]:
+                    f.write(st.get_summary())
+            writer.write_run_results(res["run_name"], res["scheme"], res["param_sets"],
+                                     res["scores"], res["scores_ep"], res["level_stats"])
     return result_file.as_posix()
 
 

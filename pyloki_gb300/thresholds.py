@@ -567,19 +567,52 @@ class DynamicThresholdScheme:
         return backtrack_best(self.states, self.thresholds, self.probs, min_probs)
 
     def save(self, outdir: str = ".") -> str:
-        """The design as ``.npz`` with the reference's attribute and dataset
-        names (``thresholding.py:965-1008``; h5py is not used)."""
+        """The design as the reference's HDF5 file (``thresholding.py:965-1008``):
+        attributes ntrials, snr_final, ref_ducy, ducy_max, wtsp, beam_width,
+        mode, and datasets branching_pattern, profile, thresholds, probs,
+        guess_path and states (``state_dtype`` records)."""
+        from pyloki_gb300 import h5
+
         fb = (f"dynscheme_nstages_{self.nstages:03d}_nthresh_{self.nthresholds:03d}_"
               f"nprobs_{self.nprobs:03d}_ntrials_{self.ntrials:04d}_snr_{self.snr_final:04.1f}_"
               f"ducy_{self.ref_ducy:04.2f}_beam_{self.beam_width:03.1f}")
-        path = Path(outdir) / f"{fb}.npz"
-        np.savez_compressed(path, ntrials=self.ntrials, snr_final=self.snr_final,
-                            ref_ducy=self.ref_ducy, ducy_max=self.ducy_max, wtsp=self.wtsp,
-                            beam_width=self.beam_width, mode=self.mode,
-                            branching_pattern=self.branching_pattern, profile=self.profile,
-                            thresholds=self.thresholds, probs=self.probs,
-                            guess_path=self.guess_path, states=self.states)
+        path = Path(outdir) / f"{fb}.h5"
+        with h5.File(path, "w") as f:
+            f.attrs.update({"ntrials": np.int64(self.ntrials),
+                            "snr_final": float(self.snr_final), "ref_ducy": float(self.ref_ducy),
+                            "ducy_max": float(self.ducy_max), "wtsp": float(self.wtsp),
+                            "beam_width": float(self.beam_width), "mode": str(self.mode)})
+            for name in ("branching_pattern", "profile", "thresholds", "probs", "guess_path",
+                         "states"):
+                f.create_dataset(name, data=np.asarray(getattr(self, name)))
         return path.as_posix()
+
+
+class DynamicThresholdSchemeAnalyser:
+    """A saved design read back (``detection/schemes.py:614-660``
+    ``DynamicThresholdSchemeAnalyser.from_file``): its states, thresholds,
+    probability bins, branching pattern, guess path and beam width, and the
+    best-path backtrack over them."""
+
+    def __init__(self, states, thresholds, probs, branching_pattern, guess_path,
+                 beam_width: float) -> None:
+        self.states = np.asarray(states)
+        self.thresholds = np.asarray(thresholds)
+        self.probs = np.asarray(probs)
+        self.branching_pattern = np.asarray(branching_pattern)
+        self.guess_path = np.asarray(guess_path)
+        self.beam_width = float(beam_width)
+
+    @classmethod
+    def from_file(cls, filename: str) -> DynamicThresholdSchemeAnalyser:
+        from pyloki_gb300 import h5
+
+        f = h5.read_file(filename)
+        return cls(f["states"].data, f["thresholds"].data, f["probs"].data,
+                   f["branching_pattern"].data, f["guess_path"].data, f.attrs["beam_width"])
+
+    def backtrack_best(self, min_probs: list[float] | None = None) -> list[np.ndarray]:
+        return backtrack_best(self.states, self.thresholds, self.probs, min_probs)
 
 
 def backtrack_best(states: np.ndarray, thresholds: np.ndarray, probs: np.ndarray,
@@ -625,7 +658,8 @@ def backtrack_best(states: np.ndarray, thresholds: np.ndarray, probs: np.ndarray
     return out
 
 
-__all__ = ["DynamicThresholdScheme", "FoldSim", "backtrack_best", "bound_scheme",
+__all__ = ["DynamicThresholdScheme", "DynamicThresholdSchemeAnalyser", "FoldSim",
+           "backtrack_best", "bound_scheme",
            "determine_scheme",
            "evaluate_scheme", "generate_folded_profile", "get_next_state",
            "neighbouring_indices", "state_dtype", "trials_scheme"]

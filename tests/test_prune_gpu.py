@@ -128,11 +128,21 @@ def test_prune_dyp_tree_writes_results(cuda_device, tmp_path):
     from pyloki_gb300.prune import prune_dyp_tree
 
     d, prn = _run("prune_taylor", cuda_device)
+    from pyloki_gb300.results import LEVEL_DTYPE, read_prune_results
+
     path = prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=2, max_sugg=int(d["max_sugg"]),
                           batch_size=int(d["batch_size"]), outdir=tmp_path, n_workers=1)
-    res = np.load(path)
-    runs = sorted({k.split("/")[1] for k in res.files if k.startswith("runs/")})
-    assert len(runs) == 2
+    assert path.endswith("_results.h5")
+    res = read_prune_results(path)
+    assert len(res["runs"]) == 2
+    assert list(res["attrs"]["param_names"]) == list(prn.dyp.cfg.param_names)
+    assert int(res["attrs"]["nsegments"]) == prn.dyp.nsegments
+    np.testing.assert_array_equal(res["threshold_scheme"], d["thresholds"])
+    for run in res["runs"].values():
+        assert run["level_stats"].dtype == LEVEL_DTYPE
+        assert len(run["level_stats"]) == prn.dyp.nsegments
+        assert run["scores"].dtype == np.float32
+        assert len(run["param_sets"]) == len(run["scores"])
     with pytest.raises(FileExistsError):
         prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=2, outdir=tmp_path, n_workers=1)
     with pytest.raises(ValueError):
@@ -146,18 +156,21 @@ def test_prune_dyp_tree_drivers_match_serial(cuda_device, tmp_path, name):
     another."""
     from pyloki_gb300.prune import prune_dyp_tree
 
+    from pyloki_gb300.results import read_prune_results
+
     d, prn = _run(name, cuda_device)
     kw = dict(max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]))
-    a = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "a",
-                               n_workers=1, driver="threads", **kw))
-    b = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "b",
-                               n_workers=3, driver="threads", **kw))
-    c = np.load(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4, outdir=tmp_path / "c",
-                               **kw))
-    assert sorted(a.files) == sorted(b.files) == sorted(c.files)
-    for k in a.files:
-        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
-        np.testing.assert_array_equal(a[k], c[k], err_msg=k)
+    a, b, c = (read_prune_results(prune_dyp_tree(prn.dyp, d["thresholds"], n_runs=4,
+                                                 outdir=tmp_path / sub, **kw, **extra))
+               for sub, extra in (("a", {"n_workers": 1, "driver": "threads"}),
+                                  ("b", {"n_workers": 3, "driver": "threads"}),
+                                  ("c", {})))
+    assert list(a["runs"]) == list(b["runs"]) == list(c["runs"])
+    assert len(a["runs"]) == 4
+    for run in a["runs"]:
+        for k in a["runs"][run]:
+            np.testing.assert_array_equal(a["runs"][run][k], b["runs"][run][k], err_msg=k)
+            np.testing.assert_array_equal(a["runs"][run][k], c["runs"][run][k], err_msg=k)
 
 
 def test_best_intermediate_matches_get_best_k(cuda_device):

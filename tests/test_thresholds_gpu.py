@@ -126,7 +126,16 @@ def test_dynamic_scheme_designs_a_path(cuda_device, mode, tmp_path):
             assert ds.probs[k] <= p or np.isclose(ds.probs[k], p)
     path = ds.best_path()
     assert 1 <= len(path) <= ds.nstages
-    assert ds.save(str(tmp_path)).endswith(".npz")
+    from pyloki_gb300.thresholds import DynamicThresholdSchemeAnalyser
+
+    saved = ds.save(str(tmp_path))
+    assert saved.endswith(".h5")
+    an = DynamicThresholdSchemeAnalyser.from_file(saved)
+    np.testing.assert_array_equal(an.states, ds.states)
+    np.testing.assert_array_equal(an.thresholds, ds.thresholds)
+    assert an.beam_width == ds.beam_width
+    for a, b in zip(an.backtrack_best([0.1]), ds.backtrack_best([0.1]), strict=True):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_dynamic_scheme_with_unit_first_branching(cuda_device):
