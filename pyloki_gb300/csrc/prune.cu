@@ -1967,29 +1967,17 @@ prune_ascend_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
 // (detection/scoring.py:285-292) of the complex Taylor kernels.
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kPruneWarps * 32)
-circ_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                          const float2* __restrict__ folds, int64_t batch,
-                          const LokiBranchInfo* __restrict__ info,
-                          const CircChild* __restrict__ map,
-                          const int64_t* __restrict__ valid_ids, int64_t n_valid,
-                          const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
-                          float* __restrict__ scores, int32_t* __restrict__ cidx,
-                          double* __restrict__ cphase, int8_t* __restrict__ ccls,
-                          int32_t* __restrict__ batch_taylor,
-                          unsigned* __restrict__ minmax_keys) {
-  extern __shared__ float smem[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Valid child v of the complex circular tree: resolve, rotate + add into
+// the lane's comb buffer, irfft into trow, score (tw: the block's twiddles).
+__device__ __forceinline__ void circ_score_one_complex(
+    const LokiPruneLevel& D, const double* __restrict__ leaves, const float2* __restrict__ folds,
+    int64_t batch, const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+    const int64_t* __restrict__ valid_ids, const float2* __restrict__ seg,
+    const LokiScoreSpec& sp, const float* tw, float2* comb, float* trow,
+    float* __restrict__ scores, int32_t* __restrict__ cidx, double* __restrict__ cphase,
+    int8_t* __restrict__ ccls, int32_t* __restrict__ batch_taylor,
+    unsigned* __restrict__ minmax_keys, int64_t v) {
   const int nb = D.nbins, nbf = nb / 2 + 1, P = 5;
-  const int stride = score_stride(nb, sp.wmax);
-  float* tw = smem;
-  load_twiddles(tw, nb);
-  __syncthreads();
-  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
-  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
-  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
-  const int64_t v = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
-  if (v >= n_valid) return;
   const CircChild ch = map[valid_ids[v]];
   const LokiBranchInfo B = info[ch.parent];
   const double* lf = leaves + (int64_t)ch.parent * (P + 2) * 2;
@@ -2005,7 +1993,6 @@ circ_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   const int64_t row = (int64_t)r.ia * D.n_freq + r.iff;
   rotate_add(seg + row * 2 * nbf, folds + (int64_t)ch.parent * 2 * nbf,
              prune_phasor(r.phase, nb), nbf, comb);
-  float* trow = tile + lane * stride;
   irfft_norm(comb, nb, nbf, tw, trow);
   float s;
   score_row(trow, nb, sp, &s);
@@ -2016,22 +2003,45 @@ circ_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   }
 }
 
-// Survivors of the complex circular tree: leaves, basis flag and backtracks as
-// circ_emit_kernel, the fold written as the complex sum.
 __global__ void __launch_bounds__(kPruneWarps * 32)
-circ_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
-                         const float2* __restrict__ folds, int64_t batch,
-                         const LokiBranchInfo* __restrict__ info,
-                         const CircChild* __restrict__ map,
-                         const int64_t* __restrict__ valid_ids, const float2* __restrict__ seg,
-                         const int64_t* __restrict__ surv, int64_t n_surv,
-                         const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
-                         const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
-                         const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
-                         float2* __restrict__ fout, float* __restrict__ sout,
-                         float* __restrict__ seout, int32_t* __restrict__ bout) {
-  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= n_surv) return;
+circ_score_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                          const float2* __restrict__ folds, int64_t batch,
+                          const LokiBranchInfo* __restrict__ info,
+                          const CircChild* __restrict__ map,
+                          const int64_t* __restrict__ valid_ids, int64_t n_valid,
+                          const float2* __restrict__ seg, LokiScoreSpec sp, ScoreK SK,
+                          float* __restrict__ scores, int32_t* __restrict__ cidx,
+                          double* __restrict__ cphase, int8_t* __restrict__ ccls,
+                          int32_t* __restrict__ batch_taylor,
+                          unsigned* __restrict__ minmax_keys) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* tile = wbase + (size_t)32 * 2 * nbf * 2;
+  const int64_t v = ((int64_t)blockIdx.x * kPruneWarps + warp) * 32 + lane;
+  if (v >= n_valid) return;
+  circ_score_one_complex(D, leaves, folds, batch, info, map, valid_ids, seg, sp, tw, comb,
+                         tile + lane * stride, scores, cidx, cphase, ccls, batch_taylor,
+                         minmax_keys, v);
+}
+
+// Survivor s of the complex circular tree (circ_emit_one's leaves, basis
+// flag and backtracks; the fold written as the complex sum).
+__device__ __forceinline__ void circ_emit_one_complex(
+    const LokiPruneLevel& D, const double* __restrict__ leaves, const float2* __restrict__ folds,
+    int64_t batch, const LokiBranchInfo* __restrict__ info, const CircChild* __restrict__ map,
+    const int64_t* __restrict__ valid_ids, const float2* __restrict__ seg,
+    const int64_t* __restrict__ surv, const float* __restrict__ cscores,
+    const int32_t* __restrict__ cidx, const double* __restrict__ cphase,
+    const int8_t* __restrict__ ccls, const int32_t* __restrict__ batch_taylor,
+    double* __restrict__ lout, float2* __restrict__ fout, float* __restrict__ sout,
+    float* __restrict__ seout, int32_t* __restrict__ bout, int64_t s) {
   const int nb = D.nbins, nbf = nb / 2 + 1, P = 5, m = 6;
   const int64_t v = surv[s];
   const CircChild ch = map[valid_ids[v]];
@@ -2084,6 +2094,26 @@ circ_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
   const int64_t row = (int64_t)ia * D.n_freq + iff;
   rotate_add(seg + row * 2 * nbf, folds + (int64_t)ch.parent * 2 * nbf,
              prune_phasor(cphase[v], nb), nbf, fout + s * 2 * nbf);
+}
+
+// Survivors of the complex circular tree: leaves, basis flag and backtracks as
+// circ_emit_kernel, the fold written as the complex sum.
+__global__ void __launch_bounds__(kPruneWarps * 32)
+circ_emit_complex_kernel(LokiPruneLevel D, const double* __restrict__ leaves,
+                         const float2* __restrict__ folds, int64_t batch,
+                         const LokiBranchInfo* __restrict__ info,
+                         const CircChild* __restrict__ map,
+                         const int64_t* __restrict__ valid_ids, const float2* __restrict__ seg,
+                         const int64_t* __restrict__ surv, int64_t n_surv,
+                         const float* __restrict__ cscores, const int32_t* __restrict__ cidx,
+                         const double* __restrict__ cphase, const int8_t* __restrict__ ccls,
+                         const int32_t* __restrict__ batch_taylor, double* __restrict__ lout,
+                         float2* __restrict__ fout, float* __restrict__ sout,
+                         float* __restrict__ seout, int32_t* __restrict__ bout) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n_surv) return;
+  circ_emit_one_complex(D, leaves, folds, batch, info, map, valid_ids, seg, surv, cscores, cidx,
+                        cphase, ccls, batch_taylor, lout, fout, sout, seout, bout, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -3666,6 +3696,65 @@ bj_circ_emit_kernel(BatchTabs T, int l, int64_t batch) {
                    out.backtracks, t * 32);
 }
 
+// the circular tree over complex folds: lane per valid child / survivor
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_circ_score_complex_kernel(BatchTabs T, int l, LokiScoreSpec sp, int64_t batch) {
+  extern __shared__ float smem[];
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const float2* seg =
+      reinterpret_cast<const float2*>(J.ffa_fold) + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = D.nbins, nbf = nb / 2 + 1;
+  const int stride = score_stride(nb, sp.wmax);
+  float* tw = smem;
+  load_twiddles(tw, nb);
+  __syncthreads();
+  float* wbase = smem + 2 * nb + (size_t)warp * cplx_warp_floats(nb, stride);
+  float2* comb = reinterpret_cast<float2*>(wbase) + (size_t)lane * 2 * nbf;
+  float* trow = wbase + (size_t)32 * 2 * nbf * 2 + lane * stride;
+  int64_t* cnt = R.counts;
+  const int64_t n_valid = job_pos(w)[cnt[1]];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    cnt[4] = n_valid;
+    R.stats[l - 1].n_valid = n_valid;
+  }
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n_valid;
+       v += (int64_t)gridDim.x * blockDim.x)
+    circ_score_one_complex(D, in.leaves, reinterpret_cast<const float2*>(in.folds), batch,
+                           reinterpret_cast<const LokiBranchInfo*>(w.info),
+                           reinterpret_cast<const CircChild*>(R.child_map), R.valid_ids, seg, sp,
+                           tw, comb, trow, w.child_scores, w.child_idx, w.child_phase,
+                           R.child_class, R.batch_taylor, reinterpret_cast<unsigned*>(w.minmax),
+                           v);
+}
+
+__global__ void __launch_bounds__(kPruneWarps * 32)
+bj_circ_emit_complex_kernel(BatchTabs T, int l, int64_t batch) {
+  const LokiPruneJob& J = T.jobs[blockIdx.y];
+  const size_t li = (size_t)blockIdx.y * T.nlevels + (l - 1);
+  const LokiPruneLevel& D = T.levels[li];
+  const LokiPruneRun& R = J.run;
+  const LokiPruneWork& w = R.work;
+  const LokiPruneTree& in = R.trees[(l - 1) & 1];
+  const LokiPruneTree& out = R.trees[l & 1];
+  const float2* seg =
+      reinterpret_cast<const float2*>(J.ffa_fold) + (int64_t)T.seg_idx[li] * J.seg_stride;
+  const int64_t n_surv = R.counts[2];
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_surv;
+       s += (int64_t)gridDim.x * blockDim.x)
+    circ_emit_one_complex(D, in.leaves, reinterpret_cast<const float2*>(in.folds), batch,
+                          reinterpret_cast<const LokiBranchInfo*>(w.info),
+                          reinterpret_cast<const CircChild*>(R.child_map), R.valid_ids, seg,
+                          w.surv, w.child_scores, w.child_idx, w.child_phase, R.child_class,
+                          R.batch_taylor, out.leaves, reinterpret_cast<float2*>(out.folds),
+                          out.scores, out.scores_ep, out.backtracks, s);
+}
+
 __global__ void bj_bt_kernel(BatchTabs T, int l, int row) {
   const LokiPruneJob& J = T.jobs[blockIdx.y];
   const LokiPruneRun& R = J.run;
@@ -3729,9 +3818,8 @@ static int batch_tables(const LokiPruneJob* jobs, int32_t njobs, const LokiPrune
       return set_error(LOKI_ERR_INVALID, "levels of different trees");
   }
   const bool circ = levels[0].basis == 2;
-  if (circ && (fourier || P != 5))
-    return set_error(LOKI_ERR_UNSUPPORTED,
-                     "the circular-orbit tree runs on real folds with poly_order 5");
+  if (circ && P != 5)
+    return set_error(LOKI_ERR_UNSUPPORTED, "the circular-orbit tree has poly_order 5");
   for (int j = 0; j < njobs; ++j) {
     const LokiPruneJob& J = jobs[j];
     const LokiPruneRun& R = J.run;
@@ -3800,10 +3888,11 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
            : score_smem_bytes(nb, sp.wmax, kPruneWarps);
   if (smem > 200 * 1024)
     return set_error(LOKI_ERR_UNSUPPORTED, "nbins + wmax too large for pruning");
-  if (smem > 48 * 1024 && (cplx ? set_smem_limit(bj_score_complex_kernel, smem)
-                                : shape.circ ? set_smem_limit(bj_circ_score_kernel, smem)
-                                             : set_smem_limit(bj_score_kernel, smem)) !=
-                              cudaSuccess)
+  if (smem > 48 * 1024 &&
+      (cplx ? (shape.circ ? set_smem_limit(bj_circ_score_complex_kernel, smem)
+                          : set_smem_limit(bj_score_complex_kernel, smem))
+            : shape.circ ? set_smem_limit(bj_circ_score_kernel, smem)
+                         : set_smem_limit(bj_score_kernel, smem)) != cudaSuccess)
     return set_error(LOKI_ERR_CUDA, "cudaFuncSetAttribute failed");
   int dev = 0, nsm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -3866,15 +3955,23 @@ static int batch_enqueue(void* dev_scratch, int32_t njobs, int32_t nlevels,
       bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, 3);
       bj_circ_clear_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, batch_size);
       if (ev_score) cudaEventRecord(ev_score[2 * (l - 1)], s);
-      bj_circ_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK,
-                                                                               batch_size);
+      if (cplx)
+        bj_circ_score_complex_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(
+            T, l, sp, batch_size);
+      else
+        bj_circ_score_kernel<<<dim3(g_score, njobs), kPruneWarps * 32, smem, s>>>(T, l, sp, SK,
+                                                                                 batch_size);
       if (ev_score) cudaEventRecord(ev_score[2 * (l - 1) + 1], s);
       bj_circ_boff_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T);
       scan(4, g_scan_c);
       bj_scatter_kernel<<<dim3(g_flat, njobs), 256, 0, s>>>(T, l, 4);
       bj_overflow_kernel<<<(unsigned)njobs, kSelThreads, 0, s>>>(T, l, max_sugg, batch_size,
                                                                  1);
-      bj_circ_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l, batch_size);
+      if (cplx)
+        bj_circ_emit_complex_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(
+            T, l, batch_size);
+      else
+        bj_circ_emit_kernel<<<dim3(g_emit, njobs), kPruneWarps * 32, 0, s>>>(T, l, batch_size);
     } else {
       for (int i = 0; i < 11; ++i) note_launch();
       bj_branch_kernel<<<dim3(g_par, njobs), 256, 0, s>>>(T, l);
@@ -3956,7 +4053,7 @@ extern "C" int loki_prune_batch_score_times(void* dev_scratch, int32_t njobs, in
   shape.circ = shape_in[5] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
       shape.max_par < 1 || shape.max_child < 1 ||
-      (shape.circ && (shape.fourier || shape.poly_order != 5)))
+      (shape.circ && shape.poly_order != 5))
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
   int rc = prune_spec_check(spec, shape.nbins);
   if (rc) return rc;
@@ -3995,7 +4092,7 @@ extern "C" int loki_prune_batch_enqueue(void* dev_scratch, int32_t njobs, int32_
   shape.circ = shape_in[5] != 0;
   if (shape.nbins < 1 || shape.poly_order < 1 || shape.poly_order > LOKI_MAX_PARAMS ||
       shape.max_par < 1 || shape.max_child < 1 ||
-      (shape.circ && (shape.fourier || shape.poly_order != 5)))
+      (shape.circ && shape.poly_order != 5))
     return set_error(LOKI_ERR_INVALID, "bad batch shape");
   int rc = prune_spec_check(spec, shape.nbins);
   if (rc) return rc;
@@ -4095,9 +4192,6 @@ extern "C" int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs,
         !J.dt_seg || !J.seg_idx || !J.ffa_fold || J.seg_stride < 1 || !J.dev_err)
       return set_error(LOKI_ERR_INVALID, "ascend job %d: null pointer or bad stride", j);
   }
-  if (jobs[0].lvl.basis == 2 && fourier)
-    return set_error(LOKI_ERR_UNSUPPORTED,
-                     "the circular-orbit ascend over complex folds runs per job");
   int rc = prune_spec_check(spec, nb);
   if (rc) return rc;
   LokiScoreSpec sp = *spec;

@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import itertools
 import math
 from pathlib import Path
 
@@ -994,11 +995,10 @@ class Pruning:
 
     @property
     def block_batch_supported(self) -> bool:
-        """``PruneBlockBatch`` covers this configuration: every tree without
-        a parent hook and one best leaf per level, except the circular-orbit
-        tree over complex folds."""
-        return (self.intermediate_k == 1 and self.parent_hook is None
-                and not (self.fourier and self.circular))
+        """``PruneBlockBatch`` covers this configuration: every tree, real or
+        complex folds, without a parent hook and with one best leaf per
+        level."""
+        return self.intermediate_k == 1 and self.parent_hook is None
 
     def run_device(self, ref_seg: int, *, graph: bool = False, levels: int | None = None) -> None:
         """Every level of one reference segment with the counts kept on the
@@ -1469,13 +1469,12 @@ class _DeviceRun:
         pinned copies (after the stream has been waited on)."""
         stats = self._h_stats.numpy().view(_lib.PRUNE_STATS_DTYPE)
         err = int(self._h_err[0])
-        last, n_final = 0, self.seed.size
-        for lvl in range(1, self.nlev + 1):
-            last = lvl
-            n_final = int(stats[lvl - 1]["n_surv"])
-            if n_final == 0:
-                break
-        return stats, err, last, n_final
+        if self.nlev == 0:
+            return stats, err, 0, self.seed.size
+        n_surv = stats["n_surv"][: self.nlev]
+        dead = np.flatnonzero(n_surv == 0)  # the run stops at its first empty level
+        last = int(dead[0]) + 1 if dead.size else self.nlev
+        return stats, err, last, int(n_surv[last - 1])
 
     def copy_tree_async(self, n: int) -> None:
         """Enqueue the copies of the final tree's first n rows (leaves, scores,
@@ -1497,16 +1496,16 @@ class _DeviceRun:
                           score_max=float(s0.max()) if seed.size else 0.0,
                           n_branches=seed.size, n_leaves=seed.size, n_leaves_phy=seed.size,
                           n_leaves_surv=seed.size)]
-        seg, thr = self.seg_idx[:last].tolist(), self.thresholds[:last].tolist()
         f = stats[:last]
-        for lvl, (npar, nch, nval, nsurv, smin, smax) in enumerate(
-                zip(f["n_parents"].tolist(), f["n_children"].tolist(), f["n_valid"].tolist(),
-                    f["n_surv"].tolist(), f["score_min"].tolist(), f["score_max"].tolist()),
-                start=1):
-            out.append(PruneStats(
-                level=lvl, seg_idx=seg[lvl - 1], threshold=thr[lvl - 1],
-                score_min=smin if nch else 0.0, score_max=smax if nch else 0.0,
-                n_branches=npar, n_leaves=nch, n_leaves_phy=nval, n_leaves_surv=nsurv))
+        nch = f["n_children"]
+        # positional fields (level, seg_idx, threshold, score_min, score_max,
+        # n_branches, n_leaves, n_leaves_phy, n_leaves_surv); a level without
+        # children has no score range
+        out.extend(itertools.starmap(PruneStats, zip(
+            range(1, last + 1), self.seg_idx[:last].tolist(), self.thresholds[:last].tolist(),
+            np.where(nch != 0, f["score_min"], 0.0).tolist(),
+            np.where(nch != 0, f["score_max"], 0.0).tolist(), f["n_parents"].tolist(),
+            nch.tolist(), f["n_valid"].tolist(), f["n_surv"].tolist())))
         return out
 
     def finish(self, prn: Pruning) -> bool:
@@ -1637,8 +1636,7 @@ def prune_dyp_tree(dyp, threshold_scheme, n_runs: int | None = None,
     kw = {"max_sugg": max_sugg, "batch_size": batch_size, "poly_basis": poly_basis,
           "use_moving_grid": use_moving_grid}
     probe = Pruning(dyp, threshold_scheme, **kw)
-    batched = driver == "auto" and ascend_levels is None and probe.block_batch_supported and (
-        probe.device_run_supported or not probe.circular)
+    batched = driver == "auto" and ascend_levels is None and probe.block_batch_supported
     if batched:
         res_list = PruneBlockBatch(threshold_scheme, **kw).run([(dyp, r) for r in ref_segs])
         results = dict(zip(ref_segs, res_list, strict=True))
@@ -1771,9 +1769,9 @@ class PruneBlockBatch(PruneBatch):
     and run buffers (kept across calls, rebound to each job's fold). The
     ascend, the read-back and the results are those of ``PruneBatch``; a job
     that outgrows its workspace is repeated with grown buffers through
-    ``loki_prune_run``. Taylor, Chebyshev and (with the level-synchronous
-    driver, real folds) circular-orbit trees; the block-per-run driver passes
-    circular-orbit trees to ``PruneBatch``.
+    the same driver. Taylor, Chebyshev and circular-orbit trees over real
+    folds, and (with the level-synchronous driver) over complex folds; the
+    block-per-run driver passes circular-orbit trees to ``PruneBatch``.
     """
 
     def __init__(self, threshold_scheme, *, max_jobs: int = 152, driver: str = "batch",
@@ -1841,15 +1839,15 @@ class PruneBlockBatch(PruneBatch):
             return []
         first = self._slot(0, jobs[0][0])
         if not first.block_batch_supported:
-            msg = ("the batched drivers cover trees without a parent hook, one best leaf per "
-                   "level, and no circular-orbit tree over complex folds")
+            msg = ("the batched drivers cover trees without a parent hook and with one best "
+                   "leaf per level")
             raise ValueError(msg)
-        if first.circular and self.driver == "blocks":
-            return PruneBatch.run(self, jobs, ascend=ascend)
         fourier = first.fourier
         if fourier and self.driver == "blocks":
             msg = "complex (Fourier-domain) trees run with driver='batch'"
             raise ValueError(msg)
+        if first.circular and self.driver == "blocks":
+            return PruneBatch.run(self, jobs, ascend=ascend)
         dev = jobs[0][0].device
         st = torch.cuda.current_stream(dev)
         out: list[dict] = [{} for _ in jobs]
@@ -1861,79 +1859,33 @@ class PruneBlockBatch(PruneBatch):
                 prn = self._slot(k, dyp)
                 prn._stream_ptr = None  # the current stream
                 runs.append((prn, prn._device_run_obj(ref, dyp.nsegments - 1, ascend)))
-            nlev = runs[0][1].nlev
-            n = len(runs)
-            if not fourier and all(prn.dyp.fold.dtype == torch.float32 for prn, _ in runs):
-                sjobs = (_lib.LokiSeedJob * n)()  # every job's seed in one launch
-                for i, (prn, dr) in enumerate(runs):
-                    sjobs[i] = dr.seed_job()
-                p0 = runs[0][0]
-                sbuf = self._dev_buf("seed", n * C.sizeof(_lib.LokiSeedJob), dev)
-                _lib.check(lib.loki_prune_seed_batch(
-                    sjobs, n, p0.dyp.cfg.nbins, p0.poly_order, p0.spec, _lib.ptr(sbuf),
-                    sbuf.numel(), _lib.stream_ptr(st)))
-            else:  # complex folds, or a fold stored in another type: per-job seeds
-                for prn, dr in runs:
-                    dr.prepare_block()
-            if nlev > 0:
-                tab = (_lib.LokiPruneJob * n)()
-                lv = (_lib.LokiPruneLevel * (n * nlev))()
-                seg = np.empty((n, nlev), np.int32)
-                thr = np.empty((n, nlev), np.float64)
-                size = C.sizeof(_lib.LokiPruneLevel)
-                for i, (prn, dr) in enumerate(runs):
-                    tab[i] = dr.job()
-                    C.memmove(C.byref(lv, i * nlev * size), dr.descs, nlev * size)
-                    seg[i] = dr.seg_idx
-                    thr[i] = dr.thresholds
-                need = int(lib.loki_prune_run_blocks_scratch_bytes(n, nlev))
-                if self._scratch is None or self._scratch.numel() < need:
-                    self._scratch = torch.empty(need, dtype=torch.uint8, device=dev)
-                    self._graphs = {}  # captured over the old scratch
-                p0 = runs[0][0]
-                args = (p0.spec, p0.max_sugg, p0.batch_size)
-                if self.driver == "blocks":
-                    _lib.check(lib.loki_prune_run_blocks(
-                        tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
-                        _lib.ptr(self._scratch), self._scratch.numel(), _lib.stream_ptr(st)))
-                else:
-                    shape = np.zeros(6, np.int64)
-                    _lib.check(lib.loki_prune_batch_tables(
-                        tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
-                        int(fourier), _lib.ptr(self._scratch), self._scratch.numel(),
-                        shape.ctypes.data, _lib.stream_ptr(st)))
-                    self._enqueue_batch(lib, dev, st, n, nlev, args, shape)
-            if ascend and nlev > 0:  # every job's ascend in one launch
-                ajobs = (_lib.LokiAscendJob * n)()
-                for i, (prn, dr) in enumerate(runs):
-                    ajobs[i] = dr.ascend_job()
-                p0 = runs[0][0]
-                abuf = self._dev_buf("ascend", n * C.sizeof(_lib.LokiAscendJob), dev)
-                _lib.check(lib.loki_prune_ascend_batch(
-                    ajobs, n, runs[0][1].asc[4], p0.spec, p0.max_sugg, int(fourier),
-                    _lib.ptr(abuf), abuf.numel(), _lib.stream_ptr(st)))
-            elif ascend:
-                for prn, dr in runs:
-                    dr._ascend_enqueue()
-            # every job's level records, error word and seed scores: one
-            # gather launch and one copy
-            isz = _lib.PRUNE_STATS_DTYPE.itemsize
-            raw = self._gather_read(
-                lib, dev, st, [[(dr.bufs.mem["stats"], dr.nlev * isz), (prn._err, 4),
-                                (dr.bufs.mem["seed_scores"], dr.seed.size * 4)]
-                               for prn, dr in runs], "stats")
-            for (prn, dr), (b_st, b_err, b_seed) in zip(runs, raw, strict=True):
-                dr._h_stats = torch.from_numpy(np.frombuffer(b_st, np.uint8).copy())
-                dr._h_err = torch.from_numpy(np.frombuffer(b_err, np.int32).copy())
-                dr._h_seed = torch.from_numpy(np.frombuffer(b_seed, np.float32).copy())
+            self._run_jobs(lib, dev, st, runs, ascend, fourier)
+            # a job that outgrew its workspace is repeated, through the same
+            # driver, with grown buffers (the others keep their results)
+            todo = list(range(len(runs)))
+            while todo:
+                grown = []
+                for i in todo:
+                    prn, dr = runs[i]
+                    err = int(dr._h_err[0])
+                    if err & _lib.LOKI_DEVERR_CAPACITY:
+                        stats = dr._h_stats.numpy().view(_lib.PRUNE_STATS_DTYPE)
+                        dr.need_child = int(stats["n_children"].max() * 1.25) + 1
+                        dr.need_bt = int(stats["n_surv"].sum() * 1.25) + 1
+                        prn._err.zero_()
+                        new = _DeviceRun(prn, dr.ref_seg, dr.nlev, grow=dr, ascend=dr.ascend)
+                        prn.__dict__.setdefault("_device_runs", {})[
+                            (dr.ref_seg, dr.nlev, dr.ascend)] = new
+                        runs[i] = (prn, new)
+                        grown.append(i)
+                    elif err:
+                        _lib.check_dev_err(prn._err)
+                if grown:
+                    self._run_jobs(lib, dev, st, [runs[i] for i in grown], ascend, fourier)
+                todo = grown
             ready = []
             for prn, dr in runs:
-                stats, err, last, nf = dr.stats_host()
-                if err:  # a workspace to grow, or a device error to raise
-                    dr = prn._device_finish(dr, False)
-                    dr.copy_stats_async()
-                    st.synchronize()
-                    stats, err, last, nf = dr.stats_host()
+                stats, _, last, nf = dr.stats_host()
                 ready.append((prn, dr, stats, last, nf))
             host = self._read_trees(lib, dev, st, ready)
             P = ready[0][0].poly_order
@@ -1948,6 +1900,91 @@ class PruneBlockBatch(PruneBatch):
                     "scores_ep": np.frombuffer(ep_b, np.float32).copy(),
                     "level_stats": dr.level_stats(stats, last)}
         return out
+
+    def _run_jobs(self, lib, dev, st, runs, ascend: bool, fourier: bool) -> None:
+        """Seeds, levels and ascends of ``runs`` (one slot each), then every
+        job's level records, error word and seed scores on the host (one
+        gather and one copy)."""
+        nlev = runs[0][1].nlev
+        n = len(runs)
+        if not fourier and all(prn.dyp.fold.dtype == torch.float32 for prn, _ in runs):
+            sjobs = (_lib.LokiSeedJob * n)()  # every job's seed in one launch
+            for i, (prn, dr) in enumerate(runs):
+                sjobs[i] = dr.seed_job()
+            p0 = runs[0][0]
+            sbuf = self._dev_buf("seed", n * C.sizeof(_lib.LokiSeedJob), dev)
+            _lib.check(lib.loki_prune_seed_batch(
+                sjobs, n, p0.dyp.cfg.nbins, p0.poly_order, p0.spec, _lib.ptr(sbuf),
+                sbuf.numel(), _lib.stream_ptr(st)))
+        else:  # complex folds, or a fold stored in another type: per-job seeds
+            for prn, dr in runs:
+                dr.prepare_block()
+        if nlev > 0:
+            tab = (_lib.LokiPruneJob * n)()
+            for i, (prn, dr) in enumerate(runs):
+                tab[i] = dr.job()
+            lv, seg, thr = self._level_tables(runs, nlev)
+            need = int(lib.loki_prune_run_blocks_scratch_bytes(n, nlev))
+            if self._scratch is None or self._scratch.numel() < need:
+                self._scratch = torch.empty(need, dtype=torch.uint8, device=dev)
+                self._graphs = {}  # captured over the old scratch
+            p0 = runs[0][0]
+            args = (p0.spec, p0.max_sugg, p0.batch_size)
+            if self.driver == "blocks":
+                _lib.check(lib.loki_prune_run_blocks(
+                    tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
+                    _lib.ptr(self._scratch), self._scratch.numel(), _lib.stream_ptr(st)))
+            else:
+                shape = np.zeros(6, np.int64)
+                _lib.check(lib.loki_prune_batch_tables(
+                    tab, n, lv, seg.ctypes.data, thr.ctypes.data, nlev, *args,
+                    int(fourier), _lib.ptr(self._scratch), self._scratch.numel(),
+                    shape.ctypes.data, _lib.stream_ptr(st)))
+                self._enqueue_batch(lib, dev, st, n, nlev, args, shape)
+        if ascend and nlev > 0:  # every job's ascend in one launch
+            ajobs = (_lib.LokiAscendJob * n)()
+            for i, (prn, dr) in enumerate(runs):
+                ajobs[i] = dr.ascend_job()
+            p0 = runs[0][0]
+            abuf = self._dev_buf("ascend", n * C.sizeof(_lib.LokiAscendJob), dev)
+            _lib.check(lib.loki_prune_ascend_batch(
+                ajobs, n, runs[0][1].asc[4], p0.spec, p0.max_sugg, int(fourier),
+                _lib.ptr(abuf), abuf.numel(), _lib.stream_ptr(st)))
+        isz = _lib.PRUNE_STATS_DTYPE.itemsize
+        raw = self._gather_read(
+            lib, dev, st, [[(dr.bufs.mem["stats"], dr.nlev * isz), (prn._err, 4),
+                            (dr.bufs.mem["seed_scores"], dr.seed.size * 4)]
+                           for prn, dr in runs], "stats")
+        for (prn, dr), (b_st, b_err, b_seed) in zip(runs, raw, strict=True):
+            dr._h_stats = torch.from_numpy(np.frombuffer(b_st, np.uint8).copy())
+            dr._h_err = torch.from_numpy(np.frombuffer(b_err, np.int32).copy())
+            dr._h_seed = torch.from_numpy(np.frombuffer(b_seed, np.float32).copy())
+
+    def _level_tables(self, runs, nlev: int):
+        """Level descriptors (in pinned memory, so that their copy to the
+        device is one DMA), segment order and thresholds of ``runs``, job
+        after job. They depend only on each run's configuration, reference
+        segment and levels, so a call over the same runs (new folds or not)
+        reuses them."""
+        key = tuple((id(prn), dr.ref_seg, dr.nlev, id(dr)) for prn, dr in runs)
+        cached = self.__dict__.get("_lv_cache")
+        if cached is not None and cached[0] == key:
+            return cached[1:4]
+        n = len(runs)
+        size = C.sizeof(_lib.LokiPruneLevel)
+        nbytes = n * nlev * size
+        pin = self.__dict__.get("_lv_pin")
+        if pin is None or pin.numel() < nbytes:
+            pin = self._lv_pin = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        lv = (_lib.LokiPruneLevel * (n * nlev)).from_address(pin.data_ptr())
+        seg = np.empty((n, nlev), np.int32)
+        thr = np.empty((n, nlev), np.float64)
+        for i, (_, dr) in enumerate(runs):
+            C.memmove(C.byref(lv, i * nlev * size), dr.descs, nlev * size)
+            seg[i] = dr.seg_idx
+            thr[i] = dr.thresholds
+        self._lv_cache = (key, lv, seg, thr, pin)
+        return lv, seg, thr
 
     def _dev_buf(self, name: str, nbytes: int, dev):
         bufs = self.__dict__.setdefault("_dev_bufs", {})

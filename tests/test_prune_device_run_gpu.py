@@ -265,12 +265,14 @@ def test_block_batch_passes_circular_to_streams(cuda_device):
         np.testing.assert_array_equal(g["param_sets"], w["param_sets"])
 
 
-@pytest.mark.parametrize("name", ["prune_taylor_fourier", "prune_cheby_fourier"])
+@pytest.mark.parametrize("name", ["prune_taylor_fourier", "prune_cheby_fourier",
+                                  "prune_circ_fourier"])
 def test_block_batch_fourier_matches_level_path(cuda_device, name):
     """Complex (Fourier-domain) trees in the level-synchronous batch: every
     job's level records, final scores, ascend and report equal the
-    level-by-level complex run's, uncaptured, captured and replayed; the
-    block-per-run driver declines them."""
+    level-by-level complex run's, uncaptured, captured and replayed, and
+    with a workspace too small for some levels (repeated through the batch
+    with grown buffers); the block-per-run driver declines them."""
     from pyloki_gb300.config import PulsarSearchConfig
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.prune import PruneBlockBatch, Pruning
@@ -303,5 +305,14 @@ def test_block_batch_fourier_matches_level_path(cuda_device, name):
             np.testing.assert_array_equal(g["scores"], want[1])
             np.testing.assert_array_equal(g["scores_ep"], want[2])
             np.testing.assert_array_equal(g["param_sets"], want[3])
+    small = PruneBlockBatch(d["thresholds"], max_jobs=4, **kw)
+    for k in range(2):
+        small._slot(k, dyp).device_child_cap = 64
+    got = small.run([(dyp, r) for r in refs[:2]])
+    for ref, g in zip(refs[:2], got, strict=True):
+        want = _level_path_results(lambda: Pruning(dyp, d["thresholds"], **kw), dyp, ref, d)
+        assert max(s.n_leaves for s in g["level_stats"]) > 64
+        np.testing.assert_array_equal(g["scores"], want[1])
+        np.testing.assert_array_equal(g["param_sets"], want[3])
     with pytest.raises(ValueError, match="driver='batch'"):
         PruneBlockBatch(d["thresholds"], driver="blocks", **kw).run([(dyp, refs[0])])
