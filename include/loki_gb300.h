@@ -666,11 +666,11 @@ int64_t loki_prune_run_blocks_scratch_bytes(int32_t njobs, int32_t nlevels);
  * a batch costs the launches of a single run and each step spreads over the
  * whole GPU; no host wait, so the enqueue can be captured in a CUDA graph.
  * dev_scratch of loki_prune_run_blocks_scratch_bytes bytes; njobs <= 65535.
- * Taylor and Chebyshev trees, and the circular-orbit tree on real folds
- * (basis 2, poly_order 5, the jobs' runs with their circular fields): its
- * level adds the crackle-expansion scan, the batch-ordered child map, the
- * validity compaction and the valid-child batch offsets of loki_prune_run's
- * circular level, each one launch over every job. */
+ * Taylor and Chebyshev trees, and the circular-orbit tree (basis 2,
+ * poly_order 5, the jobs' runs with their circular fields): its level adds
+ * the crackle-expansion scan, the batch-ordered child map, the validity
+ * compaction and the valid-child batch offsets of loki_prune_run's circular
+ * level, each one launch over every job. */
 int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPruneLevel* levels,
                          const int32_t* seg_idx, const double* thresholds, int32_t nlevels,
                          const LokiScoreSpec* spec, int64_t max_sugg, int64_t batch_size,
@@ -687,8 +687,8 @@ int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPrun
  * runs the new jobs. fourier != 0: complex (Fourier-domain) trees, the
  * jobs' tree folds (cap, 2, nbins / 2 + 1) complex64, fold rows and
  * seg_stride in complex elements (the complex level kernels' per-child code,
- * prune.py:165-332 with PruneTaylorComplexDPFuncts; Taylor and Chebyshev
- * trees). */
+ * prune.py:165-332 with PruneTaylorComplexDPFuncts, the Chebyshev
+ * counterpart and PruneCircTaylorComplexDPFuncts). */
 int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
                             const LokiPruneLevel* levels, const int32_t* seg_idx,
                             const double* thresholds, int32_t nlevels,
@@ -751,9 +751,9 @@ typedef struct {
 /* loki_prune_ascend_dev for njobs runs in one launch (grid y = job): the
  * jobs (host array) are checked and copied into dev_scratch of at least
  * njobs * sizeof(LokiAscendJob) bytes. Every job has nseg segments and at
- * most n_cap survivors. Taylor and Chebyshev trees; fourier != 0: complex
- * trees as loki_prune_ascend_complex (folds and seg_stride in complex
- * elements). */
+ * most n_cap survivors. Taylor, Chebyshev and circular-orbit trees;
+ * fourier != 0: complex trees as loki_prune_ascend_complex (folds and
+ * seg_stride in complex elements). */
 int loki_prune_ascend_batch(const LokiAscendJob* jobs, int32_t njobs, int32_t nseg,
                             const LokiScoreSpec* spec, int64_t n_cap, int32_t fourier,
                             void* dev_scratch, int64_t dev_scratch_bytes, void* stream);
