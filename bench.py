@@ -1359,14 +1359,15 @@ def profile_prune_batch_once(args) -> None:
     """One batched pruning step (``PruneBlockBatch``, the first call of a
     fresh runner, so its kernels are launched directly) over args.prune_runs
     reference segments, with no timing; the command the batched-pruning ncu
-    summaries are captured from."""
+    summaries are captured from. ``--prune-circ``: the circular-orbit tree
+    of order 5 on the same series."""
     import torch
 
     from pyloki_gb300.ffa import DynamicProgramming
     from pyloki_gb300.prune import PruneBlockBatch
 
     dev = torch.device("cuda", 0)
-    cfg = make_prune_cfg()
+    cfg = make_prune_cfg(circular=args.prune_circ)
     ts, _ = make_prune_series(seed=2000)
     dyp = DynamicProgramming(ts, cfg, device=dev)
     dyp.initialize()
@@ -1433,6 +1434,8 @@ def main() -> None:
                     help="run exactly one search (for ncu captures) and exit")
     ap.add_argument("--profile-prune-once", action="store_true",
                     help="run the pruning workload twice (warm-up + one run) and exit")
+    ap.add_argument("--prune-circ", action="store_true",
+                    help="with --profile-prune-batch-once: the circular-orbit tree of order 5")
     ap.add_argument("--profile-prune-batch-once", action="store_true",
                     help="one batched pruning step over --prune-runs segments, then exit")
     ap.add_argument("--detail-out", default=None,
