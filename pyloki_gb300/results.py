@@ -118,8 +118,7 @@ class PruneResultWriter:
         self.file.attrs["param_names"] = [str(p) for p in param_names]
         self.file.attrs["nsegments"] = np.int64(nsegments)
         self.file.attrs["max_sugg"] = np.int64(max_sugg)
-        if "threshold_scheme" in self.file:
-            del self.file.members["threshold_scheme"]
+        # a second call fails as h5py's create_dataset does: the name exists
         self.file.create_dataset("threshold_scheme", data=np.asarray(threshold_scheme))
 
     def write_run_results(self, run_name: str, scheme, leaves_report, scores, scores_ep,

@@ -188,6 +188,8 @@ def test_prune_result_writer_layout(tmp_path):
     thr = np.linspace(0, 4, 15)
     with PruneResultWriter(path) as w:
         w.write_metadata(["freq", "accel"], 16, 2**18, thr)
+    with PruneResultWriter(path, mode="a") as w, pytest.raises(ValueError, match="exists"):
+        w.write_metadata(["freq", "accel"], 16, 2**18, thr)  # the dataset exists already
     rng = np.random.default_rng(1)
     runs = {}
     for ref in (3, 8):
