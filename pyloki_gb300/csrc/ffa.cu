@@ -698,6 +698,14 @@ __device__ __forceinline__ float2 tile_ld(uint32_t base, uint32_t off, int j) {
   return r;
 }
 
+// The same bin as one 64-bit word: pack2(e, v) (e in the low half).
+__device__ __forceinline__ unsigned long long tile_ld64(uint32_t base, uint32_t off, int j) {
+  const uint32_t a = base | ((off + 8u * (uint32_t)j) & 511u);
+  unsigned long long r;
+  asm volatile("ld.shared.b64 %0, [%1];" : "=l"(r) : "r"(a));
+  return r;
+}
+
 // S/N of one final trial from its tail and head rows (lane-per-trial). The
 // prefix sum runs sequentially in float32 as circular_prefix_sum does and is
 // kept as register pairs P2[k] = (P[2k], P[2k + 1]); every even width's
@@ -719,9 +727,13 @@ __device__ __forceinline__ void tile_score_trial(uint32_t bt, uint32_t ot, uint3
     float nv[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      const float2 a = tile_ld(bt, ot, 2 * k + q), c = tile_ld(bh, oh, 2 * k + q);
-      const float e = __fadd_rn(a.x, c.x);
-      const float v = __fadd_rn(a.y, c.y);
+      // tail + head, e and v in one packed add (each half rounded as __fadd_rn)
+      unsigned long long ev;
+      asm("add.rn.f32x2 %0, %1, %2;"
+          : "=l"(ev)
+          : "l"(tile_ld64(bt, ot, 2 * k + q)), "l"(tile_ld64(bh, oh, 2 * k + q)));
+      float e, v;
+      unpack2(ev, e, v);
       nv[q] = FAST ? __fmul_rn(e, rsqrtf(v)) : __fdiv_rn(e, __fsqrt_rn(v));
     }
     const float s0 = k == 0 ? nv[0] : __fadd_rn(s, nv[0]);
