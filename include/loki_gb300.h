@@ -687,7 +687,7 @@ int loki_prune_run_batch(const LokiPruneJob* jobs, int32_t njobs, const LokiPrun
  * runs the new jobs. fourier != 0: complex (Fourier-domain) trees, the
  * jobs' tree folds (cap, 2, nbins / 2 + 1) complex64, fold rows and
  * seg_stride in complex elements (the complex level kernels' per-child code,
- * prune.py:165-332 with PruneTaylorComplexDPFuncts, the Chebyshev
+ * prune.py:165-332 with PrunePolyTaylorComplexDPFuncts, the Chebyshev
  * counterpart and PruneCircTaylorComplexDPFuncts). */
 int loki_prune_batch_tables(const LokiPruneJob* jobs, int32_t njobs,
                             const LokiPruneLevel* levels, const int32_t* seg_idx,
