@@ -1,5 +1,6 @@
 /*
- * CPU oracle for the Taylor enumerate-prune level (test infrastructure only:
+ * CPU oracle for the Taylor and Chebyshev enumerate-prune levels (test
+ * infrastructure only:
  * the parity checker in tests/ and the CPU baseline of bench.py; the product
  * never links or calls this file).
  *
@@ -15,6 +16,14 @@
  *             utils/transforms.py:93-138, backtrack prune.py:298-304
  *   add       utils/world_tree.py:482-551 add_batch / prune_on_overload,
  *             600-614 keep
+ * With basis = 1 the level is the PrunePolyChebyshevDPFuncts plugin
+ * (dynamic/dyn_poly_cheby.py:537-840): the parents are first shifted from
+ * the previous to the current Chebyshev domain (core/chebyshev.py:75-179
+ * with utils/transforms.py:661-710 shift_cheby_full), then branched with
+ * the Chebyshev steps (utils/psr_utils.py:259-278), resolved through
+ * cheby_to_taylor_param_shift (core/chebyshev.py:182-251,
+ * utils/transforms.py:713-738 and 554-579) and transformed to the next
+ * domain (core/chebyshev.py:340-356).
  * Batches of parents are processed in order exactly as the reference does;
  * inside a batch the children are independent and are resolved, folded and
  * scored in parallel (OpenMP), like the numba prange loops.
@@ -49,6 +58,16 @@ typedef struct {
   double dt_phase;        /* t0_add - t0_init */
   int64_t n_accel, n_freq;
   double accel_min, accel_max, freq_min, freq_max;
+  /* Chebyshev basis (basis = 1). Matrices in row-product form: row k of
+   * M is column k of the reference's matrix, so x @ A is mat_row(x, M, k). */
+  int basis;
+  double cm_prev[M6][M6]; /* shift_cheby_full coord_prev -> coord_cur (branch) */
+  double cm_add[M6][M6];  /* coord_cur domain re-centred at t0_add (fixed: t0_init domain) */
+  double cm_init[M6][M6]; /* coord_cur domain re-centred at t0_init (moving resolve) */
+  double cm_next[M6][M6]; /* shift_cheby_full coord_cur -> coord_next (transform) */
+  double r_mat[M6][M6];   /* compute_connection_matrix_r, row-product form */
+  double k_fact[M6];      /* k! */
+  double k_tspow[M6];     /* ts^k, ts the scale of the resolve domain */
 } OPruneLevel;
 
 static void set_threads(int nthreads) {
@@ -252,6 +271,73 @@ static void transform(const OPruneLevel* L, const double* in, double* out) {
   out[2 * m + 1] = in[2 * m + 1];
 }
 
+/* utils/transforms.py:661-710 shift_cheby_full of rows 0..P (values and
+ * errors; the tiling strategy propagates the errors). */
+static void cheby_shift(const OPruneLevel* L, const double M[M6][M6], const double* in,
+                        double* out) {
+  const int m = L->poly_order + 1;
+  double v[M6], e[M6];
+  for (int i = 0; i < m; ++i) {
+    v[i] = in[2 * i];
+    e[i] = in[2 * i + 1];
+  }
+  for (int k = 0; k < m; ++k) out[2 * k] = mat_row(v, M, k, m);
+  if (L->tiling == 0) {
+    for (int k = 0; k < m; ++k) out[2 * k + 1] = e[k] * fabs(M[k][k]);
+  } else if (L->tiling == 2) {
+    double A[M6][M6];
+    for (int i = 0; i < M6; ++i)
+      for (int j = 0; j < M6; ++j) A[i][j] = fabs(M[i][j]);
+    for (int k = 0; k < m; ++k) out[2 * k + 1] = mat_row(e, A, k, m);
+  } else {
+    double A[M6][M6], e2[M6];
+    for (int i = 0; i < M6; ++i)
+      for (int j = 0; j < M6; ++j) A[i][j] = M[i][j] * M[i][j];
+    for (int j = 0; j < m; ++j) e2[j] = e[j] * e[j];
+    for (int k = 0; k < m; ++k) out[2 * k + 1] = sqrt(mat_row(e2, A, k, m));
+  }
+}
+
+/* utils/transforms.py:713-738 cheby_to_taylor_param_shift: the Chebyshev
+ * values re-centred by M, then cheby_to_taylor (554-579): ascending power
+ * coefficients d[k] = (alpha_asc @ R)[k] * k! / ts^k. */
+static void cheby_taylor(const OPruneLevel* L, const double M[M6][M6], const double* alpha,
+                         double* d) {
+  const int m = L->poly_order + 1;
+  double a[M6], asc[M6];
+  for (int k = 0; k < m; ++k) a[k] = mat_row(alpha, M, k, m);
+  for (int k = 0; k < m; ++k) asc[k] = a[m - 1 - k];
+  for (int k = 0; k < m; ++k) d[k] = mat_row(asc, L->r_mat, k, m) * L->k_fact[k] / L->k_tspow[k];
+}
+
+/* core/chebyshev.py:182-282 (moving and fixed grid) */
+static void resolve_cheby(const OPruneLevel* L, Child* ch) {
+  const int m = L->poly_order + 1;
+  double alpha[M6], da[M6];
+  for (int i = 0; i < m; ++i) alpha[i] = ch->leaf[2 * i];
+  const double f0 = ch->leaf[2 * m];
+  cheby_taylor(L, L->cm_add, alpha, da);
+  double accel = da[2], vel = da[1], dd = da[0];
+  if (L->moving) {
+    double di[M6];
+    cheby_taylor(L, L->cm_init, alpha, di);
+    vel = da[1] - di[1];
+    dd = da[0] - di[0];
+  }
+  const double freq = f0 * (1 - vel / C_VAL);
+  const double delay = dd / C_VAL;
+  ch->phase = phase_idx(L->dt_phase, f0, L->nbins, delay);
+  ch->ia = (int32_t)nearest(accel, L->accel_min, L->accel_max, L->n_accel);
+  ch->iff = (int32_t)nearest(freq, L->freq_min, L->freq_max, L->n_freq);
+}
+
+/* core/chebyshev.py:340-356 (moving grid; the fixed grid keeps the leaf) */
+static void transform_cheby(const OPruneLevel* L, const double* in, double* out) {
+  const int P = L->poly_order;
+  memcpy(out, in, sizeof(double) * 2 * (P + 2));
+  if (L->moving) cheby_shift(L, L->cm_next, in, out);
+}
+
 /* np.partition order: ascending, NaN last. */
 static int cmp_float(const void* a, const void* b) {
   const float x = *(const float*)a, y = *(const float*)b;
@@ -338,16 +424,27 @@ int64_t oracle_prune_level(const OPruneLevel* L, const double* leaves, const flo
   double smin = INFINITY, smax = -INFINITY;
   if (batch_size > n_par) batch_size = n_par;
   if (batch_size < 1) batch_size = 1;
+  const int cheby = L->basis == 1;
   Branch* br = (Branch*)malloc(sizeof(Branch) * batch_size);
   int64_t* off = (int64_t*)malloc(sizeof(int64_t) * (batch_size + 1));
+  /* Chebyshev: the batch's parents shifted to the current domain */
+  double* shifted = cheby ? (double*)malloc(sizeof(double) * batch_size * 2 * (P + 2)) : NULL;
   for (int64_t b0 = 0; b0 < n_par; b0 += batch_size) {
     const int64_t b1 = b0 + batch_size < n_par ? b0 + batch_size : n_par;
     const int64_t nbat = b1 - b0;
     off[0] = 0;
     for (int64_t i = 0; i < nbat; ++i) {
-      if (branch_parent(L, leaves + (b0 + i) * 2 * (P + 2), &br[i])) {
+      const double* lf = leaves + (b0 + i) * 2 * (P + 2);
+      if (cheby) {
+        double* sh = shifted + i * 2 * (P + 2);
+        memcpy(sh, lf, sizeof(double) * 2 * (P + 2));
+        cheby_shift(L, L->cm_prev, lf, sh);
+        lf = sh;
+      }
+      if (branch_parent(L, lf, &br[i])) {
         free(br);
         free(off);
+        free(shifted);
         return -1;
       }
       off[i + 1] = off[i] + br[i].total;
@@ -361,12 +458,13 @@ int64_t oracle_prune_level(const OPruneLevel* L, const double* leaves, const flo
       float norm[512], prefix[1024];
 #pragma omp for schedule(static)
       for (int64_t i = 0; i < nbat; ++i) {
-        const double* lf = leaves + (b0 + i) * 2 * (P + 2);
+        const double* lf = cheby ? shifted + i * 2 * (P + 2) : leaves + (b0 + i) * 2 * (P + 2);
         for (int64_t k = 0; k < br[i].total; ++k) {
           Child* c = &ch[off[i] + k];
           make_child(L, lf, &br[i], k, c->leaf);
           c->parent = b0 + i;
-          resolve(L, c);
+          if (cheby) resolve_cheby(L, c);
+          else resolve(L, c);
           const int s = round_shift(c->phase, nb);
           const float* pf = folds + (b0 + i) * 2 * nb;
           const float* sf = seg + ((int64_t)c->ia * L->n_freq + c->iff) * 2 * nb;
@@ -406,7 +504,8 @@ int64_t oracle_prune_level(const OPruneLevel* L, const double* leaves, const flo
       int64_t w = 0;
       for (int64_t c = 0; c < nch; ++c) {
         if (!((double)ch[c].score >= thr)) continue;
-        transform(L, ch[c].leaf, tl + w * 2 * (P + 2));
+        if (cheby) transform_cheby(L, ch[c].leaf, tl + w * 2 * (P + 2));
+        else transform(L, ch[c].leaf, tl + w * 2 * (P + 2));
         int32_t* bt = tb + w * (P + 2);
         memset(bt, 0, sizeof(int32_t) * (P + 2));
         bt[0] = (int32_t)ch[c].parent;
@@ -431,6 +530,7 @@ int64_t oracle_prune_level(const OPruneLevel* L, const double* leaves, const flo
   }
   free(br);
   free(off);
+  free(shifted);
   stats[0] = n_leaves;
   stats[1] = n_leaves;
   smm[0] = isfinite(smin) ? smin : 0.0;
@@ -465,9 +565,18 @@ void oracle_prune_ascend(const OPruneLevel* L, const double* leaves, float* fold
       for (int j = 0; j < 2 * nb; ++j) acc[j] = 0.0f;
       for (int s = 0; s < nseg; ++s) {
         const double(*T)[M6] = (const double(*)[M6])(tm + s * M6 * M6);
-        const double accel = mat_row(pv, T, P - 2, m);
-        const double freq = f0 * (1 - mat_row(pv, T, P - 1, m) / C_VAL);
-        const double delay = mat_row(pv, T, P, m) / C_VAL;
+        double accel, freq, delay;
+        if (L->basis == 1) {  /* core/chebyshev.py:254-300: tm holds the re-centring */
+          double d[M6];
+          cheby_taylor(L, T, pv, d);
+          accel = d[2];
+          freq = f0 * (1 - d[1] / C_VAL);
+          delay = d[0] / C_VAL;
+        } else {
+          accel = mat_row(pv, T, P - 2, m);
+          freq = f0 * (1 - mat_row(pv, T, P - 1, m) / C_VAL);
+          delay = mat_row(pv, T, P, m) / C_VAL;
+        }
         const double ph = phase_idx(dt[s], f0, nb, delay);
         const int64_t ia = nearest(accel, L->accel_min, L->accel_max, L->n_accel);
         const int64_t iff = nearest(freq, L->freq_min, L->freq_max, L->n_freq);
@@ -484,4 +593,13 @@ void oracle_prune_ascend(const OPruneLevel* L, const double* leaves, float* fold
       scores[r] = score_fold(acc, nb, widths, nw, norm, prefix);
     }
   }
+}
+
+/* out[r] = x[r] @ A for n rows of m values, with M the row-product form of
+ * A (forward fused multiply-adds, the dgemm order of the reference's numpy
+ * matmul); used for the Chebyshev seed (utils/transforms.py:458-487). */
+void oracle_rowprod(const double* x, int64_t n, int m, const double* M, double* out) {
+  const double(*T)[M6] = (const double(*)[M6])M;
+  for (int64_t r = 0; r < n; ++r)
+    for (int k = 0; k < m; ++k) out[r * m + k] = mat_row(x + r * m, T, k, m);
 }

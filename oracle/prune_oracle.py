@@ -1,4 +1,4 @@
-"""CPU oracle of the Taylor enumerate-prune run (``prune_oracle.c``).
+"""CPU oracle of the Taylor and Chebyshev enumerate-prune runs (``prune_oracle.c``).
 
 Test infrastructure only: the checker for the GPU pruning path in tests/ and
 the CPU leg of bench.py's pruning measurement. It drives one run the way the
@@ -8,7 +8,10 @@ reference segment of the FFA fold (``core/taylor.py:14-65``), one
 final ascend (``dynamic/dyn_poly_taylor.py:587-628``). The per-level Taylor
 matrices and grid-step factors are restated here from the reference's numpy
 expressions (``utils/transforms.py:41-45``, ``utils/psr_utils.py:59-95,
-227-248``).
+227-248``). With ``basis="chebyshev"`` the seed is ``poly_chebyshev_seed``
+(``core/chebyshev.py:14-72``) and the per-level Chebyshev matrices are
+restated from ``utils/maths.py:400-570`` (connection coefficients S and R,
+the domain-change matrix C) in the reference's order of evaluation.
 """
 
 from __future__ import annotations
@@ -37,7 +40,80 @@ class OPruneLevel(C.Structure):
         ("n_accel", C.c_int64), ("n_freq", C.c_int64),
         ("accel_min", C.c_double), ("accel_max", C.c_double),
         ("freq_min", C.c_double), ("freq_max", C.c_double),
+        ("basis", C.c_int),
+        ("cm_prev", _M6), ("cm_add", _M6), ("cm_init", _M6), ("cm_next", _M6),
+        ("r_mat", _M6), ("k_fact", C.c_double * (MAXP + 1)),
+        ("k_tspow", C.c_double * (MAXP + 1)),
     ]
+
+
+# Chebyshev connection coefficients (utils/maths.py:37-52, 400-475) --------------
+def _nbinom(n: int, k: int) -> float:
+    from math import factorial
+
+    if k < 0 or k > n:
+        return 0.0
+    if k in (0, n):
+        return 1.0
+    k = min(k, n - k)
+    return float(factorial(n)) // (float(factorial(k)) * float(factorial(n - k)))
+
+
+def _conn_s(k: int, m: int) -> float:
+    """S_{k,m}: x^k in Chebyshev polynomials T_m."""
+    if k < 0 or m < 0 or m > k or (k - m) % 2:
+        return 0.0
+    half = (k - m) // 2
+    return 2.0 ** (1 - k - (1 if m == 0 else 0)) * _nbinom(k, half)
+
+
+def _conn_r(k: int, m: int) -> float:
+    """R_{k,m}: T_k in powers x^m."""
+    if k < 0 or m < 0 or m > k or (k - m) % 2:
+        return 0.0
+    if m == 0 and k % 2 == 0:
+        return float((-1) ** (k // 2))
+    half, mid = (k - m) // 2, (k + m) // 2
+    return ((-1) ** half) * (2.0 ** (m - 1)) * (2.0 * k / (k + m)) * _nbinom(mid, half)
+
+
+def _coef_c(n: int, k: int, p: float, q: float) -> float:
+    """C_{n,k}(p, q): T_n of the old domain in T_k of the new one."""
+    if k > n:
+        return 0.0
+    total = 0.0
+    for m in range(k, n + 1):
+        inner = 0.0
+        for i in range(k, m + 1):
+            inner += _nbinom(m, i) * p**i * q ** (m - i) * _conn_s(i, k)
+        total += _conn_r(n, m) * inner
+    return total
+
+
+def _cheby_matrix(order: int, tc1: float, ts1: float, tc2: float, ts2: float) -> np.ndarray:
+    """poly_chebyshev_transform_matrix(order, tc1, ts1, tc2, ts2, 1): the
+    domain change of descending coefficients [a_k .. a_0]."""
+    p = ts2 / ts1
+    q = (tc2 - tc1) / ts1
+    size = order + 1
+    c = np.zeros((size, size), np.float64)
+    for i in range(size):
+        for j in range(size):
+            c[i, j] = _coef_c(order - i, order - j, p, q)
+    return c
+
+
+def _conn_matrix(fn, order: int) -> np.ndarray:
+    m = np.zeros((order + 1, order + 1), np.float64)
+    for k in range(order + 1):
+        for j in range(k + 1):
+            m[k, j] = fn(k, j)
+    return m
+
+
+def _set_rowprod(dst, a: np.ndarray) -> None:
+    """x @ a in the oracle's row-product form (row k = column k of a)."""
+    _set(dst, np.ascontiguousarray(a.T))
 
 
 def _fact(k):
@@ -78,7 +154,19 @@ def _bind(lib):
                                        I64, P, P, P, P, P, P, I32]
     lib.oracle_prune_ascend.argtypes = [C.POINTER(OPruneLevel), P, P, P, P, I64, I32, P, P,
                                         P, P, I32, I32]
+    lib.oracle_rowprod.argtypes = [P, I64, I32, P, P]
     lib._prune_bound = True
+
+
+def _rowprod(lib, x: np.ndarray, a: np.ndarray) -> np.ndarray:
+    """x @ a over the last axis with forward fused multiply-adds."""
+    m = a.shape[0]
+    mat = np.zeros((MAXP + 1, MAXP + 1), np.float64)
+    mat[:m, :m] = a.T
+    xs = np.ascontiguousarray(x.reshape(-1, m), np.float64)
+    out = np.empty_like(xs)
+    lib.oracle_rowprod(_p(xs), xs.shape[0], m, _p(mat), _p(out))
+    return out.reshape(x.shape)
 
 
 class PruneRun:
@@ -86,7 +174,7 @@ class PruneRun:
 
     def __init__(self, cfg, fold: np.ndarray, param_arr, dparams, thresholds, *,
                  max_sugg: int = 2**17, batch_size: int = 1024, moving: bool = True,
-                 nthreads: int = 0) -> None:
+                 nthreads: int = 0, basis: str = "taylor") -> None:
         from pyloki_gb300.scheme import MiddleOutScheme
 
         self.cfg = cfg
@@ -103,6 +191,10 @@ class PruneRun:
         self.nseg = self.fold.shape[0]
         self.counts = np.array([len(p) for p in param_arr], np.int64)
         self._scheme_cls = MiddleOutScheme
+        if basis not in ("taylor", "chebyshev"):
+            msg = f"basis must be 'taylor' or 'chebyshev', got {basis!r}"
+            raise ValueError(msg)
+        self.cheby = basis == "chebyshev"
         self.lib = load()
         _bind(self.lib)
 
@@ -119,11 +211,27 @@ class PruneRun:
         d.branch_max = cfg.branch_max
         d.eta = cfg.eta
         tobs = c_cur[1]
-        sf, fa = _step_f(P, tobs, cfg.nbins, cfg.eta), _shift_factors(P, tobs, cfg.nbins)
+        if self.cheby:
+            # poly_cheb_step_vec / poly_cheb_shift_vec (utils/psr_utils.py:259-278)
+            # in the Taylor branch's expressions: (dphi * c) / f0 and
+            # |dcur - dnew| * (nbins * (f0 / c))
+            sf = np.full(P, cfg.eta / cfg.nbins)
+            fa = np.full(P, float(cfg.nbins))
+        else:
+            sf, fa = _step_f(P, tobs, cfg.nbins, cfg.eta), _shift_factors(P, tobs, cfg.nbins)
         for j in range(P):
             d.dparams_f[j] = float(sf[j])
             d.factors[j] = float(fa[j])
-        if self.moving:
+        if self.cheby:
+            c_prev = sc.get_previous_coord(level, self.moving)
+            d.basis = 1
+            _set_rowprod(d.cm_prev, _cheby_matrix(P, c_prev[0], c_prev[1], c_cur[0], c_cur[1]))
+            t_from = c_cur[0] if self.moving else c_init[0]
+            _set_rowprod(d.cm_add, _cheby_matrix(P, t_from, c_cur[1], c_add[0], c_cur[1]))
+            _set_rowprod(d.cm_init, _cheby_matrix(P, c_cur[0], c_cur[1], c_init[0], c_cur[1]))
+            _set_rowprod(d.cm_next, _cheby_matrix(P, c_cur[0], c_cur[1], c_next[0], c_next[1]))
+            self._set_scale(d, c_cur[1])
+        elif self.moving:
             _set(d.tm_add, _taylor(c_add[0] - c_cur[0], P + 1))
             _set(d.tm_init, _taylor(c_init[0] - c_cur[0], P + 1))
             _set(d.tm_next, _taylor(c_next[0] - c_cur[0], P + 1))
@@ -136,6 +244,40 @@ class PruneRun:
         d.freq_min, d.freq_max = float(lim[-1][0]), float(lim[-1][1])
         return d
 
+    def _set_scale(self, d: OPruneLevel, ts: float) -> None:
+        """R and the k! / ts^k scaling of cheby_to_taylor at scale ts."""
+        k = np.arange(self.P + 1)
+        _set_rowprod(d.r_mat, _conn_matrix(_conn_r, self.P))
+        fact = _fact(k)
+        tsk = np.float64(ts) ** k
+        for i in range(MAXP + 1):
+            d.k_fact[i] = float(fact[i]) if i <= self.P else 0.0
+            d.k_tspow[i] = float(tsk[i]) if i <= self.P else 1.0
+
+    def _cheby_seed(self, cart: np.ndarray) -> np.ndarray:
+        """poly_chebyshev_seed (core/chebyshev.py:14-72): the grid leaves in
+        Taylor form (velocity error from the frequency step), then
+        taylor_to_cheby_full (utils/transforms.py:458-487) at the initial
+        segment's scale."""
+        P = self.P
+        n = cart.shape[0]
+        f0 = cart[:, -1]
+        taylor = np.zeros((n, P + 1, 2), np.float64)
+        taylor[:, :-2, 0] = cart[:, :-1]
+        taylor[:, :-2, 1] = self.dparams[:-1]
+        taylor[:, -2, 1] = self.dparams[-1] * (C_VAL / f0)
+        k = np.arange(P + 1)
+        scale = np.float64(self.scheme.get_coord(0)[1]) ** k / _fact(k)
+        s_mat = _conn_matrix(_conn_s, P)
+        vals = _rowprod(self.lib, np.ascontiguousarray(taylor[:, ::-1, 0]) * scale, s_mat)
+        errs = np.sqrt(_rowprod(self.lib, (np.ascontiguousarray(taylor[:, ::-1, 1]) * scale) ** 2,
+                                s_mat**2))
+        leaves = np.zeros((n, P + 2, 2), np.float64)
+        leaves[:, :-1, 0] = vals[:, ::-1]
+        leaves[:, :-1, 1] = errs[:, ::-1]
+        leaves[:, -1, 0] = f0
+        return leaves
+
     def seed(self, ref_seg: int) -> None:
         from oracle.oracle import snr_score_batch
 
@@ -145,11 +287,14 @@ class PruneRun:
         cart = np.stack([m.ravel() for m in mesh], axis=1)
         n = cart.shape[0]
         f0 = cart[:, -1]
-        leaves = np.zeros((n, P + 2, 2), np.float64)
-        leaves[:, : P - 1, 0] = cart[:, :-1]
-        leaves[:, : P - 1, 1] = self.dparams[:-1]
-        leaves[:, -3, 1] = self.dparams[-1] * (C_VAL / f0)
-        leaves[:, -1, 0] = f0
+        if self.cheby:
+            leaves = self._cheby_seed(cart)
+        else:
+            leaves = np.zeros((n, P + 2, 2), np.float64)
+            leaves[:, : P - 1, 0] = cart[:, :-1]
+            leaves[:, : P - 1, 1] = self.dparams[:-1]
+            leaves[:, -3, 1] = self.dparams[-1] * (C_VAL / f0)
+            leaves[:, -1, 0] = f0
         self.leaves = leaves
         self.folds = np.ascontiguousarray(self.fold[self.scheme.ref_idx].reshape(n, 2, nb))
         self.scores = snr_score_batch(self.folds, self.widths, self.nthreads)
@@ -208,11 +353,17 @@ class PruneRun:
         dts = np.zeros(nseg, np.float64)
         for s in range(nseg):
             dt = seg_coords[s, 0] - coord_end[0]
-            tm[s, : P + 1, : P + 1] = _taylor(dt, P + 1)
+            if self.cheby:  # core/chebyshev.py:254-300: re-centred at each segment
+                tm[s, : P + 1, : P + 1] = _cheby_matrix(
+                    P, coord_end[0], coord_end[1], seg_coords[s, 0], coord_end[1]).T
+            else:
+                tm[s, : P + 1, : P + 1] = _taylor(dt, P + 1)
             dts[s] = dt
         segs = [np.ascontiguousarray(self.fold[i]) for i in seg_idx]
         ptrs = (C.c_void_p * nseg)(*[s.ctypes.data for s in segs])
         d = self._level(self.level)
+        if self.cheby:
+            self._set_scale(d, coord_end[1])
         self.lib.oracle_prune_ascend(
             C.byref(d), _p(self.leaves), _p(self.folds), _p(self.scores), _p(self.scores_ep),
             n, nseg, _p(tm), _p(dts), C.cast(ptrs, C.c_void_p), _p(self.widths),

@@ -12,8 +12,10 @@ import pytest
 from tests.conftest import load_golden
 
 CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
-         "prune_taylor_overflow"]
-TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature"}
+         "prune_taylor_overflow", "prune_cheby", "prune_cheby_fixed", "prune_cheby_cons",
+         "prune_cheby_quad"]
+TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature",
+          "prune_cheby_cons": "conservative", "prune_cheby_quad": "quadrature"}
 
 
 def _run(name):
@@ -31,7 +33,8 @@ def _run(name):
     param_arr = cfg.get_param_arr(cfg.get_dparams(n))
     run = PruneRun(cfg, d["fold_ffa"], param_arr, cfg.get_dparams_actual(n), d["thresholds"],
                    max_sugg=int(d["max_sugg"]), batch_size=int(d["batch_size"]),
-                   moving=bool(d["moving"]), nthreads=2)
+                   moving=bool(d["moving"]), nthreads=2,
+                   basis=str(d["basis"]) if "basis" in d else "taylor")
     return d, run
 
 
@@ -64,3 +67,41 @@ def test_prune_oracle_matches_reference(name):
     np.testing.assert_array_equal(run.scores_ep, d["asc_scores_ep"])
     if "asc_folds" in d:
         np.testing.assert_array_equal(run.folds, d["asc_folds"])
+
+
+def test_prune_oracle_chebyshev_full_size():
+    """The Chebyshev oracle over the pruning benchmark's series at full size
+    (2^22 samples, 128 segments, 127 levels, designed thresholds) against a
+    full run of the reference's own Pruning (prune_large_chebyshev.npz):
+    every level's statistics and score range, the survivors' scores and
+    backtracks after the last level, and the ascend."""
+    import bench
+    from oracle import oracle as O
+    from oracle.prune_oracle import PruneRun
+
+    d = load_golden("prune_large_chebyshev")
+    cfg = bench.make_prune_cfg()
+    ts, _ = bench.make_prune_series(seed=int(d["seed"]))
+    fold = O.ffa_execute(ts.ts_e, ts.ts_v, cfg)
+    n = cfg.niters_ffa
+    run = PruneRun(cfg, fold, cfg.get_param_arr(cfg.get_dparams(n)), cfg.get_dparams_actual(n),
+                   d["thresholds"], max_sugg=bench.PRUNE_MAX_SUGG, batch_size=bench.PRUNE_BATCH,
+                   basis="chebyshev")
+    run.seed(int(d["ref_seg"]))
+    levels = int(d["levels_done"])
+    for _ in range(levels):
+        if not run.step():
+            break
+    np.testing.assert_array_equal(np.array(run.stats, np.int64), d["stats"])
+    for lvl in range(1, levels + 1):
+        np.testing.assert_array_equal(
+            run.smm[lvl - 1], d[f"smm_{lvl}"].astype(np.float32).astype(np.float64),
+            err_msg=f"score range level {lvl}")
+    np.testing.assert_array_equal(run.scores, d["scores_last"])
+    nparams = cfg.nparams
+    bt = run.backtracks
+    np.testing.assert_array_equal(np.concatenate([bt[:, : nparams + 1], bt[:, -1:]], axis=1),
+                                  d["bt_last"])
+    run.ascend()
+    np.testing.assert_array_equal(run.scores, d["asc_scores"])
+    np.testing.assert_array_equal(run.scores_ep, d["asc_scores_ep"])
