@@ -68,6 +68,14 @@ typedef struct {
   double r_mat[M6][M6];   /* compute_connection_matrix_r, row-product form */
   double k_fact[M6];      /* k! */
   double k_tspow[M6];     /* ts^k, ts the scale of the resolve domain */
+  /* circular-orbit tree (basis = 2, poly_order 5) */
+  double sig_prop;        /* propagator_significance */
+  double sig_val;         /* validation_significance */
+  double omega_max_sq;    /* (2 pi / p_orb_min)^2 */
+  double x_mass_const;
+  double dt_add;          /* moving: t0_add - t0_cur; fixed: t0_add - t0_init */
+  double dt_init;         /* moving: t0_init - t0_cur */
+  double dt_next;         /* moving: t0_next - t0_cur */
 } OPruneLevel;
 
 static void set_threads(int nthreads) {
@@ -200,6 +208,7 @@ typedef struct {
   int64_t parent;
   int32_t ia, iff;
   double phase;
+  int cls; /* circular tree: 1 snap, 2 crackle, 0 Taylor */
 } Child;
 
 /* Child k (C-order odometer, last parameter fastest) of parent lf. */
@@ -338,6 +347,233 @@ static void transform_cheby(const OPruneLevel* L, const double* in, double* out)
   if (L->moving) cheby_shift(L, L->cm_next, in, out);
 }
 
+/* core/circular.py:14-81 get_circ_mask for one leaf (values v, errors e,
+ * rows [crackle, snap, jerk, accel, ...]): 1 circular by snap-accel, 2 by
+ * crackle-jerk (the hole), 0 Taylor. */
+static int circ_class(const double* v, const double* e, double sig) {
+  const int sig_snap = fabs(v[1]) > sig * e[1];
+  const int sig_accel = fabs(v[3]) > sig * e[3];
+  const int sig_jerk = fabs(v[2]) > sig * e[2];
+  if (sig_snap && sig_accel && (-v[1] * v[3]) > 0) return 1;
+  if (sig_jerk && (-v[0] * v[2]) > 0) return 2;
+  return 0;
+}
+
+/* utils/transforms.py:248-310 shift_taylor_circular_params of one leaf's
+ * values [d5 .. d0] by dt (in_hole: omega from crackle-jerk). */
+static void circ_shift(const double* v, double dt, int in_hole, double* o) {
+  const double d5 = v[0], d4 = v[1], d3 = v[2], d2 = v[3], d1 = v[4], d0 = v[5];
+  const double w2 = in_hole ? -d5 / d3 : -d4 / d2;
+  const double w = sqrt(w2);
+  const double wdt = w * dt;
+  const double c = cos(wdt), sn = sin(wdt);
+  const double d2j = d2 * c + (d3 / w) * sn;
+  const double d3j = d3 * c - (d2 * w) * sn;
+  const double d1ci = -d3 / w2, d1cj = -d3j / w2;
+  const double d0cj = -d2j / w2, d0ci = -d2 / w2;
+  o[0] = -w2 * d3j;
+  o[1] = -w2 * d2j;
+  o[2] = d3j;
+  o[3] = d2j;
+  o[4] = d1cj + (d1 - d1ci);
+  o[5] = d0cj + (d0 - d0ci) + (d1 - d1ci) * dt;
+}
+
+/* core/circular.py:83-125 circ_validate_batch for one leaf */
+static int circ_valid(const OPruneLevel* L, const double* v, const double* e) {
+  const double vs = L->sig_val;
+  const int sig_snap = fabs(v[1]) > vs * e[1];
+  const int sig_accel = fabs(v[3]) > vs * e[3];
+  const int phys = (-v[1] * v[3]) > 0.0;
+  if (!(sig_snap && sig_accel)) return 1; /* the hole is never validated */
+  if (!phys) return 0;
+  const double w2 = -v[1] / v[3];
+  const double limit = L->x_mass_const * pow(w2, 2.0 / 3.0);
+  return w2 <= L->omega_max_sq && fabs(v[3]) <= limit;
+}
+
+/* core/circular.py:444-597 (moving and fixed grid) for one child; sets its class */
+static void resolve_circ(const OPruneLevel* L, Child* ch) {
+  const int P = 5, m = 6;
+  double v[M6], e[M6];
+  for (int i = 0; i < m; ++i) {
+    v[i] = ch->leaf[2 * i];
+    e[i] = ch->leaf[2 * i + 1];
+  }
+  ch->cls = circ_class(v, e, L->sig_prop);
+  if (ch->cls == 0) {
+    resolve(L, ch);
+    return;
+  }
+  const double f0 = ch->leaf[2 * (P + 1)];
+  double a[M6];
+  circ_shift(v, L->dt_add, ch->cls == 2, a);
+  double accel = a[3], vel = a[4], dd = a[5];
+  if (L->moving) {
+    double b[M6];
+    circ_shift(v, L->dt_init, ch->cls == 2, b);
+    vel = a[4] - b[4];
+    dd = a[5] - b[5];
+  }
+  const double freq = f0 * (1 - vel / C_VAL);
+  const double delay = dd / C_VAL;
+  ch->phase = phase_idx(L->dt_phase, f0, L->nbins, delay);
+  ch->ia = (int32_t)nearest(accel, L->accel_min, L->accel_max, L->n_accel);
+  ch->iff = (int32_t)nearest(freq, L->freq_min, L->freq_max, L->n_freq);
+}
+
+/* core/circular.py:670-706 (moving grid): closed-form shift of the values
+ * (errors unchanged) for the circular classes, the Taylor transform else */
+static void transform_circ(const OPruneLevel* L, const Child* ch, double* out) {
+  const int P = 5;
+  if (!L->moving) {
+    memcpy(out, ch->leaf, sizeof(double) * 2 * (P + 2));
+    return;
+  }
+  if (ch->cls == 0) {
+    transform(L, ch->leaf, out);
+    return;
+  }
+  memcpy(out, ch->leaf, sizeof(double) * 2 * (P + 2));
+  double v[M6], o[M6];
+  for (int i = 0; i < P + 1; ++i) v[i] = ch->leaf[2 * i];
+  circ_shift(v, L->dt_next, ch->cls == 2, o);
+  for (int i = 0; i < P + 1; ++i) out[2 * i] = o[i];
+}
+
+/* core/circular.py:205-395 circ_taylor_branch_batch over parents [b0, b1)
+ * then circ_taylor_validate_batch (398-441): the validated children in the
+ * reference's order (the kept children of every parent, then each
+ * expanded cell's crackle children). Returns the validated count, or -1
+ * when a parameter needs more than branch_max children; *n_branch gets the
+ * count before validation. */
+static int64_t circ_children(const OPruneLevel* L, const double* leaves, int64_t b0,
+                             int64_t b1, Child** out, int64_t* n_branch) {
+  const int P = 5;
+  const int64_t nbat = b1 - b0;
+  Branch* br = (Branch*)malloc(sizeof(Branch) * nbat);
+  int* needs0 = (int*)malloc(sizeof(int) * nbat);
+  double* d0new = (double*)malloc(sizeof(double) * nbat);
+  int64_t total = 0;
+  int rc = 0;
+  for (int64_t i = 0; i < nbat && !rc; ++i) {
+    const double* lf = leaves + (b0 + i) * 2 * (P + 2);
+    rc = branch_parent(L, lf, &br[i]);
+    /* crackle: held at the parent value with the would-be child step
+     * (psr_utils.py:383-398), or the parent step when it needs no branching */
+    const double f0 = lf[2 * (P + 1)];
+    const double dcur = lf[1], dnew = L->dparams_f[0] * C_VAL / f0;
+    const double shift = fabs(dcur - dnew) * (L->factors[0] * (f0 / C_VAL));
+    needs0[i] = !(shift < L->eta - FLOAT_EPSILON);
+    d0new[i] = dnew;
+    double dact = dcur;
+    if (needs0[i] && dcur > 0.0 && dnew > 0.0) {
+      int64_t num = (int64_t)ceil(dcur / dnew - FLOAT_EPSILON);
+      if (num < 1) num = 1;
+      dact = dcur / (double)num;
+    }
+    br[i].total /= br[i].count[0];
+    br[i].count[0] = 1;
+    br[i].branched[0] = 0;
+    br[i].first[0] = lf[0];
+    br[i].dact[0] = dact;
+    total += br[i].total;
+  }
+  if (rc) {
+    free(br);
+    free(needs0);
+    free(d0new);
+    return -1;
+  }
+  /* first product; cells in the hole whose crackle step is too coarse expand */
+  typedef struct {
+    double leaf[2 * (MAXP + 2)];
+    int64_t parent;
+  } Cell;
+  Cell* first = (Cell*)malloc(sizeof(Cell) * (total > 0 ? total : 1));
+  int* expand = (int*)malloc(sizeof(int) * (total > 0 ? total : 1));
+  int64_t n_keep = 0, n_exp_children = 0, c = 0;
+  for (int64_t i = 0; i < nbat; ++i) {
+    const double* lf = leaves + (b0 + i) * 2 * (P + 2);
+    for (int64_t k = 0; k < br[i].total; ++k, ++c) {
+      make_child(L, lf, &br[i], k, first[c].leaf);
+      first[c].parent = b0 + i;
+      double v[M6], e[M6];
+      for (int j = 0; j < P + 1; ++j) {
+        v[j] = first[c].leaf[2 * j];
+        e[j] = first[c].leaf[2 * j + 1];
+      }
+      const double sg = L->sig_prop;
+      const int snap = fabs(v[1]) > sg * e[1] && fabs(v[3]) > sg * e[3] && (-v[1] * v[3]) > 0;
+      expand[c] = !snap && fabs(v[2]) > sg * e[2] && needs0[i];
+      if (!expand[c]) {
+        ++n_keep;
+      } else {
+        const double dcur = lf[1];
+        int64_t num = (int64_t)ceil(dcur / d0new[i] - FLOAT_EPSILON);
+        if (num < 1) num = 1;
+        if (num > L->branch_max) rc = -1;
+        n_exp_children += num;
+      }
+    }
+  }
+  *n_branch = n_keep + n_exp_children;
+  Child* ch = (Child*)malloc(sizeof(Child) * (*n_branch > 0 ? *n_branch : 1));
+  int64_t w = 0;
+  for (int pass = 0; pass < 2 && !rc; ++pass) {
+    for (int64_t q = 0; q < total; ++q) {
+      if (expand[q] != pass) continue;
+      const Cell* src = &first[q];
+      if (!pass) {
+        memcpy(ch[w].leaf, src->leaf, sizeof(src->leaf));
+        ch[w++].parent = src->parent;
+        continue;
+      }
+      /* psr_utils.py:347-380 branch_param_padded of the crackle */
+      const double* lf = leaves + src->parent * 2 * (P + 2);
+      const double pcur = src->leaf[0], dcur = lf[1];
+      const double dnew = d0new[src->parent - b0];
+      int64_t num = (int64_t)ceil(dcur / dnew - FLOAT_EPSILON);
+      if (num < 1) num = 1;
+      const double dact = dcur / (double)num;
+      const double first_center = (pcur - dcur / 2.0) + dact / 2.0;
+      for (int64_t k = 0; k < num; ++k) {
+        memcpy(ch[w].leaf, src->leaf, sizeof(src->leaf));
+        ch[w].parent = src->parent;
+        ch[w].leaf[0] = first_center + (double)k * dact;
+        ch[w].leaf[1] = dact;
+        ++w;
+      }
+    }
+  }
+  free(first);
+  free(expand);
+  free(br);
+  free(needs0);
+  free(d0new);
+  if (rc) {
+    free(ch);
+    return -1;
+  }
+  /* validation keeps the order */
+  int64_t nv = 0;
+  for (int64_t q = 0; q < w; ++q) {
+    double v[M6], e[M6];
+    for (int j = 0; j < P + 1; ++j) {
+      v[j] = ch[q].leaf[2 * j];
+      e[j] = ch[q].leaf[2 * j + 1];
+    }
+    if (!circ_valid(L, v, e)) continue;
+    if (nv != q) {
+      memcpy(ch[nv].leaf, ch[q].leaf, sizeof(ch[q].leaf));
+      ch[nv].parent = ch[q].parent;
+    }
+    ++nv;
+  }
+  *out = ch;
+  return nv;
+}
+
 /* np.partition order: ascending, NaN last. */
 static int cmp_float(const void* a, const void* b) {
   const float x = *(const float*)a, y = *(const float*)b;
@@ -403,6 +639,78 @@ static double add_batch(Tree* T, int64_t n, double* const* leaves, float* const*
   return eff;
 }
 
+/* core/common.py:375-400 shift_add_batch + scoring.py:249-282 for one child */
+static void fold_score(const OPruneLevel* L, Child* c, const float* folds, const float* seg,
+                       const int64_t* widths, int nw, float* norm, float* prefix) {
+  const int nb = L->nbins;
+  const int s = round_shift(c->phase, nb);
+  const float* pf = folds + c->parent * 2 * nb;
+  const float* sf = seg + ((int64_t)c->ia * L->n_freq + c->iff) * 2 * nb;
+  int src = (nb - s) % nb;
+  for (int j = 0; j < nb; ++j) {
+    c->fold[j] = pf[j] + sf[src];
+    c->fold[nb + j] = pf[nb + j] + sf[nb + src];
+    if (++src == nb) src = 0;
+  }
+  c->score = score_fold(c->fold, nb, widths, nw, norm, prefix);
+}
+
+/* prune.py:276-323 for one batch's scored children: score range,
+ * threshold, transform of the survivors, backtracks, add_batch. */
+static void select_add(const OPruneLevel* L, Child* ch, int64_t nch, double threshold,
+                       double* current, Tree* T, double* smin, double* smax) {
+  const int P = L->poly_order;
+  /* np.min/np.max over the batch; Python min/max then skip a NaN batch value */
+  float bmin = ch[0].score, bmax = ch[0].score;
+  int has_nan = 0;
+  for (int64_t c = 0; c < nch; ++c) {
+    const float s = ch[c].score;
+    if (s != s) has_nan = 1;
+    if (s < bmin) bmin = s;
+    if (s > bmax) bmax = s;
+  }
+  if (!has_nan) {
+    if ((double)bmin < *smin) *smin = bmin;
+    if ((double)bmax > *smax) *smax = bmax;
+  }
+  const double thr = threshold > *current ? threshold : *current;
+  int64_t npass = 0;
+  for (int64_t c = 0; c < nch; ++c) npass += (double)ch[c].score >= thr;
+  if (npass == 0) return;
+  double** pl = (double**)malloc(sizeof(double*) * npass);
+  float** pfo = (float**)malloc(sizeof(float*) * npass);
+  int32_t** pbt = (int32_t**)malloc(sizeof(int32_t*) * npass);
+  float* ps = (float*)malloc(sizeof(float) * npass);
+  double* tl = (double*)malloc(sizeof(double) * npass * 2 * (P + 2));
+  int32_t* tb = (int32_t*)malloc(sizeof(int32_t) * npass * (P + 2));
+  int64_t w = 0;
+  for (int64_t c = 0; c < nch; ++c) {
+    if (!((double)ch[c].score >= thr)) continue;
+    double* out = tl + w * 2 * (P + 2);
+    if (L->basis == 2) transform_circ(L, &ch[c], out);
+    else if (L->basis == 1) transform_cheby(L, ch[c].leaf, out);
+    else transform(L, ch[c].leaf, out);
+    int32_t* bt = tb + w * (P + 2);
+    memset(bt, 0, sizeof(int32_t) * (P + 2));
+    bt[0] = (int32_t)ch[c].parent;
+    bt[L->nparams_ffa - 1] = ch[c].ia;
+    bt[L->nparams_ffa] = ch[c].iff;
+    bt[P + 1] = (int32_t)ch[c].phase;
+    pl[w] = out;
+    pfo[w] = ch[c].fold;
+    pbt[w] = bt;
+    ps[w] = ch[c].score;
+    ++w;
+  }
+  *current = add_batch(T, npass, pl, pfo, ps, pbt, *current);
+  free(pl);
+  free(pfo);
+  free(pbt);
+  free(ps);
+  free(tl);
+  free(tb);
+}
+
 /*
  * One pruning level. leaves (n_par, P+2, 2) f64, folds (n_par, 2, nbins) f32,
  * seg = FFA fold of the added segment (n_accel*n_freq rows of (2, nbins)).
@@ -417,122 +725,96 @@ int64_t oracle_prune_level(const OPruneLevel* L, const double* leaves, const flo
                            int64_t* stats, double* smm, int nthreads) {
   set_threads(nthreads);
   const int P = L->poly_order, nb = L->nbins;
-  if (nb > 256 || P < 2 || P > MAXP) return -2;
+  if (nb > 256 || P < 2 || P > MAXP || (L->basis == 2 && P != 5)) return -2;
   Tree T = {lout, fout, sout, bout, 0, max_sugg, P, nb};
   double current = threshold;
-  int64_t n_leaves = 0;
+  int64_t n_leaves = 0, n_phy = 0;
   double smin = INFINITY, smax = -INFINITY;
   if (batch_size > n_par) batch_size = n_par;
   if (batch_size < 1) batch_size = 1;
-  const int cheby = L->basis == 1;
+  const int cheby = L->basis == 1, circ = L->basis == 2;
   Branch* br = (Branch*)malloc(sizeof(Branch) * batch_size);
   int64_t* off = (int64_t*)malloc(sizeof(int64_t) * (batch_size + 1));
   /* Chebyshev: the batch's parents shifted to the current domain */
   double* shifted = cheby ? (double*)malloc(sizeof(double) * batch_size * 2 * (P + 2)) : NULL;
-  for (int64_t b0 = 0; b0 < n_par; b0 += batch_size) {
+  int rc = 0;
+  for (int64_t b0 = 0; b0 < n_par && !rc; b0 += batch_size) {
     const int64_t b1 = b0 + batch_size < n_par ? b0 + batch_size : n_par;
     const int64_t nbat = b1 - b0;
-    off[0] = 0;
-    for (int64_t i = 0; i < nbat; ++i) {
-      const double* lf = leaves + (b0 + i) * 2 * (P + 2);
-      if (cheby) {
-        double* sh = shifted + i * 2 * (P + 2);
-        memcpy(sh, lf, sizeof(double) * 2 * (P + 2));
-        cheby_shift(L, L->cm_prev, lf, sh);
-        lf = sh;
+    Child* ch = NULL;
+    int64_t nch = 0;
+    if (circ) {
+      int64_t nbr = 0;
+      nch = circ_children(L, leaves, b0, b1, &ch, &nbr);
+      if (nch < 0) {
+        rc = -1;
+        break;
       }
-      if (branch_parent(L, lf, &br[i])) {
-        free(br);
-        free(off);
-        free(shifted);
-        return -1;
-      }
-      off[i + 1] = off[i] + br[i].total;
-    }
-    const int64_t nch = off[nbat];
-    n_leaves += nch;
-    if (nch == 0) continue;
-    Child* ch = (Child*)malloc(sizeof(Child) * nch);
+      n_leaves += nbr;
+      n_phy += nch;
 #pragma omp parallel
-    {
-      float norm[512], prefix[1024];
+      {
+        float norm[512], prefix[1024];
 #pragma omp for schedule(static)
-      for (int64_t i = 0; i < nbat; ++i) {
-        const double* lf = cheby ? shifted + i * 2 * (P + 2) : leaves + (b0 + i) * 2 * (P + 2);
-        for (int64_t k = 0; k < br[i].total; ++k) {
-          Child* c = &ch[off[i] + k];
-          make_child(L, lf, &br[i], k, c->leaf);
-          c->parent = b0 + i;
-          if (cheby) resolve_cheby(L, c);
-          else resolve(L, c);
-          const int s = round_shift(c->phase, nb);
-          const float* pf = folds + (b0 + i) * 2 * nb;
-          const float* sf = seg + ((int64_t)c->ia * L->n_freq + c->iff) * 2 * nb;
-          int src = (nb - s) % nb;
-          for (int j = 0; j < nb; ++j) {
-            c->fold[j] = pf[j] + sf[src];
-            c->fold[nb + j] = pf[nb + j] + sf[nb + src];
-            if (++src == nb) src = 0;
+        for (int64_t c = 0; c < nch; ++c) {
+          resolve_circ(L, &ch[c]);
+          fold_score(L, &ch[c], folds, seg, widths, nw, norm, prefix);
+        }
+      }
+      if (L->moving) { /* core/circular.py:478-509: the basis flag of the batch */
+        int has_taylor = 0;
+        for (int64_t c = 0; c < nch; ++c) has_taylor |= ch[c].cls == 0;
+        for (int64_t c = 0; c < nch; ++c) {
+          double* flag = &ch[c].leaf[2 * (P + 1) + 1];
+          if (ch[c].cls == 1) *flag = 1.0;
+          else if (ch[c].cls == 2) *flag = has_taylor ? 0.0 : 2.0;
+        }
+      }
+    } else {
+      off[0] = 0;
+      for (int64_t i = 0; i < nbat && !rc; ++i) {
+        const double* lf = leaves + (b0 + i) * 2 * (P + 2);
+        if (cheby) {
+          double* sh = shifted + i * 2 * (P + 2);
+          memcpy(sh, lf, sizeof(double) * 2 * (P + 2));
+          cheby_shift(L, L->cm_prev, lf, sh);
+          lf = sh;
+        }
+        rc = branch_parent(L, lf, &br[i]);
+        off[i + 1] = off[i] + br[i].total;
+      }
+      if (rc) break;
+      nch = off[nbat];
+      n_leaves += nch;
+      n_phy += nch;
+      if (nch > 0) ch = (Child*)malloc(sizeof(Child) * nch);
+#pragma omp parallel
+      {
+        float norm[512], prefix[1024];
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < nbat; ++i) {
+          const double* lf =
+              cheby ? shifted + i * 2 * (P + 2) : leaves + (b0 + i) * 2 * (P + 2);
+          for (int64_t k = 0; k < br[i].total; ++k) {
+            Child* c = &ch[off[i] + k];
+            make_child(L, lf, &br[i], k, c->leaf);
+            c->parent = b0 + i;
+            if (cheby) resolve_cheby(L, c);
+            else resolve(L, c);
+            fold_score(L, c, folds, seg, widths, nw, norm, prefix);
           }
-          c->score = score_fold(c->fold, nb, widths, nw, norm, prefix);
         }
       }
     }
-    /* np.min/np.max over the batch; Python min/max then skip a NaN batch value */
-    float bmin = ch[0].score, bmax = ch[0].score;
-    int has_nan = 0;
-    for (int64_t c = 0; c < nch; ++c) {
-      const float s = ch[c].score;
-      if (s != s) has_nan = 1;
-      if (s < bmin) bmin = s;
-      if (s > bmax) bmax = s;
-    }
-    if (!has_nan) {
-      if ((double)bmin < smin) smin = bmin;
-      if ((double)bmax > smax) smax = bmax;
-    }
-    const double thr = threshold > current ? threshold : current;
-    int64_t npass = 0;
-    for (int64_t c = 0; c < nch; ++c) npass += (double)ch[c].score >= thr;
-    if (npass > 0) {
-      double** pl = (double**)malloc(sizeof(double*) * npass);
-      float** pfo = (float**)malloc(sizeof(float*) * npass);
-      int32_t** pbt = (int32_t**)malloc(sizeof(int32_t*) * npass);
-      float* ps = (float*)malloc(sizeof(float) * npass);
-      double* tl = (double*)malloc(sizeof(double) * npass * 2 * (P + 2));
-      int32_t* tb = (int32_t*)malloc(sizeof(int32_t) * npass * (P + 2));
-      int64_t w = 0;
-      for (int64_t c = 0; c < nch; ++c) {
-        if (!((double)ch[c].score >= thr)) continue;
-        if (cheby) transform_cheby(L, ch[c].leaf, tl + w * 2 * (P + 2));
-        else transform(L, ch[c].leaf, tl + w * 2 * (P + 2));
-        int32_t* bt = tb + w * (P + 2);
-        memset(bt, 0, sizeof(int32_t) * (P + 2));
-        bt[0] = (int32_t)ch[c].parent;
-        bt[L->nparams_ffa - 1] = ch[c].ia;
-        bt[L->nparams_ffa] = ch[c].iff;
-        bt[P + 1] = (int32_t)ch[c].phase;
-        pl[w] = tl + w * 2 * (P + 2);
-        pfo[w] = ch[c].fold;
-        pbt[w] = bt;
-        ps[w] = ch[c].score;
-        ++w;
-      }
-      current = add_batch(&T, npass, pl, pfo, ps, pbt, current);
-      free(pl);
-      free(pfo);
-      free(pbt);
-      free(ps);
-      free(tl);
-      free(tb);
-    }
+    if (nch > 0) select_add(L, ch, nch, threshold, &current, &T, &smin, &smax);
     free(ch);
   }
   free(br);
   free(off);
   free(shifted);
+  if (rc) return -1;
   stats[0] = n_leaves;
-  stats[1] = n_leaves;
+  stats[1] = n_phy;
   smm[0] = isfinite(smin) ? smin : 0.0;
   smm[1] = isfinite(smax) ? smax : 0.0;
   return T.valid;
@@ -561,12 +843,24 @@ void oracle_prune_ascend(const OPruneLevel* L, const double* leaves, float* fold
       double pv[M6];
       for (int i = 0; i < m; ++i) pv[i] = lf[2 * i];
       const double f0 = lf[2 * m];
+      int cls = 0;
+      if (L->basis == 2) {
+        double ev[M6];
+        for (int i = 0; i < m; ++i) ev[i] = lf[2 * i + 1];
+        cls = circ_class(pv, ev, L->sig_prop);
+      }
       float* acc = folds + r * 2 * nb;
       for (int j = 0; j < 2 * nb; ++j) acc[j] = 0.0f;
       for (int s = 0; s < nseg; ++s) {
         const double(*T)[M6] = (const double(*)[M6])(tm + s * M6 * M6);
         double accel, freq, delay;
-        if (L->basis == 1) {  /* core/chebyshev.py:254-300: tm holds the re-centring */
+        if (L->basis == 2 && cls != 0) {  /* core/circular.py:598-667 */
+          double o[M6];
+          circ_shift(pv, dt[s], cls == 2, o);
+          accel = o[3];
+          freq = f0 * (1 - o[4] / C_VAL);
+          delay = o[5] / C_VAL;
+        } else if (L->basis == 1) {  /* core/chebyshev.py:254-300: tm holds the re-centring */
           double d[M6];
           cheby_taylor(L, T, pv, d);
           accel = d[2];

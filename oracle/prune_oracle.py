@@ -1,4 +1,5 @@
-"""CPU oracle of the Taylor and Chebyshev enumerate-prune runs (``prune_oracle.c``).
+"""CPU oracle of the Taylor, Chebyshev and circular-orbit enumerate-prune runs
+(``prune_oracle.c``).
 
 Test infrastructure only: the checker for the GPU pruning path in tests/ and
 the CPU leg of bench.py's pruning measurement. It drives one run the way the
@@ -11,7 +12,11 @@ expressions (``utils/transforms.py:41-45``, ``utils/psr_utils.py:59-95,
 227-248``). With ``basis="chebyshev"`` the seed is ``poly_chebyshev_seed``
 (``core/chebyshev.py:14-72``) and the per-level Chebyshev matrices are
 restated from ``utils/maths.py:400-570`` (connection coefficients S and R,
-the domain-change matrix C) in the reference's order of evaluation.
+the domain-change matrix C) in the reference's order of evaluation. A
+Taylor tree of order 5 is the circular-orbit tree (``PruneCircTaylorDPFuncts``,
+the reference's dispatch key ``prune.py:373-381``): Taylor seed and matrices,
+plus the classification, validation and closed-form orbit constants of
+``core/circular.py`` per level.
 """
 
 from __future__ import annotations
@@ -44,6 +49,9 @@ class OPruneLevel(C.Structure):
         ("cm_prev", _M6), ("cm_add", _M6), ("cm_init", _M6), ("cm_next", _M6),
         ("r_mat", _M6), ("k_fact", C.c_double * (MAXP + 1)),
         ("k_tspow", C.c_double * (MAXP + 1)),
+        ("sig_prop", C.c_double), ("sig_val", C.c_double), ("omega_max_sq", C.c_double),
+        ("x_mass_const", C.c_double), ("dt_add", C.c_double), ("dt_init", C.c_double),
+        ("dt_next", C.c_double),
     ]
 
 
@@ -195,6 +203,10 @@ class PruneRun:
             msg = f"basis must be 'taylor' or 'chebyshev', got {basis!r}"
             raise ValueError(msg)
         self.cheby = basis == "chebyshev"
+        self.circ = not self.cheby and self.P == 5
+        if self.circ and not cfg.p_orb_min > 0:
+            msg = "the circular-orbit tree needs p_orb_min"
+            raise ValueError(msg)
         self.lib = load()
         _bind(self.lib)
 
@@ -237,6 +249,18 @@ class PruneRun:
             _set(d.tm_next, _taylor(c_next[0] - c_cur[0], P + 1))
         else:
             _set(d.tm_add, _taylor(c_add[0] - c_init[0], P + 1))
+        if self.circ:  # core/circular.py:83-125, 444-706 and their constants
+            d.basis = 2
+            d.sig_prop = cfg.propagator_significance
+            d.sig_val = cfg.validation_significance
+            d.omega_max_sq = (2 * np.pi / cfg.p_orb_min) ** 2
+            d.x_mass_const = cfg.x_mass_const
+            if self.moving:
+                d.dt_add = c_add[0] - c_cur[0]
+                d.dt_init = c_init[0] - c_cur[0]
+                d.dt_next = c_next[0] - c_cur[0]
+            else:
+                d.dt_add = c_add[0] - c_init[0]
         d.dt_phase = c_add[0] - c_init[0]
         lim = cfg.param_limits
         d.n_accel, d.n_freq = int(self.counts[-2]), int(self.counts[-1])

@@ -13,9 +13,11 @@ from tests.conftest import load_golden
 
 CASES = ["prune_taylor", "prune_taylor_fixed", "prune_taylor_cons", "prune_taylor_quad",
          "prune_taylor_overflow", "prune_cheby", "prune_cheby_fixed", "prune_cheby_cons",
-         "prune_cheby_quad"]
+         "prune_cheby_quad", "prune_circ", "prune_circ_b4", "prune_circ_quad",
+         "prune_circ_fixed"]
 TILING = {"prune_taylor_cons": "conservative", "prune_taylor_quad": "quadrature",
-          "prune_cheby_cons": "conservative", "prune_cheby_quad": "quadrature"}
+          "prune_cheby_cons": "conservative", "prune_cheby_quad": "quadrature",
+          "prune_circ_quad": "quadrature"}
 
 
 def _run(name):
@@ -28,7 +30,8 @@ def _run(name):
         eta=float(d["eta"]), param_limits=d["param_limits"], ducy_max=float(d["ducy_max"]),
         wtsp=float(d["wtsp"]), use_fourier=False, bseg_ffa=int(d["bseg_ffa"]),
         prune_poly_order=int(d["poly_order"]), branch_max=int(d["branch_max"]),
-        tiling_strategy=TILING.get(name, "aggressive"))
+        tiling_strategy=TILING.get(name, "aggressive"),
+        p_orb_min=float(d["p_orb_min"]) if "p_orb_min" in d else 0.0)
     n = cfg.niters_ffa
     param_arr = cfg.get_param_arr(cfg.get_dparams(n))
     run = PruneRun(cfg, d["fold_ffa"], param_arr, cfg.get_dparams_actual(n), d["thresholds"],
@@ -69,24 +72,26 @@ def test_prune_oracle_matches_reference(name):
         np.testing.assert_array_equal(run.folds, d["asc_folds"])
 
 
-def test_prune_oracle_chebyshev_full_size():
-    """The Chebyshev oracle over the pruning benchmark's series at full size
-    (2^22 samples, 128 segments, 127 levels, designed thresholds) against a
-    full run of the reference's own Pruning (prune_large_chebyshev.npz):
-    every level's statistics and score range, the survivors' scores and
-    backtracks after the last level, and the ascend."""
+@pytest.mark.parametrize("tree", ["chebyshev", "circular"])
+def test_prune_oracle_full_size(tree):
+    """The Chebyshev oracle, and the circular-orbit oracle of order 5, over
+    the pruning benchmark's series at full size (2^22 samples, 128
+    segments, 127 levels, designed thresholds) against full runs of the
+    reference's own Pruning (prune_large_{tree}.npz): every level's
+    statistics and score range, the survivors' scores and backtracks after
+    the last level, and the ascend."""
     import bench
     from oracle import oracle as O
     from oracle.prune_oracle import PruneRun
 
-    d = load_golden("prune_large_chebyshev")
-    cfg = bench.make_prune_cfg()
+    d = load_golden(f"prune_large_{tree}")
+    cfg = bench.make_prune_cfg(circular=tree == "circular")
     ts, _ = bench.make_prune_series(seed=int(d["seed"]))
     fold = O.ffa_execute(ts.ts_e, ts.ts_v, cfg)
     n = cfg.niters_ffa
     run = PruneRun(cfg, fold, cfg.get_param_arr(cfg.get_dparams(n)), cfg.get_dparams_actual(n),
                    d["thresholds"], max_sugg=bench.PRUNE_MAX_SUGG, batch_size=bench.PRUNE_BATCH,
-                   basis="chebyshev")
+                   basis="chebyshev" if tree == "chebyshev" else "taylor")
     run.seed(int(d["ref_seg"]))
     levels = int(d["levels_done"])
     for _ in range(levels):
