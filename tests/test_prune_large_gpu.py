@@ -1,4 +1,4 @@
-"""GPU enumerate-prune against the CPU oracle on the benchmark workload.
+"""GPU enumerate-prune against the CPU oracle and the reference on the benchmark workload.
 
 The circular-orbit search with a Taylor tree to the 4th derivative (2^22
 samples, 128 segments, FFA grid (1, 1, 1, 146)) with its designed per-level
@@ -125,3 +125,64 @@ def test_prune_full_size_matches_reference(cuda_device, tree, device_run):
         _leaves_close(prn.report(), d["report"], "report", circular=True)
     else:
         np.testing.assert_allclose(prn.report(), d["report"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("tree", ["chebyshev", "circular"])
+def test_prune_full_size_matches_oracle(cuda_device, tree):
+    """The Chebyshev tree, and the circular-orbit tree of order 5, on the
+    benchmark workload level by level against the C oracle (itself pinned
+    to the reference's full runs by test_prune_oracle_golden.py): every
+    level's statistics, survivor scores and backtracks, the folds and
+    leaves every 16 levels and at the end, then the ascend."""
+    import bench
+    from oracle import oracle as O
+    from oracle.prune_oracle import PruneRun
+    from pyloki_gb300.ffa import DynamicProgramming
+    from pyloki_gb300.prune import Pruning
+    from tests.test_prune_gpu import _leaves_close
+
+    circ = tree == "circular"
+    cfg = bench.make_prune_cfg(circular=circ)
+    ts, _ = bench.make_prune_series(seed=2000)
+    dyp = DynamicProgramming(ts, cfg, device=cuda_device)
+    dyp.initialize()
+    dyp.execute()
+    fold_cpu = O.ffa_execute(ts.ts_e, ts.ts_v, cfg)
+    np.testing.assert_array_equal(dyp.fold.cpu().numpy(), fold_cpu)
+    nseg = dyp.nsegments
+    thr = bench.prune_thresholds(nseg)
+    n = cfg.niters_ffa
+    basis = "taylor" if circ else "chebyshev"
+    run = PruneRun(cfg, fold_cpu, cfg.get_param_arr(cfg.get_dparams(n)),
+                   cfg.get_dparams_actual(n), thr, max_sugg=bench.PRUNE_MAX_SUGG,
+                   batch_size=bench.PRUNE_BATCH, basis=basis)
+    prn = Pruning(dyp, thr, max_sugg=bench.PRUNE_MAX_SUGG, batch_size=bench.PRUNE_BATCH,
+                  poly_basis=basis)
+    ref = nseg // 2
+    run.seed(ref)
+    prn.initialize(ref)
+    np.testing.assert_array_equal(prn.world_tree.scores.cpu().numpy(), run.scores)
+    nparams = cfg.nparams
+    for lvl in range(1, nseg):
+        alive = run.step()
+        prn.execute_iter()
+        st = prn.pstats[-1]
+        np.testing.assert_array_equal(
+            [st.n_branches, st.n_leaves, st.n_leaves_phy, st.n_leaves_surv],
+            list(run.stats[-1]), err_msg=f"level {lvl}")
+        wt = prn.world_tree
+        np.testing.assert_array_equal(wt.scores.cpu().numpy(), run.scores,
+                                      err_msg=f"scores level {lvl}")
+        bt = wt.backtracks.cpu().numpy()
+        np.testing.assert_array_equal(bt[:, : nparams + 1], run.backtracks[:, : nparams + 1],
+                                      err_msg=f"bt {lvl}")
+        np.testing.assert_array_equal(bt[:, -1], run.backtracks[:, -1], err_msg=f"phase {lvl}")
+        if lvl % 16 == 0 or not alive:
+            np.testing.assert_array_equal(wt.folds.cpu().numpy(), run.folds)
+            _leaves_close(wt.leaves.cpu().numpy(), run.leaves, f"leaves {lvl}", circ)
+        if not alive:
+            break
+    prn._do_ascend()
+    run.ascend()
+    np.testing.assert_array_equal(prn.world_tree.scores.cpu().numpy(), run.scores)
+    np.testing.assert_array_equal(prn.world_tree.folds.cpu().numpy(), run.folds)
