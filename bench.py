@@ -134,12 +134,13 @@ def prune_thresholds(nseg: int) -> np.ndarray:
     return thr
 
 
-def prune_cpu(nthreads: int = 0) -> dict:
-    """The same pruning run on the CPU oracle (all host threads)."""
+def prune_cpu(nthreads: int = 0, circular: bool = False) -> dict:
+    """The same pruning run on the CPU oracle (all host threads); with
+    ``circular``, the circular-orbit tree of order 5."""
     from oracle import oracle as O
     from oracle.prune_oracle import PruneRun
 
-    cfg = make_prune_cfg()
+    cfg = make_prune_cfg(circular=circular)
     ts, _ = make_prune_series(seed=2000)
     fold = O.ffa_execute(ts.ts_e, ts.ts_v, cfg, nthreads)
     n = cfg.niters_ffa
@@ -432,7 +433,8 @@ def bench_prune_circ(args, dev) -> dict:
                                  f"{args.prune_streams} runs at once on their own streams")},
             "config": {"workload": "circ5_prune_circular_orbit_2^22",
                        "ref_segments": len(refs), "poly_order": 5,
-                       "driver": "level-synchronous batch (loki_prune_run_batch, basis 2)"}}
+                       "driver": "level-synchronous batch (loki_prune_run_batch, basis 2)"},
+            "cpu_baseline": prune_cpu(circular=True) if not args.no_cpu_baseline else None}
 
 
 def final_trials(cfg) -> int:
