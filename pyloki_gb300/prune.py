@@ -1863,7 +1863,7 @@ class PruneBlockBatch(PruneBatch):
             # a job that outgrew its workspace is repeated, through the same
             # driver, with grown buffers (the others keep their results)
             todo = list(range(len(runs)))
-            while todo:
+            for attempt in range(17):  # each round grows the workspaces by at least 1.25x
                 grown = []
                 for i in todo:
                     prn, dr = runs[i]
@@ -1880,8 +1880,12 @@ class PruneBlockBatch(PruneBatch):
                         grown.append(i)
                     elif err:
                         _lib.check_dev_err(prn._err)
-                if grown:
-                    self._run_jobs(lib, dev, st, [runs[i] for i in grown], ascend, fourier)
+                if not grown:
+                    break
+                if attempt == 16:
+                    msg = "pruning runs still outgrow their workspaces after 16 enlargements"
+                    raise RuntimeError(msg)
+                self._run_jobs(lib, dev, st, [runs[i] for i in grown], ascend, fourier)
                 todo = grown
             ready = []
             for prn, dr in runs:
