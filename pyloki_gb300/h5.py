@@ -678,8 +678,13 @@ class _FileReader(_Reader):
             msg = f"object header version {ver} at {addr:#x}"
             raise ValueError(msg)
         blocks = [(addr + 16, size)]
+        seen = set()
         while blocks and len(out) < nmsg:
             start, length = blocks.pop(0)
+            if start in seen:
+                msg = f"object header at {addr:#x}: continuation blocks form a cycle"
+                raise ValueError(msg)
+            seen.add(start)
             data = self.at(start, length)
             q = 0
             while q + 8 <= length and len(out) < nmsg:
@@ -703,8 +708,13 @@ class _FileReader(_Reader):
         q += nsz
         blocks = [(q, size)]
         track = bool(flags & 0x04)
+        seen = set()
         while blocks:
             start, length = blocks.pop(0)
+            if start in seen:
+                msg = f"object header at {addr:#x}: continuation blocks form a cycle"
+                raise ValueError(msg)
+            seen.add(start)
             data = self.at(start, length)
             p = 0
             while p + 4 <= length:
@@ -827,8 +837,13 @@ class _FileReader(_Reader):
         dsize, _, daddr = self.u(heap + 8, "QQQ")
         names = self.at(daddr, dsize)
         out = []
+        seen: set[int] = set()
 
         def walk(node: int) -> None:
+            if node in seen:
+                msg = f"group B-tree node {node:#x} is reached twice"
+                raise ValueError(msg)
+            seen.add(node)
             if self.at(node, 4) != b"TREE":
                 msg = f"no B-tree node at {node:#x}"
                 raise ValueError(msg)
@@ -918,6 +933,7 @@ class _FileReader(_Reader):
         if btree == UNDEF:
             return out.tobytes()
         key_size = 8 + 8 * (nd + 1)
+        seen: set[int] = set()
 
         def unfilter(data: bytes, mask: int) -> bytes:
             for k in range(len(flist) - 1, -1, -1):
@@ -940,6 +956,10 @@ class _FileReader(_Reader):
             return data
 
         def walk(node: int) -> None:
+            if node in seen:
+                msg = f"chunk B-tree node {node:#x} is reached twice"
+                raise ValueError(msg)
+            seen.add(node)
             if self.at(node, 4) != b"TREE":
                 msg = f"no B-tree node at {node:#x}"
                 raise ValueError(msg)

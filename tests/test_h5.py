@@ -304,3 +304,34 @@ def test_reads_chunked_deflate_shuffle(tmp_path):
         p = tmp_path / "gz.h5"
         _chunked_dataset_file(p, data, chunk)
         np.testing.assert_array_equal(h5.read_file(p)["gz"].data, data)
+
+
+def test_rejects_damaged_files(tmp_path):
+    """Truncated files, a B-tree node that points back to itself and a
+    continuation block that points back to itself raise ValueError instead
+    of looping or reading out of the file."""
+    g = h5.Group()
+    g.create_dataset("x", data=np.arange(5))
+    h5.write_file(tmp_path / "ok.h5", g)
+    raw = (tmp_path / "ok.h5").read_bytes()
+    (tmp_path / "short.h5").write_bytes(raw[: len(raw) // 2])
+    with pytest.raises(ValueError):
+        h5.read_file(tmp_path / "short.h5")
+    # the root group's B-tree: make its single child the node itself
+    r = h5._FileReader(raw)
+    btree, _ = struct.unpack_from("<QQ", dict(r.messages(r.root_addr))[0x11])
+    bad = bytearray(raw)
+    struct.pack_into("<BBH", bad, btree + 4, 0, 1, 1)  # level 1: children are nodes
+    struct.pack_into("<Q", bad, btree + 24 + 8, btree)
+    (tmp_path / "cycle.h5").write_bytes(bytes(bad))
+    with pytest.raises(ValueError, match="twice"):
+        h5.read_file(tmp_path / "cycle.h5")
+    # an object header whose continuation message points at its own messages
+    w = h5._Writer()
+    hdr = w.header([w.msg(0x10, struct.pack("<QQ", 0, 8)), w.msg(0x01, w.dataspace((1,)))])
+    struct.pack_into("<H", w.out, hdr + 2, 5)  # claim more messages than there are
+    struct.pack_into("<Q", w.out, hdr + 16 + 8, hdr + 16)
+    r2 = h5._FileReader(w.finish(hdr, 0, 0))
+    with pytest.raises(ValueError, match="cycle"):
+        r2.messages(hdr)
+
