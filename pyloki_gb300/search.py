@@ -3,7 +3,8 @@
 ``ffa_search`` returns ``(DynamicProgramming, Periodogram)`` like the
 reference. The S/N array stays on the device; ``Periodogram`` offers the
 reference's ``find_best_indices`` / ``find_best_params`` / ``get_summary``
-(``periodogram.py:25-200``) without the xarray/plotting layer.
+(``periodogram.py:25-200``) and ``save`` / ``load`` in xarray's NetCDF
+layout, without the xarray/plotting layer.
 """
 
 from __future__ import annotations
@@ -65,6 +66,59 @@ class Periodogram:
     def __repr__(self) -> str:
         info = ", ".join(f"{p}: {len(self.params[p])}" for p in self.param_names)
         return f"Periodogram({info}, tobs: {self.tobs})"
+
+    #: the variable name xarray gives an unnamed DataArray in a file
+    DATA_VAR = "__xarray_dataarray_variable__"
+
+    def save(self, filename) -> None:
+        """The periodogram as xarray's ``DataArray.to_netcdf`` writes it
+        (``periodogram.py:165-166``) when no netCDF-4 library is present:
+        a NetCDF-3 (64-bit offset) file with one coordinate variable per
+        parameter and the S/N variable carrying ``tobs``. Integer
+        coordinates are stored as int32, as xarray coerces them for
+        NetCDF-3."""
+        from scipy.io import netcdf_file
+
+        snrs = self.snrs.cpu().numpy() if isinstance(self.snrs, torch.Tensor) else self.snrs
+        with netcdf_file(filename, "w", version=2) as f:
+            for name in self.param_names:
+                vals = np.asarray(self.params[name])
+                if vals.dtype.kind in "iu":
+                    vals = vals.astype(np.int32)
+                else:
+                    vals = vals.astype(np.float64)
+                f.createDimension(name, len(vals))
+                var = f.createVariable(name, vals.dtype, (name,))
+                var[:] = vals
+            data = np.ascontiguousarray(snrs, np.float32)
+            var = f.createVariable(self.DATA_VAR, data.dtype, tuple(self.param_names))
+            var[...] = data
+            var.tobs = np.float64(self.tobs)  # NC_DOUBLE (a Python float would be NC_FLOAT)
+
+    @classmethod
+    def load(cls, filename) -> Periodogram:
+        """A periodogram written by ``save`` or by the reference with
+        xarray's NetCDF-3 backend (``periodogram.py:168-172``)."""
+        from scipy.io import netcdf_file
+
+        with open(filename, "rb") as fh:
+            if fh.read(3) != b"CDF":
+                msg = f"{filename}: not a NetCDF-3 file (NetCDF-4 files need a netCDF-4 reader)"
+                raise ValueError(msg)
+        with netcdf_file(filename, "r", mmap=False) as f:
+            data_vars = [k for k, v in f.variables.items()
+                         if not (v.dimensions == (k,))]
+            if len(data_vars) != 1:
+                msg = f"{filename}: expected one data variable, found {data_vars}"
+                raise ValueError(msg)
+            var = f.variables[data_vars[0]]
+            params = {}
+            for dim in var.dimensions:
+                vals = np.array(f.variables[dim][:])
+                params[dim] = vals.astype(np.int64) if vals.dtype.kind in "iu" else vals
+            snrs = np.array(var[...])
+            tobs = float(var.tobs)
+        return cls(params=params, snrs=snrs, tobs=tobs)
 
 
 def ffa_search(tseries: TimeSeries, search_cfg: PulsarSearchConfig, *, quiet: bool = False,

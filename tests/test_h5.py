@@ -1,6 +1,6 @@
-"""HDF5 files written and read without h5py (pyloki_gb300.h5) and the
+"""HDF5 files written and read without h5py (pyloki_gb300.h5), the
 pruning result files on top of them (pyloki_gb300.results,
-io/cands.py:106-411).
+io/cands.py:106-411), and the periodogram's NetCDF file.
 
 No HDF5 library is installed, so the format is pinned two ways:
 - the encoder's datatype, dataspace and attribute bytes against those
@@ -335,3 +335,33 @@ def test_rejects_damaged_files(tmp_path):
     with pytest.raises(ValueError, match="cycle"):
         r2.messages(hdr)
 
+
+
+def test_periodogram_netcdf_round_trip(tmp_path):
+    """Periodogram.save / load (periodogram.py:165-172) in xarray's NetCDF-3
+    layout: coordinate variables per parameter, the unnamed DataArray's
+    variable with ``tobs`` as a double attribute, int32 integer coordinates."""
+    from scipy.io import netcdf_file
+
+    from pyloki_gb300.search import Periodogram
+
+    rng = np.random.default_rng(4)
+    params = {"accel": np.linspace(-5, 5, 3), "freq": np.linspace(1, 2, 4) * 1.1,
+              "width": np.array([1, 2, 4, 8])}
+    p = Periodogram(params, rng.random((3, 4, 4)).astype(np.float32), 1234.5678901234)
+    path = tmp_path / "pgram.nc"
+    p.save(path)
+    with netcdf_file(path, "r", mmap=False) as f:
+        var = f.variables[Periodogram.DATA_VAR]
+        assert var.dimensions == ("accel", "freq", "width")
+        assert f.variables["width"].data.dtype == np.dtype(">i4")
+        assert var._attributes["tobs"].dtype == np.float64
+    q = Periodogram.load(path)
+    assert q.param_names == p.param_names and q.tobs == p.tobs
+    np.testing.assert_array_equal(q.snrs, p.snrs)
+    for k in params:
+        np.testing.assert_array_equal(q.params[k], params[k])
+    assert q.find_best_params() == p.find_best_params()
+    (tmp_path / "x.nc").write_bytes(b"\x89HDF\r\n\x1a\n" + bytes(64))
+    with pytest.raises(ValueError, match="NetCDF-3"):
+        Periodogram.load(tmp_path / "x.nc")
